@@ -1,0 +1,68 @@
+/*
+ * ORACLE — test infrastructure only: the CPU restatement of the reference
+ * prover used as the parity checker by tests/, the smoke check and the CPU
+ * baseline in bench.py. The product (proving_gb300, include/) never links it.
+ *
+ * Arrays of M31 values are uint32_t words in [0, P). QM31 values are 4 words
+ * (a, b, c, d) for (a + b i) + (c + d i) u. Hashes are 32 raw bytes.
+ */
+#ifndef STWO_ORACLE_H
+#define STWO_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    uint8_t digest[32];
+    uint32_t n_draws;
+} orc_channel;
+
+int orc_num_threads(void);
+void orc_bit_reverse(uint32_t *v, uint32_t log_n);
+void orc_circle_index_to_point(uint32_t idx, uint32_t out[2]);
+void orc_m31_mul_batch(const uint32_t *a, const uint32_t *b, uint32_t *out, uint64_t n);
+void orc_qm31_mul(const uint32_t a[4], const uint32_t b[4], uint32_t out[4]);
+void orc_qm31_inv(const uint32_t a[4], uint32_t out[4]);
+
+void orc_precompute_twiddles(uint32_t initial_index, uint32_t log_size, uint32_t *tw, uint32_t *itw);
+void orc_interpolate(uint32_t *v, uint32_t log_n, const uint32_t *itw, uint32_t tw_log);
+void orc_evaluate(const uint32_t *coeffs, uint32_t log_coeffs, uint32_t *out, uint32_t log_n,
+                  const uint32_t *tw, uint32_t tw_log);
+void orc_interpolate_batch(uint32_t **cols, const uint32_t *log_sizes, uint32_t n_cols,
+                           const uint32_t *itw, uint32_t tw_log);
+void orc_evaluate_batch(const uint32_t **coeffs, const uint32_t *log_coeffs, uint32_t **outs,
+                        const uint32_t *log_ns, uint32_t n_cols, const uint32_t *tw, uint32_t tw_log);
+void orc_eval_at_point(const uint32_t *coeffs, uint32_t log_n, const uint32_t px[4], const uint32_t py[4],
+                       uint32_t out[4]);
+
+void orc_merkle_build_leaves(const uint32_t **cols, const uint32_t *log_sizes, uint32_t n_cols,
+                             uint32_t lifting_log_size, uint8_t *out);
+void orc_merkle_build_next_layer(const uint8_t *prev, uint32_t out_log_size, uint8_t *out);
+void orc_merkle_commit(const uint32_t **cols, const uint32_t *log_sizes, uint32_t n_cols,
+                       uint32_t lifting_log_size, uint8_t root[32], uint8_t *layers_out);
+
+void orc_fold_line(const uint32_t *const in[4], uint32_t initial_index, uint32_t log_n,
+                   const uint32_t alpha[4], uint32_t *const out[4]);
+void orc_fold_circle_into_line(const uint32_t *const in[4], uint32_t log_n, const uint32_t alpha[4],
+                               uint32_t *const out[4]);
+
+void orc_blake2s(const uint8_t *data, uint64_t len, uint8_t out[32]);
+void orc_channel_mix_u32s(orc_channel *ch, const uint32_t *data, uint32_t n);
+void orc_channel_mix_u64(orc_channel *ch, uint64_t v);
+void orc_channel_mix_felts(orc_channel *ch, const uint32_t *felts, uint32_t n_felts);
+void orc_channel_mix_root(orc_channel *ch, const uint8_t root[32]);
+void orc_channel_draw_u32s(orc_channel *ch, uint32_t out[8]);
+void orc_channel_draw_secure_felt(orc_channel *ch, uint32_t out[4]);
+void orc_channel_draw_queries(orc_channel *ch, uint32_t log_domain_size, uint32_t n_queries, uint32_t *out);
+void orc_pow_prefixed_digest(const uint8_t digest[32], uint32_t n_bits, uint8_t out[32]);
+int orc_verify_pow_nonce(const uint8_t digest[32], uint32_t n_bits, uint64_t nonce);
+uint64_t orc_grind(const uint8_t digest[32], uint32_t n_bits);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,319 @@
+"""ORACLE — test infrastructure only: ctypes bindings to the C restatement.
+
+Used by tests/, the smoke check and bench.py's CPU-baseline leg as the checker.
+Every function takes and returns numpy arrays of uint32 words (M31 values in
+[0, P)) or bytes (Blake2s digests).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liboracle.so"
+
+P = (1 << 31) - 1
+
+u32p = ctypes.POINTER(ctypes.c_uint32)
+u8p = ctypes.POINTER(ctypes.c_uint8)
+
+
+class Channel(ctypes.Structure):
+    _fields_ = [("digest", ctypes.c_uint8 * 32), ("n_draws", ctypes.c_uint32)]
+
+
+def build() -> Path:
+    """Compile the oracle with its Makefile (plain gcc + OpenMP)."""
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        L = ctypes.CDLL(str(LIB_PATH))
+        vp = ctypes.c_void_p
+        L.orc_num_threads.restype = ctypes.c_int
+        L.orc_grind.restype = ctypes.c_uint64
+        L.orc_grind.argtypes = [vp, ctypes.c_uint32]
+        L.orc_verify_pow_nonce.restype = ctypes.c_int
+        L.orc_verify_pow_nonce.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint64]
+        L.orc_channel_mix_u64.argtypes = [vp, ctypes.c_uint64]
+        L.orc_blake2s.argtypes = [vp, ctypes.c_uint64, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _u32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint32))
+
+
+def _ptr_array(arrs):
+    arr = (ctypes.c_void_p * max(1, len(arrs)))()
+    for i, a in enumerate(arrs):
+        arr[i] = a.ctypes.data
+    return arr
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
+
+
+# ------------------------------------------------------------------ fields
+
+def qm31_mul(a, b):
+    a, b = _u32(a), _u32(b)
+    out = np.zeros(4, np.uint32)
+    lib().orc_qm31_mul(_p(a), _p(b), _p(out))
+    return out
+
+
+def qm31_inv(a):
+    a = _u32(a)
+    out = np.zeros(4, np.uint32)
+    lib().orc_qm31_inv(_p(a), _p(out))
+    return out
+
+
+def m31_mul(a, b):
+    a, b = _u32(a), _u32(b)
+    out = np.zeros_like(a)
+    lib().orc_m31_mul_batch(_p(a), _p(b), _p(out), ctypes.c_uint64(a.size))
+    return out
+
+
+def circle_index_to_point(idx: int):
+    out = np.zeros(2, np.uint32)
+    lib().orc_circle_index_to_point(ctypes.c_uint32(idx), _p(out))
+    return int(out[0]), int(out[1])
+
+
+def bit_reverse(v) -> np.ndarray:
+    v = _u32(v).copy()
+    n = v.size
+    lib().orc_bit_reverse(_p(v), ctypes.c_uint32(n.bit_length() - 1))
+    return v
+
+
+# ---------------------------------------------------------------- polys
+
+def subgroup_gen(log_size: int) -> int:
+    return 1 << (31 - log_size)
+
+
+def canonic_half_coset_initial_index(log_size: int) -> int:
+    """Initial index of CanonicCoset(log_size).half_coset() = half_odds(log_size-1)."""
+    return subgroup_gen(log_size + 1)
+
+
+def precompute_twiddles(initial_index: int, log_size: int):
+    n = 1 << log_size
+    tw = np.zeros(n, np.uint32)
+    itw = np.zeros(n, np.uint32)
+    lib().orc_precompute_twiddles(ctypes.c_uint32(initial_index), ctypes.c_uint32(log_size), _p(tw), _p(itw))
+    return tw, itw
+
+
+def canonic_twiddles(domain_log_size: int):
+    """Twiddle tree rooted at CanonicCoset(domain_log_size).half_coset()."""
+    return precompute_twiddles(canonic_half_coset_initial_index(domain_log_size), domain_log_size - 1)
+
+
+def interpolate(evals, itw: np.ndarray) -> np.ndarray:
+    v = _u32(evals).copy()
+    lib().orc_interpolate(_p(v), ctypes.c_uint32(v.size.bit_length() - 1), _p(itw),
+                          ctypes.c_uint32(itw.size.bit_length() - 1))
+    return v
+
+
+def evaluate(coeffs, log_n: int, tw: np.ndarray) -> np.ndarray:
+    c = _u32(coeffs)
+    out = np.zeros(1 << log_n, np.uint32)
+    lib().orc_evaluate(_p(c), ctypes.c_uint32(c.size.bit_length() - 1), _p(out), ctypes.c_uint32(log_n),
+                       _p(tw), ctypes.c_uint32(tw.size.bit_length() - 1))
+    return out
+
+
+def interpolate_batch(cols, itw: np.ndarray):
+    cols = [_u32(c).copy() for c in cols]
+    logs = _u32([c.size.bit_length() - 1 for c in cols])
+    lib().orc_interpolate_batch(_ptr_array(cols), _p(logs), ctypes.c_uint32(len(cols)), _p(itw),
+                                ctypes.c_uint32(itw.size.bit_length() - 1))
+    return cols
+
+
+def evaluate_batch(coeffs, log_ns, tw: np.ndarray):
+    coeffs = [_u32(c) for c in coeffs]
+    outs = [np.zeros(1 << int(l), np.uint32) for l in log_ns]
+    lc = _u32([c.size.bit_length() - 1 for c in coeffs])
+    ln = _u32(log_ns)
+    lib().orc_evaluate_batch(_ptr_array(coeffs), _p(lc), _ptr_array(outs), _p(ln), ctypes.c_uint32(len(coeffs)),
+                             _p(tw), ctypes.c_uint32(tw.size.bit_length() - 1))
+    return outs
+
+
+def eval_at_point(coeffs, px, py):
+    c, x, y = _u32(coeffs), _u32(px), _u32(py)
+    out = np.zeros(4, np.uint32)
+    lib().orc_eval_at_point(_p(c), ctypes.c_uint32(c.size.bit_length() - 1), _p(x), _p(y), _p(out))
+    return out
+
+
+# ---------------------------------------------------------------- Merkle
+
+def merkle_build_leaves(sorted_cols, lifting_log_size: int) -> np.ndarray:
+    cols = [_u32(c) for c in sorted_cols]
+    logs = _u32([c.size.bit_length() - 1 for c in cols])
+    n = 1 if not cols else 1 << lifting_log_size
+    out = np.zeros((n, 32), np.uint8)
+    lib().orc_merkle_build_leaves(_ptr_array(cols), _p(logs), ctypes.c_uint32(len(cols)),
+                                  ctypes.c_uint32(lifting_log_size), _p(out))
+    return out
+
+
+def merkle_build_next_layer(prev: np.ndarray) -> np.ndarray:
+    prev = np.ascontiguousarray(prev, dtype=np.uint8).reshape(-1, 32)
+    n = prev.shape[0] // 2
+    out = np.zeros((n, 32), np.uint8)
+    lib().orc_merkle_build_next_layer(_p(prev), ctypes.c_uint32(n.bit_length() - 1), _p(out))
+    return out
+
+
+def merkle_commit(cols, lifting_log_size: int, with_layers: bool = False):
+    """Returns the root (32 bytes), or (root, [layers leaves-first]) when asked."""
+    cols = [_u32(c) for c in cols]
+    logs = _u32([c.size.bit_length() - 1 for c in cols])
+    root = np.zeros(32, np.uint8)
+    layers = None
+    if with_layers:
+        total = (1 << (lifting_log_size + 1)) - 1 if cols else 1
+        layers = np.zeros((total, 32), np.uint8)
+    lib().orc_merkle_commit(_ptr_array(cols), _p(logs), ctypes.c_uint32(len(cols)),
+                            ctypes.c_uint32(lifting_log_size), _p(root),
+                            _p(layers) if layers is not None else None)
+    if not with_layers:
+        return root.tobytes()
+    out, off = [], 0
+    for k in range(lifting_log_size, -1, -1):
+        out.append(layers[off:off + (1 << k)].copy())
+        off += 1 << k
+    return root.tobytes(), out
+
+
+# ---------------------------------------------------------------- FRI
+
+def fold_line(coords, line_initial_index: int, alpha):
+    """coords: 4 arrays (SoA QM31) on the line domain x(coset(initial, log n))."""
+    ins = [_u32(c) for c in coords]
+    n = ins[0].size
+    outs = [np.zeros(n // 2, np.uint32) for _ in range(4)]
+    a = _u32(alpha)
+    lib().orc_fold_line(_ptr_array(ins), ctypes.c_uint32(line_initial_index),
+                        ctypes.c_uint32(n.bit_length() - 1), _p(a), _ptr_array(outs))
+    return outs
+
+
+def fold_circle_into_line(coords, alpha):
+    ins = [_u32(c) for c in coords]
+    n = ins[0].size
+    outs = [np.zeros(n // 2, np.uint32) for _ in range(4)]
+    a = _u32(alpha)
+    lib().orc_fold_circle_into_line(_ptr_array(ins), ctypes.c_uint32(n.bit_length() - 1), _p(a),
+                                    _ptr_array(outs))
+    return outs
+
+
+def line_domain_initial_index(line_log_size: int) -> int:
+    """LineDomain(Coset::half_odds(line_log_size)) — the first FRI line domain."""
+    return subgroup_gen(line_log_size + 2)
+
+
+def double_index(idx: int) -> int:
+    return (idx * 2) & ((1 << 31) - 1)
+
+
+# ---------------------------------------------------------------- channel
+
+def blake2s(data: bytes) -> bytes:
+    buf = np.frombuffer(bytes(data), dtype=np.uint8).copy() if data else np.zeros(1, np.uint8)
+    out = np.zeros(32, np.uint8)
+    lib().orc_blake2s(_p(buf), ctypes.c_uint64(len(data)), _p(out))
+    return out.tobytes()
+
+
+class Blake2sChannel:
+    """Blake2sChannel (crates/stwo/src/core/channel/blake2s.rs:16-118) over the C oracle."""
+
+    def __init__(self, digest: bytes = bytes(32)):
+        self.ch = Channel()
+        ctypes.memmove(self.ch.digest, digest, 32)
+        self.ch.n_draws = 0
+
+    @property
+    def digest(self) -> bytes:
+        return bytes(self.ch.digest)
+
+    @property
+    def n_draws(self) -> int:
+        return self.ch.n_draws
+
+    def mix_u32s(self, words):
+        w = _u32(words)
+        lib().orc_channel_mix_u32s(ctypes.byref(self.ch), _p(w) if w.size else None, ctypes.c_uint32(w.size))
+
+    def mix_u64(self, v: int):
+        lib().orc_channel_mix_u64(ctypes.byref(self.ch), ctypes.c_uint64(v))
+
+    def mix_felts(self, felts):
+        f = _u32(felts).reshape(-1)
+        lib().orc_channel_mix_felts(ctypes.byref(self.ch), _p(f), ctypes.c_uint32(f.size // 4))
+
+    def mix_root(self, root: bytes):
+        r = np.frombuffer(root, np.uint8).copy()
+        lib().orc_channel_mix_root(ctypes.byref(self.ch), _p(r))
+
+    def draw_u32s(self):
+        out = np.zeros(8, np.uint32)
+        lib().orc_channel_draw_u32s(ctypes.byref(self.ch), _p(out))
+        return out
+
+    def draw_secure_felt(self):
+        out = np.zeros(4, np.uint32)
+        lib().orc_channel_draw_secure_felt(ctypes.byref(self.ch), _p(out))
+        return out
+
+    def draw_queries(self, log_domain_size: int, n_queries: int):
+        out = np.zeros(n_queries, np.uint32)
+        lib().orc_channel_draw_queries(ctypes.byref(self.ch), ctypes.c_uint32(log_domain_size),
+                                       ctypes.c_uint32(n_queries), _p(out))
+        return out
+
+    def verify_pow_nonce(self, n_bits: int, nonce: int) -> bool:
+        d = np.frombuffer(self.digest, np.uint8).copy()
+        return bool(lib().orc_verify_pow_nonce(_p(d), n_bits, nonce))
+
+
+def grind(digest: bytes, n_bits: int) -> int:
+    d = np.frombuffer(digest, np.uint8).copy()
+    return int(lib().orc_grind(_p(d), n_bits))
+
+
+def pow_prefixed_digest(digest: bytes, n_bits: int) -> bytes:
+    d = np.frombuffer(digest, np.uint8).copy()
+    out = np.zeros(32, np.uint8)
+    lib().orc_pow_prefixed_digest(_p(d), ctypes.c_uint32(n_bits), _p(out))
+    return out.tobytes()
