@@ -1,0 +1,407 @@
+"""Commit-stage microbenchmark of the Stwo prover hot path on GB300.
+
+Workload (one step = one "proof" of the commit stage):
+  256 M31 columns of 2^20 rows (uniform in [0, P), seeded), interpolate, evaluate
+  on the 4x blown-up canonic domain (log 22), lifted Blake2s Merkle tree over the
+  256-wide leaves (height 22), then 22 FRI folds (fold_circle_into_line + 21
+  fold_line) of a seeded QM31 column of log 22 with seeded QM31 challenges.
+
+`value` times the step with the trace already resident in HBM; `e2e` times the
+same step through the C ABI with the trace in pinned host memory, including the
+host->device copy of the trace and FRI column and the device->host read of the
+Merkle root and the last FRI value. The trace (1 GiB) and the extended
+evaluation (4 GiB) exceed L2 (129 MB), so no L2 flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference (the oracle; the
+Rust reference cannot be built here) on a bounded sample of the same
+workload, with all host threads, extrapolated per stage to the full step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "proofs/s, p50/p99 prove latency on 1 GB300: batched vs plain CUDA, bit-exact"
+UNIT = "proofs/s"
+N_COLS, LOG_ROWS, LOG_BLOWUP = 256, 20, 2
+LOG_EXT = LOG_ROWS + LOG_BLOWUP
+FRI_LOG = 22
+WORKLOAD = (f"commit-stage microbench: {N_COLS} M31 cols x 2^{LOG_ROWS}, interpolate, evaluate on log {LOG_EXT}, "
+            f"lifted Blake2s Merkle over {N_COLS}-wide leaves, 22 FRI folds of a QM31 col of log {FRI_LOG}")
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- GPU arm
+
+class CommitStage:
+    """Device buffers and the step, all through the C ABI (proving_gb300._lib)."""
+
+    def __init__(self, torch, seed: int = 2026):
+        from proving_gb300 import _lib
+        from proving_gb300.backend import canonic_half_coset, subgroup_gen
+        self.torch, self.L = torch, _lib
+        dev = torch.device("cuda", torch.cuda.current_device())
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        P = (1 << 31) - 1
+        self.evals = torch.randint(0, P, (N_COLS, 1 << LOG_ROWS), generator=g, device=dev, dtype=torch.int64).to(
+            torch.int32)
+        self.fri_src = torch.randint(0, P, (4, 1 << FRI_LOG), generator=g, device=dev, dtype=torch.int64).to(
+            torch.int32)
+        self.alphas = torch.randint(0, P, (FRI_LOG, 4), generator=g, dtype=torch.int64, device="cpu").numpy().astype(
+            np.uint32)
+        self.coeffs = torch.empty_like(self.evals)
+        self.ext = torch.empty((N_COLS, 1 << LOG_EXT), dtype=torch.int32, device=dev)
+        total = (1 << (LOG_EXT + 1)) - 1
+        self.layers = torch.empty((total, 8), dtype=torch.int32, device=dev)
+        # FRI layers: 2^21, 2^20, ..., 2^0 QM31 values (4 coordinate arrays each)
+        self.fri_layers = [torch.empty((4, 1 << k), dtype=torch.int32, device=dev) for k in range(FRI_LOG - 1, -1, -1)]
+        root = canonic_half_coset(LOG_EXT + 1)
+        self.tw_log = root.log_size
+        self.tw = torch.empty(1 << self.tw_log, dtype=torch.int32, device=dev)
+        self.itw = torch.empty_like(self.tw)
+        _lib.call("cs_precompute_twiddles", root.initial_index, root.log_size, self.tw.data_ptr(),
+                  self.itw.data_ptr(), self.stream())
+        vp = ctypes.c_void_p
+        self.t_evals = (vp * N_COLS)(*[self.evals[i].data_ptr() for i in range(N_COLS)])
+        self.t_coeffs = (vp * N_COLS)(*[self.coeffs[i].data_ptr() for i in range(N_COLS)])
+        self.t_ext = (vp * N_COLS)(*[self.ext[i].data_ptr() for i in range(N_COLS)])
+        self.logs = (ctypes.c_uint32 * N_COLS)(*([LOG_EXT] * N_COLS))
+        self.fri_tabs = [(vp * 4)(*[self.fri_src[k].data_ptr() for k in range(4)])]
+        for lay in self.fri_layers:
+            self.fri_tabs.append((vp * 4)(*[lay[k].data_ptr() for k in range(4)]))
+        self.alpha_tabs = [(ctypes.c_uint32 * 4)(*[int(x) for x in a]) for a in self.alphas]
+        self.layer_ptr = []
+        off = 0
+        for k in range(LOG_EXT, -1, -1):
+            self.layer_ptr.append(self.layers[off].data_ptr())
+            off += 1 << k
+        torch.cuda.synchronize()
+
+    def stream(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def step(self, ev=None):
+        """One commit-stage pass. ev: optional list of 6 CUDA events bracketing the stages."""
+        call, st = self.L.call, self.stream()
+        rec = (lambda i: ev[i].record()) if ev else (lambda i: None)
+        rec(0)
+        call("cs_interpolate_columns_into", self.t_evals, self.t_coeffs, N_COLS, LOG_ROWS, self.itw.data_ptr(),
+             self.tw_log, st)
+        rec(1)
+        call("cs_evaluate_columns", self.t_coeffs, self.t_ext, N_COLS, LOG_ROWS, LOG_EXT, self.tw.data_ptr(),
+             self.tw_log, st)
+        rec(2)
+        call("cs_merkle_build_leaves", self.t_ext, self.logs, N_COLS, LOG_EXT, self.layer_ptr[0], st)
+        rec(3)
+        for k in range(LOG_EXT, 0, -1):
+            call("cs_merkle_build_next_layer", self.layer_ptr[LOG_EXT - k], k - 1, self.layer_ptr[LOG_EXT - k + 1], st)
+        rec(4)
+        call("cs_fold_circle_into_line", self.fri_tabs[0], FRI_LOG, self.alpha_tabs[0], self.fri_tabs[1],
+             self.itw.data_ptr(), self.tw_log, st)
+        for j in range(1, FRI_LOG):
+            call("cs_fold_line", self.fri_tabs[j], FRI_LOG - j, self.alpha_tabs[j], self.fri_tabs[j + 1],
+                 self.itw.data_ptr(), self.tw_log, st)
+        rec(5)
+
+    def root(self) -> bytes:
+        return self.layers[-1].cpu().numpy().astype("<i4").tobytes()
+
+
+def run_gpu(args):
+    import torch
+    from proving_gb300 import _lib
+    from proving_gb300 import build as cuda_build
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+        torch.cuda.set_device(0)
+    if rank == 0 or world == 1:
+        cuda_build.build()
+    if dist:
+        dist.barrier()
+    L = _lib.load()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    cs = CommitStage(torch)
+    for _ in range(args.warmup):
+        cs.step()
+    barrier()
+
+    n_ev = 6
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n_ev)] for _ in range(args.steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = L.cs_kernel_launch_count()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        barrier()
+        start.record()
+        for k in range(args.steps):
+            cs.step(evs[k])
+        end.record()
+        barrier()
+    launches = L.cs_kernel_launch_count() - launches0
+    elapsed_ms = start.elapsed_time(end)
+    stage_names = ["interpolate", "evaluate", "merkle_leaves", "merkle_nodes", "fri_folds"]
+    stage_ms = {n: statistics.mean(evs[k][i].elapsed_time(evs[k][i + 1]) for k in range(args.steps))
+                for i, n in enumerate(stage_names)}
+    step_lat = [evs[k][0].elapsed_time(evs[k][5]) for k in range(args.steps)]
+    t = torch.tensor([elapsed_ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = world * args.steps / (max_ms / 1e3)
+
+    # ---- e2e through the C ABI with host buffers
+    host_evals = torch.empty((N_COLS, 1 << LOG_ROWS), dtype=torch.int32, pin_memory=True)
+    host_evals.copy_(cs.evals.cpu())
+    host_fri = torch.empty((4, 1 << FRI_LOG), dtype=torch.int32, pin_memory=True)
+    host_fri.copy_(cs.fri_src.cpu())
+    host_out = torch.empty(16, dtype=torch.int32, pin_memory=True)
+    h2d = host_evals.numel() * 4 + host_fri.numel() * 4
+    d2h = 32 + 16
+
+    def e2e_step():
+        st = cs.stream()
+        _lib.call("cs_memcpy_h2d", cs.evals.data_ptr(), host_evals.data_ptr(), host_evals.numel() * 4, st)
+        _lib.call("cs_memcpy_h2d", cs.fri_src.data_ptr(), host_fri.data_ptr(), host_fri.numel() * 4, st)
+        cs.step()
+        _lib.call("cs_memcpy_d2h", host_out.data_ptr(), cs.layers[-1].data_ptr(), 32, st)
+        _lib.call("cs_memcpy_d2h", host_out.data_ptr() + 32, cs.fri_layers[-1].data_ptr(), 16, st)
+        _lib.call("cs_stream_synchronize", st)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_lat = []
+    e_start.record()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        e2e_step()
+        e_lat.append((time.perf_counter() - t0) * 1e3)
+    e_end.record()
+    barrier()
+    e2e_ms = e_start.elapsed_time(e_end)
+    t = torch.tensor([e2e_ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_value = world * args.steps / (float(t.item()) / 1e3)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    hbm, peak_kind = peaks()
+    # dominant kernel: the Blake2s leaf hashing (one launch per step)
+    leaf_ms = stage_ms["merkle_leaves"]
+    leaf_bytes = N_COLS * (1 << LOG_EXT) * 4 + (1 << LOG_EXT) * 32
+    achieved = leaf_bytes / (leaf_ms / 1e3) / 1e9
+    leaf_comp = (1 << LOG_EXT) * ((N_COLS * 4 + 63) // 64)
+    traffic = None
+    tr_file = ROOT / "profiles" / "traffic.json"
+    if tr_file.exists():
+        traffic = json.loads(tr_file.read_text()).get("merkle_leaves_kernel_bytes_per_launch")
+    cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
+    ff = lambda x: float(f"{x:.6g}")
+    res = {
+        "metric": METRIC, "value": ff(value), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ff(max_ms / args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "n_cols": N_COLS, "log_rows": LOG_ROWS, "log_blowup": LOG_BLOWUP,
+                   "merkle_height": LOG_EXT, "fri_log_size": FRI_LOG, "fri_folds": 22,
+                   "l2": "inputs larger than L2 (1 GiB trace, 4 GiB extension); no flush",
+                   "parallelism": f"replicas x{world}"},
+        "latency_ms": {"p50": ff(float(np.percentile(step_lat, 50))), "p99": ff(float(np.percentile(step_lat, 99))),
+                       "e2e_p50": ff(float(np.percentile(e_lat, 50))), "e2e_p99": ff(float(np.percentile(e_lat, 99)))},
+        "stages_ms": {k: ff(v) for k, v in stage_ms.items()},
+        "e2e": {"value": ff(e2e_value), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": "merkle_leaves_kernel", "achieved": ff(achieved), "peak": hbm,
+                     "unit": "GB/s", "frac": ff(achieved / hbm), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json)",
+                     "traffic": traffic, "algorithmic_bytes_per_launch": leaf_bytes,
+                     "note": "Blake2s leaf hashing is integer-pipe bound; see int_pipe"},
+        "int_pipe": {"kernel": "merkle_leaves_kernel", "compressions_per_launch": leaf_comp,
+                     "gcompressions_per_s": ff(leaf_comp / (leaf_ms / 1e3) / 1e9),
+                     "int_ops_per_compression": 1120,
+                     "tops_achieved": ff(leaf_comp * 1120 / (leaf_ms / 1e3) / 1e12)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(res))
+    if dist:
+        dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------- CPU arm
+
+def cpu_sample_times(n_fft_cols: int = 32, leaf_log: int = 17):
+    """Times the oracle on a bounded sample; returns per-stage seconds scaled to one full step."""
+    from oracle import oracle as O
+    from proving_gb300.synthetic import m31_columns, qm31_column, seeded_qm31
+    tw, itw = O.canonic_twiddles(LOG_EXT + 1)
+    evals = list(m31_columns(11, n_fft_cols, LOG_ROWS))
+    t0 = time.perf_counter()
+    coeffs = O.interpolate_batch(evals, itw)
+    t1 = time.perf_counter()
+    O.evaluate_batch(coeffs, [LOG_EXT] * n_fft_cols, tw)
+    t2 = time.perf_counter()
+    leaf_cols = list(m31_columns(12, N_COLS, leaf_log))
+    t3 = time.perf_counter()
+    O.merkle_commit(leaf_cols, leaf_log)  # leaves + node layers over 2^leaf_log leaves
+    t4 = time.perf_counter()
+    fri = qm31_column(13, FRI_LOG)
+    t5 = time.perf_counter()
+    lay = O.fold_circle_into_line(fri, seeded_qm31(0))
+    init = O.line_domain_initial_index(FRI_LOG - 1)
+    for k in range(1, FRI_LOG):
+        lay = O.fold_line(lay, init, seeded_qm31(k))
+        init = O.double_index(init)
+    t6 = time.perf_counter()
+    fft_scale = N_COLS / n_fft_cols
+    leaf_scale = (1 << LOG_EXT) / (1 << leaf_log)
+    stages = {"interpolate": (t1 - t0) * fft_scale, "evaluate": (t2 - t1) * fft_scale,
+              "merkle": (t4 - t3) * leaf_scale, "fri_folds": t6 - t5}
+    sample = (f"oracle on {n_fft_cols}/{N_COLS} columns for interpolate+evaluate, {N_COLS} cols x 2^{leaf_log} "
+              f"leaves for the Merkle tree (1/{int(leaf_scale)} of the leaves), the full 22-fold FRI chain; "
+              f"each stage scaled to the full step")
+    return stages, sample
+
+
+def cpu_baseline(args):
+    from oracle import oracle as O
+    stages, sample = cpu_sample_times()
+    total = sum(stages.values())
+    return {"value": float(f"{1.0 / total:.6g}"), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": sample, "stages_s": {k: float(f"{v:.4g}") for k, v in stages.items()}}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+    from oracle import oracle as O
+    for _ in range(args.warmup):
+        cpu_sample_times(n_fft_cols=8, leaf_log=14)
+    totals = []
+    t0 = time.perf_counter()
+    sample = ""
+    for _ in range(args.steps):
+        stages, sample = cpu_sample_times(n_fft_cols=8, leaf_log=14)
+        totals.append(sum(stages.values()))
+    wall = time.perf_counter() - t0
+    value = args.steps / sum(totals)
+    res = {
+        "metric": METRIC, "value": float(f"{value:.6g}"), "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": float(f"{1e3 * sum(totals) / args.steps:.6g}"),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
+        "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": WORKLOAD, "n_cols": N_COLS, "log_rows": LOG_ROWS, "log_blowup": LOG_BLOWUP},
+        "cpu_baseline": {"value": float(f"{value:.6g}"), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+                         "sample": sample + " (the Rust reference cannot be built: no cargo on this image)"},
+        "e2e": {"value": float(f"{value:.6g}"), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": float(f"{wall:.4g}"),
+    }
+    print(json.dumps(res))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the timed oracle sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,283 @@
+"""Host-side mirror of the reference backend trait family over the C ABI.
+
+Names, argument meanings and error behaviour follow the reference:
+`ColumnOps::bit_reverse_column`, `PolyOps::{precompute_twiddles,
+interpolate_columns, evaluate_polynomials}`, `MerkleOpsLifted::{build_leaves,
+build_next_layer}`, `MerkleProverLifted::commit`, `PackLeavesOps`,
+`FriOps::{fold_line, fold_circle_into_line}`, `GrindOps::grind`
+(crates/stwo/src/prover/backend/mod.rs:17-35 and the files cited per method).
+Misuse raises (the reference panics). Columns live in HBM as torch int32
+tensors holding M31 words; torch is used only for device memory and streams.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+
+P = (1 << 31) - 1
+M31_CIRCLE_LOG_ORDER = 31
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t: torch.Tensor) -> int:
+    assert t.is_cuda and t.is_contiguous()
+    return t.data_ptr()
+
+
+def _ptr_table(ts) -> ctypes.Array:
+    arr = (ctypes.c_void_p * max(1, len(ts)))()
+    for i, t in enumerate(ts):
+        arr[i] = _ptr(t)
+    return arr
+
+
+def _u32_table(vals) -> ctypes.Array:
+    arr = (ctypes.c_uint32 * max(1, len(vals)))()
+    for i, v in enumerate(vals):
+        arr[i] = int(v)
+    return arr
+
+
+def subgroup_gen(log_size: int) -> int:
+    return 1 << (M31_CIRCLE_LOG_ORDER - log_size)
+
+
+# ------------------------------------------------------------------ columns
+
+class BaseColumn:
+    """BaseColumn (crates/stwo/src/prover/backend/simd/column.rs:26-30): 2^k M31 words in HBM."""
+
+    def __init__(self, data: torch.Tensor):
+        assert data.dtype == torch.int32 and data.dim() == 1 and data.is_cuda
+        self.data = data
+
+    @classmethod
+    def zeros(cls, length: int, device="cuda"):
+        return cls(torch.zeros(length, dtype=torch.int32, device=device))
+
+    @classmethod
+    def uninitialized(cls, length: int, device="cuda"):
+        return cls(torch.empty(length, dtype=torch.int32, device=device))
+
+    @classmethod
+    def from_cpu(cls, values: np.ndarray, device="cuda"):
+        v = np.ascontiguousarray(values, dtype=np.uint32).view(np.int32)
+        return cls(torch.from_numpy(v).to(device, non_blocking=False))
+
+    def to_cpu(self) -> np.ndarray:
+        return self.data.cpu().numpy().view(np.uint32)
+
+    def __len__(self):
+        return self.data.numel()
+
+    @property
+    def log_size(self) -> int:
+        n = len(self)
+        return n.bit_length() - 1
+
+    def at(self, i: int) -> int:
+        return int(self.data[i].item()) & 0xFFFFFFFF
+
+
+class SecureColumnByCoords:
+    """SecureColumnByCoords (crates/stwo/src/prover/secure_column.rs:13-15): 4 coordinate columns."""
+
+    def __init__(self, columns):
+        assert len(columns) == 4
+        self.columns = [c if isinstance(c, BaseColumn) else BaseColumn(c) for c in columns]
+
+    @classmethod
+    def zeros(cls, length: int):
+        return cls([BaseColumn.zeros(length) for _ in range(4)])
+
+    @classmethod
+    def uninitialized(cls, length: int):
+        return cls([BaseColumn.uninitialized(length) for _ in range(4)])
+
+    @classmethod
+    def from_cpu(cls, coords):
+        return cls([BaseColumn.from_cpu(c) for c in coords])
+
+    def to_cpu(self):
+        return [c.to_cpu() for c in self.columns]
+
+    def __len__(self):
+        return len(self.columns[0])
+
+    def at(self, i: int):
+        return [c.at(i) for c in self.columns]
+
+
+@dataclass
+class Coset:
+    """Coset initial_index + <G_{2^log_size}> (crates/stwo/src/core/circle.rs:262-282)."""
+    initial_index: int
+    log_size: int
+
+    @staticmethod
+    def half_odds(log_size: int) -> "Coset":
+        return Coset(subgroup_gen(log_size + 2), log_size)
+
+
+def canonic_half_coset(log_size: int) -> Coset:
+    """CanonicCoset(log_size).half_coset() (crates/stwo/src/core/poly/circle/canonic.rs:61-63)."""
+    return Coset.half_odds(log_size - 1)
+
+
+class TwiddleTree:
+    """TwiddleTree (crates/stwo/src/prover/poly/twiddles.rs:10-15) resident in HBM."""
+
+    def __init__(self, root_coset: Coset, twiddles: torch.Tensor, itwiddles: torch.Tensor):
+        self.root_coset = root_coset
+        self.twiddles = twiddles
+        self.itwiddles = itwiddles
+
+    @property
+    def log_size(self) -> int:
+        return self.root_coset.log_size
+
+
+# ------------------------------------------------------------------ backend
+
+class CudaBackend:
+    """The GB300 backend. Every method enqueues on torch's current CUDA stream."""
+
+    # ColumnOps -------------------------------------------------------------
+    @staticmethod
+    def bit_reverse_column(col: BaseColumn) -> None:
+        _lib.call("cs_bit_reverse_m31", _ptr(col.data), col.log_size, _stream())
+
+    # PolyOps ---------------------------------------------------------------
+    @staticmethod
+    def precompute_twiddles(coset: Coset) -> TwiddleTree:
+        n = 1 << coset.log_size
+        tw = torch.empty(n, dtype=torch.int32, device="cuda")
+        itw = torch.empty(n, dtype=torch.int32, device="cuda")
+        _lib.call("cs_precompute_twiddles", coset.initial_index, coset.log_size, _ptr(tw), _ptr(itw), _stream())
+        return TwiddleTree(coset, tw, itw)
+
+    @staticmethod
+    def interpolate_columns(columns, twiddles: TwiddleTree) -> None:
+        """In place: bit-reversed evaluations on CanonicCoset(log) -> coefficients.
+        Columns of several sizes are grouped by size, one batched call per size."""
+        by_size = {}
+        for c in columns:
+            by_size.setdefault(c.log_size, []).append(c)
+        for log_size, cols in by_size.items():
+            tab = _ptr_table([c.data for c in cols])
+            _lib.call("cs_interpolate_columns", tab, len(cols), log_size, _ptr(twiddles.itwiddles),
+                      twiddles.log_size, _stream())
+
+    @staticmethod
+    def evaluate_polynomials(coeffs, log_size: int, twiddles: TwiddleTree, out=None):
+        """Evaluates coefficient columns on CanonicCoset(log_size); returns new columns."""
+        if out is None:
+            out = [BaseColumn.uninitialized(1 << log_size) for _ in coeffs]
+        by_size = {}
+        for i, c in enumerate(coeffs):
+            by_size.setdefault(c.log_size, []).append(i)
+        for lc, idxs in by_size.items():
+            src = _ptr_table([coeffs[i].data for i in idxs])
+            dst = _ptr_table([out[i].data for i in idxs])
+            _lib.call("cs_evaluate_columns", src, dst, len(idxs), lc, log_size, _ptr(twiddles.twiddles),
+                      twiddles.log_size, _stream())
+        return out
+
+    # MerkleOpsLifted ---------------------------------------------------------
+    @staticmethod
+    def build_leaves(columns, lifting_log_size: int) -> torch.Tensor:
+        """Columns sorted by length; returns (2^L, 8) int32 digests."""
+        n = 1 if not columns else 1 << lifting_log_size
+        out = torch.empty((n, 8), dtype=torch.int32, device="cuda")
+        tab = _ptr_table([c.data for c in columns])
+        logs = _u32_table([c.log_size for c in columns])
+        _lib.call("cs_merkle_build_leaves", tab, logs, len(columns), lifting_log_size, _ptr(out), _stream())
+        return out
+
+    @staticmethod
+    def build_next_layer(prev: torch.Tensor) -> torch.Tensor:
+        n = prev.shape[0] // 2
+        out = torch.empty((n, 8), dtype=torch.int32, device="cuda")
+        _lib.call("cs_merkle_build_next_layer", _ptr(prev), n.bit_length() - 1, _ptr(out), _stream())
+        return out
+
+    @staticmethod
+    def merkle_commit(columns, lifting_log_size: int) -> "MerkleProverLifted":
+        """MerkleProverLifted::commit (crates/stwo/src/prover/vcs_lifted/prover.rs:35-80), no leaf packing."""
+        total = (1 << (lifting_log_size + 1)) - 1 if columns else 1
+        layers = torch.empty((total, 8), dtype=torch.int32, device="cuda")
+        tab = _ptr_table([c.data for c in columns])
+        logs = _u32_table([c.log_size for c in columns])
+        _lib.call("cs_merkle_commit", tab, logs, len(columns), lifting_log_size, _ptr(layers), _stream())
+        return MerkleProverLifted(layers, lifting_log_size if columns else 0)
+
+    @staticmethod
+    def pack_leaves_input(values) -> list:
+        n = len(values[0])
+        outs = [BaseColumn.uninitialized(n // 4) for _ in range(16)]
+        ins = _ptr_table([v.data for v in values])
+        o = _ptr_table([c.data for c in outs])
+        _lib.call("cs_pack_leaves_input", ins, n.bit_length() - 1, o, _stream())
+        return outs
+
+    # FriOps -------------------------------------------------------------------
+    @staticmethod
+    def fold_line(values: SecureColumnByCoords, alphas, twiddles: TwiddleTree) -> SecureColumnByCoords:
+        """fold_line on the line domain x(half_odds(log n)); alphas as in FriOps::fold_line."""
+        cur = values
+        for alpha in alphas:
+            n = len(cur)
+            dst = SecureColumnByCoords.uninitialized(n // 2)
+            a = _u32_table(alpha)
+            _lib.call("cs_fold_line", _ptr_table([c.data for c in cur.columns]), n.bit_length() - 1, a,
+                      _ptr_table([c.data for c in dst.columns]), _ptr(twiddles.itwiddles), twiddles.log_size,
+                      _stream())
+            cur = dst
+        return cur
+
+    @staticmethod
+    def fold_circle_into_line(src: SecureColumnByCoords, alpha, twiddles: TwiddleTree) -> SecureColumnByCoords:
+        n = len(src)
+        dst = SecureColumnByCoords.uninitialized(n // 2)
+        a = _u32_table(alpha)
+        _lib.call("cs_fold_circle_into_line", _ptr_table([c.data for c in src.columns]), n.bit_length() - 1, a,
+                  _ptr_table([c.data for c in dst.columns]), _ptr(twiddles.itwiddles), twiddles.log_size, _stream())
+        return dst
+
+    # GrindOps -----------------------------------------------------------------
+    @staticmethod
+    def grind(digest: bytes, pow_bits: int, max_nonce: int = 1 << 48) -> int:
+        d = (ctypes.c_uint8 * 32).from_buffer_copy(digest)
+        out = ctypes.c_uint64(0)
+        _lib.call("cs_grind_blake2s", d, pow_bits, max_nonce, ctypes.byref(out), _stream())
+        return out.value
+
+
+class MerkleProverLifted:
+    """Layer stack of a committed lifted tree (crates/stwo/src/prover/vcs_lifted/prover.rs:18-22).
+    `layers` holds leaves first; `layer(k)` returns the layer with 2^k digests."""
+
+    def __init__(self, layers: torch.Tensor, lifting_log_size: int):
+        self.all = layers
+        self.lifting_log_size = lifting_log_size
+
+    def layer(self, k: int) -> torch.Tensor:
+        L = self.lifting_log_size
+        off = sum(1 << j for j in range(k + 1, L + 1))
+        return self.all[off:off + (1 << k)]
+
+    def root(self) -> bytes:
+        return self.all[-1].cpu().numpy().view(np.uint32).astype("<u4").tobytes()
+
+
+def digests_to_bytes(t: torch.Tensor) -> np.ndarray:
+    """(n, 8) int32 digests -> (n, 32) uint8 (little-endian words = Blake2s digest bytes)."""
+    return t.cpu().numpy().astype("<i4").view(np.uint8).reshape(-1, 32)

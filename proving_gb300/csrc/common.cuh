@@ -1,0 +1,47 @@
+// Shared helpers for the C-ABI: status codes, the per-thread error message,
+// launch checks and the batch size of column-pointer tables passed by value.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "stwo_cuda.h"
+
+namespace cs {
+
+// Column-pointer tables travel as kernel parameters (no device allocation);
+// larger batches are split into several launches by the host wrappers.
+constexpr int kMaxBatch = 256;
+
+void set_error(const char* fmt, ...);
+// Counts kernel launches made by this library (reported by cs_kernel_launch_count).
+void note_launch();
+cs_status from_cuda(cudaError_t e, const char* what);
+
+inline cudaStream_t to_stream(cs_stream s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline uint32_t subgroup_gen(uint32_t log_size) { return 1u << (31 - log_size); }
+
+}  // namespace cs
+
+#define CS_CHECK_ARG(cond, ...)            \
+  do {                                     \
+    if (!(cond)) {                         \
+      cs::set_error(__VA_ARGS__);          \
+      return CS_ERR_INVALID_ARG;           \
+    }                                      \
+  } while (0)
+
+#define CS_CUDA(call)                                         \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cs::from_cuda(e_, #call);   \
+  } while (0)
+
+#define CS_LAUNCHED(name)                                           \
+  do {                                                              \
+    cs::note_launch();                                              \
+    cudaError_t e_ = cudaGetLastError();                            \
+    if (e_ != cudaSuccess) return cs::from_cuda(e_, "launch " name); \
+  } while (0)

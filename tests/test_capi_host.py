@@ -1,0 +1,83 @@
+"""CPU-only checks of the C ABI: the library loads, exports every function the
+public header declares, and rejects bad arguments before touching a device."""
+import ctypes
+from pathlib import Path
+
+import pytest
+
+from proving_gb300 import _lib
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADERS = sorted((ROOT / "include").glob("*.h"))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from proving_gb300 import build
+    build.build()
+    return _lib.load()
+
+
+def declared():
+    names = []
+    for h in HEADERS:
+        names += _lib.exported_names_from_header(h)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared()
+    assert "cs_interpolate_columns" in names and "cs_merkle_build_leaves" in names
+    assert len(names) >= 20
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in declared():
+        assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+
+
+def test_bindings_cover_header():
+    # every declared function has a ctypes signature in the Python mirror
+    assert set(declared()) <= set(_lib.SIGNATURES), set(declared()) - set(_lib.SIGNATURES)
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.cs_version()
+
+
+def _status(lib, name, *args):
+    return getattr(lib, name)(*args)
+
+
+def test_invalid_arguments_are_rejected_on_host(lib):
+    INVALID = 1
+    null = ctypes.c_void_p(0)
+    # log size out of range
+    assert _status(lib, "cs_interpolate_columns", null, 0, 0, null, 10, null) == INVALID
+    assert b"log_size" in lib.cs_last_error()
+    # twiddle tree too small for the domain
+    tab = (ctypes.c_void_p * 1)(1 << 20)
+    assert _status(lib, "cs_interpolate_columns", tab, 1, 12, ctypes.c_void_p(1 << 21), 5, null) == INVALID
+    # evaluate with fewer output than input coefficients
+    assert _status(lib, "cs_evaluate_columns", tab, tab, 1, 10, 8, ctypes.c_void_p(1 << 21), 12, null) == INVALID
+    # grind beyond 32 bits
+    d = (ctypes.c_uint8 * 32)()
+    out = ctypes.c_uint64()
+    assert _status(lib, "cs_grind_blake2s", d, 33, 1 << 20, ctypes.byref(out), null) == INVALID
+    # Merkle columns not sorted by length
+    logs = (ctypes.c_uint32 * 2)(5, 4)
+    cols = (ctypes.c_void_p * 2)(1 << 20, 1 << 21)
+    assert _status(lib, "cs_merkle_build_leaves", cols, logs, 2, 5, ctypes.c_void_p(1 << 22), null) == INVALID
+    assert b"sorted" in lib.cs_last_error()
+    # empty tree must be committed at height 0 (prover.rs:41-50)
+    assert _status(lib, "cs_merkle_build_leaves", null, null, 0, 3, ctypes.c_void_p(1 << 22), null) == INVALID
+    # fold_line domain not covered by the twiddle tree
+    src = (ctypes.c_void_p * 4)(1 << 20, 1 << 21, 1 << 22, 1 << 23)
+    alpha = (ctypes.c_uint32 * 4)(1, 2, 3, 4)
+    assert _status(lib, "cs_fold_line", src, 12, alpha, src, ctypes.c_void_p(1 << 24), 10, null) == INVALID
+
+
+def test_error_raises_in_python_mirror(lib):
+    with pytest.raises(_lib.CudaBackendError) as e:
+        _lib.call("cs_bit_reverse_m31", ctypes.c_void_p(0), 4, ctypes.c_void_p(0))
+    assert "CS_ERR_INVALID_ARG" in str(e.value)

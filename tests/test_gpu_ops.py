@@ -1,0 +1,223 @@
+"""GPU parity: every CUDA op, called through the C ABI, against the CPU oracle
+on the same seeded inputs. All values are compared as raw u32 words (the
+reference hashes raw words, so canonical representatives must match too)."""
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O  # noqa: E402
+from proving_gb300.synthetic import m31_column, m31_columns, qm31_column, seeded_qm31  # noqa: E402
+
+KATS = json.loads((Path(__file__).parent / "golden" / "reference_kats.json").read_text())
+
+
+@pytest.fixture(scope="module")
+def B():
+    from proving_gb300 import build
+    build.build()
+    from proving_gb300.backend import CudaBackend
+    assert torch.cuda.is_available()
+    return CudaBackend
+
+
+def _tree(B, domain_log):
+    from proving_gb300.backend import canonic_half_coset
+    return B.precompute_twiddles(canonic_half_coset(domain_log))
+
+
+def _col(values):
+    from proving_gb300.backend import BaseColumn
+    return BaseColumn.from_cpu(values)
+
+
+# ------------------------------------------------------------------ twiddles
+
+@pytest.mark.parametrize("domain_log", [2, 3, 8, 13, 20, 23])
+def test_twiddles_match_oracle(B, domain_log):
+    t = _tree(B, domain_log)
+    tw, itw = O.canonic_twiddles(domain_log)
+    assert np.array_equal(t.twiddles.cpu().numpy().view(np.uint32), tw)
+    assert np.array_equal(t.itwiddles.cpu().numpy().view(np.uint32), itw)
+
+
+@pytest.mark.parametrize("log_n", [1, 3, 10, 17])
+def test_bit_reverse(B, log_n):
+    v = m31_column(9, log_n)
+    c = _col(v)
+    B.bit_reverse_column(c)
+    assert np.array_equal(c.to_cpu(), O.bit_reverse(v))
+
+
+# ------------------------------------------------------------------ FFT
+
+@pytest.mark.parametrize("log_n", list(range(1, 15)) + [16, 19, 20, 22])
+def test_interpolate_matches_oracle(B, log_n):
+    tree = _tree(B, log_n + 1)
+    _, itw = O.canonic_twiddles(log_n + 1)
+    cols_np = m31_columns(log_n, 3, log_n)
+    cols = [_col(c) for c in cols_np]
+    B.interpolate_columns(cols, tree)
+    want = O.interpolate_batch(list(cols_np), itw)
+    for c, w in zip(cols, want):
+        assert np.array_equal(c.to_cpu(), w)
+
+
+@pytest.mark.parametrize("log_c,log_n", [(0, 3), (1, 1), (1, 2), (2, 2), (2, 5), (3, 3), (3, 4), (5, 7), (8, 10),
+                                         (11, 12), (12, 14), (13, 13), (14, 15), (16, 18), (18, 20), (20, 22),
+                                         (20, 20), (21, 22)])
+def test_evaluate_matches_oracle(B, log_c, log_n):
+    tree = _tree(B, log_n + 1)
+    tw, _ = O.canonic_twiddles(log_n + 1)
+    coeffs_np = m31_columns(100 + log_c, 2, log_c)
+    coeffs = [_col(c) for c in coeffs_np]
+    out = B.evaluate_polynomials(coeffs, log_n, tree)
+    want = O.evaluate_batch(list(coeffs_np), [log_n] * 2, tw)
+    for o, w in zip(out, want):
+        assert np.array_equal(o.to_cpu(), w)
+
+
+def test_twiddle_tree_larger_than_domain(B):
+    # A tree for a bigger root coset serves every smaller canonic domain.
+    tree = _tree(B, 16)
+    _, itw = O.canonic_twiddles(16)
+    v = m31_column(3, 11)
+    c = _col(v)
+    B.interpolate_columns([c], tree)
+    assert np.array_equal(c.to_cpu(), O.interpolate(v, itw))
+
+
+def test_batch_over_256_columns(B):
+    # more columns than one launch's pointer table
+    tree = _tree(B, 9)
+    _, itw = O.canonic_twiddles(9)
+    cols_np = m31_columns(5, 300, 8)
+    cols = [_col(c) for c in cols_np]
+    B.interpolate_columns(cols, tree)
+    want = O.interpolate_batch(list(cols_np), itw)
+    assert all(np.array_equal(c.to_cpu(), w) for c, w in zip(cols, want))
+
+
+# ------------------------------------------------------------------ Merkle
+
+def _digests(t):
+    from proving_gb300.backend import digests_to_bytes
+    return digests_to_bytes(t)
+
+
+def test_merkle_leaves_kat(B):
+    k = KATS["lifted_merkle_leaves"]
+    cols = [_col(np.arange(1 << l, dtype=np.uint32)) for l in k["column_log_sizes"]]
+    leaves = _digests(B.build_leaves(cols, k["lifting_log_size"]))
+    for idx, hexd in k["leaves"].items():
+        assert leaves[int(idx)].tobytes().hex() == hexd
+
+
+@pytest.mark.parametrize("log_sizes,L", [([4], 4), ([3, 5, 5, 9], 9), ([1, 2], 6), ([6] * 16, 6), ([6] * 17, 6),
+                                         ([7] * 33, 10), (list(range(1, 13)) * 3, 14)])
+def test_merkle_commit_matches_oracle(B, log_sizes, L):
+    cols_np = [m31_column(i * 31 + l, l) for i, l in enumerate(log_sizes)]
+    perm = np.random.default_rng(0).permutation(len(cols_np))  # commit sorts (stably) by length
+    cols_np = [cols_np[i] for i in perm]
+    tree = B.merkle_commit([_col(c) for c in cols_np], L)
+    root, layers = O.merkle_commit(cols_np, L, with_layers=True)
+    assert tree.root() == root
+    for k, want in zip(range(L, -1, -1), layers):
+        assert np.array_equal(_digests(tree.layer(k)), want)
+
+
+def test_merkle_empty(B):
+    tree = B.merkle_commit([], 0)
+    assert tree.root() == hashlib.blake2s(b"").digest()
+
+
+def test_merkle_next_layer(B):
+    prev = np.frombuffer(np.random.default_rng(3).bytes(32 * 64), np.uint8).reshape(64, 32)
+    t = torch.from_numpy(prev.copy().view(np.int32).reshape(64, 8)).cuda()
+    got = _digests(B.build_next_layer(t))
+    assert np.array_equal(got, O.merkle_build_next_layer(prev))
+
+
+def test_pack_leaves_input(B):
+    coords = qm31_column(4, 6)
+    from proving_gb300.backend import BaseColumn
+    outs = B.pack_leaves_input([BaseColumn.from_cpu(c) for c in coords])
+    for coord in range(4):
+        for off in range(4):
+            assert np.array_equal(outs[coord + 4 * off].to_cpu(), coords[coord][off::4])
+
+
+# ------------------------------------------------------------------ FRI
+
+@pytest.mark.parametrize("log_n", [3, 4, 10, 16, 22])
+def test_fold_circle_into_line(B, log_n):
+    from proving_gb300.backend import SecureColumnByCoords
+    tree = _tree(B, log_n)
+    coords = qm31_column(log_n, log_n)
+    alpha = seeded_qm31(log_n)
+    got = B.fold_circle_into_line(SecureColumnByCoords.from_cpu(coords), alpha, tree).to_cpu()
+    want = O.fold_circle_into_line(coords, alpha)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+@pytest.mark.parametrize("log_n", [1, 2, 5, 12, 21])
+def test_fold_line(B, log_n):
+    from proving_gb300.backend import SecureColumnByCoords
+    tree = _tree(B, log_n + 1)
+    coords = qm31_column(50 + log_n, log_n)
+    alpha = seeded_qm31(log_n + 7)
+    got = B.fold_line(SecureColumnByCoords.from_cpu(coords), [alpha], tree).to_cpu()
+    want = O.fold_line(coords, O.line_domain_initial_index(log_n), alpha)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+def test_fri_fold_chain_22(B):
+    # Config-2 FRI: one QM31 column of log 22, fold_circle_into_line, then 21
+    # fold_line steps with seeded challenges, bit-exact at every layer.
+    from proving_gb300.backend import SecureColumnByCoords
+    log_n = 22
+    tree = _tree(B, log_n)
+    coords = qm31_column(22, log_n)
+    alphas = [seeded_qm31(1000 + k) for k in range(22)]
+    g = B.fold_circle_into_line(SecureColumnByCoords.from_cpu(coords), alphas[0], tree)
+    w = O.fold_circle_into_line(coords, alphas[0])
+    init = O.line_domain_initial_index(log_n - 1)
+    for k in range(1, 22):
+        g = B.fold_line(g, [alphas[k]], tree)
+        w = O.fold_line(w, init, alphas[k])
+        init = O.double_index(init)
+        if k % 5 == 0 or k == 21:
+            assert all(np.array_equal(a, b) for a, b in zip(g.to_cpu(), w))
+    assert len(g) == 1
+
+
+# ------------------------------------------------------------------ grind
+
+def test_grind_pow_kat(B):
+    k = KATS["verify_pow_nonce"]
+    digest = b"".join(int(w).to_bytes(4, "little") for w in k["digest_words"])
+    nonce = B.grind(digest, 10)
+    assert nonce == O.grind(digest, 10)
+    assert nonce <= 649  # 649 passes at 10 bits (blake2s.rs:234)
+
+
+@pytest.mark.parametrize("bits", [0, 1, 5, 12, 16])
+def test_grind_smallest_nonce(B, bits):
+    ch = O.Blake2sChannel()
+    ch.mix_u64(0x1111222233334344 + bits)
+    assert B.grind(ch.digest, bits) == O.grind(ch.digest, bits)
+
+
+def test_grind_gives_up(B):
+    from proving_gb300._lib import CudaBackendError
+    ch = O.Blake2sChannel()
+    with pytest.raises(CudaBackendError) as e:
+        B.grind(ch.digest, 32, max_nonce=1000)
+    assert "TIMEOUT" in str(e.value)
