@@ -39,8 +39,18 @@ UNIT = "proofs/s"
 N_COLS, LOG_ROWS, LOG_BLOWUP = 256, 20, 2
 LOG_EXT = LOG_ROWS + LOG_BLOWUP
 FRI_LOG = 22
-WORKLOAD = (f"commit-stage microbench: {N_COLS} M31 cols x 2^{LOG_ROWS}, interpolate, evaluate on log {LOG_EXT}, "
-            f"lifted Blake2s Merkle over {N_COLS}-wide leaves, 22 FRI folds of a QM31 col of log {FRI_LOG}")
+
+
+def workload_name():
+    return (f"commit-stage microbench: {N_COLS} M31 cols x 2^{LOG_ROWS}, interpolate, evaluate on log {LOG_EXT}, "
+            f"lifted Blake2s Merkle over {N_COLS}-wide leaves, {FRI_LOG} FRI folds of a QM31 col of log {FRI_LOG}")
+
+
+def set_shape(n_cols: int, log_rows: int):
+    global N_COLS, LOG_ROWS, LOG_EXT, FRI_LOG
+    N_COLS, LOG_ROWS = n_cols, log_rows
+    LOG_EXT = LOG_ROWS + LOG_BLOWUP
+    FRI_LOG = LOG_EXT
 
 
 def peaks():
@@ -121,8 +131,7 @@ class CommitStage:
             torch.int32)
         self.fri_src = torch.randint(0, P, (4, 1 << FRI_LOG), generator=g, device=dev, dtype=torch.int64).to(
             torch.int32)
-        self.alphas = torch.randint(0, P, (FRI_LOG, 4), generator=g, dtype=torch.int64, device="cpu").numpy().astype(
-            np.uint32)
+        self.alphas = np.random.default_rng(seed).integers(0, P, (FRI_LOG, 4), dtype=np.int64).astype(np.uint32)
         self.coeffs = torch.empty_like(self.evals)
         self.ext = torch.empty((N_COLS, 1 << LOG_EXT), dtype=torch.int32, device=dev)
         total = (1 << (LOG_EXT + 1)) - 1
@@ -253,19 +262,22 @@ def run_gpu(args):
         _lib.call("cs_memcpy_d2h", host_out.data_ptr() + 32, cs.fri_layers[-1].data_ptr(), 16, st)
         _lib.call("cs_stream_synchronize", st)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    barrier()
-    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e_lat = []
-    e_start.record()
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        e2e_step()
-        e_lat.append((time.perf_counter() - t0) * 1e3)
-    e_end.record()
-    barrier()
-    e2e_ms = e_start.elapsed_time(e_end)
+    e_lat = [float("nan")]
+    e2e_ms = float("nan")
+    if not args.skip_e2e:
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        barrier()
+        e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e_lat = []
+        e_start.record()
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            e2e_step()
+            e_lat.append((time.perf_counter() - t0) * 1e3)
+        e_end.record()
+        barrier()
+        e2e_ms = e_start.elapsed_time(e_end)
     t = torch.tensor([e2e_ms], device="cuda")
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -291,8 +303,8 @@ def run_gpu(args):
         "metric": METRIC, "value": ff(value), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ff(max_ms / args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "n_cols": N_COLS, "log_rows": LOG_ROWS, "log_blowup": LOG_BLOWUP,
-                   "merkle_height": LOG_EXT, "fri_log_size": FRI_LOG, "fri_folds": 22,
+        "config": {"workload": workload_name(), "n_cols": N_COLS, "log_rows": LOG_ROWS, "log_blowup": LOG_BLOWUP,
+                   "merkle_height": LOG_EXT, "fri_log_size": FRI_LOG, "fri_folds": FRI_LOG,
                    "l2": "inputs larger than L2 (1 GiB trace, 4 GiB extension); no flush",
                    "parallelism": f"replicas x{world}"},
         "latency_ms": {"p50": ff(float(np.percentile(step_lat, 50))), "p99": ff(float(np.percentile(step_lat, 99))),
@@ -380,7 +392,7 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": float(f"{1e3 * sum(totals) / args.steps:.6g}"),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
         "data": "synthetic (seeded)", "impl": "reference",
-        "config": {"workload": WORKLOAD, "n_cols": N_COLS, "log_rows": LOG_ROWS, "log_blowup": LOG_BLOWUP},
+        "config": {"workload": workload_name(), "n_cols": N_COLS, "log_rows": LOG_ROWS, "log_blowup": LOG_BLOWUP},
         "cpu_baseline": {"value": float(f"{value:.6g}"), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
                          "sample": sample + " (the Rust reference cannot be built: no cargo on this image)"},
         "e2e": {"value": float(f"{value:.6g}"), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -396,7 +408,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the timed oracle sample")
+    ap.add_argument("--n-cols", type=int, default=N_COLS, help="trace columns (smaller cases for profiling)")
+    ap.add_argument("--log-rows", type=int, default=LOG_ROWS, help="log2 rows per trace column")
+    ap.add_argument("--skip-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     args = ap.parse_args()
+    set_shape(args.n_cols, args.log_rows)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -169,6 +169,93 @@ cs_status cs_fold_circle_into_line(const uint32_t *const h_src[4], uint32_t log_
                                    uint32_t *const h_dst[4], const uint32_t *d_itwiddles,
                                    uint32_t twiddle_log_size, cs_stream stream);
 
+/* Same as cs_interpolate_columns on the subdomain of log size log_size of
+   CanonicCoset(domain_log_size): its first 2^log_size points in bit-reversed
+   order, a non-canonic circle domain. Its twiddles are the prefixes of the
+   domain's layers (TwiddleBuffer::extract_subdomain_twiddles,
+   crates/stwo/src/prover/poly/twiddles.rs:40-76); used by the quotient
+   combination (crates/stwo/src/prover/backend/cpu/quotients.rs:82-99) and
+   DomainEvaluationAccumulator::finalize
+   (crates/stwo/src/prover/air/accumulation.rs:153-167). In place. */
+cs_status cs_interpolate_columns_on_subdomain(uint32_t *const *h_cols, uint32_t n_cols, uint32_t log_size,
+                                              uint32_t domain_log_size, const uint32_t *d_itwiddles,
+                                              uint32_t twiddle_log_size, cs_stream stream);
+
+/* ------------------------------------------------------- accumulation */
+
+/* AccumulationOps::accumulate (crates/stwo/src/prover/air/accumulation.rs:186;
+   CPU crates/stwo/src/prover/backend/cpu/accumulation.rs:9-14): col += other
+   for QM31 columns of 2^log_size. */
+cs_status cs_accumulate(uint32_t *const h_col[4], const uint32_t *const h_other[4], uint32_t log_size,
+                        cs_stream stream);
+
+/* AccumulationOps::generate_secure_powers (accumulation.rs:189; CPU
+   cpu/accumulation.rs:16-24): felt^0 .. felt^(n-1) into h_out (4 words each).
+   Host computation, synchronous. */
+cs_status cs_generate_secure_powers(const uint32_t felt[4], uint32_t n_powers, uint32_t *h_out);
+
+/* AccumulationOps::lift_and_accumulate (accumulation.rs:198-200; CPU
+   cpu/accumulation.rs:26-47): h_cols holds n_cols x 4 coordinate pointers of
+   QM31 columns with strictly increasing log sizes; each column is updated in
+   place with the lift of the running sum, so the last holds the result. */
+cs_status cs_lift_and_accumulate(uint32_t *const *h_cols, const uint32_t *h_log_sizes, uint32_t n_cols,
+                                 cs_stream stream);
+
+/* ------------------------------------------------- out-of-domain samples */
+
+/* PolyOps::barycentric_weights_into (crates/stwo/src/prover/poly/circle/ops.rs:54-58;
+   CPU crates/stwo/src/prover/backend/cpu/circle.rs:100-132) for
+   CanonicCoset(log_size) and the QM31 point (px, py): 2^log_size QM31 weights
+   in bit-reversed order. The point must lie outside the domain. */
+cs_status cs_barycentric_weights(uint32_t log_size, const uint32_t px[4], const uint32_t py[4],
+                                 uint32_t *const h_out[4], cs_stream stream);
+
+/* PolyOps::barycentric_eval_at_point (ops.rs:70-78; CPU cpu/circle.rs:134-140)
+   for n_cols columns of 2^log_size sharing one weight column: d_out[4 i .. 4 i + 3]
+   receives column i's value (QM31). */
+cs_status cs_barycentric_eval(const uint32_t *const *h_cols, uint32_t n_cols, uint32_t log_size,
+                              const uint32_t *const h_weights[4], uint32_t *d_out, cs_stream stream);
+
+/* PolyOps::eval_at_point on coefficients (ops.rs:44-47; CPU cpu/circle.rs:81-98)
+   for n_cols coefficient columns of 2^log_size at the QM31 point (px, py):
+   d_out[4 i ..] receives column i's value. */
+cs_status cs_eval_at_point(const uint32_t *const *h_coeffs, uint32_t n_cols, uint32_t log_size, const uint32_t px[4],
+                           const uint32_t py[4], uint32_t *d_out, cs_stream stream);
+
+/* ------------------------------------------------------ DEEP quotients */
+
+/* QuotientOps::accumulate_numerators for one ColumnSampleBatch
+   (crates/stwo/src/prover/pcs/quotient_ops.rs:29-34; CPU
+   crates/stwo/src/prover/backend/cpu/quotients.rs:23-49): the batch's n_terms
+   columns (all of 2^log_size), and per term the line coefficients (a, b, c)
+   already scaled by the term's random power (12 words per term, from
+   complex_conjugate_line_coeffs, crates/stwo/src/core/constraints.rs:119-135).
+   Row r < 2^(log_size - log_blowup) of h_out gets sum_t (c_t col_t[r] - b_t);
+   first_linear_out = sum_t a_t. */
+cs_status cs_accumulate_numerators(const uint32_t *const *h_cols, uint32_t n_terms, uint32_t log_size,
+                                   uint32_t log_blowup, const uint32_t *h_coeffs, uint32_t *const h_out[4],
+                                   uint32_t first_linear_out[4], cs_stream stream);
+
+/* First half of QuotientOps::compute_quotients_and_combine
+   (quotient_ops.rs:47-52; CPU cpu/quotients.rs:51-81): for each of n_points
+   sample points (h_points: x then y, 8 words each) with its lifted partial
+   numerator column (h_accs: 4 coordinate pointers per point, log size
+   h_acc_log_sizes[k] <= L - b) and first linear term (4 words), the quotient
+   sum_k (acc_k[lifted r] - a_k * y) / den_k(x, y) on the subdomain of log
+   L - b of CanonicCoset(L), bit-reversed. The caller then interpolates it on
+   that subdomain and evaluates it on CanonicCoset(L). Up to 16 points. */
+cs_status cs_quotients_on_subdomain(const uint32_t *const *h_accs, const uint32_t *h_acc_log_sizes, uint32_t n_points,
+                                    const uint32_t *h_points, const uint32_t *h_first_linear, uint32_t lifting_log_size,
+                                    uint32_t log_blowup, uint32_t *const h_out[4], cs_stream stream);
+
+/* FriOps::decompose (crates/stwo/src/prover/fri.rs:73-75; CPU
+   crates/stwo/src/prover/backend/cpu/fri.rs:39-61,134-145): lambda = (sum of
+   the first half - sum of the second half) / 2^log_size; dst = src - lambda
+   on the first half, src + lambda on the second. Synchronous: lambda_out is
+   valid on return. Uses an 8-word stream-ordered device scratch buffer. */
+cs_status cs_decompose(const uint32_t *const h_src[4], uint32_t log_size, uint32_t *const h_dst[4],
+                       uint32_t lambda_out[4], cs_stream stream);
+
 /* -------------------------------------------------------- proof of work */
 
 /* GrindOps<Blake2sChannel>::grind (crates/stwo/src/core/proof_of_work.rs:10-14;

@@ -61,6 +61,21 @@ void orc_pow_prefixed_digest(const uint8_t digest[32], uint32_t n_bits, uint8_t 
 int orc_verify_pow_nonce(const uint8_t digest[32], uint32_t n_bits, uint64_t nonce);
 uint64_t orc_grind(const uint8_t digest[32], uint32_t n_bits);
 
+/* accumulation, quotients, out-of-domain sampling (oracle_pcs.c) */
+void orc_accumulate(uint32_t *const col[4], const uint32_t *const other[4], uint64_t n);
+void orc_generate_secure_powers(const uint32_t felt[4], uint32_t n, uint32_t *out);
+void orc_lift_and_accumulate(uint32_t *const *cols, const uint32_t *log_sizes, uint32_t n_cols);
+void orc_barycentric_weights(uint32_t log_n, const uint32_t px[4], const uint32_t py[4], uint32_t *const out[4]);
+void orc_barycentric_eval(const uint32_t *evals, uint32_t log_n, const uint32_t *const weights[4], uint32_t out[4]);
+void orc_line_coeffs(const uint32_t py[4], const uint32_t value[4], const uint32_t alpha[4], uint32_t out[12]);
+void orc_accumulate_numerators(const uint32_t **cols, uint32_t n_terms, uint32_t log_size, uint32_t log_blowup,
+                               const uint32_t *coeffs, uint32_t *const out[4], uint32_t first_linear_out[4]);
+void orc_quotients_on_subdomain(const uint32_t *const *accs, const uint32_t *acc_logs, uint32_t n_points,
+                                const uint32_t *points, const uint32_t *first_linear, uint32_t lifting_log_size,
+                                uint32_t log_blowup, uint32_t *const out[4]);
+void orc_decompose(const uint32_t *const in[4], uint32_t log_n, uint32_t *const out[4], uint32_t lambda_out[4]);
+void orc_random_point_from_t(const uint32_t t[4], uint32_t px[4], uint32_t py[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -317,3 +317,114 @@ def pow_prefixed_digest(digest: bytes, n_bits: int) -> bytes:
     out = np.zeros(32, np.uint8)
     lib().orc_pow_prefixed_digest(_p(d), ctypes.c_uint32(n_bits), _p(out))
     return out.tobytes()
+
+
+# ------------------------------------------------------- accumulation / PCS
+
+def _soa(coords):
+    return [_u32(c) for c in coords]
+
+
+def accumulate(col, other):
+    col = [_u32(c).copy() for c in col]
+    other = _soa(other)
+    lib().orc_accumulate(_ptr_array(col), _ptr_array(other), ctypes.c_uint64(col[0].size))
+    return col
+
+
+def generate_secure_powers(felt, n: int):
+    f = _u32(felt)
+    out = np.zeros(4 * max(n, 1), np.uint32)
+    lib().orc_generate_secure_powers(_p(f), ctypes.c_uint32(n), _p(out))
+    return out[: 4 * n].reshape(n, 4)
+
+
+def lift_and_accumulate(cols):
+    """cols: list of SoA QM31 columns (4 arrays each), strictly increasing length."""
+    cols = [[_u32(c).copy() for c in col] for col in cols]
+    flat = [c for col in cols for c in col]
+    logs = _u32([col[0].size.bit_length() - 1 for col in cols])
+    lib().orc_lift_and_accumulate(_ptr_array(flat), _p(logs), ctypes.c_uint32(len(cols)))
+    return cols[-1]
+
+
+def barycentric_weights(log_n: int, px, py):
+    out = [np.zeros(1 << log_n, np.uint32) for _ in range(4)]
+    x, y = _u32(px), _u32(py)
+    lib().orc_barycentric_weights(ctypes.c_uint32(log_n), _p(x), _p(y), _ptr_array(out))
+    return out
+
+
+def barycentric_eval(evals, weights):
+    e = _u32(evals)
+    w = _soa(weights)
+    out = np.zeros(4, np.uint32)
+    lib().orc_barycentric_eval(_p(e), ctypes.c_uint32(e.size.bit_length() - 1), _ptr_array(w), _p(out))
+    return out
+
+
+def line_coeffs(py, value, alpha):
+    y, v, a = _u32(py), _u32(value), _u32(alpha)
+    out = np.zeros(12, np.uint32)
+    lib().orc_line_coeffs(_p(y), _p(v), _p(a), _p(out))
+    return out.reshape(3, 4)
+
+
+def accumulate_numerators(cols, log_blowup: int, coeffs):
+    """cols: the batch's columns (same log size); coeffs: (n_terms, 3, 4) (a, b, c)."""
+    cols = [_u32(c) for c in cols]
+    co = np.ascontiguousarray(np.asarray(coeffs, np.uint32).reshape(-1))
+    log_size = cols[0].size.bit_length() - 1
+    rows = 1 << (log_size - log_blowup)
+    out = [np.zeros(rows, np.uint32) for _ in range(4)]
+    fl = np.zeros(4, np.uint32)
+    lib().orc_accumulate_numerators(_ptr_array(cols), ctypes.c_uint32(len(cols)), ctypes.c_uint32(log_size),
+                                    ctypes.c_uint32(log_blowup), _p(co), _ptr_array(out), _p(fl))
+    return out, fl
+
+
+def quotients_on_subdomain(accs, points, first_linear, lifting_log_size: int, log_blowup: int):
+    """accs: per sample point a SoA column; points: per point (x[4], y[4])."""
+    accs = [[_u32(c) for c in a] for a in accs]
+    flat = [c for a in accs for c in a]
+    logs = _u32([a[0].size.bit_length() - 1 for a in accs])
+    pts = np.ascontiguousarray(np.asarray([np.concatenate([_u32(x), _u32(y)]) for x, y in points],
+                                          np.uint32).reshape(-1))
+    fl = np.ascontiguousarray(np.asarray(first_linear, np.uint32).reshape(-1))
+    rows = 1 << (lifting_log_size - log_blowup)
+    out = [np.zeros(rows, np.uint32) for _ in range(4)]
+    lib().orc_quotients_on_subdomain(_ptr_array(flat), _p(logs), ctypes.c_uint32(len(accs)), _p(pts), _p(fl),
+                                     ctypes.c_uint32(lifting_log_size), ctypes.c_uint32(log_blowup), _ptr_array(out))
+    return out
+
+
+def decompose(coords):
+    ins = _soa(coords)
+    n = ins[0].size
+    out = [np.zeros(n, np.uint32) for _ in range(4)]
+    lam = np.zeros(4, np.uint32)
+    lib().orc_decompose(_ptr_array(ins), ctypes.c_uint32(n.bit_length() - 1), _ptr_array(out), _p(lam))
+    return out, lam
+
+
+def random_point_from_t(t):
+    tt = _u32(t)
+    x, y = np.zeros(4, np.uint32), np.zeros(4, np.uint32)
+    lib().orc_random_point_from_t(_p(tt), _p(x), _p(y))
+    return x, y
+
+
+def extract_subdomain_twiddles(buf: np.ndarray, domain_log_size: int, subdomain_log_size: int) -> np.ndarray:
+    """TwiddleBuffer::extract_subdomain_twiddles (crates/stwo/src/prover/poly/twiddles.rs:40-76)."""
+    dh, sh = domain_log_size - 1, subdomain_log_size - 1
+    bh = buf.size.bit_length() - 1
+    assert sh <= dh <= bh
+    skip = bh - dh
+    bsz = 1 << bh
+    out = []
+    for layer in range(sh):
+        root_layer = skip + layer
+        start = bsz - (bsz >> root_layer)
+        out.append(buf[start:start + (1 << (sh - 1 - layer))])
+    out.append(buf[-1:])
+    return np.concatenate(out).astype(np.uint32)

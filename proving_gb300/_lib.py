@@ -44,6 +44,16 @@ SIGNATURES = {
     "cs_fold_line": [vp, u32, vp, vp, vp, u32, vp],
     "cs_fold_circle_into_line": [vp, u32, vp, vp, vp, u32, vp],
     "cs_grind_blake2s": [vp, u32, u64, ctypes.POINTER(ctypes.c_uint64), vp],
+    "cs_interpolate_columns_on_subdomain": [vp, u32, u32, u32, vp, u32, vp],
+    "cs_accumulate": [vp, vp, u32, vp],
+    "cs_generate_secure_powers": [vp, u32, vp],
+    "cs_lift_and_accumulate": [vp, vp, u32, vp],
+    "cs_barycentric_weights": [u32, vp, vp, vp, vp],
+    "cs_barycentric_eval": [vp, u32, u32, vp, vp, vp],
+    "cs_eval_at_point": [vp, u32, u32, vp, vp, vp, vp],
+    "cs_accumulate_numerators": [vp, u32, u32, u32, vp, vp, vp, vp],
+    "cs_quotients_on_subdomain": [vp, vp, u32, vp, vp, u32, u32, vp, vp],
+    "cs_decompose": [vp, u32, vp, vp, vp],
 }
 _RESTYPES = {"cs_last_error": ctypes.c_char_p, "cs_version": ctypes.c_char_p,
              "cs_kernel_launch_count": ctypes.c_uint64}

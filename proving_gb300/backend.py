@@ -252,6 +252,101 @@ class CudaBackend:
                   _ptr_table([c.data for c in dst.columns]), _ptr(twiddles.itwiddles), twiddles.log_size, _stream())
         return dst
 
+    @staticmethod
+    def decompose(src: SecureColumnByCoords):
+        """FriOps::decompose: returns (g, lambda)."""
+        n = len(src)
+        dst = SecureColumnByCoords.uninitialized(n)
+        lam = (ctypes.c_uint32 * 4)()
+        _lib.call("cs_decompose", _ptr_table([c.data for c in src.columns]), n.bit_length() - 1,
+                  _ptr_table([c.data for c in dst.columns]), lam, _stream())
+        return dst, np.array(list(lam), np.uint32)
+
+    # AccumulationOps -------------------------------------------------------------
+    @staticmethod
+    def accumulate(col: SecureColumnByCoords, other: SecureColumnByCoords) -> None:
+        _lib.call("cs_accumulate", _ptr_table([c.data for c in col.columns]),
+                  _ptr_table([c.data for c in other.columns]), len(col).bit_length() - 1, _stream())
+
+    @staticmethod
+    def generate_secure_powers(felt, n_powers: int) -> np.ndarray:
+        out = (ctypes.c_uint32 * max(4, 4 * n_powers))()
+        _lib.call("cs_generate_secure_powers", _u32_table(felt), n_powers, out)
+        return np.array(list(out), np.uint32)[: 4 * n_powers].reshape(n_powers, 4)
+
+    @staticmethod
+    def lift_and_accumulate(cols):
+        """Columns with strictly increasing sizes, updated in place; returns the last (or None)."""
+        if not cols:
+            return None
+        tab = _ptr_table([c.data for col in cols for c in col.columns])
+        logs = _u32_table([len(c).bit_length() - 1 for c in cols])
+        _lib.call("cs_lift_and_accumulate", tab, logs, len(cols), _stream())
+        return cols[-1]
+
+    # out-of-domain sampling ------------------------------------------------------
+    @staticmethod
+    def barycentric_weights(log_size: int, point) -> SecureColumnByCoords:
+        px, py = point
+        out = SecureColumnByCoords.uninitialized(1 << log_size)
+        _lib.call("cs_barycentric_weights", log_size, _u32_table(px), _u32_table(py),
+                  _ptr_table([c.data for c in out.columns]), _stream())
+        return out
+
+    @staticmethod
+    def barycentric_eval_at_point(evals, weights: SecureColumnByCoords) -> torch.Tensor:
+        out = torch.empty((len(evals), 4), dtype=torch.int32, device="cuda")
+        _lib.call("cs_barycentric_eval", _ptr_table([e.data for e in evals]), len(evals),
+                  len(weights).bit_length() - 1, _ptr_table([c.data for c in weights.columns]), _ptr(out),
+                  _stream())
+        return out
+
+    @staticmethod
+    def eval_at_point(coeffs, point) -> torch.Tensor:
+        px, py = point
+        out = torch.empty((len(coeffs), 4), dtype=torch.int32, device="cuda")
+        _lib.call("cs_eval_at_point", _ptr_table([c.data for c in coeffs]), len(coeffs),
+                  coeffs[0].log_size, _u32_table(px), _u32_table(py), _ptr(out), _stream())
+        return out
+
+    # QuotientOps -------------------------------------------------------------------
+    @staticmethod
+    def accumulate_numerators(columns, line_coeffs, log_blowup: int):
+        """One sample batch: columns (same size) and their (a, b, c) line coefficients (n, 3, 4).
+        Returns (partial_numerators_acc, first_linear_term_acc)."""
+        log_size = columns[0].log_size
+        out = SecureColumnByCoords.uninitialized(1 << (log_size - log_blowup))
+        co = np.ascontiguousarray(np.asarray(line_coeffs, np.uint32).reshape(-1))
+        fl = (ctypes.c_uint32 * 4)()
+        _lib.call("cs_accumulate_numerators", _ptr_table([c.data for c in columns]), len(columns), log_size,
+                  log_blowup, co.ctypes.data, _ptr_table([c.data for c in out.columns]), fl, _stream())
+        return out, np.array(list(fl), np.uint32)
+
+    @staticmethod
+    def interpolate_on_subdomain(columns, domain_log_size: int, twiddles: TwiddleTree) -> None:
+        _lib.call("cs_interpolate_columns_on_subdomain", _ptr_table([c.data for c in columns]), len(columns),
+                  columns[0].log_size, domain_log_size, _ptr(twiddles.itwiddles), twiddles.log_size, _stream())
+
+    @staticmethod
+    def quotients_on_subdomain(accs, points, first_linear, lifting_log_size: int, log_blowup: int):
+        out = SecureColumnByCoords.uninitialized(1 << (lifting_log_size - log_blowup))
+        tab = _ptr_table([c.data for a in accs for c in a.columns])
+        logs = _u32_table([len(a).bit_length() - 1 for a in accs])
+        pts = np.ascontiguousarray(np.concatenate([np.concatenate([np.asarray(x, np.uint32), np.asarray(y, np.uint32)])
+                                                   for x, y in points]))
+        fl = np.ascontiguousarray(np.asarray(first_linear, np.uint32).reshape(-1))
+        _lib.call("cs_quotients_on_subdomain", tab, logs, len(accs), pts.ctypes.data, fl.ctypes.data,
+                  lifting_log_size, log_blowup, _ptr_table([c.data for c in out.columns]), _stream())
+        return out
+
+    @classmethod
+    def compute_quotients_and_combine(cls, accs, points, first_linear, lifting_log_size: int, log_blowup: int,
+                                      twiddles: TwiddleTree) -> SecureColumnByCoords:
+        """QuotientOps::compute_quotients_and_combine (crates/stwo/src/prover/pcs/quotient_ops.rs:47-52)."""
+        q = cls.quotients_on_subdomain(accs, points, first_linear, lifting_log_size, log_blowup)
+        cls.interpolate_on_subdomain(q.columns, lifting_log_size, twiddles)
+        return SecureColumnByCoords(cls.evaluate_polynomials(q.columns, lifting_log_size, twiddles))
+
     # GrindOps -----------------------------------------------------------------
     @staticmethod
     def grind(digest: bytes, pow_bits: int, max_nonce: int = 1 << 48) -> int:

@@ -46,12 +46,14 @@ struct FftPass {
   uint32_t scale;     // 0: none; else outputs are multiplied by it
   const uint32_t* tw; // twiddle (forward) or itwiddle (inverse) tree
   uint32_t tw_log;    // log2 of the tree length
+  uint32_t tw_dom;    // log size of the canonic domain whose twiddle layers are used (>= log_n;
+                      // larger for a subdomain, which takes the prefix of each layer)
 };
 
 __device__ __forceinline__ uint32_t twiddle_at(const FftPass& p, uint32_t layer, uint32_t h) {
   const uint32_t tw_len = 1u << p.tw_log;
   if (layer == 0) {
-    const uint32_t* lt1 = p.tw + (tw_len - (1u << (p.log_n - 1)));
+    const uint32_t* lt1 = p.tw + (tw_len - (1u << (p.tw_dom - 1)));
     const uint32_t pair = (h >> 2) << 1;
     const uint32_t x = __ldg(lt1 + pair), y = __ldg(lt1 + pair + 1);
     switch (h & 3) {
@@ -61,7 +63,7 @@ __device__ __forceinline__ uint32_t twiddle_at(const FftPass& p, uint32_t layer,
       default: return x;
     }
   }
-  return __ldg(p.tw + (tw_len - (1u << (p.log_n - layer))) + h);
+  return __ldg(p.tw + (tw_len - (1u << (p.tw_dom - layer))) + h);
 }
 
 struct Tile {
@@ -248,13 +250,14 @@ cpoint index_to_point_host(uint32_t idx) {
   return r;
 }
 
-SmallParams small_constants(uint32_t log_n, uint32_t log_src, bool inverse) {
+SmallParams small_constants(uint32_t log_n, uint32_t log_src, bool inverse, uint32_t tw_dom) {
   SmallParams sp{};
   sp.log_n = log_n;
   sp.log_src = log_src;
   sp.inverse = inverse ? 1 : 0;
-  // CanonicCoset(log_n).half_coset() = half_odds(log_n - 1): initial index 2^(31 - (log_n + 1)).
-  const cpoint init = index_to_point_host(subgroup_gen(log_n + 1));
+  // The half coset of CanonicCoset(tw_dom) starts at index 2^(31 - (tw_dom + 1)); a subdomain
+  // (its bit-reversed prefix) shares that first point.
+  const cpoint init = index_to_point_host(subgroup_gen(tw_dom + 1));
   if (log_n == 1) {
     if (inverse) {
       const uint32_t nn = 2;
@@ -338,7 +341,9 @@ cs_status launch_pass(const FftBatch& b, uint32_t n_cols, const FftPass& p, cons
 // Runs the FFT over a batch of columns. inverse: interpolate in place
 // (src == dst); forward: evaluate from coefficients of log_src into dst of log_n.
 cs_status run_fft(const uint32_t* const* srcs, uint32_t* const* dsts, uint32_t n_cols, uint32_t log_src,
-                  uint32_t log_n, bool inverse, const uint32_t* tw, uint32_t tw_log, cudaStream_t st) {
+                  uint32_t log_n, bool inverse, const uint32_t* tw, uint32_t tw_log, cudaStream_t st,
+                  uint32_t tw_dom = 0) {
+  if (tw_dom == 0) tw_dom = log_n;
   for (uint32_t b0 = 0; b0 < n_cols; b0 += kMaxBatch) {
     const uint32_t nb = std::min<uint32_t>(kMaxBatch, n_cols - b0);
     FftBatch batch;
@@ -347,7 +352,7 @@ cs_status run_fft(const uint32_t* const* srcs, uint32_t* const* dsts, uint32_t n
       batch.dst[i] = dsts[b0 + i];
     }
     if (log_n <= 2) {
-      SmallParams sp = small_constants(log_n, log_src, inverse);
+      SmallParams sp = small_constants(log_n, log_src, inverse, tw_dom);
       fft_small_kernel<<<(nb + 127) / 128, 128, 0, st>>>(batch, nb, sp);
       CS_LAUNCHED("fft_small_kernel");
       continue;
@@ -358,6 +363,7 @@ cs_status run_fft(const uint32_t* const* srcs, uint32_t* const* dsts, uint32_t n
     p.log_n = log_n;
     p.tw = tw;
     p.tw_log = tw_log;
+    p.tw_dom = tw_dom;
     if (inverse) {
       for (size_t k = 0; k < plan.size(); k++) {
         const PassPlan& pp = plan[k];
@@ -433,6 +439,21 @@ extern "C" cs_status cs_interpolate_columns_into(const uint32_t* const* h_evals,
     CS_CHECK_ARG(h_evals[i] != nullptr && h_coeffs[i] != nullptr, "interpolate_into: column %u is null", i);
   return run_fft(h_evals, h_coeffs, n_cols, log_size, log_size, true, d_itwiddles, twiddle_log_size,
                  to_stream(stream));
+}
+
+extern "C" cs_status cs_interpolate_columns_on_subdomain(uint32_t* const* h_cols, uint32_t n_cols, uint32_t log_size,
+                                                         uint32_t domain_log_size, const uint32_t* d_itwiddles,
+                                                         uint32_t twiddle_log_size, cs_stream stream) {
+  CS_CHECK_ARG(n_cols == 0 || h_cols != nullptr, "interpolate_on_subdomain: null column table");
+  CS_CHECK_ARG(log_size >= 1 && log_size <= domain_log_size && domain_log_size <= 28,
+               "interpolate_on_subdomain: bad sizes %u / %u", log_size, domain_log_size);
+  CS_CHECK_ARG(log_size <= 2 || (d_itwiddles != nullptr && twiddle_log_size + 1 >= domain_log_size),
+               "interpolate_on_subdomain: twiddle tree of log %u does not cover a domain of log %u",
+               twiddle_log_size, domain_log_size);
+  for (uint32_t i = 0; i < n_cols; i++)
+    CS_CHECK_ARG(h_cols[i] != nullptr, "interpolate_on_subdomain: column %u is null", i);
+  return run_fft(h_cols, h_cols, n_cols, log_size, log_size, true, d_itwiddles, twiddle_log_size,
+                 to_stream(stream), domain_log_size);
 }
 
 extern "C" cs_status cs_evaluate_columns(const uint32_t* const* h_coeffs, uint32_t* const* h_evals, uint32_t n_cols,

@@ -1,0 +1,581 @@
+// Accumulation, DEEP quotients and out-of-domain sampling on sm_103a.
+//
+//  - accumulate / lift_and_accumulate: crates/stwo/src/prover/backend/cpu/accumulation.rs:9-47
+//  - barycentric weights / eval: crates/stwo/src/prover/backend/cpu/circle.rs:100-140
+//  - eval_at_point on coefficients: cpu/circle.rs:81-98 with fold (crates/stwo/src/core/poly/utils.rs:27-38)
+//  - accumulate_numerators: crates/stwo/src/prover/backend/cpu/quotients.rs:23-49
+//  - quotients on the evaluation subdomain: cpu/quotients.rs:51-81 with
+//    denominator_inverses (crates/stwo/src/core/pcs/quotients.rs:233-256)
+//  - decompose: crates/stwo/src/prover/backend/cpu/fri.rs:39-61,134-145
+//
+// All field arithmetic is exact, so any evaluation order gives the
+// reference's values. Two identities keep the kernels cheap:
+//  * coset_vanishing(CanonicCoset(k).coset, q) = pi^(k-1)(q.x): the coset's
+//    initial point and its half step cancel (constraints.rs:12-34), so the
+//    barycentric derivative term is 4^(l-1) * prod_{k<l} pi^(k-1)(x_i).
+//  * sums of M31 products are accumulated in 64 bits and reduced once.
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "field.cuh"
+#include "pcs.cuh"
+
+namespace cs {
+
+namespace {
+
+__host__ __device__ __forceinline__ uint32_t reduce64(uint64_t v) {
+  // v < 2^62: v mod P by folding at bit 31 twice
+  uint64_t t = (v & P) + (v >> 31);
+  uint32_t u = (uint32_t)((t & P) + (t >> 31));
+  return m31_reduce_once(u);
+}
+
+__device__ __forceinline__ uint32_t dbl_x(uint32_t x) {
+  const uint32_t s = m31_sqr(x);
+  return m31_sub(m31_add(s, s), 1);
+}
+
+struct SoA {
+  uint32_t* c[4];
+};
+struct CSoA {
+  const uint32_t* c[4];
+};
+
+__device__ __forceinline__ qm31 ld(const CSoA& a, uint32_t i) {
+  return qm31_make(a.c[0][i], a.c[1][i], a.c[2][i], a.c[3][i]);
+}
+__device__ __forceinline__ qm31 ld(const SoA& a, uint32_t i) {
+  return qm31_make(a.c[0][i], a.c[1][i], a.c[2][i], a.c[3][i]);
+}
+__device__ __forceinline__ void st(const SoA& a, uint32_t i, qm31 v) {
+  a.c[0][i] = v.a.a;
+  a.c[1][i] = v.a.b;
+  a.c[2][i] = v.b.a;
+  a.c[3][i] = v.b.b;
+}
+
+uint32_t grid_for(uint64_t n, uint32_t threads) {
+  return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((n + threads - 1) / threads, 152 * 16));
+}
+
+// ---------------------------------------------------------------- accumulation
+
+__global__ void accumulate_kernel(SoA col, CSoA other, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    st(col, i, qm31_add(ld(col, i), ld(other, i)));
+}
+
+// col[i] += prev[(i >> (log_ratio + 1) << 1) + (i & 1)]; prev == nullptr means zeros.
+__global__ void lift_add_kernel(SoA col, CSoA prev, bool has_prev, uint32_t log_n, uint32_t log_ratio) {
+  const uint32_t n = 1u << log_n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!has_prev) continue;
+    const uint32_t j = ((i >> (log_ratio + 1)) << 1) + (i & 1);
+    st(col, i, qm31_add(ld(col, i), ld(prev, j)));
+  }
+}
+
+// ---------------------------------------------------------------- barycentric
+
+struct BaryParams {
+  cpoint gen_pow[31];   // 2^b * G
+  uint32_t half_init;   // initial index of the canonic half coset
+  uint32_t half_step;   // its step index
+  uint32_t log_n;
+  uint32_t four_pow;    // 4^(log_n - 1)
+  qm31 px, py, vn_p;    // sample point and V_n(p) = pi^(log_n - 1)(p.x)
+};
+
+__device__ __forceinline__ cpoint point_at(const cpoint* g, uint32_t idx) {
+  cpoint r{1, 0};
+#pragma unroll 1
+  for (int b = 0; b < 31; b++)
+    if ((idx >> b) & 1) r = cpoint_add(r, g[b]);
+  return r;
+}
+
+// Point of natural index j of a circle domain with the given half coset.
+__device__ __forceinline__ cpoint domain_point(const cpoint* g, uint32_t half_init, uint32_t half_step,
+                                               uint32_t half_log, uint32_t j) {
+  const uint32_t hs = 1u << half_log;
+  uint32_t idx;
+  if (j < hs)
+    idx = (half_init + j * half_step) & 0x7fffffffu;
+  else
+    idx = (0u - (half_init + (j - hs) * half_step)) & 0x7fffffffu;
+  return point_at(g, idx);
+}
+
+__global__ void bary_weights_kernel(const BaryParams p, SoA out) {
+  const uint32_t n = 1u << p.log_n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t j = __brev(i) >> (32 - p.log_n);
+    const cpoint xi = domain_point(p.gen_pow, p.half_init, p.half_step, p.log_n - 1, j);
+    // si = -2 y_i * 4^(l-1) * prod_{k=1}^{l-1} pi^(k-1)(x_i)
+    uint32_t prod = 1, x = xi.x;
+    for (uint32_t k = 1; k < p.log_n; k++) {
+      prod = m31_mul(prod, x);
+      x = dbl_x(x);
+    }
+    const uint32_t si = m31_mul(m31_mul(xi.y, m31_neg(2)), m31_mul(p.four_pow, prod));
+    // h = p - x_i = (px*x + py*y, py*x - px*y)
+    const qm31 hx = qm31_add(qm31_mul_m31(p.px, xi.x), qm31_mul_m31(p.py, xi.y));
+    const qm31 hy = qm31_sub(qm31_mul_m31(p.py, xi.x), qm31_mul_m31(p.px, xi.y));
+    // W = V_n(p) * (1 + h.x) / (h.y * si)
+    const qm31 num = qm31_mul(p.vn_p, qm31_add_m31(hx, 1));
+    const qm31 den = qm31_mul_m31(hy, si);
+    st(out, i, qm31_mul(num, qm31_inv(den)));
+  }
+}
+
+// ---------------------------------------------------------------- reductions
+
+__device__ __forceinline__ void block_reduce_u64x4(uint64_t acc[4], uint64_t* sh /* 4 * warps */) {
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int k = 0; k < 4; k++) sh[4 * warp + k] = acc[k];
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int k = 0; k < 4; k++) acc[k] = lane < nw ? sh[4 * lane + k] : 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
+  }
+}
+
+// One block per column: sum_i W_i * v[i]. Partial sums stay below 2^64:
+// every term is reduced to < 2^31 before it is added, at most 2^30 terms.
+__global__ void bary_eval_kernel(const BaryColumns cols, uint32_t log_n, CSoA w, uint32_t* out) {
+  __shared__ uint64_t sh[4 * 32];
+  const uint32_t n = 1u << log_n;
+  const uint32_t* v = cols.ptr[blockIdx.x];
+  uint64_t acc[4] = {0, 0, 0, 0};
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const uint32_t x = __ldg(v + i);
+#pragma unroll
+    for (int k = 0; k < 4; k++) acc[k] += m31_mul(__ldg(w.c[k] + i), x);
+  }
+  block_reduce_u64x4(acc, sh);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 4; k++) out[4 * blockIdx.x + k] = reduce64(acc[k] % P);
+}
+
+// ---------------------------------------------------------------- eval_at_point
+
+struct FoldFactors {
+  qm31 f[32];  // f[0] = y, f[1] = x, f[j] = pi^(j-1)(x)
+  uint32_t log_n;
+};
+
+// One block per column. A warp folds a 256-coefficient chunk against the
+// table T[m] = prod_{bits j of m} f[j] (m < 256), then scales by the chunk's
+// high factor prod_{bits j of h} f[8 + j].
+__global__ void eval_at_point_kernel(const BaryColumns cols, const FoldFactors ff, uint32_t* out) {
+  __shared__ qm31 T[256];
+  __shared__ qm31 warp_acc[32];
+  const uint32_t log_n = ff.log_n;
+  const uint32_t* c = cols.ptr[blockIdx.x];
+  const uint32_t low = min(log_n, 8u);
+  const uint32_t tsize = 1u << low;
+  for (uint32_t m = threadIdx.x; m < tsize; m += blockDim.x) {
+    qm31 b = qm31_make(1, 0, 0, 0);
+    for (uint32_t j = 0; j < low; j++)
+      if ((m >> j) & 1) b = qm31_mul(b, ff.f[j]);
+    T[m] = b;
+  }
+  __syncthreads();
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const uint32_t n_chunks = 1u << (log_n - low);
+  qm31 wacc = qm31_make(0, 0, 0, 0);
+  for (uint32_t h = warp; h < n_chunks; h += nw) {
+    uint64_t a[4] = {0, 0, 0, 0};
+    for (uint32_t m = lane; m < tsize; m += 32) {
+      const uint32_t x = __ldg(c + ((size_t)h << low) + m);
+      const qm31 t = T[m];
+      a[0] += m31_mul(t.a.a, x);
+      a[1] += m31_mul(t.a.b, x);
+      a[2] += m31_mul(t.b.a, x);
+      a[3] += m31_mul(t.b.b, x);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      for (int o = 16; o > 0; o >>= 1) a[k] += __shfl_down_sync(0xffffffffu, a[k], o);
+    if (lane == 0) {
+      qm31 s = qm31_make(reduce64(a[0] % P), reduce64(a[1] % P), reduce64(a[2] % P), reduce64(a[3] % P));
+      for (uint32_t j = 0; (h >> j) != 0; j++)
+        if ((h >> j) & 1) s = qm31_mul(s, ff.f[low + j]);
+      wacc = qm31_add(wacc, s);
+    }
+  }
+  if (lane == 0) warp_acc[warp] = wacc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    qm31 r = qm31_make(0, 0, 0, 0);
+    for (uint32_t k = 0; k < nw; k++) r = qm31_add(r, warp_acc[k]);
+    out[4 * blockIdx.x + 0] = r.a.a;
+    out[4 * blockIdx.x + 1] = r.a.b;
+    out[4 * blockIdx.x + 2] = r.b.a;
+    out[4 * blockIdx.x + 3] = r.b.b;
+  }
+}
+
+// ---------------------------------------------------------------- numerators
+
+// row r: sum_t c_t * col_t[r] - sum_t b_t (the batch's partial numerator).
+__global__ void numerators_kernel(const NumeratorTerms terms, uint32_t rows, SoA out, bool accumulate) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    uint64_t a[4] = {0, 0, 0, 0};
+    for (uint32_t t = 0; t < terms.n; t++) {
+      const uint32_t v = __ldg(terms.col[t] + r);
+      const qm31 c = terms.c[t];
+      a[0] += m31_mul(c.a.a, v);
+      a[1] += m31_mul(c.a.b, v);
+      a[2] += m31_mul(c.b.a, v);
+      a[3] += m31_mul(c.b.b, v);
+    }
+    qm31 s = qm31_make(reduce64(a[0] % P), reduce64(a[1] % P), reduce64(a[2] % P), reduce64(a[3] % P));
+    s = qm31_sub(s, terms.b_sum);
+    if (accumulate) s = qm31_add(s, ld(out, r));
+    st(out, r, s);
+  }
+}
+
+// ---------------------------------------------------------------- quotients
+
+__global__ void quotients_kernel(const QuotientParams q, SoA out) {
+  const uint32_t rows = 1u << q.sub_log;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    const uint32_t j = __brev(r) >> (32 - q.sub_log);
+    const cpoint dp = domain_point(q.gen_pow, q.half_init, q.half_step, q.sub_log - 1, j);
+    qm31 acc = qm31_make(0, 0, 0, 0);
+    for (uint32_t k = 0; k < q.n_points; k++) {
+      const qm31 px = q.px[k], py = q.py[k];
+      // (prx - x) * piy - (pry - y) * pix in CM31
+      const cm31 dx = cm31_sub(px.a, cm31{dp.x, 0}), dy = cm31_sub(py.a, cm31{dp.y, 0});
+      const cm31 den = cm31_sub(cm31_mul(dx, py.b), cm31_mul(dy, px.b));
+      const cm31 den_inv = cm31_inv(den);
+      const uint32_t log_ratio = q.sub_log - q.acc_log[k];
+      const uint32_t li = ((r >> (log_ratio + 1)) << 1) + (r & 1);
+      const qm31 partial = qm31_make(q.acc[k].c[0][li], q.acc[k].c[1][li], q.acc[k].c[2][li], q.acc[k].c[3][li]);
+      const qm31 num = qm31_sub(partial, qm31_mul_m31(q.first_linear[k], dp.y));
+      acc = qm31_add(acc, qm31_mul_cm31(num, den_inv));
+    }
+    st(out, r, acc);
+  }
+}
+
+// ---------------------------------------------------------------- decompose
+
+__global__ void half_sums_kernel(CSoA in, uint32_t log_n, uint32_t* sums /* 8 words */) {
+  __shared__ uint64_t sh[4 * 32];
+  const uint32_t half = 1u << (log_n - 1);
+  const uint32_t which = blockIdx.x;  // 0: first half, 1: second half
+  uint64_t acc[4] = {0, 0, 0, 0};
+  for (uint32_t i = threadIdx.x; i < half; i += blockDim.x) {
+    const uint32_t idx = which * half + i;
+#pragma unroll
+    for (int k = 0; k < 4; k++) acc[k] += in.c[k][idx];
+  }
+  block_reduce_u64x4(acc, sh);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 4; k++) sums[4 * which + k] = reduce64(acc[k] % P);
+}
+
+__global__ void decompose_apply_kernel(CSoA in, SoA out, uint32_t log_n, qm31 lambda) {
+  const uint32_t n = 1u << log_n, half = n >> 1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    st(out, i, i < half ? qm31_sub(ld(in, i), lambda) : qm31_add(ld(in, i), lambda));
+}
+
+}  // namespace
+
+GenPowersTable gen_powers() {
+  GenPowersTable t;
+  cpoint cur{2u, 1268011823u};
+  for (int b = 0; b < 31; b++) {
+    t.p[b] = cur;
+    cur = cpoint_add(cur, cur);
+  }
+  return t;
+}
+
+cs_status quotients_on_subdomain(const QuotientParams& q, uint32_t* const out[4], cudaStream_t st) {
+  SoA o;
+  for (int k = 0; k < 4; k++) o.c[k] = out[k];
+  const uint32_t rows = 1u << q.sub_log;
+  quotients_kernel<<<grid_for(rows, 256), 256, 0, st>>>(q, o);
+  CS_LAUNCHED("quotients_kernel");
+  return CS_OK;
+}
+
+}  // namespace cs
+
+using namespace cs;
+
+static cs_status check4(const uint32_t* const p[4], const char* what) {
+  CS_CHECK_ARG(p != nullptr, "%s: null coordinate table", what);
+  for (int k = 0; k < 4; k++) CS_CHECK_ARG(p[k] != nullptr, "%s: coordinate %d is null", what, k);
+  return CS_OK;
+}
+
+extern "C" cs_status cs_accumulate(uint32_t* const h_col[4], const uint32_t* const h_other[4], uint32_t log_size,
+                                   cs_stream stream) {
+  cs_status s = check4(h_col, "accumulate");
+  if (s == CS_OK) s = check4(h_other, "accumulate");
+  if (s != CS_OK) return s;
+  CS_CHECK_ARG(log_size <= 30, "accumulate: log size %u too large", log_size);
+  SoA c;
+  CSoA o;
+  for (int k = 0; k < 4; k++) {
+    c.c[k] = h_col[k];
+    o.c[k] = h_other[k];
+  }
+  const uint32_t n = 1u << log_size;
+  accumulate_kernel<<<grid_for(n, 256), 256, 0, to_stream(stream)>>>(c, o, n);
+  CS_LAUNCHED("accumulate_kernel");
+  return CS_OK;
+}
+
+extern "C" cs_status cs_generate_secure_powers(const uint32_t felt[4], uint32_t n_powers, uint32_t* h_out) {
+  CS_CHECK_ARG(felt != nullptr && (n_powers == 0 || h_out != nullptr), "generate_secure_powers: null pointer");
+  const qm31 f = qm31_make(felt[0], felt[1], felt[2], felt[3]);
+  qm31 acc = qm31_make(1, 0, 0, 0);
+  for (uint32_t i = 0; i < n_powers; i++) {
+    h_out[4 * i] = acc.a.a;
+    h_out[4 * i + 1] = acc.a.b;
+    h_out[4 * i + 2] = acc.b.a;
+    h_out[4 * i + 3] = acc.b.b;
+    acc = qm31_mul(acc, f);
+  }
+  return CS_OK;
+}
+
+extern "C" cs_status cs_lift_and_accumulate(uint32_t* const* h_cols, const uint32_t* h_log_sizes, uint32_t n_cols,
+                                            cs_stream stream) {
+  CS_CHECK_ARG(n_cols == 0 || (h_cols != nullptr && h_log_sizes != nullptr), "lift_and_accumulate: null table");
+  uint32_t prev_log = 1;
+  for (uint32_t k = 0; k < n_cols; k++) {
+    const uint32_t l = h_log_sizes[k];
+    CS_CHECK_ARG(l >= 1 && l <= 30, "lift_and_accumulate: column %u has log size %u", k, l);
+    CS_CHECK_ARG(k == 0 ? l >= 1 : l > prev_log, "lift_and_accumulate: sizes must be strictly increasing (column %u)",
+                 k);
+    for (int c = 0; c < 4; c++) CS_CHECK_ARG(h_cols[4 * k + c] != nullptr, "lift_and_accumulate: null column");
+    prev_log = l;
+  }
+  prev_log = 1;
+  for (uint32_t k = 0; k < n_cols; k++) {
+    const uint32_t l = h_log_sizes[k];
+    if (k == 0) {
+      prev_log = l;  // lifting zeros adds nothing
+      continue;
+    }
+    SoA col;
+    CSoA prev;
+    for (int c = 0; c < 4; c++) {
+      col.c[c] = h_cols[4 * k + c];
+      prev.c[c] = h_cols[4 * (k - 1) + c];
+    }
+    lift_add_kernel<<<grid_for(1u << l, 256), 256, 0, to_stream(stream)>>>(col, prev, true, l, l - prev_log);
+    CS_LAUNCHED("lift_add_kernel");
+    prev_log = l;
+  }
+  return CS_OK;
+}
+
+extern "C" cs_status cs_barycentric_weights(uint32_t log_size, const uint32_t px[4], const uint32_t py[4],
+                                            uint32_t* const h_out[4], cs_stream stream) {
+  CS_CHECK_ARG(px != nullptr && py != nullptr, "barycentric_weights: null point");
+  cs_status s = check4(h_out, "barycentric_weights");
+  if (s != CS_OK) return s;
+  CS_CHECK_ARG(log_size >= 1 && log_size <= 28, "barycentric_weights: log size %u out of range", log_size);
+  static const GenPowersTable g = gen_powers();
+  BaryParams p;
+  for (int b = 0; b < 31; b++) p.gen_pow[b] = g.p[b];
+  p.half_init = subgroup_gen(log_size + 1);
+  p.half_step = subgroup_gen(log_size - 1);
+  p.log_n = log_size;
+  p.four_pow = 1;
+  for (uint32_t i = 1; i < log_size; i++) p.four_pow = m31_mul(p.four_pow, 4);
+  p.px = qm31_make(px[0], px[1], px[2], px[3]);
+  p.py = qm31_make(py[0], py[1], py[2], py[3]);
+  qm31 x = p.px;
+  for (uint32_t i = 1; i < log_size; i++) {
+    const qm31 sq = qm31_mul(x, x);
+    x = qm31_sub(qm31_add(sq, sq), qm31_make(1, 0, 0, 0));
+  }
+  p.vn_p = x;
+  SoA o;
+  for (int k = 0; k < 4; k++) o.c[k] = h_out[k];
+  bary_weights_kernel<<<grid_for(1u << log_size, 256), 256, 0, to_stream(stream)>>>(p, o);
+  CS_LAUNCHED("bary_weights_kernel");
+  return CS_OK;
+}
+
+extern "C" cs_status cs_barycentric_eval(const uint32_t* const* h_cols, uint32_t n_cols, uint32_t log_size,
+                                         const uint32_t* const h_weights[4], uint32_t* d_out, cs_stream stream) {
+  cs_status s = check4(h_weights, "barycentric_eval");
+  if (s != CS_OK) return s;
+  CS_CHECK_ARG(n_cols == 0 || (h_cols != nullptr && d_out != nullptr), "barycentric_eval: null pointer");
+  CS_CHECK_ARG(log_size <= 30, "barycentric_eval: log size %u too large", log_size);
+  CSoA w;
+  for (int k = 0; k < 4; k++) w.c[k] = h_weights[k];
+  for (uint32_t b0 = 0; b0 < n_cols; b0 += kMaxBatch) {
+    const uint32_t nb = std::min<uint32_t>(kMaxBatch, n_cols - b0);
+    BaryColumns cols;
+    for (uint32_t i = 0; i < nb; i++) {
+      CS_CHECK_ARG(h_cols[b0 + i] != nullptr, "barycentric_eval: column %u is null", b0 + i);
+      cols.ptr[i] = h_cols[b0 + i];
+    }
+    bary_eval_kernel<<<nb, 512, 0, to_stream(stream)>>>(cols, log_size, w, d_out + 4 * b0);
+    CS_LAUNCHED("bary_eval_kernel");
+  }
+  return CS_OK;
+}
+
+extern "C" cs_status cs_eval_at_point(const uint32_t* const* h_coeffs, uint32_t n_cols, uint32_t log_size,
+                                      const uint32_t px[4], const uint32_t py[4], uint32_t* d_out, cs_stream stream) {
+  CS_CHECK_ARG(px != nullptr && py != nullptr, "eval_at_point: null point");
+  CS_CHECK_ARG(n_cols == 0 || (h_coeffs != nullptr && d_out != nullptr), "eval_at_point: null pointer");
+  CS_CHECK_ARG(log_size <= 30, "eval_at_point: log size %u too large", log_size);
+  FoldFactors ff;
+  ff.log_n = log_size;
+  // mappings: y, x, pi(x), pi^2(x), ... (cpu/circle.rs:89-95)
+  ff.f[0] = qm31_make(py[0], py[1], py[2], py[3]);
+  qm31 x = qm31_make(px[0], px[1], px[2], px[3]);
+  for (uint32_t j = 1; j < 32; j++) {
+    ff.f[j] = x;
+    const qm31 sq = qm31_mul(x, x);
+    x = qm31_sub(qm31_add(sq, sq), qm31_make(1, 0, 0, 0));
+  }
+  for (uint32_t b0 = 0; b0 < n_cols; b0 += kMaxBatch) {
+    const uint32_t nb = std::min<uint32_t>(kMaxBatch, n_cols - b0);
+    BaryColumns cols;
+    for (uint32_t i = 0; i < nb; i++) {
+      CS_CHECK_ARG(h_coeffs[b0 + i] != nullptr, "eval_at_point: column %u is null", b0 + i);
+      cols.ptr[i] = h_coeffs[b0 + i];
+    }
+    eval_at_point_kernel<<<nb, 256, 0, to_stream(stream)>>>(cols, ff, d_out + 4 * b0);
+    CS_LAUNCHED("eval_at_point_kernel");
+  }
+  return CS_OK;
+}
+
+extern "C" cs_status cs_accumulate_numerators(const uint32_t* const* h_cols, uint32_t n_terms, uint32_t log_size,
+                                              uint32_t log_blowup, const uint32_t* h_coeffs,
+                                              uint32_t* const h_out[4], uint32_t first_linear_out[4],
+                                              cs_stream stream) {
+  cs_status s = check4(h_out, "accumulate_numerators");
+  if (s != CS_OK) return s;
+  CS_CHECK_ARG(n_terms > 0 && h_cols != nullptr && h_coeffs != nullptr && first_linear_out != nullptr,
+               "accumulate_numerators: empty batch or null pointer");
+  CS_CHECK_ARG(log_blowup <= log_size && log_size <= 30, "accumulate_numerators: bad sizes %u/%u", log_size,
+               log_blowup);
+  qm31 sum_a = qm31_make(0, 0, 0, 0);
+  for (uint32_t t = 0; t < n_terms; t++) {
+    CS_CHECK_ARG(h_cols[t] != nullptr, "accumulate_numerators: column %u is null", t);
+    const uint32_t* a = h_coeffs + 12 * t;
+    sum_a = qm31_add(sum_a, qm31_make(a[0], a[1], a[2], a[3]));
+  }
+  first_linear_out[0] = sum_a.a.a;
+  first_linear_out[1] = sum_a.a.b;
+  first_linear_out[2] = sum_a.b.a;
+  first_linear_out[3] = sum_a.b.b;
+  SoA o;
+  for (int k = 0; k < 4; k++) o.c[k] = h_out[k];
+  const uint32_t rows = 1u << (log_size - log_blowup);
+  static thread_local NumeratorTerms terms;
+  for (uint32_t t0 = 0; t0 < n_terms; t0 += kMaxTerms) {
+    const uint32_t nt = std::min<uint32_t>(kMaxTerms, n_terms - t0);
+    terms.n = nt;
+    qm31 b_sum = qm31_make(0, 0, 0, 0);
+    for (uint32_t t = 0; t < nt; t++) {
+      const uint32_t* co = h_coeffs + 12 * (t0 + t);
+      terms.col[t] = h_cols[t0 + t];
+      b_sum = qm31_add(b_sum, qm31_make(co[4], co[5], co[6], co[7]));
+      terms.c[t] = qm31_make(co[8], co[9], co[10], co[11]);
+    }
+    terms.b_sum = b_sum;
+    numerators_kernel<<<grid_for(rows, 256), 256, 0, to_stream(stream)>>>(terms, rows, o, t0 > 0);
+    CS_LAUNCHED("numerators_kernel");
+  }
+  return CS_OK;
+}
+
+extern "C" cs_status cs_quotients_on_subdomain(const uint32_t* const* h_accs, const uint32_t* h_acc_log_sizes,
+                                               uint32_t n_points, const uint32_t* h_points,
+                                               const uint32_t* h_first_linear, uint32_t lifting_log_size,
+                                               uint32_t log_blowup, uint32_t* const h_out[4], cs_stream stream) {
+  cs_status s = check4(h_out, "quotients");
+  if (s != CS_OK) return s;
+  CS_CHECK_ARG(n_points >= 1 && n_points <= kMaxPoints, "quotients: %u sample points (1..%u supported)", n_points,
+               kMaxPoints);
+  CS_CHECK_ARG(h_accs && h_acc_log_sizes && h_points && h_first_linear, "quotients: null pointer");
+  CS_CHECK_ARG(log_blowup < lifting_log_size && lifting_log_size <= 30, "quotients: bad sizes");
+  static const GenPowersTable g = gen_powers();
+  QuotientParams q;
+  for (int b = 0; b < 31; b++) q.gen_pow[b] = g.p[b];
+  q.sub_log = lifting_log_size - log_blowup;
+  CS_CHECK_ARG(q.sub_log >= 1, "quotients: empty subdomain");
+  // eval_domain.split(log_blowup).0: half coset (eval half initial, log L - 1 - b)
+  q.half_init = subgroup_gen(lifting_log_size + 1);
+  q.half_step = subgroup_gen(q.sub_log - 1);
+  q.n_points = n_points;
+  for (uint32_t k = 0; k < n_points; k++) {
+    const uint32_t* pt = h_points + 8 * k;
+    q.px[k] = qm31_make(pt[0], pt[1], pt[2], pt[3]);
+    q.py[k] = qm31_make(pt[4], pt[5], pt[6], pt[7]);
+    const uint32_t* fl = h_first_linear + 4 * k;
+    q.first_linear[k] = qm31_make(fl[0], fl[1], fl[2], fl[3]);
+    q.acc_log[k] = h_acc_log_sizes[k];
+    CS_CHECK_ARG(q.acc_log[k] >= 1 && q.acc_log[k] <= q.sub_log, "quotients: accumulation %u has log size %u", k,
+                 q.acc_log[k]);
+    for (int c = 0; c < 4; c++) {
+      CS_CHECK_ARG(h_accs[4 * k + c] != nullptr, "quotients: null accumulation column");
+      q.acc[k].c[c] = h_accs[4 * k + c];
+    }
+  }
+  return quotients_on_subdomain(q, h_out, to_stream(stream));
+}
+
+extern "C" cs_status cs_decompose(const uint32_t* const h_src[4], uint32_t log_size, uint32_t* const h_dst[4],
+                                  uint32_t lambda_out[4], cs_stream stream) {
+  cs_status s = check4(h_src, "decompose");
+  if (s == CS_OK) s = check4(h_dst, "decompose");
+  if (s != CS_OK) return s;
+  CS_CHECK_ARG(lambda_out != nullptr && log_size >= 1 && log_size <= 30, "decompose: bad arguments");
+  cudaStream_t st = to_stream(stream);
+  CSoA in;
+  SoA out;
+  for (int k = 0; k < 4; k++) {
+    in.c[k] = h_src[k];
+    out.c[k] = h_dst[k];
+  }
+  uint32_t* d_sums = nullptr;
+  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_sums), 8 * sizeof(uint32_t), st));
+  half_sums_kernel<<<2, 512, 0, st>>>(in, log_size, d_sums);
+  note_launch();
+  uint32_t sums[8];
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(sums, d_sums, sizeof(sums), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(d_sums, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return from_cuda(e, "decompose");
+  const qm31 a = qm31_make(sums[0], sums[1], sums[2], sums[3]);
+  const qm31 b = qm31_make(sums[4], sums[5], sums[6], sums[7]);
+  // lambda = (a - b) / n, n = 2^log_size, 1/n = 2^(31 - log_size)
+  const qm31 lambda = qm31_mul_m31(qm31_sub(a, b), 1u << (31 - log_size));
+  lambda_out[0] = lambda.a.a;
+  lambda_out[1] = lambda.a.b;
+  lambda_out[2] = lambda.b.a;
+  lambda_out[3] = lambda.b.b;
+  decompose_apply_kernel<<<grid_for(1u << log_size, 256), 256, 0, st>>>(in, out, log_size, lambda);
+  CS_LAUNCHED("decompose_apply_kernel");
+  return CS_OK;
+}
