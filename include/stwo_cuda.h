@@ -256,6 +256,26 @@ cs_status cs_quotients_on_subdomain(const uint32_t *const *h_accs, const uint32_
 cs_status cs_decompose(const uint32_t *const h_src[4], uint32_t log_size, uint32_t *const h_dst[4],
                        uint32_t lambda_out[4], cs_stream stream);
 
+/* ------------------------------------------------ AIR: Wide-Fibonacci */
+
+/* Constraint quotients of the Wide-Fibonacci component on its evaluation
+   domain: the device analogue of FrameworkComponent::
+   evaluate_constraint_quotients_on_domain
+   (crates/constraint-framework/src/prover/component_prover.rs:195-268) for
+   WideFibonacciEval (crates/examples/src/wide_fibonacci/mod.rs:87-97), in
+   the SubDomain mode with log_expansion 0. h_cols: the n_cols trace
+   evaluations on CanonicCoset(eval_log) (bit-reversed); h_rc: the component's
+   n_cols - 2 random-coefficient powers in constraint order (4 words each).
+   Row r adds sum_k rc[k] (c_{k+2} - c_k^2 - c_{k+1}^2) / V_trace(x_r) to the
+   QM31 accumulator h_accum (2^eval_log values). */
+cs_status cs_wide_fib_composition(const uint32_t *const *h_cols, uint32_t n_cols, uint32_t eval_log, uint32_t trace_log,
+                                  const uint32_t *h_rc, uint32_t *const h_accum[4], cs_stream stream);
+
+/* Wide-Fibonacci trace generation (crates/examples/src/wide_fibonacci/mod.rs:27-48)
+   on the device: column 0 = a, column 1 = b, then (a, b) <- (b, a^2 + b^2). */
+cs_status cs_wide_fib_trace(const uint32_t *d_a, const uint32_t *d_b, uint32_t log_n, uint32_t n_cols,
+                            uint32_t *const *h_cols, cs_stream stream);
+
 /* -------------------------------------------------------- proof of work */
 
 /* GrindOps<Blake2sChannel>::grind (crates/stwo/src/core/proof_of_work.rs:10-14;

@@ -1,0 +1,128 @@
+"""ORACLE — test infrastructure only: the device operations of the host
+prover (proving_gb300.prover) implemented with the CPU oracle, so the same
+prover code can run on the CPU restatement and on the GPU and the two proofs
+can be compared byte for byte."""
+from __future__ import annotations
+
+import numpy as np
+
+from . import oracle as O
+
+
+class Col:
+    """An M31 column held in host memory."""
+
+    def __init__(self, v):
+        self.v = np.ascontiguousarray(v, dtype=np.uint32)
+
+    @property
+    def log_size(self):
+        return self.v.size.bit_length() - 1
+
+
+class SCol:
+    """A QM31 column as four coordinate columns."""
+
+    def __init__(self, coords):
+        self.c = [np.ascontiguousarray(x, dtype=np.uint32) for x in coords]
+
+    def __len__(self):
+        return self.c[0].size
+
+
+class Tree:
+    def __init__(self, root: bytes, layers, height: int):
+        self.root = root
+        self.layers = layers  # leaves first: layers[i] has 2^(height - i) hashes
+        self.height = height
+
+    def hashes(self, layer_log: int, idx):
+        lay = self.layers[self.height - layer_log]
+        return [lay[i].tobytes() for i in idx]
+
+
+class Twiddles:
+    def __init__(self, domain_log: int):
+        self.tw, self.itw = O.canonic_twiddles(domain_log)
+        self.log_size = domain_log - 1
+
+
+class CpuOps:
+    def twiddles(self, root_log_domain: int):
+        return Twiddles(root_log_domain)
+
+    def columns_from_host(self, cols):
+        return [Col(c) for c in cols]
+
+    def log_size(self, col) -> int:
+        return col.log_size
+
+    def interpolate(self, cols, tw):
+        res = O.interpolate_batch([c.v for c in cols], tw.itw)
+        for c, r in zip(cols, res):
+            c.v = r
+
+    def evaluate(self, coeffs, log_size, tw):
+        return [Col(e) for e in O.evaluate_batch([c.v for c in coeffs], [log_size] * len(coeffs), tw.tw)]
+
+    def merkle_commit(self, cols, L):
+        root, layers = O.merkle_commit([c.v for c in cols], L, with_layers=True)
+        return Tree(root, layers, L)
+
+    def gather(self, col, idx):
+        return col.v[np.asarray(idx, dtype=np.int64)]
+
+    def secure_zeros(self, n):
+        return SCol([np.zeros(n, np.uint32) for _ in range(4)])
+
+    def secure_len(self, col) -> int:
+        return len(col)
+
+    def secure_columns(self, col):
+        return [Col(c) for c in col.c]
+
+    def gather_secure(self, col, idx):
+        ix = np.asarray(idx, dtype=np.int64)
+        vals = [c[ix] for c in col.c]
+        return [tuple(int(vals[k][i]) for k in range(4)) for i in range(len(idx))]
+
+    def wide_fib_composition(self, evals, trace_log, rc, accum):
+        eval_log = len(accum).bit_length() - 1
+        accum.c = O.wide_fib_composition([e.v for e in evals], eval_log, trace_log, np.asarray(rc, np.uint32),
+                                         out=accum.c)
+
+    def interpolate_secure(self, accum, tw):
+        return [Col(c) for c in O.interpolate_batch(accum.c, tw.itw)]
+
+    def split_at_mid(self, coeff_cols):
+        half = coeff_cols[0].v.size // 2
+        return [Col(c.v[:half]) for c in coeff_cols], [Col(c.v[half:]) for c in coeff_cols]
+
+    def grind(self, digest, bits):
+        return O.grind(digest, bits)
+
+    def barycentric_weights(self, log_size, point):
+        return SCol(O.barycentric_weights(log_size, point[0], point[1]))
+
+    def barycentric_eval(self, cols, weights):
+        return [tuple(int(x) for x in O.barycentric_eval(c.v, weights.c)) for c in cols]
+
+    def accumulate_numerators(self, cols, coeffs, log_blowup):
+        arr = np.asarray([[list(a), list(b), list(c)] for a, b, c in coeffs], np.uint32)
+        out, fl = O.accumulate_numerators([c.v for c in cols], log_blowup, arr)
+        return SCol(out), fl
+
+    def lift_and_accumulate(self, cols):
+        return SCol(O.lift_and_accumulate([c.c for c in cols]))
+
+    def compute_quotients_and_combine(self, parts, points, fls, lifting, log_blowup, tw):
+        sub = O.quotients_on_subdomain([p.c for p in parts], points, fls, lifting, log_blowup)
+        sub_itw = O.extract_subdomain_twiddles(tw.itw, lifting, lifting - log_blowup)
+        return SCol([O.evaluate(O.interpolate(c, sub_itw), lifting, tw.tw) for c in sub])
+
+    def fold_circle_into_line(self, col, alpha, tw):
+        return SCol(O.fold_circle_into_line(col.c, alpha))
+
+    def fold_line(self, col, alpha, tw):
+        n = len(col)
+        return SCol(O.fold_line(col.c, O.line_domain_initial_index(n.bit_length() - 1), alpha))

@@ -75,6 +75,9 @@ void orc_quotients_on_subdomain(const uint32_t *const *accs, const uint32_t *acc
                                 uint32_t log_blowup, uint32_t *const out[4]);
 void orc_decompose(const uint32_t *const in[4], uint32_t log_n, uint32_t *const out[4], uint32_t lambda_out[4]);
 void orc_random_point_from_t(const uint32_t t[4], uint32_t px[4], uint32_t py[4]);
+void orc_wide_fib_composition(const uint32_t **cols, uint32_t n_cols, uint32_t eval_log, uint32_t trace_log,
+                              const uint32_t *rc, uint32_t *const out[4]);
+void orc_wide_fib_trace(const uint32_t *a0, const uint32_t *b0, uint32_t log_n, uint32_t n_cols, uint32_t **cols);
 
 #ifdef __cplusplus
 }

@@ -428,3 +428,26 @@ def extract_subdomain_twiddles(buf: np.ndarray, domain_log_size: int, subdomain_
         out.append(buf[start:start + (1 << (sh - 1 - layer))])
     out.append(buf[-1:])
     return np.concatenate(out).astype(np.uint32)
+
+
+# ------------------------------------------------------------ Wide-Fibonacci
+
+def wide_fib_trace(a0, b0, n_cols: int):
+    a, b = _u32(a0), _u32(b0)
+    n = a.size
+    cols = [np.zeros(n, np.uint32) for _ in range(n_cols)]
+    lib().orc_wide_fib_trace(_p(a), _p(b), ctypes.c_uint32(n.bit_length() - 1), ctypes.c_uint32(n_cols),
+                             _ptr_array(cols))
+    return cols
+
+
+def wide_fib_composition(cols, eval_log: int, trace_log: int, rc, out=None):
+    """rc: (n_cols - 2, 4) reversed random-coefficient powers; out: SoA accumulator (added to)."""
+    cols = [_u32(c) for c in cols]
+    r = np.ascontiguousarray(np.asarray(rc, np.uint32).reshape(-1))
+    if out is None:
+        out = [np.zeros(1 << eval_log, np.uint32) for _ in range(4)]
+    out = [_u32(o).copy() for o in out]
+    lib().orc_wide_fib_composition(_ptr_array(cols), ctypes.c_uint32(len(cols)), ctypes.c_uint32(eval_log),
+                                   ctypes.c_uint32(trace_log), _p(r), _ptr_array(out))
+    return out

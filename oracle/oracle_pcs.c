@@ -214,3 +214,58 @@ void orc_random_point_from_t(const uint32_t t_w[4], uint32_t px[4], uint32_t py[
     qm31_to_words(qm31_mul(qm31_sub(qm31_from_m31(1), t2), inv), px);
     qm31_to_words(qm31_mul(qm31_add(t, t), inv), py);
 }
+
+/* ------------------------------------------------------ Wide-Fibonacci AIR */
+
+/*
+ * FrameworkComponent<WideFibonacciEval<N>>::evaluate_constraint_quotients_on_domain
+ * for CpuBackend (crates/constraint-framework/src/prover/component_prover.rs:195-268)
+ * in the SubDomain mode with log_expansion 0: the evaluation domain is
+ * CanonicCoset(eval_log).circle_domain(); row r accumulates
+ * sum_k rc[k] * (c_{k+2}[r] - (c_k[r]^2 + c_{k+1}[r]^2))
+ * (crates/examples/src/wide_fibonacci/mod.rs:87-97) with rc the reversed
+ * powers of the random coefficient, times
+ * denom_inv[r >> trace_log] = bit-reversed 1/V_trace(eval_domain.at(i))
+ * (component_prover.rs:101-108). out is added to (accumulator semantics).
+ */
+void orc_wide_fib_composition(const uint32_t **cols, uint32_t n_cols, uint32_t eval_log, uint32_t trace_log,
+                              const uint32_t *rc, uint32_t *const out[4]) {
+    uint32_t log_expand = eval_log - trace_log;
+    uint32_t n_den = 1u << log_expand;
+    m31 *den = (m31 *)malloc(sizeof(m31) * n_den);
+    coset_t eval_half = canonic_half_coset(eval_log);
+    coset_t trace_coset = coset_odds(trace_log);
+    for (uint32_t i = 0; i < n_den; i++) den[i] = m31_inv(coset_vanishing_m(trace_coset, domain_at(eval_half, i)));
+    orc_bit_reverse(den, log_expand);
+    uint64_t n = 1ull << eval_log;
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < (int64_t)n; r++) {
+        qm31 acc = qm31_from_m31(0);
+        for (uint32_t k = 0; k + 2 < n_cols; k++) {
+            m31 a = cols[k][r], b = cols[k + 1][r], c = cols[k + 2][r];
+            m31 cons = m31_sub(c, m31_add(m31_sqr(a), m31_sqr(b)));
+            acc = qm31_add(acc, qm31_mul_m31(qm31_from_words(rc + 4 * k), cons));
+        }
+        acc = qm31_mul_m31(acc, den[(uint64_t)r >> trace_log]);
+        qm31 prev = soa_at((const uint32_t *const *)out, r);
+        soa_set(out, r, qm31_add(prev, acc));
+    }
+    free(den);
+}
+
+/* Wide-Fibonacci trace (crates/examples/src/wide_fibonacci/mod.rs:27-48): column 0 = a,
+   column 1 = b, then (a, b) <- (b, a^2 + b^2). */
+void orc_wide_fib_trace(const uint32_t *a0, const uint32_t *b0, uint32_t log_n, uint32_t n_cols, uint32_t **cols) {
+    uint64_t n = 1ull << log_n;
+    for (uint64_t r = 0; r < n; r++) {
+        m31 a = a0[r], b = b0[r];
+        cols[0][r] = a;
+        cols[1][r] = b;
+        for (uint32_t k = 2; k < n_cols; k++) {
+            m31 c = m31_add(m31_sqr(a), m31_sqr(b));
+            a = b;
+            b = c;
+            cols[k][r] = b;
+        }
+    }
+}

@@ -54,6 +54,8 @@ SIGNATURES = {
     "cs_accumulate_numerators": [vp, u32, u32, u32, vp, vp, vp, vp],
     "cs_quotients_on_subdomain": [vp, vp, u32, vp, vp, u32, u32, vp, vp],
     "cs_decompose": [vp, u32, vp, vp, vp],
+    "cs_wide_fib_composition": [vp, u32, u32, u32, vp, vp, vp],
+    "cs_wide_fib_trace": [vp, vp, u32, u32, vp, vp],
 }
 _RESTYPES = {"cs_last_error": ctypes.c_char_p, "cs_version": ctypes.c_char_p,
              "cs_kernel_launch_count": ctypes.c_uint64}

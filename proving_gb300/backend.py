@@ -347,6 +347,22 @@ class CudaBackend:
         cls.interpolate_on_subdomain(q.columns, lifting_log_size, twiddles)
         return SecureColumnByCoords(cls.evaluate_polynomials(q.columns, lifting_log_size, twiddles))
 
+    # AIR (Wide-Fibonacci) ---------------------------------------------------------
+    @staticmethod
+    def wide_fib_trace(a: BaseColumn, b: BaseColumn, n_cols: int):
+        cols = [BaseColumn.uninitialized(len(a)) for _ in range(n_cols)]
+        _lib.call("cs_wide_fib_trace", _ptr(a.data), _ptr(b.data), a.log_size, n_cols,
+                  _ptr_table([c.data for c in cols]), _stream())
+        return cols
+
+    @staticmethod
+    def wide_fib_composition(evals, trace_log: int, rc, accum: SecureColumnByCoords) -> None:
+        """Adds the Wide-Fibonacci constraint quotients to accum (evaluation domain of accum's size)."""
+        r = np.ascontiguousarray(np.asarray(rc, np.uint32).reshape(-1))
+        _lib.call("cs_wide_fib_composition", _ptr_table([c.data for c in evals]), len(evals),
+                  len(accum).bit_length() - 1, trace_log, r.ctypes.data,
+                  _ptr_table([c.data for c in accum.columns]), _stream())
+
     # GrindOps -----------------------------------------------------------------
     @staticmethod
     def grind(digest: bytes, pow_bits: int, max_nonce: int = 1 << 48) -> int:

@@ -30,7 +30,6 @@ namespace cs {
 
 namespace {
 
-constexpr int kFftThreads = 256;
 
 struct FftBatch {
   uint32_t* dst[kMaxBatch];
@@ -50,34 +49,13 @@ struct FftPass {
                       // larger for a subdomain, which takes the prefix of each layer)
 };
 
-__device__ __forceinline__ uint32_t twiddle_at(const FftPass& p, uint32_t layer, uint32_t h) {
-  const uint32_t tw_len = 1u << p.tw_log;
-  if (layer == 0) {
-    const uint32_t* lt1 = p.tw + (tw_len - (1u << (p.tw_dom - 1)));
-    const uint32_t pair = (h >> 2) << 1;
-    const uint32_t x = __ldg(lt1 + pair), y = __ldg(lt1 + pair + 1);
-    switch (h & 3) {
-      case 0: return y;
-      case 1: return m31_neg(y);
-      case 2: return m31_neg(x);
-      default: return x;
-    }
-  }
-  return __ldg(p.tw + (tw_len - (1u << (p.tw_dom - layer))) + h);
-}
-
 struct Tile {
-  uint32_t o, ib;  // outer group and inner block (inner case) / first outer group (outer case)
+  uint32_t o, ib;  // outer group and inner block (inner tiles) / first outer group (outer tiles)
 };
 
 __device__ __forceinline__ uint32_t tile_gidx(const FftPass& p, const Tile& t, uint32_t m, uint32_t e) {
   if (p.outer) return ((t.o + e) << p.hi) | m;
   return (t.o << p.hi) | (m << p.lo) | (t.ib << p.c) | e;
-}
-
-__device__ __forceinline__ uint32_t tile_sidx(const FftPass& p, uint32_t m, uint32_t e) {
-  const uint32_t T = p.hi - p.lo;
-  return p.outer ? (e << T) | m : (m << p.c) | e;
 }
 
 __device__ __forceinline__ void bfly(uint32_t& v0, uint32_t& v1, uint32_t t) {
@@ -93,108 +71,172 @@ __device__ __forceinline__ void ibfly(uint32_t& v0, uint32_t& v1, uint32_t t) {
   v1 = m31_mul(m31_sub(tmp, v1), t);
 }
 
-// One register stage: R consecutive local layers [d0, d0 + R) on groups of 2^R elements.
-template <int R, bool INV>
-__device__ __forceinline__ void run_stage(const FftPass& p, const Tile& t, uint32_t* s, uint32_t d0) {
-  const uint32_t T = p.hi - p.lo;
-  const uint32_t E = 1u << p.c;
-  const uint32_t W = (1u << (T - R)) << p.c;
-  for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) {
-    uint32_t e, mb;
-    if (p.outer) {
-      mb = w & ((1u << (T - R)) - 1);
-      e = w >> (T - R);
-    } else {
-      e = w & (E - 1);
-      mb = w >> p.c;
-    }
-    const uint32_t m0 = (mb & ((1u << d0) - 1)) | ((mb >> d0) << (d0 + R));
-    uint32_t v[1 << R];
+// Shared-memory layout of a tile. Outer (contiguous) tiles hold [e][m] and
+// insert one pad word per 32; inner (strided) tiles hold [m][e] with 8 values
+// of e and insert 8 pad words per 256. Both make every 32-wide access of the
+// two register stages and of the global load/store phase hit distinct banks,
+// and keep a register group's addresses at compile-time offsets from one base.
+template <bool OUTER>
+__device__ __forceinline__ uint32_t pad(uint32_t L) {
+  return OUTER ? L + (L >> 5) : L + ((L >> 8) << 3);
+}
+
+template <bool OUTER>
+__host__ __device__ constexpr uint32_t padded_words(uint32_t n) {
+  return OUTER ? n + (n >> 5) : n + ((n >> 8) << 3);
+}
+
+template <bool OUTER>
+__device__ __forceinline__ uint32_t lin(uint32_t m, uint32_t e, int T, uint32_t EB) {
+  return OUTER ? ((e << T) | m) : ((m << EB) | e);
+}
+
+// CNT consecutive twiddles of FFT layer `layer`, starting at twiddle index h0.
+template <int CNT>
+__device__ __forceinline__ void load_twiddles(const FftPass& p, uint32_t layer, uint32_t h0, uint32_t* w) {
+  const uint32_t tw_len = 1u << p.tw_log;
+  if (layer == 0) {
+    // circle layer: [y, -y, -x, x] of the line-layer-1 pair (cpu/circle.rs:306-323)
+    const uint32_t* lt1 = p.tw + (tw_len - (1u << (p.tw_dom - 1)));
+    if (CNT >= 16) {
+      // h0 is a multiple of 16: pairs (h0 >> 2) .. + 3, 8 aligned words
 #pragma unroll
-    for (int k = 0; k < (1 << R); k++) v[k] = s[tile_sidx(p, m0 + ((uint32_t)k << d0), e)];
-    const uint32_t g0 = tile_gidx(p, t, m0, e);
-    const uint32_t gstep = d0 + p.lo;
+      for (int q8 = 0; q8 < CNT / 8; q8++) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(lt1 + ((h0 >> 2) << 1)) + q8);
+        const uint32_t xs[2] = {v.x, v.z}, ys[2] = {v.y, v.w};
 #pragma unroll
-    for (int tt = 0; tt < R; tt++) {
-      const int lt = INV ? tt : (R - 1 - tt);
-      const uint32_t layer = p.lo + d0 + (uint32_t)lt;
-#pragma unroll
-      for (int k = 0; k < (1 << R); k++) {
-        if (k & (1 << lt)) continue;
-        const uint32_t g = g0 + ((uint32_t)k << gstep);
-        const uint32_t tw = twiddle_at(p, layer, g >> (layer + 1));
-        if (INV)
-          ibfly(v[k], v[k | (1 << lt)], tw);
-        else
-          bfly(v[k], v[k | (1 << lt)], tw);
+        for (int k = 0; k < 2; k++) {
+          w[8 * q8 + 4 * k + 0] = ys[k];
+          w[8 * q8 + 4 * k + 1] = m31_neg(ys[k]);
+          w[8 * q8 + 4 * k + 2] = m31_neg(xs[k]);
+          w[8 * q8 + 4 * k + 3] = xs[k];
+        }
       }
+      return;
     }
 #pragma unroll
-    for (int k = 0; k < (1 << R); k++) s[tile_sidx(p, m0 + ((uint32_t)k << d0), e)] = v[k];
+    for (int q = 0; q < CNT; q++) {
+      const uint32_t h = h0 + q;
+      const uint32_t pair = (h >> 2) << 1;
+      const uint32_t x = __ldg(lt1 + pair), y = __ldg(lt1 + pair + 1);
+      const uint32_t sel = h & 3;
+      const uint32_t val = sel < 2 ? y : x;
+      w[q] = (sel == 1 || sel == 2) ? m31_neg(val) : val;
+    }
+    return;
+  }
+  const uint32_t* lt = p.tw + (tw_len - (1u << (p.tw_dom - layer))) + h0;
+  if (CNT >= 4) {
+#pragma unroll
+    for (int q = 0; q < CNT / 4; q++) {
+      const uint4 v = __ldg(reinterpret_cast<const uint4*>(lt) + q);
+      w[4 * q] = v.x;
+      w[4 * q + 1] = v.y;
+      w[4 * q + 2] = v.z;
+      w[4 * q + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < CNT; q++) w[q] = __ldg(lt + q);
   }
 }
 
-template <bool INV>
-__global__ void __launch_bounds__(kFftThreads) fft_pass_kernel(const FftBatch batch, const FftPass p) {
+// R local layers [D0, D0 + R) on the 2^R register values v, whose local index
+// j maps to global index g0 + (j << (D0 + lo)). INV runs the layers upward
+// with ibutterflies (interpolate), otherwise downward with butterflies. Step K
+// of the stage handles local layer t; its 2^(R-1-t) twiddles are consecutive.
+template <bool INV, int R, int D0, int K>
+struct RegStage {
+  static __device__ __forceinline__ void run(const FftPass& p, uint32_t g0, uint32_t* v) {
+    constexpr int t = INV ? K : (R - 1 - K);
+    constexpr int CNT = 1 << (R - 1 - t);
+    const uint32_t layer = p.lo + D0 + t;
+    uint32_t w[CNT];
+    load_twiddles<CNT>(p, layer, g0 >> (layer + 1), w);
+#pragma unroll
+    for (int j = 0; j < (1 << R); j++) {
+      if (j & (1 << t)) continue;
+      if (INV)
+        ibfly(v[j], v[j | (1 << t)], w[j >> (t + 1)]);
+      else
+        bfly(v[j], v[j | (1 << t)], w[j >> (t + 1)]);
+    }
+    RegStage<INV, R, D0, K + 1>::run(p, g0, v);
+  }
+};
+template <bool INV, int R, int D0>
+struct RegStage<INV, R, D0, R> {
+  static __device__ __forceinline__ void run(const FftPass&, uint32_t, uint32_t*) {}
+};
+
+// One pass over layers [lo, lo + T) of a tile of 2^T x 2^EB values: stage A
+// runs local layers [0, TA) on groups m = (ma << TA) | j, stage B runs
+// [TA, T) on groups m = (j << TA) | mb, with one shared-memory exchange.
+template <int T, bool OUTER>
+constexpr int tile_max_threads() {
+  return OUTER ? 256 : (1 << (T / 2 + 3));
+}
+
+template <bool INV, int T, bool OUTER>
+__global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), 2) fft_tile_kernel(const FftBatch batch, const FftPass p) {
+  constexpr int TA = T / 2, TB = T - TA;
+  constexpr uint32_t M = 1u << T;
   extern __shared__ uint32_t s[];
-  const uint32_t T = p.hi - p.lo;
-  const uint32_t N = 1u << (T + p.c);
+  const uint32_t EB = OUTER ? p.c : 3u;  // inner tiles always hold 8 groups
+  const uint32_t N = M << EB;
   uint32_t* dst = batch.dst[blockIdx.y];
   const uint32_t* src = batch.src[blockIdx.y];
-  Tile t;
-  if (p.outer) {
-    t.o = blockIdx.x << p.c;
-    t.ib = 0;
+  Tile tl;
+  if (OUTER) {
+    tl.o = blockIdx.x << EB;
+    tl.ib = 0;
   } else {
     const uint32_t outer_bits = p.log_n - p.hi;
-    t.o = blockIdx.x & ((1u << outer_bits) - 1);
-    t.ib = blockIdx.x >> outer_bits;
+    tl.o = blockIdx.x & ((1u << outer_bits) - 1);
+    tl.ib = blockIdx.x >> outer_bits;
   }
   for (uint32_t L = threadIdx.x; L < N; L += blockDim.x) {
-    uint32_t m, e;
-    if (p.outer) {
-      m = L & ((1u << T) - 1);
-      e = L >> T;
-    } else {
-      e = L & ((1u << p.c) - 1);
-      m = L >> p.c;
-    }
-    s[L] = __ldg(src + (tile_gidx(p, t, m, e) & p.src_mask));
+    const uint32_t m = OUTER ? (L & (M - 1)) : (L >> EB);
+    const uint32_t e = OUTER ? (L >> T) : (L & ((1u << EB) - 1));
+    s[pad<OUTER>(L)] = __ldg(src + (tile_gidx(p, tl, m, e) & p.src_mask));
   }
   __syncthreads();
-  if (INV) {
-    uint32_t d = 0;
-    while (d < T) {
-      const uint32_t r = min(3u, T - d);
-      if (r == 3) run_stage<3, INV>(p, t, s, d);
-      else if (r == 2) run_stage<2, INV>(p, t, s, d);
-      else run_stage<1, INV>(p, t, s, d);
-      d += r;
-      __syncthreads();
+  const uint32_t t = threadIdx.x;
+  for (int phase = 0; phase < 2; phase++) {
+    const bool stage_a = INV ? phase == 0 : phase == 1;
+    if (stage_a) {
+      if (TA > 0) {
+#pragma unroll 1
+        for (uint32_t r = 0; r < (1u << (TB - TA)); r++) {
+          const uint32_t e = OUTER ? (t >> TA) : (t & ((1u << EB) - 1));
+          const uint32_t ma = (OUTER ? (t & ((1u << TA) - 1)) : (t >> EB)) + (r << TA);
+          const uint32_t mbase = ma << TA;
+          uint32_t v[1 << TA];
+#pragma unroll
+          for (int j = 0; j < (1 << TA); j++) v[j] = s[pad<OUTER>(lin<OUTER>(mbase | j, e, T, EB))];
+          RegStage<INV, TA, 0, 0>::run(p, tile_gidx(p, tl, mbase, e), v);
+#pragma unroll
+          for (int j = 0; j < (1 << TA); j++) s[pad<OUTER>(lin<OUTER>(mbase | j, e, T, EB))] = v[j];
+        }
+      }
+    } else {
+      const uint32_t e = OUTER ? (t >> TA) : (t & ((1u << EB) - 1));
+      const uint32_t mb = OUTER ? (t & ((1u << TA) - 1)) : (t >> EB);
+      uint32_t v[1 << TB];
+#pragma unroll
+      for (int j = 0; j < (1 << TB); j++) v[j] = s[pad<OUTER>(lin<OUTER>((j << TA) | mb, e, T, EB))];
+      RegStage<INV, TB, TA, 0>::run(p, tile_gidx(p, tl, mb, e), v);
+#pragma unroll
+      for (int j = 0; j < (1 << TB); j++) s[pad<OUTER>(lin<OUTER>((j << TA) | mb, e, T, EB))] = v[j];
     }
-  } else {
-    uint32_t d = T;
-    while (d > 0) {
-      const uint32_t r = min(3u, d);
-      d -= r;
-      if (r == 3) run_stage<3, INV>(p, t, s, d);
-      else if (r == 2) run_stage<2, INV>(p, t, s, d);
-      else run_stage<1, INV>(p, t, s, d);
-      __syncthreads();
-    }
+    __syncthreads();
   }
   for (uint32_t L = threadIdx.x; L < N; L += blockDim.x) {
-    uint32_t m, e;
-    if (p.outer) {
-      m = L & ((1u << T) - 1);
-      e = L >> T;
-    } else {
-      e = L & ((1u << p.c) - 1);
-      m = L >> p.c;
-    }
-    uint32_t v = s[L];
+    const uint32_t m = OUTER ? (L & (M - 1)) : (L >> EB);
+    const uint32_t e = OUTER ? (L >> T) : (L & ((1u << EB) - 1));
+    uint32_t v = s[pad<OUTER>(L)];
     if (p.scale) v = m31_mul(v, p.scale);
-    dst[tile_gidx(p, t, m, e)] = v;
+    dst[tile_gidx(p, tl, m, e)] = v;
   }
 }
 
@@ -283,35 +325,32 @@ SmallParams small_constants(uint32_t log_n, uint32_t log_src, bool inverse, uint
 }
 
 struct PassPlan {
-  uint32_t lo, hi, c, outer;
+  uint32_t lo, hi, c, outer;  // layers [lo, hi); c = extra tile bits
 };
 
-// Splits layers [0, n_layers) of a column of log size log_n into passes.
+// Splits layers [0, n_layers) of a column of log size log_n into passes of at
+// most 12 layers (11 for strided passes); the first pass is contiguous.
 std::vector<PassPlan> plan_passes(uint32_t log_n, uint32_t n_layers) {
   std::vector<PassPlan> plan;
-  const uint32_t max_first = 12, max_strided = 11;
   uint32_t n_pass = 1;
-  while (true) {
-    // first pass gets the remainder, strided passes are balanced
-    if (n_layers <= max_first + (n_pass - 1) * max_strided) break;
-    n_pass++;
-  }
+  while (n_layers > 12 + (n_pass - 1) * 11) n_pass++;
   std::vector<uint32_t> sizes(n_pass);
-  uint32_t base = n_layers / n_pass, extra = n_layers % n_pass;
+  const uint32_t base = n_layers / n_pass, extra = n_layers % n_pass;
+  // the contiguous first pass takes the remainder, so strided passes stay <= 11
   for (uint32_t i = 0; i < n_pass; i++) sizes[i] = base + (i < extra ? 1 : 0);
   uint32_t lo = 0;
   for (uint32_t i = 0; i < n_pass; i++) {
     PassPlan pp;
     pp.lo = lo;
     pp.hi = lo + sizes[i];
+    const uint32_t TA = sizes[i] / 2;
     if (lo == 0) {
-      // contiguous tile: 2^T elements, widened by outer groups up to 2^11 words
-      pp.outer = 1;
-      const uint32_t want = sizes[i] >= 11 ? 0 : 11 - sizes[i];
+      pp.outer = 1;  // contiguous tile, widened by outer groups to about 256 threads
+      const uint32_t want = TA >= 8 ? 0 : 8 - TA;
       pp.c = std::min(want, log_n - pp.hi);
     } else {
-      pp.outer = 0;
-      pp.c = std::min(3u, lo);
+      pp.outer = 0;  // strided tile: 8 neighbouring groups (32-byte runs in HBM)
+      pp.c = 3;
     }
     plan.push_back(pp);
     lo = pp.hi;
@@ -319,23 +358,67 @@ std::vector<PassPlan> plan_passes(uint32_t log_n, uint32_t n_layers) {
   return plan;
 }
 
-size_t pass_smem(const PassPlan& pp) { return (size_t)4 << (pp.hi - pp.lo + pp.c); }
-
-template <bool INV>
-cs_status launch_pass(const FftBatch& b, uint32_t n_cols, const FftPass& p, const PassPlan& pp,
-                      cudaStream_t st) {
-  const size_t smem = pass_smem(pp);
+template <bool INV, int T, bool OUTER>
+cs_status launch_tile(const FftBatch& b, uint32_t n_cols, const FftPass& p, cudaStream_t st) {
+  const size_t smem = (size_t)4 * padded_words<OUTER>(1u << (T + p.c));
   static bool configured = false;
   if (!configured) {
-    CS_CUDA(cudaFuncSetAttribute(fft_pass_kernel<INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+    CS_CUDA(cudaFuncSetAttribute(fft_tile_kernel<INV, T, OUTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 160 * 1024));
     configured = true;
   }
-  const uint32_t T = pp.hi - pp.lo;
-  const uint32_t tiles = 1u << (p.log_n - T - pp.c);
+  const uint32_t threads = (1u << (T / 2)) << p.c;
+  const uint32_t tiles = 1u << (p.log_n - T - p.c);
   dim3 grid(tiles, n_cols);
-  fft_pass_kernel<INV><<<grid, kFftThreads, smem, st>>>(b, p);
-  CS_LAUNCHED("fft_pass_kernel");
+  fft_tile_kernel<INV, T, OUTER><<<grid, threads, smem, st>>>(b, p);
+  CS_LAUNCHED("fft_tile_kernel");
   return CS_OK;
+}
+
+template <bool INV, bool OUTER>
+cs_status dispatch_tile(const FftBatch& b, uint32_t n_cols, const FftPass& p, cudaStream_t st) {
+  switch (p.hi - p.lo) {
+    case 1: return launch_tile<INV, 1, OUTER>(b, n_cols, p, st);
+    case 2: return launch_tile<INV, 2, OUTER>(b, n_cols, p, st);
+    case 3: return launch_tile<INV, 3, OUTER>(b, n_cols, p, st);
+    case 4: return launch_tile<INV, 4, OUTER>(b, n_cols, p, st);
+    case 5: return launch_tile<INV, 5, OUTER>(b, n_cols, p, st);
+    case 6: return launch_tile<INV, 6, OUTER>(b, n_cols, p, st);
+    case 7: return launch_tile<INV, 7, OUTER>(b, n_cols, p, st);
+    case 8: return launch_tile<INV, 8, OUTER>(b, n_cols, p, st);
+    case 9: return launch_tile<INV, 9, OUTER>(b, n_cols, p, st);
+    case 10: return launch_tile<INV, 10, OUTER>(b, n_cols, p, st);
+    case 11: return launch_tile<INV, 11, OUTER>(b, n_cols, p, st);
+    case 12: return launch_tile<INV, 12, OUTER>(b, n_cols, p, st);
+    default:
+      set_error("fft: unsupported pass of %u layers", p.hi - p.lo);
+      return CS_ERR_INVALID_ARG;
+  }
+}
+
+// Constant columns (no layers): every output word is the single coefficient.
+__global__ void replicate_kernel(const FftBatch batch, uint32_t log_n) {
+  const uint32_t n = 1u << log_n;
+  const uint32_t v = batch.src[blockIdx.y][0];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    batch.dst[blockIdx.y][i] = v;
+}
+
+cs_status dispatch_copy(const FftBatch& b, uint32_t n_cols, const FftPass& p, cudaStream_t st) {
+  const uint32_t n = 1u << p.log_n;
+  dim3 grid(std::min<uint32_t>((n + 255) / 256, 64), n_cols);
+  replicate_kernel<<<grid, 256, 0, st>>>(b, p.log_n);
+  CS_LAUNCHED("replicate_kernel");
+  return CS_OK;
+}
+
+template <bool INV>
+cs_status launch_pass(const FftBatch& b, uint32_t n_cols, const FftPass& p, cudaStream_t st) {
+  if (p.hi == p.lo) {
+    // zero layers: a copy (replication of a constant column)
+    return dispatch_copy(b, n_cols, p, st);
+  }
+  return p.outer ? dispatch_tile<INV, true>(b, n_cols, p, st) : dispatch_tile<INV, false>(b, n_cols, p, st);
 }
 
 // Runs the FFT over a batch of columns. inverse: interpolate in place
@@ -344,6 +427,8 @@ cs_status run_fft(const uint32_t* const* srcs, uint32_t* const* dsts, uint32_t n
                   uint32_t log_n, bool inverse, const uint32_t* tw, uint32_t tw_log, cudaStream_t st,
                   uint32_t tw_dom = 0) {
   if (tw_dom == 0) tw_dom = log_n;
+  // twiddle runs are read as 16-byte vectors
+  CS_CHECK_ARG(log_n <= 2 || (reinterpret_cast<uintptr_t>(tw) & 15) == 0, "fft: twiddle buffer not 16-byte aligned");
   for (uint32_t b0 = 0; b0 < n_cols; b0 += kMaxBatch) {
     const uint32_t nb = std::min<uint32_t>(kMaxBatch, n_cols - b0);
     FftBatch batch;
@@ -371,20 +456,18 @@ cs_status run_fft(const uint32_t* const* srcs, uint32_t* const* dsts, uint32_t n
         p.src_mask = 0xffffffffu;
         // 1/n = 2^(31 - n) in M31 since 2^31 = 1
         p.scale = (k + 1 == plan.size()) ? (1u << (31 - log_n)) : 0;
-        cs_status s = launch_pass<true>(batch, nb, p, pp, st);
+        cs_status s = launch_pass<true>(batch, nb, p, st);
         if (s != CS_OK) return s;
         // the first pass may read a separate source; later passes work in place
         for (uint32_t i = 0; i < nb; i++) batch.src[i] = batch.dst[i];
       }
     } else {
       if (log_src == 0) {
-        // constant polynomial: every evaluation is the constant; a pass over
-        // zero layers would be empty, so replicate with a trivial 1-layer-free copy
-        PassPlan pp{0, 0, std::min(11u, log_n), 1};
-        p.lo = 0; p.hi = 0; p.c = pp.c; p.outer = 1;
+        // constant polynomial: every evaluation is the constant coefficient
+        p.lo = 0; p.hi = 0; p.c = 0; p.outer = 1;
         p.src_mask = 0;
         p.scale = 0;
-        cs_status s = launch_pass<false>(batch, nb, p, pp, st);
+        cs_status s = launch_pass<false>(batch, nb, p, st);
         if (s != CS_OK) return s;
         continue;
       }
@@ -395,12 +478,12 @@ cs_status run_fft(const uint32_t* const* srcs, uint32_t* const* dsts, uint32_t n
         if (k + 1 == plan.size()) {
           p.src_mask = (1u << log_src) - 1;
           FftBatch first = batch;
-          cs_status s = launch_pass<false>(first, nb, p, pp, st);
+          cs_status s = launch_pass<false>(first, nb, p, st);
           if (s != CS_OK) return s;
           for (uint32_t i = 0; i < nb; i++) batch.src[i] = batch.dst[i];
         } else {
           p.src_mask = 0xffffffffu;
-          cs_status s = launch_pass<false>(batch, nb, p, pp, st);
+          cs_status s = launch_pass<false>(batch, nb, p, st);
           if (s != CS_OK) return s;
         }
       }

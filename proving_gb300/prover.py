@@ -1,0 +1,727 @@
+"""The reference's generic prover, restated on the host over a backend.
+
+The reference prover is generic over its backend (`prove_ex`,
+crates/stwo/src/prover/mod.rs:39-138); this module restates that caller for
+the Wide-Fibonacci AIR so that the CUDA backend runs inside a whole proof:
+the commitment scheme (crates/stwo/src/prover/pcs/mod.rs:83-398), DEEP
+quotients (crates/stwo/src/prover/pcs/quotient_ops.rs:86-160), FRI commit and
+decommit (crates/stwo/src/prover/fri.rs:113-438), lifted Merkle decommitment
+(crates/stwo/src/prover/vcs_lifted/prover.rs:97-162), the Blake2s channel
+(crates/stwo/src/core/channel/blake2s.rs:16-118) and query sampling
+(crates/stwo/src/core/queries.rs:11-58). Every mix and draw happens in the
+reference's order. The device work goes through an `ops` object: `GpuOps`
+below drives libstwo_cuda.so; the tests drive the same code with the CPU
+oracle to compare proofs byte for byte.
+"""
+from __future__ import annotations
+
+import hashlib
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+P = (1 << 31) - 1
+
+# ------------------------------------------------------------ QM31 scalars
+# Host arithmetic on single QM31 values (tuples of 4 ints): channel draws,
+# line coefficients and random powers.
+
+
+def m_inv(a: int) -> int:
+    return pow(a, P - 2, P)
+
+
+def cm_mul(x, y):
+    return ((x[0] * y[0] - x[1] * y[1]) % P, (x[0] * y[1] + x[1] * y[0]) % P)
+
+
+def qm(a, b=0, c=0, d=0):
+    return (a % P, b % P, c % P, d % P)
+
+
+def qm_add(x, y):
+    return tuple((a + b) % P for a, b in zip(x, y))
+
+
+def qm_sub(x, y):
+    return tuple((a - b) % P for a, b in zip(x, y))
+
+
+def qm_neg(x):
+    return tuple((-a) % P for a in x)
+
+
+def qm_mul(x, y):
+    # (a + b u)(c + d u) = (ac + (2+i) bd) + (ad + bc) u  (crates/stwo/src/core/fields/qm31.rs:75-81)
+    a, b = (x[0], x[1]), (x[2], x[3])
+    c, d = (y[0], y[1]), (y[2], y[3])
+    ac, bd, ad, bc = cm_mul(a, c), cm_mul(b, d), cm_mul(a, d), cm_mul(b, c)
+    rbd = cm_mul((2, 1), bd)
+    return ((ac[0] + rbd[0]) % P, (ac[1] + rbd[1]) % P, (ad[0] + bc[0]) % P, (ad[1] + bc[1]) % P)
+
+
+def qm_mul_m31(x, m: int):
+    return tuple((a * m) % P for a in x)
+
+
+def qm_inv(x):
+    # (a + b u)^-1 = (a - b u) / (a^2 - (2+i) b^2)  (qm31.rs:113-122)
+    a, b = (x[0], x[1]), (x[2], x[3])
+    b2 = cm_mul(b, b)
+    ib2 = ((-b2[1]) % P, b2[0])
+    a2 = cm_mul(a, a)
+    den = ((a2[0] - 2 * b2[0] - ib2[0]) % P, (a2[1] - 2 * b2[1] - ib2[1]) % P)
+    n = m_inv((den[0] * den[0] + den[1] * den[1]) % P)
+    di = ((den[0] * n) % P, (-den[1] * n) % P)
+    r0 = cm_mul(a, di)
+    r1 = cm_mul(((-b[0]) % P, (-b[1]) % P), di)
+    return (r0[0], r0[1], r1[0], r1[1])
+
+
+def qm_conj(x):
+    """Conjugate with respect to CM31: (a + b u) -> (a - b u)."""
+    return (x[0], x[1], (-x[2]) % P, (-x[3]) % P)
+
+
+def q_double_x(x):
+    s = qm_mul(x, x)
+    return qm_sub(qm_add(s, s), qm(1))
+
+
+def m_double_x(x: int) -> int:
+    return (2 * x * x - 1) % P
+
+
+def from_partial_evals(ev):
+    """QM31::from_partial_evals (crates/stwo/src/core/fields/qm31.rs:48-54)."""
+    r = ev[0]
+    r = qm_add(r, qm_mul(ev[1], qm(0, 1, 0, 0)))
+    r = qm_add(r, qm_mul(ev[2], qm(0, 0, 1, 0)))
+    r = qm_add(r, qm_mul(ev[3], qm(0, 0, 0, 1)))
+    return r
+
+
+def secure_powers(felt, n: int):
+    out, acc = [], qm(1)
+    for _ in range(n):
+        out.append(acc)
+        acc = qm_mul(acc, felt)
+    return out
+
+
+# ------------------------------------------------------------ circle points
+
+def cpoint_add(p, q):
+    return ((p[0] * q[0] - p[1] * q[1]) % P, (p[0] * q[1] + p[1] * q[0]) % P)
+
+
+def index_to_point(idx: int):
+    r, cur = (1, 0), (2, 1268011823)
+    idx &= (1 << 31) - 1
+    while idx:
+        if idx & 1:
+            r = cpoint_add(r, cur)
+        cur = cpoint_add(cur, cur)
+        idx >>= 1
+    return r
+
+
+def qpoint_add(p, q):
+    return (qm_sub(qm_mul(p[0], q[0]), qm_mul(p[1], q[1])), qm_add(qm_mul(p[0], q[1]), qm_mul(p[1], q[0])))
+
+
+def random_point(t):
+    """CirclePoint::get_random_point from a drawn t (crates/stwo/src/core/circle.rs:150-160)."""
+    t2 = qm_mul(t, t)
+    inv = qm_inv(qm_add(t2, qm(1)))
+    return (qm_mul(qm_sub(qm(1), t2), inv), qm_mul(qm_add(t, t), inv))
+
+
+def canonic_domain_point(log_size: int, j: int):
+    """CanonicCoset(log_size).circle_domain().at(j) (crates/stwo/src/core/poly/circle/domain.rs:148-160)."""
+    half_init, half_step, hs = 1 << (31 - (log_size + 1)), 1 << (31 - (log_size - 1)), 1 << (log_size - 1)
+    mask = (1 << 31) - 1
+    if j < hs:
+        return index_to_point((half_init + j * half_step) & mask)
+    return index_to_point((-(half_init + (j - hs) * half_step)) & mask)
+
+
+def bit_reverse_index(i: int, log_size: int) -> int:
+    if log_size == 0:
+        return i
+    return int(format(i, f"0{log_size}b")[::-1], 2)
+
+
+# ------------------------------------------------------------ channel
+
+class Blake2sChannel:
+    """Blake2sChannel (crates/stwo/src/core/channel/blake2s.rs:16-118), hashlib's Blake2s-256."""
+
+    POW_PREFIX = 0x12345678
+
+    def __init__(self, digest: bytes = bytes(32)):
+        self.digest = digest
+        self.n_draws = 0
+        self.log = []  # transcript: (op, data) pairs, for diffing two provers
+
+    def _update(self, d: bytes):
+        self.digest = d
+        self.n_draws = 0
+
+    def mix_u32s(self, words):
+        h = hashlib.blake2s(self.digest)
+        h.update(b"".join(struct.pack("<I", int(w) & 0xFFFFFFFF) for w in words))
+        self._update(h.digest())
+        self.log.append(("mix_u32s", len(words)))
+
+    def mix_u64(self, v: int):
+        self.mix_u32s([v & 0xFFFFFFFF, v >> 32])
+
+    def mix_felts(self, felts):
+        self.mix_u32s([w for f in felts for w in f])
+
+    def mix_root(self, root: bytes):
+        """Blake2sMerkleChannel::mix_hash (crates/stwo/src/core/vcs_lifted/blake2_merkle.rs:56-58)."""
+        self._update(hashlib.blake2s(self.digest + root).digest())
+        self.log.append(("mix_root", root.hex()))
+
+    def draw_u32s(self):
+        h = hashlib.blake2s(self.digest + struct.pack("<I", self.n_draws) + b"\x00").digest()
+        self.n_draws += 1
+        return list(struct.unpack("<8I", h))
+
+    def draw_secure_felt(self):
+        f = [w % P for w in self.draw_u32s()]
+        return tuple((f[2 * i] + 2 * f[2 * i + 1]) % P for i in range(4))
+
+    def draw_queries(self, log_domain_size: int, n_queries: int):
+        mask, out = (1 << log_domain_size) - 1, []
+        while len(out) < n_queries:
+            for w in self.draw_u32s():
+                out.append(w & mask)
+                if len(out) == n_queries:
+                    break
+        return out
+
+    def verify_pow_nonce(self, n_bits: int, nonce: int) -> bool:
+        pre = hashlib.blake2s(struct.pack("<I", self.POW_PREFIX) + self.digest + struct.pack("<I", n_bits)).digest()
+        h = hashlib.blake2s(pre + struct.pack("<Q", nonce)).digest()
+        v = int.from_bytes(h[:16], "little")
+        return v == 0 or (v & -v).bit_length() - 1 >= n_bits
+
+
+# ------------------------------------------------------------ configuration
+
+@dataclass(frozen=True)
+class FriParams:
+    """FriParams (crates/stwo/src/core/fri.rs:31-100)."""
+    pow_bits: int = 10
+    log_blowup_factor: int = 1
+    log_last_layer_degree_bound: int = 0
+    n_queries: int = 70
+    fold_step: int = 1
+
+    def last_layer_domain_size(self) -> int:
+        return 1 << (self.log_last_layer_degree_bound + self.log_blowup_factor)
+
+
+@dataclass(frozen=True)
+class PcsConfig:
+    """PcsConfig (crates/stwo/src/core/pcs/mod.rs:43-76)."""
+    fri_params: FriParams
+    trace_lifting_log_size: int
+    preprocessed_lifting_log_size: int = 0
+
+    def lifting_log_size(self, tree_index: int) -> int:
+        return self.preprocessed_lifting_log_size if tree_index == 0 else self.trace_lifting_log_size
+
+
+OODS_POW_BITS = 16  # crates/stwo/src/core/proof_of_work.rs:8
+
+
+# ------------------------------------------------------------ complex-conjugate lines
+
+def line_coeffs(py, value, alpha):
+    """complex_conjugate_line_coeffs (crates/stwo/src/core/constraints.rs:119-135), scaled by alpha."""
+    a = qm_sub(qm_conj(value), value)
+    c = qm_sub(qm_conj(py), py)
+    b = qm_sub(qm_mul(value, c), qm_mul(a, py))
+    return (qm_mul(alpha, a), qm_mul(alpha, b), qm_mul(alpha, c))
+
+
+# ------------------------------------------------------------ Merkle decommitment
+
+def merkle_decommit(tree, query_positions, columns, ops):
+    """MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:97-162).
+    tree: ops Merkle handle; columns: the committed columns in commit order (may be empty)."""
+    L = tree.height
+    queried = []
+    for col in columns:
+        l = ops.log_size(col)
+        shift = L - l
+        idx = [((p >> (shift + 1)) << 1) + (p & 1) for p in query_positions]
+        queried.append([int(v) for v in ops.gather(col, idx)])
+    witness = []
+    prev = sorted(set(query_positions))
+    for layer_log in range(L - 1, -1, -1):
+        # hashes of layer layer_log + 1 (the children)
+        need, cur = [], []
+        i = 0
+        while i < len(prev):
+            first = prev[i]
+            if i + 1 < len(prev) and prev[i + 1] == first ^ 1:
+                i += 2
+            else:
+                need.append(first ^ 1)
+                i += 1
+            cur.append(first >> 1)
+        if need:
+            witness.extend(tree.hashes(layer_log + 1, need))
+        prev = cur
+    return queried, witness
+
+
+# ------------------------------------------------------------ FRI
+
+def decommitment_positions_and_witness(column_values_at, query_positions, fold_step: int):
+    """compute_decommitment_positions_and_witness_evals (crates/stwo/src/prover/fri.rs:408-438).
+    column_values_at(positions) -> list of QM31 for those positions."""
+    groups, i = [], 0
+    while i < len(query_positions):
+        j = i
+        while j + 1 < len(query_positions) and query_positions[j + 1] >> fold_step == query_positions[i] >> fold_step:
+            j += 1
+        groups.append(query_positions[i:j + 1])
+        i = j + 1
+    positions = []
+    for g in groups:
+        start = (g[0] >> fold_step) << fold_step
+        positions.extend(range(start, start + (1 << fold_step)))
+    values = column_values_at(positions)
+    witness, k = [], 0
+    for g in groups:
+        qs = list(g)
+        start = (g[0] >> fold_step) << fold_step
+        for pos in range(start, start + (1 << fold_step)):
+            v = values[k]
+            k += 1
+            if qs and qs[0] == pos:
+                qs.pop(0)
+            else:
+                witness.append(v)
+    return positions, witness
+
+
+def fold_queries(positions, n_folds: int):
+    """Queries::fold (crates/stwo/src/core/queries.rs:50-56)."""
+    out = []
+    for q in positions:
+        f = q >> n_folds
+        if not out or out[-1] != f:
+            out.append(f)
+    return out
+
+
+# ------------------------------------------------------------ the proof
+
+@dataclass
+class StarkProof:
+    """CommitmentSchemeProof (crates/stwo/src/core/pcs/quotients.rs:26-36) + FriProof (crates/stwo/src/core/fri.rs)."""
+    config: PcsConfig
+    commitments: list = field(default_factory=list)          # roots (bytes)
+    oods_proof_of_work: int = 0
+    sampled_values: list = field(default_factory=list)       # per tree, per column, list of QM31
+    decommitments: list = field(default_factory=list)        # per tree, list of hash witness (bytes)
+    queried_values: list = field(default_factory=list)       # per tree, per column, list of M31
+    fri_first_layer: dict = field(default_factory=dict)
+    fri_inner_layers: list = field(default_factory=list)
+    fri_last_layer_poly: list = field(default_factory=list)
+    fri_proof_of_work: int = 0
+
+    def to_words(self) -> list:
+        """A felt stream in the field order of CairoSerialize for StarkProof
+        (crates/cairo-serialize/src/serialize.rs:121-210): vectors are a length
+        followed by items, QM31 = 4 words, Blake2s hash = 8 LE words, u64 = one felt."""
+        w = []
+
+        def vec(items, f):
+            w.append(len(items))
+            for it in items:
+                f(it)
+
+        def h(b):
+            w.extend(struct.unpack("<8I", b))
+
+        def q(x):
+            w.extend(x)
+
+        fp = self.config.fri_params
+        w.extend([fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound, fp.n_queries, fp.fold_step])
+        w.extend([self.config.trace_lifting_log_size, self.config.preprocessed_lifting_log_size])
+        vec(self.commitments, h)
+        w.append(self.oods_proof_of_work)
+        vec(self.sampled_values, lambda tree: vec(tree, lambda col: vec(col, q)))
+        vec(self.decommitments, lambda wit: vec(wit, h))
+        vec(self.queried_values, lambda tree: vec(tree, lambda col: vec(col, w.append)))
+
+        def layer(lp):
+            vec(lp["fri_witness"], q)
+            vec(lp["decommitment"], h)
+            h(lp["commitment"])
+
+        layer(self.fri_first_layer)
+        vec(self.fri_inner_layers, layer)
+        vec(self.fri_last_layer_poly, q)
+        w.append(self.fri_proof_of_work)
+        return w
+
+    def to_bytes(self) -> bytes:
+        return b"".join(struct.pack("<Q", int(x)) for x in self.to_words())
+
+
+def prove_wide_fib(ops, trace, log_n_rows: int, config: PcsConfig, channel: Blake2sChannel, twiddles):
+    """Commits the (empty) preprocessed tree and the Wide-Fibonacci trace, then
+    runs prove_ex (crates/stwo/src/prover/mod.rs:39-138). `trace`: the
+    column evaluations on CanonicCoset(log_n_rows), as ops columns (consumed)."""
+    fp = config.fri_params
+    b = fp.log_blowup_factor
+    L = config.trace_lifting_log_size
+    n_cols = len(trace)
+
+    # --- preprocessed tree: empty, a single hash of no data at height 0 (pcs/mod.rs:83-96)
+    pre_root = hashlib.blake2s(b"").digest()
+    channel.mix_root(pre_root)
+
+    # --- trace tree (TreeBuilder::extend_evals + commit, pcs/mod.rs:325-349, 360-386)
+    ops.interpolate(trace, twiddles)
+    trace_evals = ops.evaluate(trace, log_n_rows + b, twiddles)
+    trace_tree = ops.merkle_commit(trace_evals, L)
+    channel.mix_root(trace_tree.root)
+
+    # --- prove_ex: composition polynomial (air/component_prover.rs:95-116)
+    random_coeff = channel.draw_secure_felt()
+    n_constraints = n_cols - 2
+    # EvaluationMode::infer: constraint log degree 1 <= blowup -> SubDomain{b - 1}
+    log_expansion = b - 1
+    eval_log = log_n_rows + 1
+    if log_expansion != 0:
+        raise NotImplementedError("the Wide-Fibonacci prover supports log_blowup_factor = 1")
+    # the component's powers are the accumulator's last n, reversed (accumulation.rs:102-122,
+    # component_prover.rs:194): constraint k gets alpha^(N-1-k)
+    rc = list(reversed(secure_powers(random_coeff, n_constraints)))
+    accum = ops.secure_zeros(1 << eval_log)
+    ops.wide_fib_composition(trace_evals, log_n_rows, rc, accum)
+    # finalize: lift_and_accumulate of one column is itself; interpolate on CanonicCoset(eval_log)
+    comp_coeffs = ops.interpolate_secure(accum, twiddles)
+    left, right = ops.split_at_mid(comp_coeffs)
+    comp_polys = left + right  # extend_polys(left coords), extend_polys(right coords)
+    comp_evals = ops.evaluate(comp_polys, (eval_log - 1) + b, twiddles)
+    comp_tree = ops.merkle_commit(comp_evals, L)
+    channel.mix_root(comp_tree.root)
+
+    # --- OODS proof of work and point (mod.rs:75-83)
+    oods_pow = ops.grind(channel.digest, OODS_POW_BITS)
+    channel.mix_u64(oods_pow)
+    oods = random_point(channel.draw_secure_felt())
+
+    # --- prove_values (pcs/mod.rs:224-315)
+    lifting = L
+    columns = [[], trace_evals, comp_evals]
+    sample_points = [[], [[oods]] * n_cols, [[oods]] * 8]
+    sampled = []
+    for tree_cols, pts in zip(columns, sample_points):
+        vals = [[] for _ in tree_cols]
+        by_size = {}
+        for ci, col in enumerate(tree_cols):
+            by_size.setdefault(ops.log_size(col), []).append(ci)
+        for log_size, cis in by_size.items():
+            # one weight column per (log size, point.repeated_double(lifting - log_size))
+            pt = pts[cis[0]][0]
+            for _ in range(lifting - log_size):
+                pt = (q_double_x(pt[0]), qm_mul(qm(2), qm_mul(pt[0], pt[1])))
+            w = ops.barycentric_weights(log_size, pt)
+            res = ops.barycentric_eval([tree_cols[ci] for ci in cis], w)
+            for ci, v in zip(cis, res):
+                vals[ci] = [tuple(int(x) for x in v)]
+        sampled.append(vals)
+    channel.mix_felts([v for tree in sampled for col in tree for v in col])
+
+    quotient_coeff = channel.draw_secure_felt()
+    quotients = compute_fri_quotients(ops, columns, sample_points, sampled, quotient_coeff, lifting, b, twiddles)
+
+    # --- FRI commit (fri.rs:113-226)
+    fri = fri_commit(ops, channel, fp, quotients, lifting, twiddles)
+
+    # --- FRI decommit (fri.rs:229-283)
+    fri_pow = ops.grind(channel.digest, fp.pow_bits)
+    channel.mix_u64(fri_pow)
+    unsorted = channel.draw_queries(lifting, fp.n_queries)
+    queries = sorted(set(unsorted))
+    first = fri["first"]
+    pos, wit = decommitment_positions_and_witness(lambda ps: ops.gather_secure(quotients, ps), queries, fp.fold_step)
+    _, dec = merkle_decommit(first["tree"], pos, [], ops)
+    proof = StarkProof(config=config)
+    proof.fri_first_layer = {"fri_witness": wit, "decommitment": dec, "commitment": first["tree"].root}
+    layer_queries = fold_queries(queries, fp.fold_step)
+    for layer in fri["inner"]:
+        pos, wit = decommitment_positions_and_witness(lambda ps, ev=layer["eval"]: ops.gather_secure(ev, ps),
+                                                      layer_queries, layer["fold_step"])
+        _, dec = merkle_decommit(layer["tree"], pos, [], ops)
+        proof.fri_inner_layers.append({"fri_witness": wit, "decommitment": dec, "commitment": layer["tree"].root})
+        layer_queries = fold_queries(layer_queries, layer["fold_step"])
+    proof.fri_last_layer_poly = fri["last_poly"]
+    proof.fri_proof_of_work = fri_pow
+
+    # --- tree decommitments (pcs/mod.rs:259-287); the empty preprocessed tree has height 0
+    proof.commitments = [pre_root, trace_tree.root, comp_tree.root]
+    proof.oods_proof_of_work = oods_pow
+    proof.sampled_values = sampled
+    proof.decommitments = [[]]
+    proof.queried_values = [[]]
+    for tree, cols in ((trace_tree, trace_evals), (comp_tree, comp_evals)):
+        qv, wit = merkle_decommit(tree, queries, cols, ops)
+        proof.queried_values.append(qv)
+        proof.decommitments.append(wit)
+
+    # --- sanity check: composition value at the OODS point (mod.rs:121-132)
+    max_log_degree_bound = lifting - b
+    comp = sampled[2]
+    left_v = from_partial_evals([comp[k][0] for k in range(4)])
+    right_v = from_partial_evals([comp[k][0] for k in range(4, 8)])
+    x = oods[0]
+    for _ in range(max_log_degree_bound - 1):
+        x = q_double_x(x)
+    composition_oods = qm_add(left_v, qm_mul(x, right_v))
+    expected = wide_fib_composition_at_point(oods, [c[0] for c in sampled[1]], random_coeff, max_log_degree_bound)
+    if composition_oods != expected:
+        raise RuntimeError("constraints not satisfied (ProvingError::ConstraintsNotSatisfied)")
+    return proof
+
+
+def wide_fib_composition_at_point(point, mask, random_coeff, max_log_degree_bound: int):
+    """Components::eval_composition_polynomial_at_point for the Wide-Fibonacci component
+    (crates/constraint-framework/src/component.rs:220-243, PointEvaluationAccumulator,
+    crates/stwo/src/core/air/accumulation.rs:13-33): Horner over the constraints,
+    each divided by V_trace(point)."""
+    x = point[0]
+    for _ in range(max_log_degree_bound - 1):
+        x = q_double_x(x)
+    den_inv = qm_inv(x)
+    acc = qm(0)
+    for k in range(len(mask) - 2):
+        a, bb, c = mask[k], mask[k + 1], mask[k + 2]
+        cons = qm_sub(c, qm_add(qm_mul(a, a), qm_mul(bb, bb)))
+        acc = qm_add(qm_mul(acc, random_coeff), qm_mul(cons, den_inv))
+    return acc
+
+
+def compute_fri_quotients(ops, columns, sample_points, sampled, random_coeff, lifting: int, log_blowup: int,
+                          twiddles):
+    """compute_fri_quotients (crates/stwo/src/prover/pcs/quotient_ops.rs:86-160) for columns with one
+    sample each (no periodicity samples, crates/stwo/src/core/pcs/quotients.rs:274-319)."""
+    pows = iter(secure_powers(random_coeff, sum(len(c) for tree in sampled for c in tree)))
+    entries = []  # (column, point, value, random power) in tree/column order
+    for tree_cols, pts, vals in zip(columns, sample_points, sampled):
+        for col, cp, cv in zip(tree_cols, pts, vals):
+            if len(cp) == 2:
+                raise NotImplementedError("periodicity samples")
+            for p_, v_ in zip(cp, cv):
+                entries.append((col, p_, v_, next(pows)))
+    # stable sort by column log size, group by size, batch by point in insertion order
+    entries_sorted = sorted(enumerate(entries), key=lambda e: ops.log_size(e[1][0]))
+    accs = []  # (point, partial numerator column, first linear term)
+    i = 0
+    while i < len(entries_sorted):
+        ls = ops.log_size(entries_sorted[i][1][0])
+        j = i
+        while j < len(entries_sorted) and ops.log_size(entries_sorted[j][1][0]) == ls:
+            j += 1
+        group = [e[1] for e in entries_sorted[i:j]]
+        batches = {}
+        for col, p_, v_, rp in group:
+            batches.setdefault(p_, []).append((col, v_, rp))
+        for p_, items in batches.items():
+            coeffs = [line_coeffs(p_[1], v_, rp) for _, v_, rp in items]
+            part, first_linear = ops.accumulate_numerators([c for c, _, _ in items], coeffs, log_blowup)
+            accs.append((p_, part, tuple(int(x) for x in first_linear)))
+        i = j
+    # group per sample point (sorted by (x, y)), lift and accumulate ascending sizes
+    per_point = {}
+    for p_, part, fl in accs:
+        per_point.setdefault(p_, []).append((part, fl))
+    points, parts, fls = [], [], []
+    for p_ in sorted(per_point, key=lambda pt: (pt[0], pt[1])):
+        items = per_point[p_]
+        fl = qm(0)
+        for _, f in items:
+            fl = qm_add(fl, f)
+        col = ops.lift_and_accumulate([part for part, _ in sorted(items, key=lambda it: ops.secure_len(it[0]))])
+        points.append(p_)
+        parts.append(col)
+        fls.append(fl)
+    return ops.compute_quotients_and_combine(parts, points, fls, lifting, log_blowup, twiddles)
+
+
+def fri_commit(ops, channel, fp: FriParams, column, log_size: int, twiddles):
+    """FriProver::commit (crates/stwo/src/prover/fri.rs:113-226), fold_step 1 (no leaf packing)."""
+    if fp.fold_step != 1:
+        raise NotImplementedError("fold_step > 1")
+    first_tree = ops.merkle_commit(ops.secure_columns(column), log_size)
+    channel.mix_root(first_tree.root)
+    alpha = channel.draw_secure_felt()
+    layer = ops.fold_circle_into_line(column, alpha, twiddles)
+    line_log = log_size - 1
+    last_log = (fp.last_layer_domain_size()).bit_length() - 1
+    inner = []
+    while line_log > last_log + fp.fold_step:
+        tree = ops.merkle_commit(ops.secure_columns(layer), line_log)
+        channel.mix_root(tree.root)
+        alpha = channel.draw_secure_felt()
+        inner.append({"tree": tree, "eval": layer, "fold_step": fp.fold_step})
+        layer = ops.fold_line(layer, alpha, twiddles)
+        line_log -= fp.fold_step
+    last_step = line_log - last_log
+    tree = ops.merkle_commit(ops.secure_columns(layer), line_log)
+    channel.mix_root(tree.root)
+    alpha = channel.draw_secure_felt()
+    inner.append({"tree": tree, "eval": layer, "fold_step": last_step})
+    for _ in range(last_step):
+        layer = ops.fold_line(layer, alpha, twiddles)
+        alpha = qm_mul(alpha, alpha)
+    # commit_last_layer (fri.rs:208-226): interpolate the last evaluation on its line domain
+    values = ops.gather_secure(layer, list(range(fp.last_layer_domain_size())))
+    coeffs = line_interpolate(values, last_log)
+    bound = 1 << fp.log_last_layer_degree_bound
+    if any(c != qm(0) for c in coeffs[bound:]):
+        raise RuntimeError("invalid degree in the last FRI layer")
+    # LinePoly::from_ordered_coefficients stores them bit-reversed; that order is mixed
+    last_poly = [coeffs[:bound][bit_reverse_index(i, fp.log_last_layer_degree_bound)] for i in range(bound)]
+    channel.mix_felts(last_poly)
+    return {"first": {"tree": first_tree}, "inner": inner, "last_poly": last_poly}
+
+
+def line_interpolate(values, log_size: int):
+    """LineEvaluation::interpolate + LinePoly::into_ordered_coefficients
+    (crates/stwo/src/prover/line.rs:54-99, crates/stwo/src/core/poly/line.rs:151-154)
+    for an evaluation on LineDomain(half_odds(log_size)) given in bit-reversed
+    order; returns the coefficients in natural order."""
+    n = 1 << log_size
+    v = [values[bit_reverse_index(i, log_size)] for i in range(n)]
+    mask = (1 << 31) - 1
+    init, step, dom_log = 1 << (31 - (log_size + 2)), 1 << (31 - log_size), log_size
+    while dom_log > 0:
+        size = 1 << dom_log
+        xs = [index_to_point((init + i * step) & mask)[0] for i in range(size // 2)]
+        for start in range(0, n, size):
+            for i in range(size // 2):
+                a, c = v[start + i], v[start + size // 2 + i]
+                v[start + i] = qm_add(a, c)
+                v[start + size // 2 + i] = qm_mul_m31(qm_sub(a, c), m_inv(xs[i]))
+        init, step, dom_log = (init * 2) & mask, (step * 2) & mask, dom_log - 1
+    ninv = m_inv(n % P)
+    v = [qm_mul_m31(x, ninv) for x in v]
+    return [v[bit_reverse_index(i, log_size)] for i in range(n)]
+
+
+# ------------------------------------------------------------ GPU ops
+
+class GpuMerkle:
+    def __init__(self, prover, height: int):
+        self.t = prover
+        self.height = height
+        self.root = prover.root()
+
+    def hashes(self, layer_log: int, idx):
+        import torch
+        lay = self.t.layer(layer_log)
+        sel = lay[torch.as_tensor(idx, device=lay.device, dtype=torch.long)]
+        arr = sel.cpu().numpy().astype("<i4")
+        return [arr[i].tobytes() for i in range(arr.shape[0])]
+
+
+class GpuOps:
+    """Device operations of the prover through libstwo_cuda.so (proving_gb300.backend)."""
+
+    def __init__(self):
+        from . import backend as be
+        self.be = be
+        self.B = be.CudaBackend
+
+    def twiddles(self, root_log_domain: int):
+        return self.B.precompute_twiddles(self.be.canonic_half_coset(root_log_domain))
+
+    def columns_from_host(self, cols):
+        return [self.be.BaseColumn.from_cpu(c) for c in cols]
+
+    def log_size(self, col) -> int:
+        return col.log_size
+
+    def interpolate(self, cols, tw):
+        self.B.interpolate_columns(cols, tw)
+
+    def evaluate(self, coeffs, log_size, tw):
+        return self.B.evaluate_polynomials(coeffs, log_size, tw)
+
+    def merkle_commit(self, cols, L):
+        return GpuMerkle(self.B.merkle_commit(cols, L), L)
+
+    def gather(self, col, idx):
+        import torch
+        t = col.data[torch.as_tensor(idx, device=col.data.device, dtype=torch.long)]
+        return t.cpu().numpy().view(np.uint32)
+
+    def secure_zeros(self, n):
+        return self.be.SecureColumnByCoords.zeros(n)
+
+    def secure_len(self, col) -> int:
+        return len(col)
+
+    def secure_columns(self, col):
+        return col.columns
+
+    def gather_secure(self, col, idx):
+        vals = [self.gather(c, idx) for c in col.columns]
+        return [tuple(int(vals[k][i]) for k in range(4)) for i in range(len(idx))]
+
+    def wide_fib_composition(self, evals, trace_log, rc, accum):
+        self.B.wide_fib_composition(evals, trace_log, np.asarray(rc, np.uint32), accum)
+
+    def interpolate_secure(self, accum, tw):
+        self.B.interpolate_columns(accum.columns, tw)
+        return accum.columns
+
+    def split_at_mid(self, coeff_cols):
+        be = self.be
+        half = len(coeff_cols[0]) // 2
+        left = [be.BaseColumn(c.data[:half]) for c in coeff_cols]
+        right = [be.BaseColumn(c.data[half:]) for c in coeff_cols]
+        return left, right
+
+    def grind(self, digest, bits):
+        return self.B.grind(digest, bits)
+
+    def barycentric_weights(self, log_size, point):
+        return self.B.barycentric_weights(log_size, point)
+
+    def barycentric_eval(self, cols, weights):
+        out = self.B.barycentric_eval_at_point(cols, weights).cpu().numpy().view(np.uint32)
+        return [tuple(int(x) for x in row) for row in out]
+
+    def accumulate_numerators(self, cols, coeffs, log_blowup):
+        arr = np.asarray([[list(a), list(b_), list(c)] for a, b_, c in coeffs], np.uint32)
+        return self.B.accumulate_numerators(cols, arr, log_blowup)
+
+    def lift_and_accumulate(self, cols):
+        return self.B.lift_and_accumulate(cols)
+
+    def compute_quotients_and_combine(self, parts, points, fls, lifting, log_blowup, tw):
+        pts = [(np.asarray(p_[0], np.uint32), np.asarray(p_[1], np.uint32)) for p_ in points]
+        return self.B.compute_quotients_and_combine(parts, pts, [np.asarray(f, np.uint32) for f in fls], lifting,
+                                                    log_blowup, tw)
+
+    def fold_circle_into_line(self, col, alpha, tw):
+        return self.B.fold_circle_into_line(col, np.asarray(alpha, np.uint32), tw)
+
+    def fold_line(self, col, alpha, tw):
+        return self.B.fold_line(col, [np.asarray(alpha, np.uint32)], tw)

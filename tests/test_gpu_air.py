@@ -1,0 +1,39 @@
+"""GPU parity of the Wide-Fibonacci AIR kernels (trace generation and
+constraint quotients on the evaluation domain) against the oracle."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O  # noqa: E402
+from proving_gb300.synthetic import m31_column, seeded_qm31  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def B():
+    from proving_gb300 import build
+    build.build()
+    from proving_gb300.backend import CudaBackend
+    return CudaBackend
+
+
+@pytest.mark.parametrize("n_cols,log_n", [(3, 4), (100, 10), (100, 14)])
+def test_trace_and_composition(B, n_cols, log_n):
+    from proving_gb300.backend import BaseColumn, SecureColumnByCoords, canonic_half_coset
+    a, b = m31_column(1, log_n), m31_column(2, log_n)
+    cols = B.wide_fib_trace(BaseColumn.from_cpu(a), BaseColumn.from_cpu(b), n_cols)
+    want_cols = O.wide_fib_trace(a, b, n_cols)
+    for c, w in zip(cols, want_cols):
+        assert np.array_equal(c.to_cpu(), w)
+    # extend to the evaluation domain (log + 1) and evaluate the constraints there
+    tree = B.precompute_twiddles(canonic_half_coset(log_n + 2))
+    tw, itw = O.canonic_twiddles(log_n + 2)
+    B.interpolate_columns(cols, tree)
+    ev = B.evaluate_polynomials(cols, log_n + 1, tree)
+    ev_o = O.evaluate_batch(O.interpolate_batch(want_cols, itw), [log_n + 1] * n_cols, tw)
+    rc = np.stack([seeded_qm31(k) for k in range(n_cols - 2)])
+    acc = SecureColumnByCoords.zeros(1 << (log_n + 1))
+    B.wide_fib_composition(ev, log_n, rc, acc)
+    want = O.wide_fib_composition(ev_o, log_n + 1, log_n, rc)
+    assert all(np.array_equal(g, w) for g, w in zip(acc.to_cpu(), want))
