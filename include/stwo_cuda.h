@@ -287,6 +287,22 @@ cs_status cs_wide_fib_trace(const uint32_t *d_a, const uint32_t *d_b, uint32_t l
 cs_status cs_grind_blake2s(const uint8_t digest[32], uint32_t pow_bits, uint64_t max_nonce, uint64_t *nonce_out,
                            cs_stream stream);
 
+/* Allocation-free proof-of-work search. It has no counterpart in the
+   reference. It is for callers that cannot allocate device memory: a prover
+   embedded in a service that carves all device memory into a fixed arena up
+   front, or code that must not add allocation calls to a stream it does not
+   own. It gives the same nonces as cs_grind_blake2s, one per digest
+   (digests: n_digests x 32 bytes, nonces_out: n_digests values), but keeps
+   its best-nonce slots in a static device array of 64 slots (512 bytes,
+   resident on every GPU that loads this library until the process exits)
+   instead of allocating, so n_digests above 64 is rejected with
+   CS_ERR_INVALID_ARG. The first call on a device, with that device current,
+   looks up the array's device address; make that call before any stream
+   capture. Calls share the array: calls that overlap on the GPU race.
+   Synchronous on `stream`. */
+cs_status cs_grind_blake2s_noalloc(const uint8_t *digests, uint32_t n_digests, uint32_t pow_bits, uint64_t max_nonce,
+                                   uint64_t *nonces_out, cs_stream stream);
+
 #ifdef __cplusplus
 }
 #endif
