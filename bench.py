@@ -190,6 +190,32 @@ class CommitStage:
         return self.layers[-1].cpu().numpy().astype("<i4").tobytes()
 
 
+def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: int = 100):
+    """Full Wide-Fibonacci proves (config 1 shape: 100 columns x 2^14 rows, blowup 2,
+    70 queries, pow 10) through the restated prover on the CUDA backend; the
+    trace is generated on the device from seeded inputs. Returns wall-clock
+    latencies in ms (host orchestration included)."""
+    from proving_gb300 import prover as pr
+    from proving_gb300.backend import BaseColumn, CudaBackend
+    from proving_gb300.synthetic import m31_column
+    ops = pr.GpuOps()
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=log_n + 1)
+    tw = ops.twiddles(log_n + 2)
+    lat = []
+    for k in range(n_proofs + 2):
+        a = BaseColumn.from_cpu(m31_column(100 + k, log_n))
+        b = BaseColumn.from_cpu(m31_column(200 + k, log_n))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        trace = CudaBackend.wide_fib_trace(a, b, n_cols)
+        proof = pr.prove_wide_fib(ops, trace, log_n, cfg, pr.Blake2sChannel(), tw)
+        torch.cuda.synchronize()
+        if k >= 2:
+            lat.append((time.perf_counter() - t0) * 1e3)
+    return lat
+
+
 def run_gpu(args):
     import torch
     from proving_gb300 import _lib
@@ -283,6 +309,7 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     e2e_value = world * args.steps / (float(t.item()) / 1e3)
 
+    wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -319,6 +346,11 @@ def run_gpu(args):
                      "gcompressions_per_s": ff(leaf_comp / (leaf_ms / 1e3) / 1e9),
                      "int_ops_per_compression": 1120,
                      "tops_achieved": ff(leaf_comp * 1120 / (leaf_ms / 1e3) / 1e12)},
+        "wide_fib_prove": ({"workload": "Wide-Fibonacci 100 cols x 2^14 rows, blowup 2, 70 queries, pow 10, "
+                                         "full prove (trace generated on device)",
+                            "proofs_per_s": ff(1e3 / statistics.mean(wf_lat)),
+                            "p50_ms": ff(float(np.percentile(wf_lat, 50))),
+                            "p99_ms": ff(float(np.percentile(wf_lat, 99)))} if wf_lat else None),
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
@@ -411,6 +443,7 @@ def main():
     ap.add_argument("--n-cols", type=int, default=N_COLS, help="trace columns (smaller cases for profiling)")
     ap.add_argument("--log-rows", type=int, default=LOG_ROWS, help="log2 rows per trace column")
     ap.add_argument("--skip-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--skip-prove", action="store_true", help="skip the Wide-Fibonacci full-prove latency leg")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
     if args.impl == "reference":

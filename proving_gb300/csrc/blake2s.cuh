@@ -25,14 +25,29 @@ inline uint32_t rotr12(uint32_t x) { return (x >> 12) | (x << 20); }
 inline uint32_t rotr7(uint32_t x) { return (x >> 7) | (x << 25); }
 #endif
 
+// Integer multiply-add with a multiplier the compiler cannot see is 1: it
+// issues on the FMA pipe, which the ALU-bound rounds otherwise leave idle.
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ uint32_t fma_add(uint32_t a, uint32_t one, uint32_t b) {
+  uint32_t r;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(one), "r"(b));
+  return r;
+}
+#else
+inline uint32_t fma_add(uint32_t a, uint32_t one, uint32_t b) { return a * one + b; }
+#endif
+
+// One G step. Of its six additions, c + d (twice) and the outer add of
+// a + (b + m) (twice) go to the FMA pipe; xors, rotations and b + m stay on
+// the ALU pipe.
 #define CS_B2S_G(a, b, c, d, x, y) \
-  a = a + b + (x);                 \
+  a = fma_add(a, one, b + (x));    \
   d = rotr16(d ^ a);               \
-  c = c + d;                       \
+  c = fma_add(c, one, d);          \
   b = rotr12(b ^ c);               \
-  a = a + b + (y);                 \
+  a = fma_add(a, one, b + (y));    \
   d = rotr8(d ^ a);                \
-  c = c + d;                       \
+  c = fma_add(c, one, d);          \
   b = rotr7(b ^ c);
 
 #define CS_B2S_ROUND(s0, s1, s2, s3, s4, s5, s6, s7, s8, s9, s10, s11, s12, s13, s14, s15) \
@@ -46,9 +61,10 @@ inline uint32_t rotr7(uint32_t x) { return (x >> 7) | (x << 25); }
   CS_B2S_G(v3, v4, v9, v14, m[s14], m[s15])
 
 // h: chaining value (in/out). m: 16 message words. t: byte counter after this
-// block. last: whether this is the final block.
+// block. last: whether this is the final block. one: the value 1, passed in at
+// run time (a kernel parameter) so the additions above stay multiply-adds.
 __host__ __device__ __forceinline__ void b2s_compress(uint32_t h[8], const uint32_t m[16], uint32_t t_lo,
-                                                      uint32_t t_hi, bool last) {
+                                                      uint32_t t_hi, bool last, uint32_t one = 1) {
   uint32_t v0 = h[0], v1 = h[1], v2 = h[2], v3 = h[3], v4 = h[4], v5 = h[5], v6 = h[6], v7 = h[7];
   uint32_t v8 = 0x6A09E667u, v9 = 0xBB67AE85u, v10 = 0x3C6EF372u, v11 = 0xA54FF53Au;
   uint32_t v12 = 0x510E527Fu ^ t_lo, v13 = 0x9B05688Cu ^ t_hi;

@@ -112,16 +112,16 @@ __device__ __forceinline__ void load_twiddles(const FftPass& p, uint32_t layer, 
           w[8 * q8 + 4 * k + 3] = xs[k];
         }
       }
-      return;
-    }
+    } else {
 #pragma unroll
-    for (int q = 0; q < CNT; q++) {
-      const uint32_t h = h0 + q;
-      const uint32_t pair = (h >> 2) << 1;
-      const uint32_t x = __ldg(lt1 + pair), y = __ldg(lt1 + pair + 1);
-      const uint32_t sel = h & 3;
-      const uint32_t val = sel < 2 ? y : x;
-      w[q] = (sel == 1 || sel == 2) ? m31_neg(val) : val;
+      for (int q = 0; q < CNT; q++) {
+        const uint32_t h = h0 + q;
+        const uint32_t pair = (h >> 2) << 1;
+        const uint32_t x = __ldg(lt1 + pair), y = __ldg(lt1 + pair + 1);
+        const uint32_t sel = h & 3;
+        const uint32_t val = sel < 2 ? y : x;
+        w[q] = (sel == 1 || sel == 2) ? m31_neg(val) : val;
+      }
     }
     return;
   }
@@ -176,9 +176,15 @@ template <int T, bool OUTER>
 constexpr int tile_max_threads() {
   return OUTER ? 256 : (1 << (T / 2 + 3));
 }
+// Blocks per SM the register budget is sized for: contiguous tiles of up to
+// 10 layers fit three without spills, the others two.
+template <int T, bool OUTER>
+constexpr int tile_min_blocks() {
+  return (OUTER && T <= 10) ? 3 : 2;
+}
 
 template <bool INV, int T, bool OUTER>
-__global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), 2) fft_tile_kernel(const FftBatch batch, const FftPass p) {
+__global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), tile_min_blocks<T, OUTER>()) fft_tile_kernel(const FftBatch batch, const FftPass p) {
   constexpr int TA = T / 2, TB = T - TA;
   constexpr uint32_t M = 1u << T;
   extern __shared__ uint32_t s[];

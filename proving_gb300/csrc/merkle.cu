@@ -27,6 +27,7 @@ struct LeafParams {
   uint8_t shift[kMaxLeafCols];  // L - l + 1
   uint32_t n_cols;
   uint32_t log_leaves;
+  uint32_t one;  // 1, opaque to the compiler (see b2s_compress)
 };
 
 __global__ void __launch_bounds__(kLeafThreads) merkle_leaves_kernel(const __grid_constant__ LeafParams p,
@@ -58,7 +59,7 @@ __global__ void __launch_bounds__(kLeafThreads) merkle_leaves_kernel(const __gri
         }
         m[k] = v;
       }
-      b2s_compress(h, m, (base + cnt) * 4, 0, last);
+      b2s_compress(h, m, (base + cnt) * 4, 0, last, p.one);
     }
   }
   uint4* o = reinterpret_cast<uint4*>(out + (size_t)i * 8);
@@ -66,7 +67,8 @@ __global__ void __launch_bounds__(kLeafThreads) merkle_leaves_kernel(const __gri
   o[1] = make_uint4(h[4], h[5], h[6], h[7]);
 }
 
-__global__ void merkle_node_kernel(const uint32_t* __restrict__ prev, uint32_t log_out, uint32_t* __restrict__ out) {
+__global__ void merkle_node_kernel(const uint32_t* __restrict__ prev, uint32_t log_out, uint32_t* __restrict__ out,
+                                   uint32_t one) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (1u << log_out)) return;
   const uint4* src = reinterpret_cast<const uint4*>(prev + (size_t)i * 16);
@@ -81,7 +83,7 @@ __global__ void merkle_node_kernel(const uint32_t* __restrict__ prev, uint32_t l
   }
   uint32_t h[8];
   b2s_init(h);
-  b2s_compress(h, m, 64, 0, true);
+  b2s_compress(h, m, 64, 0, true, one);
   uint4* o = reinterpret_cast<uint4*>(out + (size_t)i * 8);
   o[0] = make_uint4(h[0], h[1], h[2], h[3]);
   o[1] = make_uint4(h[4], h[5], h[6], h[7]);
@@ -98,6 +100,7 @@ cs_status merkle_leaves(const uint32_t* const* cols, const uint32_t* log_sizes, 
   static thread_local LeafParams p;
   p.n_cols = n_cols;
   p.log_leaves = n_cols == 0 ? 0 : L;
+  p.one = 1;
   uint32_t prev = 0;
   for (uint32_t c = 0; c < n_cols; c++) {
     CS_CHECK_ARG(cols[c] != nullptr, "build_leaves: column %u is null", c);
@@ -119,7 +122,7 @@ cs_status merkle_next_layer(const uint32_t* d_prev, uint32_t log_out, uint32_t* 
   CS_CHECK_ARG(log_out <= 29, "build_next_layer: log size %u too large", log_out);
   const uint32_t n = 1u << log_out;
   const uint32_t threads = 128;
-  merkle_node_kernel<<<(n + threads - 1) / threads, threads, 0, st>>>(d_prev, log_out, d_out);
+  merkle_node_kernel<<<(n + threads - 1) / threads, threads, 0, st>>>(d_prev, log_out, d_out, 1u);
   CS_LAUNCHED("merkle_node_kernel");
   return CS_OK;
 }

@@ -1,0 +1,54 @@
+"""Whole Wide-Fibonacci proofs with the CUDA backend: the same restated prover
+driven by the GPU backend and by the CPU oracle gives byte-identical proofs
+(and transcripts), and the restated verifier accepts them. Sizes include the
+config-1 shape (100 columns, 2^14 rows, blowup 2, 70 queries, pow 10)."""
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O  # noqa: E402
+from oracle.cpu_ops import CpuOps  # noqa: E402
+from oracle.verifier import verify_wide_fib  # noqa: E402
+from proving_gb300 import prover as pr  # noqa: E402
+from proving_gb300.synthetic import m31_column  # noqa: E402
+
+N_COLS = 100
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from proving_gb300 import build
+    build.build()
+    return pr.GpuOps()
+
+
+def _prove(ops, trace_host, log_n):
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=log_n + 1)
+    ch = pr.Blake2sChannel()
+    proof = pr.prove_wide_fib(ops, ops.columns_from_host(trace_host), log_n, cfg, ch, ops.twiddles(log_n + 2))
+    return proof, ch
+
+
+@pytest.mark.parametrize("log_n", [4, 7, 10, 14])
+def test_gpu_proof_bytes_equal_oracle(gpu, log_n):
+    trace = O.wide_fib_trace(m31_column(11, log_n), m31_column(12, log_n), N_COLS)
+    g, gch = _prove(gpu, trace, log_n)
+    c, cch = _prove(CpuOps(), trace, log_n)
+    assert gch.digest == cch.digest
+    assert g.to_bytes() == c.to_bytes()
+    verify_wide_fib(g, N_COLS, log_n)
+
+
+def test_device_trace_generation_proof(gpu):
+    # trace generated on the device (cs_wide_fib_trace) proves the same statement
+    log_n = 10
+    a, b = m31_column(21, log_n), m31_column(22, log_n)
+    from proving_gb300.backend import BaseColumn, CudaBackend
+    dev_trace = CudaBackend.wide_fib_trace(BaseColumn.from_cpu(a), BaseColumn.from_cpu(b), N_COLS)
+    fp = pr.FriParams()
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=log_n + 1)
+    proof = pr.prove_wide_fib(gpu, dev_trace, log_n, cfg, pr.Blake2sChannel(), gpu.twiddles(log_n + 2))
+    host, _ = _prove(CpuOps(), O.wide_fib_trace(a, b, N_COLS), log_n)
+    assert proof.to_bytes() == host.to_bytes()

@@ -1,0 +1,64 @@
+"""Whole-proof host logic on the CPU: the restated prover driven by the oracle
+backend produces Wide-Fibonacci proofs that the restated verifier accepts
+(crates/examples/src/wide_fibonacci/mod.rs:182-241) and rejects when tampered
+with (a bad OODS nonce, :245-309; a changed queried value; a changed FRI value)."""
+import copy
+
+import pytest
+
+from oracle import oracle as O
+from oracle.cpu_ops import CpuOps
+from oracle.verifier import VerificationError, verify_wide_fib
+from proving_gb300 import prover as pr
+from proving_gb300.synthetic import m31_column
+
+N_COLS = 100
+
+
+def make_proof(log_n, n_queries=70):
+    ops = CpuOps()
+    trace = O.wide_fib_trace(m31_column(1, log_n), m31_column(2, log_n), N_COLS)
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=n_queries,
+                      fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=log_n + 1)
+    return pr.prove_wide_fib(ops, ops.columns_from_host(trace), log_n, cfg, pr.Blake2sChannel(),
+                             ops.twiddles(log_n + 2))
+
+
+@pytest.mark.parametrize("log_n", [4, 5, 8])
+def test_prove_then_verify(log_n):
+    verify_wide_fib(make_proof(log_n), N_COLS, log_n)
+
+
+def test_tampering_is_rejected():
+    proof = make_proof(5)
+    bad = copy.deepcopy(proof)
+    bad.oods_proof_of_work += 1
+    with pytest.raises(VerificationError):
+        verify_wide_fib(bad, N_COLS, 5)
+    bad = copy.deepcopy(proof)
+    bad.queried_values[1][7][3] = (bad.queried_values[1][7][3] + 1) % O.P
+    with pytest.raises(VerificationError):
+        verify_wide_fib(bad, N_COLS, 5)
+    bad = copy.deepcopy(proof)
+    w = list(bad.fri_first_layer["fri_witness"][0])
+    w[0] = (w[0] + 1) % O.P
+    bad.fri_first_layer["fri_witness"][0] = tuple(w)
+    with pytest.raises(VerificationError):
+        verify_wide_fib(bad, N_COLS, 5)
+
+
+def test_invalid_trace_is_refused():
+    # a trace that violates a constraint fails the prover's own OODS check
+    ops = CpuOps()
+    log_n = 4
+    trace = O.wide_fib_trace(m31_column(1, log_n), m31_column(2, log_n), N_COLS)
+    trace[50][3] = (int(trace[50][3]) + 1) % O.P
+    fp = pr.FriParams(n_queries=20)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=log_n + 1)
+    with pytest.raises(RuntimeError, match="constraints not satisfied"):
+        pr.prove_wide_fib(ops, ops.columns_from_host(trace), log_n, cfg, pr.Blake2sChannel(), ops.twiddles(log_n + 2))
+
+
+def test_proof_bytes_are_deterministic():
+    assert make_proof(4).to_bytes() == make_proof(4).to_bytes()
