@@ -46,6 +46,9 @@ def workload_name():
             f"lifted Blake2s Merkle over {N_COLS}-wide leaves, {FRI_LOG} FRI folds of a QM31 col of log {FRI_LOG}")
 
 
+LEAVES_TRAFFIC_BYTES = 4425.2e6
+
+
 def set_shape(n_cols: int, log_rows: int):
     global N_COLS, LOG_ROWS, LOG_EXT, FRI_LOG
     N_COLS, LOG_ROWS = n_cols, log_rows
@@ -190,6 +193,138 @@ class CommitStage:
         return self.layers[-1].cpu().numpy().astype("<i4").tobytes()
 
 
+class MixedCommit:
+    """Config 3 (batched mixed-size trace): 600 M31 columns with log sizes
+    10 + min(12, G), G geometric with mean ~6 (so the mean log size is ~16),
+    plus 120 QM31 interaction columns (480 M31 columns) with sizes drawn the
+    same way; blowup 2; lifted Blake2s commit of all 1,080 columns at the
+    largest extended size. Column contents are seeded uniform M31 (the commit's
+    cost does not depend on them)."""
+
+    def __init__(self, torch, seed: int = 7):
+        from proving_gb300 import _lib
+        from proving_gb300.backend import canonic_half_coset
+        from proving_gb300.synthetic import seeded_log_sizes
+        self.torch, self.L = torch, _lib
+        logs = list(seeded_log_sizes(seed, 600, 10, 22, 16.0))
+        inter = seeded_log_sizes(seed + 1, 120, 10, 22, 16.0)
+        logs += [int(l) for l in inter for _ in range(4)]
+        self.logs = [int(l) for l in logs]
+        self.max_ext = max(self.logs) + 1
+        dev = torch.device("cuda", torch.cuda.current_device())
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        P = (1 << 31) - 1
+        self.evals = [torch.randint(0, P, (1 << l,), generator=g, device=dev, dtype=torch.int64).to(torch.int32)
+                      for l in self.logs]
+        self.coeffs = [torch.empty_like(e) for e in self.evals]
+        self.ext = [torch.empty(1 << (l + 1), dtype=torch.int32, device=dev) for l in self.logs]
+        self.layers = torch.empty(((1 << (self.max_ext + 1)) - 1, 8), dtype=torch.int32, device=dev)
+        root = canonic_half_coset(self.max_ext + 1)
+        self.tw_log = root.log_size
+        self.tw = torch.empty(1 << self.tw_log, dtype=torch.int32, device=dev)
+        self.itw = torch.empty_like(self.tw)
+        _lib.call("cs_precompute_twiddles", root.initial_index, root.log_size, self.tw.data_ptr(),
+                  self.itw.data_ptr(), self.stream())
+        vp = ctypes.c_void_p
+        self.groups = {}
+        for i, l in enumerate(self.logs):
+            self.groups.setdefault(l, []).append(i)
+        self.tabs = {}
+        for l, idx in self.groups.items():
+            self.tabs[l] = ((vp * len(idx))(*[self.evals[i].data_ptr() for i in idx]),
+                            (vp * len(idx))(*[self.coeffs[i].data_ptr() for i in idx]),
+                            (vp * len(idx))(*[self.ext[i].data_ptr() for i in idx]))
+        self.all_ext = (vp * len(self.logs))(*[e.data_ptr() for e in self.ext])
+        self.all_logs = (ctypes.c_uint32 * len(self.logs))(*[l + 1 for l in self.logs])
+        self.elements = sum(1 << l for l in self.logs)
+        torch.cuda.synchronize()
+
+    def stream(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def step(self, plain: bool = False):
+        call, st, vp = self.L.call, self.stream(), ctypes.c_void_p
+        for l, idx in self.groups.items():
+            ev, co, ex = self.tabs[l]
+            if plain:
+                # one launch per column per stage
+                for k in range(len(idx)):
+                    call("cs_interpolate_columns_into", ctypes.byref(vp(ev[k])), ctypes.byref(vp(co[k])), 1, l,
+                         self.itw.data_ptr(), self.tw_log, st)
+                    call("cs_evaluate_columns", ctypes.byref(vp(co[k])), ctypes.byref(vp(ex[k])), 1, l, l + 1,
+                         self.tw.data_ptr(), self.tw_log, st)
+            else:
+                call("cs_interpolate_columns_into", ev, co, len(idx), l, self.itw.data_ptr(), self.tw_log, st)
+                call("cs_evaluate_columns", co, ex, len(idx), l, l + 1, self.tw.data_ptr(), self.tw_log, st)
+        call("cs_merkle_commit", self.all_ext, self.all_logs, len(self.logs), self.max_ext, self.layers.data_ptr(), st)
+
+
+def time_steps(torch, fn, steps: int, warmup: int):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def batched_vs_plain(torch, cs, steps: int = 5, warmup: int = 2):
+    """The BASELINE comparison: batched launches (one per stage and size) and the
+    same captured in a CUDA graph, against plain one-launch-per-column stages."""
+    out = {}
+    plain_ms = time_steps(torch, lambda: plain_commit_step(cs), steps, warmup)
+    batched_ms = time_steps(torch, cs.step, steps, warmup)
+    out["commit_stage"] = {"plain_ms": round(plain_ms, 4), "batched_ms": round(batched_ms, 4),
+                           "batched_speedup": round(plain_ms / batched_ms, 3)}
+    mixed = MixedCommit(torch)
+    m_plain = time_steps(torch, lambda: mixed.step(plain=True), steps, warmup)
+    m_batched = time_steps(torch, mixed.step, steps, warmup)
+    graph = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        mixed.step()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=s):
+            mixed.step()
+    torch.cuda.current_stream().wait_stream(s)
+    m_graph = time_steps(torch, graph.replay, steps, warmup)
+    out["mixed_commit"] = {
+        "workload": "600 M31 + 120 QM31 (480 M31) columns, log sizes 10..22 geometric (mean ~16), blowup 2, "
+                    "lifted Blake2s commit",
+        "columns": len(mixed.logs), "distinct_sizes": len(mixed.groups), "trace_elements": mixed.elements,
+        "plain_ms": round(m_plain, 4), "batched_ms": round(m_batched, 4), "graph_ms": round(m_graph, 4),
+        "plain_commits_per_s": round(1e3 / m_plain, 3), "batched_commits_per_s": round(1e3 / m_batched, 3),
+        "graph_commits_per_s": round(1e3 / m_graph, 3),
+        "batched_speedup": round(m_plain / m_batched, 3), "graph_speedup": round(m_plain / m_graph, 3)}
+    del mixed
+    return out
+
+
+def plain_commit_step(cs):
+    """Config 2 with one launch per column for interpolate and evaluate."""
+    call, st, vp = cs.L.call, cs.stream(), ctypes.c_void_p
+    for k in range(N_COLS):
+        call("cs_interpolate_columns_into", ctypes.byref(vp(cs.t_evals[k])), ctypes.byref(vp(cs.t_coeffs[k])), 1,
+             LOG_ROWS, cs.itw.data_ptr(), cs.tw_log, st)
+    for k in range(N_COLS):
+        call("cs_evaluate_columns", ctypes.byref(vp(cs.t_coeffs[k])), ctypes.byref(vp(cs.t_ext[k])), 1, LOG_ROWS,
+             LOG_EXT, cs.tw.data_ptr(), cs.tw_log, st)
+    call("cs_merkle_build_leaves", cs.t_ext, cs.logs, N_COLS, LOG_EXT, cs.layer_ptr[0], st)
+    for k in range(LOG_EXT, 0, -1):
+        call("cs_merkle_build_next_layer", cs.layer_ptr[LOG_EXT - k], k - 1, cs.layer_ptr[LOG_EXT - k + 1], st)
+    call("cs_fold_circle_into_line", cs.fri_tabs[0], FRI_LOG, cs.alpha_tabs[0], cs.fri_tabs[1], cs.itw.data_ptr(),
+         cs.tw_log, st)
+    for j in range(1, FRI_LOG):
+        call("cs_fold_line", cs.fri_tabs[j], FRI_LOG - j, cs.alpha_tabs[j], cs.fri_tabs[j + 1], cs.itw.data_ptr(),
+             cs.tw_log, st)
+
+
 def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: int = 100):
     """Full Wide-Fibonacci proves (config 1 shape: 100 columns x 2^14 rows, blowup 2,
     70 queries, pow 10) through the restated prover on the CUDA backend; the
@@ -214,6 +349,21 @@ def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: in
         if k >= 2:
             lat.append((time.perf_counter() - t0) * 1e3)
     return lat
+
+
+def serving_leg(n_requests: int = 24, rate_per_s: float = 40.0):
+    """Config 5 (Wide-Fibonacci only): a seeded Poisson stream of proofs with
+    log_n_rows uniform in [12, 20], served with 4 concurrent workers and with
+    one request at a time (plain)."""
+    from proving_gb300 import serving
+    out = {"workload": f"{n_requests} Wide-Fibonacci proofs (100 cols), log_n_rows uniform in [12, 20], Poisson "
+                       f"arrivals at {rate_per_s}/s; Poseidon2 requests not included"}
+    for name, workers in (("plain", 1), ("served", 4)):
+        reqs = serving.poisson_requests(n_requests, rate_per_s, 12, 20, seed=5)
+        done, wall = serving.run_stream(workers, reqs, max_log=20)
+        out[name] = serving.summarize(done, wall)
+    out["served_speedup"] = round(out["served"]["proofs_per_s"] / out["plain"]["proofs_per_s"], 3)
+    return out
 
 
 def run_gpu(args):
@@ -310,6 +460,8 @@ def run_gpu(args):
     e2e_value = world * args.steps / (float(t.item()) / 1e3)
 
     wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
+    bvp = batched_vs_plain(torch, cs) if not args.skip_plain else None
+    serving_res = serving_leg() if not args.skip_serving else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -320,10 +472,9 @@ def run_gpu(args):
     leaf_bytes = N_COLS * (1 << LOG_EXT) * 4 + (1 << LOG_EXT) * 32
     achieved = leaf_bytes / (leaf_ms / 1e3) / 1e9
     leaf_comp = (1 << LOG_EXT) * ((N_COLS * 4 + 63) // 64)
-    traffic = None
-    tr_file = ROOT / "profiles" / "traffic.json"
-    if tr_file.exists():
-        traffic = json.loads(tr_file.read_text()).get("merkle_leaves_kernel_bytes_per_launch")
+    # DRAM bytes (read + write) of one merkle_leaves_kernel launch on this workload, from the
+    # ncu launch list recorded in profiles/launch_list_commit_stage_256x2^20.md
+    traffic = LEAVES_TRAFFIC_BYTES if (N_COLS, LOG_EXT) == (256, 22) else None
     cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
     ff = lambda x: float(f"{x:.6g}")
     res = {
@@ -351,6 +502,8 @@ def run_gpu(args):
                             "proofs_per_s": ff(1e3 / statistics.mean(wf_lat)),
                             "p50_ms": ff(float(np.percentile(wf_lat, 50))),
                             "p99_ms": ff(float(np.percentile(wf_lat, 99)))} if wf_lat else None),
+        "batched_vs_plain": bvp,
+        "serving": serving_res,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
@@ -444,6 +597,8 @@ def main():
     ap.add_argument("--log-rows", type=int, default=LOG_ROWS, help="log2 rows per trace column")
     ap.add_argument("--skip-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--skip-prove", action="store_true", help="skip the Wide-Fibonacci full-prove latency leg")
+    ap.add_argument("--skip-plain", action="store_true", help="skip the batched-vs-plain comparison legs")
+    ap.add_argument("--skip-serving", action="store_true", help="skip the proof-service leg")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
     if args.impl == "reference":

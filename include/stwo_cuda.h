@@ -276,6 +276,17 @@ cs_status cs_wide_fib_composition(const uint32_t *const *h_cols, uint32_t n_cols
 cs_status cs_wide_fib_trace(const uint32_t *d_a, const uint32_t *d_b, uint32_t log_n, uint32_t n_cols,
                             uint32_t *const *h_cols, cs_stream stream);
 
+/* LogUp interaction column on the device: the last column of
+   LogupTraceGenerator (crates/constraint-framework/src/prover/logup.rs:50-130)
+   with numerator 1 and denominator z - v_i for the M31 column d_values
+   (2^log_size values, bit-reversed circle-domain order, log_size >= 10):
+   claimed_sum = sum_i 1/(z - v_i) (returned on the host, synchronous), then
+   the shifted fractions' inclusive prefix sum in coset order
+   (inclusive_prefix_sum, crates/stwo/src/prover/backend/simd/prefix_sum.rs:20)
+   into the QM31 column h_out. Uses stream-ordered device scratch. */
+cs_status cs_logup_running_sum(const uint32_t *d_values, uint32_t log_size, const uint32_t z[4], uint32_t *const h_out[4],
+                               uint32_t claimed_sum_out[4], cs_stream stream);
+
 /* -------------------------------------------------------- proof of work */
 
 /* GrindOps<Blake2sChannel>::grind (crates/stwo/src/core/proof_of_work.rs:10-14;

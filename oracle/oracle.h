@@ -78,6 +78,8 @@ void orc_random_point_from_t(const uint32_t t[4], uint32_t px[4], uint32_t py[4]
 void orc_wide_fib_composition(const uint32_t **cols, uint32_t n_cols, uint32_t eval_log, uint32_t trace_log,
                               const uint32_t *rc, uint32_t *const out[4]);
 void orc_wide_fib_trace(const uint32_t *a0, const uint32_t *b0, uint32_t log_n, uint32_t n_cols, uint32_t **cols);
+void orc_logup_running_sum(const uint32_t *values, uint32_t log_n, const uint32_t z[4], uint32_t *const out[4],
+                           uint32_t claimed_out[4]);
 
 #ifdef __cplusplus
 }

@@ -451,3 +451,12 @@ def wide_fib_composition(cols, eval_log: int, trace_log: int, rc, out=None):
     lib().orc_wide_fib_composition(_ptr_array(cols), ctypes.c_uint32(len(cols)), ctypes.c_uint32(eval_log),
                                    ctypes.c_uint32(trace_log), _p(r), _ptr_array(out))
     return out
+
+
+def logup_running_sum(values, z):
+    v, zz = _u32(values), _u32(z)
+    n = v.size
+    out = [np.zeros(n, np.uint32) for _ in range(4)]
+    claimed = np.zeros(4, np.uint32)
+    lib().orc_logup_running_sum(_p(v), ctypes.c_uint32(n.bit_length() - 1), _p(zz), _ptr_array(out), _p(claimed))
+    return out, claimed

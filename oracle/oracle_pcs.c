@@ -269,3 +269,37 @@ void orc_wide_fib_trace(const uint32_t *a0, const uint32_t *b0, uint32_t log_n, 
         }
     }
 }
+
+/* ------------------------------------------------------------------ LogUp */
+
+/*
+ * One LogUp interaction column finalized as the last column
+ * (LogupTraceGenerator::col_from_iter + finalize_last,
+ * crates/constraint-framework/src/prover/logup.rs:50-130): fractions
+ * 1 / (z - v_i), claimed_sum = sum of them, each shifted by claimed_sum / n,
+ * then inclusive_prefix_sum in coset order
+ * (inclusive_prefix_sum_slow, crates/stwo/src/prover/backend/simd/prefix_sum.rs:132-149,
+ * coset_order_to_circle_domain_order, crates/stwo/src/core/utils.rs:177-188).
+ * values and out are in bit-reversed circle-domain order.
+ */
+void orc_logup_running_sum(const uint32_t *values, uint32_t log_n, const uint32_t z_w[4], uint32_t *const out[4],
+                           uint32_t claimed_out[4]) {
+    uint64_t n = 1ull << log_n;
+    qm31 z = qm31_from_words(z_w);
+    qm31 *f = (qm31 *)malloc(sizeof(qm31) * n);
+    qm31 claimed = qm31_from_m31(0);
+    for (uint64_t i = 0; i < n; i++) {
+        f[i] = qm31_inv(qm31_sub(z, qm31_from_m31(values[i])));
+        claimed = qm31_add(claimed, f[i]);
+    }
+    qm31_to_words(claimed, claimed_out);
+    qm31 shift = qm31_mul_m31(claimed, m31_inv((m31)(n % M31_P)));
+    qm31 acc = qm31_from_m31(0);
+    for (uint64_t k = 0; k < n; k++) {
+        uint64_t c = (k & 1) ? n / 2 + (n - 1 - k) / 2 : k / 2;  /* circle-domain index of coset index k */
+        uint64_t p = bit_reverse_index((uint32_t)c, log_n);
+        acc = qm31_add(acc, qm31_sub(f[p], shift));
+        soa_set(out, p, acc);
+    }
+    free(f);
+}

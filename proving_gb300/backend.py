@@ -363,6 +363,15 @@ class CudaBackend:
                   len(accum).bit_length() - 1, trace_log, r.ctypes.data,
                   _ptr_table([c.data for c in accum.columns]), _stream())
 
+    @staticmethod
+    def logup_running_sum(values: BaseColumn, z):
+        """LogUp interaction column (last-column finalization) for fractions 1 / (z - v)."""
+        out = SecureColumnByCoords.uninitialized(len(values))
+        claimed = (ctypes.c_uint32 * 4)()
+        _lib.call("cs_logup_running_sum", _ptr(values.data), values.log_size, _u32_table(z),
+                  _ptr_table([c.data for c in out.columns]), claimed, _stream())
+        return out, np.array(list(claimed), np.uint32)
+
     # GrindOps -----------------------------------------------------------------
     @staticmethod
     def grind(digest: bytes, pow_bits: int, max_nonce: int = 1 << 48) -> int:

@@ -37,3 +37,14 @@ def test_trace_and_composition(B, n_cols, log_n):
     B.wide_fib_composition(ev, log_n, rc, acc)
     want = O.wide_fib_composition(ev_o, log_n + 1, log_n, rc)
     assert all(np.array_equal(g, w) for g, w in zip(acc.to_cpu(), want))
+
+
+@pytest.mark.parametrize("log_n", [10, 13, 16])
+def test_logup_running_sum(B, log_n):
+    from proving_gb300.backend import BaseColumn
+    v = m31_column(log_n + 40, log_n)
+    z = seeded_qm31(log_n)
+    got, claimed = B.logup_running_sum(BaseColumn.from_cpu(v), z)
+    want, wclaimed = O.logup_running_sum(v, z)
+    assert list(claimed) == list(wclaimed)
+    assert all(np.array_equal(g, w) for g, w in zip(got.to_cpu(), want))

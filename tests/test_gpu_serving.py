@@ -1,0 +1,39 @@
+"""The proof service: requests of different sizes proved concurrently on
+separate streams give the same proof bytes as each request proved alone, and
+admission keeps the in-flight HBM estimate within the budget."""
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from proving_gb300 import serving  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from proving_gb300 import build
+    build.build()
+
+
+def test_results_alone_equal_results_in_the_mix():
+    sizes = [8, 11, 9, 12, 8, 10]
+    reqs = [serving.ProofRequest(i, s, 1000 + 7 * i) for i, s in enumerate(sizes)]
+    mixed, _ = serving.run_stream(4, [(0.0, r) for r in reqs], max_log=12)
+    assert all(r.error is None for r in mixed)
+    alone_reqs = [serving.ProofRequest(i, s, 1000 + 7 * i) for i, s in enumerate(sizes)]
+    alone, _ = serving.run_stream(1, [(0.0, r) for r in alone_reqs], max_log=12)
+    by_id = {r.request_id: r.proof.to_bytes() for r in alone}
+    for r in mixed:
+        assert r.proof.to_bytes() == by_id[r.request_id]
+
+
+def test_admission_respects_the_budget():
+    # a budget that fits one size-12 proof at a time still finishes every request
+    budget = serving.hbm_estimate(12) + serving.hbm_estimate(8) // 2
+    reqs = [serving.ProofRequest(i, 12, 50 + i) for i in range(3)]
+    done, _ = serving.run_stream(3, [(0.0, r) for r in reqs], hbm_budget=budget, max_log=12)
+    assert len(done) == 3 and all(r.error is None for r in done)
+    # admitted one after another: each admission is after the previous completion
+    done.sort(key=lambda r: r.admitted)
+    for prev, nxt in zip(done, done[1:]):
+        assert nxt.admitted >= prev.done - 1e-3

@@ -87,3 +87,22 @@ def test_extract_subdomain_twiddles_matches_direct():
     init = O.canonic_half_coset_initial_index(committed)
     direct, _ = O.precompute_twiddles(init, sub - 1)
     assert np.array_equal(extracted[:-1], direct[:-1])
+
+
+def test_logup_running_sum_ends_at_zero_and_steps_by_fractions():
+    # the shifted running sum ends at 0 and its coset-order differences are the
+    # fractions minus claimed/n (crates/constraint-framework/src/prover/logup.rs:96-130)
+    log_n, n = 6, 64
+    v = m31_column(5, log_n)
+    z = seeded_qm31(6)
+    out, claimed = O.logup_running_sum(v, z)
+    br = O.bit_reverse(np.arange(n))
+    pos = [int(br[(k // 2) if k % 2 == 0 else n // 2 + (n - 1 - k) // 2]) for k in range(n)]
+    assert [int(o[pos[-1]]) for o in out] == [0, 0, 0, 0]
+    shift = O.qm31_mul(claimed, [pow(n, P - 2, P), 0, 0, 0])
+    for k in range(1, n):
+        cur = np.array([o[pos[k]] for o in out], np.int64)
+        prev = np.array([o[pos[k - 1]] for o in out], np.int64)
+        frac = O.qm31_inv([(int(z[0]) - int(v[pos[k]])) % P, z[1], z[2], z[3]])
+        want = (frac.astype(np.int64) - shift.astype(np.int64)) % P
+        assert list((cur - prev) % P) == list(want)
