@@ -287,6 +287,20 @@ cs_status cs_wide_fib_trace(const uint32_t *d_a, const uint32_t *d_b, uint32_t l
 cs_status cs_logup_running_sum(const uint32_t *d_values, uint32_t log_size, const uint32_t z[4], uint32_t *const h_out[4],
                                uint32_t claimed_sum_out[4], cs_stream stream);
 
+/* ------------------------------------------------------- decommitment */
+
+/* Batched reads for decommitment. Replaces the element-wise Column::at reads
+   of MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:97-162)
+   and compute_decommitment_positions_and_witness_evals
+   (crates/stwo/src/prover/fri.rs:408-438): h_out[k] = h_table[h_slot[k]][h_index[k]]
+   for k < n, where h_table holds n_table device pointers to u32 words (column
+   data, or Merkle layers as 8 words per digest) of h_lengths[t] words each.
+   Every slot and index is checked on the host (CS_ERR_INVALID_ARG, nothing
+   read). One upload, one launch, one copy back; synchronous on `stream`. */
+cs_status cs_gather_u32(const uint32_t *const *h_table, const uint64_t *h_lengths, uint32_t n_table,
+                        const uint32_t *h_slot, const uint32_t *h_index, uint32_t n, uint32_t *h_out,
+                        cs_stream stream);
+
 /* -------------------------------------------------------- proof of work */
 
 /* GrindOps<Blake2sChannel>::grind (crates/stwo/src/core/proof_of_work.rs:10-14;

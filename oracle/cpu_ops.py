@@ -81,6 +81,22 @@ class CpuOps:
     def secure_columns(self, col):
         return [Col(c) for c in col.c]
 
+    def secure_coords(self, col):
+        return [Col(c) for c in col.c]
+
+    def gather_many(self, items):
+        """Column values ("col", col, idx) and Merkle digests ("dig", tree, layer_log, nodes),
+        the latter as (n, 8) little-endian words."""
+        out = []
+        for it in items:
+            if it[0] == "col":
+                out.append(it[1].v[np.asarray(it[2], dtype=np.int64)])
+            else:
+                tree, k, nodes = it[1], it[2], it[3]
+                lay = tree.layers[tree.height - k]
+                out.append(np.ascontiguousarray(lay[np.asarray(nodes, dtype=np.int64)]).view("<u4").reshape(-1, 8))
+        return out
+
     def gather_secure(self, col, idx):
         ix = np.asarray(idx, dtype=np.int64)
         vals = [c[ix] for c in col.c]

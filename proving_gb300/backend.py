@@ -372,6 +372,22 @@ class CudaBackend:
                   _ptr_table([c.data for c in out.columns]), claimed, _stream())
         return out, np.array(list(claimed), np.uint32)
 
+    # Decommitment -------------------------------------------------------------
+    @staticmethod
+    def gather_words(tensors, slots: np.ndarray, indices: np.ndarray) -> np.ndarray:
+        """Word k = tensors[slots[k]].flatten()[indices[k]] for contiguous int32 device tensors, read
+        in one batched call (cs_gather_u32): the element-wise Column::at reads of
+        MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:97-162)."""
+        slots = np.ascontiguousarray(slots, np.uint32)
+        indices = np.ascontiguousarray(indices, np.uint32)
+        out = np.empty(slots.size, np.uint32)
+        if slots.size == 0:
+            return out
+        lengths = (ctypes.c_uint64 * len(tensors))(*[t.numel() for t in tensors])
+        _lib.call("cs_gather_u32", _ptr_table(tensors), lengths, len(tensors), slots.ctypes.data_as(ctypes.c_void_p),
+                  indices.ctypes.data_as(ctypes.c_void_p), slots.size, out.ctypes.data_as(ctypes.c_void_p), _stream())
+        return out
+
     # GrindOps -----------------------------------------------------------------
     @staticmethod
     def grind(digest: bytes, pow_bits: int, max_nonce: int = 1 << 48) -> int:

@@ -92,10 +92,10 @@ __device__ __forceinline__ uint32_t lin(uint32_t m, uint32_t e, int T, uint32_t 
 }
 
 // CNT consecutive twiddles of FFT layer `layer`, starting at twiddle index h0.
-template <int CNT>
+template <int CNT, bool CIRCLE>
 __device__ __forceinline__ void load_twiddles(const FftPass& p, uint32_t layer, uint32_t h0, uint32_t* w) {
   const uint32_t tw_len = 1u << p.tw_log;
-  if (layer == 0) {
+  if (CIRCLE) {
     // circle layer: [y, -y, -x, x] of the line-layer-1 pair (cpu/circle.rs:306-323)
     const uint32_t* lt1 = p.tw + (tw_len - (1u << (p.tw_dom - 1)));
     if (CNT >= 16) {
@@ -141,33 +141,46 @@ __device__ __forceinline__ void load_twiddles(const FftPass& p, uint32_t layer, 
   }
 }
 
+
 // R local layers [D0, D0 + R) on the 2^R register values v, whose local index
 // j maps to global index g0 + (j << (D0 + lo)). INV runs the layers upward
-// with ibutterflies (interpolate), otherwise downward with butterflies. Step K
-// of the stage handles local layer t; its 2^(R-1-t) twiddles are consecutive.
-template <bool INV, int R, int D0, int K>
-struct RegStage {
-  static __device__ __forceinline__ void run(const FftPass& p, uint32_t g0, uint32_t* v) {
+// with ibutterflies (interpolate), otherwise downward with butterflies. Local
+// layer t needs 2^(R-1-t) consecutive twiddles. Only contiguous tiles
+// (OUTER, lo = 0) contain the circle layer: local layer 0 of stage A.
+template <int R>
+__host__ __device__ constexpr int tw_off(int t) {
+  return (1 << R) - (1 << (R - t));
+}
+
+template <bool INV, bool OUTER, int R, int D0, int K>
+struct Layers {
+  static __device__ __forceinline__ void run(const FftPass& p, uint32_t g0, uint32_t* v, uint32_t* w) {
     constexpr int t = INV ? K : (R - 1 - K);
-    constexpr int CNT = 1 << (R - 1 - t);
-    const uint32_t layer = p.lo + D0 + t;
-    uint32_t w[CNT];
-    load_twiddles<CNT>(p, layer, g0 >> (layer + 1), w);
+    {
+      const uint32_t layer = p.lo + D0 + t;
+      load_twiddles<(1 << (R - 1 - t)), OUTER && D0 == 0 && t == 0>(p, layer, g0 >> (layer + 1), w + tw_off<R>(t));
+    }
 #pragma unroll
     for (int j = 0; j < (1 << R); j++) {
       if (j & (1 << t)) continue;
       if (INV)
-        ibfly(v[j], v[j | (1 << t)], w[j >> (t + 1)]);
+        ibfly(v[j], v[j | (1 << t)], w[tw_off<R>(t) + (j >> (t + 1))]);
       else
-        bfly(v[j], v[j | (1 << t)], w[j >> (t + 1)]);
+        bfly(v[j], v[j | (1 << t)], w[tw_off<R>(t) + (j >> (t + 1))]);
     }
-    RegStage<INV, R, D0, K + 1>::run(p, g0, v);
+    Layers<INV, OUTER, R, D0, K + 1>::run(p, g0, v, w);
   }
 };
-template <bool INV, int R, int D0>
-struct RegStage<INV, R, D0, R> {
-  static __device__ __forceinline__ void run(const FftPass&, uint32_t, uint32_t*) {}
+template <bool INV, bool OUTER, int R, int D0>
+struct Layers<INV, OUTER, R, D0, R> {
+  static __device__ __forceinline__ void run(const FftPass&, uint32_t, uint32_t*, uint32_t*) {}
 };
+
+template <bool INV, bool OUTER, int R, int D0>
+__device__ __forceinline__ void reg_stage(const FftPass& p, uint32_t g0, uint32_t* v) {
+  uint32_t w[1 << R];  // 2^R - 1 used
+  Layers<INV, OUTER, R, D0, 0>::run(p, g0, v, w);
+}
 
 // One pass over layers [lo, lo + T) of a tile of 2^T x 2^EB values: stage A
 // runs local layers [0, TA) on groups m = (ma << TA) | j, stage B runs
@@ -176,11 +189,11 @@ template <int T, bool OUTER>
 constexpr int tile_max_threads() {
   return OUTER ? 256 : (1 << (T / 2 + 3));
 }
-// Blocks per SM the register budget is sized for: contiguous tiles of up to
-// 10 layers fit three without spills, the others two.
+// Blocks per SM the register budget is sized for: tiles of up to 10 layers
+// fit three without spills, larger ones two.
 template <int T, bool OUTER>
 constexpr int tile_min_blocks() {
-  return (OUTER && T <= 10) ? 3 : 2;
+  return T <= 10 ? 3 : 2;
 }
 
 template <bool INV, int T, bool OUTER>
@@ -189,7 +202,6 @@ __global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), tile_min_blocks<
   constexpr uint32_t M = 1u << T;
   extern __shared__ uint32_t s[];
   const uint32_t EB = OUTER ? p.c : 3u;  // inner tiles always hold 8 groups
-  const uint32_t N = M << EB;
   uint32_t* dst = batch.dst[blockIdx.y];
   const uint32_t* src = batch.src[blockIdx.y];
   Tile tl;
@@ -201,10 +213,23 @@ __global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), tile_min_blocks<
     tl.o = blockIdx.x & ((1u << outer_bits) - 1);
     tl.ib = blockIdx.x >> outer_bits;
   }
-  for (uint32_t L = threadIdx.x; L < N; L += blockDim.x) {
-    const uint32_t m = OUTER ? (L & (M - 1)) : (L >> EB);
-    const uint32_t e = OUTER ? (L >> T) : (L & ((1u << EB) - 1));
-    s[pad<OUTER>(L)] = __ldg(src + (tile_gidx(p, tl, m, e) & p.src_mask));
+  // every thread moves exactly 2^TB words (the tile holds 2^(T + EB) words, the block has
+  // 2^(TA + EB) threads); up to 32 of a thread's loads are in flight before its first store
+  {
+    constexpr int G = (1 << TB) < 32 ? (1 << TB) : 32;
+#pragma unroll 1
+    for (int k0 = 0; k0 < (1 << TB); k0 += G) {
+      uint32_t r[G];
+#pragma unroll
+      for (int k = 0; k < G; k++) {
+        const uint32_t L = threadIdx.x + (k0 + k) * blockDim.x;
+        const uint32_t m = OUTER ? (L & (M - 1)) : (L >> EB);
+        const uint32_t e = OUTER ? (L >> T) : (L & ((1u << EB) - 1));
+        r[k] = __ldg(src + (tile_gidx(p, tl, m, e) & p.src_mask));
+      }
+#pragma unroll
+      for (int k = 0; k < G; k++) s[pad<OUTER>(threadIdx.x + (k0 + k) * blockDim.x)] = r[k];
+    }
   }
   __syncthreads();
   const uint32_t t = threadIdx.x;
@@ -220,7 +245,7 @@ __global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), tile_min_blocks<
           uint32_t v[1 << TA];
 #pragma unroll
           for (int j = 0; j < (1 << TA); j++) v[j] = s[pad<OUTER>(lin<OUTER>(mbase | j, e, T, EB))];
-          RegStage<INV, TA, 0, 0>::run(p, tile_gidx(p, tl, mbase, e), v);
+          reg_stage<INV, OUTER, TA, 0>(p, tile_gidx(p, tl, mbase, e), v);
 #pragma unroll
           for (int j = 0; j < (1 << TA); j++) s[pad<OUTER>(lin<OUTER>(mbase | j, e, T, EB))] = v[j];
         }
@@ -231,18 +256,24 @@ __global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), tile_min_blocks<
       uint32_t v[1 << TB];
 #pragma unroll
       for (int j = 0; j < (1 << TB); j++) v[j] = s[pad<OUTER>(lin<OUTER>((j << TA) | mb, e, T, EB))];
-      RegStage<INV, TB, TA, 0>::run(p, tile_gidx(p, tl, mb, e), v);
+      reg_stage<INV, OUTER, TB, TA>(p, tile_gidx(p, tl, mb, e), v);
 #pragma unroll
       for (int j = 0; j < (1 << TB); j++) s[pad<OUTER>(lin<OUTER>((j << TA) | mb, e, T, EB))] = v[j];
     }
     __syncthreads();
   }
-  for (uint32_t L = threadIdx.x; L < N; L += blockDim.x) {
-    const uint32_t m = OUTER ? (L & (M - 1)) : (L >> EB);
-    const uint32_t e = OUTER ? (L >> T) : (L & ((1u << EB) - 1));
-    uint32_t v = s[pad<OUTER>(L)];
-    if (p.scale) v = m31_mul(v, p.scale);
-    dst[tile_gidx(p, tl, m, e)] = v;
+  // stores in groups of four, which keeps the register budget of three blocks per SM
+#pragma unroll 1
+  for (int k0 = 0; k0 < (1 << TB); k0 += 4) {
+#pragma unroll
+    for (int k = 0; k < ((1 << TB) < 4 ? (1 << TB) : 4); k++) {
+      const uint32_t L = threadIdx.x + (k0 + k) * blockDim.x;
+      const uint32_t m = OUTER ? (L & (M - 1)) : (L >> EB);
+      const uint32_t e = OUTER ? (L >> T) : (L & ((1u << EB) - 1));
+      uint32_t v = s[pad<OUTER>(L)];
+      if (p.scale) v = m31_mul(v, p.scale);
+      dst[tile_gidx(p, tl, m, e)] = v;
+    }
   }
 }
 
@@ -395,7 +426,10 @@ cs_status dispatch_tile(const FftBatch& b, uint32_t n_cols, const FftPass& p, cu
     case 9: return launch_tile<INV, 9, OUTER>(b, n_cols, p, st);
     case 10: return launch_tile<INV, 10, OUTER>(b, n_cols, p, st);
     case 11: return launch_tile<INV, 11, OUTER>(b, n_cols, p, st);
-    case 12: return launch_tile<INV, 12, OUTER>(b, n_cols, p, st);
+    case 12:
+      // plan_passes keeps strided passes at 11 layers or fewer
+      if constexpr (OUTER) return launch_tile<INV, 12, OUTER>(b, n_cols, p, st);
+      [[fallthrough]];
     default:
       set_error("fft: unsupported pass of %u layers", p.hi - p.lo);
       return CS_ERR_INVALID_ARG;

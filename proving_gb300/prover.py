@@ -250,67 +250,117 @@ def line_coeffs(py, value, alpha):
     return (qm_mul(alpha, a), qm_mul(alpha, b), qm_mul(alpha, c))
 
 
-# ------------------------------------------------------------ Merkle decommitment
+# ------------------------------------------------------------ decommitment reads
 
-def merkle_decommit(tree, query_positions, columns, ops):
-    """MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:97-162).
-    tree: ops Merkle handle; columns: the committed columns in commit order (may be empty)."""
-    L = tree.height
-    queried = []
-    for col in columns:
-        l = ops.log_size(col)
-        shift = L - l
-        idx = [((p >> (shift + 1)) << 1) + (p & 1) for p in query_positions]
-        queried.append([int(v) for v in ops.gather(col, idx)])
-    witness = []
+class Reads:
+    """Every device read a decommitment makes, collected first and performed in
+    one batched call (ops.gather_many): column values at positions and Merkle
+    digests at (layer, node). Handles index the results of `run`."""
+
+    def __init__(self):
+        self.items = []
+        self.out = None
+
+    def values(self, col, idx) -> int:
+        self.items.append(("col", col, list(idx)))
+        return len(self.items) - 1
+
+    def digests(self, tree, layer_log: int, nodes) -> int:
+        self.items.append(("dig", tree, layer_log, list(nodes)))
+        return len(self.items) - 1
+
+    def run(self, ops):
+        self.out = ops.gather_many(self.items)
+
+    def __getitem__(self, h: int):
+        return self.out[h]
+
+
+def merkle_witness_nodes(height: int, query_positions):
+    """The witness of MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:119-150)
+    as (layer log size, node) pairs in proof order: walking down from the
+    leaves, the sibling of every queried node whose sibling is not queried."""
+    nodes = []
     prev = sorted(set(query_positions))
-    for layer_log in range(L - 1, -1, -1):
-        # hashes of layer layer_log + 1 (the children)
-        need, cur = [], []
+    for layer_log in range(height - 1, -1, -1):
+        cur = []
         i = 0
         while i < len(prev):
             first = prev[i]
             if i + 1 < len(prev) and prev[i + 1] == first ^ 1:
                 i += 2
             else:
-                need.append(first ^ 1)
+                nodes.append((layer_log + 1, first ^ 1))
                 i += 1
             cur.append(first >> 1)
-        if need:
-            witness.extend(tree.hashes(layer_log + 1, need))
         prev = cur
-    return queried, witness
+    return nodes
+
+
+class MerkleDecommit:
+    """MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:97-162) in two
+    steps: `plan` registers the queried values (col[(pos >> (shift + 1) << 1) + (pos & 1)] for a
+    column of log size L - shift) and the witness digests with a Reads; `result` assembles them."""
+
+    def __init__(self, reads: Reads, tree, query_positions, columns, ops):
+        L = tree.height
+        self.value_handles = []
+        for col in columns:
+            shift = L - ops.log_size(col)
+            self.value_handles.append(reads.values(col, [((q >> (shift + 1)) << 1) + (q & 1)
+                                                         for q in query_positions]))
+        by_layer = {}
+        for layer_log, node in merkle_witness_nodes(L, query_positions):
+            by_layer.setdefault(layer_log, []).append(node)
+        # one read per layer, in proof order (layers descend from the leaves)
+        self.witness_handles = [reads.digests(tree, k, nodes) for k, nodes in by_layer.items()]
+        self.reads = reads
+
+    def result(self):
+        queried = [[int(v) for v in self.reads[h]] for h in self.value_handles]
+        witness = []
+        for h in self.witness_handles:
+            arr = self.reads[h]
+            witness.extend(arr[i].astype("<u4").tobytes() for i in range(arr.shape[0]))
+        return queried, witness
 
 
 # ------------------------------------------------------------ FRI
 
-def decommitment_positions_and_witness(column_values_at, query_positions, fold_step: int):
-    """compute_decommitment_positions_and_witness_evals (crates/stwo/src/prover/fri.rs:408-438).
-    column_values_at(positions) -> list of QM31 for those positions."""
-    groups, i = [], 0
-    while i < len(query_positions):
-        j = i
-        while j + 1 < len(query_positions) and query_positions[j + 1] >> fold_step == query_positions[i] >> fold_step:
-            j += 1
-        groups.append(query_positions[i:j + 1])
-        i = j + 1
-    positions = []
-    for g in groups:
-        start = (g[0] >> fold_step) << fold_step
-        positions.extend(range(start, start + (1 << fold_step)))
-    values = column_values_at(positions)
-    witness, k = [], 0
-    for g in groups:
-        qs = list(g)
-        start = (g[0] >> fold_step) << fold_step
+def decommitment_positions(query_positions, fold_step: int):
+    """compute_decommitment_positions_and_witness_evals (crates/stwo/src/prover/fri.rs:408-438)
+    without the values: the positions to open (every coset of 2^fold_step around a query) and,
+    per position, whether its value goes to the witness (it is not itself a query)."""
+    positions, is_witness = [], []
+    qset = set(query_positions)
+    seen = set()
+    for q in query_positions:
+        start = (q >> fold_step) << fold_step
+        if start in seen:
+            continue
+        seen.add(start)
         for pos in range(start, start + (1 << fold_step)):
-            v = values[k]
-            k += 1
-            if qs and qs[0] == pos:
-                qs.pop(0)
-            else:
-                witness.append(v)
-    return positions, witness
+            positions.append(pos)
+            is_witness.append(pos not in qset)
+    return positions, is_witness
+
+
+class FriLayerDecommit:
+    """One FRI layer's decommitment (FriLayerProver::decommit, crates/stwo/src/prover/fri.rs:380-406):
+    the witness values of the opened cosets and the Merkle witness of their positions."""
+
+    def __init__(self, reads: Reads, column, tree, query_positions, fold_step: int, ops):
+        self.positions, self.is_witness = decommitment_positions(query_positions, fold_step)
+        self.coord_handles = [reads.values(c, self.positions) for c in ops.secure_coords(column)]
+        self.merkle = MerkleDecommit(reads, tree, self.positions, [], ops)
+        self.reads = reads
+        self.tree = tree
+
+    def result(self):
+        coords = [self.reads[h] for h in self.coord_handles]
+        witness = [tuple(int(coords[k][i]) for k in range(4)) for i, w in enumerate(self.is_witness) if w]
+        _, dec = self.merkle.result()
+        return {"fri_witness": witness, "decommitment": dec, "commitment": self.tree.root}
 
 
 def fold_queries(positions, n_folds: int):
@@ -453,34 +503,36 @@ def prove_wide_fib(ops, trace, log_n_rows: int, config: PcsConfig, channel: Blak
     # --- FRI commit (fri.rs:113-226)
     fri = fri_commit(ops, channel, fp, quotients, lifting, twiddles)
 
-    # --- FRI decommit (fri.rs:229-283)
+    # --- FRI decommit (fri.rs:229-283) and tree decommitments (pcs/mod.rs:259-287): every value and
+    # digest the proof opens is read from the device in one batched call
     fri_pow = ops.grind(channel.digest, fp.pow_bits)
     channel.mix_u64(fri_pow)
     unsorted = channel.draw_queries(lifting, fp.n_queries)
     queries = sorted(set(unsorted))
-    first = fri["first"]
-    pos, wit = decommitment_positions_and_witness(lambda ps: ops.gather_secure(quotients, ps), queries, fp.fold_step)
-    _, dec = merkle_decommit(first["tree"], pos, [], ops)
-    proof = StarkProof(config=config)
-    proof.fri_first_layer = {"fri_witness": wit, "decommitment": dec, "commitment": first["tree"].root}
+    reads = Reads()
+    first = FriLayerDecommit(reads, quotients, fri["first"]["tree"], queries, fp.fold_step, ops)
+    inner = []
     layer_queries = fold_queries(queries, fp.fold_step)
     for layer in fri["inner"]:
-        pos, wit = decommitment_positions_and_witness(lambda ps, ev=layer["eval"]: ops.gather_secure(ev, ps),
-                                                      layer_queries, layer["fold_step"])
-        _, dec = merkle_decommit(layer["tree"], pos, [], ops)
-        proof.fri_inner_layers.append({"fri_witness": wit, "decommitment": dec, "commitment": layer["tree"].root})
+        inner.append(FriLayerDecommit(reads, layer["eval"], layer["tree"], layer_queries, layer["fold_step"], ops))
         layer_queries = fold_queries(layer_queries, layer["fold_step"])
+    trees = [MerkleDecommit(reads, tree, queries, cols, ops)
+             for tree, cols in ((trace_tree, trace_evals), (comp_tree, comp_evals))]
+    reads.run(ops)
+
+    proof = StarkProof(config=config)
+    proof.fri_first_layer = first.result()
+    proof.fri_inner_layers = [d.result() for d in inner]
     proof.fri_last_layer_poly = fri["last_poly"]
     proof.fri_proof_of_work = fri_pow
-
-    # --- tree decommitments (pcs/mod.rs:259-287); the empty preprocessed tree has height 0
+    # the empty preprocessed tree has height 0: no values, no witness
     proof.commitments = [pre_root, trace_tree.root, comp_tree.root]
     proof.oods_proof_of_work = oods_pow
     proof.sampled_values = sampled
     proof.decommitments = [[]]
     proof.queried_values = [[]]
-    for tree, cols in ((trace_tree, trace_evals), (comp_tree, comp_evals)):
-        qv, wit = merkle_decommit(tree, queries, cols, ops)
+    for d in trees:
+        qv, wit = d.result()
         proof.queried_values.append(qv)
         proof.decommitments.append(wit)
 
@@ -679,6 +731,38 @@ class GpuOps:
 
     def secure_columns(self, col):
         return col.columns
+
+    def secure_coords(self, col):
+        return col.columns
+
+    def gather_many(self, items):
+        """Column values ("col", col, idx) and Merkle digests ("dig", tree, layer_log, nodes), read in
+        one cs_gather_u32 call; digests come back as (n, 8) words."""
+        tensors, slot_of, slots, idx, sizes = [], {}, [], [], []
+        for it in items:
+            if it[0] == "col":
+                t = it[1].data
+                ix = np.asarray(it[2], dtype=np.int64)
+            else:
+                t = it[1].t.layer(it[2])
+                nodes = np.asarray(it[3], dtype=np.int64)
+                ix = (nodes[:, None] * 8 + np.arange(8)).reshape(-1)
+            key = (t.data_ptr(), t.numel())
+            if key not in slot_of:
+                slot_of[key] = len(tensors)
+                tensors.append(t)
+            slots.append(np.full(ix.size, slot_of[key], np.uint32))
+            idx.append(ix.astype(np.uint32))
+            sizes.append(ix.size)
+        if not items:
+            return []
+        words = self.B.gather_words(tensors, np.concatenate(slots), np.concatenate(idx))
+        out, off = [], 0
+        for it, n in zip(items, sizes):
+            w = words[off:off + n]
+            out.append(w if it[0] == "col" else w.reshape(-1, 8))
+            off += n
+        return out
 
     def gather_secure(self, col, idx):
         vals = [self.gather(c, idx) for c in col.columns]

@@ -81,3 +81,22 @@ def test_error_raises_in_python_mirror(lib):
     with pytest.raises(_lib.CudaBackendError) as e:
         _lib.call("cs_bit_reverse_m31", ctypes.c_void_p(0), 4, ctypes.c_void_p(0))
     assert "CS_ERR_INVALID_ARG" in str(e.value)
+
+
+def test_gather_checks_every_request_on_host(lib):
+    # slots and indices are validated against the table before any device work
+    INVALID = 1
+    null = ctypes.c_void_p(0)
+    table = (ctypes.c_void_p * 2)(1 << 20, 1 << 21)
+    lengths = (ctypes.c_uint64 * 2)(16, 4)
+    out = (ctypes.c_uint32 * 2)()
+    slot = (ctypes.c_uint32 * 2)(0, 2)
+    idx = (ctypes.c_uint32 * 2)(3, 0)
+    assert _status(lib, "cs_gather_u32", table, lengths, 2, slot, idx, 2, out, null) == INVALID
+    assert b"slot" in lib.cs_last_error()
+    slot = (ctypes.c_uint32 * 2)(0, 1)
+    idx = (ctypes.c_uint32 * 2)(15, 4)
+    assert _status(lib, "cs_gather_u32", table, lengths, 2, slot, idx, 2, out, null) == INVALID
+    assert b"word 4" in lib.cs_last_error()
+    # nothing to read: no device work at all
+    assert _status(lib, "cs_gather_u32", null, null, 0, null, null, 0, null, null) == 0

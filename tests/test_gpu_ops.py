@@ -221,3 +221,19 @@ def test_grind_gives_up(B):
     with pytest.raises(CudaBackendError) as e:
         B.grind(ch.digest, 32, max_nonce=1000)
     assert "TIMEOUT" in str(e.value)
+
+
+# ------------------------------------------------------------------ decommitment reads
+
+def test_gather_words_matches_indexing(B):
+    cols = [_col(m31_column(70 + k, 6 + k)) for k in range(3)]
+    digests = torch.arange(64 * 8, dtype=torch.int32, device="cuda").reshape(64, 8)
+    tensors = [c.data for c in cols] + [digests]
+    rng = np.random.default_rng(5)
+    slots = rng.integers(0, 4, 500).astype(np.uint32)
+    lens = [t.numel() for t in tensors]
+    idx = np.array([rng.integers(0, lens[s]) for s in slots], np.uint32)
+    got = B.gather_words(tensors, slots, idx)
+    host = [t.reshape(-1).cpu().numpy().view(np.uint32) for t in tensors]
+    want = np.array([host[s][i] for s, i in zip(slots, idx)], np.uint32)
+    assert np.array_equal(got, want)
