@@ -351,16 +351,71 @@ def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: in
     return lat
 
 
+def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
+    """Config 4: the Poseidon2 AIR at 8 permutations per row, 2^log_n_rows rows (1264 trace
+    columns), log_blowup_factor 1, 70 queries, pow 10, through prove_poseidon + prove_ex on the
+    CUDA backend (trace, interaction trace and constraint quotients on the device). The
+    reference's own prove of this AIR stops at its sanity check (lifted protocol, constraint
+    degree 5), so the proof is built with check=False. Reports the wall-clock latency and the
+    device time of the constraint-quotient kernel alone."""
+    from proving_gb300 import poseidon as ps
+    from proving_gb300 import prover as pr
+    from proving_gb300.backend import CudaBackend, SecureColumnByCoords
+    ops = pr.GpuOps()
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = ps.poseidon_pcs_config(log_n_rows + 3, fp)
+    tw = ops.twiddles(log_n_rows + ps.LOG_EXPAND + fp.log_blowup_factor)
+    lat = []
+    for k in range(n_proofs + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ps.prove_poseidon(ops, log_n_rows, cfg, pr.Blake2sChannel(), tw, check=False)
+        torch.cuda.synchronize()
+        if k >= 1:
+            lat.append((time.perf_counter() - t0) * 1e3)
+        torch.cuda.empty_cache()
+    # the constraint-quotient kernel alone on the evaluation domain CanonicCoset(log_n_rows + 2)
+    eval_log = log_n_rows + ps.LOG_EXPAND
+    trace = CudaBackend.poseidon_trace(log_n_rows)
+    lookup = [1, 2, 3, 4, 4, 3, 2, 1]
+    inter, claimed = CudaBackend.poseidon_interaction(trace, lookup)
+    coeffs = ops.interpolate_into(trace, tw)
+    del trace
+    t_eval = ops.evaluate(coeffs, eval_log, tw)
+    del coeffs
+    ops.interpolate(inter, tw)
+    i_eval = ops.evaluate(inter, eval_log, tw)
+    rc = np.random.default_rng(1).integers(0, (1 << 31) - 1, (ps.N_CONSTRAINTS, 4)).astype(np.uint32)
+    acc = SecureColumnByCoords.zeros(1 << eval_log)
+    ms = time_steps(torch, lambda: CudaBackend.poseidon_composition(t_eval, i_eval, log_n_rows, lookup, claimed, rc,
+                                                                     acc), 3, 1)
+    read_bytes = 4 * (ps.N_COLUMNS + ps.N_INTERACTION_COLUMNS) * (1 << eval_log) + 4 * 4 * (1 << eval_log)
+    out = {"workload": f"Poseidon2 AIR, 8 permutations/row, 2^{log_n_rows} rows (2^{log_n_rows + 3} permutations), "
+                       "1264 trace + 32 interaction columns, log_blowup 1, 70 queries, pow 10; prove_poseidon + "
+                       "prove_ex (the reference's sanity check fails for this AIR; proof built without it)",
+           "proofs_per_s": round(1e3 / statistics.median(lat), 3), "p50_ms": round(statistics.median(lat), 3),
+           "max_ms": round(max(lat), 3),
+           "composition_kernel": {"eval_rows": 1 << eval_log, "ms": round(ms, 4),
+                                  "gb_per_s": round(read_bytes / ms / 1e6, 1),
+                                  "rows_per_s": round((1 << eval_log) / ms * 1e3, 1)}}
+    del t_eval, i_eval, acc
+    torch.cuda.empty_cache()
+    return out
+
+
 def serving_leg(n_requests: int = 24, rate_per_s: float = 40.0):
     """Config 5 (Wide-Fibonacci only): a seeded Poisson stream of proofs with
     log_n_rows uniform in [12, 20], served with 4 concurrent workers and with
     one request at a time (plain)."""
     from proving_gb300 import serving
     out = {"workload": f"{n_requests} Wide-Fibonacci proofs (100 cols), log_n_rows uniform in [12, 20], Poisson "
-                       f"arrivals at {rate_per_s}/s; Poseidon2 requests not included"}
-    for name, workers in (("plain", 1), ("served", 4)):
+                       f"arrivals at {rate_per_s}/s; Poseidon2 requests not included",
+           "arms": "plain: one request at a time, one launch per column per stage; batched_serial: one request at "
+                   "a time, batched stage launches; served: 4 concurrent requests on separate streams with HBM-budget "
+                   "admission, batched stage launches"}
+    for name, workers, plain in (("plain", 1, True), ("batched_serial", 1, False), ("served", 4, False)):
         reqs = serving.poisson_requests(n_requests, rate_per_s, 12, 20, seed=5)
-        done, wall = serving.run_stream(workers, reqs, max_log=20)
+        done, wall = serving.run_stream(workers, reqs, max_log=20, plain=plain)
         out[name] = serving.summarize(done, wall)
     out["served_speedup"] = round(out["served"]["proofs_per_s"] / out["plain"]["proofs_per_s"], 3)
     return out
@@ -462,6 +517,7 @@ def run_gpu(args):
     wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
     bvp = batched_vs_plain(torch, cs) if not args.skip_plain else None
     serving_res = serving_leg() if not args.skip_serving else None
+    poseidon_res = poseidon_prove_leg(torch) if not args.skip_poseidon else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -504,6 +560,7 @@ def run_gpu(args):
                             "p99_ms": ff(float(np.percentile(wf_lat, 99)))} if wf_lat else None),
         "batched_vs_plain": bvp,
         "serving": serving_res,
+        "poseidon_prove": poseidon_res,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
@@ -599,6 +656,7 @@ def main():
     ap.add_argument("--skip-prove", action="store_true", help="skip the Wide-Fibonacci full-prove latency leg")
     ap.add_argument("--skip-plain", action="store_true", help="skip the batched-vs-plain comparison legs")
     ap.add_argument("--skip-serving", action="store_true", help="skip the proof-service leg")
+    ap.add_argument("--skip-poseidon", action="store_true", help="skip the Poseidon2 prove leg")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
     if args.impl == "reference":

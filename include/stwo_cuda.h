@@ -287,6 +287,41 @@ cs_status cs_wide_fib_trace(const uint32_t *d_a, const uint32_t *d_b, uint32_t l
 cs_status cs_logup_running_sum(const uint32_t *d_values, uint32_t log_size, const uint32_t z[4], uint32_t *const h_out[4],
                                uint32_t claimed_sum_out[4], cs_stream stream);
 
+/* ------------------------------------------------------- AIR: Poseidon2 */
+
+/* The Poseidon2 AIR of crates/examples/src/poseidon/mod.rs (state width 16,
+   4 + 4 full rounds, 14 partial rounds, x^5, round constants 1234, 8
+   instances of 158 columns per row: 1264 trace columns, 32 interaction
+   columns, 1144 constraints). Columns are 2^log_n words in bit-reversed
+   circle-domain order; tables hold device pointers. */
+
+/* gen_trace (mod.rs:195-275) on the device: instance k of row r starts from
+   state word i = r + i + k. h_cols: 1264 columns of 2^log_n words. */
+cs_status cs_poseidon_trace(uint32_t log_n, uint32_t *const *h_cols, cs_stream stream);
+
+/* gen_interaction_trace (mod.rs:277-303) with LogupTraceGenerator
+   (crates/constraint-framework/src/prover/logup.rs:55-130): for instance k the
+   fraction 1/combine(initial) - 1/combine(final), combine(v) = sum_i alpha^i v_i - z
+   (crates/constraint-framework/src/logup.rs:80-93); QM31 column k < 7 (h_out[4k .. 4k+4])
+   holds the row sum over instances 0..k, column 7 the row totals minus
+   claimed_sum / 2^log_n, inclusive-prefix-summed in coset order. lookup = z || alpha
+   (8 words). Synchronous: claimed_sum_out is valid on return. */
+cs_status cs_poseidon_interaction(const uint32_t *const *h_trace, uint32_t log_n, const uint32_t lookup[8],
+                                  uint32_t *const *h_out, uint32_t claimed_sum_out[4], cs_stream stream);
+
+/* Constraint quotients of the Poseidon component on CanonicCoset(eval_log):
+   the device analogue of FrameworkComponent::evaluate_constraint_quotients_on_domain
+   (crates/constraint-framework/src/prover/component_prover.rs:111-193) for
+   eval_poseidon_constraints (mod.rs:137-189). h_trace / h_inter: the 1264
+   trace and 32 interaction columns evaluated on that domain; h_rc: the 1144
+   random-coefficient powers in constraint order (host, 4 words each); row r
+   adds sum_k rc[k] C_k(r) / V_trace(x_r) to the QM31 accumulator h_accum.
+   With eval_log == trace_log the rows are the trace domain and no denominator
+   is applied (a valid trace gives all-zero rows). */
+cs_status cs_poseidon_composition(const uint32_t *const *h_trace, const uint32_t *const *h_inter, uint32_t eval_log,
+                                  uint32_t trace_log, const uint32_t lookup[8], const uint32_t claimed_sum[4],
+                                  const uint32_t *h_rc, uint32_t *const h_accum[4], cs_stream stream);
+
 /* ------------------------------------------------------- decommitment */
 
 /* Batched reads for decommitment. Replaces the element-wise Column::at reads

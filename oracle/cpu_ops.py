@@ -62,6 +62,20 @@ class CpuOps:
         for c, r in zip(cols, res):
             c.v = r
 
+    def interpolate_into(self, cols, tw):
+        return [Col(r) for r in O.interpolate_batch([c.v for c in cols], tw.itw)]
+
+    def poseidon_trace(self, log_n):
+        return [Col(c) for c in O.poseidon_trace(log_n)]
+
+    def poseidon_interaction(self, trace, lookup):
+        out, claimed = O.poseidon_interaction([c.v for c in trace], lookup[:4], lookup[4:])
+        return [Col(c) for c in out], claimed
+
+    def poseidon_composition(self, trace_evals, inter_evals, trace_log, lookup, claimed, rc, accum):
+        accum.c = O.poseidon_composition([c.v for c in trace_evals], [c.v for c in inter_evals], trace_log,
+                                         lookup, claimed, rc, out=accum.c)
+
     def evaluate(self, coeffs, log_size, tw):
         return [Col(e) for e in O.evaluate_batch([c.v for c in coeffs], [log_size] * len(coeffs), tw.tw)]
 
@@ -124,7 +138,7 @@ class CpuOps:
         return [tuple(int(x) for x in O.barycentric_eval(c.v, weights.c)) for c in cols]
 
     def accumulate_numerators(self, cols, coeffs, log_blowup):
-        arr = np.asarray([[list(a), list(b), list(c)] for a, b, c in coeffs], np.uint32)
+        arr = np.asarray(coeffs, np.uint32)
         out, fl = O.accumulate_numerators([c.v for c in cols], log_blowup, arr)
         return SCol(out), fl
 

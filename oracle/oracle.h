@@ -80,6 +80,15 @@ void orc_wide_fib_composition(const uint32_t **cols, uint32_t n_cols, uint32_t e
 void orc_wide_fib_trace(const uint32_t *a0, const uint32_t *b0, uint32_t log_n, uint32_t n_cols, uint32_t **cols);
 void orc_logup_running_sum(const uint32_t *values, uint32_t log_n, const uint32_t z[4], uint32_t *const out[4],
                            uint32_t claimed_out[4]);
+void orc_poseidon_m4(uint32_t x[4]);
+void orc_poseidon_external(uint32_t s[16]);
+void orc_poseidon_internal(uint32_t s[16]);
+void orc_poseidon_trace(uint32_t log_n, uint32_t **cols);
+void orc_poseidon_interaction(const uint32_t **trace, uint32_t log_n, const uint32_t z[4], const uint32_t alpha[4],
+                              uint32_t **out, uint32_t claimed_out[4]);
+void orc_poseidon_composition(const uint32_t **trace, const uint32_t **inter, uint32_t eval_log, uint32_t trace_log,
+                              const uint32_t lookup[8], const uint32_t claimed[4], const uint32_t *rc,
+                              uint32_t *const out[4]);
 
 #ifdef __cplusplus
 }

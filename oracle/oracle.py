@@ -460,3 +460,60 @@ def logup_running_sum(values, z):
     claimed = np.zeros(4, np.uint32)
     lib().orc_logup_running_sum(_p(v), ctypes.c_uint32(n.bit_length() - 1), _p(zz), _ptr_array(out), _p(claimed))
     return out, claimed
+
+
+# ---------------------------------------------------------------- Poseidon2 AIR
+
+POSEIDON_COLS = 1264
+POSEIDON_INTERACTION_COLS = 32
+POSEIDON_CONSTRAINTS = 1144
+
+
+def poseidon_m4(x):
+    v = _u32(x).copy()
+    lib().orc_poseidon_m4(_p(v))
+    return v
+
+
+def poseidon_external(s):
+    v = _u32(s).copy()
+    lib().orc_poseidon_external(_p(v))
+    return v
+
+
+def poseidon_internal(s):
+    v = _u32(s).copy()
+    lib().orc_poseidon_internal(_p(v))
+    return v
+
+
+def poseidon_trace(log_n: int):
+    cols = [np.zeros(1 << log_n, np.uint32) for _ in range(POSEIDON_COLS)]
+    lib().orc_poseidon_trace(ctypes.c_uint32(log_n), _ptr_array(cols))
+    return cols
+
+
+def poseidon_interaction(trace, z, alpha):
+    t = [_u32(c) for c in trace]
+    n = t[0].size
+    zz, aa = _u32(z), _u32(alpha)
+    out = [np.zeros(n, np.uint32) for _ in range(POSEIDON_INTERACTION_COLS)]
+    claimed = np.zeros(4, np.uint32)
+    lib().orc_poseidon_interaction(_ptr_array(t), ctypes.c_uint32(n.bit_length() - 1), _p(zz), _p(aa),
+                                   _ptr_array(out), _p(claimed))
+    return out, claimed
+
+
+def poseidon_composition(trace, inter, trace_log: int, lookup, claimed, rc, out=None):
+    """trace / inter on the evaluation domain; lookup = z || alpha (8 words); rc: (1144, 4) powers.
+    Adds the row quotients into out (4 coordinate arrays), created when None."""
+    t = [_u32(c) for c in trace]
+    it = [_u32(c) for c in inter]
+    n = t[0].size
+    lk, cl, r = _u32(lookup), _u32(claimed), _u32(np.asarray(rc).reshape(-1))
+    if out is None:
+        out = [np.zeros(n, np.uint32) for _ in range(4)]
+    out = [_u32(o) for o in out]
+    lib().orc_poseidon_composition(_ptr_array(t), _ptr_array(it), ctypes.c_uint32(n.bit_length() - 1),
+                                   ctypes.c_uint32(trace_log), _p(lk), _p(cl), _p(r), _ptr_array(out))
+    return out

@@ -59,6 +59,9 @@ SIGNATURES = {
     "cs_grind_blake2s_noalloc": [vp, u32, u32, u64, vp, vp],
     "cs_logup_running_sum": [vp, u32, vp, vp, vp, vp],
     "cs_gather_u32": [vp, vp, u32, vp, vp, u32, vp, vp],
+    "cs_poseidon_trace": [u32, vp, vp],
+    "cs_poseidon_interaction": [vp, u32, vp, vp, vp, vp],
+    "cs_poseidon_composition": [vp, vp, u32, u32, vp, vp, vp, vp, vp],
 }
 _RESTYPES = {"cs_last_error": ctypes.c_char_p, "cs_version": ctypes.c_char_p,
              "cs_kernel_launch_count": ctypes.c_uint64}

@@ -177,6 +177,20 @@ class CudaBackend:
                       twiddles.log_size, _stream())
 
     @staticmethod
+    def interpolate_columns_into(columns, twiddles: TwiddleTree, out=None):
+        """Out of place: the coefficients of `columns` (kept) in new columns."""
+        if out is None:
+            out = [BaseColumn.uninitialized(len(c)) for c in columns]
+        by_size = {}
+        for i, c in enumerate(columns):
+            by_size.setdefault(c.log_size, []).append(i)
+        for log_size, idxs in by_size.items():
+            _lib.call("cs_interpolate_columns_into", _ptr_table([columns[i].data for i in idxs]),
+                      _ptr_table([out[i].data for i in idxs]), len(idxs), log_size, _ptr(twiddles.itwiddles),
+                      twiddles.log_size, _stream())
+        return out
+
+    @staticmethod
     def evaluate_polynomials(coeffs, log_size: int, twiddles: TwiddleTree, out=None):
         """Evaluates coefficient columns on CanonicCoset(log_size); returns new columns."""
         if out is None:
@@ -371,6 +385,43 @@ class CudaBackend:
         _lib.call("cs_logup_running_sum", _ptr(values.data), values.log_size, _u32_table(z),
                   _ptr_table([c.data for c in out.columns]), claimed, _stream())
         return out, np.array(list(claimed), np.uint32)
+
+    # Poseidon2 AIR ------------------------------------------------------------
+    POSEIDON_COLS = 1264
+    POSEIDON_INTERACTION_COLS = 32
+    POSEIDON_CONSTRAINTS = 1144
+
+    @classmethod
+    def poseidon_trace(cls, log_n: int):
+        """gen_trace (crates/examples/src/poseidon/mod.rs:195-275): 1264 columns of 2^log_n words,
+        held in one (1264, 2^log_n) device block."""
+        block = torch.empty((cls.POSEIDON_COLS, 1 << log_n), dtype=torch.int32, device="cuda")
+        cols = [BaseColumn(block[k]) for k in range(cls.POSEIDON_COLS)]
+        _lib.call("cs_poseidon_trace", log_n, _ptr_table([c.data for c in cols]), _stream())
+        return cols
+
+    @classmethod
+    def poseidon_interaction(cls, trace, lookup):
+        """gen_interaction_trace (mod.rs:277-303): 32 interaction columns and the claimed sum.
+        lookup: z || alpha (8 words)."""
+        n = len(trace[0])
+        block = torch.empty((cls.POSEIDON_INTERACTION_COLS, n), dtype=torch.int32, device="cuda")
+        out = [BaseColumn(block[k]) for k in range(cls.POSEIDON_INTERACTION_COLS)]
+        claimed = (ctypes.c_uint32 * 4)()
+        _lib.call("cs_poseidon_interaction", _ptr_table([c.data for c in trace]), trace[0].log_size,
+                  _u32_table(lookup), _ptr_table([c.data for c in out]), claimed, _stream())
+        return out, np.array(list(claimed), np.uint32)
+
+    @staticmethod
+    def poseidon_composition(trace_evals, inter_evals, trace_log: int, lookup, claimed, rc,
+                             accum: SecureColumnByCoords) -> None:
+        """Adds the Poseidon constraint quotients on the evaluation domain of the given columns to
+        accum (FrameworkComponent::evaluate_constraint_quotients_on_domain). rc: (1144, 4) words."""
+        rc_arr = np.ascontiguousarray(np.asarray(rc, np.uint32).reshape(-1))
+        _lib.call("cs_poseidon_composition", _ptr_table([c.data for c in trace_evals]),
+                  _ptr_table([c.data for c in inter_evals]), trace_evals[0].log_size, trace_log,
+                  _u32_table(lookup), _u32_table(claimed), rc_arr.ctypes.data_as(ctypes.c_void_p),
+                  _ptr_table([c.data for c in accum.columns]), _stream())
 
     # Decommitment -------------------------------------------------------------
     @staticmethod

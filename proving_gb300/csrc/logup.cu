@@ -14,16 +14,13 @@
 
 #include "common.cuh"
 #include "field.cuh"
+#include "logup.cuh"
 
 namespace cs {
 
 namespace {
 
 constexpr uint32_t kScanBlock = 1024;
-
-struct Q4 {
-  uint32_t* c[4];
-};
 
 __device__ __forceinline__ uint32_t coset_pos(uint32_t k, uint32_t log_n) {
   const uint32_t n = 1u << log_n;
@@ -121,7 +118,62 @@ __global__ void add_offsets_kernel(Q4 io, uint32_t log_n, const uint32_t* offset
   for (int c = 0; c < 4; c++) io.c[c][pos] = m31_add(io.c[c][pos], offsets[4 * blockIdx.x + c]);
 }
 
+// Columns shorter than one scan block: one thread, in coset order.
+__global__ void small_scan_kernel(Q4 io, uint32_t log_n, qm31 shift) {
+  const uint32_t n = 1u << log_n;
+  qm31 run = qm31_make(0, 0, 0, 0);
+  for (uint32_t k = 0; k < n; k++) {
+    const uint32_t pos = coset_pos(k, log_n);
+    run = qm31_add(run, qm31_sub(qm31_make(io.c[0][pos], io.c[1][pos], io.c[2][pos], io.c[3][pos]), shift));
+    io.c[0][pos] = run.a.a;
+    io.c[1][pos] = run.a.b;
+    io.c[2][pos] = run.b.a;
+    io.c[3][pos] = run.b.b;
+  }
+}
+
 }  // namespace
+
+cs_status logup_finalize_last(Q4 col, uint32_t log_size, uint32_t claimed_sum_out[4], cudaStream_t st) {
+  const uint32_t n = 1u << log_size, n_blocks = n / kScanBlock;
+  uint32_t* scratch = nullptr;  // 4 words of sum, then 4 words per scan block
+  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(uint32_t) * 4 * (1 + n_blocks), st));
+  cs_status result = CS_OK;
+  do {
+    sum_kernel<<<1, 1024, 0, st>>>(col, n, scratch);
+    note_launch();
+    uint32_t sum[4];
+    cudaError_t e = cudaMemcpyAsync(sum, scratch, sizeof(sum), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      result = from_cuda(e, "logup finalize");
+      break;
+    }
+    for (int c = 0; c < 4; c++) claimed_sum_out[c] = sum[c];
+    // shift = claimed_sum / n, 1/n = 2^(31 - log_size)
+    const qm31 shift = qm31_mul_m31(qm31_make(sum[0], sum[1], sum[2], sum[3]), 1u << (31 - log_size));
+    if (n_blocks == 0) {
+      small_scan_kernel<<<1, 1, 0, st>>>(col, log_size, shift);
+      note_launch();
+      e = cudaGetLastError();
+      if (e != cudaSuccess) result = from_cuda(e, "logup finalize launch");
+      break;
+    }
+    uint32_t* totals = scratch + 4;
+    block_scan_kernel<<<n_blocks, kScanBlock, 0, st>>>(col, log_size, shift, totals);
+    note_launch();
+    totals_scan_kernel<<<1, kScanBlock, 0, st>>>(totals, n_blocks);
+    note_launch();
+    add_offsets_kernel<<<n_blocks, kScanBlock, 0, st>>>(col, log_size, totals);
+    note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) result = from_cuda(e, "logup finalize launch");
+  } while (false);
+  cudaError_t e = cudaFreeAsync(scratch, st);
+  if (result == CS_OK && e != cudaSuccess) return from_cuda(e, "cudaFreeAsync");
+  return result;
+}
+
 }  // namespace cs
 
 using namespace cs;
@@ -137,37 +189,10 @@ extern "C" cs_status cs_logup_running_sum(const uint32_t* d_values, uint32_t log
     out.c[c] = h_out[c];
   }
   cudaStream_t st = to_stream(stream);
-  const uint32_t n = 1u << log_size, n_blocks = n / kScanBlock;
-  uint32_t* scratch = nullptr;  // 4 words of sum, then 4 words per scan block
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(uint32_t) * 4 * (1 + n_blocks), st));
-  cs_status result = CS_OK;
-  do {
-    fractions_kernel<<<std::min<uint32_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(
-        d_values, n, qm31_make(z[0], z[1], z[2], z[3]), out);
-    note_launch();
-    sum_kernel<<<1, 1024, 0, st>>>(out, n, scratch);
-    note_launch();
-    uint32_t sum[4];
-    cudaError_t e = cudaMemcpyAsync(sum, scratch, sizeof(sum), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-      result = from_cuda(e, "logup_running_sum");
-      break;
-    }
-    for (int c = 0; c < 4; c++) claimed_sum_out[c] = sum[c];
-    // shift = claimed_sum / n, 1/n = 2^(31 - log_size)
-    const qm31 shift = qm31_mul_m31(qm31_make(sum[0], sum[1], sum[2], sum[3]), 1u << (31 - log_size));
-    uint32_t* totals = scratch + 4;
-    block_scan_kernel<<<n_blocks, kScanBlock, 0, st>>>(out, log_size, shift, totals);
-    note_launch();
-    totals_scan_kernel<<<1, kScanBlock, 0, st>>>(totals, n_blocks);
-    note_launch();
-    add_offsets_kernel<<<n_blocks, kScanBlock, 0, st>>>(out, log_size, totals);
-    note_launch();
-    e = cudaGetLastError();
-    if (e != cudaSuccess) result = from_cuda(e, "logup_running_sum launch");
-  } while (false);
-  cudaError_t e = cudaFreeAsync(scratch, st);
-  if (result == CS_OK && e != cudaSuccess) return from_cuda(e, "cudaFreeAsync");
-  return result;
+  const uint32_t n = 1u << log_size;
+  fractions_kernel<<<std::min<uint32_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(
+      d_values, n, qm31_make(z[0], z[1], z[2], z[3]), out);
+  note_launch();
+  CS_CUDA(cudaGetLastError());
+  return logup_finalize_last(out, log_size, claimed_sum_out, st);
 }

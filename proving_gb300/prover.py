@@ -110,6 +110,47 @@ def secure_powers(felt, n: int):
     return out
 
 
+# ------------------------------------------------------------ QM31 arrays
+# The same arithmetic on numpy int64 arrays of shape (..., 4) with canonical
+# coordinates: products of two words stay below 2^62 and a sum of two below 2^63.
+
+
+def qv(x):
+    return np.asarray(x, dtype=np.int64).reshape(-1, 4) if np.ndim(x) == 1 else np.asarray(x, dtype=np.int64)
+
+
+def _cm_mul_v(p0, p1, q0, q1):
+    return (p0 * q0 - p1 * q1) % P, (p0 * q1 + p1 * q0) % P
+
+
+def qv_mul(x, y):
+    x, y = np.asarray(x, np.int64), np.asarray(y, np.int64)
+    ac0, ac1 = _cm_mul_v(x[..., 0], x[..., 1], y[..., 0], y[..., 1])
+    bd0, bd1 = _cm_mul_v(x[..., 2], x[..., 3], y[..., 2], y[..., 3])
+    ad0, ad1 = _cm_mul_v(x[..., 0], x[..., 1], y[..., 2], y[..., 3])
+    bc0, bc1 = _cm_mul_v(x[..., 2], x[..., 3], y[..., 0], y[..., 1])
+    r0, r1 = (2 * bd0 - bd1) % P, (bd0 + 2 * bd1) % P
+    return np.stack([(ac0 + r0) % P, (ac1 + r1) % P, (ad0 + bc0) % P, (ad1 + bc1) % P], axis=-1)
+
+
+def qv_sub(x, y):
+    return (np.asarray(x, np.int64) - np.asarray(y, np.int64)) % P
+
+
+def qv_add(x, y):
+    return (np.asarray(x, np.int64) + np.asarray(y, np.int64)) % P
+
+
+def qv_conj(x):
+    x = np.asarray(x, np.int64)
+    return np.stack([x[..., 0], x[..., 1], (-x[..., 2]) % P, (-x[..., 3]) % P], axis=-1)
+
+
+def qv_sum(x):
+    """Sum over the leading axis, reduced."""
+    return np.asarray(x, np.int64).sum(axis=0) % P
+
+
 # ------------------------------------------------------------ circle points
 
 def cpoint_add(p, q):
@@ -250,6 +291,16 @@ def line_coeffs(py, value, alpha):
     return (qm_mul(alpha, a), qm_mul(alpha, b), qm_mul(alpha, c))
 
 
+def line_coeffs_v(py, values, alphas):
+    """line_coeffs for n sampled values at one point: (n, 3, 4) words (a, b, c per column)."""
+    v, al = np.asarray(values, np.int64), np.asarray(alphas, np.int64)
+    pyv = np.broadcast_to(np.asarray(py, np.int64), v.shape)
+    a = qv_sub(qv_conj(v), v)
+    c = qv_sub(qv_conj(pyv), pyv)
+    b = qv_sub(qv_mul(v, c), qv_mul(a, pyv))
+    return np.stack([qv_mul(al, a), qv_mul(al, b), qv_mul(al, c)], axis=1)
+
+
 # ------------------------------------------------------------ decommitment reads
 
 class Reads:
@@ -262,11 +313,11 @@ class Reads:
         self.out = None
 
     def values(self, col, idx) -> int:
-        self.items.append(("col", col, list(idx)))
+        self.items.append(("col", col, np.asarray(idx, dtype=np.int64)))
         return len(self.items) - 1
 
     def digests(self, tree, layer_log: int, nodes) -> int:
-        self.items.append(("dig", tree, layer_log, list(nodes)))
+        self.items.append(("dig", tree, layer_log, np.asarray(nodes, dtype=np.int64)))
         return len(self.items) - 1
 
     def run(self, ops):
@@ -278,50 +329,44 @@ class Reads:
 
 def merkle_witness_nodes(height: int, query_positions):
     """The witness of MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:119-150)
-    as (layer log size, node) pairs in proof order: walking down from the
-    leaves, the sibling of every queried node whose sibling is not queried."""
-    nodes = []
-    prev = sorted(set(query_positions))
+    per layer, walking down from the leaves: [(layer log size, sibling nodes)], the sibling of
+    every queried node whose sibling is not queried, in node order."""
+    out = []
+    prev = np.unique(np.asarray(query_positions, dtype=np.int64))
     for layer_log in range(height - 1, -1, -1):
-        cur = []
-        i = 0
-        while i < len(prev):
-            first = prev[i]
-            if i + 1 < len(prev) and prev[i + 1] == first ^ 1:
-                i += 2
-            else:
-                nodes.append((layer_log + 1, first ^ 1))
-                i += 1
-            cur.append(first >> 1)
-        prev = cur
-    return nodes
+        # prev is sorted and distinct: a sibling is present iff it sits next to its node
+        sib = prev ^ 1
+        at = np.minimum(np.searchsorted(prev, sib), prev.size - 1)
+        need = sib[prev[at] != sib]
+        if need.size:
+            out.append((layer_log + 1, need))
+        up = prev >> 1
+        prev = up[np.r_[True, up[1:] != up[:-1]]]
+    return out
 
 
 class MerkleDecommit:
     """MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:97-162) in two
-    steps: `plan` registers the queried values (col[(pos >> (shift + 1) << 1) + (pos & 1)] for a
-    column of log size L - shift) and the witness digests with a Reads; `result` assembles them."""
+    steps: the constructor registers the queried values (col[(pos >> (shift + 1) << 1) + (pos & 1)]
+    for a column of log size L - shift) and the witness digests with a Reads; `result` assembles
+    them once the Reads has run."""
 
     def __init__(self, reads: Reads, tree, query_positions, columns, ops):
         L = tree.height
+        q = np.asarray(query_positions, dtype=np.int64)
         self.value_handles = []
         for col in columns:
             shift = L - ops.log_size(col)
-            self.value_handles.append(reads.values(col, [((q >> (shift + 1)) << 1) + (q & 1)
-                                                         for q in query_positions]))
-        by_layer = {}
-        for layer_log, node in merkle_witness_nodes(L, query_positions):
-            by_layer.setdefault(layer_log, []).append(node)
-        # one read per layer, in proof order (layers descend from the leaves)
-        self.witness_handles = [reads.digests(tree, k, nodes) for k, nodes in by_layer.items()]
+            self.value_handles.append(reads.values(col, ((q >> (shift + 1)) << 1) + (q & 1)))
+        self.witness_handles = [reads.digests(tree, k, nodes) for k, nodes in merkle_witness_nodes(L, q)]
         self.reads = reads
 
     def result(self):
-        queried = [[int(v) for v in self.reads[h]] for h in self.value_handles]
+        queried = [self.reads[h].tolist() for h in self.value_handles]
         witness = []
         for h in self.witness_handles:
-            arr = self.reads[h]
-            witness.extend(arr[i].astype("<u4").tobytes() for i in range(arr.shape[0]))
+            b = np.ascontiguousarray(self.reads[h], dtype="<u4").tobytes()
+            witness.extend(b[i:i + 32] for i in range(0, len(b), 32))
         return queried, witness
 
 
@@ -331,18 +376,10 @@ def decommitment_positions(query_positions, fold_step: int):
     """compute_decommitment_positions_and_witness_evals (crates/stwo/src/prover/fri.rs:408-438)
     without the values: the positions to open (every coset of 2^fold_step around a query) and,
     per position, whether its value goes to the witness (it is not itself a query)."""
-    positions, is_witness = [], []
-    qset = set(query_positions)
-    seen = set()
-    for q in query_positions:
-        start = (q >> fold_step) << fold_step
-        if start in seen:
-            continue
-        seen.add(start)
-        for pos in range(start, start + (1 << fold_step)):
-            positions.append(pos)
-            is_witness.append(pos not in qset)
-    return positions, is_witness
+    q = np.asarray(query_positions, dtype=np.int64)
+    starts = np.unique(q >> fold_step) << fold_step
+    positions = (starts[:, None] + np.arange(1 << fold_step)).reshape(-1)
+    return positions, ~np.isin(positions, q)
 
 
 class FriLayerDecommit:
@@ -357,8 +394,8 @@ class FriLayerDecommit:
         self.tree = tree
 
     def result(self):
-        coords = [self.reads[h] for h in self.coord_handles]
-        witness = [tuple(int(coords[k][i]) for k in range(4)) for i, w in enumerate(self.is_witness) if w]
+        coords = np.stack([self.reads[h] for h in self.coord_handles], axis=1)[self.is_witness]
+        witness = [tuple(r) for r in coords.tolist()]
         _, dec = self.merkle.result()
         return {"fri_witness": witness, "decommitment": dec, "commitment": self.tree.root}
 
@@ -479,22 +516,7 @@ def prove_wide_fib(ops, trace, log_n_rows: int, config: PcsConfig, channel: Blak
     lifting = L
     columns = [[], trace_evals, comp_evals]
     sample_points = [[], [[oods]] * n_cols, [[oods]] * 8]
-    sampled = []
-    for tree_cols, pts in zip(columns, sample_points):
-        vals = [[] for _ in tree_cols]
-        by_size = {}
-        for ci, col in enumerate(tree_cols):
-            by_size.setdefault(ops.log_size(col), []).append(ci)
-        for log_size, cis in by_size.items():
-            # one weight column per (log size, point.repeated_double(lifting - log_size))
-            pt = pts[cis[0]][0]
-            for _ in range(lifting - log_size):
-                pt = (q_double_x(pt[0]), qm_mul(qm(2), qm_mul(pt[0], pt[1])))
-            w = ops.barycentric_weights(log_size, pt)
-            res = ops.barycentric_eval([tree_cols[ci] for ci in cis], w)
-            for ci, v in zip(cis, res):
-                vals[ci] = [tuple(int(x) for x in v)]
-        sampled.append(vals)
+    sampled = sample_values(ops, columns, sample_points, lifting)
     channel.mix_felts([v for tree in sampled for col in tree for v in col])
 
     quotient_coeff = channel.draw_secure_felt()
@@ -545,39 +567,86 @@ def prove_wide_fib(ops, trace, log_n_rows: int, config: PcsConfig, channel: Blak
     for _ in range(max_log_degree_bound - 1):
         x = q_double_x(x)
     composition_oods = qm_add(left_v, qm_mul(x, right_v))
-    expected = wide_fib_composition_at_point(oods, [c[0] for c in sampled[1]], random_coeff, max_log_degree_bound)
+    expected = wide_fib_composition_at_point(oods, [c[0] for c in sampled[1]], random_coeff, max_log_degree_bound,
+                                             powers=rc)
     if composition_oods != expected:
         raise RuntimeError("constraints not satisfied (ProvingError::ConstraintsNotSatisfied)")
     return proof
 
 
-def wide_fib_composition_at_point(point, mask, random_coeff, max_log_degree_bound: int):
+def wide_fib_composition_at_point(point, mask, random_coeff, max_log_degree_bound: int, powers=None):
     """Components::eval_composition_polynomial_at_point for the Wide-Fibonacci component
     (crates/constraint-framework/src/component.rs:220-243, PointEvaluationAccumulator,
-    crates/stwo/src/core/air/accumulation.rs:13-33): Horner over the constraints,
-    each divided by V_trace(point)."""
+    crates/stwo/src/core/air/accumulation.rs:13-33): the Horner sum over the constraints
+    sum_k alpha^(N-1-k) C_k, divided by V_trace(point). `powers`: alpha^(N-1-k) per constraint
+    when the caller has them."""
     x = point[0]
     for _ in range(max_log_degree_bound - 1):
         x = q_double_x(x)
     den_inv = qm_inv(x)
-    acc = qm(0)
-    for k in range(len(mask) - 2):
-        a, bb, c = mask[k], mask[k + 1], mask[k + 2]
-        cons = qm_sub(c, qm_add(qm_mul(a, a), qm_mul(bb, bb)))
-        acc = qm_add(qm_mul(acc, random_coeff), qm_mul(cons, den_inv))
-    return acc
+    m = np.asarray(mask, np.int64)
+    a, b, c = m[:-2], m[1:-1], m[2:]
+    cons = qv_sub(c, qv_add(qv_mul(a, a), qv_mul(b, b)))
+    if powers is None:
+        powers = list(reversed(secure_powers(random_coeff, len(cons))))
+    total = qv_sum(qv_mul(cons, np.asarray(powers, np.int64)))
+    return qm_mul(tuple(int(v) for v in total), den_inv)
+
+
+def q_double_point(pt):
+    """CirclePoint::double over QM31."""
+    return (q_double_x(pt[0]), qm_mul(qm(2), qm_mul(pt[0], pt[1])))
+
+
+def sample_values(ops, columns, sample_points, lifting: int):
+    """CommitmentSchemeProver::compute_samples (crates/stwo/src/prover/pcs/mod.rs:175-214): every
+    column at every one of its sample points, each point doubled lifting - log_size times (the
+    column is committed lifted); one barycentric weight column per (log size, doubled point).
+    Returns per tree, per column, the list of QM31 values."""
+    sampled = []
+    for tree_cols, pts in zip(columns, sample_points):
+        vals = [[None] * len(p_) for p_ in pts]
+        groups = {}
+        for ci, col in enumerate(tree_cols):
+            for si, pt in enumerate(pts[ci]):
+                groups.setdefault((ops.log_size(col), pt), []).append((ci, si))
+        for (log_size, pt), members in groups.items():
+            for _ in range(lifting - log_size):
+                pt = q_double_point(pt)
+            w = ops.barycentric_weights(log_size, pt)
+            res = ops.barycentric_eval([tree_cols[ci] for ci, _ in members], w)
+            for (ci, si), v in zip(members, res):
+                vals[ci][si] = tuple(int(x) for x in v)
+        sampled.append(vals)
+    return sampled
+
+
+def m31_subgroup_generator(log_size: int):
+    """The generator G_log_size of the circle subgroup of order 2^log_size, as an M31 point."""
+    return index_to_point(1 << (31 - log_size))
+
+
+def qpoint_add_m31(p, g):
+    """p + g for a QM31 point p and an M31 point g."""
+    return qpoint_add(p, (qm(g[0]), qm(g[1])))
 
 
 def compute_fri_quotients(ops, columns, sample_points, sampled, random_coeff, lifting: int, log_blowup: int,
                           twiddles):
-    """compute_fri_quotients (crates/stwo/src/prover/pcs/quotient_ops.rs:86-160) for columns with one
-    sample each (no periodicity samples, crates/stwo/src/core/pcs/quotients.rs:274-319)."""
-    pows = iter(secure_powers(random_coeff, sum(len(c) for tree in sampled for c in tree)))
+    """compute_fri_quotients (crates/stwo/src/prover/pcs/quotient_ops.rs:86-160): every sample of every
+    column with its random power, grouped by column size and sample point, accumulated, lifted and
+    combined into the FRI quotient column."""
+    n_samples = sum(len(c) + (1 if len(c) == 2 else 0) for tree in sampled for c in tree)
+    pows = iter(secure_powers(random_coeff, n_samples))
     entries = []  # (column, point, value, random power) in tree/column order
     for tree_cols, pts, vals in zip(columns, sample_points, sampled):
         for col, cp, cv in zip(tree_cols, pts, vals):
             if len(cp) == 2:
-                raise NotImplementedError("periodicity samples")
+                # build_samples_with_randomness_and_periodicity (crates/stwo/src/core/pcs/quotients.rs:274-319):
+                # a column sampled at (previous row, point) also opens the point shifted by the
+                # period G_(lifting - log size), with the point's value, first
+                period = m31_subgroup_generator(lifting - ops.log_size(col))
+                entries.append((col, qpoint_add_m31(cp[1], period), cv[1], next(pows)))
             for p_, v_ in zip(cp, cv):
                 entries.append((col, p_, v_, next(pows)))
     # stable sort by column log size, group by size, batch by point in insertion order
@@ -594,7 +663,7 @@ def compute_fri_quotients(ops, columns, sample_points, sampled, random_coeff, li
         for col, p_, v_, rp in group:
             batches.setdefault(p_, []).append((col, v_, rp))
         for p_, items in batches.items():
-            coeffs = [line_coeffs(p_[1], v_, rp) for _, v_, rp in items]
+            coeffs = line_coeffs_v(p_[1], [v_ for _, v_, _ in items], [rp for _, _, rp in items])
             part, first_linear = ops.accumulate_numerators([c for c, _, _ in items], coeffs, log_blowup)
             accs.append((p_, part, tuple(int(x) for x in first_linear)))
         i = j
@@ -712,11 +781,30 @@ class GpuOps:
     def interpolate(self, cols, tw):
         self.B.interpolate_columns(cols, tw)
 
+    def interpolate_into(self, cols, tw):
+        """Coefficients of the evaluations `cols` in new columns (one device block); cols are kept."""
+        return self.B.interpolate_columns_into(cols, tw, out=self._block(len(cols), cols[0].log_size))
+
     def evaluate(self, coeffs, log_size, tw):
-        return self.B.evaluate_polynomials(coeffs, log_size, tw)
+        return self.B.evaluate_polynomials(coeffs, log_size, tw, out=self._block(len(coeffs), log_size))
+
+    def _block(self, n_cols, log_size):
+        import torch
+        blk = torch.empty((n_cols, 1 << log_size), dtype=torch.int32, device="cuda")
+        return [self.be.BaseColumn(blk[k]) for k in range(n_cols)]
 
     def merkle_commit(self, cols, L):
         return GpuMerkle(self.B.merkle_commit(cols, L), L)
+
+    # Poseidon2 AIR (crates/examples/src/poseidon/mod.rs)
+    def poseidon_trace(self, log_n):
+        return self.B.poseidon_trace(log_n)
+
+    def poseidon_interaction(self, trace, lookup):
+        return self.B.poseidon_interaction(trace, lookup)
+
+    def poseidon_composition(self, trace_evals, inter_evals, trace_log, lookup, claimed, rc, accum):
+        self.B.poseidon_composition(trace_evals, inter_evals, trace_log, lookup, claimed, rc, accum)
 
     def gather(self, col, idx):
         import torch
@@ -793,8 +881,7 @@ class GpuOps:
         return [tuple(int(x) for x in row) for row in out]
 
     def accumulate_numerators(self, cols, coeffs, log_blowup):
-        arr = np.asarray([[list(a), list(b_), list(c)] for a, b_, c in coeffs], np.uint32)
-        return self.B.accumulate_numerators(cols, arr, log_blowup)
+        return self.B.accumulate_numerators(cols, np.asarray(coeffs, np.uint32), log_blowup)
 
     def lift_and_accumulate(self, cols):
         return self.B.lift_and_accumulate(cols)
@@ -809,3 +896,22 @@ class GpuOps:
 
     def fold_line(self, col, alpha, tw):
         return self.B.fold_line(col, [np.asarray(alpha, np.uint32)], tw)
+
+
+class PlainGpuOps(GpuOps):
+    """The plain CUDA form: the same kernels, one launch per column for every
+    per-column stage (interpolate, evaluate), as a backend without batched
+    overrides calls them (the default PolyOps::interpolate_columns /
+    evaluate_polynomials loop, crates/stwo/src/prover/poly/circle/ops.rs:25-40,102-140)."""
+
+    def interpolate(self, cols, tw):
+        for c in cols:
+            self.B.interpolate_columns([c], tw)
+
+    def evaluate(self, coeffs, log_size, tw):
+        return [self.B.evaluate_polynomials([c], log_size, tw)[0] for c in coeffs]
+
+    def interpolate_secure(self, accum, tw):
+        for c in accum.columns:
+            self.B.interpolate_columns([c], tw)
+        return accum.columns

@@ -58,12 +58,14 @@ def default_config(log_n_rows: int) -> pr.PcsConfig:
 
 
 class ProverService:
-    def __init__(self, n_workers: int = 4, hbm_budget: int = 64 << 30, max_log_n_rows: int = 20):
+    def __init__(self, n_workers: int = 4, hbm_budget: int = 64 << 30, max_log_n_rows: int = 20,
+                 plain: bool = False):
         import torch
         from .backend import BaseColumn, CudaBackend
         self.torch = torch
         self.BaseColumn, self.B = BaseColumn, CudaBackend
-        self.ops = pr.GpuOps()
+        # plain: one launch per column per stage; otherwise the batched stage launches
+        self.ops = pr.PlainGpuOps() if plain else pr.GpuOps()
         self.twiddles = self.ops.twiddles(max_log_n_rows + 2)
         torch.cuda.synchronize()
         self.n_workers = n_workers
@@ -135,9 +137,9 @@ def poisson_requests(n: int, rate_per_s: float, log_min: int, log_max: int, seed
     return [(float(g), ProofRequest(i, int(s), seed * 100003 + 2 * i)) for i, (g, s) in enumerate(zip(gaps, sizes))]
 
 
-def run_stream(n_workers: int, requests, hbm_budget: int = 64 << 30, max_log: int = 20):
+def run_stream(n_workers: int, requests, hbm_budget: int = 64 << 30, max_log: int = 20, plain: bool = False):
     """Serves a request stream; returns (finished requests, wall seconds)."""
-    svc = ProverService(n_workers=n_workers, hbm_budget=hbm_budget, max_log_n_rows=max_log)
+    svc = ProverService(n_workers=n_workers, hbm_budget=hbm_budget, max_log_n_rows=max_log, plain=plain)
     svc.start()
     t0 = time.perf_counter()
     for gap, req in requests:

@@ -21,7 +21,8 @@ def test_results_alone_equal_results_in_the_mix():
     mixed, _ = serving.run_stream(4, [(0.0, r) for r in reqs], max_log=12)
     assert all(r.error is None for r in mixed)
     alone_reqs = [serving.ProofRequest(i, s, 1000 + 7 * i) for i, s in enumerate(sizes)]
-    alone, _ = serving.run_stream(1, [(0.0, r) for r in alone_reqs], max_log=12)
+    # alone, and through the plain one-launch-per-column path: the same bytes
+    alone, _ = serving.run_stream(1, [(0.0, r) for r in alone_reqs], max_log=12, plain=True)
     by_id = {r.request_id: r.proof.to_bytes() for r in alone}
     for r in mixed:
         assert r.proof.to_bytes() == by_id[r.request_id]
