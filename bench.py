@@ -46,7 +46,11 @@ def workload_name():
             f"lifted Blake2s Merkle over {N_COLS}-wide leaves, {FRI_LOG} FRI folds of a QM31 col of log {FRI_LOG}")
 
 
+# DRAM bytes (read + write) measured with ncu on the 256 x 2^20 workload
+# (profiles/launch_list_commit_stage_256x2^20.md): one merkle_leaves_kernel launch, and the two
+# fft_tile_kernel launches of one evaluate
 LEAVES_TRAFFIC_BYTES = 4425.2e6
+EVALUATE_TRAFFIC_BYTES = 13925.3e6
 
 
 def set_shape(n_cols: int, log_rows: int):
@@ -517,20 +521,25 @@ def run_gpu(args):
     wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
     bvp = batched_vs_plain(torch, cs) if not args.skip_plain else None
     serving_res = serving_leg() if not args.skip_serving else None
-    poseidon_res = poseidon_prove_leg(torch) if not args.skip_poseidon else None
+    poseidon_res = poseidon_prove_leg(torch, args.poseidon_log_rows) if not args.skip_poseidon else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
     hbm, peak_kind = peaks()
-    # dominant kernel: the Blake2s leaf hashing (one launch per step)
+    default_shape = (N_COLS, LOG_ROWS, LOG_EXT) == (256, 20, 22)
+    # dominant kernel: the evaluate FFT (fft_tile_kernel, two tile passes per step); algorithmic
+    # bytes per column are 4 n_in + 4 n_out (coefficients read once, the blown-up evaluation written)
+    eval_ms = stage_ms["evaluate"]
+    eval_bytes = N_COLS * 4 * ((1 << LOG_ROWS) + (1 << LOG_EXT))
+    achieved = eval_bytes / (eval_ms / 1e3) / 1e9
+    eval_traffic = EVALUATE_TRAFFIC_BYTES if default_shape else None
+    # the Blake2s leaf hashing (one launch per step): 4 bytes per column value read, 32 per leaf written
     leaf_ms = stage_ms["merkle_leaves"]
     leaf_bytes = N_COLS * (1 << LOG_EXT) * 4 + (1 << LOG_EXT) * 32
-    achieved = leaf_bytes / (leaf_ms / 1e3) / 1e9
+    leaf_gbs = leaf_bytes / (leaf_ms / 1e3) / 1e9
     leaf_comp = (1 << LOG_EXT) * ((N_COLS * 4 + 63) // 64)
-    # DRAM bytes (read + write) of one merkle_leaves_kernel launch on this workload, from the
-    # ncu launch list recorded in profiles/launch_list_commit_stage_256x2^20.md
-    traffic = LEAVES_TRAFFIC_BYTES if (N_COLS, LOG_EXT) == (256, 22) else None
+    traffic = LEAVES_TRAFFIC_BYTES if default_shape else None
     cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
     ff = lambda x: float(f"{x:.6g}")
     res = {
@@ -545,10 +554,17 @@ def run_gpu(args):
                        "e2e_p50": ff(float(np.percentile(e_lat, 50))), "e2e_p99": ff(float(np.percentile(e_lat, 99)))},
         "stages_ms": {k: ff(v) for k, v in stage_ms.items()},
         "e2e": {"value": ff(e2e_value), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": "merkle_leaves_kernel", "achieved": ff(achieved), "peak": hbm,
-                     "unit": "GB/s", "frac": ff(achieved / hbm), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json)",
-                     "traffic": traffic, "algorithmic_bytes_per_launch": leaf_bytes,
-                     "note": "Blake2s leaf hashing is integer-pipe bound; see int_pipe"},
+        "roofline": {"bound": "hbm", "kernel": "fft_tile_kernel (evaluate: 2 tile passes per step)",
+                     "achieved": ff(achieved), "peak": hbm, "unit": "GB/s", "frac": ff(achieved / hbm),
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json)", "traffic": eval_traffic,
+                     "algorithmic_bytes_per_evaluate": eval_bytes, "launches_per_evaluate": 2,
+                     "note": "achieved and traffic are per evaluate (both passes); the passes are integer-pipe "
+                             "bound (ALU pipe ~75% busy), and traffic counts the intermediate of the two-pass "
+                             "FFT written once and read once"},
+        "leaves_roofline": {"bound": "hbm", "kernel": "merkle_leaves_kernel", "achieved": ff(leaf_gbs), "peak": hbm,
+                            "unit": "GB/s", "frac": ff(leaf_gbs / hbm), "traffic": traffic,
+                            "algorithmic_bytes_per_launch": leaf_bytes,
+                            "note": "Blake2s leaf hashing is integer-pipe bound; see int_pipe"},
         "int_pipe": {"kernel": "merkle_leaves_kernel", "compressions_per_launch": leaf_comp,
                      "gcompressions_per_s": ff(leaf_comp / (leaf_ms / 1e3) / 1e9),
                      "int_ops_per_compression": 1120,
@@ -657,6 +673,7 @@ def main():
     ap.add_argument("--skip-plain", action="store_true", help="skip the batched-vs-plain comparison legs")
     ap.add_argument("--skip-serving", action="store_true", help="skip the proof-service leg")
     ap.add_argument("--skip-poseidon", action="store_true", help="skip the Poseidon2 prove leg")
+    ap.add_argument("--poseidon-log-rows", type=int, default=18, help="log2 rows of the Poseidon2 prove leg")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
     if args.impl == "reference":

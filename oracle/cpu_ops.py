@@ -103,7 +103,10 @@ class CpuOps:
         the latter as (n, 8) little-endian words."""
         out = []
         for it in items:
-            if it[0] == "col":
+            if it[0] == "cols":
+                ix = np.asarray(it[2], dtype=np.int64)
+                out.append(np.stack([c.v[ix] for c in it[1]]) if it[1] else np.zeros((0, ix.size), np.uint32))
+            elif it[0] == "col":
                 out.append(it[1].v[np.asarray(it[2], dtype=np.int64)])
             else:
                 tree, k, nodes = it[1], it[2], it[3]

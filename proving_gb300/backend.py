@@ -58,6 +58,7 @@ class BaseColumn:
     def __init__(self, data: torch.Tensor):
         assert data.dtype == torch.int32 and data.dim() == 1 and data.is_cuda
         self.data = data
+        self._log_size = data.numel().bit_length() - 1
 
     @classmethod
     def zeros(cls, length: int, device="cuda"):
@@ -80,8 +81,7 @@ class BaseColumn:
 
     @property
     def log_size(self) -> int:
-        n = len(self)
-        return n.bit_length() - 1
+        return self._log_size
 
     def at(self, i: int) -> int:
         return int(self.data[i].item()) & 0xFFFFFFFF

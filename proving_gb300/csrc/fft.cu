@@ -71,6 +71,24 @@ __device__ __forceinline__ void ibfly(uint32_t& v0, uint32_t& v1, uint32_t t) {
   v1 = m31_mul(m31_sub(tmp, v1), t);
 }
 
+// The tile kernels multiply by doubled twiddles t2 = 2t (at most 2^32 - 4): the 64-bit product
+// a * t2 is a*t shifted left by one, so its high word is (a*t) >> 31 and its low word shifted
+// right by one is (a*t) mod 2^31, which saves the masking of the plain reduction.
+__device__ __forceinline__ uint32_t mul_doubled(uint32_t a, uint32_t t2) {
+  const uint64_t q = (uint64_t)a * t2;
+  return m31_reduce_once(((uint32_t)q >> 1) + (uint32_t)(q >> 32));
+}
+__device__ __forceinline__ void bfly2(uint32_t& v0, uint32_t& v1, uint32_t t2) {
+  const uint32_t tmp = mul_doubled(v1, t2);
+  v1 = m31_sub(v0, tmp);
+  v0 = m31_add(v0, tmp);
+}
+__device__ __forceinline__ void ibfly2(uint32_t& v0, uint32_t& v1, uint32_t t2) {
+  const uint32_t tmp = v0;
+  v0 = m31_add(tmp, v1);
+  v1 = mul_doubled(m31_sub(tmp, v1), t2);
+}
+
 // Shared-memory layout of a tile. Outer (contiguous) tiles hold [e][m] and
 // insert one pad word per 32; inner (strided) tiles hold [m][e] with 8 values
 // of e and insert 8 pad words per 256. Both make every 32-wide access of the
@@ -159,14 +177,16 @@ struct Layers {
     {
       const uint32_t layer = p.lo + D0 + t;
       load_twiddles<(1 << (R - 1 - t)), OUTER && D0 == 0 && t == 0>(p, layer, g0 >> (layer + 1), w + tw_off<R>(t));
+#pragma unroll
+      for (int q = 0; q < (1 << (R - 1 - t)); q++) w[tw_off<R>(t) + q] <<= 1;
     }
 #pragma unroll
     for (int j = 0; j < (1 << R); j++) {
       if (j & (1 << t)) continue;
       if (INV)
-        ibfly(v[j], v[j | (1 << t)], w[tw_off<R>(t) + (j >> (t + 1))]);
+        ibfly2(v[j], v[j | (1 << t)], w[tw_off<R>(t) + (j >> (t + 1))]);
       else
-        bfly(v[j], v[j | (1 << t)], w[tw_off<R>(t) + (j >> (t + 1))]);
+        bfly2(v[j], v[j | (1 << t)], w[tw_off<R>(t) + (j >> (t + 1))]);
     }
     Layers<INV, OUTER, R, D0, K + 1>::run(p, g0, v, w);
   }

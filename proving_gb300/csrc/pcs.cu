@@ -150,21 +150,76 @@ __device__ __forceinline__ void block_reduce_u64x4(uint64_t acc[4], uint64_t* sh
   }
 }
 
-// One block per column: sum_i W_i * v[i]. Partial sums stay below 2^64:
-// every term is reduced to < 2^31 before it is added, at most 2^30 terms.
-__global__ void bary_eval_kernel(const BaryColumns cols, uint32_t log_n, CSoA w, uint32_t* out) {
-  __shared__ uint64_t sh[4 * 32];
+// Many columns at once: block (x, y) takes rows [2048 x, 2048 (x + 1)) of the 16 columns of group
+// y. Each thread keeps the weights of its 8 rows in registers and adds the unreduced 64-bit
+// products for every column (folding below 2^34 every 3 terms); warps and then the block reduce
+// per column, and the block writes its per-column partial sums (below 2^42) to `partial`, which
+// bary_final_kernel sums per column (at most 2^19 chunks: below 2^61).
+constexpr int kBaryThreads = 256;
+constexpr int kBaryRows = 8;  // rows per thread
+constexpr int kBaryChunk = kBaryThreads * kBaryRows;
+constexpr int kBaryGroup = 16;  // columns per block
+
+__device__ __forceinline__ uint64_t fold34(uint64_t v) { return (v & P) + (v >> 31); }
+
+__global__ void __launch_bounds__(kBaryThreads) bary_partial_kernel(const BaryColumns cols, uint32_t nb,
+                                                                   uint32_t log_n, CSoA w,
+                                                                   unsigned long long* partial) {
+  __shared__ uint64_t sh[kBaryThreads / 32][4];
   const uint32_t n = 1u << log_n;
-  const uint32_t* v = cols.ptr[blockIdx.x];
-  uint64_t acc[4] = {0, 0, 0, 0};
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-    const uint32_t x = __ldg(v + i);
+  const uint32_t base = blockIdx.x * kBaryChunk;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t wr[kBaryRows][4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) acc[k] += m31_mul(__ldg(w.c[k] + i), x);
+  for (int j = 0; j < kBaryRows; j++) {
+    const uint32_t row = base + threadIdx.x + j * kBaryThreads;
+#pragma unroll
+    for (int k = 0; k < 4; k++) wr[j][k] = row < n ? __ldg(w.c[k] + row) : 0;
   }
-  block_reduce_u64x4(acc, sh);
-  if (threadIdx.x == 0)
-    for (int k = 0; k < 4; k++) out[4 * blockIdx.x + k] = reduce64(acc[k] % P);
+  const uint32_t c0 = blockIdx.y * kBaryGroup;
+  const uint32_t c1 = min(nb, c0 + kBaryGroup);
+  for (uint32_t col = c0; col < c1; col++) {
+    const uint32_t* v = cols.ptr[col];
+    uint32_t x[kBaryRows];
+#pragma unroll
+    for (int j = 0; j < kBaryRows; j++) {
+      const uint32_t row = base + threadIdx.x + j * kBaryThreads;
+      x[j] = row < n ? __ldg(v + row) : 0;
+    }
+    uint64_t acc[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int j = 0; j < kBaryRows; j++) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        acc[k] += (uint64_t)wr[j][k] * x[j];
+        if (j % 3 == 2) acc[k] = fold34(acc[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      acc[k] = fold34(acc[k]);
+      for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < 4; k++) sh[warp][k] = acc[k];
+    __syncthreads();
+    if (threadIdx.x < 4) {
+      uint64_t t = 0;
+#pragma unroll
+      for (int q = 0; q < kBaryThreads / 32; q++) t += sh[q][threadIdx.x];
+      partial[((size_t)blockIdx.x * nb + col) * 4 + threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void bary_final_kernel(const unsigned long long* partial, uint32_t n_chunks, uint32_t nb, uint32_t* out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // (column, coordinate)
+  if (i >= nb * 4) return;
+  uint64_t t = 0;
+  for (uint32_t ch = 0; ch < n_chunks; ch++) t += partial[(size_t)ch * nb * 4 + i];
+  out[i] = reduce64(t % P);
 }
 
 // ---------------------------------------------------------------- eval_at_point
@@ -433,8 +488,19 @@ extern "C" cs_status cs_barycentric_eval(const uint32_t* const* h_cols, uint32_t
       CS_CHECK_ARG(h_cols[b0 + i] != nullptr, "barycentric_eval: column %u is null", b0 + i);
       cols.ptr[i] = h_cols[b0 + i];
     }
-    bary_eval_kernel<<<nb, 512, 0, to_stream(stream)>>>(cols, log_size, w, d_out + 4 * b0);
-    CS_LAUNCHED("bary_eval_kernel");
+    const uint32_t n_chunks = ((1u << log_size) + kBaryChunk - 1) / kBaryChunk;
+    cudaStream_t st = to_stream(stream);
+    unsigned long long* partial = nullptr;
+    CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&partial), sizeof(unsigned long long) * 4 * nb * n_chunks, st));
+    bary_partial_kernel<<<dim3(n_chunks, (nb + kBaryGroup - 1) / kBaryGroup), kBaryThreads, 0, st>>>(
+        cols, nb, log_size, w, partial);
+    note_launch();
+    bary_final_kernel<<<(4 * nb + 255) / 256, 256, 0, st>>>(partial, n_chunks, nb, d_out + 4 * b0);
+    note_launch();
+    cudaError_t e = cudaGetLastError();
+    const cudaError_t ef = cudaFreeAsync(partial, st);
+    if (e == cudaSuccess) e = ef;
+    if (e != cudaSuccess) return from_cuda(e, "barycentric_eval");
   }
   return CS_OK;
 }

@@ -214,6 +214,20 @@ __device__ __forceinline__ void add_base(uint64_t* acc, const uint4& w, uint32_t
   acc[3] += m31_mul(w.w, cons);
 }
 
+// Lazy accumulation of weight x constraint products: each product is below 2^62 and is added
+// unreduced (one 64-bit multiply-add per coordinate); fold_acc brings the sums back below 2^34,
+// so three products may be added between folds without overflow.
+__device__ __forceinline__ void add_base_lazy(uint64_t* acc, const uint4& w, uint32_t cons) {
+  acc[0] += (uint64_t)w.x * cons;
+  acc[1] += (uint64_t)w.y * cons;
+  acc[2] += (uint64_t)w.z * cons;
+  acc[3] += (uint64_t)w.w * cons;
+}
+__device__ __forceinline__ void fold_acc(uint64_t* acc) {
+#pragma unroll
+  for (int c = 0; c < 4; c++) acc[c] = (acc[c] & P) + (acc[c] >> 31);
+}
+
 __global__ void __launch_bounds__(128) poseidon_composition_kernel(const __grid_constant__ CompParams p,
                                                                     const uint4* __restrict__ rc, uint32_t* a0,
                                                                     uint32_t* a1, uint32_t* a2, uint32_t* a3) {
@@ -281,6 +295,89 @@ __global__ void __launch_bounds__(128) poseidon_composition_kernel(const __grid_
     a1[r] = m31_add(a1[r], m31_mul(row.a.b, d));
     a2[r] = m31_add(a2[r], m31_mul(row.b.a, d));
     a3[r] = m31_add(a3[r], m31_mul(row.b.b, d));
+  }
+}
+
+
+// One block = 32 rows x the 8 instances: warp k evaluates instance k's 142 round constraints and
+// its LogUp batch for 32 consecutive rows (lane = row), the eight partial sums meet in shared
+// memory, and warp c < 4 adds coordinate c of the row sums times the denominator.
+__global__ void __launch_bounds__(256, 3) poseidon_composition_split_kernel(
+    const __grid_constant__ CompParams p, const uint4* __restrict__ rc, uint32_t* a0, uint32_t* a1, uint32_t* a2,
+    uint32_t* a3) {
+  __shared__ uint4 s_rc[kConstraints];
+  __shared__ uint32_t s_part[kInstances][4][32];
+  for (int i = threadIdx.x; i < kConstraints; i += blockDim.x) s_rc[i] = rc[i];
+  __syncthreads();
+  const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t n = 1u << p.eval_log;
+  uint32_t* const acc_out[4] = {a0, a1, a2, a3};
+  for (uint32_t base = blockIdx.x * 32; base < n; base += gridDim.x * 32) {
+    const uint32_t r = base + lane;
+    uint64_t acc[4] = {0, 0, 0, 0};
+    const uint32_t* const* col = p.trace + k * kColsPerRep;
+    uint32_t s[kState];
+#pragma unroll
+    for (int i = 0; i < kState; i++) s[i] = __ldg(col[i] + r);
+    const qm31 d0 = combine(p.lk, s);
+    int c = kState;
+    uint32_t idx = k * kRoundConstraints;
+#pragma unroll 1
+    for (int round = 0; round < 2 * kHalfFull; round++) {
+      if (round == kHalfFull) {
+#pragma unroll 1
+        for (int q = 0; q < kPartial; q++) {
+          s[0] = m31_add(s[0], kRoundConst);
+          internal_matrix(s);
+          const uint32_t m = __ldg(col[c++] + r);
+          add_base_lazy(acc, s_rc[idx++], m31_sub(pow5(s[0]), m));
+          fold_acc(acc);
+          s[0] = m;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kState; i++) s[i] = m31_add(s[i], kRoundConst);
+      external_matrix(s);
+#pragma unroll
+      for (int i = 0; i < kState; i++) {
+        const uint32_t m = __ldg(col[c + i] + r);
+        add_base_lazy(acc, s_rc[idx + i], m31_sub(pow5(s[i]), m));
+        if (i % 3 == 2 || i == kState - 1) fold_acc(acc);
+        s[i] = m;
+      }
+      c += kState;
+      idx += kState;
+    }
+    // LogUp batch k (finalize_logup_batched, crates/constraint-framework/src/lib.rs:185-222)
+    const qm31 d1 = combine(p.lk, s);
+    const uint32_t* const* ic = p.inter + 4 * k;
+    const qm31 cur = qm31_make(__ldg(ic[0] + r), __ldg(ic[1] + r), __ldg(ic[2] + r), __ldg(ic[3] + r));
+    qm31 diff = cur;
+    if (k > 0) {
+      const uint32_t* const* pc = ic - 4;
+      diff = qm31_sub(diff, qm31_make(__ldg(pc[0] + r), __ldg(pc[1] + r), __ldg(pc[2] + r), __ldg(pc[3] + r)));
+    }
+    if (k == kInstances - 1) {
+      const uint32_t pr = prev_row(r, p.trace_log, p.eval_log);
+      const qm31 prev = qm31_make(__ldg(ic[0] + pr), __ldg(ic[1] + pr), __ldg(ic[2] + pr), __ldg(ic[3] + pr));
+      diff = qm31_add(qm31_sub(diff, prev), p.shift);
+    }
+    const qm31 cons = qm31_sub(qm31_mul(diff, qm31_mul(d0, d1)), qm31_sub(d1, d0));
+    const uint4 w = s_rc[kInstances * kRoundConstraints + k];
+    const qm31 part = qm31_add(qm31_make(fold64(acc[0]), fold64(acc[1]), fold64(acc[2]), fold64(acc[3])),
+                               qm31_mul(qm31_make(w.x, w.y, w.z, w.w), cons));
+    s_part[k][0][lane] = part.a.a;
+    s_part[k][1][lane] = part.a.b;
+    s_part[k][2][lane] = part.b.a;
+    s_part[k][3][lane] = part.b.b;
+    __syncthreads();
+    if (k < 4) {
+      uint32_t v = s_part[0][k][lane];
+#pragma unroll
+      for (int j = 1; j < kInstances; j++) v = m31_add(v, s_part[j][k][lane]);
+      acc_out[k][r] = m31_add(acc_out[k][r], m31_mul(v, p.den[r >> p.trace_log]));
+    }
+    __syncthreads();
   }
 }
 
@@ -396,8 +493,11 @@ extern "C" cs_status cs_poseidon_composition(const uint32_t* const* h_trace, con
   cudaError_t e = cudaMemcpyAsync(d_rc, h_rc, sizeof(uint4) * kConstraints, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     const uint32_t n = 1u << eval_log;
-    poseidon_composition_kernel<<<grid_for(n, 128), 128, 0, st>>>(p, d_rc, h_accum[0], h_accum[1], h_accum[2],
-                                                                  h_accum[3]);
+    if (n >= 32)
+      poseidon_composition_split_kernel<<<std::min<uint32_t>(n / 32, 152u * 16), 256, 0, st>>>(
+          p, d_rc, h_accum[0], h_accum[1], h_accum[2], h_accum[3]);
+    else
+      poseidon_composition_kernel<<<1, 128, 0, st>>>(p, d_rc, h_accum[0], h_accum[1], h_accum[2], h_accum[3]);
     note_launch();
     e = cudaGetLastError();
   }

@@ -316,6 +316,11 @@ class Reads:
         self.items.append(("col", col, np.asarray(idx, dtype=np.int64)))
         return len(self.items) - 1
 
+    def block(self, cols, idx) -> int:
+        """The same positions of several columns: the result is (len(cols), len(idx))."""
+        self.items.append(("cols", list(cols), np.asarray(idx, dtype=np.int64)))
+        return len(self.items) - 1
+
     def digests(self, tree, layer_log: int, nodes) -> int:
         self.items.append(("dig", tree, layer_log, np.asarray(nodes, dtype=np.int64)))
         return len(self.items) - 1
@@ -354,15 +359,22 @@ class MerkleDecommit:
     def __init__(self, reads: Reads, tree, query_positions, columns, ops):
         L = tree.height
         q = np.asarray(query_positions, dtype=np.int64)
+        # columns of one log size read the same positions: one read per run of equal sizes
         self.value_handles = []
-        for col in columns:
-            shift = L - ops.log_size(col)
-            self.value_handles.append(reads.values(col, ((q >> (shift + 1)) << 1) + (q & 1)))
+        i = 0
+        while i < len(columns):
+            ls = ops.log_size(columns[i])
+            j = i + 1
+            while j < len(columns) and ops.log_size(columns[j]) == ls:
+                j += 1
+            shift = L - ls
+            self.value_handles.append(reads.block(columns[i:j], ((q >> (shift + 1)) << 1) + (q & 1)))
+            i = j
         self.witness_handles = [reads.digests(tree, k, nodes) for k, nodes in merkle_witness_nodes(L, q)]
         self.reads = reads
 
     def result(self):
-        queried = [self.reads[h].tolist() for h in self.value_handles]
+        queried = [row for h in self.value_handles for row in self.reads[h].tolist()]
         witness = []
         for h in self.witness_handles:
             b = np.ascontiguousarray(self.reads[h], dtype="<u4").tobytes()
@@ -608,8 +620,9 @@ def sample_values(ops, columns, sample_points, lifting: int):
         vals = [[None] * len(p_) for p_ in pts]
         groups = {}
         for ci, col in enumerate(tree_cols):
+            ls = ops.log_size(col)
             for si, pt in enumerate(pts[ci]):
-                groups.setdefault((ops.log_size(col), pt), []).append((ci, si))
+                groups.setdefault((ls, pt), []).append((ci, si))
         for (log_size, pt), members in groups.items():
             for _ in range(lifting - log_size):
                 pt = q_double_point(pt)
@@ -638,35 +651,31 @@ def compute_fri_quotients(ops, columns, sample_points, sampled, random_coeff, li
     combined into the FRI quotient column."""
     n_samples = sum(len(c) + (1 if len(c) == 2 else 0) for tree in sampled for c in tree)
     pows = iter(secure_powers(random_coeff, n_samples))
-    entries = []  # (column, point, value, random power) in tree/column order
+    entries = []  # (log size, column, point, value, random power) in tree/column order
     for tree_cols, pts, vals in zip(columns, sample_points, sampled):
         for col, cp, cv in zip(tree_cols, pts, vals):
+            ls = ops.log_size(col)
             if len(cp) == 2:
                 # build_samples_with_randomness_and_periodicity (crates/stwo/src/core/pcs/quotients.rs:274-319):
                 # a column sampled at (previous row, point) also opens the point shifted by the
                 # period G_(lifting - log size), with the point's value, first
-                period = m31_subgroup_generator(lifting - ops.log_size(col))
-                entries.append((col, qpoint_add_m31(cp[1], period), cv[1], next(pows)))
+                period = m31_subgroup_generator(lifting - ls)
+                entries.append((ls, col, qpoint_add_m31(cp[1], period), cv[1], next(pows)))
             for p_, v_ in zip(cp, cv):
-                entries.append((col, p_, v_, next(pows)))
+                entries.append((ls, col, p_, v_, next(pows)))
     # stable sort by column log size, group by size, batch by point in insertion order
-    entries_sorted = sorted(enumerate(entries), key=lambda e: ops.log_size(e[1][0]))
+    by_size = {}
+    for e in entries:
+        by_size.setdefault(e[0], []).append(e[1:])
     accs = []  # (point, partial numerator column, first linear term)
-    i = 0
-    while i < len(entries_sorted):
-        ls = ops.log_size(entries_sorted[i][1][0])
-        j = i
-        while j < len(entries_sorted) and ops.log_size(entries_sorted[j][1][0]) == ls:
-            j += 1
-        group = [e[1] for e in entries_sorted[i:j]]
+    for ls in sorted(by_size):
         batches = {}
-        for col, p_, v_, rp in group:
+        for col, p_, v_, rp in by_size[ls]:
             batches.setdefault(p_, []).append((col, v_, rp))
         for p_, items in batches.items():
             coeffs = line_coeffs_v(p_[1], [v_ for _, v_, _ in items], [rp for _, _, rp in items])
             part, first_linear = ops.accumulate_numerators([c for c, _, _ in items], coeffs, log_blowup)
             accs.append((p_, part, tuple(int(x) for x in first_linear)))
-        i = j
     # group per sample point (sorted by (x, y)), lift and accumulate ascending sizes
     per_point = {}
     for p_, part, fl in accs:
@@ -827,7 +836,21 @@ class GpuOps:
         """Column values ("col", col, idx) and Merkle digests ("dig", tree, layer_log, nodes), read in
         one cs_gather_u32 call; digests come back as (n, 8) words."""
         tensors, slot_of, slots, idx, sizes = [], {}, [], [], []
+        def slot(t):
+            key = (t.data_ptr(), t.numel())
+            if key not in slot_of:
+                slot_of[key] = len(tensors)
+                tensors.append(t)
+            return slot_of[key]
+
         for it in items:
+            if it[0] == "cols":
+                ix = np.asarray(it[2], dtype=np.int64)
+                sl = np.array([slot(c.data) for c in it[1]], np.uint32)
+                slots.append(np.repeat(sl, ix.size))
+                idx.append(np.tile(ix, len(it[1])).astype(np.uint32))
+                sizes.append(sl.size * ix.size)
+                continue
             if it[0] == "col":
                 t = it[1].data
                 ix = np.asarray(it[2], dtype=np.int64)
@@ -835,11 +858,7 @@ class GpuOps:
                 t = it[1].t.layer(it[2])
                 nodes = np.asarray(it[3], dtype=np.int64)
                 ix = (nodes[:, None] * 8 + np.arange(8)).reshape(-1)
-            key = (t.data_ptr(), t.numel())
-            if key not in slot_of:
-                slot_of[key] = len(tensors)
-                tensors.append(t)
-            slots.append(np.full(ix.size, slot_of[key], np.uint32))
+            slots.append(np.full(ix.size, slot(t), np.uint32))
             idx.append(ix.astype(np.uint32))
             sizes.append(ix.size)
         if not items:
@@ -848,7 +867,11 @@ class GpuOps:
         out, off = [], 0
         for it, n in zip(items, sizes):
             w = words[off:off + n]
-            out.append(w if it[0] == "col" else w.reshape(-1, 8))
+            if it[0] == "cols":
+                w = w.reshape(len(it[1]), -1)
+            elif it[0] == "dig":
+                w = w.reshape(-1, 8)
+            out.append(w)
             off += n
         return out
 
