@@ -50,7 +50,7 @@ def workload_name():
 # (profiles/launch_list_commit_stage_256x2^20.md): one merkle_leaves_kernel launch, and the two
 # fft_tile_kernel launches of one evaluate
 LEAVES_TRAFFIC_BYTES = 4425.2e6
-EVALUATE_TRAFFIC_BYTES = 13925.3e6
+EVALUATE_TRAFFIC_BYTES = 13935.0e6
 
 
 def set_shape(n_cols: int, log_rows: int):
