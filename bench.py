@@ -407,19 +407,26 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
     return out
 
 
-def serving_leg(n_requests: int = 24, rate_per_s: float = 40.0):
-    """Config 5 (Wide-Fibonacci only): a seeded Poisson stream of proofs with
-    log_n_rows uniform in [12, 20], served with 4 concurrent workers and with
-    one request at a time (plain)."""
+def serving_leg(n_requests: int = 24, rate_per_s: float = 200.0):
+    """Config 5: a seeded Poisson stream of proof requests, half Wide-Fibonacci (100 columns) and
+    half Poseidon2 (8 permutations per row), log_n_rows uniform in [12, 20], arriving faster than
+    they can be served (so proofs/s measures capacity). Three arms on the same stream: the plain
+    path (one request at a time, one launch per column per stage), the batched path one request at
+    a time, and the served form (4 worker processes with their own CUDA contexts, HBM-budget
+    admission, batched stage launches)."""
     from proving_gb300 import serving
-    out = {"workload": f"{n_requests} Wide-Fibonacci proofs (100 cols), log_n_rows uniform in [12, 20], Poisson "
-                       f"arrivals at {rate_per_s}/s; Poseidon2 requests not included",
-           "arms": "plain: one request at a time, one launch per column per stage; batched_serial: one request at "
-                   "a time, batched stage launches; served: 4 concurrent requests on separate streams with HBM-budget "
-                   "admission, batched stage launches"}
+    out = {"workload": f"{n_requests} requests, 50% Wide-Fibonacci (100 cols) / 50% Poseidon2 (8 perms/row), "
+                       f"log_n_rows uniform in [12, 20], Poisson arrivals at {rate_per_s}/s",
+           "arms": "plain: 1 worker, one launch per column per stage; batched_serial: 1 worker, batched stage "
+                   "launches; served: 4 worker processes (own CUDA context and stream each), HBM-budget "
+                   "admission in arrival order, batched stage launches"}
     for name, workers, plain in (("plain", 1, True), ("batched_serial", 1, False), ("served", 4, False)):
-        reqs = serving.poisson_requests(n_requests, rate_per_s, 12, 20, seed=5)
-        done, wall = serving.run_stream(workers, reqs, max_log=20, plain=plain)
+        reqs = serving.poisson_requests(n_requests, rate_per_s, 12, 20, seed=5, poseidon_share=0.5)
+        svc = serving.ProcessProverService(n_workers=workers, max_log_n_rows=20, plain=plain)
+        try:
+            done, wall = svc.run(reqs)
+        finally:
+            svc.close()
         out[name] = serving.summarize(done, wall)
     out["served_speedup"] = round(out["served"]["proofs_per_s"] / out["plain"]["proofs_per_s"], 3)
     return out

@@ -38,3 +38,21 @@ def test_admission_respects_the_budget():
     done.sort(key=lambda r: r.admitted)
     for prev, nxt in zip(done, done[1:]):
         assert nxt.admitted >= prev.done - 1e-3
+
+
+def test_worker_processes_give_the_same_proofs():
+    # the process service (own CUDA context per worker) returns the bytes the in-process prover
+    # gives alone, for both AIRs
+    reqs = [serving.ProofRequest(0, 8, 11), serving.ProofRequest(1, 5, 12, "poseidon"),
+            serving.ProofRequest(2, 9, 13), serving.ProofRequest(3, 4, 14, "poseidon")]
+    svc = serving.ProcessProverService(n_workers=2, max_log_n_rows=10, warm_logs=(("wide_fib", 6),))
+    try:
+        done, _ = svc.run([(0.0, r) for r in reqs])
+    finally:
+        svc.close()
+    assert all(r.error is None for r in done), [r.error for r in done]
+    alone = [serving.ProofRequest(r.request_id, r.log_n_rows, r.seed, r.kind) for r in reqs]
+    alone_done, _ = serving.run_stream(1, [(0.0, r) for r in alone], max_log=10)
+    want = {r.request_id: r.proof_bytes() for r in alone_done}
+    for r in done:
+        assert r.proof_bytes() == want[r.request_id]
