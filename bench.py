@@ -170,12 +170,15 @@ class CommitStage:
     def stream(self):
         return ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
 
-    def step(self, ev=None):
-        """One commit-stage pass. ev: optional list of 6 CUDA events bracketing the stages."""
+    def step(self, ev=None, inputs=None):
+        """One commit-stage pass. ev: optional list of 6 CUDA events bracketing the stages.
+        inputs: optional (trace pointer table, FRI column pointer table) to read instead of the
+        resident inputs (the double-buffered end-to-end leg)."""
         call, st = self.L.call, self.stream()
+        t_evals, fri_src = inputs if inputs else (self.t_evals, self.fri_tabs[0])
         rec = (lambda i: ev[i].record()) if ev else (lambda i: None)
         rec(0)
-        call("cs_interpolate_columns_into", self.t_evals, self.t_coeffs, N_COLS, LOG_ROWS, self.itw.data_ptr(),
+        call("cs_interpolate_columns_into", t_evals, self.t_coeffs, N_COLS, LOG_ROWS, self.itw.data_ptr(),
              self.tw_log, st)
         rec(1)
         call("cs_evaluate_columns", self.t_coeffs, self.t_ext, N_COLS, LOG_ROWS, LOG_EXT, self.tw.data_ptr(),
@@ -186,7 +189,7 @@ class CommitStage:
         for k in range(LOG_EXT, 0, -1):
             call("cs_merkle_build_next_layer", self.layer_ptr[LOG_EXT - k], k - 1, self.layer_ptr[LOG_EXT - k + 1], st)
         rec(4)
-        call("cs_fold_circle_into_line", self.fri_tabs[0], FRI_LOG, self.alpha_tabs[0], self.fri_tabs[1],
+        call("cs_fold_circle_into_line", fri_src, FRI_LOG, self.alpha_tabs[0], self.fri_tabs[1],
              self.itw.data_ptr(), self.tw_log, st)
         for j in range(1, FRI_LOG):
             call("cs_fold_line", self.fri_tabs[j], FRI_LOG - j, self.alpha_tabs[j], self.fri_tabs[j + 1],
@@ -486,40 +489,77 @@ def run_gpu(args):
     max_ms = float(t.item())
     value = world * args.steps / (max_ms / 1e3)
 
-    # ---- e2e through the C ABI with host buffers
+    # ---- e2e through the C ABI with host buffers: every step copies its trace and FRI column from
+    # pinned host memory and reads its Merkle root and last FRI value back. Inputs are double
+    # buffered: step k + 1's copy runs on a copy stream while step k computes.
     host_evals = torch.empty((N_COLS, 1 << LOG_ROWS), dtype=torch.int32, pin_memory=True)
     host_evals.copy_(cs.evals.cpu())
     host_fri = torch.empty((4, 1 << FRI_LOG), dtype=torch.int32, pin_memory=True)
     host_fri.copy_(cs.fri_src.cpu())
-    host_out = torch.empty(16, dtype=torch.int32, pin_memory=True)
+    host_out = torch.empty((max(args.steps, args.warmup, 1), 16), dtype=torch.int32, pin_memory=True)
     h2d = host_evals.numel() * 4 + host_fri.numel() * 4
     d2h = 32 + 16
+    evals2, fri2 = torch.empty_like(cs.evals), torch.empty_like(cs.fri_src)
+    vp = ctypes.c_void_p
+    buffers = [(cs.evals, cs.fri_src, (cs.t_evals, cs.fri_tabs[0])),
+               (evals2, fri2, ((vp * N_COLS)(*[evals2[i].data_ptr() for i in range(N_COLS)]),
+                               (vp * 4)(*[fri2[k].data_ptr() for k in range(4)])))]
+    copy_stream = torch.cuda.Stream()
 
-    def e2e_step():
-        st = cs.stream()
-        _lib.call("cs_memcpy_h2d", cs.evals.data_ptr(), host_evals.data_ptr(), host_evals.numel() * 4, st)
-        _lib.call("cs_memcpy_h2d", cs.fri_src.data_ptr(), host_fri.data_ptr(), host_fri.numel() * 4, st)
-        cs.step()
-        _lib.call("cs_memcpy_d2h", host_out.data_ptr(), cs.layers[-1].data_ptr(), 32, st)
-        _lib.call("cs_memcpy_d2h", host_out.data_ptr() + 32, cs.fri_layers[-1].data_ptr(), 16, st)
-        _lib.call("cs_stream_synchronize", st)
+    def e2e_run(n_steps: int, lat=None, start=None):
+        comp = torch.cuda.current_stream()
+        if start is not None:
+            copy_stream.wait_event(start)  # the first copy is inside the timed region
+        st_copy, st_comp = vp(copy_stream.cuda_stream), vp(comp.cuda_stream)
+        copied = [torch.cuda.Event() for _ in range(2)]
+        freed = [torch.cuda.Event() for _ in range(2)]
+
+        starts, ends = [], []
+
+        def copy_in(b):
+            dev_evals, dev_fri, _ = buffers[b]
+            if lat is not None:
+                starts.append(torch.cuda.Event(enable_timing=True))
+                starts[-1].record(copy_stream)
+            _lib.call("cs_memcpy_h2d", dev_evals.data_ptr(), host_evals.data_ptr(), h2d - host_fri.numel() * 4,
+                      st_copy)
+            _lib.call("cs_memcpy_h2d", dev_fri.data_ptr(), host_fri.data_ptr(), host_fri.numel() * 4, st_copy)
+            copied[b].record(copy_stream)
+
+        copy_in(0)
+        for k in range(n_steps):
+            b = k % 2
+            if k + 1 < n_steps:
+                if k >= 1:
+                    copy_stream.wait_event(freed[1 - b])
+                copy_in(1 - b)
+            comp.wait_event(copied[b])
+            cs.step(inputs=buffers[b][2])
+            freed[b].record(comp)
+            _lib.call("cs_memcpy_d2h", host_out[k].data_ptr(), cs.layers[-1].data_ptr(), 32, st_comp)
+            _lib.call("cs_memcpy_d2h", host_out[k].data_ptr() + 32, cs.fri_layers[-1].data_ptr(), 16, st_comp)
+            if lat is not None:
+                ends.append(torch.cuda.Event(enable_timing=True))
+                ends[-1].record(comp)
+        _lib.call("cs_stream_synchronize", st_comp)
+        if lat is not None:
+            # per step: from the start of its input copy to its result in host memory
+            lat.extend(a.elapsed_time(e) for a, e in zip(starts, ends))
 
     e_lat = [float("nan")]
     e2e_ms = float("nan")
     if not args.skip_e2e:
-        for _ in range(max(1, args.warmup)):
-            e2e_step()
+        e2e_run(max(1, args.warmup))
         barrier()
         e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e_lat = []
         e_start.record()
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            e2e_step()
-            e_lat.append((time.perf_counter() - t0) * 1e3)
+        e2e_run(args.steps, e_lat, e_start)
         e_end.record()
         barrier()
         e2e_ms = e_start.elapsed_time(e_end)
+        # the root read back by the last step is the resident step's root
+        assert bytes(host_out[args.steps - 1, :8].numpy().astype("<i4").tobytes()) == cs.root()
     t = torch.tensor([e2e_ms], device="cuda")
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
