@@ -358,6 +358,22 @@ def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: in
     return lat
 
 
+def int_peaks(torch):
+    """Measured integer-pipe throughput (cs_int_peak_probe): thread operations per second for
+    3-input adds, 3-input logic and funnel shifts (the ALU pipe) and multiply-adds (the FMA pipe),
+    the denominator of the integer-bound kernels."""
+    from proving_gb300 import _lib
+    blocks, iters = 152 * 8, 1 << 14
+    out = torch.empty(blocks * 256, dtype=torch.int32, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    res = {}
+    for kind, name in enumerate(("iadd3", "lop3", "shf", "imad")):
+        fn = lambda: _lib.call("cs_int_peak_probe", kind, blocks, iters, out.data_ptr(), st)
+        ms = time_steps(torch, fn, 3, 2)
+        res[f"{name}_tops"] = round(blocks * 256 * 8 * iters / (ms / 1e3) / 1e12, 3)
+    return res
+
+
 def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
     """Config 4: the Poseidon2 AIR at 8 permutations per row, 2^log_n_rows rows (1264 trace
     columns), log_blowup_factor 1, 70 queries, pow 10, through prove_poseidon + prove_ex on the
@@ -565,6 +581,7 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     e2e_value = world * args.steps / (float(t.item()) / 1e3)
 
+    peaks_int = int_peaks(torch)
     wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
     bvp = batched_vs_plain(torch, cs) if not args.skip_plain else None
     serving_res = serving_leg() if not args.skip_serving else None
@@ -615,7 +632,13 @@ def run_gpu(args):
         "int_pipe": {"kernel": "merkle_leaves_kernel", "compressions_per_launch": leaf_comp,
                      "gcompressions_per_s": ff(leaf_comp / (leaf_ms / 1e3) / 1e9),
                      "int_ops_per_compression": 1120,
-                     "tops_achieved": ff(leaf_comp * 1120 / (leaf_ms / 1e3) / 1e12)},
+                     "tops_achieved": ff(leaf_comp * 1120 / (leaf_ms / 1e3) / 1e12),
+                     "alu_peak_tops_measured": max(peaks_int["iadd3_tops"], peaks_int["lop3_tops"],
+                                                   peaks_int["shf_tops"]),
+                     "fma_peak_tops_measured": peaks_int["imad_tops"],
+                     "note": "1120 = 10 rounds x 8 G x 14 primitive 32-bit ops; the kernel issues part of the "
+                             "additions on the FMA pipe (IMAD), the XORs and rotations on the ALU pipe"},
+        "int_peaks": peaks_int,
         "wide_fib_prove": ({"workload": "Wide-Fibonacci 100 cols x 2^14 rows, blowup 2, 70 queries, pow 10, "
                                          "full prove (trace generated on device)",
                             "proofs_per_s": ff(1e3 / statistics.mean(wf_lat)),

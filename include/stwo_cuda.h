@@ -322,6 +322,16 @@ cs_status cs_poseidon_composition(const uint32_t *const *h_trace, const uint32_t
                                   uint32_t trace_log, const uint32_t lookup[8], const uint32_t claimed_sum[4],
                                   const uint32_t *h_rc, uint32_t *const h_accum[4], cs_stream stream);
 
+/* ------------------------------------------------------- measurement */
+
+/* Integer-pipe throughput probe (no counterpart in the reference): `blocks` x
+   256 threads each run 8 independent chains of `iters` operations of one kind
+   (0: 3-input add, 1: 3-input logic, 2: funnel shift, 3: multiply-add) and
+   write one word per thread to d_out (blocks x 256 words). The caller times
+   the launch; ops = blocks x 256 x 8 x iters. The measured denominator for
+   the integer-bound kernels (FFT butterflies, Blake2s). */
+cs_status cs_int_peak_probe(uint32_t kind, uint32_t blocks, uint32_t iters, uint32_t *d_out, cs_stream stream);
+
 /* ------------------------------------------------------- decommitment */
 
 /* Batched reads for decommitment. Replaces the element-wise Column::at reads
