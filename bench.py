@@ -477,6 +477,14 @@ def run_gpu(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    # the FFT pass plans for this workload's two shapes, picked by the autotuner before timing
+    from proving_gb300 import autotune
+    tuned = autotune.tune([(True, LOG_ROWS, LOG_ROWS), (False, LOG_EXT, LOG_ROWS)], n_cols=N_COLS)
+    fft_plans = {f"{'interpolate' if inv else 'evaluate'} 2^{log_n} ({n} layers)":
+                 {"default": list(r["default"]), "best": list(r["best"]),
+                  "default_ms": round(r["ms"][tuple(r["default"])], 4), "best_ms": round(r["ms"][r["best"]], 4),
+                  "candidates": len(r["ms"])}
+                 for (inv, log_n, n), r in tuned.items()}
     cs = CommitStage(torch)
     for _ in range(args.warmup):
         cs.step()
@@ -639,6 +647,7 @@ def run_gpu(args):
                      "note": "1120 = 10 rounds x 8 G x 14 primitive 32-bit ops; the kernel issues part of the "
                              "additions on the FMA pipe (IMAD), the XORs and rotations on the ALU pipe"},
         "int_peaks": peaks_int,
+        "fft_plans": fft_plans,
         "wide_fib_prove": ({"workload": "Wide-Fibonacci 100 cols x 2^14 rows, blowup 2, 70 queries, pow 10, "
                                          "full prove (trace generated on device)",
                             "proofs_per_s": ff(1e3 / statistics.mean(wf_lat)),

@@ -112,6 +112,20 @@ cs_status cs_evaluate_columns(const uint32_t *const *h_coeffs, uint32_t *const *
                               uint32_t log_coeffs, uint32_t log_size, const uint32_t *d_twiddles,
                               uint32_t twiddle_log_size, cs_stream stream);
 
+/* FFT pass plans (no counterpart in the reference; the reference's SIMD FFT
+   fixes its radix split in code). A column of 2^log_n words whose FFT runs
+   n_layers layers (interpolate: n_layers = log_n; evaluate: the coefficient
+   log size) is processed in passes of consecutive layers, each staged once
+   through shared memory. cs_fft_set_plan installs the pass sizes for one
+   (direction, log_n, n_layers) shape, process-wide (first pass 1..12 layers and
+   at least 3 when more follow, later passes 1..11, summing to n_layers);
+   n_passes = 0 removes it. Results do not depend on the plan, only speed does.
+   cs_fft_get_plan returns the plan in use (up to 32 passes). Thread-safe. */
+cs_status cs_fft_set_plan(uint32_t inverse, uint32_t log_n, uint32_t n_layers, const uint32_t *pass_layers,
+                          uint32_t n_passes);
+cs_status cs_fft_get_plan(uint32_t inverse, uint32_t log_n, uint32_t n_layers, uint32_t *pass_layers,
+                          uint32_t *n_passes);
+
 /* ------------------------------------------------------- lifted Merkle */
 
 /* MerkleOpsLifted::build_leaves (crates/stwo/src/prover/vcs_lifted/ops.rs:14-15;

@@ -63,6 +63,8 @@ SIGNATURES = {
     "cs_poseidon_interaction": [vp, u32, vp, vp, vp, vp],
     "cs_poseidon_composition": [vp, vp, u32, u32, vp, vp, vp, vp, vp],
     "cs_int_peak_probe": [u32, u32, u32, vp, vp],
+    "cs_fft_set_plan": [u32, u32, u32, vp, u32],
+    "cs_fft_get_plan": [u32, u32, u32, vp, vp],
 }
 _RESTYPES = {"cs_last_error": ctypes.c_char_p, "cs_version": ctypes.c_char_p,
              "cs_kernel_launch_count": ctypes.c_uint64}

@@ -21,6 +21,9 @@
 // from the same coefficients; replicas of a tile are adjacent CTAs and share
 // the read through L2. Interpolate's last pass folds in the 1/n scaling.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "common.cuh"
@@ -385,16 +388,38 @@ struct PassPlan {
   uint32_t lo, hi, c, outer;  // layers [lo, hi); c = extra tile bits
 };
 
+// Pass splits installed by an autotuner (cs_fft_set_plan), per (direction, column log size,
+// number of layers); the default split below is used for every other shape.
+struct PlanKey {
+  uint32_t inverse, log_n, n_layers;
+  bool operator<(const PlanKey& o) const {
+    return std::tie(inverse, log_n, n_layers) < std::tie(o.inverse, o.log_n, o.n_layers);
+  }
+};
+std::mutex g_plan_mutex;
+std::map<PlanKey, std::vector<uint32_t>> g_plans;
+
+constexpr uint32_t kMaxContiguousPass = 12, kMaxStridedPass = 11, kStridedC = 3;
+
 // Splits layers [0, n_layers) of a column of log size log_n into passes of at
 // most 12 layers (11 for strided passes); the first pass is contiguous.
-std::vector<PassPlan> plan_passes(uint32_t log_n, uint32_t n_layers) {
+std::vector<PassPlan> plan_passes(bool inverse, uint32_t log_n, uint32_t n_layers) {
   std::vector<PassPlan> plan;
-  uint32_t n_pass = 1;
-  while (n_layers > 12 + (n_pass - 1) * 11) n_pass++;
-  std::vector<uint32_t> sizes(n_pass);
-  const uint32_t base = n_layers / n_pass, extra = n_layers % n_pass;
-  // the contiguous first pass takes the remainder, so strided passes stay <= 11
-  for (uint32_t i = 0; i < n_pass; i++) sizes[i] = base + (i < extra ? 1 : 0);
+  std::vector<uint32_t> sizes;
+  {
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    auto it = g_plans.find(PlanKey{inverse ? 1u : 0u, log_n, n_layers});
+    if (it != g_plans.end()) sizes = it->second;
+  }
+  if (sizes.empty()) {
+    uint32_t n_pass = 1;
+    while (n_layers > kMaxContiguousPass + (n_pass - 1) * kMaxStridedPass) n_pass++;
+    sizes.resize(n_pass);
+    const uint32_t base = n_layers / n_pass, extra = n_layers % n_pass;
+    // the contiguous first pass takes the remainder, so strided passes stay <= 11
+    for (uint32_t i = 0; i < n_pass; i++) sizes[i] = base + (i < extra ? 1 : 0);
+  }
+  const uint32_t n_pass = (uint32_t)sizes.size();
   uint32_t lo = 0;
   for (uint32_t i = 0; i < n_pass; i++) {
     PassPlan pp;
@@ -407,7 +432,7 @@ std::vector<PassPlan> plan_passes(uint32_t log_n, uint32_t n_layers) {
       pp.c = std::min(want, log_n - pp.hi);
     } else {
       pp.outer = 0;  // strided tile: 8 neighbouring groups (32-byte runs in HBM)
-      pp.c = 3;
+      pp.c = kStridedC;
     }
     plan.push_back(pp);
     lo = pp.hi;
@@ -503,7 +528,7 @@ cs_status run_fft(const uint32_t* const* srcs, uint32_t* const* dsts, uint32_t n
       continue;
     }
     const uint32_t n_layers = inverse ? log_n : log_src;
-    std::vector<PassPlan> plan = plan_passes(log_n, n_layers);
+    std::vector<PassPlan> plan = plan_passes(inverse, log_n, n_layers);
     FftPass p;
     p.log_n = log_n;
     p.tw = tw;
@@ -613,4 +638,41 @@ extern "C" cs_status cs_evaluate_columns(const uint32_t* const* h_coeffs, uint32
   }
   return run_fft(h_coeffs, h_evals, n_cols, log_coeffs, log_size, false, d_twiddles, twiddle_log_size,
                  to_stream(stream));
+}
+
+extern "C" cs_status cs_fft_set_plan(uint32_t inverse, uint32_t log_n, uint32_t n_layers, const uint32_t* pass_layers,
+                                     uint32_t n_passes) {
+  CS_CHECK_ARG(log_n >= 3 && log_n <= 30 && n_layers >= 1 && n_layers <= log_n, "fft_set_plan: bad shape %u/%u",
+               log_n, n_layers);
+  const PlanKey key{inverse ? 1u : 0u, log_n, n_layers};
+  if (n_passes == 0) {
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    g_plans.erase(key);
+    return CS_OK;
+  }
+  CS_CHECK_ARG(pass_layers != nullptr && n_passes <= 32, "fft_set_plan: bad pass list");
+  uint32_t total = 0;
+  for (uint32_t i = 0; i < n_passes; i++) {
+    const uint32_t t = pass_layers[i];
+    CS_CHECK_ARG(t >= 1 && t <= (i == 0 ? kMaxContiguousPass : kMaxStridedPass),
+                 "fft_set_plan: pass %u has %u layers", i, t);
+    total += t;
+  }
+  CS_CHECK_ARG(total == n_layers, "fft_set_plan: passes cover %u of %u layers", total, n_layers);
+  // a strided pass keeps kStridedC low index bits in its tile, so it must start at layer >= kStridedC
+  CS_CHECK_ARG(n_passes == 1 || pass_layers[0] >= kStridedC, "fft_set_plan: first pass below %u layers",
+               kStridedC);
+  std::lock_guard<std::mutex> lock(g_plan_mutex);
+  g_plans[key] = std::vector<uint32_t>(pass_layers, pass_layers + n_passes);
+  return CS_OK;
+}
+
+extern "C" cs_status cs_fft_get_plan(uint32_t inverse, uint32_t log_n, uint32_t n_layers, uint32_t* pass_layers,
+                                     uint32_t* n_passes) {
+  CS_CHECK_ARG(pass_layers != nullptr && n_passes != nullptr, "fft_get_plan: null output");
+  CS_CHECK_ARG(log_n >= 3 && log_n <= 30 && n_layers >= 1 && n_layers <= log_n, "fft_get_plan: bad shape");
+  const std::vector<PassPlan> plan = plan_passes(inverse != 0, log_n, n_layers);
+  *n_passes = (uint32_t)plan.size();
+  for (size_t i = 0; i < plan.size() && i < 32; i++) pass_layers[i] = plan[i].hi - plan[i].lo;
+  return CS_OK;
 }

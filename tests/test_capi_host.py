@@ -100,3 +100,26 @@ def test_gather_checks_every_request_on_host(lib):
     assert b"word 4" in lib.cs_last_error()
     # nothing to read: no device work at all
     assert _status(lib, "cs_gather_u32", null, null, 0, null, null, 0, null, null) == 0
+
+
+def test_fft_plans_are_validated_and_stored_on_host(lib):
+    from proving_gb300 import autotune
+    INVALID = 1
+
+    def set_plan(inv, log_n, n_layers, plan):
+        arr = (ctypes.c_uint32 * max(1, len(plan)))(*plan)
+        return _status(lib, "cs_fft_set_plan", inv, log_n, n_layers, arr, len(plan))
+
+    assert set_plan(1, 20, 20, [10, 9]) == INVALID           # covers 19 of 20 layers
+    assert set_plan(1, 20, 20, [8, 12]) == INVALID           # a strided pass above 11 layers
+    assert set_plan(1, 20, 20, [2, 9, 9]) == INVALID         # first pass below 3 layers
+    assert set_plan(1, 20, 20, [13, 7]) == INVALID           # contiguous pass above 12 layers
+    default = autotune.get_plan(True, 20, 20)
+    assert sum(default) == 20
+    assert set_plan(1, 20, 20, [6, 7, 7]) == 0
+    assert autotune.get_plan(True, 20, 20) == (6, 7, 7)
+    assert set_plan(1, 20, 20, []) == 0                      # removed: back to the default
+    assert autotune.get_plan(True, 20, 20) == default
+    for n in range(1, 25):
+        for plan in autotune.candidate_plans(n):
+            assert sum(plan) == n and plan[0] <= 12 and all(t <= 11 for t in plan[1:])

@@ -237,3 +237,25 @@ def test_gather_words_matches_indexing(B):
     host = [t.reshape(-1).cpu().numpy().view(np.uint32) for t in tensors]
     want = np.array([host[s][i] for s, i in zip(slots, idx)], np.uint32)
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("inverse,log_n,n_layers,plan", [(True, 12, 12, (3, 4, 5)), (True, 13, 13, (7, 6)),
+                                                        (False, 12, 10, (4, 6)), (False, 14, 12, (5, 3, 4))])
+def test_fft_results_do_not_depend_on_the_pass_plan(B, inverse, log_n, n_layers, plan):
+    from proving_gb300 import autotune
+    tree = _tree(B, log_n + 1)
+    tw, itw = O.canonic_twiddles(log_n + 1)
+    vals = m31_column(90 + log_n, log_n if inverse else n_layers)
+    autotune.set_plan(inverse, log_n, n_layers, plan)
+    try:
+        assert autotune.get_plan(inverse, log_n, n_layers) == plan
+        col = _col(vals)
+        if inverse:
+            B.interpolate_columns([col], tree)
+            got, want = col.to_cpu(), O.interpolate(vals, itw)
+        else:
+            got = B.evaluate_polynomials([col], log_n, tree)[0].to_cpu()
+            want = O.evaluate(vals, log_n, tw)
+    finally:
+        autotune.set_plan(inverse, log_n, n_layers, [])
+    assert np.array_equal(got, want)
