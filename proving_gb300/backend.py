@@ -33,10 +33,9 @@ def _ptr(t: torch.Tensor) -> int:
 
 
 def _ptr_table(ts) -> ctypes.Array:
-    arr = (ctypes.c_void_p * max(1, len(ts)))()
-    for i, t in enumerate(ts):
-        arr[i] = _ptr(t)
-    return arr
+    """Device pointers of the tensors (BaseColumn data: 1-D contiguous CUDA int32, checked when the
+    column was made)."""
+    return (ctypes.c_void_p * max(1, len(ts)))(*[t.data_ptr() for t in ts])
 
 
 def _u32_table(vals) -> ctypes.Array:
@@ -59,6 +58,18 @@ class BaseColumn:
         assert data.dtype == torch.int32 and data.dim() == 1 and data.is_cuda
         self.data = data
         self._log_size = data.numel().bit_length() - 1
+
+    @classmethod
+    def rows_of(cls, block: torch.Tensor) -> list:
+        """The rows of a contiguous (n_cols, 2^k) int32 CUDA block as columns (checked once)."""
+        assert block.dtype == torch.int32 and block.dim() == 2 and block.is_cuda and block.is_contiguous()
+        log_size = block.shape[1].bit_length() - 1
+        cols = []
+        for row in block.unbind(0):
+            c = cls.__new__(cls)
+            c.data, c._log_size = row, log_size
+            cols.append(c)
+        return cols
 
     @classmethod
     def zeros(cls, length: int, device="cuda"):
@@ -396,7 +407,7 @@ class CudaBackend:
         """gen_trace (crates/examples/src/poseidon/mod.rs:195-275): 1264 columns of 2^log_n words,
         held in one (1264, 2^log_n) device block."""
         block = torch.empty((cls.POSEIDON_COLS, 1 << log_n), dtype=torch.int32, device="cuda")
-        cols = [BaseColumn(block[k]) for k in range(cls.POSEIDON_COLS)]
+        cols = BaseColumn.rows_of(block)
         _lib.call("cs_poseidon_trace", log_n, _ptr_table([c.data for c in cols]), _stream())
         return cols
 
@@ -406,7 +417,7 @@ class CudaBackend:
         lookup: z || alpha (8 words)."""
         n = len(trace[0])
         block = torch.empty((cls.POSEIDON_INTERACTION_COLS, n), dtype=torch.int32, device="cuda")
-        out = [BaseColumn(block[k]) for k in range(cls.POSEIDON_INTERACTION_COLS)]
+        out = BaseColumn.rows_of(block)
         claimed = (ctypes.c_uint32 * 4)()
         _lib.call("cs_poseidon_interaction", _ptr_table([c.data for c in trace]), trace[0].log_size,
                   _u32_table(lookup), _ptr_table([c.data for c in out]), claimed, _stream())

@@ -81,40 +81,42 @@ struct TraceOut {
   uint32_t* cols[kCols];
 };
 
-__global__ void __launch_bounds__(128) poseidon_trace_kernel(uint32_t log_n, const __grid_constant__ TraceOut out) {
+// One block = 32 rows x the 8 instances: warp k computes instance k of 32 consecutive rows
+// (lane = row) and writes its 158 columns, 128 bytes per column per warp.
+__global__ void __launch_bounds__(256) poseidon_trace_kernel(uint32_t log_n, const __grid_constant__ TraceOut out) {
   const uint32_t n = 1u << log_n;
-  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    uint32_t c = 0;
+  const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t* const* cols = out.cols + k * kColsPerRep;
+  for (uint32_t base = blockIdx.x * 32; base < n; base += gridDim.x * 32) {
+    const uint32_t r = base + lane;
+    if (r >= n) continue;
+    uint32_t s[kState];
+#pragma unroll
+    for (int i = 0; i < kState; i++) {
+      s[i] = r + i + k;  // gen_trace's input (mod.rs:215-219)
+      cols[i][r] = s[i];
+    }
+    int c = kState;
 #pragma unroll 1
-    for (int k = 0; k < kInstances; k++) {
-      uint32_t s[kState];
+    for (int round = 0; round < 2 * kHalfFull; round++) {
+      if (round == kHalfFull) {
+#pragma unroll 1
+        for (int q = 0; q < kPartial; q++) {
+          s[0] = m31_add(s[0], kRoundConst);
+          internal_matrix(s);
+          s[0] = pow5(s[0]);
+          cols[c++][r] = s[0];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kState; i++) s[i] = m31_add(s[i], kRoundConst);
+      external_matrix(s);
 #pragma unroll
       for (int i = 0; i < kState; i++) {
-        s[i] = r + i + k;  // gen_trace's input (mod.rs:215-219)
-        out.cols[c + i][r] = s[i];
+        s[i] = pow5(s[i]);
+        cols[c + i][r] = s[i];
       }
       c += kState;
-#pragma unroll 1
-      for (int round = 0; round < 2 * kHalfFull; round++) {
-        if (round == kHalfFull) {
-#pragma unroll 1
-          for (int q = 0; q < kPartial; q++) {
-            s[0] = m31_add(s[0], kRoundConst);
-            internal_matrix(s);
-            s[0] = pow5(s[0]);
-            out.cols[c++][r] = s[0];
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < kState; i++) s[i] = m31_add(s[i], kRoundConst);
-        external_matrix(s);
-#pragma unroll
-        for (int i = 0; i < kState; i++) {
-          s[i] = pow5(s[i]);
-          out.cols[c + i][r] = s[i];
-        }
-        c += kState;
-      }
     }
   }
 }
@@ -154,15 +156,18 @@ struct InterParams {
   uint32_t log_n;
 };
 
-// Row fractions 1/combine(initial) - 1/combine(final) per instance, summed
-// along the row: QM31 column k < 7 gets the sum over instances 0..k, column 7
-// the row total (finalized afterwards).
-__global__ void __launch_bounds__(128) poseidon_fractions_kernel(const __grid_constant__ InterParams p) {
+// Row fractions 1/combine(initial) - 1/combine(final) per instance, summed along the row: QM31
+// column k < 7 gets the sum over instances 0..k, column 7 the row total (finalized afterwards).
+// One block = 32 rows x the 8 instances: warp k computes instance k's fraction, and the prefix
+// over instances goes through shared memory.
+__global__ void __launch_bounds__(256) poseidon_fractions_kernel(const __grid_constant__ InterParams p) {
+  __shared__ uint32_t s_frac[kInstances][4][32];
   const uint32_t n = 1u << p.log_n;
-  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    qm31 acc = qm31_make(0, 0, 0, 0);
-#pragma unroll 1
-    for (int k = 0; k < kInstances; k++) {
+  const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (uint32_t base = blockIdx.x * 32; base < n; base += gridDim.x * 32) {
+    const uint32_t r = base + lane;
+    qm31 f = qm31_make(0, 0, 0, 0);
+    if (r < n) {
       uint32_t v[kState];
 #pragma unroll
       for (int i = 0; i < kState; i++) v[i] = __ldg(p.trace[k * kColsPerRep + i] + r);
@@ -170,12 +175,23 @@ __global__ void __launch_bounds__(128) poseidon_fractions_kernel(const __grid_co
 #pragma unroll
       for (int i = 0; i < kState; i++) v[i] = __ldg(p.trace[k * kColsPerRep + kColsPerRep - kState + i] + r);
       const qm31 d1 = combine(p.lk, v);
-      acc = qm31_add(acc, qm31_mul(qm31_sub(d1, d0), qm31_inv(qm31_mul(d0, d1))));
+      f = qm31_mul(qm31_sub(d1, d0), qm31_inv(qm31_mul(d0, d1)));
+    }
+    s_frac[k][0][lane] = f.a.a;
+    s_frac[k][1][lane] = f.a.b;
+    s_frac[k][2][lane] = f.b.a;
+    s_frac[k][3][lane] = f.b.b;
+    __syncthreads();
+    if (r < n) {
+      qm31 acc = qm31_make(s_frac[0][0][lane], s_frac[0][1][lane], s_frac[0][2][lane], s_frac[0][3][lane]);
+      for (int j = 1; j <= k; j++)
+        acc = qm31_add(acc, qm31_make(s_frac[j][0][lane], s_frac[j][1][lane], s_frac[j][2][lane], s_frac[j][3][lane]));
       p.out[4 * k][r] = acc.a.a;
       p.out[4 * k + 1][r] = acc.a.b;
       p.out[4 * k + 2][r] = acc.b.a;
       p.out[4 * k + 3][r] = acc.b.b;
     }
+    __syncthreads();
   }
 }
 
@@ -401,7 +417,8 @@ void set_lookup(Lookup& lk, const uint32_t* w) {
   }
 }
 
-uint32_t grid_for(uint32_t n, uint32_t threads) { return std::max(1u, std::min((n + threads - 1) / threads, 152u * 16)); }
+// Blocks of 32 rows x 8 instances for 2^log_n rows, at most 16 per SM (grid-stride beyond).
+uint32_t row_group_blocks(uint32_t n) { return std::max(1u, std::min((n + 31) / 32, 152u * 16)); }
 
 }  // namespace
 }  // namespace cs
@@ -417,7 +434,7 @@ extern "C" cs_status cs_poseidon_trace(uint32_t log_n, uint32_t* const* h_cols, 
     out.cols[k] = h_cols[k];
   }
   const uint32_t n = 1u << log_n;
-  poseidon_trace_kernel<<<grid_for(n, 128), 128, 0, to_stream(stream)>>>(log_n, out);
+  poseidon_trace_kernel<<<row_group_blocks(n), 256, 0, to_stream(stream)>>>(log_n, out);
   CS_LAUNCHED("poseidon_trace_kernel");
   return CS_OK;
 }
@@ -440,7 +457,7 @@ extern "C" cs_status cs_poseidon_interaction(const uint32_t* const* h_trace, uin
   p.log_n = log_n;
   cudaStream_t st = to_stream(stream);
   const uint32_t n = 1u << log_n;
-  poseidon_fractions_kernel<<<grid_for(n, 128), 128, 0, st>>>(p);
+  poseidon_fractions_kernel<<<row_group_blocks(n), 256, 0, st>>>(p);
   CS_LAUNCHED("poseidon_fractions_kernel");
   Q4 last;
   for (int c = 0; c < 4; c++) last.c[c] = h_out[4 * (kInstances - 1) + c];

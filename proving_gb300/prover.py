@@ -103,11 +103,17 @@ def from_partial_evals(ev):
 
 
 def secure_powers(felt, n: int):
-    out, acc = [], qm(1)
-    for _ in range(n):
-        out.append(acc)
-        acc = qm_mul(acc, felt)
-    return out
+    """felt^0 .. felt^(n-1) (generate_secure_powers, crates/stwo/src/prover/air/accumulation.rs:183-200),
+    built by doubling: the powers below 2^k times felt^(2^k) give the next 2^k."""
+    if n <= 0:
+        return []
+    pw = np.zeros((1, 4), np.int64)
+    pw[0, 0] = 1
+    step = np.asarray(felt, np.int64)
+    while pw.shape[0] < n:
+        pw = np.concatenate([pw, qv_mul(pw, step[None])], axis=0)
+        step = qv_mul(step, step)
+    return [tuple(r) for r in pw[:n].tolist()]
 
 
 # ------------------------------------------------------------ QM31 arrays
@@ -800,7 +806,7 @@ class GpuOps:
     def _block(self, n_cols, log_size):
         import torch
         blk = torch.empty((n_cols, 1 << log_size), dtype=torch.int32, device="cuda")
-        return [self.be.BaseColumn(blk[k]) for k in range(n_cols)]
+        return self.be.BaseColumn.rows_of(blk)
 
     def merkle_commit(self, cols, L):
         return GpuMerkle(self.B.merkle_commit(cols, L), L)
