@@ -336,6 +336,32 @@ cs_status cs_poseidon_composition(const uint32_t *const *h_trace, const uint32_t
                                   uint32_t trace_log, const uint32_t lookup[8], const uint32_t claimed_sum[4],
                                   const uint32_t *h_rc, uint32_t *const h_accum[4], cs_stream stream);
 
+/* FriOps::fold_line / fold_circle_into_line with the folding challenge read
+   from device memory (4 words at d_alpha, where cs_channel_draw_secure_felt
+   left it) instead of the host. Same results as the host-alpha forms. */
+cs_status cs_fold_line_device_alpha(const uint32_t *const h_src[4], uint32_t log_size, const uint32_t *d_alpha,
+                                    uint32_t *const h_dst[4], const uint32_t *d_itwiddles, uint32_t twiddle_log_size,
+                                    cs_stream stream);
+cs_status cs_fold_circle_into_line_device_alpha(const uint32_t *const h_src[4], uint32_t log_size,
+                                                const uint32_t *d_alpha, uint32_t *const h_dst[4],
+                                                const uint32_t *d_itwiddles, uint32_t twiddle_log_size,
+                                                cs_stream stream);
+
+/* ------------------------------------------------------- channel */
+
+/* The Blake2s channel (crates/stwo/src/core/channel/blake2s.rs:16-118) with
+   its state in device memory: d_state holds 9 words, the 32-byte digest as 8
+   LE words then the draw counter. Lets the FRI commit loop (commit a layer, mix
+   its root, draw the challenge, fold) run without a host round trip per layer;
+   the caller copies the state back once.
+   cs_channel_mix_root: Blake2sMerkleChannel::mix_hash
+   (crates/stwo/src/core/vcs_lifted/blake2_merkle.rs:56-58) of the 8-word digest
+   at d_root (e.g. the last digest of a cs_merkle_commit layer buffer).
+   cs_channel_draw_secure_felt: Channel::draw_secure_felt (blake2s.rs:69-74)
+   into d_felt (4 words). Both enqueue one single-thread kernel on `stream`. */
+cs_status cs_channel_mix_root(uint32_t *d_state, const uint32_t *d_root, cs_stream stream);
+cs_status cs_channel_draw_secure_felt(uint32_t *d_state, uint32_t *d_felt, cs_stream stream);
+
 /* ------------------------------------------------------- measurement */
 
 /* Integer-pipe throughput probe (no counterpart in the reference): `blocks` x

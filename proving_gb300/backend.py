@@ -269,6 +269,28 @@ class CudaBackend:
         return cur
 
     @staticmethod
+    def fold_line_device_alpha(values: SecureColumnByCoords, d_alpha: torch.Tensor,
+                               twiddles: TwiddleTree) -> SecureColumnByCoords:
+        """fold_line with the challenge in device memory (4 words)."""
+        n = len(values)
+        dst = SecureColumnByCoords.uninitialized(n // 2)
+        _lib.call("cs_fold_line_device_alpha", _ptr_table([c.data for c in values.columns]), n.bit_length() - 1,
+                  _ptr(d_alpha), _ptr_table([c.data for c in dst.columns]), _ptr(twiddles.itwiddles),
+                  twiddles.log_size, _stream())
+        return dst
+
+    @staticmethod
+    def fold_circle_into_line_device_alpha(src: SecureColumnByCoords, d_alpha: torch.Tensor,
+                                           twiddles: TwiddleTree) -> SecureColumnByCoords:
+        """fold_circle_into_line with the challenge in device memory (4 words)."""
+        n = len(src)
+        dst = SecureColumnByCoords.uninitialized(n // 2)
+        _lib.call("cs_fold_circle_into_line_device_alpha", _ptr_table([c.data for c in src.columns]),
+                  n.bit_length() - 1, _ptr(d_alpha), _ptr_table([c.data for c in dst.columns]),
+                  _ptr(twiddles.itwiddles), twiddles.log_size, _stream())
+        return dst
+
+    @staticmethod
     def fold_circle_into_line(src: SecureColumnByCoords, alpha, twiddles: TwiddleTree) -> SecureColumnByCoords:
         n = len(src)
         dst = SecureColumnByCoords.uninitialized(n // 2)

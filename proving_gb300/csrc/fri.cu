@@ -45,7 +45,16 @@ __device__ __forceinline__ void qm31_ibfly(qm31& v0, qm31& v1, uint32_t t) {
   v1 = qm31_mul_m31(qm31_sub(tmp, v1), t);
 }
 
-__global__ void fold_line_kernel(const Coords c, uint32_t half, const uint32_t* __restrict__ itw_layer, qm31 alpha) {
+// alpha_dev: when not null, the folding challenge is read from device memory (4 words), where a
+// device-resident channel drew it; otherwise `alpha` is used.
+__device__ __forceinline__ qm31 challenge(qm31 alpha, const uint32_t* alpha_dev) {
+  return alpha_dev ? qm31_make(__ldg(alpha_dev), __ldg(alpha_dev + 1), __ldg(alpha_dev + 2), __ldg(alpha_dev + 3))
+                   : alpha;
+}
+
+__global__ void fold_line_kernel(const Coords c, uint32_t half, const uint32_t* __restrict__ itw_layer, qm31 alpha_h,
+                                 const uint32_t* alpha_dev) {
+  const qm31 alpha = challenge(alpha_h, alpha_dev);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < half; i += gridDim.x * blockDim.x) {
     qm31 f1;
     qm31 f0 = load_pair(c, i, f1);
@@ -54,7 +63,9 @@ __global__ void fold_line_kernel(const Coords c, uint32_t half, const uint32_t* 
   }
 }
 
-__global__ void fold_circle_kernel(const Coords c, uint32_t half, const uint32_t* __restrict__ lt1, qm31 alpha) {
+__global__ void fold_circle_kernel(const Coords c, uint32_t half, const uint32_t* __restrict__ lt1, qm31 alpha_h,
+                                   const uint32_t* alpha_dev) {
+  const qm31 alpha = challenge(alpha_h, alpha_dev);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < half; i += gridDim.x * blockDim.x) {
     const uint32_t pair = (i >> 2) << 1;
     const uint32_t ix = __ldg(lt1 + pair), iy = __ldg(lt1 + pair + 1);
@@ -106,12 +117,15 @@ static cs_status check_coords(const uint32_t* const src[4], uint32_t* const dst[
   return CS_OK;
 }
 
-extern "C" cs_status cs_fold_line(const uint32_t* const h_src[4], uint32_t log_size, const uint32_t alpha[4],
-                                  uint32_t* const h_dst[4], const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
-                                  cs_stream stream) {
+namespace cs {
+namespace {
+
+cs_status fold_line_impl(const uint32_t* const h_src[4], uint32_t log_size, qm31 alpha, const uint32_t* alpha_dev,
+                         uint32_t* const h_dst[4], const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
+                         cs_stream stream) {
   cs_status s = check_coords(h_src, h_dst);
   if (s != CS_OK) return s;
-  CS_CHECK_ARG(alpha != nullptr && d_itwiddles != nullptr, "fold_line: null alpha or twiddles");
+  CS_CHECK_ARG(d_itwiddles != nullptr, "fold_line: null twiddles");
   CS_CHECK_ARG(log_size >= 1 && log_size <= twiddle_log_size,
                "fold_line: line domain of log %u is not covered by a tree of log %u", log_size, twiddle_log_size);
   Coords c;
@@ -121,19 +135,17 @@ extern "C" cs_status cs_fold_line(const uint32_t* const h_src[4], uint32_t log_s
   }
   const uint32_t half = 1u << (log_size - 1);
   const uint32_t* layer = d_itwiddles + ((1u << twiddle_log_size) - (1u << log_size));
-  fold_line_kernel<<<grid_for(half, 256), 256, 0, to_stream(stream)>>>(c, half, layer,
-                                                                       qm31_make(alpha[0], alpha[1], alpha[2], alpha[3]));
+  fold_line_kernel<<<grid_for(half, 256), 256, 0, to_stream(stream)>>>(c, half, layer, alpha, alpha_dev);
   CS_LAUNCHED("fold_line_kernel");
   return CS_OK;
 }
 
-extern "C" cs_status cs_fold_circle_into_line(const uint32_t* const h_src[4], uint32_t log_size,
-                                              const uint32_t alpha[4], uint32_t* const h_dst[4],
-                                              const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
-                                              cs_stream stream) {
+cs_status fold_circle_impl(const uint32_t* const h_src[4], uint32_t log_size, qm31 alpha, const uint32_t* alpha_dev,
+                           uint32_t* const h_dst[4], const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
+                           cs_stream stream) {
   cs_status s = check_coords(h_src, h_dst);
   if (s != CS_OK) return s;
-  CS_CHECK_ARG(alpha != nullptr && d_itwiddles != nullptr, "fold_circle_into_line: null alpha or twiddles");
+  CS_CHECK_ARG(d_itwiddles != nullptr, "fold_circle_into_line: null twiddles");
   CS_CHECK_ARG(log_size >= 3 && log_size <= twiddle_log_size + 1,
                "fold_circle_into_line: circle domain of log %u is not covered by a tree of log %u (min log 3)",
                log_size, twiddle_log_size);
@@ -144,10 +156,47 @@ extern "C" cs_status cs_fold_circle_into_line(const uint32_t* const h_src[4], ui
   }
   const uint32_t half = 1u << (log_size - 1);
   const uint32_t* lt1 = d_itwiddles + ((1u << twiddle_log_size) - (1u << (log_size - 1)));
-  fold_circle_kernel<<<grid_for(half, 256), 256, 0, to_stream(stream)>>>(
-      c, half, lt1, qm31_make(alpha[0], alpha[1], alpha[2], alpha[3]));
+  fold_circle_kernel<<<grid_for(half, 256), 256, 0, to_stream(stream)>>>(c, half, lt1, alpha, alpha_dev);
   CS_LAUNCHED("fold_circle_kernel");
   return CS_OK;
+}
+
+}  // namespace
+}  // namespace cs
+
+extern "C" cs_status cs_fold_line(const uint32_t* const h_src[4], uint32_t log_size, const uint32_t alpha[4],
+                                  uint32_t* const h_dst[4], const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
+                                  cs_stream stream) {
+  CS_CHECK_ARG(alpha != nullptr, "fold_line: null alpha");
+  return fold_line_impl(h_src, log_size, qm31_make(alpha[0], alpha[1], alpha[2], alpha[3]), nullptr, h_dst,
+                        d_itwiddles, twiddle_log_size, stream);
+}
+
+extern "C" cs_status cs_fold_line_device_alpha(const uint32_t* const h_src[4], uint32_t log_size,
+                                               const uint32_t* d_alpha, uint32_t* const h_dst[4],
+                                               const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
+                                               cs_stream stream) {
+  CS_CHECK_ARG(d_alpha != nullptr, "fold_line: null device alpha");
+  return fold_line_impl(h_src, log_size, qm31_make(0, 0, 0, 0), d_alpha, h_dst, d_itwiddles, twiddle_log_size,
+                        stream);
+}
+
+extern "C" cs_status cs_fold_circle_into_line(const uint32_t* const h_src[4], uint32_t log_size,
+                                              const uint32_t alpha[4], uint32_t* const h_dst[4],
+                                              const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
+                                              cs_stream stream) {
+  CS_CHECK_ARG(alpha != nullptr, "fold_circle_into_line: null alpha");
+  return fold_circle_impl(h_src, log_size, qm31_make(alpha[0], alpha[1], alpha[2], alpha[3]), nullptr, h_dst,
+                          d_itwiddles, twiddle_log_size, stream);
+}
+
+extern "C" cs_status cs_fold_circle_into_line_device_alpha(const uint32_t* const h_src[4], uint32_t log_size,
+                                                           const uint32_t* d_alpha, uint32_t* const h_dst[4],
+                                                           const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
+                                                           cs_stream stream) {
+  CS_CHECK_ARG(d_alpha != nullptr, "fold_circle_into_line: null device alpha");
+  return fold_circle_impl(h_src, log_size, qm31_make(0, 0, 0, 0), d_alpha, h_dst, d_itwiddles, twiddle_log_size,
+                          stream);
 }
 
 extern "C" cs_status cs_pack_leaves_input(const uint32_t* const h_in[4], uint32_t log_size, uint32_t* const h_out[16],

@@ -699,32 +699,53 @@ def compute_fri_quotients(ops, columns, sample_points, sampled, random_coeff, li
     return ops.compute_quotients_and_combine(parts, points, fls, lifting, log_blowup, twiddles)
 
 
+class HostFriChannel:
+    """The FRI commit loop's view of the channel when the channel lives on the host."""
+
+    def __init__(self, channel):
+        self.channel = channel
+
+    def mix_root(self, tree):
+        self.channel.mix_root(tree.root)
+
+    def draw(self):
+        return self.channel.draw_secure_felt()
+
+    def finish(self):
+        pass
+
+
 def fri_commit(ops, channel, fp: FriParams, column, log_size: int, twiddles):
-    """FriProver::commit (crates/stwo/src/prover/fri.rs:113-226), fold_step 1 (no leaf packing)."""
+    """FriProver::commit (crates/stwo/src/prover/fri.rs:113-226), fold_step 1 (no leaf packing). The
+    ops may keep the channel on the device for the layer loop (ops.fri_channel): mixing each
+    layer's root and drawing its challenge then need no host round trip."""
     if fp.fold_step != 1:
         raise NotImplementedError("fold_step > 1")
+    ch = ops.fri_channel(channel) if hasattr(ops, "fri_channel") else HostFriChannel(channel)
     first_tree = ops.merkle_commit(ops.secure_columns(column), log_size)
-    channel.mix_root(first_tree.root)
-    alpha = channel.draw_secure_felt()
+    ch.mix_root(first_tree)
+    alpha = ch.draw()
     layer = ops.fold_circle_into_line(column, alpha, twiddles)
     line_log = log_size - 1
     last_log = (fp.last_layer_domain_size()).bit_length() - 1
     inner = []
     while line_log > last_log + fp.fold_step:
         tree = ops.merkle_commit(ops.secure_columns(layer), line_log)
-        channel.mix_root(tree.root)
-        alpha = channel.draw_secure_felt()
+        ch.mix_root(tree)
+        alpha = ch.draw()
         inner.append({"tree": tree, "eval": layer, "fold_step": fp.fold_step})
         layer = ops.fold_line(layer, alpha, twiddles)
         line_log -= fp.fold_step
+    # with fold_step 1 the loop above leaves exactly one fold for the last layer
     last_step = line_log - last_log
+    if last_step != 1:
+        raise NotImplementedError("a last FRI step of more than one fold")
     tree = ops.merkle_commit(ops.secure_columns(layer), line_log)
-    channel.mix_root(tree.root)
-    alpha = channel.draw_secure_felt()
+    ch.mix_root(tree)
+    alpha = ch.draw()
     inner.append({"tree": tree, "eval": layer, "fold_step": last_step})
-    for _ in range(last_step):
-        layer = ops.fold_line(layer, alpha, twiddles)
-        alpha = qm_mul(alpha, alpha)
+    layer = ops.fold_line(layer, alpha, twiddles)
+    ch.finish()
     # commit_last_layer (fri.rs:208-226): interpolate the last evaluation on its line domain
     values = ops.gather_secure(layer, list(range(fp.last_layer_domain_size())))
     coeffs = line_interpolate(values, last_log)
@@ -766,7 +787,13 @@ class GpuMerkle:
     def __init__(self, prover, height: int):
         self.t = prover
         self.height = height
-        self.root = prover.root()
+        self._root = None
+
+    @property
+    def root(self) -> bytes:
+        if self._root is None:
+            self._root = self.t.root()
+        return self._root
 
     def hashes(self, layer_log: int, idx):
         import torch
@@ -921,10 +948,67 @@ class GpuOps:
                                                     log_blowup, tw)
 
     def fold_circle_into_line(self, col, alpha, tw):
+        if isinstance(alpha, DeviceFelt):
+            return self.B.fold_circle_into_line_device_alpha(col, alpha.data, tw)
         return self.B.fold_circle_into_line(col, np.asarray(alpha, np.uint32), tw)
 
     def fold_line(self, col, alpha, tw):
+        if isinstance(alpha, DeviceFelt):
+            return self.B.fold_line_device_alpha(col, alpha.data, tw)
         return self.B.fold_line(col, [np.asarray(alpha, np.uint32)], tw)
+
+    def fri_channel(self, channel):
+        return DeviceFriChannel(self, channel)
+
+
+class DeviceFelt:
+    """A QM31 drawn by the device channel, left in device memory (4 words)."""
+
+    def __init__(self, data):
+        self.data = data
+
+
+class DeviceFriChannel:
+    """The FRI commit loop's channel on the device (cs_channel_mix_root / cs_channel_draw_secure_felt):
+    the state starts from the host channel's, every layer's root is mixed and its challenge drawn
+    on the device, and `finish` reads the state and all the layer roots back in one call and
+    brings the host channel to the same state."""
+
+    def __init__(self, ops, channel):
+        import torch
+        self.ops, self.channel = ops, channel
+        words = list(struct.unpack("<8I", channel.digest)) + [channel.n_draws]
+        self.state = torch.tensor(np.array(words, np.uint32).view(np.int32), device="cuda")
+        self.felts = torch.empty((64, 4), dtype=torch.int32, device="cuda")
+        self.n_felts = 0
+        self.trees = []
+
+    def mix_root(self, tree):
+        from .backend import _stream
+        from . import _lib
+        self.trees.append(tree)
+        root = tree.t.all[-1]
+        _lib.call("cs_channel_mix_root", self.state.data_ptr(), root.data_ptr(), _stream())
+
+    def draw(self):
+        from .backend import _stream
+        from . import _lib
+        felt = self.felts[self.n_felts]
+        self.n_felts += 1
+        _lib.call("cs_channel_draw_secure_felt", self.state.data_ptr(), felt.data_ptr(), _stream())
+        return DeviceFelt(felt)
+
+    def finish(self):
+        tensors = [self.state] + [t.t.all[-1] for t in self.trees]
+        slots = np.concatenate([np.zeros(9, np.uint32)] + [np.full(8, i + 1, np.uint32)
+                                                           for i in range(len(self.trees))])
+        idx = np.concatenate([np.arange(9, dtype=np.uint32)] + [np.arange(8, dtype=np.uint32)] * len(self.trees))
+        words = self.ops.B.gather_words(tensors, slots, idx)
+        for i, tree in enumerate(self.trees):
+            tree._root = words[9 + 8 * i:17 + 8 * i].astype("<u4").tobytes()
+            self.channel.log.append(("mix_root", tree._root.hex()))
+        self.channel.digest = words[:8].astype("<u4").tobytes()
+        self.channel.n_draws = int(words[8])
 
 
 class PlainGpuOps(GpuOps):

@@ -259,3 +259,33 @@ def test_fft_results_do_not_depend_on_the_pass_plan(B, inverse, log_n, n_layers,
     finally:
         autotune.set_plan(inverse, log_n, n_layers, [])
     assert np.array_equal(got, want)
+
+
+# ------------------------------------------------------------------ device channel
+
+def test_device_channel_matches_host_channel(B):
+    # mix_root and draw_secure_felt on the device state equal Blake2sChannel's, draw counter included
+    import struct
+    from proving_gb300 import _lib
+    from proving_gb300.backend import _stream
+    from proving_gb300.prover import Blake2sChannel
+    host = Blake2sChannel(bytes(range(32)))
+    host.n_draws = 5
+    state = torch.tensor(np.array(list(struct.unpack("<8I", host.digest)) + [5], np.uint32).view(np.int32),
+                         device="cuda")
+    felt = torch.empty(4, dtype=torch.int32, device="cuda")
+    want = [host.draw_secure_felt()]
+    _lib.call("cs_channel_draw_secure_felt", state.data_ptr(), felt.data_ptr(), _stream())
+    got = [tuple(felt.cpu().numpy().view(np.uint32).tolist())]
+    for k in range(3):
+        root = np.random.default_rng(k).integers(0, 1 << 32, 8, dtype=np.uint64).astype(np.uint32)
+        host.mix_root(root.astype("<u4").tobytes())
+        d_root = torch.tensor(root.view(np.int32), device="cuda")
+        _lib.call("cs_channel_mix_root", state.data_ptr(), d_root.data_ptr(), _stream())
+        for _ in range(2):
+            want.append(host.draw_secure_felt())
+            _lib.call("cs_channel_draw_secure_felt", state.data_ptr(), felt.data_ptr(), _stream())
+            got.append(tuple(felt.cpu().numpy().view(np.uint32).tolist()))
+    assert got == want
+    words = state.cpu().numpy().view(np.uint32)
+    assert words[:8].astype("<u4").tobytes() == host.digest and int(words[8]) == host.n_draws
