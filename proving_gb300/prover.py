@@ -446,8 +446,11 @@ class StarkProof:
 
     def to_words(self) -> list:
         """A felt stream in the field order of CairoSerialize for StarkProof
-        (crates/cairo-serialize/src/serialize.rs:121-210): vectors are a length
-        followed by items, QM31 = 4 words, Blake2s hash = 8 LE words, u64 = one felt."""
+        (crates/cairo-serialize/src/serialize.rs:99-210): vectors are a length
+        followed by items, QM31 = 4 words, Blake2s hash = 8 LE words, u64 = one felt;
+        the pcs config is its 5 FRI parameters only (the lifting log sizes are not
+        serialized, serialize.rs:111-119); the last-layer LinePoly is its coefficients
+        followed by log2 of their number (serialize.rs:61-66)."""
         w = []
 
         def vec(items, f):
@@ -463,7 +466,6 @@ class StarkProof:
 
         fp = self.config.fri_params
         w.extend([fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound, fp.n_queries, fp.fold_step])
-        w.extend([self.config.trace_lifting_log_size, self.config.preprocessed_lifting_log_size])
         vec(self.commitments, h)
         w.append(self.oods_proof_of_work)
         vec(self.sampled_values, lambda tree: vec(tree, lambda col: vec(col, q)))
@@ -478,6 +480,7 @@ class StarkProof:
         layer(self.fri_first_layer)
         vec(self.fri_inner_layers, layer)
         vec(self.fri_last_layer_poly, q)
+        w.append(len(self.fri_last_layer_poly).bit_length() - 1)
         w.append(self.fri_proof_of_work)
         return w
 

@@ -62,3 +62,24 @@ def test_invalid_trace_is_refused():
 
 def test_proof_bytes_are_deterministic():
     assert make_proof(4).to_bytes() == make_proof(4).to_bytes()
+
+
+def test_felt_stream_follows_cairo_serialize():
+    # CairoSerialize for StarkProof (crates/cairo-serialize/src/serialize.rs:99-210): the pcs config
+    # is the 5 FRI parameters only, then commitments, the OODS nonce, sampled values,
+    # decommitments, queried values and the FRI proof, whose LinePoly ends with log2 of its size
+    proof = make_proof(4, n_queries=3)
+    w = proof.to_words()
+    fp = proof.config.fri_params
+    assert w[:5] == [fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound, fp.n_queries, fp.fold_step]
+    k = 5
+    assert w[k] == 3  # preprocessed, trace and composition roots
+    k += 1 + 3 * 8
+    assert w[k] == proof.oods_proof_of_work
+    k += 1
+    assert w[k] == 3 and w[k + 1] == 0 and w[k + 2] == N_COLS  # sampled values: trees, then the trace's columns
+    # the stream ends with the last-layer poly (length, coefficients, log length) and the FRI nonce
+    poly = proof.fri_last_layer_poly
+    tail = [len(poly)] + [c for q in poly for c in q] + [len(poly).bit_length() - 1, proof.fri_proof_of_work]
+    assert w[-len(tail):] == tail
+    assert len(proof.to_bytes()) == 8 * len(w)
