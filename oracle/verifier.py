@@ -117,6 +117,13 @@ def merkle_verify(root, height, column_log_sizes, query_positions, queried_value
 # ---------------------------------------------------------------- verify
 
 def verify_wide_fib(proof, n_cols: int, log_n_rows: int):
+    verify_wide_fib_components(proof, [n_cols], [log_n_rows])
+
+
+def verify_wide_fib_components(proof, n_cols_list, log_sizes):
+    """Wide-Fibonacci components in one proof, their columns in one lifted trace tree (the verifier
+    side of test_e2e_lifted_fib_prove, crates/examples/src/wide_fibonacci/mod.rs:553-575)."""
+    n_cols = sum(n_cols_list)
     cfg = proof.config
     fp = cfg.fri_params
     b = fp.log_blowup_factor
@@ -158,9 +165,14 @@ def verify_wide_fib(proof, n_cols: int, log_n_rows: int):
     dinv = qinv(xv)
     acc = qm(0)
     mask = [c[0] for c in sv[1]]
-    for k in range(n_cols - 2):
-        cons = qsub(mask[k + 2], qadd(qmul(mask[k], mask[k]), qmul(mask[k + 1], mask[k + 1])))
-        acc = qadd(qmul(acc, random_coeff), qmul(cons, dinv))
+    start = 0
+    for nc in n_cols_list:
+        # each component's constraints in order (Components::eval_composition_polynomial_at_point)
+        m = mask[start:start + nc]
+        for k in range(nc - 2):
+            cons = qsub(m[k + 2], qadd(qmul(m[k], m[k]), qmul(m[k + 1], m[k + 1])))
+            acc = qadd(qmul(acc, random_coeff), qmul(cons, dinv))
+        start += nc
     if comp != acc:
         raise VerificationError("OODS values do not match the AIR")
 
@@ -196,7 +208,8 @@ def verify_wide_fib(proof, n_cols: int, log_n_rows: int):
     queries = sorted(set(int(q) for q in ch.draw_queries(column_log, fp.n_queries)))
 
     # tree decommitments
-    sizes = [[], [log_n_rows + b] * n_cols, [max_log_degree_bound + b] * 8]
+    sizes = [[], [log_n + b for nc, log_n in zip(n_cols_list, log_sizes) for _ in range(nc)],
+             [max_log_degree_bound + b] * 8]
     heights = [0, lifting, lifting]
     for tree in range(3):
         merkle_verify(proof.commitments[tree], heights[tree], sizes[tree], queries, proof.queried_values[tree],

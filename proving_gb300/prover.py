@@ -492,39 +492,62 @@ def prove_wide_fib(ops, trace, log_n_rows: int, config: PcsConfig, channel: Blak
     """Commits the (empty) preprocessed tree and the Wide-Fibonacci trace, then
     runs prove_ex (crates/stwo/src/prover/mod.rs:39-138). `trace`: the
     column evaluations on CanonicCoset(log_n_rows), as ops columns (consumed)."""
+    return prove_wide_fib_components(ops, [trace], [log_n_rows], config, channel, twiddles)
+
+
+def prove_wide_fib_components(ops, traces, log_sizes, config: PcsConfig, channel: Blake2sChannel, twiddles):
+    """Several WideFibonacciComponents of different sizes in one proof, their traces committed in one
+    lifted tree (as test_e2e_lifted_fib_prove, crates/examples/src/wide_fibonacci/mod.rs:495-577):
+    the empty preprocessed tree, the trace tree, then prove_ex (crates/stwo/src/prover/mod.rs:39-138).
+    traces[i]: component i's column evaluations on CanonicCoset(log_sizes[i]) (consumed)."""
     fp = config.fri_params
     b = fp.log_blowup_factor
     L = config.trace_lifting_log_size
-    n_cols = len(trace)
 
     # --- preprocessed tree: empty, a single hash of no data at height 0 (pcs/mod.rs:83-96)
     pre_root = hashlib.blake2s(b"").digest()
     channel.mix_root(pre_root)
 
-    # --- trace tree (TreeBuilder::extend_evals + commit, pcs/mod.rs:325-349, 360-386)
-    ops.interpolate(trace, twiddles)
-    trace_evals = ops.evaluate(trace, log_n_rows + b, twiddles)
+    # --- trace tree (TreeBuilder::extend_evals + commit, pcs/mod.rs:325-349, 360-386): every
+    # component's columns, in component order, lifted to the tree height
+    comp_evals_by = []
+    for trace, log_n in zip(traces, log_sizes):
+        ops.interpolate(trace, twiddles)
+        comp_evals_by.append(ops.evaluate(trace, log_n + b, twiddles))
+    trace_evals = [c for ev in comp_evals_by for c in ev]
+    n_cols = len(trace_evals)
     trace_tree = ops.merkle_commit(trace_evals, L)
     channel.mix_root(trace_tree.root)
 
     # --- prove_ex: composition polynomial (air/component_prover.rs:95-116)
     random_coeff = channel.draw_secure_felt()
-    n_constraints = n_cols - 2
-    # EvaluationMode::infer: constraint log degree 1 <= blowup -> SubDomain{b - 1}
-    log_expansion = b - 1
-    eval_log = log_n_rows + 1
-    if log_expansion != 0:
+    # EvaluationMode::infer: constraint log degree 1 <= blowup for every component -> SubDomain{b - 1}
+    if b != 1:
         raise NotImplementedError("the Wide-Fibonacci prover supports log_blowup_factor = 1")
-    # the component's powers are the accumulator's last n, reversed (accumulation.rs:102-122,
-    # component_prover.rs:194): constraint k gets alpha^(N-1-k)
-    rc = list(reversed(secure_powers(random_coeff, n_constraints)))
-    accum = ops.secure_zeros(1 << eval_log)
-    ops.wide_fib_composition(trace_evals, log_n_rows, rc, accum)
-    # finalize: lift_and_accumulate of one column is itself; interpolate on CanonicCoset(eval_log)
+    n_cons = [len(t) - 2 for t in traces]
+    total = sum(n_cons)
+    powers = secure_powers(random_coeff, total)
+    # DomainEvaluationAccumulator::columns (air/accumulation.rs:102-122): each component in turn takes
+    # the last n of the remaining powers, reversed (component_prover.rs:194), so constraint k of the
+    # component whose constraints start at global index g gets alpha^(total - 1 - g - k)
+    sub_acc = {}
+    start = 0
+    for evals, log_n, n in zip(comp_evals_by, log_sizes, n_cons):
+        rc = list(reversed(powers[total - start - n:total - start]))
+        eval_log = log_n + 1
+        if eval_log not in sub_acc:
+            sub_acc[eval_log] = ops.secure_zeros(1 << eval_log)
+        ops.wide_fib_composition(evals, log_n, rc, sub_acc[eval_log])
+        start += n
+    # finalize (accumulation.rs:142-180): lift and accumulate ascending sizes, interpolate on the
+    # largest canonic domain
+    accs = [sub_acc[k] for k in sorted(sub_acc)]
+    accum = accs[0] if len(accs) == 1 else ops.lift_and_accumulate(accs)
+    comp_log = max(sub_acc)
     comp_coeffs = ops.interpolate_secure(accum, twiddles)
     left, right = ops.split_at_mid(comp_coeffs)
     comp_polys = left + right  # extend_polys(left coords), extend_polys(right coords)
-    comp_evals = ops.evaluate(comp_polys, (eval_log - 1) + b, twiddles)
+    comp_evals = ops.evaluate(comp_polys, (comp_log - 1) + b, twiddles)
     comp_tree = ops.merkle_commit(comp_evals, L)
     channel.mix_root(comp_tree.root)
 
@@ -588,30 +611,11 @@ def prove_wide_fib(ops, trace, log_n_rows: int, config: PcsConfig, channel: Blak
     for _ in range(max_log_degree_bound - 1):
         x = q_double_x(x)
     composition_oods = qm_add(left_v, qm_mul(x, right_v))
-    expected = wide_fib_composition_at_point(oods, [c[0] for c in sampled[1]], random_coeff, max_log_degree_bound,
-                                             powers=rc)
+    mask = [c[0] for c in sampled[1]]
+    expected = wide_fib_components_at_point(oods, mask, [len(t) for t in traces], random_coeff, max_log_degree_bound)
     if composition_oods != expected:
         raise RuntimeError("constraints not satisfied (ProvingError::ConstraintsNotSatisfied)")
     return proof
-
-
-def wide_fib_composition_at_point(point, mask, random_coeff, max_log_degree_bound: int, powers=None):
-    """Components::eval_composition_polynomial_at_point for the Wide-Fibonacci component
-    (crates/constraint-framework/src/component.rs:220-243, PointEvaluationAccumulator,
-    crates/stwo/src/core/air/accumulation.rs:13-33): the Horner sum over the constraints
-    sum_k alpha^(N-1-k) C_k, divided by V_trace(point). `powers`: alpha^(N-1-k) per constraint
-    when the caller has them."""
-    x = point[0]
-    for _ in range(max_log_degree_bound - 1):
-        x = q_double_x(x)
-    den_inv = qm_inv(x)
-    m = np.asarray(mask, np.int64)
-    a, b, c = m[:-2], m[1:-1], m[2:]
-    cons = qv_sub(c, qv_add(qv_mul(a, a), qv_mul(b, b)))
-    if powers is None:
-        powers = list(reversed(secure_powers(random_coeff, len(cons))))
-    total = qv_sum(qv_mul(cons, np.asarray(powers, np.int64)))
-    return qm_mul(tuple(int(v) for v in total), den_inv)
 
 
 def q_double_point(pt):
@@ -651,6 +655,26 @@ def m31_subgroup_generator(log_size: int):
 def qpoint_add_m31(p, g):
     """p + g for a QM31 point p and an M31 point g."""
     return qpoint_add(p, (qm(g[0]), qm(g[1])))
+
+
+def wide_fib_components_at_point(point, mask, n_cols_per_component, random_coeff, max_log_degree_bound: int):
+    """Components::eval_composition_polynomial_at_point (crates/stwo/src/core/air/components.rs:54-75) for
+    Wide-Fibonacci components in order: one Horner accumulation over all their constraints, each
+    divided by V(CanonicCoset(max_log_degree_bound)) at the point."""
+    x = point[0]
+    for _ in range(max_log_degree_bound - 1):
+        x = q_double_x(x)
+    den_inv = qm_inv(x)
+    m = np.asarray(mask, np.int64)
+    cons, start = [], 0
+    for n in n_cols_per_component:
+        a, b, c = m[start:start + n - 2], m[start + 1:start + n - 1], m[start + 2:start + n]
+        cons.append(qv_sub(c, qv_add(qv_mul(a, a), qv_mul(b, b))))
+        start += n
+    cons = np.concatenate(cons, axis=0)
+    powers = np.asarray(list(reversed(secure_powers(random_coeff, len(cons)))), np.int64)
+    total = qv_sum(qv_mul(cons, powers))
+    return qm_mul(tuple(int(v) for v in total), den_inv)
 
 
 def compute_fri_quotients(ops, columns, sample_points, sampled, random_coeff, lifting: int, log_blowup: int,

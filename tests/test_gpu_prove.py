@@ -52,3 +52,13 @@ def test_device_trace_generation_proof(gpu):
     proof = pr.prove_wide_fib(gpu, dev_trace, log_n, cfg, pr.Blake2sChannel(), gpu.twiddles(log_n + 2))
     host, _ = _prove(CpuOps(), O.wide_fib_trace(a, b, N_COLS), log_n)
     assert proof.to_bytes() == host.to_bytes()
+
+
+def test_lifted_components_match_oracle(gpu):
+    # two Wide-Fibonacci components of 2^9 and 2^3 rows in one lifted tree (test_e2e_lifted_fib_prove,
+    # crates/examples/src/wide_fibonacci/mod.rs:495-577): the same proof bytes on both backends
+    from oracle.verifier import verify_wide_fib_components
+    from test_prove_cpu import lifted_components_proof
+    g, c = lifted_components_proof(gpu), lifted_components_proof(CpuOps())
+    assert g.to_bytes() == c.to_bytes()
+    verify_wide_fib_components(g, [4, 5], [9, 3])

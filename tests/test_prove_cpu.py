@@ -83,3 +83,31 @@ def test_felt_stream_follows_cairo_serialize():
     tail = [len(poly)] + [c for q in poly for c in q] + [len(poly).bit_length() - 1, proof.fri_proof_of_work]
     assert w[-len(tail):] == tail
     assert len(proof.to_bytes()) == 8 * len(w)
+
+
+def lifted_components_proof(ops):
+    # test_e2e_lifted_fib_prove (crates/examples/src/wide_fibonacci/mod.rs:495-577): components of
+    # 4 columns x 2^9 and 5 columns x 2^3, inputs a = 1, b = row (generate_test_inputs, :130-134),
+    # FriParams::test_params() = (pow 10, last layer 0, blowup 1, 3 queries, fold step 1), tree
+    # height 9 + 1
+    import numpy as np
+    traces = []
+    for n_cols, log_n in ((4, 9), (5, 3)):
+        a = np.ones(1 << log_n, np.uint32)
+        b = np.arange(1 << log_n, dtype=np.uint32)
+        traces.append(ops.columns_from_host(O.wide_fib_trace(a, b, n_cols)))
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=3, fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=9 + 1)
+    return pr.prove_wide_fib_components(ops, traces, [9, 3], cfg, pr.Blake2sChannel(), ops.twiddles(10))
+
+
+def test_lifted_components_prove_then_verify():
+    from oracle.verifier import verify_wide_fib_components
+    proof = lifted_components_proof(CpuOps())
+    verify_wide_fib_components(proof, [4, 5], [9, 3])
+    # the short component's columns are lifted from 2^4 to the tree height 10
+    assert len(proof.sampled_values[1]) == 9
+    bad = copy.deepcopy(proof)
+    bad.sampled_values[1][6][0] = tuple((v + 1) % O.P for v in bad.sampled_values[1][6][0])
+    with pytest.raises(VerificationError):
+        verify_wide_fib_components(bad, [4, 5], [9, 3])
