@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import hashlib
 import json
 import os
 import statistics
@@ -358,6 +359,54 @@ def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: in
     return lat
 
 
+def mixed_prove_leg(torch, n_proofs: int = 2):
+    """Config 3 as a full proof: the batched mixed-size trace (mixed_trace_shape: Wide-Fibonacci
+    components holding 480 M31 columns and 120 single-column LogUp components, each with one M31
+    value column and one QM31 running-sum column, log sizes 10..22 geometric, mean ~16) proved by
+    prove_fib_and_lookups with log_blowup 1, 70 queries, pow 10, one lifted tree per phase.
+    Traces and lookup values are generated on the device from seeds inside the timed region.
+    Two arms: the batched path (one launch per stage and size) and the plain path (one launch
+    per column for the per-column stages); both give the same proof bytes."""
+    from proving_gb300 import prover as pr
+    from proving_gb300.backend import BaseColumn, CudaBackend
+    from proving_gb300.synthetic import m31_column, mixed_trace_shape
+    comps, lookup_logs = mixed_trace_shape()
+    max_log = max([l for _, l in comps] + lookup_logs)
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=max_log + 1)
+    seeds = [(BaseColumn.from_cpu(m31_column(300 + i, l)), BaseColumn.from_cpu(m31_column(400 + i, l)))
+             for i, (_, l) in enumerate(comps)]
+    host_values = [m31_column(500 + k, l) for k, l in enumerate(lookup_logs)]
+    out = {"workload": f"{sum(n for n, _ in comps)} Wide-Fibonacci columns in {len(comps)} components + "
+                       f"{len(lookup_logs)} LogUp components (value column + QM31 running sum), log sizes 10..22 "
+                       f"geometric (mean ~16), log_blowup 1, 70 queries, pow 10, lifting {max_log + 1}",
+           "base_columns": sum(n for n, _ in comps) + len(lookup_logs), "interaction_columns": len(lookup_logs)}
+    digests = {}
+    for name, ops in (("batched", pr.GpuOps()), ("plain", pr.PlainGpuOps())):
+        tw = ops.twiddles(max_log + 2)
+        lat = []
+        for k in range(n_proofs + 1):
+            values = [BaseColumn.from_cpu(v) for v in host_values]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            traces = [CudaBackend.wide_fib_trace(a, b, n) for (a, b), (n, _) in zip(seeds, comps)]
+            proof = pr.prove_fib_and_lookups(ops, traces, [l for _, l in comps], values, lookup_logs, cfg,
+                                             pr.Blake2sChannel(), tw)
+            torch.cuda.synchronize()
+            if k >= 1:
+                lat.append((time.perf_counter() - t0) * 1e3)
+            del traces, values
+        digests[name] = hashlib.sha256(proof.to_bytes()).hexdigest()
+        out[name] = {"proofs_per_s": round(1e3 / statistics.median(lat), 3), "p50_ms": round(statistics.median(lat), 3),
+                     "max_ms": round(max(lat), 3)}
+        del proof, tw
+        torch.cuda.empty_cache()
+    out["same_proof_bytes"] = digests["batched"] == digests["plain"]
+    out["proof_sha256"] = digests["batched"]
+    out["batched_speedup"] = round(out["plain"]["p50_ms"] / out["batched"]["p50_ms"], 3)
+    return out
+
+
 def int_peaks(torch):
     """Measured integer-pipe throughput (cs_int_peak_probe): thread operations per second for
     3-input adds, 3-input logic and funnel shifts (the ALU pipe) and multiply-adds (the FMA pipe),
@@ -594,6 +643,7 @@ def run_gpu(args):
     bvp = batched_vs_plain(torch, cs) if not args.skip_plain else None
     serving_res = serving_leg() if not args.skip_serving else None
     poseidon_res = poseidon_prove_leg(torch, args.poseidon_log_rows) if not args.skip_poseidon else None
+    mixed_res = mixed_prove_leg(torch) if not args.skip_mixed_prove else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -656,6 +706,7 @@ def run_gpu(args):
         "batched_vs_plain": bvp,
         "serving": serving_res,
         "poseidon_prove": poseidon_res,
+        "mixed_prove": mixed_res,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
@@ -753,6 +804,7 @@ def main():
     ap.add_argument("--skip-serving", action="store_true", help="skip the proof-service leg")
     ap.add_argument("--skip-poseidon", action="store_true", help="skip the Poseidon2 prove leg")
     ap.add_argument("--poseidon-log-rows", type=int, default=18, help="log2 rows of the Poseidon2 prove leg")
+    ap.add_argument("--skip-mixed-prove", action="store_true", help="skip the mixed-size full-proof leg")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
     if args.impl == "reference":

@@ -293,13 +293,25 @@ cs_status cs_wide_fib_trace(const uint32_t *d_a, const uint32_t *d_b, uint32_t l
 /* LogUp interaction column on the device: the last column of
    LogupTraceGenerator (crates/constraint-framework/src/prover/logup.rs:50-130)
    with numerator 1 and denominator z - v_i for the M31 column d_values
-   (2^log_size values, bit-reversed circle-domain order, log_size >= 10):
+   (2^log_size values, bit-reversed circle-domain order, log_size >= 1):
    claimed_sum = sum_i 1/(z - v_i) (returned on the host, synchronous), then
    the shifted fractions' inclusive prefix sum in coset order
    (inclusive_prefix_sum, crates/stwo/src/prover/backend/simd/prefix_sum.rs:20)
    into the QM31 column h_out. Uses stream-ordered device scratch. */
 cs_status cs_logup_running_sum(const uint32_t *d_values, uint32_t log_size, const uint32_t z[4], uint32_t *const h_out[4],
                                uint32_t claimed_sum_out[4], cs_stream stream);
+
+/* Constraint quotients of a single-column LogUp component (no counterpart
+   AIR in the reference; built from its constraint framework): the relation
+   entry (multiplicity -1, values [v]) finalized with finalize_logup
+   (crates/constraint-framework/src/lib.rs:185-227), whose interaction column is
+   cs_logup_running_sum's. Row r of CanonicCoset(eval_log) adds
+   rc (cur - prev + claimed_sum / 2^trace_log) (v - z) + 1 over V_trace(x_r)
+   to h_accum, with cur / prev the interaction column (h_inter, 4 coordinates)
+   at the row and one trace step before, v = d_values[r]. */
+cs_status cs_logup_composition(const uint32_t *d_values, const uint32_t *const h_inter[4], uint32_t eval_log,
+                               uint32_t trace_log, const uint32_t z[4], const uint32_t claimed_sum[4],
+                               const uint32_t rc[4], uint32_t *const h_accum[4], cs_stream stream);
 
 /* ------------------------------------------------------- AIR: Poseidon2 */
 

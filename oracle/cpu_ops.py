@@ -65,6 +65,14 @@ class CpuOps:
     def interpolate_into(self, cols, tw):
         return [Col(r) for r in O.interpolate_batch([c.v for c in cols], tw.itw)]
 
+    def logup_running_sum(self, values, z):
+        out, claimed = O.logup_running_sum(values.v, z)
+        return SCol(out), claimed
+
+    def logup_composition(self, values_eval, inter_eval, trace_log, z, claimed, rc, accum):
+        accum.c = O.logup_composition(values_eval.v, [c.v for c in inter_eval], trace_log, z, claimed, rc,
+                                      out=accum.c)
+
     def poseidon_trace(self, log_n):
         return [Col(c) for c in O.poseidon_trace(log_n)]
 

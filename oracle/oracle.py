@@ -517,3 +517,18 @@ def poseidon_composition(trace, inter, trace_log: int, lookup, claimed, rc, out=
     lib().orc_poseidon_composition(_ptr_array(t), _ptr_array(it), ctypes.c_uint32(n.bit_length() - 1),
                                    ctypes.c_uint32(trace_log), _p(lk), _p(cl), _p(r), _ptr_array(out))
     return out
+
+
+def logup_composition(values, inter, trace_log: int, z, claimed, rc, out=None):
+    """A single-column LogUp component's constraint quotients on the evaluation domain of `values`,
+    added to out (4 coordinate arrays, created when None)."""
+    v = _u32(values)
+    it = [_u32(c) for c in inter]
+    n = v.size
+    if out is None:
+        out = [np.zeros(n, np.uint32) for _ in range(4)]
+    out = [_u32(o) for o in out]
+    zz, cl, r = _u32(z), _u32(claimed), _u32(rc)
+    lib().orc_logup_composition(_p(v), _ptr_array(it), ctypes.c_uint32(n.bit_length() - 1), ctypes.c_uint32(trace_log),
+                                _p(zz), _p(cl), _p(r), _ptr_array(out))
+    return out

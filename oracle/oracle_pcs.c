@@ -303,3 +303,42 @@ void orc_logup_running_sum(const uint32_t *values, uint32_t log_n, const uint32_
     }
     free(f);
 }
+
+/*
+ * Constraint quotients of a single-column LogUp component on an evaluation
+ * domain: the relation entry (multiplicity -1, values [v]) finalized with
+ * finalize_logup (crates/constraint-framework/src/lib.rs:185-227, batch size
+ * 1): fraction -1 / (v - z); with cur and prev the interaction column at the
+ * row and one trace step before (offset -1), the constraint is
+ * (cur - prev + claimed / 2^trace_log) (v - z) + 1, weighted by rc and
+ * divided by V_trace as for any component (component_prover.rs:195-268);
+ * added to out. values / inter: the trace column and the 4 coordinates of
+ * the interaction column on CanonicCoset(eval_log).
+ */
+void orc_logup_composition(const uint32_t *values, const uint32_t *const inter[4], uint32_t eval_log,
+                           uint32_t trace_log, const uint32_t z_w[4], const uint32_t claimed_w[4],
+                           const uint32_t rc_w[4], uint32_t *const out[4]) {
+    uint32_t log_expand = eval_log - trace_log;
+    uint32_t n_den = 1u << log_expand;
+    m31 *den = (m31 *)malloc(sizeof(m31) * n_den);
+    if (log_expand == 0) {
+        den[0] = 1;
+    } else {
+        coset_t eval_half = canonic_half_coset(eval_log);
+        coset_t trace_coset = coset_odds(trace_log);
+        for (uint32_t i = 0; i < n_den; i++) den[i] = m31_inv(coset_vanishing_m(trace_coset, domain_at(eval_half, i)));
+        orc_bit_reverse(den, log_expand);
+    }
+    qm31 z = qm31_from_words(z_w), rc = qm31_from_words(rc_w);
+    qm31 shift = qm31_mul_m31(qm31_from_words(claimed_w), m31_inv((m31)((1ull << trace_log) % M31_P)));
+    uint64_t n = 1ull << eval_log;
+    for (uint64_t r = 0; r < n; r++) {
+        uint64_t pr = orc_prev_row(r, trace_log, eval_log);
+        qm31 cur = soa_at(inter, r), prev = soa_at(inter, pr);
+        qm31 shifted = qm31_add(qm31_sub(cur, prev), shift);
+        qm31 cons = qm31_add(qm31_mul(shifted, qm31_sub(qm31_from_m31(values[r]), z)), qm31_from_m31(1));
+        qm31 acc = qm31_mul_m31(qm31_mul(rc, cons), den[r >> trace_log]);
+        soa_set(out, r, qm31_add(soa_at((const uint32_t *const *)out, r), acc));
+    }
+    free(den);
+}

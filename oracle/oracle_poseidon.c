@@ -167,7 +167,7 @@ static m31 ps_coset_vanishing(coset_t c, cpoint p) {
    offset_bit_reversed_circle_domain_index (crates/stwo/src/core/utils.rs:144-160)
    when the domain is larger than the trace, the coset-order predecessor
    (crates/constraint-framework/src/prover/assert.rs:58-66) when it is the trace domain. */
-static uint64_t ps_prev_row(uint64_t r, uint32_t trace_log, uint32_t eval_log) {
+uint64_t orc_prev_row(uint64_t r, uint32_t trace_log, uint32_t eval_log) {
     uint64_t i = bit_reverse_index((uint32_t)r, eval_log);
     uint64_t n = 1ull << eval_log, half = n / 2;
     if (eval_log > trace_log) {
@@ -244,7 +244,7 @@ void orc_poseidon_composition(const uint32_t **trace, const uint32_t **inter, ui
             num[k] = qm31_sub(d1, d0);
             dn[k] = qm31_mul(d0, d1);
         }
-        uint64_t pr = ps_prev_row((uint64_t)r, trace_log, eval_log);
+        uint64_t pr = orc_prev_row((uint64_t)r, trace_log, eval_log);
         qm31 prev_col = qm31_from_m31(0);
         for (uint32_t k = 0; k < PS_INSTANCES; k++) {
             qm31 cur = qm31_make(inter[4 * k][r], inter[4 * k + 1][r], inter[4 * k + 2][r], inter[4 * k + 3][r]);

@@ -120,13 +120,55 @@ def verify_wide_fib(proof, n_cols: int, log_n_rows: int):
     verify_wide_fib_components(proof, [n_cols], [log_n_rows])
 
 
+def _draw_oods(ch, proof):
+    """The OODS proof of work and point (crates/stwo/src/core/verifier.rs:55-62)."""
+    if not ch.verify_pow_nonce(16, proof.oods_proof_of_work):
+        raise VerificationError("OODS proof of work")
+    ch.mix_u64(proof.oods_proof_of_work)
+    t = ch.draw_secure_felt()
+    px, py = O.random_point_from_t(t)
+    return (tuple(int(v) for v in px), tuple(int(v) for v in py))
+
+
+def _partial(ev):
+    """SecureField::from_partial_evals: sum of ev[k] times the k-th basis element."""
+    r = ev[0]
+    for k, e in ((1, (0, 1, 0, 0)), (2, (0, 0, 1, 0)), (3, (0, 0, 0, 1))):
+        r = qadd(r, qmul(ev[k], e))
+    return r
+
+
+def _composition_at_oods(comp_samples, oods, max_log_degree_bound):
+    """The composition value from its split halves (crates/stwo/src/core/proof.rs:27-57) and
+    1 / V(CanonicCoset(max_log_degree_bound)) at the point."""
+    left = _partial([comp_samples[k][0] for k in range(4)])
+    right = _partial([comp_samples[k][0] for k in range(4, 8)])
+    x = oods[0]
+    for _ in range(max_log_degree_bound - 1):
+        x = qdouble_x(x)
+    return qadd(left, qmul(x, right)), qinv(x)
+
+
+def _fib_constraints(mask, n_cols_list):
+    """Each Wide-Fibonacci component's constraints in order: c - (a^2 + b^2)."""
+    out, start = [], 0
+    for nc in n_cols_list:
+        m = mask[start:start + nc]
+        out += [qsub(m[k + 2], qadd(qmul(m[k], m[k]), qmul(m[k + 1], m[k + 1]))) for k in range(nc - 2)]
+        start += nc
+    return out
+
+
+def _qpoint_add(p, q):
+    return (qsub(qmul(p[0], q[0]), qmul(p[1], q[1])), qadd(qmul(p[0], q[1]), qmul(p[1], q[0])))
+
+
 def verify_wide_fib_components(proof, n_cols_list, log_sizes):
     """Wide-Fibonacci components in one proof, their columns in one lifted trace tree (the verifier
     side of test_e2e_lifted_fib_prove, crates/examples/src/wide_fibonacci/mod.rs:553-575)."""
     n_cols = sum(n_cols_list)
     cfg = proof.config
-    fp = cfg.fri_params
-    b = fp.log_blowup_factor
+    b = cfg.fri_params.log_blowup_factor
     ch = O.Blake2sChannel()
     # commitments of the preprocessed (empty) tree and the trace tree (test flow,
     # crates/examples/src/wide_fibonacci/mod.rs:228-231)
@@ -136,46 +178,86 @@ def verify_wide_fib_components(proof, n_cols_list, log_sizes):
     max_log_degree_bound = lifting - b
     random_coeff = tuple(int(v) for v in ch.draw_secure_felt())
     ch.mix_root(proof.commitments[2])
-    if not ch.verify_pow_nonce(16, proof.oods_proof_of_work):
-        raise VerificationError("OODS proof of work")
-    ch.mix_u64(proof.oods_proof_of_work)
-    t = ch.draw_secure_felt()
-    px, py = O.random_point_from_t(t)
-    oods = (tuple(int(v) for v in px), tuple(int(v) for v in py))
+    oods = _draw_oods(ch, proof)
 
     sv = proof.sampled_values
     if len(sv) != 3 or len(sv[0]) != 0 or len(sv[1]) != n_cols or len(sv[2]) != 8:
         raise VerificationError("unexpected sampled_values structure")
-    # composition value from the split halves (crates/stwo/src/core/proof.rs:27-57)
-    def partial(ev):
-        r = ev[0]
-        for k, e in ((1, (0, 1, 0, 0)), (2, (0, 0, 1, 0)), (3, (0, 0, 0, 1))):
-            r = qadd(r, qmul(ev[k], e))
-        return r
-    left = partial([sv[2][k][0] for k in range(4)])
-    right = partial([sv[2][k][0] for k in range(4, 8)])
-    x = oods[0]
-    for _ in range(max_log_degree_bound - 1):
-        x = qdouble_x(x)
-    comp = qadd(left, qmul(x, right))
-    # the AIR at the OODS point (Horner accumulation, denominator V_trace(oods))
-    xv = oods[0]
-    for _ in range(max_log_degree_bound - 1):
-        xv = qdouble_x(xv)
-    dinv = qinv(xv)
+    comp, dinv = _composition_at_oods(sv[2], oods, max_log_degree_bound)
+    # the AIR at the OODS point (Components::eval_composition_polynomial_at_point: Horner accumulation)
     acc = qm(0)
-    mask = [c[0] for c in sv[1]]
-    start = 0
-    for nc in n_cols_list:
-        # each component's constraints in order (Components::eval_composition_polynomial_at_point)
-        m = mask[start:start + nc]
-        for k in range(nc - 2):
-            cons = qsub(m[k + 2], qadd(qmul(m[k], m[k]), qmul(m[k + 1], m[k + 1])))
-            acc = qadd(qmul(acc, random_coeff), qmul(cons, dinv))
-        start += nc
+    for cons in _fib_constraints([c[0] for c in sv[1]], n_cols_list):
+        acc = qadd(qmul(acc, random_coeff), qmul(cons, dinv))
     if comp != acc:
         raise VerificationError("OODS values do not match the AIR")
 
+    sample_points = [[], [[oods]] * n_cols, [[oods]] * 8]
+    sizes = [[], [log_n + b for nc, log_n in zip(n_cols_list, log_sizes) for _ in range(nc)],
+             [max_log_degree_bound + b] * 8]
+    _verify_values(proof, ch, sample_points, sizes, [0, lifting, lifting])
+
+
+def verify_fib_and_lookups(proof, n_cols_list, fib_logs, lookup_logs, claimed_sums):
+    """Wide-Fibonacci components and single-column LogUp components in one proof (the proof of
+    proving_gb300.prover.prove_fib_and_lookups). The claimed sums are the statement: mixed into the
+    channel before the interaction commitment. Each LogUp component's constraint at the point is
+    (cur - prev + claimed / 2^n) (v - z) + 1 (crates/constraint-framework/src/logup.rs:95-150),
+    its interaction columns sampled at (point - G, point)."""
+    cfg = proof.config
+    b = cfg.fri_params.log_blowup_factor
+    lifting = cfg.trace_lifting_log_size
+    max_log_degree_bound = lifting - b
+    n_fib = sum(n_cols_list)
+    n_look = len(lookup_logs)
+    ch = O.Blake2sChannel()
+    ch.mix_root(proof.commitments[0])
+    ch.mix_root(proof.commitments[1])
+    z = tuple(int(v) for v in ch.draw_secure_felt())
+    ch.draw_secure_felt()  # alpha
+    ch.mix_felts(np.asarray([list(c) for c in claimed_sums], np.uint32).reshape(-1, 4))
+    ch.mix_root(proof.commitments[2])
+    random_coeff = tuple(int(v) for v in ch.draw_secure_felt())
+    ch.mix_root(proof.commitments[3])
+    oods = _draw_oods(ch, proof)
+
+    sv = proof.sampled_values
+    if (len(sv) != 4 or len(sv[0]) != 0 or len(sv[1]) != n_fib + n_look or len(sv[2]) != 4 * n_look
+            or len(sv[3]) != 8 or any(len(c) != 2 for c in sv[2])):
+        raise VerificationError("unexpected sampled_values structure")
+    comp, dinv = _composition_at_oods(sv[3], oods, max_log_degree_bound)
+    mask = [c[0] for c in sv[1]]
+    constraints = _fib_constraints(mask[:n_fib], n_cols_list)
+    for k, log_n in enumerate(lookup_logs):
+        v = mask[n_fib + k]
+        prev = _partial([sv[2][4 * k + j][0] for j in range(4)])
+        cur = _partial([sv[2][4 * k + j][1] for j in range(4)])
+        shift = qmul(tuple(int(c) for c in claimed_sums[k]), qm(pow(1 << log_n, P - 2, P)))
+        constraints.append(qadd(qmul(qadd(qsub(cur, prev), shift), qsub(v, z)), qm(1)))
+    acc = qm(0)
+    for cons in constraints:
+        acc = qadd(qmul(acc, random_coeff), qmul(cons, dinv))
+    if comp != acc:
+        raise VerificationError("OODS values do not match the AIR")
+
+    # the previous row: the point minus the generator of CanonicCoset(max_log_degree_bound)
+    g = point_of_index(1 << (31 - max_log_degree_bound))
+    prev_pt = _qpoint_add(oods, (qm(int(g[0])), qm(-int(g[1]))))
+    sample_points = [[], [[oods]] * (n_fib + n_look), [[prev_pt, oods]] * (4 * n_look), [[oods]] * 8]
+    trace_sizes = [log_n + b for nc, log_n in zip(n_cols_list, fib_logs) for _ in range(nc)]
+    trace_sizes += [log_n + b for log_n in lookup_logs]
+    sizes = [[], trace_sizes, [log_n + b for log_n in lookup_logs for _ in range(4)],
+             [max_log_degree_bound + b] * 8]
+    _verify_values(proof, ch, sample_points, sizes, [0, lifting, lifting, lifting])
+
+
+def _verify_values(proof, ch, sample_points, sizes, heights):
+    """verify_values (crates/stwo/src/core/pcs/verifier.rs:56-140) with the FRI verifier: sample_points
+    and sizes per tree and column (the column's evaluation log size), heights per tree."""
+    cfg = proof.config
+    fp = cfg.fri_params
+    lifting = cfg.trace_lifting_log_size
+    max_log_degree_bound = lifting - fp.log_blowup_factor
+    sv = proof.sampled_values
     # --- verify_values (pcs/verifier.rs:56-140)
     ch.mix_felts(np.asarray([list(v) for tree in sv for col in tree for v in col], np.uint32))
     quot_coeff = tuple(int(v) for v in ch.draw_secure_felt())
@@ -208,42 +290,52 @@ def verify_wide_fib_components(proof, n_cols_list, log_sizes):
     queries = sorted(set(int(q) for q in ch.draw_queries(column_log, fp.n_queries)))
 
     # tree decommitments
-    sizes = [[], [log_n + b for nc, log_n in zip(n_cols_list, log_sizes) for _ in range(nc)],
-             [max_log_degree_bound + b] * 8]
-    heights = [0, lifting, lifting]
-    for tree in range(3):
+    for tree in range(len(heights)):
         merkle_verify(proof.commitments[tree], heights[tree], sizes[tree], queries, proof.queried_values[tree],
                       proof.decommitments[tree])
 
-    # fri_answers: the DEEP quotient at every query (quotients.rs:115-184)
-    samples = [(mask_col[0]) for mask_col in sv[1]] + [c[0] for c in sv[2]]
-    queried = proof.queried_values[1] + proof.queried_values[2]
+    # fri_answers: the DEEP quotient at every query (quotients.rs:115-184). Samples in tree and column
+    # order, each with the next power of the quotient coefficient; a column sampled at (previous row,
+    # point) first opens the point shifted by the period G_(lifting - log size) with the point's
+    # value (build_samples_with_randomness_and_periodicity, crates/stwo/src/core/pcs/quotients.rs:274-319).
+    entries = []  # (point, value, queried values of the column)
+    for tree, (pts_t, sv_t) in enumerate(zip(sample_points, sv)):
+        for ci, (pts, vals) in enumerate(zip(pts_t, sv_t)):
+            col = proof.queried_values[tree][ci]
+            if len(pts) == 2:
+                per = point_of_index(1 << (31 - (lifting - sizes[tree][ci])))
+                entries.append((_qpoint_add(pts[1], (qm(int(per[0])), qm(int(per[1])))), tuple(vals[1]), col))
+            for pt, v in zip(pts, vals):
+                entries.append((pt, tuple(v), col))
     pow_ = qm(1)
     coeffs = []
-    for v in samples:
+    for pt, v, col in entries:
         a = qsub(qconj(v), v)
-        c = qsub(qconj(oods[1]), oods[1])
-        bb = qsub(qmul(v, c), qmul(a, oods[1]))
-        coeffs.append((qmul(pow_, a), qmul(pow_, bb), qmul(pow_, c)))
+        c = qsub(qconj(pt[1]), pt[1])
+        bb = qsub(qmul(v, c), qmul(a, pt[1]))
+        coeffs.append((pt, qmul(pow_, a), qmul(pow_, bb), qmul(pow_, c), col))
         pow_ = qmul(pow_, quot_coeff)
+
+    def cmul(u, w):
+        return ((u[0] * w[0] - u[1] * w[1]) % P, (u[0] * w[1] + u[1] * w[0]) % P)
+
     answers = []
     for k, pos in enumerate(queries):
         dx, dy = point_of_index(circle_domain_index(lifting, bitrev(pos, lifting)))
-        # denominator (prx - x) * piy - (pry - y) * pix in CM31
-        prx, pix = (oods[0][0], oods[0][1]), (oods[0][2], oods[0][3])
-        pry, piy = (oods[1][0], oods[1][1]), (oods[1][2], oods[1][3])
-        def cmul(u, w):
-            return ((u[0] * w[0] - u[1] * w[1]) % P, (u[0] * w[1] + u[1] * w[0]) % P)
-        d = tuple((s - t) % P for s, t in zip(cmul(((prx[0] - dx) % P, prx[1]), piy),
-                                                cmul(((pry[0] - dy) % P, pry[1]), pix)))
-        n = pow((d[0] * d[0] + d[1] * d[1]) % P, P - 2, P)
-        dinv_c = ((d[0] * n) % P, (-d[1] * n) % P)
-        num = qm(0)
-        for (a, bb, c), col in zip(coeffs, queried):
-            num = qadd(num, qsub(tuple((c_ * col[k]) % P for c_ in c), qadd(tuple((a_ * dy) % P for a_ in a), bb)))
-        r0 = cmul((num[0], num[1]), dinv_c)
-        r1 = cmul((num[2], num[3]), dinv_c)
-        answers.append((r0[0], r0[1], r1[0], r1[1]))
+        total = qm(0)
+        for pt, a, bb, c, col in coeffs:
+            # denominator (prx - x) * piy - (pry - y) * pix in CM31
+            prx, pix = (pt[0][0], pt[0][1]), (pt[0][2], pt[0][3])
+            pry, piy = (pt[1][0], pt[1][1]), (pt[1][2], pt[1][3])
+            d = tuple((s - t) % P for s, t in zip(cmul(((prx[0] - dx) % P, prx[1]), piy),
+                                                    cmul(((pry[0] - dy) % P, pry[1]), pix)))
+            n = pow((d[0] * d[0] + d[1] * d[1]) % P, P - 2, P)
+            dinv_c = ((d[0] * n) % P, (-d[1] * n) % P)
+            num = qsub(tuple((c_ * col[k]) % P for c_ in c), qadd(tuple((a_ * dy) % P for a_ in a), bb))
+            r0 = cmul((num[0], num[1]), dinv_c)
+            r1 = cmul((num[2], num[3]), dinv_c)
+            total = qadd(total, (r0[0], r0[1], r1[0], r1[1]))
+        answers.append(total)
 
     # FRI decommitment (fri.rs:306-399, 460-720), fold_step 1
     def rebuild(qs, evals, witness):

@@ -419,6 +419,14 @@ class CudaBackend:
                   _ptr_table([c.data for c in out.columns]), claimed, _stream())
         return out, np.array(list(claimed), np.uint32)
 
+    @staticmethod
+    def logup_composition(values: BaseColumn, inter: SecureColumnByCoords, trace_log: int, z, claimed, rc,
+                          accum: SecureColumnByCoords) -> None:
+        """Adds a single-column LogUp component's constraint quotients (evaluation domain of `values`)."""
+        _lib.call("cs_logup_composition", _ptr(values.data), _ptr_table([c.data for c in inter.columns]),
+                  values.log_size, trace_log, _u32_table(z), _u32_table(claimed), _u32_table(rc),
+                  _ptr_table([c.data for c in accum.columns]), _stream())
+
     # Poseidon2 AIR ------------------------------------------------------------
     POSEIDON_COLS = 1264
     POSEIDON_INTERACTION_COLS = 32

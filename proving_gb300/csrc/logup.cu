@@ -15,6 +15,7 @@
 #include "common.cuh"
 #include "field.cuh"
 #include "logup.cuh"
+#include "rows.cuh"
 
 namespace cs {
 
@@ -118,6 +119,46 @@ __global__ void add_offsets_kernel(Q4 io, uint32_t log_n, const uint32_t* offset
   for (int c = 0; c < 4; c++) io.c[c][pos] = m31_add(io.c[c][pos], offsets[4 * blockIdx.x + c]);
 }
 
+struct LookupCompParams {
+  const uint32_t* values;  // the trace column on the evaluation domain
+  const uint32_t* inter[4];
+  qm31 z, shift, rc;
+  uint32_t den[32];
+  uint32_t eval_log, trace_log;
+};
+
+// Quotient of a single-column LogUp component's one constraint
+// (cur - prev + shift) (v - z) + 1, weighted by rc, per evaluation row.
+__global__ void lookup_composition_kernel(const LookupCompParams p, uint32_t* a0, uint32_t* a1, uint32_t* a2,
+                                          uint32_t* a3) {
+  const uint32_t n = 1u << p.eval_log;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const uint32_t pr = prev_row(r, p.trace_log, p.eval_log);
+    const qm31 cur = qm31_make(__ldg(p.inter[0] + r), __ldg(p.inter[1] + r), __ldg(p.inter[2] + r),
+                               __ldg(p.inter[3] + r));
+    const qm31 prev = qm31_make(__ldg(p.inter[0] + pr), __ldg(p.inter[1] + pr), __ldg(p.inter[2] + pr),
+                                __ldg(p.inter[3] + pr));
+    const qm31 shifted = qm31_add(qm31_sub(cur, prev), p.shift);
+    const qm31 cons = qm31_add(qm31_mul(shifted, qm31_sub(qm31_make(__ldg(p.values + r), 0, 0, 0), p.z)),
+                               qm31_make(1, 0, 0, 0));
+    const qm31 v = qm31_mul_m31(qm31_mul(p.rc, cons), p.den[r >> p.trace_log]);
+    a0[r] = m31_add(a0[r], v.a.a);
+    a1[r] = m31_add(a1[r], v.a.b);
+    a2[r] = m31_add(a2[r], v.b.a);
+    a3[r] = m31_add(a3[r], v.b.b);
+  }
+}
+
+cpoint lookup_point_at(uint32_t idx) {
+  cpoint r{1, 0}, cur{2u, 1268011823u};
+  while (idx) {
+    if (idx & 1) r = cpoint_add(r, cur);
+    cur = cpoint_add(cur, cur);
+    idx >>= 1;
+  }
+  return r;
+}
+
 // Columns shorter than one scan block: one thread, in coset order.
 __global__ void small_scan_kernel(Q4 io, uint32_t log_n, qm31 shift) {
   const uint32_t n = 1u << log_n;
@@ -182,7 +223,7 @@ extern "C" cs_status cs_logup_running_sum(const uint32_t* d_values, uint32_t log
                                           uint32_t* const h_out[4], uint32_t claimed_sum_out[4], cs_stream stream) {
   CS_CHECK_ARG(d_values != nullptr && z != nullptr && h_out != nullptr && claimed_sum_out != nullptr,
                "logup_running_sum: null pointer");
-  CS_CHECK_ARG(log_size >= 10 && log_size <= 28, "logup_running_sum: log size %u outside [10, 28]", log_size);
+  CS_CHECK_ARG(log_size >= 1 && log_size <= 28, "logup_running_sum: log size %u outside [1, 28]", log_size);
   Q4 out;
   for (int c = 0; c < 4; c++) {
     CS_CHECK_ARG(h_out[c] != nullptr, "logup_running_sum: null output coordinate");
@@ -195,4 +236,47 @@ extern "C" cs_status cs_logup_running_sum(const uint32_t* d_values, uint32_t log
   note_launch();
   CS_CUDA(cudaGetLastError());
   return logup_finalize_last(out, log_size, claimed_sum_out, st);
+}
+
+extern "C" cs_status cs_logup_composition(const uint32_t* d_values, const uint32_t* const h_inter[4], uint32_t eval_log,
+                                          uint32_t trace_log, const uint32_t z[4], const uint32_t claimed_sum[4],
+                                          const uint32_t rc[4], uint32_t* const h_accum[4], cs_stream stream) {
+  CS_CHECK_ARG(d_values != nullptr && h_inter != nullptr && z != nullptr && claimed_sum != nullptr && rc != nullptr &&
+                   h_accum != nullptr,
+               "logup_composition: null pointer");
+  CS_CHECK_ARG(trace_log >= 1 && eval_log >= trace_log && eval_log - trace_log <= 5 && eval_log <= 30,
+               "logup_composition: bad sizes eval %u trace %u", eval_log, trace_log);
+  LookupCompParams p;
+  p.values = d_values;
+  for (int c = 0; c < 4; c++) {
+    CS_CHECK_ARG(h_inter[c] != nullptr && h_accum[c] != nullptr, "logup_composition: null column");
+    p.inter[c] = h_inter[c];
+  }
+  p.z = qm31_make(z[0], z[1], z[2], z[3]);
+  p.rc = qm31_make(rc[0], rc[1], rc[2], rc[3]);
+  // cumsum_shift = claimed_sum / 2^trace_log (LogupAtRow::new, crates/constraint-framework/src/logup.rs:32-40)
+  p.shift = qm31_mul_m31(qm31_make(claimed_sum[0], claimed_sum[1], claimed_sum[2], claimed_sum[3]),
+                         1u << (31 - trace_log));
+  p.eval_log = eval_log;
+  p.trace_log = trace_log;
+  const uint32_t log_expand = eval_log - trace_log, n_den = 1u << log_expand;
+  if (log_expand == 0) {
+    p.den[0] = 1;
+  } else {
+    // 1 / V_trace(eval_domain.at(i)), bit-reversed (component_prover.rs:101-108)
+    for (uint32_t i = 0; i < n_den; i++) {
+      const uint32_t idx = (subgroup_gen(eval_log + 1) + i * subgroup_gen(eval_log - 1)) & 0x7fffffffu;
+      uint32_t x = lookup_point_at(idx).x;
+      for (uint32_t k = 1; k < trace_log; k++) x = m31_sub(m31_add(m31_sqr(x), m31_sqr(x)), 1);
+      uint32_t j = 0;
+      for (uint32_t b = 0; b < log_expand; b++) j |= ((i >> b) & 1u) << (log_expand - 1 - b);
+      p.den[j] = m31_inv(x);
+    }
+  }
+  const uint32_t n = 1u << eval_log;
+  const uint32_t blocks = std::max(1u, std::min((n + 255) / 256, 152u * 8));
+  lookup_composition_kernel<<<blocks, 256, 0, to_stream(stream)>>>(p, h_accum[0], h_accum[1], h_accum[2],
+                                                                    h_accum[3]);
+  CS_LAUNCHED("lookup_composition_kernel");
+  return CS_OK;
 }

@@ -618,6 +618,199 @@ def prove_wide_fib_components(ops, traces, log_sizes, config: PcsConfig, channel
     return proof
 
 
+def _size_groups(logs):
+    """Indices grouped by log size, in first-seen order."""
+    groups = {}
+    for i, log_n in enumerate(logs):
+        groups.setdefault(log_n, []).append(i)
+    return groups
+
+
+def _evaluate_grouped(ops, coeffs, logs, log_blowup: int, twiddles):
+    """Coefficient columns of several sizes evaluated on their blown-up domains, one batched call per
+    size; returned in the input order."""
+    out = [None] * len(coeffs)
+    for log_n, idx in _size_groups(logs).items():
+        for i, e in zip(idx, ops.evaluate([coeffs[i] for i in idx], log_n + log_blowup, twiddles)):
+            out[i] = e
+    return out
+
+
+def prove_fib_and_lookups(ops, fib_traces, fib_logs, lookup_values, lookup_logs, config: PcsConfig,
+                          channel: Blake2sChannel, twiddles):
+    """Wide-Fibonacci components and single-column LogUp components in one proof (the batched mixed-size
+    trace: components of different sizes in one lifted tree, plus LogUp interaction columns). Follows
+    the example provers' flow (crates/examples/src/poseidon/mod.rs:336-379): the empty preprocessed
+    tree; the trace tree (every Wide-Fibonacci column, then each LogUp component's value column);
+    the lookup elements (z, alpha; crates/constraint-framework/src/logup.rs:70-79); the interaction
+    tree (each LogUp component's running-sum column, LogupTraceGenerator), after the claimed sums are
+    mixed into the channel; then prove_ex. A LogUp
+    component's relation entry has multiplicity -1 and values [v], so its fractions are 1 / (z - v)
+    and its one constraint is (cur - prev + claimed / 2^n) (v - z) + 1 (finalize_logup). Returns the
+    proof with `claimed_sums` (one per LogUp component, part of the statement, not serialized)."""
+    fp = config.fri_params
+    b = fp.log_blowup_factor
+    L = config.trace_lifting_log_size
+    if b != 1:
+        raise NotImplementedError("log_blowup_factor = 1 (SubDomain evaluation with log_expansion 0)")
+
+    pre_root = hashlib.blake2s(b"").digest()
+    channel.mix_root(pre_root)
+
+    # --- trace tree: every stage batched per column size across all components
+    fib_cols = [c for t in fib_traces for c in t]
+    fib_col_logs = [log_n for t, log_n in zip(fib_traces, fib_logs) for _ in t]
+    ops.interpolate(fib_cols, twiddles)
+    lookup_coeffs = [None] * len(lookup_values)
+    for log_n, idx in _size_groups(lookup_logs).items():
+        # out of place: the values stay for the interaction trace
+        for i, c in zip(idx, ops.interpolate_into([lookup_values[i] for i in idx], twiddles)):
+            lookup_coeffs[i] = c
+    trace_cols = _evaluate_grouped(ops, fib_cols + lookup_coeffs, fib_col_logs + list(lookup_logs), b, twiddles)
+    fib_evals, start = [], 0
+    for t in fib_traces:
+        fib_evals.append(trace_cols[start:start + len(t)])
+        start += len(t)
+    lookup_ext = trace_cols[start:]
+    trace_tree = ops.merkle_commit(trace_cols, L)
+    channel.mix_root(trace_tree.root)
+
+    # --- lookup elements and the interaction tree
+    z = channel.draw_secure_felt()
+    channel.draw_secure_felt()  # alpha: drawn with z; a one-value relation does not use it
+    inter_coeffs, claimed = [], []
+    for v in lookup_values:
+        col, cs = ops.logup_running_sum(v, z)
+        inter_coeffs += ops.secure_coords(col)
+        claimed.append(tuple(int(x) for x in cs))
+    inter_logs = [log_n for log_n in lookup_logs for _ in range(4)]
+    ops.interpolate(inter_coeffs, twiddles)
+    inter_cols = _evaluate_grouped(ops, inter_coeffs, inter_logs, b, twiddles)
+    inter_ext = [inter_cols[4 * k:4 * k + 4] for k in range(len(lookup_values))]
+    inter_tree = ops.merkle_commit(inter_cols, L)
+    # the claimed sums are part of the statement: mixed before the interaction commitment, as the
+    # state-machine example does with its second statement (crates/examples/src/state_machine/mod.rs:82-86)
+    channel.mix_felts(claimed)
+    channel.mix_root(inter_tree.root)
+
+    # --- composition polynomial: components in order take the last powers, reversed
+    random_coeff = channel.draw_secure_felt()
+    n_cons = [len(t) - 2 for t in fib_traces] + [1] * len(lookup_values)
+    total = sum(n_cons)
+    powers = secure_powers(random_coeff, total)
+    sub_acc, start = {}, 0
+
+    def acc_for(eval_log):
+        if eval_log not in sub_acc:
+            sub_acc[eval_log] = ops.secure_zeros(1 << eval_log)
+        return sub_acc[eval_log]
+
+    for evals, log_n, n in zip(fib_evals, fib_logs, n_cons):
+        rc = list(reversed(powers[total - start - n:total - start]))
+        ops.wide_fib_composition(evals, log_n, rc, acc_for(log_n + 1))
+        start += n
+    for k, log_n in enumerate(lookup_logs):
+        rc = powers[total - start - 1]
+        ops.logup_composition(lookup_ext[k], inter_ext[k], log_n, z, claimed[k], rc, acc_for(log_n + 1))
+        start += 1
+    accs = [sub_acc[k] for k in sorted(sub_acc)]
+    accum = accs[0] if len(accs) == 1 else ops.lift_and_accumulate(accs)
+    comp_log = max(sub_acc)
+    comp_coeffs = ops.interpolate_secure(accum, twiddles)
+    left, right = ops.split_at_mid(comp_coeffs)
+    comp_evals = ops.evaluate(left + right, (comp_log - 1) + b, twiddles)
+    comp_tree = ops.merkle_commit(comp_evals, L)
+    channel.mix_root(comp_tree.root)
+
+    # --- OODS
+    oods_pow = ops.grind(channel.digest, OODS_POW_BITS)
+    channel.mix_u64(oods_pow)
+    oods = random_point(channel.draw_secure_felt())
+    lifting = L
+    mldb = lifting - b
+    g = m31_subgroup_generator(mldb)
+    prev_pt = qpoint_add_m31(oods, (g[0], (-g[1]) % P))
+    columns = [[], trace_cols, inter_cols, comp_evals]
+    sample_points = [[], [[oods]] * len(trace_cols), [[prev_pt, oods]] * len(inter_cols), [[oods]] * 8]
+    sampled = sample_values(ops, columns, sample_points, lifting)
+    channel.mix_felts([v for tree in sampled for col in tree for v in col])
+    quotient_coeff = channel.draw_secure_felt()
+    quotients = compute_fri_quotients(ops, columns, sample_points, sampled, quotient_coeff, lifting, b, twiddles)
+    fri = fri_commit(ops, channel, fp, quotients, lifting, twiddles)
+
+    fri_pow = ops.grind(channel.digest, fp.pow_bits)
+    channel.mix_u64(fri_pow)
+    queries = sorted(set(channel.draw_queries(lifting, fp.n_queries)))
+    reads = Reads()
+    first = FriLayerDecommit(reads, quotients, fri["first"]["tree"], queries, fp.fold_step, ops)
+    inner = []
+    layer_queries = fold_queries(queries, fp.fold_step)
+    for layer in fri["inner"]:
+        inner.append(FriLayerDecommit(reads, layer["eval"], layer["tree"], layer_queries, layer["fold_step"], ops))
+        layer_queries = fold_queries(layer_queries, layer["fold_step"])
+    trees = [MerkleDecommit(reads, tree, queries, cols, ops)
+             for tree, cols in ((trace_tree, trace_cols), (inter_tree, inter_cols), (comp_tree, comp_evals))]
+    reads.run(ops)
+    proof = StarkProof(config=config)
+    proof.fri_first_layer = first.result()
+    proof.fri_inner_layers = [d.result() for d in inner]
+    proof.fri_last_layer_poly = fri["last_poly"]
+    proof.fri_proof_of_work = fri_pow
+    proof.commitments = [pre_root, trace_tree.root, inter_tree.root, comp_tree.root]
+    proof.oods_proof_of_work = oods_pow
+    proof.sampled_values = sampled
+    proof.decommitments = [[]]
+    proof.queried_values = [[]]
+    for d in trees:
+        qv, wit = d.result()
+        proof.queried_values.append(qv)
+        proof.decommitments.append(wit)
+    proof.claimed_sums = claimed
+
+    # --- sanity check (mod.rs:121-132)
+    comp = sampled[3]
+    left_v = from_partial_evals([comp[k][0] for k in range(4)])
+    right_v = from_partial_evals([comp[k][0] for k in range(4, 8)])
+    x = oods[0]
+    for _ in range(mldb - 1):
+        x = q_double_x(x)
+    composition_oods = qm_add(left_v, qm_mul(x, right_v))
+    expected = fib_and_lookups_at_point(oods, sampled, [len(t) for t in fib_traces], lookup_logs, z, claimed,
+                                        random_coeff, mldb)
+    if composition_oods != expected:
+        raise RuntimeError("constraints not satisfied (ProvingError::ConstraintsNotSatisfied)")
+    return proof
+
+
+def fib_and_lookups_at_point(point, sampled, n_cols_per_fib, lookup_logs, z, claimed, random_coeff,
+                             max_log_degree_bound: int):
+    """The composition polynomial at the point from the sampled values (Components::
+    eval_composition_polynomial_at_point): the Wide-Fibonacci constraints, then each LogUp
+    component's (cur - prev + claimed / 2^n) (v - z) + 1, Horner-combined, over V(mldb) at the point."""
+    x = point[0]
+    for _ in range(max_log_degree_bound - 1):
+        x = q_double_x(x)
+    den_inv = qm_inv(x)
+    m = np.asarray([c[0] for c in sampled[1]], np.int64)
+    cons, start = [], 0
+    for n in n_cols_per_fib:
+        a, b, c = m[start:start + n - 2], m[start + 1:start + n - 1], m[start + 2:start + n]
+        cons.append(qv_sub(c, qv_add(qv_mul(a, a), qv_mul(b, b))))
+        start += n
+    for k, log_n in enumerate(lookup_logs):
+        v = tuple(int(t) for t in m[start + k])
+        samples = sampled[2][4 * k:4 * k + 4]
+        prev = from_partial_evals([col[0] for col in samples])
+        cur = from_partial_evals([col[1] for col in samples])
+        shift = qm_mul(claimed[k], qm(m_inv(1 << log_n)))
+        shifted = qm_add(qm_sub(cur, prev), shift)
+        cons.append(np.asarray([qm_add(qm_mul(shifted, qm_sub(v, z)), qm(1))], np.int64))
+    cons = np.concatenate(cons, axis=0)
+    powers = np.asarray(list(reversed(secure_powers(random_coeff, len(cons)))), np.int64)
+    total = qv_sum(qv_mul(cons, powers))
+    return qm_mul(tuple(int(t) for t in total), den_inv)
+
+
 def q_double_point(pt):
     """CirclePoint::double over QM31."""
     return (q_double_x(pt[0]), qm_mul(qm(2), qm_mul(pt[0], pt[1])))
@@ -864,6 +1057,14 @@ class GpuOps:
 
     def merkle_commit(self, cols, L):
         return GpuMerkle(self.B.merkle_commit(cols, L), L)
+
+    # single-column LogUp components
+    def logup_running_sum(self, values, z):
+        return self.B.logup_running_sum(values, np.asarray(z, np.uint32))
+
+    def logup_composition(self, values_eval, inter_eval, trace_log, z, claimed, rc, accum):
+        self.B.logup_composition(values_eval, self.be.SecureColumnByCoords(inter_eval), trace_log, z, claimed, rc,
+                                 accum)
 
     # Poseidon2 AIR (crates/examples/src/poseidon/mod.rs)
     def poseidon_trace(self, log_n):

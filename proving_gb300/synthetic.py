@@ -83,3 +83,19 @@ def seeded_log_sizes(seed: int, n: int, lo: int, hi: int, mean: float) -> np.nda
     p = (lo_p + hi_p) / 2
     g = rng.geometric(p, n) - 1
     return (lo + np.minimum(cap, g)).astype(np.uint32)
+
+
+def mixed_trace_shape(seed: int = 7, n_base: int = 600, n_interaction: int = 120, lo: int = 10, hi: int = 22,
+                      mean: float = 16.0):
+    """The batched mixed-size trace as components: n_interaction single-column LogUp components
+    (one value column and one QM31 running-sum column each) and Wide-Fibonacci components holding
+    the other n_base - n_interaction base columns, all log sizes drawn by seeded_log_sizes. The
+    Wide-Fibonacci columns of one size form one component; a size drawn fewer than 3 times still
+    gets a 3-column component (the AIR's minimum). Returns ([(n_cols, log_n)], [lookup log_n])."""
+    fib_logs = seeded_log_sizes(seed, n_base - n_interaction, lo, hi, mean)
+    lookup_logs = [int(v) for v in seeded_log_sizes(seed + 1, n_interaction, lo, hi, mean)]
+    counts = {}
+    for v in fib_logs:
+        counts[int(v)] = counts.get(int(v), 0) + 1
+    comps = [(max(3, counts[k]), k) for k in sorted(counts)]
+    return comps, lookup_logs

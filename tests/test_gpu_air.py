@@ -39,7 +39,7 @@ def test_trace_and_composition(B, n_cols, log_n):
     assert all(np.array_equal(g, w) for g, w in zip(acc.to_cpu(), want))
 
 
-@pytest.mark.parametrize("log_n", [10, 13, 16])
+@pytest.mark.parametrize("log_n", [1, 3, 9, 10, 13, 16])
 def test_logup_running_sum(B, log_n):
     from proving_gb300.backend import BaseColumn
     v = m31_column(log_n + 40, log_n)
@@ -48,3 +48,21 @@ def test_logup_running_sum(B, log_n):
     want, wclaimed = O.logup_running_sum(v, z)
     assert list(claimed) == list(wclaimed)
     assert all(np.array_equal(g, w) for g, w in zip(got.to_cpu(), want))
+
+
+@pytest.mark.parametrize("trace_log,eval_log", [(1, 2), (4, 5), (10, 11), (13, 15)])
+def test_logup_composition(B, trace_log, eval_log):
+    # a single-column LogUp component's constraint quotients, (cur - prev + claimed / 2^n) (v - z) + 1
+    # over the vanishing polynomial, added to an accumulator that already holds values
+    from proving_gb300.backend import BaseColumn, SecureColumnByCoords
+    n = 1 << eval_log
+    v = m31_column(eval_log + 7, eval_log)
+    inter = [m31_column(eval_log + 8 + k, eval_log) for k in range(4)]
+    z, claimed, rc = seeded_qm31(1), seeded_qm31(2), seeded_qm31(3)
+    base = [m31_column(eval_log + 20 + k, eval_log) for k in range(4)]
+    acc = SecureColumnByCoords([BaseColumn.from_cpu(c) for c in base])
+    B.logup_composition(BaseColumn.from_cpu(v), SecureColumnByCoords([BaseColumn.from_cpu(c) for c in inter]),
+                        trace_log, z, claimed, rc, acc)
+    want = O.logup_composition(v, inter, trace_log, z, claimed, rc, out=[c.copy() for c in base])
+    assert len(acc) == n
+    assert all(np.array_equal(g, w) for g, w in zip(acc.to_cpu(), want))

@@ -62,3 +62,37 @@ def test_lifted_components_match_oracle(gpu):
     g, c = lifted_components_proof(gpu), lifted_components_proof(CpuOps())
     assert g.to_bytes() == c.to_bytes()
     verify_wide_fib_components(g, [4, 5], [9, 3])
+
+
+def test_fib_and_lookups_match_oracle(gpu):
+    # Wide-Fibonacci and LogUp components of four sizes in one proof: the same bytes and claimed sums
+    # on both backends, and the restated verifier accepts
+    from oracle.verifier import verify_fib_and_lookups
+    from test_prove_cpu import fib_and_lookups_proof
+    g, c = fib_and_lookups_proof(gpu), fib_and_lookups_proof(CpuOps())
+    assert g.claimed_sums == c.claimed_sums
+    assert g.to_bytes() == c.to_bytes()
+    verify_fib_and_lookups(g, [4, 5], [9, 3], [8, 4], g.claimed_sums)
+
+
+def test_mixed_shape_proof_matches_oracle(gpu):
+    # the batched mixed-size trace at a reduced scale (60 base columns, 12 LogUp components, log sizes
+    # 4..11): Wide-Fibonacci components per size plus LogUp components, same proof bytes on both backends
+    from oracle.verifier import verify_fib_and_lookups
+    from proving_gb300.synthetic import mixed_trace_shape
+    comps, lookup_logs = mixed_trace_shape(seed=3, n_base=60, n_interaction=12, lo=4, hi=11, mean=7.0)
+    max_log = max([l for _, l in comps] + lookup_logs)
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=max_log + 1)
+
+    def prove(ops):
+        traces = [ops.columns_from_host(O.wide_fib_trace(m31_column(10 + i, l), m31_column(50 + i, l), n))
+                  for i, (n, l) in enumerate(comps)]
+        values = [ops.columns_from_host([m31_column(90 + k, l)])[0] for k, l in enumerate(lookup_logs)]
+        return pr.prove_fib_and_lookups(ops, traces, [l for _, l in comps], values, lookup_logs, cfg,
+                                        pr.Blake2sChannel(), ops.twiddles(max_log + 2))
+
+    g, c = prove(gpu), prove(CpuOps())
+    assert g.to_bytes() == c.to_bytes()
+    assert g.claimed_sums == c.claimed_sums
+    verify_fib_and_lookups(g, [n for n, _ in comps], [l for _, l in comps], lookup_logs, g.claimed_sums)

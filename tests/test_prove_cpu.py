@@ -111,3 +111,38 @@ def test_lifted_components_prove_then_verify():
     bad.sampled_values[1][6][0] = tuple((v + 1) % O.P for v in bad.sampled_values[1][6][0])
     with pytest.raises(VerificationError):
         verify_wide_fib_components(bad, [4, 5], [9, 3])
+
+
+def fib_and_lookups_proof(ops):
+    # the mixed-size batched trace in one proof: Wide-Fibonacci components of 4 columns x 2^9 and
+    # 5 columns x 2^3, and single-column LogUp components of 2^8 and 2^4 rows (seeded values)
+    import numpy as np
+    traces = []
+    for n_cols, log_n in ((4, 9), (5, 3)):
+        a = np.ones(1 << log_n, np.uint32)
+        b = np.arange(1 << log_n, dtype=np.uint32)
+        traces.append(ops.columns_from_host(O.wide_fib_trace(a, b, n_cols)))
+    rng = np.random.default_rng(7)
+    lookups = [ops.columns_from_host([rng.integers(0, O.P, 1 << n, dtype=np.uint32)])[0] for n in (8, 4)]
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=3, fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=9 + 1)
+    return pr.prove_fib_and_lookups(ops, traces, [9, 3], lookups, [8, 4], cfg, pr.Blake2sChannel(),
+                                    ops.twiddles(10))
+
+
+def test_fib_and_lookups_prove_then_verify():
+    from oracle.verifier import verify_fib_and_lookups
+    proof = fib_and_lookups_proof(CpuOps())
+    claimed = proof.claimed_sums
+    verify_fib_and_lookups(proof, [4, 5], [9, 3], [8, 4], claimed)
+    assert [len(t) for t in proof.sampled_values] == [0, 11, 8, 8]
+    assert all(len(c) == 2 for c in proof.sampled_values[2])
+    # a wrong claimed sum (the statement) is rejected
+    wrong = [tuple((v + 1) % O.P for v in claimed[0])] + claimed[1:]
+    with pytest.raises(VerificationError):
+        verify_fib_and_lookups(proof, [4, 5], [9, 3], [8, 4], wrong)
+    # a tampered previous-row sample of the short LogUp component is rejected
+    bad = copy.deepcopy(proof)
+    bad.sampled_values[2][5][0] = tuple((v + 1) % O.P for v in bad.sampled_values[2][5][0])
+    with pytest.raises(VerificationError):
+        verify_fib_and_lookups(bad, [4, 5], [9, 3], [8, 4], claimed)
