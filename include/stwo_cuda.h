@@ -301,6 +301,15 @@ cs_status cs_wide_fib_trace(const uint32_t *d_a, const uint32_t *d_b, uint32_t l
 cs_status cs_logup_running_sum(const uint32_t *d_values, uint32_t log_size, const uint32_t z[4], uint32_t *const h_out[4],
                                uint32_t claimed_sum_out[4], cs_stream stream);
 
+/* cs_logup_running_sum for n_cols columns of any log sizes in [1, 28] in one
+   batch of launches (three per 48 columns), with no host synchronization:
+   column i reads h_values[i] (2^h_log_sizes[i] device words) and writes its
+   running sum into the coordinates h_out[4 i .. 4 i + 3]; its claimed sum
+   goes to d_claimed[4 i .. 4 i + 3] in device memory. Uses stream-ordered
+   device scratch. */
+cs_status cs_logup_running_sums(uint32_t n_cols, const uint32_t *const *h_values, const uint32_t *h_log_sizes,
+                                const uint32_t z[4], uint32_t *const *h_out, uint32_t *d_claimed, cs_stream stream);
+
 /* Constraint quotients of a single-column LogUp component (no counterpart
    AIR in the reference; built from its constraint framework): the relation
    entry (multiplicity -1, values [v]) finalized with finalize_logup
@@ -312,6 +321,16 @@ cs_status cs_logup_running_sum(const uint32_t *d_values, uint32_t log_size, cons
 cs_status cs_logup_composition(const uint32_t *d_values, const uint32_t *const h_inter[4], uint32_t eval_log,
                                uint32_t trace_log, const uint32_t z[4], const uint32_t claimed_sum[4],
                                const uint32_t rc[4], uint32_t *const h_accum[4], cs_stream stream);
+
+/* cs_logup_composition for n_comp components of the same trace size, their
+   quotients summed per row and added to h_accum once: component k reads
+   h_values[k] and the coordinates h_inter[4 k .. 4 k + 3], with its claimed
+   sum claimed_sums[4 k .. 4 k + 3] and weight rcs[4 k .. 4 k + 3] (host
+   words). One launch per 24 components. */
+cs_status cs_logup_compositions(uint32_t n_comp, const uint32_t *const *h_values, const uint32_t *const *h_inter,
+                                uint32_t eval_log, uint32_t trace_log, const uint32_t z[4],
+                                const uint32_t *claimed_sums, const uint32_t *rcs, uint32_t *const h_accum[4],
+                                cs_stream stream);
 
 /* ------------------------------------------------------- AIR: Poseidon2 */
 

@@ -69,6 +69,18 @@ class CpuOps:
         out, claimed = O.logup_running_sum(values.v, z)
         return SCol(out), claimed
 
+    def logup_running_sums(self, values, z):
+        cols, claimed = [], []
+        for v in values:
+            out, cs = O.logup_running_sum(v.v, z)
+            cols.append(SCol(out))
+            claimed.append(tuple(int(x) for x in cs))
+        return cols, claimed
+
+    def logup_compositions(self, values_evals, inter_evals, trace_log, z, claimed, rcs, accum):
+        for v, it, c, r in zip(values_evals, inter_evals, claimed, rcs):
+            self.logup_composition(v, it, trace_log, z, c, r, accum)
+
     def logup_composition(self, values_eval, inter_eval, trace_log, z, claimed, rc, accum):
         accum.c = O.logup_composition(values_eval.v, [c.v for c in inter_eval], trace_log, z, claimed, rc,
                                       out=accum.c)
@@ -147,6 +159,12 @@ class CpuOps:
 
     def barycentric_eval(self, cols, weights):
         return [tuple(int(x) for x in O.barycentric_eval(c.v, weights.c)) for c in cols]
+
+    def barycentric_eval_lazy(self, cols, weights):
+        return self.barycentric_eval(cols, weights)
+
+    def fetch_evals(self, handles):
+        return list(handles)
 
     def accumulate_numerators(self, cols, coeffs, log_blowup):
         arr = np.asarray(coeffs, np.uint32)

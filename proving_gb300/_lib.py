@@ -69,6 +69,8 @@ SIGNATURES = {
     "cs_fold_circle_into_line_device_alpha": [vp, u32, vp, vp, vp, u32, vp],
     "cs_channel_mix_root": [vp, vp, vp],
     "cs_channel_draw_secure_felt": [vp, vp, vp],
+    "cs_logup_running_sums": [u32, vp, vp, vp, vp, vp, vp],
+    "cs_logup_compositions": [u32, vp, vp, u32, u32, vp, vp, vp, vp, vp],
     "cs_logup_composition": [vp, vp, u32, u32, vp, vp, vp, vp, vp],
 }
 _RESTYPES = {"cs_last_error": ctypes.c_char_p, "cs_version": ctypes.c_char_p,

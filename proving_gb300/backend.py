@@ -107,11 +107,11 @@ class SecureColumnByCoords:
 
     @classmethod
     def zeros(cls, length: int):
-        return cls([BaseColumn.zeros(length) for _ in range(4)])
+        return cls(BaseColumn.rows_of(torch.zeros((4, length), dtype=torch.int32, device="cuda")))
 
     @classmethod
     def uninitialized(cls, length: int):
-        return cls([BaseColumn.uninitialized(length) for _ in range(4)])
+        return cls(BaseColumn.rows_of(torch.empty((4, length), dtype=torch.int32, device="cuda")))
 
     @classmethod
     def from_cpu(cls, coords):
@@ -420,11 +420,33 @@ class CudaBackend:
         return out, np.array(list(claimed), np.uint32)
 
     @staticmethod
+    def logup_running_sums(values, z):
+        """logup_running_sum for several columns of any sizes in one batch of launches. Returns the
+        running-sum columns and the claimed sums as an (n, 4) device tensor (not read back)."""
+        outs = [SecureColumnByCoords.uninitialized(len(v)) for v in values]
+        claimed = torch.empty((max(1, len(values)), 4), dtype=torch.int32, device="cuda")
+        _lib.call("cs_logup_running_sums", len(values), _ptr_table([v.data for v in values]),
+                  _u32_table([v.log_size for v in values]), _u32_table(z),
+                  _ptr_table([c.data for o in outs for c in o.columns]), _ptr(claimed), _stream())
+        return outs, claimed[:len(values)]
+
+    @staticmethod
     def logup_composition(values: BaseColumn, inter: SecureColumnByCoords, trace_log: int, z, claimed, rc,
                           accum: SecureColumnByCoords) -> None:
         """Adds a single-column LogUp component's constraint quotients (evaluation domain of `values`)."""
         _lib.call("cs_logup_composition", _ptr(values.data), _ptr_table([c.data for c in inter.columns]),
                   values.log_size, trace_log, _u32_table(z), _u32_table(claimed), _u32_table(rc),
+                  _ptr_table([c.data for c in accum.columns]), _stream())
+
+    @staticmethod
+    def logup_compositions(values, inters, trace_log: int, z, claimed, rcs, accum: SecureColumnByCoords) -> None:
+        """logup_composition for several components of the same trace size, summed per row before
+        they are added to the accumulator (one launch per 24 components)."""
+        if not values:
+            return
+        _lib.call("cs_logup_compositions", len(values), _ptr_table([v.data for v in values]),
+                  _ptr_table([c.data for it in inters for c in it.columns]), values[0].log_size, trace_log,
+                  _u32_table(z), _u32_table([w for c in claimed for w in c]), _u32_table([w for r in rcs for w in r]),
                   _ptr_table([c.data for c in accum.columns]), _stream())
 
     # Poseidon2 AIR ------------------------------------------------------------

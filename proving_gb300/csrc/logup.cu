@@ -7,10 +7,29 @@
 // circle-domain index k / 2 (k even) or n/2 + (n - 1 - k) / 2 (k odd)
 // (crates/stwo/src/core/utils.rs:177-188), stored at its bit reversal.
 //
-// Kernels: fractions (one QM31 inverse per row); claimed sum (one block);
-// block scans of 1024 coset-ordered values with the shift applied, writing
-// block totals; a scan of the totals; the block offsets added back.
+// Several columns of any sizes go through three launches per batch, with no
+// host round trip between them and with every HBM access coalesced. With
+// c the natural circle-domain index of storage position p (c = bitrev(p)),
+// P the inclusive prefix sum of the fractions g in natural order and
+// T = P(n - 1), the unshifted coset-order running sum at p is
+//   c < n/2 (p even, k = 2c):             P(c) + T - P(n - 1 - c)
+//   c >= n/2 (p odd, k = 2n - 1 - 2c):    P(n - 1 - c) + T - P(c) + g(c)
+// (the even coset indices walk the first half forward, the odd ones the
+// second half backward), and the mirror n - 1 - c sits at storage n - 1 - p.
+// The shift is applied last: sum_{j<=k} (f_j - s) = F_k - (k + 1) s.
+// Natural order is reached through 32 x 32 tiles: with c = (h, m, lo) (5, l - 10
+// and 5 bits), tile m holds 32 natural runs of 32 (one per h) and 32 storage
+// runs of 32 (one per lo).
+//   1. runs: per tile, the fractions (stored in place in the output) and the
+//      32 natural run totals;
+//   2. run offsets: one block per column scans its run totals into exclusive
+//      offsets (within 32 segments, plus the segment offsets); their sum is
+//      the claimed sum, kept in device memory;
+//   3. outputs: per pair of mirror tiles (m, ~m), the natural prefixes of both
+//      and then every output of both.
+// Columns of at most 2^9 rows are done by one block in the first launch.
 #include <algorithm>
+#include <vector>
 
 #include "common.cuh"
 #include "field.cuh"
@@ -21,127 +40,350 @@ namespace cs {
 
 namespace {
 
-constexpr uint32_t kScanBlock = 1024;
+constexpr uint32_t kSumBatch = 48;  // columns per launch (their pointers travel as kernel parameters)
+constexpr uint32_t kSmallLog = 9;   // columns up to 2^9 rows: one block each
+constexpr uint32_t kThreads = 1024;
 
-__device__ __forceinline__ uint32_t coset_pos(uint32_t k, uint32_t log_n) {
+struct SumBatch {
+  const uint32_t* values[kSumBatch];  // the looked-up values (fractions 1 / (z - v)), or null:
+                                      // the fractions are already in `out`
+  uint32_t* out[kSumBatch][4];
+  uint32_t log_size[kSumBatch];
+  uint32_t tile0[kSumBatch + 1];  // first launch-1 block of each column (one per tile; one if small)
+  uint32_t pair0[kSumBatch + 1];  // first launch-3 block of each column (none if small)
+  uint32_t run0[kSumBatch];       // first run total of each column in `runs` (4 words each)
+  uint32_t hoff0[kSumBatch];      // the column's 32 segment offsets in `runs`
+  uint32_t n_cols;
+  uint32_t* runs;     // 4 words per natural run of 32
+  uint32_t* claimed;  // 4 words per column
+  qm31 z;
+};
+
+__device__ __forceinline__ uint32_t rev5(uint32_t x) { return __brev(x) >> 27; }
+__device__ __forceinline__ uint32_t rev_bits(uint32_t x, uint32_t bits) { return bits ? __brev(x) >> (32 - bits) : 0; }
+
+// The column owning a block of a launch whose per-column first blocks are `first` (linear search
+// over at most kSumBatch entries of the parameter table).
+__device__ __forceinline__ uint32_t block_column(const uint32_t* first, uint32_t n_cols, uint32_t blk) {
+  uint32_t c = 0;
+  while (c + 1 < n_cols && first[c + 1] <= blk) c++;
+  return c;
+}
+
+__device__ __forceinline__ qm31 load_fraction(const SumBatch& b, uint32_t col, uint32_t p) {
+  if (b.values[col] != nullptr) return qm31_inv(qm31_sub(b.z, qm31_make(b.values[col][p], 0, 0, 0)));
+  return qm31_make(b.out[col][0][p], b.out[col][1][p], b.out[col][2][p], b.out[col][3][p]);
+}
+
+__device__ __forceinline__ void store4(const SumBatch& b, uint32_t col, uint32_t p, const qm31& v) {
+  b.out[col][0][p] = v.a.a;
+  b.out[col][1][p] = v.a.b;
+  b.out[col][2][p] = v.b.a;
+  b.out[col][3][p] = v.b.b;
+}
+
+// The shifted running sum at storage position p of natural index c, from the natural prefixes at c
+// (qp) and at its mirror (qm), the fraction g at c and the total t.
+__device__ __forceinline__ qm31 running_value(uint32_t c, uint32_t log_n, const qm31& qp, const qm31& qm,
+                                              const qm31& g, const qm31& t) {
   const uint32_t n = 1u << log_n;
-  const uint32_t c = (k & 1) ? (n >> 1) + ((n - 1 - k) >> 1) : (k >> 1);
-  return __brev(c) >> (32 - log_n);
+  const bool first_half = c < (n >> 1);
+  qm31 v = first_half ? qm31_sub(qm31_add(qp, t), qm) : qm31_add(qm31_sub(qm31_add(qm, t), qp), g);
+  const uint32_t k = first_half ? 2 * c : 2 * n - 1 - 2 * c;
+  // shift = t / n, 1 / n = 2^(31 - log_n) in M31
+  const qm31 shift = qm31_mul_m31(t, 1u << (31 - log_n));
+  return qm31_sub(v, qm31_mul_m31(shift, k + 1));
 }
 
-__global__ void fractions_kernel(const uint32_t* __restrict__ v, uint32_t n, qm31 z, Q4 out) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const qm31 f = qm31_inv(qm31_sub(z, qm31_make(v[i], 0, 0, 0)));
-    out.c[0][i] = f.a.a;
-    out.c[1][i] = f.a.b;
-    out.c[2][i] = f.b.a;
-    out.c[3][i] = f.b.b;
-  }
-}
-
-__global__ void sum_kernel(Q4 in, uint32_t n, uint32_t* sum_out) {
-  __shared__ uint64_t sh[32];
-  for (int k = 0; k < 4; k++) {
-    uint64_t acc = 0;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) acc += in.c[k][i];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint64_t t = 0;
-      for (uint32_t w = 0; w < blockDim.x / 32; w++) t += sh[w];
-      sum_out[k] = (uint32_t)(t % P);
-    }
-    __syncthreads();
-  }
-}
-
-// Inclusive scan of one M31 value per thread across a 1024-thread block.
-__device__ __forceinline__ uint32_t block_scan(uint32_t x, uint32_t* sh) {
+// Inclusive scan of four M31 values per thread across the block.
+__device__ __forceinline__ void block_scan4(uint32_t x[4], uint32_t (*sh)[32]) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= (uint32_t)o) x = m31_add(x, y);
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x[c], o);
+      if (lane >= (uint32_t)o) x[c] = m31_add(x[c], y);
+    }
   }
-  if (lane == 31) sh[warp] = x;
+  if (lane == 31) {
+#pragma unroll
+    for (int c = 0; c < 4; c++) sh[c][warp] = x[c];
+  }
   __syncthreads();
-  if (warp == 0) {
-    uint32_t t = lane < (blockDim.x >> 5) ? sh[lane] : 0;
+  if (warp < 4) {
+    uint32_t t = lane < (blockDim.x >> 5) ? sh[warp][lane] : 0;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
       if (lane >= (uint32_t)o) t = m31_add(t, y);
     }
-    sh[lane] = t;
+    sh[warp][lane] = t;
   }
   __syncthreads();
-  if (warp > 0) x = m31_add(x, sh[warp - 1]);
-  __syncthreads();
-  return x;
-}
-
-__global__ void __launch_bounds__(kScanBlock) block_scan_kernel(Q4 io, uint32_t log_n, qm31 shift,
-                                                                uint32_t* totals) {
-  __shared__ uint32_t sh[32];
-  const uint32_t k = blockIdx.x * kScanBlock + threadIdx.x;
-  const uint32_t pos = coset_pos(k, log_n);
-  const uint32_t s[4] = {shift.a.a, shift.a.b, shift.b.a, shift.b.b};
-  for (int c = 0; c < 4; c++) {
-    const uint32_t x = block_scan(m31_sub(io.c[c][pos], s[c]), sh);
-    io.c[c][pos] = x;
-    if (threadIdx.x == kScanBlock - 1) totals[4 * blockIdx.x + c] = x;
+  if (warp > 0) {
+#pragma unroll
+    for (int c = 0; c < 4; c++) x[c] = m31_add(x[c], sh[c][warp - 1]);
   }
+  __syncthreads();
 }
 
-// Exclusive scan of the block totals (one block, sequential chunks).
-__global__ void __launch_bounds__(kScanBlock) totals_scan_kernel(uint32_t* totals, uint32_t n_blocks) {
-  __shared__ uint32_t sh[32];
-  for (int c = 0; c < 4; c++) {
-    uint32_t carry = 0;
-    for (uint32_t base = 0; base < n_blocks; base += kScanBlock) {
-      const uint32_t i = base + threadIdx.x;
-      const uint32_t x = i < n_blocks ? totals[4 * i + c] : 0;
-      const uint32_t inc = block_scan(x, sh);
-      if (i < n_blocks) totals[4 * i + c] = m31_add(m31_sub(inc, x), carry);  // exclusive + carry
-      __shared__ uint32_t last;
-      if (threadIdx.x == kScanBlock - 1) last = inc;
-      __syncthreads();
-      carry = m31_add(carry, last);
-      __syncthreads();
+// Inclusive scan of four M31 values over the lanes of a warp.
+__device__ __forceinline__ void warp_scan4(uint32_t x[4]) {
+  const uint32_t lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x[c], o);
+      if (lane >= (uint32_t)o) x[c] = m31_add(x[c], y);
     }
   }
 }
 
-__global__ void add_offsets_kernel(Q4 io, uint32_t log_n, const uint32_t* offsets) {
-  const uint32_t k = blockIdx.x * kScanBlock + threadIdx.x;
-  const uint32_t pos = coset_pos(k, log_n);
-  for (int c = 0; c < 4; c++) io.c[c][pos] = m31_add(io.c[c][pos], offsets[4 * blockIdx.x + c]);
+// A column of at most 2^9 rows, all in one block.
+__device__ void small_column(const SumBatch& b, uint32_t col, uint32_t* flat, uint32_t (*sh)[32]) {
+  const uint32_t log_n = b.log_size[col], n = 1u << log_n, t = threadIdx.x;
+  qm31 g = qm31_make(0, 0, 0, 0);
+  uint32_t c = 0;
+  if (t < n) {
+    g = load_fraction(b, col, t);
+    c = rev_bits(t, log_n);
+    flat[c] = g.a.a;
+    flat[512 + c] = g.a.b;
+    flat[1024 + c] = g.b.a;
+    flat[1536 + c] = g.b.b;
+  }
+  __syncthreads();
+  uint32_t x[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) x[k] = t < n ? flat[512 * k + t] : 0;
+  block_scan4(x, sh);
+  if (t < n) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) flat[512 * k + t] = x[k];
+  }
+  __syncthreads();
+  const qm31 total = qm31_make(flat[n - 1], flat[512 + n - 1], flat[1024 + n - 1], flat[1536 + n - 1]);
+  if (t < n) {
+    const uint32_t mc = n - 1 - c;
+    const qm31 qp = qm31_make(flat[c], flat[512 + c], flat[1024 + c], flat[1536 + c]);
+    const qm31 qm = qm31_make(flat[mc], flat[512 + mc], flat[1024 + mc], flat[1536 + mc]);
+    store4(b, col, t, running_value(c, log_n, qp, qm, g, total));
+  }
+  if (t < 4) b.claimed[4 * col + t] = t == 0 ? total.a.a : t == 1 ? total.a.b : t == 2 ? total.b.a : total.b.b;
 }
 
+// Launch 1: per tile m of a column of 2^10 or more rows, thread (w, t) takes storage position
+// (rev5(w) << (l - 5)) | (rev(m) << 5) | t, i.e. natural (h = rev5(t), m, lo = w).
+__global__ void __launch_bounds__(kThreads) runs_kernel(const SumBatch b) {
+  __shared__ uint32_t tile[4][32][33];
+  __shared__ uint32_t sh[4][32];
+  const uint32_t col = block_column(b.tile0, b.n_cols, blockIdx.x);
+  const uint32_t log_n = b.log_size[col];
+  if (log_n <= kSmallLog) {
+    small_column(b, col, &tile[0][0][0], sh);
+    return;
+  }
+  const uint32_t mb = log_n - 10, m = blockIdx.x - b.tile0[col];
+  const uint32_t w = threadIdx.x >> 5, t = threadIdx.x & 31;
+  const uint32_t p = (rev5(w) << (log_n - 5)) | (rev_bits(m, mb) << 5) | t;
+  const qm31 g = load_fraction(b, col, p);
+  if (b.values[col] != nullptr) store4(b, col, p, g);
+  const uint32_t h = rev5(t);
+  tile[0][w][h] = g.a.a;
+  tile[1][w][h] = g.a.b;
+  tile[2][w][h] = g.b.a;
+  tile[3][w][h] = g.b.b;
+  __syncthreads();
+  // warp w sums natural run (h = w, m): lanes are lo
+  uint32_t x[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) x[k] = tile[k][t][w];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) x[k] = m31_add(x[k], __shfl_xor_sync(0xffffffffu, x[k], o));
+  }
+  if (t < 4) b.runs[4 * (b.run0[col] + ((w << mb) | m)) + t] = x[t];
+}
+
+// Launch 2: one block per column of 2^10 or more rows. The natural runs (h, m) are ordered h-major,
+// so warp h owns the contiguous runs [h 2^mb, (h + 1) 2^mb): it turns them into exclusive offsets
+// within its segment (coalesced, 32 runs per step), and the block turns the 32 segment totals into
+// the segment offsets `hoff` (added by launch 3); the grand total is the claimed sum.
+__global__ void __launch_bounds__(kThreads) run_offsets_kernel(const SumBatch b) {
+  __shared__ uint32_t seg_total[4][32];
+  const uint32_t col = blockIdx.x;
+  const uint32_t log_n = b.log_size[col];
+  if (log_n <= kSmallLog) return;
+  const uint32_t seg = 1u << (log_n - 10);
+  const uint32_t h = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint4* r = reinterpret_cast<uint4*>(b.runs) + b.run0[col] + (size_t)h * seg;
+  uint32_t carry[4] = {0, 0, 0, 0};
+  for (uint32_t base = 0; base < seg; base += 32) {
+    const bool live = base + lane < seg;
+    const uint4 v = live ? r[base + lane] : make_uint4(0, 0, 0, 0);
+    uint32_t x[4] = {v.x, v.y, v.z, v.w};
+    warp_scan4(x);
+    if (live)
+      r[base + lane] = make_uint4(m31_add(m31_sub(x[0], v.x), carry[0]), m31_add(m31_sub(x[1], v.y), carry[1]),
+                                  m31_add(m31_sub(x[2], v.z), carry[2]), m31_add(m31_sub(x[3], v.w), carry[3]));
+#pragma unroll
+    for (int k = 0; k < 4; k++) carry[k] = m31_add(carry[k], __shfl_sync(0xffffffffu, x[k], 31));
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) seg_total[k][h] = carry[k];
+  }
+  __syncthreads();
+  if (h == 0) {
+    uint32_t x[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) x[k] = seg_total[k][lane];
+    uint32_t own[4] = {x[0], x[1], x[2], x[3]};
+    warp_scan4(x);
+    uint4* hoff = reinterpret_cast<uint4*>(b.runs) + b.hoff0[col];
+    hoff[lane] = make_uint4(m31_sub(x[0], own[0]), m31_sub(x[1], own[1]), m31_sub(x[2], own[2]),
+                            m31_sub(x[3], own[3]));
+    if (lane == 31) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) b.claimed[4 * col + k] = x[k];
+    }
+  }
+}
+
+// Launch 3: per mirror pair of tiles (m, m' = ~m) of a column of 2^10 or more rows.
+__global__ void __launch_bounds__(kThreads) outputs_kernel(const SumBatch b) {
+  __shared__ uint32_t tiles[2][4][32][33];
+  const uint32_t col = block_column(b.pair0, b.n_cols, blockIdx.x);
+  const uint32_t log_n = b.log_size[col];
+  const uint32_t mb = log_n - 10;
+  const uint32_t m = blockIdx.x - b.pair0[col], mm = ((1u << mb) - 1) - m;
+  const uint32_t n_tiles = m == mm ? 1 : 2;
+  const uint32_t w = threadIdx.x >> 5, t = threadIdx.x & 31, h = rev5(t);
+  const uint32_t ms[2] = {m, mm};
+  qm31 g[2];
+  uint32_t pos[2];
+  for (uint32_t q = 0; q < n_tiles; q++) {
+    pos[q] = (rev5(w) << (log_n - 5)) | (rev_bits(ms[q], mb) << 5) | t;
+    const uint32_t p = pos[q];
+    g[q] = qm31_make(b.out[col][0][p], b.out[col][1][p], b.out[col][2][p], b.out[col][3][p]);
+    tiles[q][0][w][h] = g[q].a.a;
+    tiles[q][1][w][h] = g[q].a.b;
+    tiles[q][2][w][h] = g[q].b.a;
+    tiles[q][3][w][h] = g[q].b.b;
+  }
+  __syncthreads();
+  const uint32_t* r = b.runs + 4 * (size_t)b.run0[col];
+  const uint32_t* hoff = b.runs + 4 * (size_t)b.hoff0[col] + 4 * w;  // segment h = w
+  for (uint32_t q = 0; q < n_tiles; q++) {
+    // warp w: natural run (h = w, ms[q]); lanes are lo
+    uint32_t x[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) x[k] = tiles[q][k][t][w];
+    warp_scan4(x);
+    const uint32_t run = (w << mb) | ms[q];
+#pragma unroll
+    for (int k = 0; k < 4; k++) tiles[q][k][t][w] = m31_add(m31_add(x[k], r[4 * run + k]), hoff[k]);
+  }
+  __syncthreads();
+  const qm31 total = qm31_make(b.claimed[4 * col], b.claimed[4 * col + 1], b.claimed[4 * col + 2],
+                               b.claimed[4 * col + 3]);
+  for (uint32_t q = 0; q < n_tiles; q++) {
+    // element (h, ms[q], lo = w); its mirror (31 - h, ms[1 - q], 31 - w) is in the other tile
+    // (the same one when m = m')
+    const uint32_t o = n_tiles == 1 ? 0 : 1 - q;
+    const qm31 qp = qm31_make(tiles[q][0][w][h], tiles[q][1][w][h], tiles[q][2][w][h], tiles[q][3][w][h]);
+    const qm31 qm = qm31_make(tiles[o][0][31 - w][31 - h], tiles[o][1][31 - w][31 - h], tiles[o][2][31 - w][31 - h],
+                              tiles[o][3][31 - w][31 - h]);
+    const uint32_t c = (h << (log_n - 5)) | (ms[q] << 5) | w;
+    store4(b, col, pos[q], running_value(c, log_n, qp, qm, g[q], total));
+  }
+}
+
+// Runs the three launches over columns [0, n) of the tables; claimed sums to d_claimed (4 words each).
+cs_status scan_columns(const uint32_t* const* values, const Q4* outs, const uint32_t* log_sizes, uint32_t n,
+                       const qm31& z, uint32_t* d_claimed, cudaStream_t st) {
+  uint64_t all_runs = 0;  // run totals, then 32 segment offsets, per column of 2^10 or more rows
+  for (uint32_t i = 0; i < n; i++)
+    if (log_sizes[i] > kSmallLog) all_runs += (1ull << (log_sizes[i] - 5)) + 32;
+  uint32_t* runs = nullptr;
+  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&runs), sizeof(uint32_t) * 4 * std::max<uint64_t>(1, all_runs), st));
+  cs_status result = CS_OK;
+  uint64_t run_base = 0;
+  for (uint32_t b0 = 0; b0 < n && result == CS_OK; b0 += kSumBatch) {
+    SumBatch b;
+    b.n_cols = std::min<uint32_t>(kSumBatch, n - b0);
+    b.z = z;
+    b.claimed = d_claimed + 4 * b0;
+    b.runs = runs;
+    uint32_t tiles = 0, pairs = 0;
+    for (uint32_t i = 0; i < b.n_cols; i++) {
+      const uint32_t l = log_sizes[b0 + i];
+      b.values[i] = values != nullptr ? values[b0 + i] : nullptr;
+      for (int c = 0; c < 4; c++) b.out[i][c] = outs[b0 + i].c[c];
+      b.log_size[i] = l;
+      b.tile0[i] = tiles;
+      b.pair0[i] = pairs;
+      b.run0[i] = (uint32_t)run_base;
+      b.hoff0[i] = 0;
+      if (l <= kSmallLog) {
+        tiles += 1;
+      } else {
+        tiles += 1u << (l - 10);
+        pairs += l == 10 ? 1 : 1u << (l - 11);
+        b.hoff0[i] = (uint32_t)(run_base + (1ull << (l - 5)));
+        run_base += (1ull << (l - 5)) + 32;
+      }
+    }
+    b.tile0[b.n_cols] = tiles;
+    b.pair0[b.n_cols] = pairs;
+    runs_kernel<<<tiles, kThreads, 0, st>>>(b);
+    note_launch();
+    if (pairs > 0) {
+      run_offsets_kernel<<<b.n_cols, kThreads, 0, st>>>(b);
+      note_launch();
+      outputs_kernel<<<pairs, kThreads, 0, st>>>(b);
+      note_launch();
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) result = from_cuda(e, "logup running sum launch");
+  }
+  cudaError_t e = cudaFreeAsync(runs, st);
+  if (result == CS_OK && e != cudaSuccess) return from_cuda(e, "cudaFreeAsync");
+  return result;
+}
+
+constexpr uint32_t kCompBatch = 24;  // LogUp components per launch
+
 struct LookupCompParams {
-  const uint32_t* values;  // the trace column on the evaluation domain
-  const uint32_t* inter[4];
-  qm31 z, shift, rc;
+  const uint32_t* values[kCompBatch];  // each component's trace column on the evaluation domain
+  const uint32_t* inter[kCompBatch][4];
+  qm31 shift[kCompBatch], rc[kCompBatch];
+  qm31 z;
   uint32_t den[32];
-  uint32_t eval_log, trace_log;
+  uint32_t n_comp, eval_log, trace_log;
 };
 
-// Quotient of a single-column LogUp component's one constraint
-// (cur - prev + shift) (v - z) + 1, weighted by rc, per evaluation row.
-__global__ void lookup_composition_kernel(const LookupCompParams p, uint32_t* a0, uint32_t* a1, uint32_t* a2,
-                                          uint32_t* a3) {
+// Quotients of single-column LogUp components of one size: per evaluation row, the sum over the
+// components of rc (cur - prev + shift) (v - z) + 1, over V_trace, added to the accumulator once.
+__global__ void lookup_composition_kernel(const __grid_constant__ LookupCompParams p, uint32_t* a0, uint32_t* a1,
+                                          uint32_t* a2, uint32_t* a3) {
   const uint32_t n = 1u << p.eval_log;
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
     const uint32_t pr = prev_row(r, p.trace_log, p.eval_log);
-    const qm31 cur = qm31_make(__ldg(p.inter[0] + r), __ldg(p.inter[1] + r), __ldg(p.inter[2] + r),
-                               __ldg(p.inter[3] + r));
-    const qm31 prev = qm31_make(__ldg(p.inter[0] + pr), __ldg(p.inter[1] + pr), __ldg(p.inter[2] + pr),
-                                __ldg(p.inter[3] + pr));
-    const qm31 shifted = qm31_add(qm31_sub(cur, prev), p.shift);
-    const qm31 cons = qm31_add(qm31_mul(shifted, qm31_sub(qm31_make(__ldg(p.values + r), 0, 0, 0), p.z)),
-                               qm31_make(1, 0, 0, 0));
-    const qm31 v = qm31_mul_m31(qm31_mul(p.rc, cons), p.den[r >> p.trace_log]);
+    qm31 acc = qm31_make(0, 0, 0, 0);
+    for (uint32_t k = 0; k < p.n_comp; k++) {
+      const uint32_t* const* in = p.inter[k];
+      const qm31 cur = qm31_make(__ldg(in[0] + r), __ldg(in[1] + r), __ldg(in[2] + r), __ldg(in[3] + r));
+      const qm31 prev = qm31_make(__ldg(in[0] + pr), __ldg(in[1] + pr), __ldg(in[2] + pr), __ldg(in[3] + pr));
+      const qm31 shifted = qm31_add(qm31_sub(cur, prev), p.shift[k]);
+      const qm31 cons = qm31_add(qm31_mul(shifted, qm31_sub(qm31_make(__ldg(p.values[k] + r), 0, 0, 0), p.z)),
+                                 qm31_make(1, 0, 0, 0));
+      acc = qm31_add(acc, qm31_mul(p.rc[k], cons));
+    }
+    const qm31 v = qm31_mul_m31(acc, p.den[r >> p.trace_log]);
     a0[r] = m31_add(a0[r], v.a.a);
     a1[r] = m31_add(a1[r], v.a.b);
     a2[r] = m31_add(a2[r], v.b.a);
@@ -159,58 +401,18 @@ cpoint lookup_point_at(uint32_t idx) {
   return r;
 }
 
-// Columns shorter than one scan block: one thread, in coset order.
-__global__ void small_scan_kernel(Q4 io, uint32_t log_n, qm31 shift) {
-  const uint32_t n = 1u << log_n;
-  qm31 run = qm31_make(0, 0, 0, 0);
-  for (uint32_t k = 0; k < n; k++) {
-    const uint32_t pos = coset_pos(k, log_n);
-    run = qm31_add(run, qm31_sub(qm31_make(io.c[0][pos], io.c[1][pos], io.c[2][pos], io.c[3][pos]), shift));
-    io.c[0][pos] = run.a.a;
-    io.c[1][pos] = run.a.b;
-    io.c[2][pos] = run.b.a;
-    io.c[3][pos] = run.b.b;
-  }
-}
-
 }  // namespace
 
 cs_status logup_finalize_last(Q4 col, uint32_t log_size, uint32_t claimed_sum_out[4], cudaStream_t st) {
-  const uint32_t n = 1u << log_size, n_blocks = n / kScanBlock;
-  uint32_t* scratch = nullptr;  // 4 words of sum, then 4 words per scan block
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(uint32_t) * 4 * (1 + n_blocks), st));
-  cs_status result = CS_OK;
-  do {
-    sum_kernel<<<1, 1024, 0, st>>>(col, n, scratch);
-    note_launch();
-    uint32_t sum[4];
-    cudaError_t e = cudaMemcpyAsync(sum, scratch, sizeof(sum), cudaMemcpyDeviceToHost, st);
+  uint32_t* d_claimed = nullptr;
+  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_claimed), sizeof(uint32_t) * 4, st));
+  cs_status result = scan_columns(nullptr, &col, &log_size, 1, qm31_make(0, 0, 0, 0), d_claimed, st);
+  if (result == CS_OK) {
+    cudaError_t e = cudaMemcpyAsync(claimed_sum_out, d_claimed, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-      result = from_cuda(e, "logup finalize");
-      break;
-    }
-    for (int c = 0; c < 4; c++) claimed_sum_out[c] = sum[c];
-    // shift = claimed_sum / n, 1/n = 2^(31 - log_size)
-    const qm31 shift = qm31_mul_m31(qm31_make(sum[0], sum[1], sum[2], sum[3]), 1u << (31 - log_size));
-    if (n_blocks == 0) {
-      small_scan_kernel<<<1, 1, 0, st>>>(col, log_size, shift);
-      note_launch();
-      e = cudaGetLastError();
-      if (e != cudaSuccess) result = from_cuda(e, "logup finalize launch");
-      break;
-    }
-    uint32_t* totals = scratch + 4;
-    block_scan_kernel<<<n_blocks, kScanBlock, 0, st>>>(col, log_size, shift, totals);
-    note_launch();
-    totals_scan_kernel<<<1, kScanBlock, 0, st>>>(totals, n_blocks);
-    note_launch();
-    add_offsets_kernel<<<n_blocks, kScanBlock, 0, st>>>(col, log_size, totals);
-    note_launch();
-    e = cudaGetLastError();
-    if (e != cudaSuccess) result = from_cuda(e, "logup finalize launch");
-  } while (false);
-  cudaError_t e = cudaFreeAsync(scratch, st);
+    if (e != cudaSuccess) result = from_cuda(e, "logup finalize");
+  }
+  cudaError_t e = cudaFreeAsync(d_claimed, st);
   if (result == CS_OK && e != cudaSuccess) return from_cuda(e, "cudaFreeAsync");
   return result;
 }
@@ -230,33 +432,57 @@ extern "C" cs_status cs_logup_running_sum(const uint32_t* d_values, uint32_t log
     out.c[c] = h_out[c];
   }
   cudaStream_t st = to_stream(stream);
-  const uint32_t n = 1u << log_size;
-  fractions_kernel<<<std::min<uint32_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(
-      d_values, n, qm31_make(z[0], z[1], z[2], z[3]), out);
-  note_launch();
-  CS_CUDA(cudaGetLastError());
-  return logup_finalize_last(out, log_size, claimed_sum_out, st);
+  uint32_t* d_claimed = nullptr;
+  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_claimed), sizeof(uint32_t) * 4, st));
+  cs_status result = scan_columns(&d_values, &out, &log_size, 1, qm31_make(z[0], z[1], z[2], z[3]), d_claimed, st);
+  if (result == CS_OK) {
+    cudaError_t e = cudaMemcpyAsync(claimed_sum_out, d_claimed, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) result = from_cuda(e, "logup_running_sum");
+  }
+  cudaError_t e = cudaFreeAsync(d_claimed, st);
+  if (result == CS_OK && e != cudaSuccess) return from_cuda(e, "cudaFreeAsync");
+  return result;
 }
 
-extern "C" cs_status cs_logup_composition(const uint32_t* d_values, const uint32_t* const h_inter[4], uint32_t eval_log,
-                                          uint32_t trace_log, const uint32_t z[4], const uint32_t claimed_sum[4],
-                                          const uint32_t rc[4], uint32_t* const h_accum[4], cs_stream stream) {
-  CS_CHECK_ARG(d_values != nullptr && h_inter != nullptr && z != nullptr && claimed_sum != nullptr && rc != nullptr &&
-                   h_accum != nullptr,
-               "logup_composition: null pointer");
-  CS_CHECK_ARG(trace_log >= 1 && eval_log >= trace_log && eval_log - trace_log <= 5 && eval_log <= 30,
-               "logup_composition: bad sizes eval %u trace %u", eval_log, trace_log);
-  LookupCompParams p;
-  p.values = d_values;
-  for (int c = 0; c < 4; c++) {
-    CS_CHECK_ARG(h_inter[c] != nullptr && h_accum[c] != nullptr, "logup_composition: null column");
-    p.inter[c] = h_inter[c];
+extern "C" cs_status cs_logup_running_sums(uint32_t n_cols, const uint32_t* const* h_values,
+                                           const uint32_t* h_log_sizes, const uint32_t z[4],
+                                           uint32_t* const* h_out, uint32_t* d_claimed, cs_stream stream) {
+  CS_CHECK_ARG(n_cols == 0 || (h_values != nullptr && h_log_sizes != nullptr && h_out != nullptr),
+               "logup_running_sums: null table");
+  CS_CHECK_ARG(z != nullptr && (n_cols == 0 || d_claimed != nullptr), "logup_running_sums: null pointer");
+  std::vector<Q4> outs(n_cols);
+  for (uint32_t i = 0; i < n_cols; i++) {
+    CS_CHECK_ARG(h_values[i] != nullptr, "logup_running_sums: column %u has no values", i);
+    CS_CHECK_ARG(h_log_sizes[i] >= 1 && h_log_sizes[i] <= 28, "logup_running_sums: column %u log size %u outside "
+                 "[1, 28]", i, h_log_sizes[i]);
+    for (int c = 0; c < 4; c++) {
+      CS_CHECK_ARG(h_out[4 * i + c] != nullptr, "logup_running_sums: column %u coordinate %d is null", i, c);
+      outs[i].c[c] = h_out[4 * i + c];
+    }
   }
+  if (n_cols == 0) return CS_OK;
+  return scan_columns(h_values, outs.data(), h_log_sizes, n_cols, qm31_make(z[0], z[1], z[2], z[3]), d_claimed,
+                      to_stream(stream));
+}
+
+extern "C" cs_status cs_logup_compositions(uint32_t n_comp, const uint32_t* const* h_values,
+                                           const uint32_t* const* h_inter, uint32_t eval_log, uint32_t trace_log,
+                                           const uint32_t z[4], const uint32_t* claimed_sums, const uint32_t* rcs,
+                                           uint32_t* const h_accum[4], cs_stream stream) {
+  CS_CHECK_ARG(z != nullptr && h_accum != nullptr, "logup_compositions: null pointer");
+  CS_CHECK_ARG(n_comp == 0 || (h_values != nullptr && h_inter != nullptr && claimed_sums != nullptr && rcs != nullptr),
+               "logup_compositions: null table");
+  CS_CHECK_ARG(trace_log >= 1 && eval_log >= trace_log && eval_log - trace_log <= 5 && eval_log <= 30,
+               "logup_compositions: bad sizes eval %u trace %u", eval_log, trace_log);
+  for (int c = 0; c < 4; c++) CS_CHECK_ARG(h_accum[c] != nullptr, "logup_compositions: null accumulator");
+  for (uint32_t k = 0; k < n_comp; k++) {
+    CS_CHECK_ARG(h_values[k] != nullptr, "logup_compositions: component %u has no values", k);
+    for (int c = 0; c < 4; c++)
+      CS_CHECK_ARG(h_inter[4 * k + c] != nullptr, "logup_compositions: component %u coordinate %d is null", k, c);
+  }
+  static thread_local LookupCompParams p;
   p.z = qm31_make(z[0], z[1], z[2], z[3]);
-  p.rc = qm31_make(rc[0], rc[1], rc[2], rc[3]);
-  // cumsum_shift = claimed_sum / 2^trace_log (LogupAtRow::new, crates/constraint-framework/src/logup.rs:32-40)
-  p.shift = qm31_mul_m31(qm31_make(claimed_sum[0], claimed_sum[1], claimed_sum[2], claimed_sum[3]),
-                         1u << (31 - trace_log));
   p.eval_log = eval_log;
   p.trace_log = trace_log;
   const uint32_t log_expand = eval_log - trace_log, n_den = 1u << log_expand;
@@ -275,8 +501,29 @@ extern "C" cs_status cs_logup_composition(const uint32_t* d_values, const uint32
   }
   const uint32_t n = 1u << eval_log;
   const uint32_t blocks = std::max(1u, std::min((n + 255) / 256, 152u * 8));
-  lookup_composition_kernel<<<blocks, 256, 0, to_stream(stream)>>>(p, h_accum[0], h_accum[1], h_accum[2],
-                                                                    h_accum[3]);
-  CS_LAUNCHED("lookup_composition_kernel");
+  for (uint32_t k0 = 0; k0 < n_comp; k0 += kCompBatch) {
+    p.n_comp = std::min(kCompBatch, n_comp - k0);
+    for (uint32_t i = 0; i < p.n_comp; i++) {
+      const uint32_t k = k0 + i;
+      p.values[i] = h_values[k];
+      for (int c = 0; c < 4; c++) p.inter[i][c] = h_inter[4 * k + c];
+      p.rc[i] = qm31_make(rcs[4 * k], rcs[4 * k + 1], rcs[4 * k + 2], rcs[4 * k + 3]);
+      // cumsum_shift = claimed_sum / 2^trace_log (LogupAtRow::new, crates/constraint-framework/src/logup.rs:32-40)
+      p.shift[i] = qm31_mul_m31(qm31_make(claimed_sums[4 * k], claimed_sums[4 * k + 1], claimed_sums[4 * k + 2],
+                                          claimed_sums[4 * k + 3]),
+                                1u << (31 - trace_log));
+    }
+    lookup_composition_kernel<<<blocks, 256, 0, to_stream(stream)>>>(p, h_accum[0], h_accum[1], h_accum[2],
+                                                                      h_accum[3]);
+    CS_LAUNCHED("lookup_composition_kernel");
+  }
   return CS_OK;
+}
+
+extern "C" cs_status cs_logup_composition(const uint32_t* d_values, const uint32_t* const h_inter[4], uint32_t eval_log,
+                                          uint32_t trace_log, const uint32_t z[4], const uint32_t claimed_sum[4],
+                                          const uint32_t rc[4], uint32_t* const h_accum[4], cs_stream stream) {
+  CS_CHECK_ARG(d_values != nullptr && h_inter != nullptr && claimed_sum != nullptr && rc != nullptr,
+               "logup_composition: null pointer");
+  return cs_logup_compositions(1, &d_values, h_inter, eval_log, trace_log, z, claimed_sum, rc, h_accum, stream);
 }

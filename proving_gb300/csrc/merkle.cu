@@ -3,9 +3,17 @@
 // Leaves: crates/stwo/src/prover/backend/cpu/merkle_lifted.rs:46-90 — leaf i
 // hashes, in column order (columns sorted by length), the LE bytes of
 // col[(i >> (L - l + 1) << 1) + (i & 1)]; 16 columns fill one 64-byte Blake2s
-// block. One thread per leaf: a warp reads 32 consecutive words of a column
-// (coalesced), the 16 words of a block are loaded before the block is
-// compressed, and the chaining value stays in registers.
+// block. The lift of a leaf index to a shorter column is the composition of
+// the lifts through every intermediate size, so the chaining value after a
+// prefix of blocks whose columns are all of log size <= l depends only on the
+// leaf's lift to size l. Blocks are therefore compressed at the smallest size
+// that determines them (the largest log size among their 16 columns; the
+// final block at the tree height): one launch per such size, one thread per
+// index at that size, chaining values handed up through a pair of state
+// buffers (the same prefix sharing as blake2s_lifted.rs:46-200 in the SIMD
+// backend). A warp reads 32 consecutive words of a column of its own size
+// (coalesced), shorter columns through the cache. With columns of one size
+// this is a single launch at the tree height.
 // Nodes: merkle_lifted.rs:92-97 / crates/stwo/src/core/vcs_lifted/blake2_merkle.rs:29-36,
 // node = Blake2s(left || right), one 64-byte final block per node.
 #include <algorithm>
@@ -24,45 +32,58 @@ constexpr int kLeafThreads = 128;
 
 struct LeafParams {
   const uint32_t* cols[kMaxLeafCols];
-  uint8_t shift[kMaxLeafCols];  // L - l + 1
+  uint8_t log[kMaxLeafCols];  // column log sizes (sorted)
   uint32_t n_cols;
-  uint32_t log_leaves;
-  uint32_t one;  // 1, opaque to the compiler (see b2s_compress)
+  uint32_t level_log;            // the blocks of this launch are determined by the lift to this size
+  uint32_t prev_log;             // size of prev_state's indices
+  uint32_t block0, block1;       // blocks [block0, block1) of 16 columns
+  uint32_t is_final;             // block1 - 1 is the message's final block; out receives digests
+  const uint32_t* prev_state;    // chaining values after blocks [0, block0), or null (initial value)
+  uint32_t one;                  // 1, opaque to the compiler (see b2s_compress)
 };
+
+// Index of leaf-lift x (at log size `from`) in a column or state of log size `to` <= from.
+__device__ __forceinline__ uint32_t lift_index(uint32_t x, uint32_t from, uint32_t to) {
+  return from == to ? x : (((x >> (from - to + 1)) << 1) | (x & 1));
+}
 
 __global__ void __launch_bounds__(kLeafThreads) merkle_leaves_kernel(const __grid_constant__ LeafParams p,
                                                                      uint32_t* __restrict__ out) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (1u << p.log_leaves)) return;
+  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= (1u << p.level_log)) return;
   uint32_t h[8];
-  b2s_init(h);
   uint32_t m[16];
-  const uint32_t n_cols = p.n_cols;
-  if (n_cols == 0) {
+  if (p.n_cols == 0) {
+    b2s_init(h);
 #pragma unroll
     for (int k = 0; k < 16; k++) m[k] = 0;
     b2s_compress(h, m, 0, 0, true);
   } else {
-    const uint32_t n_blocks = (n_cols + 15) >> 4;
-    for (uint32_t b = 0; b < n_blocks; b++) {
+    if (p.prev_state != nullptr) {
+      const uint4* src = reinterpret_cast<const uint4*>(p.prev_state + (size_t)lift_index(x, p.level_log, p.prev_log) * 8);
+      const uint4 a = __ldg(src), b = __ldg(src + 1);
+      h[0] = a.x; h[1] = a.y; h[2] = a.z; h[3] = a.w;
+      h[4] = b.x; h[5] = b.y; h[6] = b.z; h[7] = b.w;
+    } else {
+      b2s_init(h);
+    }
+    for (uint32_t b = p.block0; b < p.block1; b++) {
       const uint32_t base = b << 4;
-      const bool last = b + 1 == n_blocks;
-      const uint32_t cnt = last ? n_cols - base : 16;
+      const bool last = p.is_final && b + 1 == p.block1;
+      const uint32_t cnt = min(16u, p.n_cols - base);
 #pragma unroll
       for (int k = 0; k < 16; k++) {
         uint32_t v = 0;
         if ((uint32_t)k < cnt) {
           const uint32_t c = base + k;
-          const uint32_t s = p.shift[c];
-          const uint32_t idx = ((i >> s) << 1) | (i & 1);
-          v = __ldg(p.cols[c] + idx);
+          v = __ldg(p.cols[c] + lift_index(x, p.level_log, p.log[c]));
         }
         m[k] = v;
       }
       b2s_compress(h, m, (base + cnt) * 4, 0, last, p.one);
     }
   }
-  uint4* o = reinterpret_cast<uint4*>(out + (size_t)i * 8);
+  uint4* o = reinterpret_cast<uint4*>(out + (size_t)x * 8);
   o[0] = make_uint4(h[0], h[1], h[2], h[3]);
   o[1] = make_uint4(h[4], h[5], h[6], h[7]);
 }
@@ -99,7 +120,6 @@ cs_status merkle_leaves(const uint32_t* const* cols, const uint32_t* log_sizes, 
   CS_CHECK_ARG(d_leaves != nullptr, "build_leaves: null output");
   static thread_local LeafParams p;
   p.n_cols = n_cols;
-  p.log_leaves = n_cols == 0 ? 0 : L;
   p.one = 1;
   uint32_t prev = 0;
   for (uint32_t c = 0; c < n_cols; c++) {
@@ -109,12 +129,57 @@ cs_status merkle_leaves(const uint32_t* const* cols, const uint32_t* log_sizes, 
     CS_CHECK_ARG(l >= prev, "build_leaves: columns must be sorted by length (column %u)", c);
     prev = l;
     p.cols[c] = cols[c];
-    p.shift[c] = (uint8_t)(L - l + 1);
+    p.log[c] = (uint8_t)l;
   }
-  const uint32_t n = 1u << p.log_leaves;
-  merkle_leaves_kernel<<<(n + kLeafThreads - 1) / kLeafThreads, kLeafThreads, 0, st>>>(p, d_leaves);
-  CS_LAUNCHED("merkle_leaves_kernel");
-  return CS_OK;
+  // launches: runs of non-final blocks by the size that determines them (the log size of their
+  // last column), then the final block (and any non-final blocks of the tree height) at L
+  const uint32_t n_blocks = n_cols == 0 ? 1 : (n_cols + 15) / 16;
+  struct Run {
+    uint32_t level, b0, b1;
+  };
+  std::vector<Run> runs;
+  for (uint32_t b = 0; b + 1 < n_blocks; b++) {
+    const uint32_t level = log_sizes[16 * b + 15];
+    if (level == L) break;
+    if (!runs.empty() && runs.back().level == level)
+      runs.back().b1 = b + 1;
+    else
+      runs.push_back({level, b, b + 1});
+  }
+  const uint32_t top_b0 = runs.empty() ? 0 : runs.back().b1;
+  uint32_t* states = nullptr;
+  size_t half = 0;  // words per state buffer
+  if (!runs.empty()) {
+    uint32_t max_level = 0;
+    for (const Run& r : runs) max_level = std::max(max_level, r.level);
+    half = (size_t)8 << max_level;
+    CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&states), sizeof(uint32_t) * 2 * half, st));
+  }
+  cs_status result = CS_OK;
+  const uint32_t* prev_state = nullptr;
+  uint32_t prev_log = 0;
+  for (size_t r = 0; r <= runs.size() && result == CS_OK; r++) {
+    const bool top = r == runs.size();
+    p.level_log = top ? (n_cols == 0 ? 0 : L) : runs[r].level;
+    p.block0 = top ? top_b0 : runs[r].b0;
+    p.block1 = top ? n_blocks : runs[r].b1;
+    p.is_final = top ? 1 : 0;
+    p.prev_state = prev_state;
+    p.prev_log = prev_log;
+    uint32_t* dst = top ? d_leaves : states + (r & 1) * half;
+    const uint32_t n = 1u << p.level_log;
+    merkle_leaves_kernel<<<(n + kLeafThreads - 1) / kLeafThreads, kLeafThreads, 0, st>>>(p, dst);
+    note_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) result = from_cuda(e, "merkle_leaves_kernel");
+    prev_state = dst;
+    prev_log = p.level_log;
+  }
+  if (states != nullptr) {
+    const cudaError_t e = cudaFreeAsync(states, st);
+    if (result == CS_OK && e != cudaSuccess) return from_cuda(e, "cudaFreeAsync");
+  }
+  return result;
 }
 
 cs_status merkle_next_layer(const uint32_t* d_prev, uint32_t log_out, uint32_t* d_out, cudaStream_t st) {

@@ -151,10 +151,13 @@ __device__ __forceinline__ void block_reduce_u64x4(uint64_t acc[4], uint64_t* sh
 }
 
 // Many columns at once: block (x, y) takes rows [2048 x, 2048 (x + 1)) of the 16 columns of group
-// y. Each thread keeps the weights of its 8 rows in registers and adds the unreduced 64-bit
-// products for every column (folding below 2^34 every 3 terms); warps and then the block reduce
-// per column, and the block writes its per-column partial sums (below 2^42) to `partial`, which
-// bary_final_kernel sums per column (at most 2^19 chunks: below 2^61).
+// y. Each thread keeps the weights of its 8 rows in registers, loads the rows of the next two columns
+// while it works on the current one, and adds the unreduced 64-bit products (folding below 2^34 every 3
+// terms). A warp reduces the four coordinates of a column at once (a butterfly that halves the
+// values per lane at each of the first two steps: 6 shuffles), writes them to shared memory, and the
+// block sums its warps for all its columns after one barrier. The per-column partial sums (below
+// 2^34) go to `partial`, one row of chunks per (column, coordinate), which bary_final_kernel sums
+// with one warp per row (at most 2^19 chunks: below 2^53).
 constexpr int kBaryThreads = 256;
 constexpr int kBaryRows = 8;  // rows per thread
 constexpr int kBaryChunk = kBaryThreads * kBaryRows;
@@ -162,13 +165,28 @@ constexpr int kBaryGroup = 16;  // columns per block
 
 __device__ __forceinline__ uint64_t fold34(uint64_t v) { return (v & P) + (v >> 31); }
 
+// The warp's sum of r[0..3] (each below P) for coordinate lane >> 3, in lanes 0, 8, 16, 24.
+__device__ __forceinline__ uint32_t warp_sum4(const uint32_t r[4], uint32_t lane) {
+  const bool hi = (lane >> 4) & 1;  // keeps coordinates 2, 3
+  uint32_t k0 = hi ? r[2] : r[0], k1 = hi ? r[3] : r[1];
+  const uint32_t s0 = hi ? r[0] : r[2], s1 = hi ? r[1] : r[3];
+  k0 = m31_add(k0, __shfl_xor_sync(0xffffffffu, s0, 16));
+  k1 = m31_add(k1, __shfl_xor_sync(0xffffffffu, s1, 16));
+  const bool odd = (lane >> 3) & 1;  // keeps the second of its pair
+  uint32_t v = odd ? k1 : k0;
+  v = m31_add(v, __shfl_xor_sync(0xffffffffu, odd ? k0 : k1, 8));
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) v = m31_add(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
 __global__ void __launch_bounds__(kBaryThreads) bary_partial_kernel(const BaryColumns cols, uint32_t nb,
                                                                    uint32_t log_n, CSoA w,
                                                                    unsigned long long* partial) {
-  __shared__ uint64_t sh[kBaryThreads / 32][4];
+  __shared__ uint32_t sh[kBaryGroup][kBaryThreads / 32][4];
   const uint32_t n = 1u << log_n;
   const uint32_t base = blockIdx.x * kBaryChunk;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t wr[kBaryRows][4];
 #pragma unroll
   for (int j = 0; j < kBaryRows; j++) {
@@ -178,13 +196,20 @@ __global__ void __launch_bounds__(kBaryThreads) bary_partial_kernel(const BaryCo
   }
   const uint32_t c0 = blockIdx.y * kBaryGroup;
   const uint32_t c1 = min(nb, c0 + kBaryGroup);
+  // rows of the current column and of the next two, loaded ahead
+  uint32_t x[kBaryRows], xn[kBaryRows], xnn[kBaryRows];
+#pragma unroll
+  for (int j = 0; j < kBaryRows; j++) {
+    const uint32_t row = base + threadIdx.x + j * kBaryThreads;
+    x[j] = row < n ? __ldg(cols.ptr[c0] + row) : 0;
+    xn[j] = (row < n && c0 + 1 < c1) ? __ldg(cols.ptr[c0 + 1] + row) : 0;
+  }
   for (uint32_t col = c0; col < c1; col++) {
-    const uint32_t* v = cols.ptr[col];
-    uint32_t x[kBaryRows];
+    const uint32_t* vnn = cols.ptr[col + 2 < c1 ? col + 2 : col];
 #pragma unroll
     for (int j = 0; j < kBaryRows; j++) {
       const uint32_t row = base + threadIdx.x + j * kBaryThreads;
-      x[j] = row < n ? __ldg(v + row) : 0;
+      xnn[j] = (row < n && col + 2 < c1) ? __ldg(vnn + row) : 0;
     }
     uint64_t acc[4] = {0, 0, 0, 0};
 #pragma unroll
@@ -195,31 +220,41 @@ __global__ void __launch_bounds__(kBaryThreads) bary_partial_kernel(const BaryCo
         if (j % 3 == 2) acc[k] = fold34(acc[k]);
       }
     }
+    uint32_t r[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      acc[k] = fold34(acc[k]);
-      for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
+      const uint64_t f = fold34(acc[k]);  // below 2^33
+      r[k] = m31_reduce_once((uint32_t)fold34(f));
     }
-    if (lane == 0)
+    const uint32_t v = warp_sum4(r, lane);
+    if ((lane & 7) == 0) sh[col - c0][warp][lane >> 3] = v;
 #pragma unroll
-      for (int k = 0; k < 4; k++) sh[warp][k] = acc[k];
-    __syncthreads();
-    if (threadIdx.x < 4) {
-      uint64_t t = 0;
-#pragma unroll
-      for (int q = 0; q < kBaryThreads / 32; q++) t += sh[q][threadIdx.x];
-      partial[((size_t)blockIdx.x * nb + col) * 4 + threadIdx.x] = t;
+    for (int j = 0; j < kBaryRows; j++) {
+      x[j] = xn[j];
+      xn[j] = xnn[j];
     }
-    __syncthreads();
+  }
+  __syncthreads();
+  const uint32_t t = threadIdx.x;
+  if (t < (c1 - c0) * 4) {
+    const uint32_t ci = t >> 2, k = t & 3;
+    uint64_t sum = 0;
+#pragma unroll
+    for (int q = 0; q < kBaryThreads / 32; q++) sum += sh[ci][q][k];
+    partial[((size_t)(c0 + ci) * 4 + k) * gridDim.x + blockIdx.x] = sum;
   }
 }
 
+// One warp per (column, coordinate): its row of per-chunk partial sums, strided over the lanes.
 __global__ void bary_final_kernel(const unsigned long long* partial, uint32_t n_chunks, uint32_t nb, uint32_t* out) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // (column, coordinate)
-  if (i >= nb * 4) return;
+  const uint32_t row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const uint32_t lane = threadIdx.x & 31;
+  if (row >= nb * 4) return;  // whole warps leave together
+  const unsigned long long* p = partial + (size_t)row * n_chunks;
   uint64_t t = 0;
-  for (uint32_t ch = 0; ch < n_chunks; ch++) t += partial[(size_t)ch * nb * 4 + i];
-  out[i] = reduce64(t % P);
+  for (uint32_t ch = lane; ch < n_chunks; ch += 32) t += p[ch];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  if (lane == 0) out[row] = reduce64(t % P);
 }
 
 // ---------------------------------------------------------------- eval_at_point
@@ -495,7 +530,7 @@ extern "C" cs_status cs_barycentric_eval(const uint32_t* const* h_cols, uint32_t
     bary_partial_kernel<<<dim3(n_chunks, (nb + kBaryGroup - 1) / kBaryGroup), kBaryThreads, 0, st>>>(
         cols, nb, log_size, w, partial);
     note_launch();
-    bary_final_kernel<<<(4 * nb + 255) / 256, 256, 0, st>>>(partial, n_chunks, nb, d_out + 4 * b0);
+    bary_final_kernel<<<(4 * nb + 7) / 8, 256, 0, st>>>(partial, n_chunks, nb, d_out + 4 * b0);
     note_launch();
     cudaError_t e = cudaGetLastError();
     const cudaError_t ef = cudaFreeAsync(partial, st);

@@ -15,6 +15,7 @@ oracle to compare proofs byte for byte.
 """
 from __future__ import annotations
 
+import functools
 import hashlib
 import struct
 from dataclasses import dataclass, field
@@ -298,7 +299,8 @@ def line_coeffs(py, value, alpha):
 
 
 def line_coeffs_v(py, values, alphas):
-    """line_coeffs for n sampled values at one point: (n, 3, 4) words (a, b, c per column)."""
+    """line_coeffs for n sampled values: (n, 3, 4) words (a, b, c per column). py: the sample
+    point's y, one for all values or one per value."""
     v, al = np.asarray(values, np.int64), np.asarray(alphas, np.int64)
     pyv = np.broadcast_to(np.asarray(py, np.int64), v.shape)
     a = qv_sub(qv_conj(v), v)
@@ -678,11 +680,8 @@ def prove_fib_and_lookups(ops, fib_traces, fib_logs, lookup_values, lookup_logs,
     # --- lookup elements and the interaction tree
     z = channel.draw_secure_felt()
     channel.draw_secure_felt()  # alpha: drawn with z; a one-value relation does not use it
-    inter_coeffs, claimed = [], []
-    for v in lookup_values:
-        col, cs = ops.logup_running_sum(v, z)
-        inter_coeffs += ops.secure_coords(col)
-        claimed.append(tuple(int(x) for x in cs))
+    sums, claimed = ops.logup_running_sums(lookup_values, z)
+    inter_coeffs = [c for col in sums for c in ops.secure_coords(col)]
     inter_logs = [log_n for log_n in lookup_logs for _ in range(4)]
     ops.interpolate(inter_coeffs, twiddles)
     inter_cols = _evaluate_grouped(ops, inter_coeffs, inter_logs, b, twiddles)
@@ -709,10 +708,14 @@ def prove_fib_and_lookups(ops, fib_traces, fib_logs, lookup_values, lookup_logs,
         rc = list(reversed(powers[total - start - n:total - start]))
         ops.wide_fib_composition(evals, log_n, rc, acc_for(log_n + 1))
         start += n
-    for k, log_n in enumerate(lookup_logs):
-        rc = powers[total - start - 1]
-        ops.logup_composition(lookup_ext[k], inter_ext[k], log_n, z, claimed[k], rc, acc_for(log_n + 1))
+    lookup_rc = []
+    for k in range(len(lookup_logs)):
+        lookup_rc.append(powers[total - start - 1])
         start += 1
+    for log_n, idx in _size_groups(lookup_logs).items():
+        # every LogUp component of one size in one pass over the evaluation domain
+        ops.logup_compositions([lookup_ext[k] for k in idx], [inter_ext[k] for k in idx], log_n, z,
+                               [claimed[k] for k in idx], [lookup_rc[k] for k in idx], acc_for(log_n + 1))
     accs = [sub_acc[k] for k in sorted(sub_acc)]
     accum = accs[0] if len(accs) == 1 else ops.lift_and_accumulate(accs)
     comp_log = max(sub_acc)
@@ -819,27 +822,32 @@ def q_double_point(pt):
 def sample_values(ops, columns, sample_points, lifting: int):
     """CommitmentSchemeProver::compute_samples (crates/stwo/src/prover/pcs/mod.rs:175-214): every
     column at every one of its sample points, each point doubled lifting - log_size times (the
-    column is committed lifted); one barycentric weight column per (log size, doubled point).
+    column is committed lifted). One barycentric weight column per (log size, point) across all
+    trees; every evaluation is launched before the values are read back once.
     Returns per tree, per column, the list of QM31 values."""
-    sampled = []
-    for tree_cols, pts in zip(columns, sample_points):
-        vals = [[None] * len(p_) for p_ in pts]
-        groups = {}
+    groups = {}
+    for ti, (tree_cols, pts) in enumerate(zip(columns, sample_points)):
         for ci, col in enumerate(tree_cols):
             ls = ops.log_size(col)
             for si, pt in enumerate(pts[ci]):
-                groups.setdefault((ls, pt), []).append((ci, si))
-        for (log_size, pt), members in groups.items():
-            for _ in range(lifting - log_size):
-                pt = q_double_point(pt)
-            w = ops.barycentric_weights(log_size, pt)
-            res = ops.barycentric_eval([tree_cols[ci] for ci, _ in members], w)
-            for (ci, si), v in zip(members, res):
-                vals[ci][si] = tuple(int(x) for x in v)
-        sampled.append(vals)
+                groups.setdefault((ls, pt), []).append((ti, ci, si))
+    doublings = {}  # point -> [point, 2 point, 4 point, ...]
+    pending = []
+    for (log_size, pt), members in groups.items():
+        chain = doublings.setdefault(pt, [pt])
+        while len(chain) <= lifting - log_size:
+            chain.append(q_double_point(chain[-1]))
+        w = ops.barycentric_weights(log_size, chain[lifting - log_size])
+        pending.append((members, ops.barycentric_eval_lazy([columns[ti][ci] for ti, ci, _ in members], w)))
+    results = ops.fetch_evals([h for _, h in pending])
+    sampled = [[[None] * len(p_) for p_ in pts] for pts in sample_points]
+    for (members, _), res in zip(pending, results):
+        for (ti, ci, si), v in zip(members, res):
+            sampled[ti][ci][si] = v
     return sampled
 
 
+@functools.lru_cache(maxsize=64)
 def m31_subgroup_generator(log_size: int):
     """The generator G_log_size of the circle subgroup of order 2^log_size, as an M31 point."""
     return index_to_point(1 << (31 - log_size))
@@ -876,8 +884,9 @@ def compute_fri_quotients(ops, columns, sample_points, sampled, random_coeff, li
     column with its random power, grouped by column size and sample point, accumulated, lifted and
     combined into the FRI quotient column."""
     n_samples = sum(len(c) + (1 if len(c) == 2 else 0) for tree in sampled for c in tree)
-    pows = iter(secure_powers(random_coeff, n_samples))
-    entries = []  # (log size, column, point, value, random power) in tree/column order
+    pows = secure_powers(random_coeff, n_samples)
+    entries = []  # (log size, column, point, value) in tree/column order; entry k has power k
+    shifted = {}  # (point, log period) -> the point shifted by the period
     for tree_cols, pts, vals in zip(columns, sample_points, sampled):
         for col, cp, cv in zip(tree_cols, pts, vals):
             ls = ops.log_size(col)
@@ -885,22 +894,26 @@ def compute_fri_quotients(ops, columns, sample_points, sampled, random_coeff, li
                 # build_samples_with_randomness_and_periodicity (crates/stwo/src/core/pcs/quotients.rs:274-319):
                 # a column sampled at (previous row, point) also opens the point shifted by the
                 # period G_(lifting - log size), with the point's value, first
-                period = m31_subgroup_generator(lifting - ls)
-                entries.append((ls, col, qpoint_add_m31(cp[1], period), cv[1], next(pows)))
+                key = (cp[1], lifting - ls)
+                if key not in shifted:
+                    shifted[key] = qpoint_add_m31(cp[1], m31_subgroup_generator(lifting - ls))
+                entries.append((ls, col, shifted[key], cv[1]))
             for p_, v_ in zip(cp, cv):
-                entries.append((ls, col, p_, v_, next(pows)))
+                entries.append((ls, col, p_, v_))
+    # every sample's line coefficients in one vectorized pass
+    all_coeffs = line_coeffs_v(np.asarray([e[2][1] for e in entries], np.int64),
+                               [e[3] for e in entries], pows[:len(entries)])
     # stable sort by column log size, group by size, batch by point in insertion order
     by_size = {}
-    for e in entries:
-        by_size.setdefault(e[0], []).append(e[1:])
+    for k, e in enumerate(entries):
+        by_size.setdefault(e[0], []).append(k)
     accs = []  # (point, partial numerator column, first linear term)
     for ls in sorted(by_size):
         batches = {}
-        for col, p_, v_, rp in by_size[ls]:
-            batches.setdefault(p_, []).append((col, v_, rp))
-        for p_, items in batches.items():
-            coeffs = line_coeffs_v(p_[1], [v_ for _, v_, _ in items], [rp for _, _, rp in items])
-            part, first_linear = ops.accumulate_numerators([c for c, _, _ in items], coeffs, log_blowup)
+        for k in by_size[ls]:
+            batches.setdefault(entries[k][2], []).append(k)
+        for p_, ks in batches.items():
+            part, first_linear = ops.accumulate_numerators([entries[k][1] for k in ks], all_coeffs[ks], log_blowup)
             accs.append((p_, part, tuple(int(x) for x in first_linear)))
     # group per sample point (sorted by (x, y)), lift and accumulate ascending sizes
     per_point = {}
@@ -1062,6 +1075,15 @@ class GpuOps:
     def logup_running_sum(self, values, z):
         return self.B.logup_running_sum(values, np.asarray(z, np.uint32))
 
+    def logup_running_sums(self, values, z):
+        """Every column's running sum in one batch of launches; the claimed sums read back once."""
+        cols, claimed = self.B.logup_running_sums(values, np.asarray(z, np.uint32))
+        return cols, [tuple(int(x) for x in row) for row in claimed.cpu().numpy().view(np.uint32)]
+
+    def logup_compositions(self, values_evals, inter_evals, trace_log, z, claimed, rcs, accum):
+        self.B.logup_compositions(values_evals, [self.be.SecureColumnByCoords(it) for it in inter_evals], trace_log,
+                                  z, claimed, [[int(w) for w in r] for r in rcs], accum)
+
     def logup_composition(self, values_eval, inter_eval, trace_log, z, claimed, rc, accum):
         self.B.logup_composition(values_eval, self.be.SecureColumnByCoords(inter_eval), trace_log, z, claimed, rc,
                                  accum)
@@ -1161,8 +1183,23 @@ class GpuOps:
         return self.B.barycentric_weights(log_size, point)
 
     def barycentric_eval(self, cols, weights):
-        out = self.B.barycentric_eval_at_point(cols, weights).cpu().numpy().view(np.uint32)
-        return [tuple(int(x) for x in row) for row in out]
+        return self.fetch_evals([self.barycentric_eval_lazy(cols, weights)])[0]
+
+    def barycentric_eval_lazy(self, cols, weights):
+        """The values of cols at the weights' point, left on the device: (n, 4) words."""
+        return self.B.barycentric_eval_at_point(cols, weights)
+
+    def fetch_evals(self, handles):
+        """Reads back the results of barycentric_eval_lazy calls in one copy."""
+        import torch
+        if not handles:
+            return []
+        flat = torch.cat(handles).cpu().numpy().view(np.uint32).tolist()
+        out, k = [], 0
+        for h in handles:
+            out.append([tuple(r) for r in flat[k:k + h.shape[0]]])
+            k += h.shape[0]
+        return out
 
     def accumulate_numerators(self, cols, coeffs, log_blowup):
         return self.B.accumulate_numerators(cols, np.asarray(coeffs, np.uint32), log_blowup)

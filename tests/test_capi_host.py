@@ -75,6 +75,17 @@ def test_invalid_arguments_are_rejected_on_host(lib):
     src = (ctypes.c_void_p * 4)(1 << 20, 1 << 21, 1 << 22, 1 << 23)
     alpha = (ctypes.c_uint32 * 4)(1, 2, 3, 4)
     assert _status(lib, "cs_fold_line", src, 12, alpha, src, ctypes.c_void_p(1 << 24), 10, null) == INVALID
+    # batched LogUp running sums: a log size of 0 and a null output coordinate
+    vals = (ctypes.c_void_p * 2)(1 << 20, 1 << 21)
+    outs = (ctypes.c_void_p * 8)(*[1 << (22 + k) for k in range(8)])
+    z = (ctypes.c_uint32 * 4)(1, 2, 3, 4)
+    assert _status(lib, "cs_logup_running_sums", 2, vals, (ctypes.c_uint32 * 2)(4, 0), z, outs,
+                   ctypes.c_void_p(1 << 30), null) == INVALID
+    assert b"log size" in lib.cs_last_error()
+    outs[5] = None
+    assert _status(lib, "cs_logup_running_sums", 2, vals, (ctypes.c_uint32 * 2)(4, 5), z, outs,
+                   ctypes.c_void_p(1 << 30), null) == INVALID
+    assert b"coordinate" in lib.cs_last_error()
 
 
 def test_error_raises_in_python_mirror(lib):

@@ -50,6 +50,20 @@ def test_logup_running_sum(B, log_n):
     assert all(np.array_equal(g, w) for g, w in zip(got.to_cpu(), want))
 
 
+def test_logup_running_sums_batched(B):
+    # 60 columns of sizes 2^1 .. 2^16 in one batch of launches (two kernel batches of 48 columns)
+    from proving_gb300.backend import BaseColumn
+    logs = [1 + (k * 7) % 16 for k in range(60)]
+    z = seeded_qm31(99)
+    vals = [m31_column(1000 + k, l) for k, l in enumerate(logs)]
+    outs, claimed = B.logup_running_sums([BaseColumn.from_cpu(v) for v in vals], z)
+    claimed = claimed.cpu().numpy().view(np.uint32)
+    for k, (v, out) in enumerate(zip(vals, outs)):
+        want, wclaimed = O.logup_running_sum(v, z)
+        assert list(claimed[k]) == list(wclaimed)
+        assert all(np.array_equal(g, w) for g, w in zip(out.to_cpu(), want))
+
+
 @pytest.mark.parametrize("trace_log,eval_log", [(1, 2), (4, 5), (10, 11), (13, 15)])
 def test_logup_composition(B, trace_log, eval_log):
     # a single-column LogUp component's constraint quotients, (cur - prev + claimed / 2^n) (v - z) + 1
@@ -65,4 +79,25 @@ def test_logup_composition(B, trace_log, eval_log):
                         trace_log, z, claimed, rc, acc)
     want = O.logup_composition(v, inter, trace_log, z, claimed, rc, out=[c.copy() for c in base])
     assert len(acc) == n
+    assert all(np.array_equal(g, w) for g, w in zip(acc.to_cpu(), want))
+
+
+def test_logup_compositions_batched(B):
+    # 30 LogUp components of one size in two launches: the same accumulator as one call each
+    from proving_gb300.backend import BaseColumn, SecureColumnByCoords
+    trace_log, eval_log = 9, 10
+    comps = []
+    for k in range(30):
+        v = m31_column(300 + k, eval_log)
+        inter = [m31_column(400 + 4 * k + c, eval_log) for c in range(4)]
+        comps.append((v, inter, seeded_qm31(500 + k), seeded_qm31(600 + k)))
+    z = seeded_qm31(7)
+    base = [m31_column(700 + c, eval_log) for c in range(4)]
+    acc = SecureColumnByCoords([BaseColumn.from_cpu(c) for c in base])
+    B.logup_compositions([BaseColumn.from_cpu(v) for v, _, _, _ in comps],
+                         [SecureColumnByCoords([BaseColumn.from_cpu(c) for c in it]) for _, it, _, _ in comps],
+                         trace_log, z, [c for _, _, c, _ in comps], [r for _, _, _, r in comps], acc)
+    want = [c.copy() for c in base]
+    for v, it, c, r in comps:
+        want = O.logup_composition(v, it, trace_log, z, c, r, out=want)
     assert all(np.array_equal(g, w) for g, w in zip(acc.to_cpu(), want))

@@ -119,7 +119,11 @@ def test_merkle_leaves_kat(B):
 
 
 @pytest.mark.parametrize("log_sizes,L", [([4], 4), ([3, 5, 5, 9], 9), ([1, 2], 6), ([6] * 16, 6), ([6] * 17, 6),
-                                         ([7] * 33, 10), (list(range(1, 13)) * 3, 14)])
+                                         ([7] * 33, 10), (list(range(1, 13)) * 3, 14),
+                                         # prefix chaining values handed up through several sizes
+                                         ([3] * 20 + [5] * 20 + [8] * 40, 9), ([2] * 16 + [4] * 16 + [6] * 16, 6),
+                                         ([5] * 10 + [7] * 40, 7), ([1] * 16 + [3] * 15 + [9] * 2, 9),
+                                         ([4] * 48 + [6] * 16 + [10] * 17, 11)])
 def test_merkle_commit_matches_oracle(B, log_sizes, L):
     cols_np = [m31_column(i * 31 + l, l) for i, l in enumerate(log_sizes)]
     perm = np.random.default_rng(0).permutation(len(cols_np))  # commit sorts (stably) by length
