@@ -445,7 +445,7 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
         torch.cuda.synchronize()
         if k >= 1:
             lat.append((time.perf_counter() - t0) * 1e3)
-        torch.cuda.empty_cache()
+    torch.cuda.empty_cache()
     # the constraint-quotient kernel alone on the evaluation domain CanonicCoset(log_n_rows + 2)
     eval_log = log_n_rows + ps.LOG_EXPAND
     trace = CudaBackend.poseidon_trace(log_n_rows)
@@ -639,11 +639,14 @@ def run_gpu(args):
     e2e_value = world * args.steps / (float(t.item()) / 1e3)
 
     peaks_int = int_peaks(torch)
-    wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
+    from proving_gb300.serving import collector_paused
+    with collector_paused():
+        wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
     bvp = batched_vs_plain(torch, cs) if not args.skip_plain else None
     serving_res = serving_leg() if not args.skip_serving else None
-    poseidon_res = poseidon_prove_leg(torch, args.poseidon_log_rows) if not args.skip_poseidon else None
-    mixed_res = mixed_prove_leg(torch) if not args.skip_mixed_prove else None
+    with collector_paused():
+        poseidon_res = poseidon_prove_leg(torch, args.poseidon_log_rows) if not args.skip_poseidon else None
+        mixed_res = mixed_prove_leg(torch) if not args.skip_mixed_prove else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()

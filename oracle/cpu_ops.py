@@ -6,6 +6,8 @@ from __future__ import annotations
 
 import numpy as np
 
+from proving_gb300 import prover as pr
+
 from . import oracle as O
 
 
@@ -48,6 +50,9 @@ class Twiddles:
 
 
 class CpuOps:
+    def secure_powers(self, felt, n):
+        return pr.secure_powers(felt, n)
+
     def twiddles(self, root_log_domain: int):
         return Twiddles(root_log_domain)
 

@@ -317,9 +317,9 @@ class CudaBackend:
 
     @staticmethod
     def generate_secure_powers(felt, n_powers: int) -> np.ndarray:
-        out = (ctypes.c_uint32 * max(4, 4 * n_powers))()
-        _lib.call("cs_generate_secure_powers", _u32_table(felt), n_powers, out)
-        return np.array(list(out), np.uint32)[: 4 * n_powers].reshape(n_powers, 4)
+        out = np.empty((max(1, n_powers), 4), np.uint32)
+        _lib.call("cs_generate_secure_powers", _u32_table(felt), n_powers, out.ctypes.data)
+        return out[:n_powers]
 
     @staticmethod
     def lift_and_accumulate(cols):
@@ -397,7 +397,7 @@ class CudaBackend:
     # AIR (Wide-Fibonacci) ---------------------------------------------------------
     @staticmethod
     def wide_fib_trace(a: BaseColumn, b: BaseColumn, n_cols: int):
-        cols = [BaseColumn.uninitialized(len(a)) for _ in range(n_cols)]
+        cols = BaseColumn.rows_of(torch.empty((n_cols, len(a)), dtype=torch.int32, device="cuda"))
         _lib.call("cs_wide_fib_trace", _ptr(a.data), _ptr(b.data), a.log_size, n_cols,
                   _ptr_table([c.data for c in cols]), _stream())
         return cols

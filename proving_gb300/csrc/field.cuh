@@ -33,7 +33,22 @@ __host__ __device__ __forceinline__ uint32_t m31_pow(uint32_t a, uint32_t e) {
   }
   return r;
 }
-__host__ __device__ __forceinline__ uint32_t m31_inv(uint32_t a) { return m31_pow(a, P - 2); }
+__host__ __device__ __forceinline__ uint32_t m31_sqn(uint32_t a, int n) {
+  for (int i = 0; i < n; i++) a = m31_sqr(a);
+  return a;
+}
+// a^(P - 2) (Fermat) by an addition chain on x^(2^k - 1): P - 2 = 4 (2^29 - 1) + 1, 30 squarings and
+// 8 multiplications.
+__host__ __device__ __forceinline__ uint32_t m31_inv(uint32_t a) {
+  const uint32_t t2 = m31_mul(m31_sqr(a), a);            // 2^2 - 1
+  const uint32_t t4 = m31_mul(m31_sqn(t2, 2), t2);       // 2^4 - 1
+  const uint32_t t8 = m31_mul(m31_sqn(t4, 4), t4);       // 2^8 - 1
+  const uint32_t t16 = m31_mul(m31_sqn(t8, 8), t8);      // 2^16 - 1
+  const uint32_t t24 = m31_mul(m31_sqn(t16, 8), t8);     // 2^24 - 1
+  const uint32_t t28 = m31_mul(m31_sqn(t24, 4), t4);     // 2^28 - 1
+  const uint32_t t29 = m31_mul(m31_sqr(t28), a);         // 2^29 - 1
+  return m31_mul(m31_sqn(t29, 2), a);                    // 4 (2^29 - 1) + 1
+}
 
 struct cm31 {
   uint32_t a, b;

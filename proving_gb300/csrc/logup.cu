@@ -368,20 +368,47 @@ struct LookupCompParams {
 
 // Quotients of single-column LogUp components of one size: per evaluation row, the sum over the
 // components of rc (cur - prev + shift) (v - z) + 1, over V_trace, added to the accumulator once.
+// Components go in pairs whose 18 loads are issued before either is evaluated.
+struct LookupRow {
+  uint32_t v, cur[4], prev[4];
+};
+
+__device__ __forceinline__ void load_lookup_row(const LookupCompParams& p, uint32_t k, uint32_t r, uint32_t pr,
+                                                LookupRow& o) {
+  const uint32_t* const* in = p.inter[k];
+  o.v = __ldg(p.values[k] + r);
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    o.cur[c] = __ldg(in[c] + r);
+    o.prev[c] = __ldg(in[c] + pr);
+  }
+}
+
+__device__ __forceinline__ qm31 lookup_term(const LookupCompParams& p, uint32_t k, const LookupRow& o) {
+  const qm31 cur = qm31_make(o.cur[0], o.cur[1], o.cur[2], o.cur[3]);
+  const qm31 prev = qm31_make(o.prev[0], o.prev[1], o.prev[2], o.prev[3]);
+  const qm31 shifted = qm31_add(qm31_sub(cur, prev), p.shift[k]);
+  const qm31 cons = qm31_add(qm31_mul(shifted, qm31_sub(qm31_make(o.v, 0, 0, 0), p.z)), qm31_make(1, 0, 0, 0));
+  return qm31_mul(p.rc[k], cons);
+}
+
 __global__ void lookup_composition_kernel(const __grid_constant__ LookupCompParams p, uint32_t* a0, uint32_t* a1,
                                           uint32_t* a2, uint32_t* a3) {
   const uint32_t n = 1u << p.eval_log;
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
     const uint32_t pr = prev_row(r, p.trace_log, p.eval_log);
     qm31 acc = qm31_make(0, 0, 0, 0);
-    for (uint32_t k = 0; k < p.n_comp; k++) {
-      const uint32_t* const* in = p.inter[k];
-      const qm31 cur = qm31_make(__ldg(in[0] + r), __ldg(in[1] + r), __ldg(in[2] + r), __ldg(in[3] + r));
-      const qm31 prev = qm31_make(__ldg(in[0] + pr), __ldg(in[1] + pr), __ldg(in[2] + pr), __ldg(in[3] + pr));
-      const qm31 shifted = qm31_add(qm31_sub(cur, prev), p.shift[k]);
-      const qm31 cons = qm31_add(qm31_mul(shifted, qm31_sub(qm31_make(__ldg(p.values[k] + r), 0, 0, 0), p.z)),
-                                 qm31_make(1, 0, 0, 0));
-      acc = qm31_add(acc, qm31_mul(p.rc[k], cons));
+    uint32_t k = 0;
+    for (; k + 2 <= p.n_comp; k += 2) {
+      LookupRow x, y;
+      load_lookup_row(p, k, r, pr, x);
+      load_lookup_row(p, k + 1, r, pr, y);
+      acc = qm31_add(acc, qm31_add(lookup_term(p, k, x), lookup_term(p, k + 1, y)));
+    }
+    if (k < p.n_comp) {
+      LookupRow x;
+      load_lookup_row(p, k, r, pr, x);
+      acc = qm31_add(acc, lookup_term(p, k, x));
     }
     const qm31 v = qm31_mul_m31(acc, p.den[r >> p.trace_log]);
     a0[r] = m31_add(a0[r], v.a.a);

@@ -32,11 +32,6 @@ __host__ __device__ __forceinline__ uint32_t reduce64(uint64_t v) {
   return m31_reduce_once(u);
 }
 
-__device__ __forceinline__ uint32_t dbl_x(uint32_t x) {
-  const uint32_t s = m31_sqr(x);
-  return m31_sub(m31_add(s, s), 1);
-}
-
 struct SoA {
   uint32_t* c[4];
 };
@@ -80,47 +75,47 @@ __global__ void lift_add_kernel(SoA col, CSoA prev, bool has_prev, uint32_t log_
 
 // ---------------------------------------------------------------- barycentric
 
+// Copies a domain's point tables into shared memory (all threads of the block).
+__device__ __forceinline__ void stage_tables(const DomainTables& d, cpoint (*tab)[512]) {
+  for (uint32_t i = threadIdx.x; i < 3 * 512; i += blockDim.x) tab[i >> 9][i & 511] = d.t[i >> 9][i & 511];
+  __syncthreads();
+}
+
+// Point jj (< 2^27) of the first half of the tables' domain: two additions.
+__device__ __forceinline__ cpoint table_point(const cpoint (*tab)[512], uint32_t jj) {
+  return cpoint_add(cpoint_add(tab[0][jj & 511], tab[1][(jj >> 9) & 511]), tab[2][(jj >> 18) & 511]);
+}
+
+// Domain point j of the first half of CanonicCoset(log_n)'s circle domain is init + j step; with
+// j = j0 + 2^9 j1 + 2^18 j2, it is T0[j0] + T1[j1] + T2[j2] (T0 holding init + j0 step), two point
+// additions from tables staged in shared memory. The second half is the conjugate (x, -y) of the
+// first: index -(init + (j - n/2) step).
 struct BaryParams {
-  cpoint gen_pow[31];   // 2^b * G
-  uint32_t half_init;   // initial index of the canonic half coset
-  uint32_t half_step;   // its step index
+  DomainTables tables;
   uint32_t log_n;
-  uint32_t four_pow;    // 4^(log_n - 1)
-  qm31 px, py, vn_p;    // sample point and V_n(p) = pi^(log_n - 1)(p.x)
+  qm31 px, py, vn_p;  // sample point and V_n(p) = pi^(log_n - 1)(p.x)
+  uint32_t si_plus;   // 2^log_n, the denominator factor of the points whose 2^(n-1) multiple is (0, -1)
+  uint32_t half_init, half_step;  // index of the first point and index step of the first half
 };
 
-__device__ __forceinline__ cpoint point_at(const cpoint* g, uint32_t idx) {
-  cpoint r{1, 0};
-#pragma unroll 1
-  for (int b = 0; b < 31; b++)
-    if ((idx >> b) & 1) r = cpoint_add(r, g[b]);
-  return r;
-}
-
-// Point of natural index j of a circle domain with the given half coset.
-__device__ __forceinline__ cpoint domain_point(const cpoint* g, uint32_t half_init, uint32_t half_step,
-                                               uint32_t half_log, uint32_t j) {
-  const uint32_t hs = 1u << half_log;
-  uint32_t idx;
-  if (j < hs)
-    idx = (half_init + j * half_step) & 0x7fffffffu;
-  else
-    idx = (0u - (half_init + (j - hs) * half_step)) & 0x7fffffffu;
-  return point_at(g, idx);
-}
-
-__global__ void bary_weights_kernel(const BaryParams p, SoA out) {
-  const uint32_t n = 1u << p.log_n;
+__global__ void bary_weights_kernel(const __grid_constant__ BaryParams p, SoA out) {
+  __shared__ cpoint tab[3][512];
+  stage_tables(p.tables, tab);
+  const uint32_t n = 1u << p.log_n, hs = n >> 1;
+  const uint32_t quarter = 3u << 29;  // index of (0, 1)
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t j = __brev(i) >> (32 - p.log_n);
-    const cpoint xi = domain_point(p.gen_pow, p.half_init, p.half_step, p.log_n - 1, j);
-    // si = -2 y_i * 4^(l-1) * prod_{k=1}^{l-1} pi^(k-1)(x_i)
-    uint32_t prod = 1, x = xi.x;
-    for (uint32_t k = 1; k < p.log_n; k++) {
-      prod = m31_mul(prod, x);
-      x = dbl_x(x);
+    const bool second = j >= hs;
+    const uint32_t jj = second ? j - hs : j;
+    cpoint xi = table_point(tab, jj);
+    uint32_t idx = (p.half_init + jj * p.half_step) & 0x7fffffffu;
+    if (second) {
+      xi.y = m31_neg(xi.y);
+      idx = (0u - idx) & 0x7fffffffu;
     }
-    const uint32_t si = m31_mul(m31_mul(xi.y, m31_neg(2)), m31_mul(p.four_pow, prod));
+    // si = -2 y_i 4^(l-1) prod_{k=1}^{l-1} pi^(k-1)(x_i) = -2 y_i V'(x_i) = -2^l y(2^(l-1) x_i), and
+    // 2^(l-1) x_i is (0, 1) or (0, -1) (V(x_i) = 0)
+    const uint32_t si = ((idx << (p.log_n - 1)) & 0x7fffffffu) == quarter ? m31_neg(p.si_plus) : p.si_plus;
     // h = p - x_i = (px*x + py*y, py*x - px*y)
     const qm31 hx = qm31_add(qm31_mul_m31(p.px, xi.x), qm31_mul_m31(p.py, xi.y));
     const qm31 hy = qm31_sub(qm31_mul_m31(p.py, xi.x), qm31_mul_m31(p.px, xi.y));
@@ -152,8 +147,8 @@ __device__ __forceinline__ void block_reduce_u64x4(uint64_t acc[4], uint64_t* sh
 
 // Many columns at once: block (x, y) takes rows [2048 x, 2048 (x + 1)) of the 16 columns of group
 // y. Each thread keeps the weights of its 8 rows in registers, loads the rows of the next two columns
-// while it works on the current one, and adds the unreduced 64-bit products (folding below 2^34 every 3
-// terms). A warp reduces the four coordinates of a column at once (a butterfly that halves the
+// while it works on the current one, and adds the unreduced 64-bit products (folding below 2^34 after
+// the first 4 of its 8 rows: 4 products below P^2 < 2^62 on top of a folded value stay below 2^64). A warp reduces the four coordinates of a column at once (a butterfly that halves the
 // values per lane at each of the first two steps: 6 shuffles), writes them to shared memory, and the
 // block sums its warps for all its columns after one barrier. The per-column partial sums (below
 // 2^34) go to `partial`, one row of chunks per (column, coordinate), which bary_final_kernel sums
@@ -164,6 +159,13 @@ constexpr int kBaryChunk = kBaryThreads * kBaryRows;
 constexpr int kBaryGroup = 16;  // columns per block
 
 __device__ __forceinline__ uint64_t fold34(uint64_t v) { return (v & P) + (v >> 31); }
+
+// acc + a * b with the 64-bit addend in the multiply (mad.wide.u32).
+__device__ __forceinline__ uint64_t mad_wide(uint32_t a, uint32_t b, uint64_t acc) {
+  uint64_t d;
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(acc));
+  return d;
+}
 
 // The warp's sum of r[0..3] (each below P) for coordinate lane >> 3, in lanes 0, 8, 16, 24.
 __device__ __forceinline__ uint32_t warp_sum4(const uint32_t r[4], uint32_t lane) {
@@ -216,14 +218,14 @@ __global__ void __launch_bounds__(kBaryThreads) bary_partial_kernel(const BaryCo
     for (int j = 0; j < kBaryRows; j++) {
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        acc[k] += (uint64_t)wr[j][k] * x[j];
-        if (j % 3 == 2) acc[k] = fold34(acc[k]);
+        acc[k] = mad_wide(wr[j][k], x[j], acc[k]);
+        if (j == 3) acc[k] = fold34(acc[k]);
       }
     }
     uint32_t r[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const uint64_t f = fold34(acc[k]);  // below 2^33
+      const uint64_t f = fold34(acc[k]);  // below 2^34
       r[k] = m31_reduce_once((uint32_t)fold34(f));
     }
     const uint32_t v = warp_sum4(r, lane);
@@ -318,17 +320,37 @@ __global__ void eval_at_point_kernel(const BaryColumns cols, const FoldFactors f
 
 // ---------------------------------------------------------------- numerators
 
-// row r: sum_t c_t * col_t[r] - sum_t b_t (the batch's partial numerator).
+// row r: sum_t c_t * col_t[r] - sum_t b_t (the batch's partial numerator). Terms go in groups of 8:
+// the 8 column values are loaded first, then their unreduced 64-bit products are added, folded below
+// 2^34 after every 4 (4 products below P^2 < 2^62 on top of a folded value stay below 2^64).
 __global__ void numerators_kernel(const NumeratorTerms terms, uint32_t rows, SoA out, bool accumulate) {
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
     uint64_t a[4] = {0, 0, 0, 0};
-    for (uint32_t t = 0; t < terms.n; t++) {
+    uint32_t t = 0;
+    for (; t + 8 <= terms.n; t += 8) {
+      uint32_t v[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) v[u] = __ldg(terms.col[t + u] + r);
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const qm31 c = terms.c[t + u];
+        a[0] += (uint64_t)c.a.a * v[u];
+        a[1] += (uint64_t)c.a.b * v[u];
+        a[2] += (uint64_t)c.b.a * v[u];
+        a[3] += (uint64_t)c.b.b * v[u];
+        if (u == 3 || u == 7) {
+#pragma unroll
+          for (int k = 0; k < 4; k++) a[k] = fold34(a[k]);
+        }
+      }
+    }
+    for (; t < terms.n; t++) {
       const uint32_t v = __ldg(terms.col[t] + r);
       const qm31 c = terms.c[t];
-      a[0] += m31_mul(c.a.a, v);
-      a[1] += m31_mul(c.a.b, v);
-      a[2] += m31_mul(c.b.a, v);
-      a[3] += m31_mul(c.b.b, v);
+      a[0] = fold34(a[0] + (uint64_t)c.a.a * v);
+      a[1] = fold34(a[1] + (uint64_t)c.a.b * v);
+      a[2] = fold34(a[2] + (uint64_t)c.b.a * v);
+      a[3] = fold34(a[3] + (uint64_t)c.b.b * v);
     }
     qm31 s = qm31_make(reduce64(a[0] % P), reduce64(a[1] % P), reduce64(a[2] % P), reduce64(a[3] % P));
     s = qm31_sub(s, terms.b_sum);
@@ -339,11 +361,14 @@ __global__ void numerators_kernel(const NumeratorTerms terms, uint32_t rows, SoA
 
 // ---------------------------------------------------------------- quotients
 
-__global__ void quotients_kernel(const QuotientParams q, SoA out) {
-  const uint32_t rows = 1u << q.sub_log;
+__global__ void quotients_kernel(const __grid_constant__ QuotientParams q, SoA out) {
+  __shared__ cpoint tab[3][512];
+  stage_tables(q.tables, tab);
+  const uint32_t rows = 1u << q.sub_log, hs = rows >> 1;
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
     const uint32_t j = __brev(r) >> (32 - q.sub_log);
-    const cpoint dp = domain_point(q.gen_pow, q.half_init, q.half_step, q.sub_log - 1, j);
+    cpoint dp = table_point(tab, j < hs ? j : j - hs);
+    if (j >= hs) dp.y = m31_neg(dp.y);
     qm31 acc = qm31_make(0, 0, 0, 0);
     for (uint32_t k = 0; k < q.n_points; k++) {
       const qm31 px = q.px[k], py = q.py[k];
@@ -394,6 +419,22 @@ GenPowersTable gen_powers() {
     cur = cpoint_add(cur, cur);
   }
   return t;
+}
+
+void fill_domain_tables(DomainTables& d, uint32_t half_init, uint32_t half_step) {
+  static const GenPowersTable g = gen_powers();
+  const auto point_at_host = [&](uint32_t idx) {
+    cpoint r{1, 0};
+    for (int b = 0; b < 31; b++)
+      if ((idx >> b) & 1) r = cpoint_add(r, g.p[b]);
+    return r;
+  };
+  for (uint32_t t = 0; t < 3; t++) {
+    // T0[a] = init + a step, T1[a] = 2^9 a step, T2[a] = 2^18 a step, one addition per entry
+    const cpoint step = point_at_host(((1u << (9 * t)) * half_step) & 0x7fffffffu);
+    d.t[t][0] = t == 0 ? point_at_host(half_init) : cpoint{1, 0};
+    for (uint32_t a = 1; a < 512; a++) d.t[t][a] = cpoint_add(d.t[t][a - 1], step);
+  }
 }
 
 cs_status quotients_on_subdomain(const QuotientParams& q, uint32_t* const out[4], cudaStream_t st) {
@@ -485,14 +526,12 @@ extern "C" cs_status cs_barycentric_weights(uint32_t log_size, const uint32_t px
   cs_status s = check4(h_out, "barycentric_weights");
   if (s != CS_OK) return s;
   CS_CHECK_ARG(log_size >= 1 && log_size <= 28, "barycentric_weights: log size %u out of range", log_size);
-  static const GenPowersTable g = gen_powers();
-  BaryParams p;
-  for (int b = 0; b < 31; b++) p.gen_pow[b] = g.p[b];
+  static thread_local BaryParams p;
   p.half_init = subgroup_gen(log_size + 1);
-  p.half_step = subgroup_gen(log_size - 1);
+  p.half_step = log_size >= 2 ? subgroup_gen(log_size - 1) : 0;
   p.log_n = log_size;
-  p.four_pow = 1;
-  for (uint32_t i = 1; i < log_size; i++) p.four_pow = m31_mul(p.four_pow, 4);
+  fill_domain_tables(p.tables, p.half_init, p.half_step);
+  p.si_plus = 1u << log_size;
   p.px = qm31_make(px[0], px[1], px[2], px[3]);
   p.py = qm31_make(py[0], py[1], py[2], py[3]);
   qm31 x = p.px;
@@ -619,14 +658,13 @@ extern "C" cs_status cs_quotients_on_subdomain(const uint32_t* const* h_accs, co
                kMaxPoints);
   CS_CHECK_ARG(h_accs && h_acc_log_sizes && h_points && h_first_linear, "quotients: null pointer");
   CS_CHECK_ARG(log_blowup < lifting_log_size && lifting_log_size <= 30, "quotients: bad sizes");
-  static const GenPowersTable g = gen_powers();
-  QuotientParams q;
-  for (int b = 0; b < 31; b++) q.gen_pow[b] = g.p[b];
+  static thread_local QuotientParams q;
   q.sub_log = lifting_log_size - log_blowup;
-  CS_CHECK_ARG(q.sub_log >= 1, "quotients: empty subdomain");
+  CS_CHECK_ARG(q.sub_log >= 1 && q.sub_log <= 28, "quotients: subdomain log size %u outside [1, 28]", q.sub_log);
   // eval_domain.split(log_blowup).0: half coset (eval half initial, log L - 1 - b)
   q.half_init = subgroup_gen(lifting_log_size + 1);
-  q.half_step = subgroup_gen(q.sub_log - 1);
+  q.half_step = q.sub_log >= 2 ? subgroup_gen(q.sub_log - 1) : 0;
+  fill_domain_tables(q.tables, q.half_init, q.half_step);
   q.n_points = n_points;
   for (uint32_t k = 0; k < n_points; k++) {
     const uint32_t* pt = h_points + 8 * k;

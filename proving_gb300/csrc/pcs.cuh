@@ -30,8 +30,15 @@ struct QuotientAcc {
   const uint32_t* c[4];
 };
 
+// The first half of a circle domain: point j = init + j step = T[0][j0] + T[1][j1] + T[2][j2] with
+// j = j0 + 2^9 j1 + 2^18 j2 (T[0] holding init + j0 step); the second half is its conjugate.
+struct DomainTables {
+  cpoint t[3][512];
+};
+void fill_domain_tables(DomainTables& d, uint32_t half_init, uint32_t half_step);
+
 struct QuotientParams {
-  cpoint gen_pow[31];
+  DomainTables tables;
   uint32_t half_init, half_step, sub_log, n_points;
   qm31 px[kMaxPoints], py[kMaxPoints], first_linear[kMaxPoints];
   uint32_t acc_log[kMaxPoints];

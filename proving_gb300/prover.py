@@ -343,18 +343,33 @@ class Reads:
 def merkle_witness_nodes(height: int, query_positions):
     """The witness of MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:119-150)
     per layer, walking down from the leaves: [(layer log size, sibling nodes)], the sibling of
-    every queried node whose sibling is not queried, in node order."""
+    every queried node whose sibling is not queried, in node order. All layers at once: row k holds
+    the sorted queries shifted down k layers; a node's sibling is present iff it sits next to the
+    node's run of equal values."""
+    q = np.unique(np.asarray(query_positions, dtype=np.int64))
+    if height == 0 or q.size == 0:
+        return []
+    r = q[None, :] >> np.arange(height, dtype=np.int64)[:, None]
+    n = r.shape[1]
+    first = np.ones(r.shape, bool)
+    first[:, 1:] = r[:, 1:] != r[:, :-1]
+    last = np.ones(r.shape, bool)
+    last[:, :-1] = r[:, :-1] != r[:, 1:]
+    next_is_sib = np.zeros(r.shape, bool)
+    next_is_sib[:, :-1] = r[:, 1:] == r[:, :-1] + 1
+    prev_is_sib = np.zeros(r.shape, bool)
+    prev_is_sib[:, 1:] = r[:, :-1] == r[:, 1:] - 1
+    even = (r & 1) == 0
+    need = (last & even & ~next_is_sib) | (first & ~even & ~prev_is_sib)
     out = []
-    prev = np.unique(np.asarray(query_positions, dtype=np.int64))
-    for layer_log in range(height - 1, -1, -1):
-        # prev is sorted and distinct: a sibling is present iff it sits next to its node
-        sib = prev ^ 1
-        at = np.minimum(np.searchsorted(prev, sib), prev.size - 1)
-        need = sib[prev[at] != sib]
-        if need.size:
-            out.append((layer_log + 1, need))
-        up = prev >> 1
-        prev = up[np.r_[True, up[1:] != up[:-1]]]
+    rows, cols = np.nonzero(need)
+    if rows.size == 0:
+        return out
+    sib = r[rows, cols] ^ 1
+    bounds = np.searchsorted(rows, np.arange(height + 1))
+    for k in range(height):
+        if bounds[k + 1] > bounds[k]:
+            out.append((height - k, sib[bounds[k]:bounds[k + 1]]))
     return out
 
 
@@ -528,7 +543,7 @@ def prove_wide_fib_components(ops, traces, log_sizes, config: PcsConfig, channel
         raise NotImplementedError("the Wide-Fibonacci prover supports log_blowup_factor = 1")
     n_cons = [len(t) - 2 for t in traces]
     total = sum(n_cons)
-    powers = secure_powers(random_coeff, total)
+    powers = ops.secure_powers(random_coeff, total)
     # DomainEvaluationAccumulator::columns (air/accumulation.rs:102-122): each component in turn takes
     # the last n of the remaining powers, reversed (component_prover.rs:194), so constraint k of the
     # component whose constraints start at global index g gets alpha^(total - 1 - g - k)
@@ -696,7 +711,7 @@ def prove_fib_and_lookups(ops, fib_traces, fib_logs, lookup_values, lookup_logs,
     random_coeff = channel.draw_secure_felt()
     n_cons = [len(t) - 2 for t in fib_traces] + [1] * len(lookup_values)
     total = sum(n_cons)
-    powers = secure_powers(random_coeff, total)
+    powers = ops.secure_powers(random_coeff, total)
     sub_acc, start = {}, 0
 
     def acc_for(eval_log):
@@ -779,14 +794,14 @@ def prove_fib_and_lookups(ops, fib_traces, fib_logs, lookup_values, lookup_logs,
         x = q_double_x(x)
     composition_oods = qm_add(left_v, qm_mul(x, right_v))
     expected = fib_and_lookups_at_point(oods, sampled, [len(t) for t in fib_traces], lookup_logs, z, claimed,
-                                        random_coeff, mldb)
+                                        random_coeff, mldb, powers)
     if composition_oods != expected:
         raise RuntimeError("constraints not satisfied (ProvingError::ConstraintsNotSatisfied)")
     return proof
 
 
 def fib_and_lookups_at_point(point, sampled, n_cols_per_fib, lookup_logs, z, claimed, random_coeff,
-                             max_log_degree_bound: int):
+                             max_log_degree_bound: int, powers=None):
     """The composition polynomial at the point from the sampled values (Components::
     eval_composition_polynomial_at_point): the Wide-Fibonacci constraints, then each LogUp
     component's (cur - prev + claimed / 2^n) (v - z) + 1, Horner-combined, over V(mldb) at the point."""
@@ -809,8 +824,9 @@ def fib_and_lookups_at_point(point, sampled, n_cols_per_fib, lookup_logs, z, cla
         shifted = qm_add(qm_sub(cur, prev), shift)
         cons.append(np.asarray([qm_add(qm_mul(shifted, qm_sub(v, z)), qm(1))], np.int64))
     cons = np.concatenate(cons, axis=0)
-    powers = np.asarray(list(reversed(secure_powers(random_coeff, len(cons)))), np.int64)
-    total = qv_sum(qv_mul(cons, powers))
+    if powers is None:
+        powers = secure_powers(random_coeff, len(cons))
+    total = qv_sum(qv_mul(cons, np.asarray(list(reversed(powers[:len(cons)])), np.int64)))
     return qm_mul(tuple(int(t) for t in total), den_inv)
 
 
@@ -884,7 +900,7 @@ def compute_fri_quotients(ops, columns, sample_points, sampled, random_coeff, li
     column with its random power, grouped by column size and sample point, accumulated, lifted and
     combined into the FRI quotient column."""
     n_samples = sum(len(c) + (1 if len(c) == 2 else 0) for tree in sampled for c in tree)
-    pows = secure_powers(random_coeff, n_samples)
+    pows = ops.secure_powers(random_coeff, n_samples)
     entries = []  # (log size, column, point, value) in tree/column order; entry k has power k
     shifted = {}  # (point, log period) -> the point shifted by the period
     for tree_cols, pts, vals in zip(columns, sample_points, sampled):
@@ -1043,6 +1059,10 @@ class GpuOps:
         from . import backend as be
         self.be = be
         self.B = be.CudaBackend
+
+    def secure_powers(self, felt, n):
+        """felt^0 .. felt^(n-1) on the host (cs_generate_secure_powers)."""
+        return [tuple(r) for r in self.B.generate_secure_powers(np.asarray(felt, np.uint32), n).tolist()]
 
     def twiddles(self, root_log_domain: int):
         return self.B.precompute_twiddles(self.be.canonic_half_coset(root_log_domain))

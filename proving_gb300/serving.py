@@ -22,6 +22,8 @@ stages (prover.PlainGpuOps).
 """
 from __future__ import annotations
 
+import contextlib
+import gc
 import queue
 import threading
 import time
@@ -101,6 +103,21 @@ def prove_request(ops, twiddles, req: ProofRequest):
     trace = CudaBackend.wide_fib_trace(a, b, N_COLS)
     return pr.prove_wide_fib(ops, trace, req.log_n_rows, default_config(req.log_n_rows), pr.Blake2sChannel(),
                              twiddles)
+
+
+@contextlib.contextmanager
+def collector_paused():
+    """Automatic garbage collection off while proofs run: a proof's objects are freed by reference
+    counting, and a full collection in the middle of a proof (tens of ms with the prover's working
+    set) would land in that proof's latency. A collection also leaves the next proof a few ms slower
+    (its allocations start cold), so workers collect only when idle."""
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if was:
+            gc.enable()
 
 
 def _ops(plain: bool):
@@ -200,8 +217,14 @@ def _process_worker(worker_id: int, plain: bool, max_log: int, warm_logs, tasks,
             prove_request(ops, twiddles, ProofRequest(-1, log_n, 1, kind))
         stream.synchronize()
     results.put(("ready", worker_id))
+    gc.collect()
+    gc.disable()  # collections run between requests (collector_paused)
     while True:
-        msg = tasks.get()
+        try:
+            msg = tasks.get(timeout=0.05)
+        except queue.Empty:
+            gc.collect()  # idle: collect off the latency path
+            msg = tasks.get()
         if msg is None:
             break
         rid, kind, log_n, seed = msg
