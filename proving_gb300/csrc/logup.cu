@@ -141,7 +141,7 @@ __device__ __forceinline__ void warp_scan4(uint32_t x[4]) {
   }
 }
 
-// A column of at most 2^9 rows, all in one block.
+// A column of at most 2^9 rows, all in one block (at least 2^9 threads).
 __device__ void small_column(const SumBatch& b, uint32_t col, uint32_t* flat, uint32_t (*sh)[32]) {
   const uint32_t log_n = b.log_size[col], n = 1u << log_n, t = threadIdx.x;
   qm31 g = qm31_make(0, 0, 0, 0);
@@ -174,9 +174,37 @@ __device__ void small_column(const SumBatch& b, uint32_t col, uint32_t* flat, ui
   if (t < 4) b.claimed[4 * col + t] = t == 0 ? total.a.a : t == 1 ? total.a.b : t == 2 ? total.b.a : total.b.b;
 }
 
-// Launch 1: per tile m of a column of 2^10 or more rows, thread (w, t) takes storage position
-// (rev5(w) << (l - 5)) | (rev(m) << 5) | t, i.e. natural (h = rev5(t), m, lo = w).
-__global__ void __launch_bounds__(kThreads) runs_kernel(const SumBatch b) {
+// 1 / (z - v0) and 1 / (z - v1) with one M31 inversion (Montgomery's trick on the norms): for
+// x = a + b u, 1 / x = (a - b u) / (a^2 - (2 + i) b^2), and 1 / d = conj(d) / |d|^2 for d in CM31.
+__device__ __forceinline__ void fraction_pair(const qm31& z, uint32_t v0, uint32_t v1, qm31& f0, qm31& f1) {
+  const qm31 x0 = qm31_sub(z, qm31_make(v0, 0, 0, 0)), x1 = qm31_sub(z, qm31_make(v1, 0, 0, 0));
+  const auto denom = [](const qm31& x) {
+    const cm31 b2 = cm31_mul(x.b, x.b);
+    const cm31 ib2 = {m31_neg(b2.b), b2.a};
+    return cm31_sub(cm31_mul(x.a, x.a), cm31_add(cm31_add(b2, b2), ib2));
+  };
+  const cm31 d0 = denom(x0), d1 = denom(x1);
+  const uint32_t n0 = m31_add(m31_sqr(d0.a), m31_sqr(d0.b)), n1 = m31_add(m31_sqr(d1.a), m31_sqr(d1.b));
+  const uint32_t prod = m31_mul(n0, n1);
+  uint32_t i0, i1;
+  if (prod != 0) {
+    const uint32_t inv = m31_inv(prod);
+    i0 = m31_mul(inv, n1);
+    i1 = m31_mul(inv, n0);
+  } else {  // z = v for one of them: each inverted alone (the inverse of 0 taken as 0, as in qm31_inv)
+    i0 = m31_inv(n0);
+    i1 = m31_inv(n1);
+  }
+  const cm31 di0 = {m31_mul(d0.a, i0), m31_mul(m31_neg(d0.b), i0)};
+  const cm31 di1 = {m31_mul(d1.a, i1), m31_mul(m31_neg(d1.b), i1)};
+  f0 = {cm31_mul(x0.a, di0), cm31_mul(cm31_neg(x0.b), di0)};
+  f1 = {cm31_mul(x1.a, di1), cm31_mul(cm31_neg(x1.b), di1)};
+}
+
+// Launch 1 (512 threads): per tile m of a column of 2^10 or more rows, thread (w, t) (w < 16) takes
+// the storage positions (rev5(lo) << (l - 5)) | (rev(m) << 5) | t for lo = w and w + 16, i.e.
+// natural (h = rev5(t), m, lo); their two fractions share one M31 inversion.
+__global__ void __launch_bounds__(kThreads / 2) runs_kernel(const SumBatch b) {
   __shared__ uint32_t tile[4][32][33];
   __shared__ uint32_t sh[4][32];
   const uint32_t col = block_column(b.tile0, b.n_cols, blockIdx.x);
@@ -186,26 +214,41 @@ __global__ void __launch_bounds__(kThreads) runs_kernel(const SumBatch b) {
     return;
   }
   const uint32_t mb = log_n - 10, m = blockIdx.x - b.tile0[col];
-  const uint32_t w = threadIdx.x >> 5, t = threadIdx.x & 31;
-  const uint32_t p = (rev5(w) << (log_n - 5)) | (rev_bits(m, mb) << 5) | t;
-  const qm31 g = load_fraction(b, col, p);
-  if (b.values[col] != nullptr) store4(b, col, p, g);
-  const uint32_t h = rev5(t);
-  tile[0][w][h] = g.a.a;
-  tile[1][w][h] = g.a.b;
-  tile[2][w][h] = g.b.a;
-  tile[3][w][h] = g.b.b;
-  __syncthreads();
-  // warp w sums natural run (h = w, m): lanes are lo
-  uint32_t x[4];
-#pragma unroll
-  for (int k = 0; k < 4; k++) x[k] = tile[k][t][w];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-    for (int k = 0; k < 4; k++) x[k] = m31_add(x[k], __shfl_xor_sync(0xffffffffu, x[k], o));
+  const uint32_t w = threadIdx.x >> 5, t = threadIdx.x & 31, h = rev5(t);
+  const uint32_t mid = (rev_bits(m, mb) << 5) | t;
+  const uint32_t p0 = (rev5(w) << (log_n - 5)) | mid, p1 = (rev5(w + 16) << (log_n - 5)) | mid;
+  qm31 g[2];
+  if (b.values[col] != nullptr) {
+    fraction_pair(b.z, b.values[col][p0], b.values[col][p1], g[0], g[1]);
+    store4(b, col, p0, g[0]);
+    store4(b, col, p1, g[1]);
+  } else {
+    g[0] = load_fraction(b, col, p0);
+    g[1] = load_fraction(b, col, p1);
   }
-  if (t < 4) b.runs[4 * (b.run0[col] + ((w << mb) | m)) + t] = x[t];
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const uint32_t lo = w + 16 * q;
+    tile[0][lo][h] = g[q].a.a;
+    tile[1][lo][h] = g[q].a.b;
+    tile[2][lo][h] = g[q].b.a;
+    tile[3][lo][h] = g[q].b.b;
+  }
+  __syncthreads();
+  // warp w sums natural runs (h' = w and w + 16, m): lanes are lo
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const uint32_t hh = w + 16 * q;
+    uint32_t x[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) x[k] = tile[k][t][hh];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) x[k] = m31_add(x[k], __shfl_xor_sync(0xffffffffu, x[k], o));
+    }
+    if (t < 4) b.runs[4 * (b.run0[col] + ((hh << mb) | m)) + t] = x[t];
+  }
 }
 
 // Launch 2: one block per column of 2^10 or more rows. The natural runs (h, m) are ordered h-major,
@@ -339,7 +382,7 @@ cs_status scan_columns(const uint32_t* const* values, const Q4* outs, const uint
     }
     b.tile0[b.n_cols] = tiles;
     b.pair0[b.n_cols] = pairs;
-    runs_kernel<<<tiles, kThreads, 0, st>>>(b);
+    runs_kernel<<<tiles, kThreads / 2, 0, st>>>(b);
     note_launch();
     if (pairs > 0) {
       run_offsets_kernel<<<b.n_cols, kThreads, 0, st>>>(b);
@@ -357,11 +400,13 @@ cs_status scan_columns(const uint32_t* const* values, const Q4* outs, const uint
 
 constexpr uint32_t kCompBatch = 24;  // LogUp components per launch
 
+// rc ((cur - prev + shift)(v - z) + 1) = (v rc - rc z)(cur - prev + shift) + rc: per component the
+// weight rc and rc z, per launch the sum of the weights.
 struct LookupCompParams {
   const uint32_t* values[kCompBatch];  // each component's trace column on the evaluation domain
   const uint32_t* inter[kCompBatch][4];
-  qm31 shift[kCompBatch], rc[kCompBatch];
-  qm31 z;
+  qm31 shift[kCompBatch], rc[kCompBatch], rcz[kCompBatch];
+  qm31 rc_sum;
   uint32_t den[32];
   uint32_t n_comp, eval_log, trace_log;
 };
@@ -384,12 +429,12 @@ __device__ __forceinline__ void load_lookup_row(const LookupCompParams& p, uint3
   }
 }
 
+// (v rc - rc z)(cur - prev + shift); the rc term is added once per launch (rc_sum).
 __device__ __forceinline__ qm31 lookup_term(const LookupCompParams& p, uint32_t k, const LookupRow& o) {
   const qm31 cur = qm31_make(o.cur[0], o.cur[1], o.cur[2], o.cur[3]);
   const qm31 prev = qm31_make(o.prev[0], o.prev[1], o.prev[2], o.prev[3]);
   const qm31 shifted = qm31_add(qm31_sub(cur, prev), p.shift[k]);
-  const qm31 cons = qm31_add(qm31_mul(shifted, qm31_sub(qm31_make(o.v, 0, 0, 0), p.z)), qm31_make(1, 0, 0, 0));
-  return qm31_mul(p.rc[k], cons);
+  return qm31_mul(qm31_sub(qm31_mul_m31(p.rc[k], o.v), p.rcz[k]), shifted);
 }
 
 __global__ void lookup_composition_kernel(const __grid_constant__ LookupCompParams p, uint32_t* a0, uint32_t* a1,
@@ -397,7 +442,7 @@ __global__ void lookup_composition_kernel(const __grid_constant__ LookupCompPara
   const uint32_t n = 1u << p.eval_log;
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
     const uint32_t pr = prev_row(r, p.trace_log, p.eval_log);
-    qm31 acc = qm31_make(0, 0, 0, 0);
+    qm31 acc = p.rc_sum;
     uint32_t k = 0;
     for (; k + 2 <= p.n_comp; k += 2) {
       LookupRow x, y;
@@ -509,7 +554,7 @@ extern "C" cs_status cs_logup_compositions(uint32_t n_comp, const uint32_t* cons
       CS_CHECK_ARG(h_inter[4 * k + c] != nullptr, "logup_compositions: component %u coordinate %d is null", k, c);
   }
   static thread_local LookupCompParams p;
-  p.z = qm31_make(z[0], z[1], z[2], z[3]);
+  const qm31 zz = qm31_make(z[0], z[1], z[2], z[3]);
   p.eval_log = eval_log;
   p.trace_log = trace_log;
   const uint32_t log_expand = eval_log - trace_log, n_den = 1u << log_expand;
@@ -530,11 +575,14 @@ extern "C" cs_status cs_logup_compositions(uint32_t n_comp, const uint32_t* cons
   const uint32_t blocks = std::max(1u, std::min((n + 255) / 256, 152u * 8));
   for (uint32_t k0 = 0; k0 < n_comp; k0 += kCompBatch) {
     p.n_comp = std::min(kCompBatch, n_comp - k0);
+    p.rc_sum = qm31_make(0, 0, 0, 0);
     for (uint32_t i = 0; i < p.n_comp; i++) {
       const uint32_t k = k0 + i;
       p.values[i] = h_values[k];
       for (int c = 0; c < 4; c++) p.inter[i][c] = h_inter[4 * k + c];
-      p.rc[i] = qm31_make(rcs[4 * k], rcs[4 * k + 1], rcs[4 * k + 2], rcs[4 * k + 3]);
+      p.rc[i] = qm31_make(rcs[4 * k] % P, rcs[4 * k + 1] % P, rcs[4 * k + 2] % P, rcs[4 * k + 3] % P);
+      p.rcz[i] = qm31_mul(p.rc[i], zz);
+      p.rc_sum = qm31_add(p.rc_sum, p.rc[i]);
       // cumsum_shift = claimed_sum / 2^trace_log (LogupAtRow::new, crates/constraint-framework/src/logup.rs:32-40)
       p.shift[i] = qm31_mul_m31(qm31_make(claimed_sums[4 * k], claimed_sums[4 * k + 1], claimed_sums[4 * k + 2],
                                           claimed_sums[4 * k + 3]),
