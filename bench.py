@@ -359,7 +359,7 @@ def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: in
     return lat
 
 
-def mixed_prove_leg(torch, n_proofs: int = 2):
+def mixed_prove_leg(torch, n_proofs: int = 2, arms=("batched", "plain")):
     """Config 3 as a full proof: the batched mixed-size trace (mixed_trace_shape: Wide-Fibonacci
     components holding 480 M31 columns and 120 single-column LogUp components, each with one M31
     value column and one QM31 running-sum column, log sizes 10..22 geometric, mean ~16) proved by
@@ -383,6 +383,8 @@ def mixed_prove_leg(torch, n_proofs: int = 2):
            "base_columns": sum(n for n, _ in comps) + len(lookup_logs), "interaction_columns": len(lookup_logs)}
     digests = {}
     for name, ops in (("batched", pr.GpuOps()), ("plain", pr.PlainGpuOps())):
+        if name not in arms:
+            continue
         tw = ops.twiddles(max_log + 2)
         lat = []
         for k in range(n_proofs + 1):
@@ -401,9 +403,10 @@ def mixed_prove_leg(torch, n_proofs: int = 2):
                      "max_ms": round(max(lat), 3)}
         del proof, tw
         torch.cuda.empty_cache()
-    out["same_proof_bytes"] = digests["batched"] == digests["plain"]
     out["proof_sha256"] = digests["batched"]
-    out["batched_speedup"] = round(out["plain"]["p50_ms"] / out["batched"]["p50_ms"], 3)
+    if "plain" in arms:
+        out["same_proof_bytes"] = digests["batched"] == digests["plain"]
+        out["batched_speedup"] = round(out["plain"]["p50_ms"] / out["batched"]["p50_ms"], 3)
     return out
 
 
@@ -792,6 +795,58 @@ def run_reference(args):
     print(json.dumps(res))
 
 
+def case_mixed_kernels(torch):
+    """Small cases of the mixed-size proof's kernels, for ncu (about 3 GB on the device): barycentric
+    weights and partial sums (64 columns x 2^22), quotient numerators (64 x 2^22, one point), LogUp
+    quotients (16 components x 2^22), LogUp running sums (8 x 2^22 and 8 x 2^16) and a lifted Merkle
+    commit of 64 x 2^22, 64 x 2^18 and 64 x 2^14 columns (leaf launches at three sizes). Every kernel
+    runs twice, the first run warming up."""
+    from proving_gb300.backend import BaseColumn, CudaBackend as B, SecureColumnByCoords
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1)
+    P = (1 << 31) - 1
+
+    def col(l):
+        return BaseColumn(torch.randint(0, P, (1 << l,), generator=g, device="cuda", dtype=torch.int64)
+                          .to(torch.int32))
+    L = 22
+    cols = [col(L) for _ in range(64)]
+    pt = ((1, 2, 3, 4), (5, 6, 7, 8))
+    for _ in range(2):
+        B.barycentric_eval_at_point(cols, B.barycentric_weights(L, pt))
+    coeffs = np.random.default_rng(0).integers(0, P, (64, 3, 4)).astype(np.uint32)
+    for _ in range(2):
+        B.accumulate_numerators(cols, coeffs, 1)
+    vals = [col(L) for _ in range(16)]
+    inters = [SecureColumnByCoords([col(L) for _ in range(4)]) for _ in range(16)]
+    acc = SecureColumnByCoords.zeros(1 << L)
+    rcs = [(k + 1, 2, 3, 4) for k in range(16)]
+    claimed = [(5, k + 6, 7, 8) for k in range(16)]
+    for _ in range(2):
+        B.logup_compositions(vals, inters, L - 1, (9, 10, 11, 12), claimed, rcs, acc)
+    del inters, acc
+    values = vals[:8] + [col(16) for _ in range(8)]
+    for _ in range(2):
+        B.logup_running_sums(values, (9, 10, 11, 12))
+    del values, vals
+    mixed = cols + [col(18) for _ in range(64)] + [col(14) for _ in range(64)]
+    for _ in range(2):
+        B.merkle_commit(mixed, L)
+    torch.cuda.synchronize()
+    return {"case": "mixed-kernels", "ok": True}
+
+
+def run_case(args):
+    import torch
+    from proving_gb300 import build as cuda_build
+    cuda_build.build()
+    if args.case == "mixed-kernels":
+        res = case_mixed_kernels(torch)
+    else:  # one mixed-size proof after one warm-up proof, batched arm only
+        res = mixed_prove_leg(torch, n_proofs=1, arms=("batched",))
+    print(json.dumps(res))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -808,9 +863,13 @@ def main():
     ap.add_argument("--skip-poseidon", action="store_true", help="skip the Poseidon2 prove leg")
     ap.add_argument("--poseidon-log-rows", type=int, default=18, help="log2 rows of the Poseidon2 prove leg")
     ap.add_argument("--skip-mixed-prove", action="store_true", help="skip the mixed-size full-proof leg")
+    ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove"],
+                    help="run one small profiling case instead of the benchmark (for ncu)")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
