@@ -133,6 +133,11 @@ class CpuOps:
                 out.append(np.stack([c.v[ix] for c in it[1]]) if it[1] else np.zeros((0, ix.size), np.uint32))
             elif it[0] == "col":
                 out.append(it[1].v[np.asarray(it[2], dtype=np.int64)])
+            elif it[0] == "digs":
+                tree = it[1]
+                parts = [np.ascontiguousarray(tree.layers[tree.height - k][np.asarray(n, dtype=np.int64)])
+                         .view("<u4").reshape(-1, 8) for k, n in it[2]]
+                out.append(np.concatenate(parts) if parts else np.zeros((0, 8), np.uint32))
             else:
                 tree, k, nodes = it[1], it[2], it[3]
                 lay = tree.layers[tree.height - k]

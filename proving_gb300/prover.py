@@ -103,6 +103,25 @@ def from_partial_evals(ev):
     return r
 
 
+def qv_times_i(x):
+    """x i for QM31 arrays: (c0 + c1 i) + (c2 + c3 i) u -> (-c1 + c0 i) + (-c3 + c2 i) u."""
+    return np.stack([(-x[..., 1]) % P, x[..., 0], (-x[..., 3]) % P, x[..., 2]], axis=-1)
+
+
+def qv_times_u(x):
+    """x u for QM31 arrays: (A + B u) u = (2 + i) B + A u."""
+    b0, b1 = x[..., 2], x[..., 3]
+    return np.stack([(2 * b0 - b1) % P, (b0 + 2 * b1) % P, x[..., 0], x[..., 1]], axis=-1)
+
+
+def qv_partial_evals(e):
+    """from_partial_evals over arrays: e[..., j, :] are the 4 coordinate values; returns
+    e0 + e1 i + e2 u + e3 i u."""
+    e = np.asarray(e, np.int64)
+    return (e[..., 0, :] + qv_times_i(e[..., 1, :]) + qv_times_u(e[..., 2, :])
+            + qv_times_u(qv_times_i(e[..., 3, :]))) % P
+
+
 def secure_powers(felt, n: int):
     """felt^0 .. felt^(n-1) (generate_secure_powers, crates/stwo/src/prover/air/accumulation.rs:183-200),
     built by doubling: the powers below 2^k times felt^(2^k) give the next 2^k."""
@@ -333,6 +352,12 @@ class Reads:
         self.items.append(("dig", tree, layer_log, np.asarray(nodes, dtype=np.int64)))
         return len(self.items) - 1
 
+    def tree_digests(self, tree, layers) -> int:
+        """Digests of several layers of one tree, [(layer_log, nodes)], as one (n, 8) result in
+        that order."""
+        self.items.append(("digs", tree, [(k, np.asarray(nodes, dtype=np.int64)) for k, nodes in layers]))
+        return len(self.items) - 1
+
     def run(self, ops):
         self.out = ops.gather_many(self.items)
 
@@ -393,16 +418,13 @@ class MerkleDecommit:
             shift = L - ls
             self.value_handles.append(reads.block(columns[i:j], ((q >> (shift + 1)) << 1) + (q & 1)))
             i = j
-        self.witness_handles = [reads.digests(tree, k, nodes) for k, nodes in merkle_witness_nodes(L, q)]
+        self.witness_handle = reads.tree_digests(tree, merkle_witness_nodes(L, q))
         self.reads = reads
 
     def result(self):
         queried = [row for h in self.value_handles for row in self.reads[h].tolist()]
-        witness = []
-        for h in self.witness_handles:
-            b = np.ascontiguousarray(self.reads[h], dtype="<u4").tobytes()
-            witness.extend(b[i:i + 32] for i in range(0, len(b), 32))
-        return queried, witness
+        b = np.ascontiguousarray(self.reads[self.witness_handle], dtype="<u4").tobytes()
+        return queried, [b[i:i + 32] for i in range(0, len(b), 32)]
 
 
 # ------------------------------------------------------------ FRI
@@ -810,19 +832,23 @@ def fib_and_lookups_at_point(point, sampled, n_cols_per_fib, lookup_logs, z, cla
         x = q_double_x(x)
     den_inv = qm_inv(x)
     m = np.asarray([c[0] for c in sampled[1]], np.int64)
-    cons, start = [], 0
-    for n in n_cols_per_fib:
-        a, b, c = m[start:start + n - 2], m[start + 1:start + n - 1], m[start + 2:start + n]
-        cons.append(qv_sub(c, qv_add(qv_mul(a, a), qv_mul(b, b))))
-        start += n
-    for k, log_n in enumerate(lookup_logs):
-        v = tuple(int(t) for t in m[start + k])
-        samples = sampled[2][4 * k:4 * k + 4]
-        prev = from_partial_evals([col[0] for col in samples])
-        cur = from_partial_evals([col[1] for col in samples])
-        shift = qm_mul(claimed[k], qm(m_inv(1 << log_n)))
-        shifted = qm_add(qm_sub(cur, prev), shift)
-        cons.append(np.asarray([qm_add(qm_mul(shifted, qm_sub(v, z)), qm(1))], np.int64))
+    # every Wide-Fibonacci constraint c - (a^2 + b^2) at once, component after component
+    starts = np.cumsum([0] + list(n_cols_per_fib))[:-1]
+    i0 = np.concatenate([st + np.arange(n - 2) for st, n in zip(starts, n_cols_per_fib)]).astype(np.int64)
+    sq = qv_mul(m, m)
+    cons = [qv_sub(m[i0 + 2], qv_add(sq[i0], sq[i0 + 1]))]
+    start = int(sum(n_cols_per_fib))
+    n_look = len(lookup_logs)
+    if n_look:
+        # every LogUp component at once: samples (component, coordinate, prev / cur, QM31)
+        smp = np.asarray(sampled[2], np.int64).reshape(n_look, 4, 2, 4)
+        prev, cur = qv_partial_evals(smp[:, :, 0]), qv_partial_evals(smp[:, :, 1])
+        inv_n = np.asarray([m_inv(1 << log_n) for log_n in lookup_logs], np.int64)
+        shift = np.asarray(claimed, np.int64) * inv_n[:, None] % P
+        shifted = qv_add(qv_sub(cur, prev), shift)
+        v = m[start:start + n_look]
+        one = np.asarray([1, 0, 0, 0], np.int64)
+        cons.append(qv_add(qv_mul(shifted, qv_sub(v, np.asarray(z, np.int64))), one))
     cons = np.concatenate(cons, axis=0)
     if powers is None:
         powers = secure_powers(random_coeff, len(cons))
@@ -964,13 +990,10 @@ class HostFriChannel:
         pass
 
 
-def fri_commit(ops, channel, fp: FriParams, column, log_size: int, twiddles):
-    """FriProver::commit (crates/stwo/src/prover/fri.rs:113-226), fold_step 1 (no leaf packing). The
-    ops may keep the channel on the device for the layer loop (ops.fri_channel): mixing each
-    layer's root and drawing its challenge then need no host round trip."""
-    if fp.fold_step != 1:
-        raise NotImplementedError("fold_step > 1")
-    ch = ops.fri_channel(channel) if hasattr(ops, "fri_channel") else HostFriChannel(channel)
+def fri_layers(ops, ch, fp: FriParams, column, log_size: int, twiddles):
+    """The layer loop of FriProver::commit (crates/stwo/src/prover/fri.rs:113-206), fold_step 1:
+    commit a layer, mix its root, draw the challenge, fold. Returns (first tree, inner layers,
+    the last evaluation); the channel `ch` is finished by the caller."""
     first_tree = ops.merkle_commit(ops.secure_columns(column), log_size)
     ch.mix_root(first_tree)
     alpha = ch.draw()
@@ -994,7 +1017,22 @@ def fri_commit(ops, channel, fp: FriParams, column, log_size: int, twiddles):
     alpha = ch.draw()
     inner.append({"tree": tree, "eval": layer, "fold_step": last_step})
     layer = ops.fold_line(layer, alpha, twiddles)
-    ch.finish()
+    return first_tree, inner, layer
+
+
+def fri_commit(ops, channel, fp: FriParams, column, log_size: int, twiddles):
+    """FriProver::commit (crates/stwo/src/prover/fri.rs:113-226), fold_step 1 (no leaf packing). The
+    ops may run the layer loop themselves (ops.fri_layers: the channel kept on the device, so that
+    mixing each root and drawing each challenge needs no host round trip)."""
+    if fp.fold_step != 1:
+        raise NotImplementedError("fold_step > 1")
+    if hasattr(ops, "fri_layers"):
+        first_tree, inner, layer = ops.fri_layers(channel, fp, column, log_size, twiddles)
+    else:
+        ch = HostFriChannel(channel)
+        first_tree, inner, layer = fri_layers(ops, ch, fp, column, log_size, twiddles)
+        ch.finish()
+    last_log = (fp.last_layer_domain_size()).bit_length() - 1
     # commit_last_layer (fri.rs:208-226): interpolate the last evaluation on its line domain
     values = ops.gather_secure(layer, list(range(fp.last_layer_domain_size())))
     coeffs = line_interpolate(values, last_log)
@@ -1059,6 +1097,7 @@ class GpuOps:
         from . import backend as be
         self.be = be
         self.B = be.CudaBackend
+        self._fri_graphs = {}
 
     def secure_powers(self, felt, n):
         """felt^0 .. felt^(n-1) on the host (cs_generate_secure_powers)."""
@@ -1157,6 +1196,13 @@ class GpuOps:
             if it[0] == "col":
                 t = it[1].data
                 ix = np.asarray(it[2], dtype=np.int64)
+            elif it[0] == "digs":
+                # every layer of the tree in its one buffer: layer k starts at node 2^(L+1) - 2^(k+1)
+                t = it[1].t.all
+                top = 1 << (it[1].height + 1)
+                nodes = (np.concatenate([top - (2 << k) + n for k, n in it[2]]) if it[2]
+                         else np.zeros(0, np.int64))
+                ix = (nodes[:, None] * 8 + np.arange(8)).reshape(-1)
             else:
                 t = it[1].t.layer(it[2])
                 nodes = np.asarray(it[3], dtype=np.int64)
@@ -1172,7 +1218,7 @@ class GpuOps:
             w = words[off:off + n]
             if it[0] == "cols":
                 w = w.reshape(len(it[1]), -1)
-            elif it[0] == "dig":
+            elif it[0] in ("dig", "digs"):
                 w = w.reshape(-1, 8)
             out.append(w)
             off += n
@@ -1242,8 +1288,46 @@ class GpuOps:
             return self.B.fold_line_device_alpha(col, alpha.data, tw)
         return self.B.fold_line(col, [np.asarray(alpha, np.uint32)], tw)
 
-    def fri_channel(self, channel):
-        return DeviceFriChannel(self, channel)
+    fri_graphs = True  # replay the FRI layer loop as a CUDA graph per (stream, size, parameters)
+
+    def fri_layers(self, channel, fp, column, log_size, tw):
+        """The FRI layer loop with the channel on the device. The loop has no host synchronisation,
+        so after its first run for a (stream, log size, FRI parameters, twiddles) it is captured
+        once as a CUDA graph over static buffers; later proofs copy their column and channel state
+        in, replay it, and read the state and the roots back in one call."""
+        if not self.fri_graphs:
+            ch = DeviceFriChannel(self, channel)
+            out = fri_layers(self, ch, fp, column, log_size, tw)
+            ch.finish()
+            return out
+        import torch
+        # the entry keeps `tw` alive, so its id cannot be reused while the graph refers to it
+        key = (torch.cuda.current_stream().cuda_stream, log_size, fp, id(tw))
+        g = self._fri_graphs.get(key)
+        if g is None:
+            ch = DeviceFriChannel(self, channel)
+            out = fri_layers(self, ch, fp, column, log_size, tw)
+            ch.finish()
+            if len(self._fri_graphs) >= 8:  # oldest first out
+                self._fri_graphs.pop(next(iter(self._fri_graphs)))
+            self._fri_graphs[key] = self._capture_fri(channel, fp, column, log_size, tw) + (tw,)
+            return out
+        graph, static_in, ch, out, _ = g
+        for dst, src in zip(static_in.columns, column.columns):
+            dst.data.copy_(src.data)
+        ch.reset(channel)
+        graph.replay()
+        ch.finish()
+        return out
+
+    def _capture_fri(self, channel, fp, column, log_size, tw):
+        import torch
+        static_in = self.be.SecureColumnByCoords.uninitialized(len(column))
+        ch = DeviceFriChannel(self, channel)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            out = fri_layers(self, ch, fp, static_in, log_size, tw)
+        return graph, static_in, ch, out
 
 
 class DeviceFelt:
@@ -1267,6 +1351,13 @@ class DeviceFriChannel:
         self.felts = torch.empty((64, 4), dtype=torch.int32, device="cuda")
         self.n_felts = 0
         self.trees = []
+
+    def reset(self, channel):
+        """Starts from the host channel's state again (for a replayed layer loop)."""
+        import torch
+        self.channel = channel
+        words = list(struct.unpack("<8I", channel.digest)) + [channel.n_draws]
+        self.state.copy_(torch.from_numpy(np.array(words, np.uint32).view(np.int32)))
 
     def mix_root(self, tree):
         from .backend import _stream
@@ -1300,7 +1391,10 @@ class PlainGpuOps(GpuOps):
     """The plain CUDA form: the same kernels, one launch per column for every
     per-column stage (interpolate, evaluate), as a backend without batched
     overrides calls them (the default PolyOps::interpolate_columns /
-    evaluate_polynomials loop, crates/stwo/src/prover/poly/circle/ops.rs:25-40,102-140)."""
+    evaluate_polynomials loop, crates/stwo/src/prover/poly/circle/ops.rs:25-40,102-140), and
+    the FRI layer loop launched eagerly every time (no graph)."""
+
+    fri_graphs = False
 
     def interpolate(self, cols, tw):
         for c in cols:

@@ -132,6 +132,9 @@ class ProverService:
         import torch
         self.torch = torch
         self.ops = _ops(plain)
+        # the worker threads share one CUDA context: a graph capture in one of them would stop the
+        # others' work, so the FRI layer loop runs eagerly here (worker processes replay graphs)
+        self.ops.fri_graphs = False
         self.twiddles = self.ops.twiddles(twiddle_domain(max_log_n_rows))
         torch.cuda.synchronize()
         self.n_workers = n_workers

@@ -96,3 +96,23 @@ def test_mixed_shape_proof_matches_oracle(gpu):
     assert g.to_bytes() == c.to_bytes()
     assert g.claimed_sums == c.claimed_sums
     verify_fib_and_lookups(g, [n for n, _ in comps], [l for _, l in comps], lookup_logs, g.claimed_sums)
+
+
+def test_fri_graph_replay_matches_oracle():
+    # the second and third proofs of one size replay the captured FRI layer loop: each equals the
+    # oracle's proof of its own trace
+    from proving_gb300 import build
+    build.build()
+    ops = pr.GpuOps()
+    log_n = 8
+    tw = ops.twiddles(log_n + 2)
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=log_n + 1)
+    seen = set()
+    for seed in (31, 33, 35):
+        trace = O.wide_fib_trace(m31_column(seed, log_n), m31_column(seed + 1, log_n), N_COLS)
+        g = pr.prove_wide_fib(ops, ops.columns_from_host(trace), log_n, cfg, pr.Blake2sChannel(), tw)
+        c, _ = _prove(CpuOps(), trace, log_n)
+        assert g.to_bytes() == c.to_bytes()
+        seen.add(g.to_bytes())
+    assert len(seen) == 3 and len(ops._fri_graphs) == 1
