@@ -332,6 +332,33 @@ cs_status cs_logup_compositions(uint32_t n_comp, const uint32_t *const *h_values
                                 const uint32_t *claimed_sums, const uint32_t *rcs, uint32_t *const h_accum[4],
                                 cs_stream stream);
 
+/* ------------------------------------------- run-time compiled constraints */
+
+/* The generic constraint path: the source of one kernel, made by
+   proving_gb300/framework.py from an AIR's constraints (the reference's
+   ExprEvaluator form, crates/constraint-framework/src/expr/evaluator.rs:58-123),
+   compiled with NVRTC for sm_103a (libnvrtc opened at run time) and loaded with
+   the runtime's library API. The kernel is
+     extern "C" __global__ void cs_air_composition(const uint32_t* const* cols,
+         const uint32_t* rc, const uint32_t* params, const uint32_t* den,
+         uint32_t eval_log, uint32_t trace_log,
+         uint32_t* a0, uint32_t* a1, uint32_t* a2, uint32_t* a3)
+   and adds, at every row of CanonicCoset(eval_log), the sum over the
+   constraints of rc[k] C_k(row) over V_trace(row) to the accumulator.
+   cs_rtc_available reports whether NVRTC can be opened. cs_rtc_compile_air
+   compiles `source` with the given in-memory headers and returns a handle (and
+   the compiler log, truncated to log_capacity). cs_rtc_air_composition runs it:
+   h_cols holds the n_cols mask columns (device, evaluation domain), h_rc 4
+   words per constraint and h_params 4 words per QM31 parameter (host). */
+cs_status cs_rtc_available(void);
+cs_status cs_rtc_compile_air(const char *source, uint32_t n_headers, const char *const *header_sources,
+                             const char *const *header_names, uint32_t n_cols, uint32_t n_constraints,
+                             uint32_t n_params, void **handle_out, char *log_out, size_t log_capacity);
+cs_status cs_rtc_air_composition(void *handle, const uint32_t *const *h_cols, const uint32_t *h_rc,
+                                 const uint32_t *h_params, uint32_t eval_log, uint32_t trace_log,
+                                 uint32_t *const h_accum[4], cs_stream stream);
+cs_status cs_rtc_release(void *handle);
+
 /* ------------------------------------------------------- AIR: Poseidon2 */
 
 /* The Poseidon2 AIR of crates/examples/src/poseidon/mod.rs (state width 16,

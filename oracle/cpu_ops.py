@@ -82,6 +82,11 @@ class CpuOps:
             claimed.append(tuple(int(x) for x in cs))
         return cols, claimed
 
+    def air_composition(self, air, columns_by_interaction, trace_log, params, rc, accum):
+        from .air_eval import air_composition
+        cols = {k: [c.v for c in v] for k, v in columns_by_interaction.items()}
+        accum.c = air_composition(air, cols, len(accum).bit_length() - 1, trace_log, params, rc, out=accum.c)
+
     def logup_compositions(self, values_evals, inter_evals, trace_log, z, claimed, rcs, accum):
         for v, it, c, r in zip(values_evals, inter_evals, claimed, rcs):
             self.logup_composition(v, it, trace_log, z, c, r, accum)

@@ -81,6 +81,7 @@ void orc_wide_fib_trace(const uint32_t *a0, const uint32_t *b0, uint32_t log_n, 
 void orc_logup_running_sum(const uint32_t *values, uint32_t log_n, const uint32_t z[4], uint32_t *const out[4],
                            uint32_t claimed_out[4]);
 uint64_t orc_prev_row(uint64_t r, uint32_t trace_log, uint32_t eval_log);
+void orc_prev_rows(uint32_t trace_log, uint32_t eval_log, uint64_t *out);
 void orc_logup_composition(const uint32_t *values, const uint32_t *const inter[4], uint32_t eval_log,
                            uint32_t trace_log, const uint32_t z[4], const uint32_t claimed[4], const uint32_t rc[4],
                            uint32_t *const out[4]);

@@ -453,6 +453,33 @@ def wide_fib_composition(cols, eval_log: int, trace_log: int, rc, out=None):
     return out
 
 
+def prev_rows(trace_log: int, eval_log: int) -> np.ndarray:
+    """The previous-row index of every row of a bit-reversed evaluation domain (orc_prev_row)."""
+    out = np.zeros(1 << eval_log, np.uint64)
+    lib().orc_prev_rows(ctypes.c_uint32(trace_log), ctypes.c_uint32(eval_log), _p(out))
+    return out.astype(np.int64)
+
+
+def vanishing_inverses(eval_log: int, trace_log: int) -> np.ndarray:
+    """1 / V_trace at every row of CanonicCoset(eval_log) in bit-reversed order, each row's point
+    computed from its index (the denominators of evaluate_constraint_quotients_on_domain,
+    crates/constraint-framework/src/prover/component_prover.rs:101-108)."""
+    n = 1 << eval_log
+    hs = n >> 1
+    half_init = 1 << (31 - (eval_log + 1))
+    half_step = (1 << (31 - (eval_log - 1))) if eval_log >= 1 else 0
+    mask = (1 << 31) - 1
+    nat = bit_reverse(np.arange(n, dtype=np.uint32)).astype(np.int64) if n > 1 else np.zeros(1, np.int64)
+    xs = np.zeros(n, np.int64)
+    for r in range(n):
+        j = int(nat[r])
+        t = (half_init + j * half_step) & mask if j < hs else (-(half_init + (j - hs) * half_step)) & mask
+        xs[r] = int(circle_index_to_point(t)[0])
+    for _ in range(trace_log - 1):
+        xs = (2 * xs * xs - 1) % P
+    return np.asarray([pow(int(x), P - 2, P) for x in xs], np.int64)
+
+
 def logup_running_sum(values, z):
     v, zz = _u32(values), _u32(z)
     n = v.size

@@ -181,6 +181,11 @@ uint64_t orc_prev_row(uint64_t r, uint32_t trace_log, uint32_t eval_log) {
     return bit_reverse_index((uint32_t)i, eval_log);
 }
 
+/* orc_prev_row for every row of the domain. */
+void orc_prev_rows(uint32_t trace_log, uint32_t eval_log, uint64_t *out) {
+    for (uint64_t r = 0; r < (1ull << eval_log); r++) out[r] = orc_prev_row(r, trace_log, eval_log);
+}
+
 /*
  * Constraint quotients of the Poseidon component on an evaluation domain
  * (FrameworkComponent::evaluate_constraint_quotients_on_domain,

@@ -70,6 +70,10 @@ SIGNATURES = {
     "cs_channel_mix_root": [vp, vp, vp],
     "cs_channel_draw_secure_felt": [vp, vp, vp],
     "cs_logup_running_sums": [u32, vp, vp, vp, vp, vp, vp],
+    "cs_rtc_available": [],
+    "cs_rtc_compile_air": [vp, u32, vp, vp, u32, u32, u32, vp, vp, ctypes.c_size_t],
+    "cs_rtc_air_composition": [vp, vp, vp, vp, u32, u32, vp, vp],
+    "cs_rtc_release": [vp],
     "cs_logup_compositions": [u32, vp, vp, u32, u32, vp, vp, vp, vp, vp],
     "cs_logup_composition": [vp, vp, u32, u32, vp, vp, vp, vp, vp],
 }

@@ -676,7 +676,7 @@ def _evaluate_grouped(ops, coeffs, logs, log_blowup: int, twiddles):
 
 
 def prove_fib_and_lookups(ops, fib_traces, fib_logs, lookup_values, lookup_logs, config: PcsConfig,
-                          channel: Blake2sChannel, twiddles):
+                          channel: Blake2sChannel, twiddles, generic: bool = False):
     """Wide-Fibonacci components and single-column LogUp components in one proof (the batched mixed-size
     trace: components of different sizes in one lifted tree, plus LogUp interaction columns). Follows
     the example provers' flow (crates/examples/src/poseidon/mod.rs:336-379): the empty preprocessed
@@ -686,7 +686,10 @@ def prove_fib_and_lookups(ops, fib_traces, fib_logs, lookup_values, lookup_logs,
     mixed into the channel; then prove_ex. A LogUp
     component's relation entry has multiplicity -1 and values [v], so its fractions are 1 / (z - v)
     and its one constraint is (cur - prev + claimed / 2^n) (v - z) + 1 (finalize_logup). Returns the
-    proof with `claimed_sums` (one per LogUp component, part of the statement, not serialized)."""
+    proof with `claimed_sums` (one per LogUp component, part of the statement, not serialized).
+    generic=True evaluates the constraints through the generic path (proving_gb300.framework: the
+    AIRs written against the constraint evaluator, compiled at run time) instead of the
+    hand-written kernels; the proof is the same."""
     fp = config.fri_params
     b = fp.log_blowup_factor
     L = config.trace_lifting_log_size
@@ -741,15 +744,28 @@ def prove_fib_and_lookups(ops, fib_traces, fib_logs, lookup_values, lookup_logs,
             sub_acc[eval_log] = ops.secure_zeros(1 << eval_log)
         return sub_acc[eval_log]
 
+    if generic:
+        from . import framework as fw
+        lookup_air = fw.compile_air("single_lookup", fw.single_lookup_air)
     for evals, log_n, n in zip(fib_evals, fib_logs, n_cons):
         rc = list(reversed(powers[total - start - n:total - start]))
-        ops.wide_fib_composition(evals, log_n, rc, acc_for(log_n + 1))
+        if generic:
+            air = fw.compile_air(f"wide_fib_{n + 2}", fw.wide_fib_air, n + 2)
+            ops.air_composition(air, {1: evals}, log_n, {}, rc, acc_for(log_n + 1))
+        else:
+            ops.wide_fib_composition(evals, log_n, rc, acc_for(log_n + 1))
         start += n
     lookup_rc = []
     for k in range(len(lookup_logs)):
         lookup_rc.append(powers[total - start - 1])
         start += 1
     for log_n, idx in _size_groups(lookup_logs).items():
+        if generic:
+            for k in idx:
+                shift = tuple(int(c) * m_inv(1 << log_n) % P for c in claimed[k])
+                ops.air_composition(lookup_air, {1: [lookup_ext[k]], 2: inter_ext[k]}, log_n,
+                                    {"z": z, "shift": shift}, [lookup_rc[k]], acc_for(log_n + 1))
+            continue
         # every LogUp component of one size in one pass over the evaluation domain
         ops.logup_compositions([lookup_ext[k] for k in idx], [inter_ext[k] for k in idx], log_n, z,
                                [claimed[k] for k in idx], [lookup_rc[k] for k in idx], acc_for(log_n + 1))
@@ -1138,6 +1154,11 @@ class GpuOps:
         """Every column's running sum in one batch of launches; the claimed sums read back once."""
         cols, claimed = self.B.logup_running_sums(values, np.asarray(z, np.uint32))
         return cols, [tuple(int(x) for x in row) for row in claimed.cpu().numpy().view(np.uint32)]
+
+    def air_composition(self, air, columns_by_interaction, trace_log, params, rc, accum):
+        """An AIR's constraint quotients through the generic path (run-time compiled kernel)."""
+        from .framework import CompiledAir
+        CompiledAir.get(air).composition(columns_by_interaction, trace_log, params, rc, accum)
 
     def logup_compositions(self, values_evals, inter_evals, trace_log, z, claimed, rcs, accum):
         self.B.logup_compositions(values_evals, [self.be.SecureColumnByCoords(it) for it in inter_evals], trace_log,
