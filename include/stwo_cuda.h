@@ -332,6 +332,34 @@ cs_status cs_logup_compositions(uint32_t n_comp, const uint32_t *const *h_values
                                 const uint32_t *claimed_sums, const uint32_t *rcs, uint32_t *const h_accum[4],
                                 cs_stream stream);
 
+/* ------------------------------------------------- native Wide-Fibonacci prover */
+
+/* The whole proof of Wide-Fibonacci components (the generic prover's loop,
+   prove_ex, crates/stwo/src/prover/mod.rs:39-138, over this library's
+   kernels, with the host work in native code): the empty preprocessed tree,
+   the components' traces in one lifted tree, the constraint quotients, the
+   OODS samples, FRI with fold_step 1 and the decommitments, returned as the
+   CairoSerialize felt stream of the StarkProof (one u64 per felt). The
+   channel starts from the zero digest. d_trace holds the components'
+   columns one after another (2^log_sizes[k] words each, bit-reversed
+   evaluations on CanonicCoset(log_sizes[k]); interpolated in place).
+   lifting_log_size must be the largest log size + 1 (log_blowup_factor 1).
+   The twiddle trees cover CanonicCoset(lifting_log_size). With h_words null
+   only *n_words is set. */
+typedef struct {
+  uint32_t n_components;
+  const uint32_t *n_cols;    /* per component, >= 3 */
+  const uint32_t *log_sizes; /* per component */
+  uint32_t lifting_log_size;
+  uint32_t pow_bits, log_blowup_factor, log_last_layer_degree_bound, n_queries;
+  const uint32_t *d_twiddles, *d_itwiddles;
+  uint32_t twiddle_log_size;
+} cs_wide_fib_proof_params;
+cs_status cs_prove_wide_fib(const cs_wide_fib_proof_params *params, uint32_t *const *d_trace, uint64_t *h_words,
+                            size_t capacity, size_t *n_words, cs_stream stream);
+/* Blake2s-256 of a message on the host (RFC 7693), the native prover's channel hash. */
+cs_status cs_host_blake2s(const uint8_t *msg, size_t n, uint8_t out[32]);
+
 /* ------------------------------------------- run-time compiled constraints */
 
 /* The generic constraint path: the source of one kernel, made by

@@ -98,6 +98,15 @@ class BaseColumn:
         return int(self.data[i].item()) & 0xFFFFFFFF
 
 
+class _WideFibProofParams(ctypes.Structure):
+    """cs_wide_fib_proof_params (include/stwo_cuda.h)."""
+    _fields_ = [("n_components", ctypes.c_uint32), ("n_cols", ctypes.c_void_p), ("log_sizes", ctypes.c_void_p),
+                ("lifting_log_size", ctypes.c_uint32), ("pow_bits", ctypes.c_uint32),
+                ("log_blowup_factor", ctypes.c_uint32), ("log_last_layer_degree_bound", ctypes.c_uint32),
+                ("n_queries", ctypes.c_uint32), ("d_twiddles", ctypes.c_void_p), ("d_itwiddles", ctypes.c_void_p),
+                ("twiddle_log_size", ctypes.c_uint32)]
+
+
 class SecureColumnByCoords:
     """SecureColumnByCoords (crates/stwo/src/prover/secure_column.rs:13-15): 4 coordinate columns."""
 
@@ -448,6 +457,31 @@ class CudaBackend:
                   _ptr_table([c.data for it in inters for c in it.columns]), values[0].log_size, trace_log,
                   _u32_table(z), _u32_table([w for c in claimed for w in c]), _u32_table([w for r in rcs for w in r]),
                   _ptr_table([c.data for c in accum.columns]), _stream())
+
+    @staticmethod
+    def prove_wide_fib_native(traces, log_sizes, fri_params, twiddles: TwiddleTree) -> bytes:
+        """cs_prove_wide_fib: the whole proof of Wide-Fibonacci components with the host work in
+        native code. traces[k]: component k's columns (BaseColumns of 2^log_sizes[k] evaluations,
+        interpolated in place). fri_params: (pow_bits, log_blowup_factor,
+        log_last_layer_degree_bound, n_queries). Returns the proof bytes (u64 LE felts)."""
+        cols = [c for t in traces for c in t]
+        params = _WideFibProofParams()
+        n_cols = (ctypes.c_uint32 * len(traces))(*[len(t) for t in traces])
+        logs = (ctypes.c_uint32 * len(traces))(*log_sizes)
+        params.n_components = len(traces)
+        params.n_cols = ctypes.cast(n_cols, ctypes.c_void_p)
+        params.log_sizes = ctypes.cast(logs, ctypes.c_void_p)
+        params.lifting_log_size = max(log_sizes) + fri_params[1]
+        params.pow_bits, params.log_blowup_factor, params.log_last_layer_degree_bound, params.n_queries = fri_params
+        params.d_twiddles = twiddles.twiddles.data_ptr()
+        params.d_itwiddles = twiddles.itwiddles.data_ptr()
+        params.twiddle_log_size = twiddles.log_size
+        n = ctypes.c_size_t(0)
+        cap = 1 << 22
+        words = np.empty(cap, np.uint64)
+        _lib.call("cs_prove_wide_fib", ctypes.byref(params), _ptr_table([c.data for c in cols]), words.ctypes.data,
+                  cap, ctypes.byref(n), _stream())
+        return words[:n.value].astype("<u8").tobytes()
 
     # Poseidon2 AIR ------------------------------------------------------------
     POSEIDON_COLS = 1264

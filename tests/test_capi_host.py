@@ -134,3 +134,27 @@ def test_fft_plans_are_validated_and_stored_on_host(lib):
     for n in range(1, 25):
         for plan in autotune.candidate_plans(n):
             assert sum(plan) == n and plan[0] <= 12 and all(t <= 11 for t in plan[1:])
+
+
+def test_host_blake2s_matches_hashlib(lib):
+    # the native prover's channel hash (RFC 7693), every block-boundary case
+    import hashlib
+    import os
+    for msg in [b"", b"a", b"x" * 63, b"y" * 64, b"z" * 65, b"w" * 128, os.urandom(200)]:
+        out = (ctypes.c_uint8 * 32)()
+        _lib.call("cs_host_blake2s", msg, len(msg), out)
+        assert bytes(out) == hashlib.blake2s(msg).digest()
+
+
+def test_native_prover_checks_arguments_on_host(lib):
+    from proving_gb300.backend import _WideFibProofParams
+    p = _WideFibProofParams()
+    n_cols = (ctypes.c_uint32 * 1)(2)   # fewer than 3 columns
+    logs = (ctypes.c_uint32 * 1)(5)
+    p.n_components, p.n_cols, p.log_sizes = 1, ctypes.cast(n_cols, ctypes.c_void_p), ctypes.cast(logs, ctypes.c_void_p)
+    p.lifting_log_size, p.pow_bits, p.log_blowup_factor, p.log_last_layer_degree_bound, p.n_queries = 6, 10, 1, 0, 3
+    p.d_twiddles, p.d_itwiddles, p.twiddle_log_size = 1 << 20, 1 << 21, 6
+    cols = (ctypes.c_void_p * 2)(1 << 22, 1 << 23)
+    n = ctypes.c_size_t(0)
+    assert _status(lib, "cs_prove_wide_fib", ctypes.byref(p), cols, None, 0, ctypes.byref(n), None) == 1
+    assert b"columns" in lib.cs_last_error()
