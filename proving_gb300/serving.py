@@ -18,7 +18,9 @@ Two forms:
   host cores instead of sharing one interpreter.
 
 `plain=True` gives the plain form: one launch per column for the per-column
-stages (prover.PlainGpuOps).
+stages (prover.PlainGpuOps), orchestrated by the restated prover. Otherwise the
+process workers prove Wide-Fibonacci requests with the native prover
+(cs_prove_wide_fib), whose bytes are the same.
 """
 from __future__ import annotations
 
@@ -89,9 +91,10 @@ def twiddle_domain(max_log_n_rows: int) -> int:
     return max_log_n_rows + 3
 
 
-def prove_request(ops, twiddles, req: ProofRequest):
+def prove_request(ops, twiddles, req: ProofRequest, native: bool = False):
     """One proof on the current CUDA stream: the trace generated on the device from the request's
-    seed, then the restated prover."""
+    seed, then the restated prover, or for a Wide-Fibonacci request with native=True the native
+    prover (cs_prove_wide_fib, the same bytes; returned as bytes)."""
     from .backend import BaseColumn, CudaBackend
     if req.kind == "poseidon":
         from . import poseidon as ps
@@ -101,6 +104,11 @@ def prove_request(ops, twiddles, req: ProofRequest):
     a = BaseColumn.from_cpu(m31_column(req.seed, req.log_n_rows))
     b = BaseColumn.from_cpu(m31_column(req.seed + 1, req.log_n_rows))
     trace = CudaBackend.wide_fib_trace(a, b, N_COLS)
+    if native:
+        fp = fri_params()
+        return CudaBackend.prove_wide_fib_native(
+            [trace], [req.log_n_rows], (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound,
+                                        fp.n_queries), twiddles)
     return pr.prove_wide_fib(ops, trace, req.log_n_rows, default_config(req.log_n_rows), pr.Blake2sChannel(),
                              twiddles)
 
@@ -217,7 +225,7 @@ def _process_worker(worker_id: int, plain: bool, max_log: int, warm_logs, tasks,
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
         for kind, log_n in warm_logs:
-            prove_request(ops, twiddles, ProofRequest(-1, log_n, 1, kind))
+            prove_request(ops, twiddles, ProofRequest(-1, log_n, 1, kind), native=not plain)
         stream.synchronize()
     results.put(("ready", worker_id))
     gc.collect()
@@ -235,7 +243,8 @@ def _process_worker(worker_id: int, plain: bool, max_log: int, warm_logs, tasks,
         out, err = None, None
         try:
             with torch.cuda.stream(stream):
-                out = prove_request(ops, twiddles, ProofRequest(rid, log_n, seed, kind)).to_bytes()
+                out = prove_request(ops, twiddles, ProofRequest(rid, log_n, seed, kind), native=not plain)
+                out = out if isinstance(out, bytes) else out.to_bytes()
                 stream.synchronize()
         except Exception as e:  # one failed request does not stop the worker
             err = repr(e)
