@@ -357,6 +357,29 @@ typedef struct {
 } cs_wide_fib_proof_params;
 cs_status cs_prove_wide_fib(const cs_wide_fib_proof_params *params, uint32_t *const *d_trace, uint64_t *h_words,
                             size_t capacity, size_t *n_words, cs_stream stream);
+/* cs_prove_wide_fib with n_lookups single-column LogUp components beside the
+   Wide-Fibonacci components (relation entry of multiplicity -1 and values [v]):
+   component k's looked-up values are d_values[k] (2^h_lookup_log_sizes[k] words,
+   trace domain, kept); their value columns follow the Wide-Fibonacci columns in
+   the trace tree, their QM31 running sums form the interaction tree (mixed into
+   the channel after the claimed sums, which go to h_claimed, 4 words each).
+   The lifting log size is the largest of all log sizes + 1. */
+cs_status cs_prove_fib_and_lookups(const cs_wide_fib_proof_params *params, uint32_t *const *d_trace,
+                                   uint32_t n_lookups, const uint32_t *const *d_values,
+                                   const uint32_t *h_lookup_log_sizes, uint32_t *h_claimed, uint64_t *h_words,
+                                   size_t capacity, size_t *n_words, cs_stream stream);
+
+/* The whole proof of the Poseidon2 AIR at 2^log_n_rows rows (8 instances per
+   row, prove_poseidon, crates/examples/src/poseidon/mod.rs:320-379), trace and
+   interaction generated on the device, constraint quotients on
+   CanonicCoset(log_n_rows + 2). params: the FRI parameters and twiddles
+   (n_components, n_cols and log_sizes unused); lifting_log_size =
+   log_n_rows + 2. Without the sanity check, which the reference's own prove of
+   this AIR fails (lifted protocol, constraint degree 5): the words are the
+   proof it computes before it. */
+cs_status cs_prove_poseidon(uint32_t log_n_rows, const cs_wide_fib_proof_params *params, uint64_t *h_words,
+                            size_t capacity, size_t *n_words, cs_stream stream);
+
 /* Blake2s-256 of a message on the host (RFC 7693), the native prover's channel hash. */
 cs_status cs_host_blake2s(const uint8_t *msg, size_t n, uint8_t out[32]);
 

@@ -75,6 +75,8 @@ SIGNATURES = {
     "cs_rtc_air_composition": [vp, vp, vp, vp, u32, u32, vp, vp],
     "cs_rtc_release": [vp],
     "cs_prove_wide_fib": [vp, vp, vp, ctypes.c_size_t, vp, vp],
+    "cs_prove_fib_and_lookups": [vp, vp, u32, vp, vp, vp, vp, ctypes.c_size_t, vp, vp],
+    "cs_prove_poseidon": [u32, vp, vp, ctypes.c_size_t, vp, vp],
     "cs_host_blake2s": [vp, ctypes.c_size_t, vp],
     "cs_logup_compositions": [u32, vp, vp, u32, u32, vp, vp, vp, vp, vp],
     "cs_logup_composition": [vp, vp, u32, u32, vp, vp, vp, vp, vp],

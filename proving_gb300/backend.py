@@ -459,28 +459,57 @@ class CudaBackend:
                   _ptr_table([c.data for c in accum.columns]), _stream())
 
     @staticmethod
+    def _proof_params(n_cols, log_sizes, lifting_log_size: int, fri_params, twiddles: TwiddleTree):
+        params = _WideFibProofParams()
+        keep = ((ctypes.c_uint32 * max(1, len(n_cols)))(*n_cols), (ctypes.c_uint32 * max(1, len(log_sizes)))(*log_sizes))
+        params.n_components = len(n_cols)
+        params.n_cols = ctypes.cast(keep[0], ctypes.c_void_p)
+        params.log_sizes = ctypes.cast(keep[1], ctypes.c_void_p)
+        params.lifting_log_size = lifting_log_size
+        params.pow_bits, params.log_blowup_factor, params.log_last_layer_degree_bound, params.n_queries = fri_params
+        params.d_twiddles = twiddles.twiddles.data_ptr()
+        params.d_itwiddles = twiddles.itwiddles.data_ptr()
+        params.twiddle_log_size = twiddles.log_size
+        return params, keep
+
+    @staticmethod
     def prove_wide_fib_native(traces, log_sizes, fri_params, twiddles: TwiddleTree) -> bytes:
         """cs_prove_wide_fib: the whole proof of Wide-Fibonacci components with the host work in
         native code. traces[k]: component k's columns (BaseColumns of 2^log_sizes[k] evaluations,
         interpolated in place). fri_params: (pow_bits, log_blowup_factor,
         log_last_layer_degree_bound, n_queries). Returns the proof bytes (u64 LE felts)."""
+        return CudaBackend.prove_fib_and_lookups_native(traces, log_sizes, [], [], fri_params, twiddles)[0]
+
+    @staticmethod
+    def prove_fib_and_lookups_native(traces, log_sizes, lookup_values, lookup_logs, fri_params,
+                                     twiddles: TwiddleTree):
+        """cs_prove_fib_and_lookups: Wide-Fibonacci components and single-column LogUp components
+        (lookup_values: BaseColumns on their trace domains, kept). Returns (proof bytes, claimed sums)."""
         cols = [c for t in traces for c in t]
-        params = _WideFibProofParams()
-        n_cols = (ctypes.c_uint32 * len(traces))(*[len(t) for t in traces])
-        logs = (ctypes.c_uint32 * len(traces))(*log_sizes)
-        params.n_components = len(traces)
-        params.n_cols = ctypes.cast(n_cols, ctypes.c_void_p)
-        params.log_sizes = ctypes.cast(logs, ctypes.c_void_p)
-        params.lifting_log_size = max(log_sizes) + fri_params[1]
-        params.pow_bits, params.log_blowup_factor, params.log_last_layer_degree_bound, params.n_queries = fri_params
-        params.d_twiddles = twiddles.twiddles.data_ptr()
-        params.d_itwiddles = twiddles.itwiddles.data_ptr()
-        params.twiddle_log_size = twiddles.log_size
+        lifting = max(list(log_sizes) + list(lookup_logs)) + fri_params[1]
+        params, keep = CudaBackend._proof_params([len(t) for t in traces], log_sizes, lifting, fri_params, twiddles)
         n = ctypes.c_size_t(0)
         cap = 1 << 22
         words = np.empty(cap, np.uint64)
-        _lib.call("cs_prove_wide_fib", ctypes.byref(params), _ptr_table([c.data for c in cols]), words.ctypes.data,
-                  cap, ctypes.byref(n), _stream())
+        claimed = np.zeros((max(1, len(lookup_values)), 4), np.uint32)
+        _lib.call("cs_prove_fib_and_lookups", ctypes.byref(params), _ptr_table([c.data for c in cols]),
+                  len(lookup_values), _ptr_table([v.data for v in lookup_values]), _u32_table(lookup_logs),
+                  claimed.ctypes.data, words.ctypes.data, cap, ctypes.byref(n), _stream())
+        del keep
+        return (words[:n.value].astype("<u8").tobytes(),
+                [tuple(int(x) for x in row) for row in claimed[:len(lookup_values)]])
+
+    @staticmethod
+    def prove_poseidon_native(log_n_rows: int, fri_params, twiddles: TwiddleTree) -> bytes:
+        """cs_prove_poseidon: the Poseidon2 AIR's proof (2^log_n_rows rows, 8 instances per row), trace
+        generated on the device, the words the reference computes before its sanity check."""
+        params, keep = CudaBackend._proof_params([], [], log_n_rows + 2, fri_params, twiddles)
+        n = ctypes.c_size_t(0)
+        cap = 1 << 22
+        words = np.empty(cap, np.uint64)
+        _lib.call("cs_prove_poseidon", log_n_rows, ctypes.byref(params), words.ctypes.data, cap, ctypes.byref(n),
+                  _stream())
+        del keep
         return words[:n.value].astype("<u8").tobytes()
 
     # Poseidon2 AIR ------------------------------------------------------------

@@ -210,6 +210,13 @@ struct Arena {
     ptrs.push_back(p);
     return static_cast<uint32_t*>(p);
   }
+  // frees one allocation early (stream-ordered)
+  void release(void* p) {
+    auto it = std::find(ptrs.begin(), ptrs.end(), p);
+    if (it == ptrs.end()) return;
+    cudaFreeAsync(p, st);
+    ptrs.erase(it);
+  }
   ~Arena() {
     for (void* p : ptrs) cudaFreeAsync(p, st);
   }
@@ -386,208 +393,368 @@ struct FriLayer {
   uint32_t log_size;
 };
 
+struct Col {
+  uint32_t* p;
+  uint32_t log;
+};
+
+bool same(const qpoint& a, const qpoint& b) { return std::memcmp(&a, &b, sizeof(qpoint)) == 0; }
+
+bool point_less(const qpoint& a, const qpoint& b) {
+  const uint32_t ka[8] = {a.x.a.a, a.x.a.b, a.x.b.a, a.x.b.b, a.y.a.a, a.y.a.b, a.y.b.a, a.y.b.b};
+  const uint32_t kb[8] = {b.x.a.a, b.x.a.b, b.x.b.a, b.x.b.b, b.y.a.a, b.y.a.b, b.y.b.a, b.y.b.b};
+  return std::lexicographical_compare(ka, ka + 8, kb, kb + 8);
+}
+
+qpoint add_m31_point(const qpoint& p, const cpoint& g) {
+  const qm31 gx = qm(g.x), gy = qm(g.y);
+  return {qm31_sub(qm31_mul(p.x, gx), qm31_mul(p.y, gy)), qm31_add(qm31_mul(p.x, gy), qm31_mul(p.y, gx))};
+}
+
+qm31 from_partial_evals(const qm31* e) {
+  qm31 r = e[0];
+  r = qm31_add(r, qm31_mul(e[1], qm31_make(0, 1, 0, 0)));
+  r = qm31_add(r, qm31_mul(e[2], qm31_make(0, 0, 1, 0)));
+  r = qm31_add(r, qm31_mul(e[3], qm31_make(0, 0, 0, 1)));
+  return r;
+}
+
+struct ProofConfig {
+  uint32_t L, b, pow_bits, log_last_layer_degree_bound, n_queries;
+  const uint32_t *tw, *itw;
+  uint32_t tw_log;
+};
+
 }  // namespace
 
 void blake2s_public(const uint8_t* msg, size_t n, uint8_t out[32]) { blake2s(msg, n, out); }
 
-cs_status prove_wide_fib(const cs_wide_fib_proof_params& pp, uint32_t* const* d_trace, std::vector<uint64_t>& words,
-                         cudaStream_t st) {
-  Arena A(st);
-  const uint32_t b = pp.log_blowup_factor, L = pp.lifting_log_size;
-  const uint32_t n_comp = pp.n_components;
+// The prover's device state and the helpers the AIRs use.
+struct Prover {
+  Arena A;
+  cudaStream_t st;
   Channel ch;
+  ProofConfig cfg;
+  Prover(cudaStream_t s, const ProofConfig& c) : A(s), st(s), cfg(c) {}
+
+  // Evaluations (in place: coefficients) of columns of one size.
+  cs_status interpolate(const std::vector<uint32_t*>& cols, uint32_t log) {
+    if (cols.empty()) return CS_OK;
+    std::vector<uint32_t*> c(cols);
+    return cs_interpolate_columns(c.data(), (uint32_t)c.size(), log, cfg.itw, cfg.tw_log, st);
+  }
+  // Coefficient columns of one size evaluated on CanonicCoset(to_log) into one new block.
+  cs_status evaluate(const std::vector<uint32_t*>& coeffs, uint32_t log, uint32_t to_log, std::vector<uint32_t*>& out) {
+    out.clear();
+    if (coeffs.empty()) return CS_OK;
+    uint32_t* blk = A.alloc(coeffs.size() << to_log);
+    if (!blk) return A.status;
+    for (size_t j = 0; j < coeffs.size(); j++) out.push_back(blk + (j << to_log));
+    std::vector<const uint32_t*> src(coeffs.begin(), coeffs.end());
+    return cs_evaluate_columns(src.data(), out.data(), (uint32_t)coeffs.size(), log, to_log, cfg.tw, cfg.tw_log, st);
+  }
+  std::vector<uint32_t*>& acc_for(std::map<uint32_t, std::vector<uint32_t*>>& acc, uint32_t el) {
+    if (!acc.count(el)) {
+      uint32_t* blk = A.alloc(4ull << el);
+      if (blk) cudaMemsetAsync(blk, 0, 16ull << el, st);
+      acc[el] = {blk, blk + (1ull << el), blk + (2ull << el), blk + (3ull << el)};
+    }
+    return acc[el];
+  }
+};
+
+// The AIR-specific parts of a proof, called by prove() between its generic phases.
+struct Air {
+  virtual ~Air() = default;
+  // the trace tree's columns (evaluations on their blown-up domains), in tree order
+  virtual cs_status trace(Prover& P, std::vector<Col>& cols) = 0;
+  virtual bool has_interaction() const { return false; }
+  virtual bool mix_claimed() const { return false; }
+  // the interaction tree's columns, whether each is also sampled at the previous row, and the
+  // claimed sums (z, alpha: the lookup elements)
+  virtual cs_status interaction(Prover&, const qm31&, const qm31&, std::vector<Col>&, std::vector<bool>&,
+                                std::vector<qm31>&) {
+    return CS_OK;
+  }
+  virtual uint32_t n_constraints() const = 0;
+  // the constraint quotients added to per-size accumulators, powers of the random coefficient given
+  virtual cs_status composition(Prover& P, const std::vector<qm31>& powers,
+                                std::map<uint32_t, std::vector<uint32_t*>>& acc) = 0;
+  // the composition polynomial at the point from the samples (sampled[tree][col][k]), or false for
+  // no check
+  virtual bool at_point(const qpoint&, uint32_t, const qm31&, const std::vector<std::vector<std::vector<qm31>>>&,
+                        qm31&) {
+    return false;
+  }
+};
+
+// prove_ex (crates/stwo/src/prover/mod.rs:39-138) over the trees [preprocessed (empty), trace,
+// interaction (if any), composition], FRI with fold_step 1, the felt stream of the StarkProof.
+cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, std::vector<qm31>& claimed,
+                cudaStream_t st) {
+  Prover P(st, cfg);
+  Arena& A = P.A;
+  Channel& ch = P.ch;
+  const uint32_t L = cfg.L, b = cfg.b, mldb = L - b;
   // --- preprocessed tree: empty (a single hash of no data at height 0, pcs/mod.rs:83-96)
   uint8_t pre_root[32];
   blake2s(nullptr, 0, pre_root);
   ch.mix_root(pre_root);
-  // --- trace tree: every component's columns (interpolated in place, evaluated on log + b)
-  std::vector<uint32_t*> trace_evals;
-  std::vector<uint32_t> trace_logs;
-  std::vector<std::vector<uint32_t*>> comp_evals(n_comp);
-  size_t c0 = 0;
-  for (uint32_t k = 0; k < n_comp; k++) {
-    const uint32_t n = pp.n_cols[k], lg = pp.log_sizes[k];
-    std::vector<uint32_t*> cols(d_trace + c0, d_trace + c0 + n);
-    HP_TRY(cs_interpolate_columns(cols.data(), n, lg, pp.d_itwiddles, pp.twiddle_log_size, st));
-    uint32_t* block = A.alloc((size_t)n << (lg + b));
-    if (!block) return A.status;
-    for (uint32_t j = 0; j < n; j++) comp_evals[k].push_back(block + ((size_t)j << (lg + b)));
-    std::vector<const uint32_t*> src(cols.begin(), cols.end());
-    HP_TRY(cs_evaluate_columns(src.data(), comp_evals[k].data(), n, lg, lg + b, pp.d_twiddles, pp.twiddle_log_size,
-                               st));
-    for (uint32_t* e : comp_evals[k]) {
-      trace_evals.push_back(e);
-      trace_logs.push_back(lg + b);
+  struct TreeCols {
+    std::vector<Col> cols;
+    std::vector<bool> two;  // also sampled at the previous row
+    Tree tree;
+  };
+  std::vector<TreeCols> trees;
+  // --- trace tree (TreeBuilder::extend_evals + commit)
+  trees.emplace_back();
+  HP_TRY(air.trace(P, trees.back().cols));
+  trees.back().two.assign(trees.back().cols.size(), false);
+  const auto commit_tree = [&](TreeCols& t) -> cs_status {
+    std::vector<uint32_t*> c;
+    std::vector<uint32_t> l;
+    for (const Col& x : t.cols) {
+      c.push_back(x.p);
+      l.push_back(x.log);
     }
-    c0 += n;
+    HP_TRY(commit(A, c, l, L, t.tree));
+    return read_root(A, t.tree);
+  };
+  HP_TRY(commit_tree(trees.back()));
+  ch.mix_root(trees.back().tree.root);
+  // --- lookup elements and the interaction tree
+  if (air.has_interaction()) {
+    const qm31 z = ch.draw_secure_felt();
+    const qm31 alpha = ch.draw_secure_felt();
+    trees.emplace_back();
+    HP_TRY(air.interaction(P, z, alpha, trees.back().cols, trees.back().two, claimed));
+    HP_TRY(commit_tree(trees.back()));
+    if (air.mix_claimed()) ch.mix_felts(claimed);
+    ch.mix_root(trees.back().tree.root);
   }
-  Tree trace_tree;
-  HP_TRY(commit(A, trace_evals, trace_logs, L, trace_tree));
-  HP_TRY(read_root(A, trace_tree));
-  ch.mix_root(trace_tree.root);
-
-  // --- composition (component_prover.rs:95-116): components take the last powers, reversed
+  // --- composition polynomial (component_prover.rs:95-116, accumulation.rs:142-180)
   const qm31 random_coeff = ch.draw_secure_felt();
-  uint32_t total = 0;
-  for (uint32_t k = 0; k < n_comp; k++) total += pp.n_cols[k] - 2;
-  const std::vector<qm31> pw = powers(random_coeff, total);
-  std::map<uint32_t, std::vector<uint32_t*>> sub_acc;  // eval log -> 4 coordinates
-  uint32_t start = 0;
-  for (uint32_t k = 0; k < n_comp; k++) {
-    const uint32_t n = pp.n_cols[k] - 2, lg = pp.log_sizes[k], el = lg + 1;
-    if (!sub_acc.count(el)) {
-      uint32_t* blk = A.alloc(4ull << el);
-      if (!blk) return A.status;
-      CS_CUDA(cudaMemsetAsync(blk, 0, 16ull << el, st));
-      sub_acc[el] = {blk, blk + (1ull << el), blk + (2ull << el), blk + (3ull << el)};
-    }
-    std::vector<uint32_t> rc(4 * n);
-    for (uint32_t j = 0; j < n; j++) {  // rc[j] = powers[total - start - 1 - j]
-      const qm31 x = pw[total - start - 1 - j];
-      rc[4 * j] = x.a.a;
-      rc[4 * j + 1] = x.a.b;
-      rc[4 * j + 2] = x.b.a;
-      rc[4 * j + 3] = x.b.b;
-    }
-    std::vector<const uint32_t*> ev(comp_evals[k].begin(), comp_evals[k].end());
-    HP_TRY(cs_wide_fib_composition(ev.data(), n + 2, el, lg, rc.data(), sub_acc[el].data(), st));
-    start += n;
-  }
+  const std::vector<qm31> pw = powers(random_coeff, air.n_constraints());
+  std::map<uint32_t, std::vector<uint32_t*>> sub_acc;
+  HP_TRY(air.composition(P, pw, sub_acc));
   std::vector<uint32_t*> acc_cols;
   std::vector<uint32_t> acc_logs;
   for (auto& [el, coords] : sub_acc) {
     acc_cols.insert(acc_cols.end(), coords.begin(), coords.end());
     acc_logs.push_back(el);
   }
-  if (sub_acc.size() > 1) HP_TRY(cs_lift_and_accumulate(acc_cols.data(), acc_logs.data(), (uint32_t)acc_logs.size(), st));
+  if (acc_logs.size() > 1)
+    HP_TRY(cs_lift_and_accumulate(acc_cols.data(), acc_logs.data(), (uint32_t)acc_logs.size(), st));
   const uint32_t comp_log = acc_logs.back();
   std::vector<uint32_t*> accum(acc_cols.end() - 4, acc_cols.end());
-  HP_TRY(cs_interpolate_columns(accum.data(), 4, comp_log, pp.d_itwiddles, pp.twiddle_log_size, st));
+  HP_TRY(P.interpolate(accum, comp_log));
   const size_t half = 1ull << (comp_log - 1);
-  std::vector<const uint32_t*> split;
-  for (int c = 0; c < 4; c++) split.push_back(accum[c]);
+  std::vector<uint32_t*> split(accum);
   for (int c = 0; c < 4; c++) split.push_back(accum[c] + half);
   const uint32_t comp_eval_log = (comp_log - 1) + b;
-  uint32_t* cblk = A.alloc(8ull << comp_eval_log);
-  if (!cblk) return A.status;
   std::vector<uint32_t*> comp_cols;
-  for (int c = 0; c < 8; c++) comp_cols.push_back(cblk + ((size_t)c << comp_eval_log));
-  HP_TRY(cs_evaluate_columns(split.data(), comp_cols.data(), 8, comp_log - 1, comp_eval_log, pp.d_twiddles,
-                             pp.twiddle_log_size, st));
-  Tree comp_tree;
-  HP_TRY(commit(A, comp_cols, std::vector<uint32_t>(8, comp_eval_log), L, comp_tree));
-  HP_TRY(read_root(A, comp_tree));
-  ch.mix_root(comp_tree.root);
+  HP_TRY(P.evaluate(split, comp_log - 1, comp_eval_log, comp_cols));
+  trees.emplace_back();
+  for (uint32_t* c : comp_cols) trees.back().cols.push_back({c, comp_eval_log});
+  trees.back().two.assign(8, false);
+  HP_TRY(commit_tree(trees.back()));
+  ch.mix_root(trees.back().tree.root);
 
-  // --- OODS proof of work and point (mod.rs:75-83)
+  // --- OODS proof of work and point (mod.rs:75-83); the previous row (component.rs:202-214)
   uint64_t oods_pow = 0;
   HP_TRY(cs_grind_blake2s(ch.digest, 16, 1ull << 48, &oods_pow, st));
   ch.mix_u64(oods_pow);
   const qpoint oods = random_point(ch.draw_secure_felt());
+  const cpoint g = index_to_point(1u << (31 - mldb));
+  const qpoint prev_pt = add_m31_point(oods, {g.x, m31_neg(g.y)});
 
-  // --- sampled values (pcs/mod.rs:175-214): every column at the point doubled L - size times; one
-  // weight column per size; every value read back once
-  std::vector<uint32_t*> all_cols(trace_evals);
-  std::vector<uint32_t> all_logs(trace_logs);
-  all_cols.insert(all_cols.end(), comp_cols.begin(), comp_cols.end());
-  all_logs.insert(all_logs.end(), 8, comp_eval_log);
-  const size_t n_all = all_cols.size();
-  uint32_t* d_samples = A.alloc(4 * n_all);
+  // --- sampled values (pcs/mod.rs:175-214): one weight column per (size, point); values read once
+  struct Sample {
+    size_t tree, col, slot;
+  };
+  std::vector<std::pair<std::pair<uint32_t, int>, std::vector<Sample>>> groups;  // (log, 0 oods / 1 prev)
+  for (size_t t = 0; t < trees.size(); t++)
+    for (size_t c = 0; c < trees[t].cols.size(); c++) {
+      std::vector<int> pts = trees[t].two[c] ? std::vector<int>{1, 0} : std::vector<int>{0};
+      for (size_t k = 0; k < pts.size(); k++) {
+        const std::pair<uint32_t, int> key{trees[t].cols[c].log, pts[k]};
+        auto it = std::find_if(groups.begin(), groups.end(), [&](auto& g) { return g.first == key; });
+        if (it == groups.end()) {
+          groups.push_back({key, {}});
+          it = groups.end() - 1;
+        }
+        it->second.push_back({t, c, k});
+      }
+    }
+  size_t n_samples = 0;
+  for (auto& gr : groups) n_samples += gr.second.size();
+  uint32_t* d_samples = A.alloc(4 * n_samples);
   if (!d_samples) return A.status;
-  std::map<uint32_t, std::vector<size_t>> by_log;
-  for (size_t i = 0; i < n_all; i++) by_log[all_logs[i]].push_back(i);
-  std::vector<size_t> order;  // column index of each row of d_samples
-  for (auto& [ls, idx] : by_log) {
-    qpoint pt = oods;
-    for (uint32_t d = ls; d < L; d++) pt = q_double(pt);
+  size_t row = 0;
+  for (auto& [key, members] : groups) {
+    qpoint pt = key.second ? prev_pt : oods;
+    for (uint32_t d = key.first; d < L; d++) pt = q_double(pt);
+    const uint32_t ls = key.first;
     uint32_t* w = A.alloc(4ull << ls);
     if (!w) return A.status;
     uint32_t* wc[4] = {w, w + (1ull << ls), w + (2ull << ls), w + (3ull << ls)};
     const uint32_t px[4] = {pt.x.a.a, pt.x.a.b, pt.x.b.a, pt.x.b.b}, py[4] = {pt.y.a.a, pt.y.a.b, pt.y.b.a, pt.y.b.b};
     HP_TRY(cs_barycentric_weights(ls, px, py, wc, st));
     std::vector<const uint32_t*> cols;
-    for (size_t i : idx) cols.push_back(all_cols[i]);
+    for (const Sample& m : members) cols.push_back(trees[m.tree].cols[m.col].p);
     const uint32_t* wcc[4] = {wc[0], wc[1], wc[2], wc[3]};
-    HP_TRY(cs_barycentric_eval(cols.data(), (uint32_t)cols.size(), ls, wcc, d_samples + 4 * order.size(), st));
-    order.insert(order.end(), idx.begin(), idx.end());
+    HP_TRY(cs_barycentric_eval(cols.data(), (uint32_t)cols.size(), ls, wcc, d_samples + 4 * row, st));
+    row += members.size();
+    A.release(w);
   }
-  std::vector<uint32_t> samples(4 * n_all);
-  CS_CUDA(cudaMemcpyAsync(samples.data(), d_samples, 16 * n_all, cudaMemcpyDeviceToHost, st));
+  std::vector<uint32_t> samples(4 * n_samples);
+  CS_CUDA(cudaMemcpyAsync(samples.data(), d_samples, 16 * n_samples, cudaMemcpyDeviceToHost, st));
   CS_CUDA(cudaStreamSynchronize(st));
-  std::vector<qm31> sampled(n_all);
-  for (size_t j = 0; j < n_all; j++)
-    sampled[order[j]] = qm31_make(samples[4 * j], samples[4 * j + 1], samples[4 * j + 2], samples[4 * j + 3]);
-  ch.mix_felts(sampled);
-
-  // --- FRI quotients (quotient_ops.rs:86-160): one sample point; batches by size, ascending
-  const qm31 quotient_coeff = ch.draw_secure_felt();
-  const std::vector<qm31> qp = powers(quotient_coeff, (uint32_t)n_all);
-  std::vector<uint32_t*> parts;
-  std::vector<uint32_t> part_logs;
-  qm31 first_linear = qm31_make(0, 0, 0, 0);
-  for (auto& [ls, idx] : by_log) {
-    std::vector<uint32_t> coeffs(12 * idx.size());
-    std::vector<const uint32_t*> cols;
-    for (size_t j = 0; j < idx.size(); j++) {
-      line_coeffs(oods.y, sampled[idx[j]], qp[idx[j]], &coeffs[12 * j]);
-      cols.push_back(all_cols[idx[j]]);
-    }
-    const uint32_t pl = ls - b;
-    uint32_t* blk = A.alloc(4ull << pl);
-    if (!blk) return A.status;
-    uint32_t* out[4] = {blk, blk + (1ull << pl), blk + (2ull << pl), blk + (3ull << pl)};
-    uint32_t fl[4];
-    HP_TRY(cs_accumulate_numerators(cols.data(), (uint32_t)cols.size(), ls, b, coeffs.data(), out, fl, st));
-    first_linear = qm31_add(first_linear, qm31_make(fl[0], fl[1], fl[2], fl[3]));
-    parts.insert(parts.end(), out, out + 4);
-    part_logs.push_back(pl);
+  std::vector<std::vector<std::vector<qm31>>> sampled(trees.size() + 1);  // [0]: the preprocessed tree
+  for (size_t t = 0; t < trees.size(); t++) {
+    sampled[t + 1].resize(trees[t].cols.size());
+    for (size_t c = 0; c < trees[t].cols.size(); c++) sampled[t + 1][c].resize(trees[t].two[c] ? 2 : 1);
   }
-  if (part_logs.size() > 1) HP_TRY(cs_lift_and_accumulate(parts.data(), part_logs.data(), (uint32_t)part_logs.size(), st));
+  row = 0;
+  for (auto& [key, members] : groups)
+    for (const Sample& m : members) {
+      sampled[m.tree + 1][m.col][m.slot] =
+          qm31_make(samples[4 * row], samples[4 * row + 1], samples[4 * row + 2], samples[4 * row + 3]);
+      row++;
+    }
+  {
+    std::vector<qm31> all;
+    for (auto& tr : sampled)
+      for (auto& col : tr) all.insert(all.end(), col.begin(), col.end());
+    ch.mix_felts(all);
+  }
+
+  // --- FRI quotients (quotient_ops.rs:86-160; periodicity samples, quotients.rs:274-319)
+  const qm31 quotient_coeff = ch.draw_secure_felt();
+  struct Entry {
+    uint32_t log;
+    uint32_t* col;
+    qpoint pt;
+    qm31 value;
+  };
+  std::vector<Entry> entries;
+  for (size_t t = 0; t < trees.size(); t++)
+    for (size_t c = 0; c < trees[t].cols.size(); c++) {
+      const Col& col = trees[t].cols[c];
+      const auto& v = sampled[t + 1][c];
+      if (trees[t].two[c]) {
+        const qpoint shifted = add_m31_point(oods, index_to_point(1u << (31 - (L - col.log))));
+        entries.push_back({col.log, col.p, shifted, v[1]});
+        entries.push_back({col.log, col.p, prev_pt, v[0]});
+        entries.push_back({col.log, col.p, oods, v[1]});
+      } else {
+        entries.push_back({col.log, col.p, oods, v[0]});
+      }
+    }
+  const std::vector<qm31> qp = powers(quotient_coeff, (uint32_t)entries.size());
+  struct Acc {
+    qpoint pt;
+    uint32_t* cols[4];
+    uint32_t log;
+    qm31 fl;
+  };
+  std::vector<Acc> accs;
+  std::vector<uint32_t> sizes;
+  for (const Entry& e : entries)
+    if (std::find(sizes.begin(), sizes.end(), e.log) == sizes.end()) sizes.push_back(e.log);
+  std::sort(sizes.begin(), sizes.end());
+  for (uint32_t ls : sizes) {
+    std::vector<std::pair<qpoint, std::vector<size_t>>> batches;  // by point, in insertion order
+    for (size_t k = 0; k < entries.size(); k++) {
+      if (entries[k].log != ls) continue;
+      auto it = std::find_if(batches.begin(), batches.end(), [&](auto& bt) { return same(bt.first, entries[k].pt); });
+      if (it == batches.end()) {
+        batches.push_back({entries[k].pt, {}});
+        it = batches.end() - 1;
+      }
+      it->second.push_back(k);
+    }
+    for (auto& [pt, ks] : batches) {
+      std::vector<uint32_t> coeffs(12 * ks.size());
+      std::vector<const uint32_t*> cols;
+      for (size_t j = 0; j < ks.size(); j++) {
+        line_coeffs(pt.y, entries[ks[j]].value, qp[ks[j]], &coeffs[12 * j]);
+        cols.push_back(entries[ks[j]].col);
+      }
+      const uint32_t pl = ls - b;
+      uint32_t* blk = A.alloc(4ull << pl);
+      if (!blk) return A.status;
+      Acc a;
+      a.pt = pt;
+      a.log = pl;
+      for (int c = 0; c < 4; c++) a.cols[c] = blk + ((size_t)c << pl);
+      uint32_t fl[4];
+      HP_TRY(cs_accumulate_numerators(cols.data(), (uint32_t)cols.size(), ls, b, coeffs.data(), a.cols, fl, st));
+      a.fl = qm31_make(fl[0], fl[1], fl[2], fl[3]);
+      accs.push_back(a);
+    }
+  }
+  // per point (sorted), lifted and accumulated over ascending sizes
+  std::vector<qpoint> points;
+  for (const Acc& a : accs)
+    if (std::find_if(points.begin(), points.end(), [&](const qpoint& p) { return same(p, a.pt); }) == points.end())
+      points.push_back(a.pt);
+  std::stable_sort(points.begin(), points.end(), point_less);
+  std::vector<const uint32_t*> qaccs;
+  std::vector<uint32_t> qlogs, qpts, qfl;
+  for (const qpoint& p : points) {
+    std::vector<uint32_t*> cols;
+    std::vector<uint32_t> logs;
+    qm31 fl = qm31_make(0, 0, 0, 0);
+    for (const Acc& a : accs)
+      if (same(a.pt, p)) {
+        cols.insert(cols.end(), a.cols, a.cols + 4);
+        logs.push_back(a.log);
+        fl = qm31_add(fl, a.fl);
+      }
+    if (logs.size() > 1) HP_TRY(cs_lift_and_accumulate(cols.data(), logs.data(), (uint32_t)logs.size(), st));
+    qaccs.insert(qaccs.end(), cols.end() - 4, cols.end());
+    qlogs.push_back(logs.back());
+    const uint32_t pw8[8] = {p.x.a.a, p.x.a.b, p.x.b.a, p.x.b.b, p.y.a.a, p.y.a.b, p.y.b.a, p.y.b.b};
+    qpts.insert(qpts.end(), pw8, pw8 + 8);
+    const uint32_t f4[4] = {fl.a.a, fl.a.b, fl.b.a, fl.b.b};
+    qfl.insert(qfl.end(), f4, f4 + 4);
+  }
   const uint32_t sub_log = L - b;
   uint32_t* qblk = A.alloc(4ull << sub_log);
   if (!qblk) return A.status;
   uint32_t* qcols[4] = {qblk, qblk + (1ull << sub_log), qblk + (2ull << sub_log), qblk + (3ull << sub_log)};
-  const uint32_t* accs[4] = {parts[parts.size() - 4], parts[parts.size() - 3], parts[parts.size() - 2],
-                             parts[parts.size() - 1]};
-  const uint32_t acc_log = part_logs.back();
-  const uint32_t pts[8] = {oods.x.a.a, oods.x.a.b, oods.x.b.a, oods.x.b.b,
-                           oods.y.a.a, oods.y.a.b, oods.y.b.a, oods.y.b.b};
-  const uint32_t flw[4] = {first_linear.a.a, first_linear.a.b, first_linear.b.a, first_linear.b.b};
-  HP_TRY(cs_quotients_on_subdomain(accs, &acc_log, 1, pts, flw, L, b, qcols, st));
-  HP_TRY(cs_interpolate_columns_on_subdomain(qcols, 4, sub_log, L, pp.d_itwiddles, pp.twiddle_log_size, st));
-  uint32_t* fblk = A.alloc(4ull << L);
-  if (!fblk) return A.status;
-  std::vector<uint32_t*> quotients = {fblk, fblk + (1ull << L), fblk + (2ull << L), fblk + (3ull << L)};
-  const uint32_t* qsrc[4] = {qcols[0], qcols[1], qcols[2], qcols[3]};
-  HP_TRY(cs_evaluate_columns(qsrc, quotients.data(), 4, sub_log, L, pp.d_twiddles, pp.twiddle_log_size, st));
+  HP_TRY(cs_quotients_on_subdomain(qaccs.data(), qlogs.data(), (uint32_t)points.size(), qpts.data(), qfl.data(), L,
+                                   b, qcols, st));
+  HP_TRY(cs_interpolate_columns_on_subdomain(qcols, 4, sub_log, L, cfg.itw, cfg.tw_log, st));
+  std::vector<uint32_t*> quotients;
+  HP_TRY(P.evaluate(std::vector<uint32_t*>(qcols, qcols + 4), sub_log, L, quotients));
 
   // --- FRI commit (fri.rs:113-226), fold_step 1, the channel kept on the device for the layer loop
-  const uint32_t last_log = pp.log_last_layer_degree_bound + b;
-  // 9 state words, then (from word 12, 16-byte aligned) room for the 64 challenges of up to 64 layers
+  const uint32_t last_log = cfg.log_last_layer_degree_bound + b;
+  // 9 state words, then (from word 12, 16-byte aligned) room for the challenges of up to 64 layers
   uint32_t* d_state = A.alloc(12 + 4 * 64);
   if (!d_state) return A.status;
   uint32_t state[9];
   std::memcpy(state, ch.digest, 32);
   state[8] = ch.n_draws;
   CS_CUDA(cudaMemcpyAsync(d_state, state, sizeof(state), cudaMemcpyHostToDevice, st));
-  uint32_t* d_felts = d_state + 12;  // 16-byte aligned
+  uint32_t* d_felts = d_state + 12;
   uint32_t n_felts = 0;
   std::vector<FriLayer> layers;
   Tree first_tree;
   HP_TRY(commit(A, quotients, std::vector<uint32_t>(4, L), L, first_tree));
   HP_TRY(cs_channel_mix_root(d_state, first_tree.layers + first_tree.words() - 8, st));
   HP_TRY(cs_channel_draw_secure_felt(d_state, d_felts + 4 * n_felts, st));
-  std::vector<uint32_t*> cur = quotients;
+  std::vector<uint32_t*> cur;
   uint32_t line_log = L - 1;
   {
     uint32_t* blk = A.alloc(4ull << line_log);
     if (!blk) return A.status;
-    std::vector<uint32_t*> nxt = {blk, blk + (1ull << line_log), blk + (2ull << line_log), blk + (3ull << line_log)};
-    const uint32_t* src[4] = {cur[0], cur[1], cur[2], cur[3]};
-    HP_TRY(cs_fold_circle_into_line_device_alpha(src, L, d_felts + 4 * n_felts, nxt.data(), pp.d_itwiddles,
-                                                 pp.twiddle_log_size, st));
+    cur = {blk, blk + (1ull << line_log), blk + (2ull << line_log), blk + (3ull << line_log)};
+    const uint32_t* src[4] = {quotients[0], quotients[1], quotients[2], quotients[3]};
+    HP_TRY(cs_fold_circle_into_line_device_alpha(src, L, d_felts + 4 * n_felts, cur.data(), cfg.itw, cfg.tw_log, st));
     n_felts++;
-    cur = nxt;
   }
   while (line_log >= last_log + 1 && n_felts < 64) {  // every layer above the last folds once
     FriLayer lay;
@@ -601,8 +768,7 @@ cs_status prove_wide_fib(const cs_wide_fib_proof_params& pp, uint32_t* const* d_
     if (!blk) return A.status;
     std::vector<uint32_t*> nxt = {blk, blk + (1ull << nl), blk + (2ull << nl), blk + (3ull << nl)};
     const uint32_t* src[4] = {cur[0], cur[1], cur[2], cur[3]};
-    HP_TRY(cs_fold_line_device_alpha(src, line_log, d_felts + 4 * n_felts, nxt.data(), pp.d_itwiddles,
-                                     pp.twiddle_log_size, st));
+    HP_TRY(cs_fold_line_device_alpha(src, line_log, d_felts + 4 * n_felts, nxt.data(), cfg.itw, cfg.tw_log, st));
     n_felts++;
     layers.push_back(lay);
     cur = nxt;
@@ -613,9 +779,9 @@ cs_status prove_wide_fib(const cs_wide_fib_proof_params& pp, uint32_t* const* d_
   {
     Reads R;
     for (int i = 0; i < 9; i++) R.add(d_state, 9, i);
-    std::vector<Tree*> trees = {&first_tree};
-    for (FriLayer& l : layers) trees.push_back(&l.tree);
-    for (Tree* t : trees)
+    std::vector<Tree*> ts = {&first_tree};
+    for (FriLayer& l : layers) ts.push_back(&l.tree);
+    for (Tree* t : ts)
       for (int i = 0; i < 8; i++) R.add(t->layers, t->words(), t->words() - 8 + i);
     const uint32_t last_n = 1u << last_log;
     for (int c = 0; c < 4; c++)
@@ -625,7 +791,7 @@ cs_status prove_wide_fib(const cs_wide_fib_proof_params& pp, uint32_t* const* d_
       for (int k = 0; k < 4; k++) ch.digest[4 * i + k] = (uint8_t)(R.out[i] >> (8 * k));
     ch.n_draws = R.out[8];
     size_t o = 9;
-    for (Tree* t : trees) {
+    for (Tree* t : ts) {
       for (int i = 0; i < 8; i++)
         for (int k = 0; k < 4; k++) t->root[4 * i + k] = (uint8_t)(R.out[o + i] >> (8 * k));
       o += 8;
@@ -636,20 +802,20 @@ cs_status prove_wide_fib(const cs_wide_fib_proof_params& pp, uint32_t* const* d_
                                  R.out[o + 3 * last_n + i]);
     // commit_last_layer (fri.rs:208-226)
     const std::vector<qm31> coeffs = line_interpolate(last_values, last_log);
-    const uint32_t bound = 1u << pp.log_last_layer_degree_bound;
+    const uint32_t bound = 1u << cfg.log_last_layer_degree_bound;
     for (uint32_t i = bound; i < last_n; i++)
       CS_CHECK_ARG(coeffs[i].a.a == 0 && coeffs[i].a.b == 0 && coeffs[i].b.a == 0 && coeffs[i].b.b == 0,
-                   "prove_wide_fib: invalid degree in the last FRI layer");
+                   "prove: invalid degree in the last FRI layer");
     last_poly.resize(bound);
-    for (uint32_t i = 0; i < bound; i++) last_poly[i] = coeffs[bitrev(i, pp.log_last_layer_degree_bound)];
+    for (uint32_t i = 0; i < bound; i++) last_poly[i] = coeffs[bitrev(i, cfg.log_last_layer_degree_bound)];
     ch.mix_felts(last_poly);
   }
 
   // --- FRI proof of work and queries (fri.rs:229-283)
   uint64_t fri_pow = 0;
-  HP_TRY(cs_grind_blake2s(ch.digest, pp.pow_bits, 1ull << 48, &fri_pow, st));
+  HP_TRY(cs_grind_blake2s(ch.digest, cfg.pow_bits, 1ull << 48, &fri_pow, st));
   ch.mix_u64(fri_pow);
-  std::vector<uint32_t> qraw = ch.draw_queries(L, pp.n_queries);
+  const std::vector<uint32_t> qraw = ch.draw_queries(L, cfg.n_queries);
   std::vector<uint64_t> queries(qraw.begin(), qraw.end());
   std::sort(queries.begin(), queries.end());
   queries.erase(std::unique(queries.begin(), queries.end()), queries.end());
@@ -668,10 +834,10 @@ cs_status prove_wide_fib(const cs_wide_fib_proof_params& pp, uint32_t* const* d_
     std::vector<uint64_t> starts;
     for (uint64_t x : q)
       if (starts.empty() || starts.back() != ((x >> 1) << 1)) starts.push_back((x >> 1) << 1);
-    for (uint64_t s : starts)
+    for (uint64_t s0 : starts)
       for (uint64_t j = 0; j < 2; j++) {
-        d.positions.push_back(s + j);
-        d.is_witness.push_back(!std::binary_search(q.begin(), q.end(), s + j));
+        d.positions.push_back(s0 + j);
+        d.is_witness.push_back(!std::binary_search(q.begin(), q.end(), s0 + j));
       }
     d.coord_first = R.slots.size();
     for (int c = 0; c < 4; c++)
@@ -679,7 +845,7 @@ cs_status prove_wide_fib(const cs_wide_fib_proof_params& pp, uint32_t* const* d_
     d.wit = read_witness(R, t, d.positions);
     return d;
   };
-  LayerDec first_dec = fri_layer(quotients, L, first_tree, queries);
+  const LayerDec first_dec = fri_layer(quotients, L, first_tree, queries);
   std::vector<LayerDec> inner_dec;
   std::vector<uint64_t> lq;
   for (uint64_t x : queries)
@@ -691,95 +857,69 @@ cs_status prove_wide_fib(const cs_wide_fib_proof_params& pp, uint32_t* const* d_
       if (nq.empty() || nq.back() != (x >> 1)) nq.push_back(x >> 1);
     lq = nq;
   }
-  // tree decommitments (MerkleProverLifted::decommit): queried values per column, then the witness
   struct TreeDec {
     size_t values_first;
     std::pair<size_t, size_t> wit;
   };
-  const auto tree_dec = [&](const Tree& t, const std::vector<uint32_t*>& cols, const std::vector<uint32_t>& logs) {
+  std::vector<TreeDec> tree_decs;
+  for (TreeCols& t : trees) {  // MerkleProverLifted::decommit: queried values per column, then the witness
     TreeDec d;
     d.values_first = R.slots.size();
-    for (size_t c = 0; c < cols.size(); c++) {
-      const uint32_t shift = t.height - logs[c];
-      for (uint64_t q : queries) R.add(cols[c], 1ull << logs[c], ((q >> (shift + 1)) << 1) + (q & 1));
+    for (const Col& c : t.cols) {
+      const uint32_t shift = L - c.log;
+      for (uint64_t q : queries) R.add(c.p, 1ull << c.log, ((q >> (shift + 1)) << 1) + (q & 1));
     }
-    d.wit = read_witness(R, t, queries);
-    return d;
-  };
-  TreeDec trace_dec = tree_dec(trace_tree, trace_evals, trace_logs);
-  TreeDec comp_dec = tree_dec(comp_tree, comp_cols, std::vector<uint32_t>(8, comp_eval_log));
+    d.wit = read_witness(R, t.tree, queries);
+    tree_decs.push_back(d);
+  }
   HP_TRY(R.run(st));
 
-  // --- sanity check (mod.rs:121-132): the composition at the OODS point against the AIR
+  // --- sanity check (mod.rs:121-132)
   {
-    const uint32_t mldb = L - b;
-    const qm31* cs = sampled.data() + trace_evals.size();
-    const auto from_partial_evals = [](const qm31* e) {
-      qm31 r = e[0];
-      r = qm31_add(r, qm31_mul(e[1], qm31_make(0, 1, 0, 0)));
-      r = qm31_add(r, qm31_mul(e[2], qm31_make(0, 0, 1, 0)));
-      r = qm31_add(r, qm31_mul(e[3], qm31_make(0, 0, 0, 1)));
-      return r;
-    };
-    const qm31 left = from_partial_evals(cs), right = from_partial_evals(cs + 4);
-    qm31 x = oods.x;
-    for (uint32_t i = 0; i + 1 < mldb; i++) x = q_double_x(x);
-    const qm31 comp = qm31_add(left, qm31_mul(x, right));
-    qm31 acc = qm31_make(0, 0, 0, 0);
-    size_t s = 0;
-    for (uint32_t k = 0; k < n_comp; k++) {
-      const qm31* m = sampled.data() + s;
-      for (uint32_t j = 0; j + 2 < pp.n_cols[k]; j++) {
-        const qm31 cons = qm31_sub(m[j + 2], qm31_add(qm31_mul(m[j], m[j]), qm31_mul(m[j + 1], m[j + 1])));
-        acc = qm31_add(qm31_mul(acc, random_coeff), cons);
-      }
-      s += pp.n_cols[k];
+    qm31 expected;
+    if (air.at_point(oods, mldb, random_coeff, sampled, expected)) {
+      std::vector<qm31> cs;
+      for (auto& col : sampled.back()) cs.push_back(col[0]);
+      const qm31 left = from_partial_evals(cs.data()), right = from_partial_evals(cs.data() + 4);
+      qm31 x = oods.x;
+      for (uint32_t i = 0; i + 1 < mldb; i++) x = q_double_x(x);
+      const qm31 comp = qm31_add(left, qm31_mul(x, right));
+      CS_CHECK_ARG(std::memcmp(&comp, &expected, sizeof(qm31)) == 0,
+                   "prove: constraints not satisfied (ProvingError::ConstraintsNotSatisfied)");
     }
-    const qm31 expected = qm31_mul(acc, qm31_inv(x));
-    CS_CHECK_ARG(std::memcmp(&comp, &expected, sizeof(qm31)) == 0,
-                 "prove_wide_fib: constraints not satisfied (ProvingError::ConstraintsNotSatisfied)");
   }
 
   // --- the felt stream (CairoSerialize for StarkProof)
   Words W;
-  W.u(pp.pow_bits);
+  W.u(cfg.pow_bits);
   W.u(b);
-  W.u(pp.log_last_layer_degree_bound);
-  W.u(pp.n_queries);
+  W.u(cfg.log_last_layer_degree_bound);
+  W.u(cfg.n_queries);
   W.u(1);
-  W.u(3);  // commitments
+  W.u(trees.size() + 1);  // commitments
   W.h(pre_root);
-  W.h(trace_tree.root);
-  W.h(comp_tree.root);
+  for (TreeCols& t : trees) W.h(t.tree.root);
   W.u(oods_pow);
-  W.u(3);  // sampled values: trees
-  W.u(0);
-  W.u(trace_evals.size());
-  for (size_t i = 0; i < trace_evals.size(); i++) {
-    W.u(1);
-    W.q(sampled[i]);
+  W.u(sampled.size());
+  for (auto& tr : sampled) {
+    W.u(tr.size());
+    for (auto& col : tr) {
+      W.u(col.size());
+      for (const qm31& v : col) W.q(v);
+    }
   }
-  W.u(8);
-  for (size_t i = 0; i < 8; i++) {
-    W.u(1);
-    W.q(sampled[trace_evals.size() + i]);
-  }
-  W.u(3);  // decommitments
+  W.u(trees.size() + 1);  // decommitments
   W.u(0);
-  W.hw(R.out, trace_dec.wit.first, trace_dec.wit.second);
-  W.hw(R.out, comp_dec.wit.first, comp_dec.wit.second);
-  W.u(3);  // queried values
+  for (TreeDec& d : tree_decs) W.hw(R.out, d.wit.first, d.wit.second);
+  W.u(trees.size() + 1);  // queried values
   W.u(0);
   const size_t nq = queries.size();
-  W.u(trace_evals.size());
-  for (size_t c = 0; c < trace_evals.size(); c++) {
-    W.u(nq);
-    for (size_t i = 0; i < nq; i++) W.u(R.out[trace_dec.values_first + c * nq + i]);
-  }
-  W.u(8);
-  for (size_t c = 0; c < 8; c++) {
-    W.u(nq);
-    for (size_t i = 0; i < nq; i++) W.u(R.out[comp_dec.values_first + c * nq + i]);
+  for (size_t t = 0; t < trees.size(); t++) {
+    W.u(trees[t].cols.size());
+    for (size_t c = 0; c < trees[t].cols.size(); c++) {
+      W.u(nq);
+      for (size_t i = 0; i < nq; i++) W.u(R.out[tree_decs[t].values_first + c * nq + i]);
+    }
   }
   const auto layer_words = [&](const LayerDec& d, const Tree& t) {
     const size_t np = d.positions.size();
@@ -798,11 +938,240 @@ cs_status prove_wide_fib(const cs_wide_fib_proof_params& pp, uint32_t* const* d_
   for (size_t i = 0; i < layers.size(); i++) layer_words(inner_dec[i], layers[i].tree);
   W.u(last_poly.size());
   for (const qm31& c : last_poly) W.q(c);
-  W.u(pp.log_last_layer_degree_bound);
+  W.u(cfg.log_last_layer_degree_bound);
   W.u(fri_pow);
   words.swap(W.w);
   return CS_OK;
 }
+
+// ---------------------------------------------------------------- AIRs
+
+// Wide-Fibonacci components (WideFibonacciEval, crates/examples/src/wide_fibonacci/mod.rs:87-97)
+// and single-column LogUp components beside them.
+struct FibLookupAir : Air {
+  std::vector<uint32_t> n_cols, logs, lookup_logs;
+  uint32_t* const* d_trace;
+  const uint32_t* const* d_values;  // the LogUp components' looked-up values (trace domain)
+  std::vector<std::vector<uint32_t*>> fib_evals;
+  std::vector<uint32_t*> lookup_evals;
+  std::vector<std::vector<uint32_t*>> inter_evals;
+  qm31 z;
+
+  cs_status trace(Prover& P, std::vector<Col>& cols) override {
+    size_t c0 = 0;
+    for (size_t k = 0; k < n_cols.size(); k++) {
+      std::vector<uint32_t*> c(d_trace + c0, d_trace + c0 + n_cols[k]);
+      HP_TRY(P.interpolate(c, logs[k]));
+      std::vector<uint32_t*> ev;
+      HP_TRY(P.evaluate(c, logs[k], logs[k] + P.cfg.b, ev));
+      for (uint32_t* e : ev) cols.push_back({e, logs[k] + P.cfg.b});
+      fib_evals.push_back(ev);
+      c0 += n_cols[k];
+    }
+    for (size_t k = 0; k < lookup_logs.size(); k++) {  // out of place: the values stay for the sums
+      const uint32_t l = lookup_logs[k];
+      uint32_t* coeffs = P.A.alloc(1ull << l);
+      if (!coeffs) return P.A.status;
+      const uint32_t* src = d_values[k];
+      HP_TRY(cs_interpolate_columns_into(&src, &coeffs, 1, l, P.cfg.itw, P.cfg.tw_log, P.st));
+      std::vector<uint32_t*> ev;
+      HP_TRY(P.evaluate({coeffs}, l, l + P.cfg.b, ev));
+      lookup_evals.push_back(ev[0]);
+      cols.push_back({ev[0], l + P.cfg.b});
+      P.A.release(coeffs);
+    }
+    return CS_OK;
+  }
+  bool has_interaction() const override { return !lookup_logs.empty(); }
+  bool mix_claimed() const override { return true; }
+  cs_status interaction(Prover& P, const qm31& zz, const qm31&, std::vector<Col>& cols, std::vector<bool>& two,
+                        std::vector<qm31>& claimed) override {
+    z = zz;
+    const size_t n = lookup_logs.size();
+    std::vector<uint32_t*> sums(4 * n);
+    for (size_t k = 0; k < n; k++) {
+      uint32_t* blk = P.A.alloc(4ull << lookup_logs[k]);
+      if (!blk) return P.A.status;
+      for (int c = 0; c < 4; c++) sums[4 * k + c] = blk + ((size_t)c << lookup_logs[k]);
+    }
+    uint32_t* d_claimed = P.A.alloc(4 * n);
+    if (!d_claimed) return P.A.status;
+    const uint32_t zw[4] = {z.a.a, z.a.b, z.b.a, z.b.b};
+    std::vector<const uint32_t*> vals(d_values, d_values + n);
+    HP_TRY(cs_logup_running_sums((uint32_t)n, vals.data(), lookup_logs.data(), zw, sums.data(), d_claimed, P.st));
+    std::vector<uint32_t> cl(4 * n);
+    CS_CUDA(cudaMemcpyAsync(cl.data(), d_claimed, 16 * n, cudaMemcpyDeviceToHost, P.st));
+    CS_CUDA(cudaStreamSynchronize(P.st));
+    claimed.clear();
+    for (size_t k = 0; k < n; k++) claimed.push_back(qm31_make(cl[4 * k], cl[4 * k + 1], cl[4 * k + 2], cl[4 * k + 3]));
+    for (size_t k = 0; k < n; k++) {
+      std::vector<uint32_t*> coords(sums.begin() + 4 * k, sums.begin() + 4 * k + 4);
+      HP_TRY(P.interpolate(coords, lookup_logs[k]));
+      std::vector<uint32_t*> ev;
+      HP_TRY(P.evaluate(coords, lookup_logs[k], lookup_logs[k] + P.cfg.b, ev));
+      inter_evals.push_back(ev);
+      for (uint32_t* e : ev) {
+        cols.push_back({e, lookup_logs[k] + P.cfg.b});
+        two.push_back(true);
+      }
+    }
+    this->claimed = claimed;
+    return CS_OK;
+  }
+  std::vector<qm31> claimed;
+  uint32_t n_constraints() const override {
+    uint32_t t = 0;
+    for (uint32_t n : n_cols) t += n - 2;
+    return t + (uint32_t)lookup_logs.size();
+  }
+  cs_status composition(Prover& P, const std::vector<qm31>& pw,
+                        std::map<uint32_t, std::vector<uint32_t*>>& acc) override {
+    const uint32_t total = n_constraints();
+    uint32_t start = 0;
+    for (size_t k = 0; k < n_cols.size(); k++) {  // each component takes the last powers, reversed
+      const uint32_t n = n_cols[k] - 2, el = logs[k] + 1;
+      std::vector<uint32_t> rc(4 * n);
+      for (uint32_t j = 0; j < n; j++) {
+        const qm31 x = pw[total - start - 1 - j];
+        rc[4 * j] = x.a.a;
+        rc[4 * j + 1] = x.a.b;
+        rc[4 * j + 2] = x.b.a;
+        rc[4 * j + 3] = x.b.b;
+      }
+      std::vector<const uint32_t*> ev(fib_evals[k].begin(), fib_evals[k].end());
+      HP_TRY(cs_wide_fib_composition(ev.data(), n + 2, el, logs[k], rc.data(), P.acc_for(acc, el).data(), P.st));
+      start += n;
+    }
+    // LogUp components of one size in one pass (cs_logup_compositions), in first-seen size order
+    std::vector<uint32_t> order;
+    for (uint32_t l : lookup_logs)
+      if (std::find(order.begin(), order.end(), l) == order.end()) order.push_back(l);
+    for (uint32_t l : order) {
+      std::vector<const uint32_t*> vals, inter;
+      std::vector<uint32_t> cl, rcs;
+      for (size_t k = 0; k < lookup_logs.size(); k++) {
+        if (lookup_logs[k] != l) continue;
+        vals.push_back(lookup_evals[k]);
+        for (int c = 0; c < 4; c++) inter.push_back(inter_evals[k][c]);
+        const qm31 w = pw[total - start - 1 - (uint32_t)k];
+        const uint32_t ww[4] = {w.a.a, w.a.b, w.b.a, w.b.b};
+        const uint32_t cw[4] = {claimed[k].a.a, claimed[k].a.b, claimed[k].b.a, claimed[k].b.b};
+        rcs.insert(rcs.end(), ww, ww + 4);
+        cl.insert(cl.end(), cw, cw + 4);
+      }
+      const uint32_t zw[4] = {z.a.a, z.a.b, z.b.a, z.b.b};
+      HP_TRY(cs_logup_compositions((uint32_t)vals.size(), vals.data(), inter.data(), l + 1, l, zw, cl.data(),
+                                   rcs.data(), P.acc_for(acc, l + 1).data(), P.st));
+    }
+    return CS_OK;
+  }
+  bool at_point(const qpoint& oods, uint32_t mldb, const qm31& random_coeff,
+                const std::vector<std::vector<std::vector<qm31>>>& sampled, qm31& expected) override {
+    qm31 x = oods.x;
+    for (uint32_t i = 0; i + 1 < mldb; i++) x = q_double_x(x);
+    qm31 acc = qm31_make(0, 0, 0, 0);
+    const auto& tr = sampled[1];
+    size_t s0 = 0;
+    for (size_t k = 0; k < n_cols.size(); k++) {
+      for (uint32_t j = 0; j + 2 < n_cols[k]; j++) {
+        const qm31 a = tr[s0 + j][0], bb = tr[s0 + j + 1][0], c = tr[s0 + j + 2][0];
+        acc = qm31_add(qm31_mul(acc, random_coeff), qm31_sub(c, qm31_add(qm31_mul(a, a), qm31_mul(bb, bb))));
+      }
+      s0 += n_cols[k];
+    }
+    for (size_t k = 0; k < lookup_logs.size(); k++) {
+      const qm31 v = tr[s0 + k][0];
+      qm31 pe[4], ce[4];
+      for (int c = 0; c < 4; c++) {
+        pe[c] = sampled[2][4 * k + c][0];
+        ce[c] = sampled[2][4 * k + c][1];
+      }
+      const qm31 shift = qm31_mul_m31(claimed[k], m31_inv(1u << lookup_logs[k]));
+      const qm31 shifted = qm31_add(qm31_sub(from_partial_evals(ce), from_partial_evals(pe)), shift);
+      const qm31 cons = qm31_add(qm31_mul(shifted, qm31_sub(v, z)), q1());
+      acc = qm31_add(qm31_mul(acc, random_coeff), cons);
+    }
+    expected = qm31_mul(acc, qm31_inv(x));
+    return true;
+  }
+};
+
+// The Poseidon2 AIR (crates/examples/src/poseidon/mod.rs:320-379): 1264 trace columns generated on the
+// device, 32 interaction columns (the last four also sampled at the previous row), constraint quotients
+// on CanonicCoset(n + 2) (ExtendToEvalDomain). No sanity check: the reference's own prove of this AIR
+// stops there (lifted protocol, constraint degree 5), and the proof is built as it computes it.
+struct PoseidonAir : Air {
+  static constexpr uint32_t kCols = 1264, kInter = 32, kConstraints = 1144, kExpand = 2;
+  uint32_t log_n = 0;
+  std::vector<uint32_t*> trace_vals, trace_coeffs, inter_coeffs;
+  uint32_t lookup[8];
+  qm31 claimed_sum;
+
+  cs_status trace(Prover& P, std::vector<Col>& cols) override {
+    const uint32_t n = log_n;
+    uint32_t* blk = P.A.alloc((size_t)kCols << n);
+    uint32_t* cblk = P.A.alloc((size_t)kCols << n);
+    if (!blk || !cblk) return P.A.status;
+    for (uint32_t j = 0; j < kCols; j++) {
+      trace_vals.push_back(blk + ((size_t)j << n));
+      trace_coeffs.push_back(cblk + ((size_t)j << n));
+    }
+    HP_TRY(cs_poseidon_trace(n, trace_vals.data(), P.st));
+    std::vector<const uint32_t*> src(trace_vals.begin(), trace_vals.end());
+    HP_TRY(cs_interpolate_columns_into(src.data(), trace_coeffs.data(), kCols, n, P.cfg.itw, P.cfg.tw_log, P.st));
+    std::vector<uint32_t*> ev;
+    HP_TRY(P.evaluate(trace_coeffs, n, n + P.cfg.b, ev));
+    for (uint32_t* e : ev) cols.push_back({e, n + P.cfg.b});
+    return CS_OK;
+  }
+  bool has_interaction() const override { return true; }
+  cs_status interaction(Prover& P, const qm31& z, const qm31& alpha, std::vector<Col>& cols, std::vector<bool>& two,
+                        std::vector<qm31>& claimed) override {
+    const uint32_t n = log_n;
+    const uint32_t lk[8] = {z.a.a, z.a.b, z.b.a, z.b.b, alpha.a.a, alpha.a.b, alpha.b.a, alpha.b.b};
+    std::copy(lk, lk + 8, lookup);
+    uint32_t* blk = P.A.alloc((size_t)kInter << n);
+    if (!blk) return P.A.status;
+    for (uint32_t j = 0; j < kInter; j++) inter_coeffs.push_back(blk + ((size_t)j << n));
+    std::vector<const uint32_t*> src(trace_vals.begin(), trace_vals.end());
+    uint32_t cs[4];
+    HP_TRY(cs_poseidon_interaction(src.data(), n, lookup, inter_coeffs.data(), cs, P.st));
+    P.A.release(trace_vals[0]);  // the trace values are no longer needed
+    claimed_sum = qm31_make(cs[0], cs[1], cs[2], cs[3]);
+    claimed = {claimed_sum};
+    HP_TRY(P.interpolate(inter_coeffs, n));
+    std::vector<uint32_t*> ev;
+    HP_TRY(P.evaluate(inter_coeffs, n, n + P.cfg.b, ev));
+    for (uint32_t j = 0; j < kInter; j++) {
+      cols.push_back({ev[j], n + P.cfg.b});
+      two.push_back(j >= kInter - 4);
+    }
+    return CS_OK;
+  }
+  uint32_t n_constraints() const override { return kConstraints; }
+  cs_status composition(Prover& P, const std::vector<qm31>& pw,
+                        std::map<uint32_t, std::vector<uint32_t*>>& acc) override {
+    const uint32_t n = log_n, el = n + kExpand;
+    // EvaluationMode::infer: constraint log degree 2 > log_blowup 1 -> ExtendToEvalDomain
+    std::vector<uint32_t*> tev, iev;
+    HP_TRY(P.evaluate(trace_coeffs, n, el, tev));
+    HP_TRY(P.evaluate(inter_coeffs, n, el, iev));
+    std::vector<uint32_t> rc(4 * kConstraints);
+    for (uint32_t j = 0; j < kConstraints; j++) {
+      const qm31 x = pw[kConstraints - 1 - j];
+      rc[4 * j] = x.a.a;
+      rc[4 * j + 1] = x.a.b;
+      rc[4 * j + 2] = x.b.a;
+      rc[4 * j + 3] = x.b.b;
+    }
+    const uint32_t cl[4] = {claimed_sum.a.a, claimed_sum.a.b, claimed_sum.b.a, claimed_sum.b.b};
+    std::vector<const uint32_t*> t(tev.begin(), tev.end()), i(iev.begin(), iev.end());
+    HP_TRY(cs_poseidon_composition(t.data(), i.data(), el, n, lookup, cl, rc.data(), P.acc_for(acc, el).data(), P.st));
+    P.A.release(tev[0]);
+    P.A.release(iev[0]);
+    return CS_OK;
+  }
+};
 
 }  // namespace hp
 }  // namespace cs
@@ -815,34 +1184,96 @@ extern "C" cs_status cs_host_blake2s(const uint8_t* msg, size_t n, uint8_t out[3
   return CS_OK;
 }
 
+namespace {
+
+cs_status finish(std::vector<uint64_t>& words, uint64_t* h_words, size_t capacity, size_t* n_words) {
+  *n_words = words.size();
+  CS_CHECK_ARG(h_words == nullptr || capacity >= words.size(), "prove: %zu words do not fit in %zu", words.size(),
+               capacity);
+  if (h_words != nullptr) std::copy(words.begin(), words.end(), h_words);
+  return CS_OK;
+}
+
+cs_status check_common(const cs_wide_fib_proof_params& pp, uint32_t max_log) {
+  CS_CHECK_ARG(pp.log_blowup_factor == 1, "prove: log_blowup_factor 1 (SubDomain evaluation)");
+  CS_CHECK_ARG(pp.d_twiddles != nullptr && pp.d_itwiddles != nullptr, "prove: null twiddles");
+  CS_CHECK_ARG(pp.pow_bits <= 32 && pp.n_queries >= 1, "prove: bad FRI parameters");
+  CS_CHECK_ARG(pp.lifting_log_size == max_log + pp.log_blowup_factor,
+               "prove: lifting_log_size must be the largest evaluation size (%u)", max_log + 1);
+  CS_CHECK_ARG(pp.lifting_log_size > pp.log_last_layer_degree_bound + pp.log_blowup_factor + 1 &&
+                   pp.lifting_log_size <= 28,
+               "prove: lifting_log_size %u outside the FRI parameters' range", pp.lifting_log_size);
+  CS_CHECK_ARG(pp.twiddle_log_size >= pp.lifting_log_size, "prove: twiddle tree too small");
+  return CS_OK;
+}
+
+hp::ProofConfig config_of(const cs_wide_fib_proof_params& pp) {
+  return {pp.lifting_log_size, pp.log_blowup_factor, pp.pow_bits, pp.log_last_layer_degree_bound,
+          pp.n_queries, pp.d_twiddles, pp.d_itwiddles, pp.twiddle_log_size};
+}
+
+}  // namespace
+
 extern "C" cs_status cs_prove_wide_fib(const cs_wide_fib_proof_params* params, uint32_t* const* d_trace,
                                        uint64_t* h_words, size_t capacity, size_t* n_words, cs_stream stream) {
-  CS_CHECK_ARG(params != nullptr && d_trace != nullptr && n_words != nullptr, "prove_wide_fib: null pointer");
+  return cs_prove_fib_and_lookups(params, d_trace, 0, nullptr, nullptr, nullptr, h_words, capacity, n_words, stream);
+}
+
+extern "C" cs_status cs_prove_fib_and_lookups(const cs_wide_fib_proof_params* params, uint32_t* const* d_trace,
+                                              uint32_t n_lookups, const uint32_t* const* d_values,
+                                              const uint32_t* h_lookup_log_sizes, uint32_t* h_claimed,
+                                              uint64_t* h_words, size_t capacity, size_t* n_words,
+                                              cs_stream stream) {
+  CS_CHECK_ARG(params != nullptr && d_trace != nullptr && n_words != nullptr, "prove: null pointer");
   const cs_wide_fib_proof_params& pp = *params;
-  CS_CHECK_ARG(pp.n_components >= 1 && pp.n_cols != nullptr && pp.log_sizes != nullptr,
-               "prove_wide_fib: no components");
-  CS_CHECK_ARG(pp.log_blowup_factor == 1, "prove_wide_fib: log_blowup_factor 1 (SubDomain evaluation)");
-  CS_CHECK_ARG(pp.d_twiddles != nullptr && pp.d_itwiddles != nullptr, "prove_wide_fib: null twiddles");
-  CS_CHECK_ARG(pp.pow_bits <= 32 && pp.n_queries >= 1, "prove_wide_fib: bad FRI parameters");
+  CS_CHECK_ARG(pp.n_components >= 1 && pp.n_cols != nullptr && pp.log_sizes != nullptr, "prove: no components");
+  CS_CHECK_ARG(n_lookups == 0 || (d_values != nullptr && h_lookup_log_sizes != nullptr && h_claimed != nullptr),
+               "prove: null lookup table");
   uint32_t max_log = 0, n_total = 0;
   for (uint32_t k = 0; k < pp.n_components; k++) {
-    CS_CHECK_ARG(pp.n_cols[k] >= 3 && pp.log_sizes[k] >= 1, "prove_wide_fib: component %u: %u columns of 2^%u", k,
+    CS_CHECK_ARG(pp.n_cols[k] >= 3 && pp.log_sizes[k] >= 1, "prove: component %u: %u columns of 2^%u", k,
                  pp.n_cols[k], pp.log_sizes[k]);
     max_log = std::max(max_log, pp.log_sizes[k]);
     n_total += pp.n_cols[k];
   }
-  for (uint32_t c = 0; c < n_total; c++) CS_CHECK_ARG(d_trace[c] != nullptr, "prove_wide_fib: column %u is null", c);
-  CS_CHECK_ARG(pp.lifting_log_size == max_log + pp.log_blowup_factor,
-               "prove_wide_fib: lifting_log_size must be the largest evaluation size (%u)", max_log + 1);
-  CS_CHECK_ARG(pp.lifting_log_size > pp.log_last_layer_degree_bound + pp.log_blowup_factor + 1,
-               "prove_wide_fib: the trace is too small for the FRI parameters");
-  CS_CHECK_ARG(pp.twiddle_log_size >= pp.lifting_log_size, "prove_wide_fib: twiddle tree too small");
+  for (uint32_t c = 0; c < n_total; c++) CS_CHECK_ARG(d_trace[c] != nullptr, "prove: column %u is null", c);
+  for (uint32_t k = 0; k < n_lookups; k++) {
+    CS_CHECK_ARG(d_values[k] != nullptr && h_lookup_log_sizes[k] >= 1, "prove: lookup %u is empty", k);
+    max_log = std::max(max_log, h_lookup_log_sizes[k]);
+  }
+  const cs_status cs = check_common(pp, max_log);
+  if (cs != CS_OK) return cs;
+  hp::FibLookupAir air;
+  air.n_cols.assign(pp.n_cols, pp.n_cols + pp.n_components);
+  air.logs.assign(pp.log_sizes, pp.log_sizes + pp.n_components);
+  if (n_lookups) air.lookup_logs.assign(h_lookup_log_sizes, h_lookup_log_sizes + n_lookups);
+  air.d_trace = d_trace;
+  air.d_values = d_values;
   std::vector<uint64_t> words;
-  cs_status s = hp::prove_wide_fib(pp, d_trace, words, to_stream(stream));
+  std::vector<qm31> claimed;
+  const cs_status s = hp::prove(config_of(pp), air, words, claimed, to_stream(stream));
   if (s != CS_OK) return s;
-  *n_words = words.size();
-  CS_CHECK_ARG(h_words == nullptr || capacity >= words.size(), "prove_wide_fib: %zu words do not fit in %zu",
-               words.size(), capacity);
-  if (h_words != nullptr) std::copy(words.begin(), words.end(), h_words);
-  return CS_OK;
+  for (uint32_t k = 0; k < n_lookups; k++) {
+    h_claimed[4 * k] = claimed[k].a.a;
+    h_claimed[4 * k + 1] = claimed[k].a.b;
+    h_claimed[4 * k + 2] = claimed[k].b.a;
+    h_claimed[4 * k + 3] = claimed[k].b.b;
+  }
+  return finish(words, h_words, capacity, n_words);
+}
+
+extern "C" cs_status cs_prove_poseidon(uint32_t log_n_rows, const cs_wide_fib_proof_params* params,
+                                       uint64_t* h_words, size_t capacity, size_t* n_words, cs_stream stream) {
+  CS_CHECK_ARG(params != nullptr && n_words != nullptr, "prove_poseidon: null pointer");
+  CS_CHECK_ARG(log_n_rows >= 1 && log_n_rows <= 22, "prove_poseidon: log_n_rows %u outside [1, 22]", log_n_rows);
+  // poseidon_pcs_config (mod.rs:305-318): the tree height is log_n_rows + 2 - 1 + log_blowup
+  const cs_status cs = check_common(*params, log_n_rows + 1);
+  if (cs != CS_OK) return cs;
+  hp::PoseidonAir air;
+  air.log_n = log_n_rows;
+  std::vector<uint64_t> words;
+  std::vector<qm31> claimed;
+  const cs_status s = hp::prove(config_of(*params), air, words, claimed, to_stream(stream));
+  if (s != CS_OK) return s;
+  return finish(words, h_words, capacity, n_words);
 }

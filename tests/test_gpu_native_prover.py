@@ -49,3 +49,44 @@ def test_native_proof_bytes_equal_restated_prover(B, shape, n_queries):
                                               pr.Blake2sChannel(), cpu.twiddles(L + 1))
         assert native == oracle.to_bytes()
         verify_wide_fib_components(restated, [n for n, _ in shape], logs)
+
+
+def _fib_lookup_inputs(shape, lookup_logs, seed):
+    traces = _traces(shape, seed)
+    rng = np.random.default_rng(seed)
+    values = [rng.integers(0, O.P, 1 << l, dtype=np.uint32) for l in lookup_logs]
+    return traces, values
+
+
+@pytest.mark.parametrize("shape,lookup_logs,n_queries", [([(4, 9), (5, 3)], [8, 4], 3),
+                                                         ([(10, 5), (3, 8)], [8, 2, 5, 8], 70)])
+def test_native_fib_and_lookups_equal_restated_prover(B, shape, lookup_logs, n_queries):
+    from proving_gb300.backend import BaseColumn
+    host, values = _fib_lookup_inputs(shape, lookup_logs, 7)
+    logs = [l for _, l in shape]
+    L = max(logs + lookup_logs) + 1
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=n_queries, fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=L)
+    ops = pr.GpuOps()
+    tw = ops.twiddles(L + 1)
+    native, claimed = B.prove_fib_and_lookups_native(
+        [[BaseColumn.from_cpu(c) for c in t] for t in host], logs, [BaseColumn.from_cpu(v) for v in values],
+        lookup_logs, (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound, fp.n_queries), tw)
+    restated = pr.prove_fib_and_lookups(ops, [ops.columns_from_host(t) for t in host], logs,
+                                        [ops.columns_from_host([v])[0] for v in values], lookup_logs, cfg,
+                                        pr.Blake2sChannel(), tw)
+    assert claimed == restated.claimed_sums
+    assert native == restated.to_bytes()
+
+
+@pytest.mark.parametrize("log_n", [4, 7])
+def test_native_poseidon_equals_restated_prover(B, log_n):
+    from proving_gb300 import poseidon as ps
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = ps.poseidon_pcs_config(log_n + 3, fp)
+    ops = pr.GpuOps()
+    tw = ops.twiddles(log_n + 3)
+    native = B.prove_poseidon_native(log_n, (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound,
+                                             fp.n_queries), tw)
+    restated = ps.prove_poseidon(ops, log_n, cfg, pr.Blake2sChannel(), tw, check=False)
+    assert native == restated.to_bytes()
