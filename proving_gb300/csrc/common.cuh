@@ -18,6 +18,10 @@ void set_error(const char* fmt, ...);
 // Counts kernel launches made by this library (reported by cs_kernel_launch_count).
 void note_launch();
 cs_status from_cuda(cudaError_t e, const char* what);
+// cudaMallocAsync from the device's default pool, which first (once per device) is set to keep
+// the memory freed back to it instead of returning it to the driver at every synchronisation:
+// the scratch and proof buffers of one call are reused by the next without remapping.
+cudaError_t stream_alloc(void** ptr, size_t bytes, cudaStream_t st);
 
 inline cudaStream_t to_stream(cs_stream s) { return reinterpret_cast<cudaStream_t>(s); }
 

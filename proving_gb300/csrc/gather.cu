@@ -49,7 +49,7 @@ extern "C" cs_status cs_gather_u32(const uint32_t* const* h_table, const uint64_
   std::memcpy(host.data() + table_bytes + req_bytes, h_index, req_bytes);
   cudaStream_t st = to_stream(stream);
   uint8_t* dev = nullptr;
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dev), in_bytes + req_bytes, st));
+  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&dev), in_bytes + req_bytes, st));
   cudaError_t e = cudaMemcpyAsync(dev, host.data(), in_bytes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     const uint32_t blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;

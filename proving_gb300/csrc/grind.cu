@@ -93,7 +93,7 @@ extern "C" cs_status cs_grind_blake2s(const uint8_t digest[32], uint32_t pow_bit
   CS_CHECK_ARG(pow_bits <= 32, "grind: pow_bits %u > 32 is not supported", pow_bits);
   cudaStream_t st = to_stream(stream);
   unsigned long long* d_best = nullptr;
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_best), sizeof(unsigned long long), st));
+  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&d_best), sizeof(unsigned long long), st));
   cs_status s = grind_with_slot(digest, pow_bits, max_nonce, nonce_out, d_best, st);
   cudaError_t e = cudaFreeAsync(d_best, st);
   if (s == CS_OK && e != cudaSuccess) return from_cuda(e, "cudaFreeAsync");

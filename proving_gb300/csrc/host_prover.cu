@@ -203,7 +203,7 @@ struct Arena {
   explicit Arena(cudaStream_t s) : st(s) {}
   uint32_t* alloc(size_t words) {
     void* p = nullptr;
-    if (cudaMallocAsync(&p, std::max<size_t>(4, 4 * words), st) != cudaSuccess) {
+    if (stream_alloc(&p, std::max<size_t>(4, 4 * words), st) != cudaSuccess) {
       status = CS_ERR_OOM;
       return nullptr;
     }

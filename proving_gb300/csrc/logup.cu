@@ -352,7 +352,7 @@ cs_status scan_columns(const uint32_t* const* values, const Q4* outs, const uint
   for (uint32_t i = 0; i < n; i++)
     if (log_sizes[i] > kSmallLog) all_runs += (1ull << (log_sizes[i] - 5)) + 32;
   uint32_t* runs = nullptr;
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&runs), sizeof(uint32_t) * 4 * std::max<uint64_t>(1, all_runs), st));
+  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&runs), sizeof(uint32_t) * 4 * std::max<uint64_t>(1, all_runs), st));
   cs_status result = CS_OK;
   uint64_t run_base = 0;
   for (uint32_t b0 = 0; b0 < n && result == CS_OK; b0 += kSumBatch) {
@@ -477,7 +477,7 @@ cpoint lookup_point_at(uint32_t idx) {
 
 cs_status logup_finalize_last(Q4 col, uint32_t log_size, uint32_t claimed_sum_out[4], cudaStream_t st) {
   uint32_t* d_claimed = nullptr;
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_claimed), sizeof(uint32_t) * 4, st));
+  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&d_claimed), sizeof(uint32_t) * 4, st));
   cs_status result = scan_columns(nullptr, &col, &log_size, 1, qm31_make(0, 0, 0, 0), d_claimed, st);
   if (result == CS_OK) {
     cudaError_t e = cudaMemcpyAsync(claimed_sum_out, d_claimed, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st);
@@ -505,7 +505,7 @@ extern "C" cs_status cs_logup_running_sum(const uint32_t* d_values, uint32_t log
   }
   cudaStream_t st = to_stream(stream);
   uint32_t* d_claimed = nullptr;
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_claimed), sizeof(uint32_t) * 4, st));
+  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&d_claimed), sizeof(uint32_t) * 4, st));
   cs_status result = scan_columns(&d_values, &out, &log_size, 1, qm31_make(z[0], z[1], z[2], z[3]), d_claimed, st);
   if (result == CS_OK) {
     cudaError_t e = cudaMemcpyAsync(claimed_sum_out, d_claimed, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st);

@@ -153,7 +153,7 @@ cs_status merkle_leaves(const uint32_t* const* cols, const uint32_t* log_sizes, 
     uint32_t max_level = 0;
     for (const Run& r : runs) max_level = std::max(max_level, r.level);
     half = (size_t)8 << max_level;
-    CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&states), sizeof(uint32_t) * 2 * half, st));
+    CS_CUDA(stream_alloc(reinterpret_cast<void**>(&states), sizeof(uint32_t) * 2 * half, st));
   }
   cs_status result = CS_OK;
   const uint32_t* prev_state = nullptr;

@@ -565,7 +565,7 @@ extern "C" cs_status cs_barycentric_eval(const uint32_t* const* h_cols, uint32_t
     const uint32_t n_chunks = ((1u << log_size) + kBaryChunk - 1) / kBaryChunk;
     cudaStream_t st = to_stream(stream);
     unsigned long long* partial = nullptr;
-    CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&partial), sizeof(unsigned long long) * 4 * nb * n_chunks, st));
+    CS_CUDA(stream_alloc(reinterpret_cast<void**>(&partial), sizeof(unsigned long long) * 4 * nb * n_chunks, st));
     bary_partial_kernel<<<dim3(n_chunks, (nb + kBaryGroup - 1) / kBaryGroup), kBaryThreads, 0, st>>>(
         cols, nb, log_size, w, partial);
     note_launch();
@@ -697,7 +697,7 @@ extern "C" cs_status cs_decompose(const uint32_t* const h_src[4], uint32_t log_s
     out.c[k] = h_dst[k];
   }
   uint32_t* d_sums = nullptr;
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_sums), 8 * sizeof(uint32_t), st));
+  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&d_sums), 8 * sizeof(uint32_t), st));
   half_sums_kernel<<<2, 512, 0, st>>>(in, log_size, d_sums);
   note_launch();
   uint32_t sums[8];

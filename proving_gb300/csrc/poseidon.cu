@@ -491,7 +491,7 @@ extern "C" cs_status cs_poseidon_composition(const uint32_t* const* h_trace, con
   }
   cudaStream_t st = to_stream(stream);
   uint4* d_rc = nullptr;
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_rc), sizeof(uint4) * kConstraints, st));
+  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&d_rc), sizeof(uint4) * kConstraints, st));
   cudaError_t e = cudaMemcpyAsync(d_rc, h_rc, sizeof(uint4) * kConstraints, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     const uint32_t n = 1u << eval_log;

@@ -189,7 +189,7 @@ extern "C" cs_status cs_rtc_air_composition(void* handle, const uint32_t* const*
   }
   cudaStream_t st = to_stream(stream);
   uint32_t* dev = nullptr;
-  CS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dev), sizeof(uint32_t) * n_words, st));
+  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&dev), sizeof(uint32_t) * n_words, st));
   cs_status result = CS_OK;
   cudaError_t e = cudaMemcpyAsync(dev, host.data(), sizeof(uint32_t) * n_words, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {

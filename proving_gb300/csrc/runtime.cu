@@ -1,5 +1,7 @@
 // Runtime part of the C ABI: error reporting, device memory and copies.
 #include <atomic>
+#include <cstdint>
+#include <mutex>
 #include <cstdarg>
 #include <cstdio>
 #include <string>
@@ -14,6 +16,26 @@ std::atomic<uint64_t> g_launches{0};
 }
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+cudaError_t stream_alloc(void** ptr, size_t bytes, cudaStream_t st) {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64) {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!done[dev]) {
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+      done[dev] = true;
+    }
+  }
+  return cudaMallocAsync(ptr, bytes, st);
+}
 
 void set_error(const char* fmt, ...) {
   char buf[512];

@@ -19,8 +19,8 @@ Two forms:
 
 `plain=True` gives the plain form: one launch per column for the per-column
 stages (prover.PlainGpuOps), orchestrated by the restated prover. Otherwise the
-process workers prove Wide-Fibonacci requests with the native prover
-(cs_prove_wide_fib), whose bytes are the same.
+process workers prove requests with the native prover (cs_prove_wide_fib,
+cs_prove_poseidon), whose bytes are the same.
 """
 from __future__ import annotations
 
@@ -93,11 +93,16 @@ def twiddle_domain(max_log_n_rows: int) -> int:
 
 def prove_request(ops, twiddles, req: ProofRequest, native: bool = False):
     """One proof on the current CUDA stream: the trace generated on the device from the request's
-    seed, then the restated prover, or for a Wide-Fibonacci request with native=True the native
-    prover (cs_prove_wide_fib, the same bytes; returned as bytes)."""
+    seed, then the restated prover, or with native=True the native prover (cs_prove_wide_fib /
+    cs_prove_poseidon, the same bytes; returned as bytes)."""
     from .backend import BaseColumn, CudaBackend
     if req.kind == "poseidon":
         from . import poseidon as ps
+        if native:
+            fp = fri_params()
+            return CudaBackend.prove_poseidon_native(
+                req.log_n_rows, (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound, fp.n_queries),
+                twiddles)
         cfg = ps.poseidon_pcs_config(req.log_n_rows + 3, fri_params())
         # the reference's own sanity check fails for this AIR (lifted protocol): check=False
         return ps.prove_poseidon(ops, req.log_n_rows, cfg, pr.Blake2sChannel(), twiddles, check=False)
