@@ -332,6 +332,55 @@ cs_status cs_logup_compositions(uint32_t n_comp, const uint32_t *const *h_values
                                 const uint32_t *claimed_sums, const uint32_t *rcs, uint32_t *const h_accum[4],
                                 cs_stream stream);
 
+/* ------------------------------------------------- GKR lookups (GkrOps, MleOps) */
+
+/* The backend's GkrOps and MleOps (crates/stwo/src/prover/lookups/gkr_prover.rs:22-42,
+   crates/stwo/src/prover/lookups/mle.rs:9-14). A multilinear extension of n
+   variables is its 2^n values on the boolean hypercube (variable j = index bit
+   n-1-j): a secure MLE is 4 coordinate columns, a base MLE one column. Layer
+   kinds follow gkr_prover.rs Layer: a grand-product layer is one secure column,
+   passed as the denominators; LogUp layers have numerators (secure, base for
+   multiplicities, none for singles, whose numerators are all 1) and secure
+   denominators. Input columns of next_layer and sum_as_poly are 8-byte aligned. */
+enum {
+  CS_GKR_GRAND_PRODUCT = 0,
+  CS_GKR_LOGUP_GENERIC = 1,
+  CS_GKR_LOGUP_MULTIPLICITIES = 2,
+  CS_GKR_LOGUP_SINGLES = 3
+};
+
+/* GkrOps::gen_eq_evals: h_out[k][i] = coordinate k of v * eq(x, y) for the
+   2^n_y points x of the hypercube (n_y <= 28; y is n_y QM31 values of 4 host
+   words each, v 4 host words). */
+cs_status cs_gkr_gen_eq_evals(const uint32_t *h_y, uint32_t n_y, const uint32_t h_v[4], uint32_t *const h_out[4],
+                              cs_stream stream);
+
+/* MleOps::fix_first_variable for a base (src_is_base != 0: h_src[0] only) or
+   secure MLE of 2^log_n values: the 2^(log_n - 1) secure values
+   a * (rhs - lhs) + lhs of the two halves. h_dst may alias h_src. */
+cs_status cs_mle_fix_first_variable(const uint32_t *const h_src[4], uint32_t src_is_base, uint32_t log_n,
+                                    const uint32_t h_assignment[4], uint32_t *const h_dst[4], cs_stream stream);
+
+/* GkrOps::next_layer for an input layer of 2^log_n values per column
+   (log_n >= 1): a grand-product layer gives the pairwise products in
+   h_out_den; a LogUp layer gives the pairwise fraction sums as a generic
+   LogUp layer (h_out_num, h_out_den). */
+cs_status cs_gkr_next_layer(uint32_t kind, const uint32_t *const h_num[4], const uint32_t *const h_den[4],
+                            uint32_t log_n, uint32_t *const h_out_num[4], uint32_t *const h_out_den[4],
+                            cs_stream stream);
+
+/* The device sums of GkrOps::sum_as_poly_in_first_variable for the oracle
+   whose input layer has 2^log_n values per column (log_n >= 2): with
+   n_terms = 2^(log_n - 2), sum over i < n_terms of eq[i] times the gate's
+   output on the input layer at t = 0 and t = 2 (LogUp gates combined as
+   numerator + lambda * denominator), written as 8 words (f(0), f(2)) to
+   device memory d_out. The eq column holds at least n_terms values. The host
+   applies eq_fixed_var_correction and correct_sum_as_poly_in_first_variable.
+   Uses stream-ordered device scratch. */
+cs_status cs_gkr_sum_as_poly(uint32_t kind, const uint32_t *const h_eq[4], const uint32_t *const h_num[4],
+                             const uint32_t *const h_den[4], uint32_t log_n, const uint32_t h_lambda[4], uint32_t *d_out,
+                             cs_stream stream);
+
 /* ------------------------------------------------- native Wide-Fibonacci prover */
 
 /* The whole proof of Wide-Fibonacci components (the generic prover's loop,

@@ -88,6 +88,27 @@ def test_invalid_arguments_are_rejected_on_host(lib):
     assert b"coordinate" in lib.cs_last_error()
 
 
+def test_gkr_arguments_are_checked_on_host(lib):
+    INVALID = 1
+    null = ctypes.c_void_p(0)
+    q = (ctypes.c_uint32 * 4)(1, 2, 3, 4)
+    cols = (ctypes.c_void_p * 4)(*[1 << (22 + k) for k in range(4)])
+    ys = (ctypes.c_uint32 * (4 * 29))()
+    # more eq variables than the kernel's parameter block holds
+    assert _status(lib, "cs_gkr_gen_eq_evals", ys, 29, q, cols, null) == INVALID
+    # unknown layer kind, a layer of one value, a misaligned column
+    assert _status(lib, "cs_gkr_next_layer", 4, cols, cols, 5, cols, cols, null) == INVALID
+    assert _status(lib, "cs_gkr_next_layer", 1, cols, cols, 0, cols, cols, null) == INVALID
+    odd = (ctypes.c_void_p * 4)((1 << 22) + 4, 1 << 23, 1 << 24, 1 << 25)
+    assert _status(lib, "cs_gkr_next_layer", 0, null, odd, 5, null, cols, null) == INVALID
+    assert b"aligned" in lib.cs_last_error()
+    # a generic LogUp layer needs its numerators
+    assert _status(lib, "cs_gkr_next_layer", 1, null, cols, 5, cols, cols, null) == INVALID
+    # the sum-check sums need an input layer of at least 4 values
+    assert _status(lib, "cs_gkr_sum_as_poly", 0, cols, null, cols, 1, q, ctypes.c_void_p(1 << 30), null) == INVALID
+    assert _status(lib, "cs_mle_fix_first_variable", cols, 0, 0, q, cols, null) == INVALID
+
+
 def test_error_raises_in_python_mirror(lib):
     with pytest.raises(_lib.CudaBackendError) as e:
         _lib.call("cs_bit_reverse_m31", ctypes.c_void_p(0), 4, ctypes.c_void_p(0))
