@@ -161,6 +161,7 @@ class CommitStage:
         for lay in self.fri_layers:
             self.fri_tabs.append((vp * 4)(*[lay[k].data_ptr() for k in range(4)]))
         self.alpha_tabs = [(ctypes.c_uint32 * 4)(*[int(x) for x in a]) for a in self.alphas]
+        self.line_alphas = (ctypes.c_uint32 * (4 * (FRI_LOG - 1)))(*[int(x) for a in self.alphas[1:] for x in a])
         self.layer_ptr = []
         off = 0
         for k in range(LOG_EXT, -1, -1):
@@ -192,9 +193,9 @@ class CommitStage:
         rec(4)
         call("cs_fold_circle_into_line", fri_src, FRI_LOG, self.alpha_tabs[0], self.fri_tabs[1],
              self.itw.data_ptr(), self.tw_log, st)
-        for j in range(1, FRI_LOG):
-            call("cs_fold_line", self.fri_tabs[j], FRI_LOG - j, self.alpha_tabs[j], self.fri_tabs[j + 1],
-                 self.itw.data_ptr(), self.tw_log, st)
+        # FriOps::fold_line with the 21 remaining challenges: one call, the folds staged in shared memory
+        call("cs_fold_line_steps", self.fri_tabs[1], FRI_LOG - 1, FRI_LOG - 1, self.line_alphas,
+             self.fri_tabs[FRI_LOG], self.itw.data_ptr(), self.tw_log, st)
         rec(5)
 
     def root(self) -> bytes:
@@ -295,7 +296,8 @@ def batched_vs_plain(torch, cs, steps: int = 5, warmup: int = 2):
     graph = torch.cuda.CUDAGraph()
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(s):
+    from proving_gb300.serving import collector_paused
+    with torch.cuda.stream(s), collector_paused():
         mixed.step()
         torch.cuda.synchronize()
         with torch.cuda.graph(graph, stream=s):
@@ -724,6 +726,7 @@ def run_gpu(args):
     leaf_gbs = leaf_bytes / (leaf_ms / 1e3) / 1e9
     leaf_comp = (1 << LOG_EXT) * ((N_COLS * 4 + 63) // 64)
     traffic = LEAVES_TRAFFIC_BYTES if default_shape else None
+    fold_bytes = 16 * (1 << FRI_LOG) + 16 * (1 << (FRI_LOG - 1)) + 16 * (1 << (FRI_LOG - 1)) + 16
     cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
     ff = lambda x: float(f"{x:.6g}")
     res = {
@@ -749,6 +752,13 @@ def run_gpu(args):
                             "unit": "GB/s", "frac": ff(leaf_gbs / hbm), "traffic": traffic,
                             "algorithmic_bytes_per_launch": leaf_bytes,
                             "note": "Blake2s leaf hashing is integer-pipe bound; see int_pipe"},
+        "fold_roofline": {"bound": "hbm", "kernels": "fold_circle_kernel + fold_line_tile_kernel (3 launches)",
+                          "achieved": ff(fold_bytes / (stage_ms["fri_folds"] / 1e3) / 1e9), "peak": hbm,
+                          "unit": "GB/s", "frac": ff(fold_bytes / (stage_ms["fri_folds"] / 1e3) / 1e9 / hbm),
+                          "algorithmic_bytes": fold_bytes,
+                          "note": "fold_circle_into_line 16 n + 16 n/2 bytes, then fold_line with 21 challenges "
+                                  "16 n/2 + 16 bytes (input read once, last layer written); the FRI column was "
+                                  "last touched a step earlier, so it is read from HBM"},
         "int_pipe": {"kernel": "merkle_leaves_kernel", "compressions_per_launch": leaf_comp,
                      "gcompressions_per_s": ff(leaf_comp / (leaf_ms / 1e3) / 1e9),
                      "int_ops_per_compression": 1120,

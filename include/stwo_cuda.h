@@ -169,11 +169,20 @@ cs_status cs_pack_leaves_input(const uint32_t *const h_in[4], uint32_t log_size,
    evaluation (4 coordinate columns of 2^log_size) on the line domain
    x(half_odds(log_size)) folds to 2^(log_size-1) values
    f0 + alpha * f1 with (f0, f1) = ibutterfly(f(x), f(-x), 1/x). The inverse
-   x-coordinates come from the itwiddle tree. fold_step > 1 calls it with
-   alpha, alpha^2, ... in turn. */
+   x-coordinates come from the itwiddle tree. */
 cs_status cs_fold_line(const uint32_t *const h_src[4], uint32_t log_size, const uint32_t alpha[4],
                        uint32_t *const h_dst[4], const uint32_t *d_itwiddles, uint32_t twiddle_log_size,
                        cs_stream stream);
+
+/* FriOps::fold_line with n_alphas challenges (crates/stwo/src/prover/fri.rs:27-45):
+   the evaluation folded n_alphas times (1 <= n_alphas <= log_size), fold j
+   with h_alphas[4 j .. 4 j + 3] (host words), into 2^(log_size - n_alphas)
+   values in h_dst; only the last layer is written. Up to 10 folds per launch
+   on tiles staged in shared memory; uses stream-ordered device scratch between
+   launches. */
+cs_status cs_fold_line_steps(const uint32_t *const h_src[4], uint32_t log_size, uint32_t n_alphas,
+                             const uint32_t *h_alphas, uint32_t *const h_dst[4], const uint32_t *d_itwiddles,
+                             uint32_t twiddle_log_size, cs_stream stream);
 
 /* FriOps::fold_circle_into_line (crates/stwo/src/prover/fri.rs:62-66; CPU
    crates/stwo/src/prover/backend/cpu/fri.rs:94-116; SIMD

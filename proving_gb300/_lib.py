@@ -66,6 +66,7 @@ SIGNATURES = {
     "cs_fft_set_plan": [u32, u32, u32, vp, u32],
     "cs_fft_get_plan": [u32, u32, u32, vp, vp],
     "cs_fold_line_device_alpha": [vp, u32, vp, vp, vp, u32, vp],
+    "cs_fold_line_steps": [vp, u32, u32, vp, vp, vp, u32, vp],
     "cs_fold_circle_into_line_device_alpha": [vp, u32, vp, vp, vp, u32, vp],
     "cs_channel_mix_root": [vp, vp, vp],
     "cs_channel_draw_secure_felt": [vp, vp, vp],

@@ -265,17 +265,18 @@ class CudaBackend:
     # FriOps -------------------------------------------------------------------
     @staticmethod
     def fold_line(values: SecureColumnByCoords, alphas, twiddles: TwiddleTree) -> SecureColumnByCoords:
-        """fold_line on the line domain x(half_odds(log n)); alphas as in FriOps::fold_line."""
-        cur = values
-        for alpha in alphas:
-            n = len(cur)
-            dst = SecureColumnByCoords.uninitialized(n // 2)
-            a = _u32_table(alpha)
-            _lib.call("cs_fold_line", _ptr_table([c.data for c in cur.columns]), n.bit_length() - 1, a,
-                      _ptr_table([c.data for c in dst.columns]), _ptr(twiddles.itwiddles), twiddles.log_size,
-                      _stream())
-            cur = dst
-        return cur
+        """fold_line on the line domain x(half_odds(log n)); alphas as in FriOps::fold_line: one
+        fold per challenge, only the last layer returned."""
+        alphas = [tuple(a) for a in alphas]
+        if not alphas:
+            raise ValueError("fold_line needs at least one challenge")
+        n = len(values)
+        dst = SecureColumnByCoords.uninitialized(n >> len(alphas))
+        words = _u32_table([w for a in alphas for w in a])
+        _lib.call("cs_fold_line_steps", _ptr_table([c.data for c in values.columns]), n.bit_length() - 1,
+                  len(alphas), words, _ptr_table([c.data for c in dst.columns]), _ptr(twiddles.itwiddles),
+                  twiddles.log_size, _stream())
+        return dst
 
     @staticmethod
     def fold_line_device_alpha(values: SecureColumnByCoords, d_alpha: torch.Tensor,

@@ -1342,12 +1342,23 @@ class GpuOps:
         return out
 
     def _capture_fri(self, channel, fp, column, log_size, tw):
+        """Captures the layer loop. Python's collector is paused while the capture is open: a
+        collection there could destroy an evicted graph caught in a reference cycle, and the
+        release of its memory pool would end the capture (torch.cuda.graph collects once
+        before the capture begins)."""
+        import gc
         import torch
         static_in = self.be.SecureColumnByCoords.uninitialized(len(column))
         ch = DeviceFriChannel(self, channel)
         graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(graph):
-            out = fri_layers(self, ch, fp, static_in, log_size, tw)
+        was_enabled = gc.isenabled()
+        gc.disable()
+        try:
+            with torch.cuda.graph(graph):
+                out = fri_layers(self, ch, fp, static_in, log_size, tw)
+        finally:
+            if was_enabled:
+                gc.enable()
         return graph, static_in, ch, out
 
 

@@ -202,6 +202,44 @@ def test_fri_fold_chain_22(B):
     assert len(g) == 1
 
 
+@pytest.mark.parametrize("log_n,k", [(1, 1), (3, 3), (4, 2), (10, 10), (11, 11), (12, 3), (15, 1),
+                                     (20, 13), (21, 10), (21, 20), (21, 21)])
+def test_fold_line_with_several_alphas(B, log_n, k):
+    # FriOps::fold_line with k challenges (one launch per 10 folds, tiles in shared memory)
+    # equals k single folds of the oracle; only the last layer is returned.
+    from proving_gb300.backend import SecureColumnByCoords
+    tree = _tree(B, log_n + 1)
+    coords = qm31_column(300 + log_n, log_n)
+    alphas = [seeded_qm31(2000 + 31 * log_n + j) for j in range(k)]
+    got = B.fold_line(SecureColumnByCoords.from_cpu(coords), alphas, tree)
+    assert len(got) == 1 << (log_n - k)
+    w, init = coords, O.line_domain_initial_index(log_n)
+    for a in alphas:
+        w = O.fold_line(w, init, a)
+        init = O.double_index(init)
+    assert all(np.array_equal(a, b) for a, b in zip(got.to_cpu(), w))
+
+
+def test_fold_line_unaligned_source_takes_scalar_loads(B):
+    # coordinates offset by 8 bytes (not 16): the tile kernel stages them with 4-byte loads
+    import torch
+    from proving_gb300.backend import BaseColumn, SecureColumnByCoords
+    log_n = 9
+    tree = _tree(B, log_n + 1)
+    coords = qm31_column(77, log_n)
+    block = torch.zeros((4, (1 << log_n) + 2), dtype=torch.int32, device="cuda")
+    for c in range(4):
+        block[c, 2:] = torch.from_numpy(np.asarray(coords[c], np.uint32).view(np.int32)).cuda()
+    src = SecureColumnByCoords([BaseColumn(block[c, 2:]) for c in range(4)])
+    alphas = [seeded_qm31(5000 + j) for j in range(4)]
+    got = B.fold_line(src, alphas, tree).to_cpu()
+    w, init = coords, O.line_domain_initial_index(log_n)
+    for a in alphas:
+        w = O.fold_line(w, init, a)
+        init = O.double_index(init)
+    assert all(np.array_equal(a, b) for a, b in zip(got, w))
+
+
 # ------------------------------------------------------------------ grind
 
 def test_grind_pow_kat(B):
