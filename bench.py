@@ -588,7 +588,8 @@ def run_gpu(args):
 
     # the FFT pass plans for this workload's two shapes, picked by the autotuner before timing
     from proving_gb300 import autotune
-    tuned = autotune.tune([(True, LOG_ROWS, LOG_ROWS), (False, LOG_EXT, LOG_ROWS)], n_cols=N_COLS)
+    tuned = {} if args.skip_autotune else autotune.tune([(True, LOG_ROWS, LOG_ROWS), (False, LOG_EXT, LOG_ROWS)],
+                                                        n_cols=N_COLS)
     fft_plans = {f"{'interpolate' if inv else 'evaluate'} 2^{log_n} ({n} layers)":
                  {"default": list(r["default"]), "best": list(r["best"]),
                   "default_ms": round(r["ms"][tuple(r["default"])], 4), "best_ms": round(r["ms"][r["best"]], 4),
@@ -708,6 +709,7 @@ def run_gpu(args):
     with collector_paused():
         poseidon_res = poseidon_prove_leg(torch, args.poseidon_log_rows) if not args.skip_poseidon else None
         mixed_res = mixed_prove_leg(torch) if not args.skip_mixed_prove else None
+    gkr_res = gkr_leg(torch) if not args.skip_gkr else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -783,6 +785,7 @@ def run_gpu(args):
         "serving": serving_res,
         "poseidon_prove": poseidon_res,
         "mixed_prove": mixed_res,
+        "gkr": gkr_res,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
@@ -906,12 +909,86 @@ def case_mixed_kernels(torch):
     return {"case": "mixed-kernels", "ok": True}
 
 
+def gkr_leg(torch, log_logup: int = 22, log_gp: int = 20, n_proofs: int = 3, kernel_log: int = 24):
+    """GKR lookups (GkrOps / MleOps, crates/stwo/src/prover/lookups/): a batch proof of a generic
+    LogUp instance of 2^log_logup fractions and a grand product of 2^log_gp values (seeded inputs on
+    the device), and the streaming kernels alone at 2^kernel_log values (larger than L2) against
+    HBM. Algorithmic bytes: next_layer reads 2 x 16 B and writes 2 x 16 B per output pair
+    (numerators and denominators); fix_first_variable reads 2 x 16 B and writes 16 B per output;
+    the sum-check sums read 4 x 16 B per term from each of the two columns plus 16 B of eq."""
+    from proving_gb300 import gkr as G
+    from proving_gb300 import prover as pr
+    from proving_gb300.serving import collector_paused
+    P = (1 << 31) - 1
+    dev = G.DeviceGkrOps()
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    rnd = lambda n: torch.randint(0, P, (4, n), dtype=torch.int32, device="cuda", generator=gen)
+    layers = [G.Layer(G.LOGUP_GENERIC, [G.Mle(rnd(1 << log_logup), log_logup), G.Mle(rnd(1 << log_logup), log_logup)]),
+              G.Layer(G.GRAND_PRODUCT, [G.Mle(rnd(1 << log_gp), log_gp)])]
+    lat, lat_native = [], []
+    with collector_paused():
+        for i in range(n_proofs + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            proof, _ = G.prove_batch(dev, pr.Blake2sChannel(), layers)
+            torch.cuda.synchronize()
+            if i:
+                lat.append((time.perf_counter() - t0) * 1e3)
+        for i in range(n_proofs + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            native, _ = G.prove_batch_native(pr.Blake2sChannel(), layers)
+            torch.cuda.synchronize()
+            if i:
+                lat_native.append((time.perf_counter() - t0) * 1e3)
+    same = (native.sumcheck_proofs == proof.sumcheck_proofs
+            and native.output_claims_by_instance == proof.output_claims_by_instance)
+    n = 1 << kernel_log
+    num, den = G.Mle(rnd(n), kernel_log), G.Mle(rnd(n), kernel_log)
+    lay = G.Layer(G.LOGUP_GENERIC, [num, den])
+    eqm = G.Mle(rnd(n // 4), kernel_log - 2)
+    lam = (1, 2, 3, 4)
+    hbm, _ = peaks()
+
+    def timed(fn, reps=10):
+        fn()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(reps):
+            fn()
+        e.record()
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) / reps
+
+    kernels = {}
+    for name, fn, nbytes in (("next_layer", lambda: dev.next_layer(lay), 32 * n + 16 * n),
+                             ("fix_first_variable", lambda: dev.fix_first_variable(den, lam), 16 * n + 8 * n),
+                             ("sum_as_poly", lambda: dev.sum_as_poly_evals([(lay, eqm, lam)]), 32 * n + 4 * n),
+                             ("gen_eq_evals", lambda: dev.gen_eq_evals([(i, 1, 2, 3) for i in range(kernel_log)], lam),
+                              16 * n)):
+        ms = timed(fn)
+        gbs = nbytes / (ms / 1e3) / 1e9
+        kernels[name] = {"ms": round(ms, 4), "gb_per_s": round(gbs, 1), "frac_of_hbm": round(gbs / hbm, 3)}
+    return {"workload": f"GKR batch proof: generic LogUp 2^{log_logup} + grand product 2^{log_gp} (secure values); "
+                        f"kernels alone at 2^{kernel_log} values",
+            "layers": log_logup, "sumcheck_rounds": log_logup * (log_logup - 1) // 2,
+            "native_prove_p50_ms": round(float(np.percentile(lat_native, 50)), 3),
+            "prove_p50_ms": round(float(np.percentile(lat, 50)), 3), "prove_max_ms": round(max(lat), 3),
+            "native_equals_driver": bool(same),
+            "kernels": kernels,
+            "note": "prove_p50_ms: the protocol in Python over the device ops (proving_gb300.gkr.prove_batch); "
+                    "native_prove_p50_ms: the protocol in C++ (cs_gkr_prove_batch), one read-back per round"}
+
+
 def run_case(args):
     import torch
     from proving_gb300 import build as cuda_build
     cuda_build.build()
     if args.case == "mixed-kernels":
         res = case_mixed_kernels(torch)
+    elif args.case == "gkr":
+        res = gkr_leg(torch, log_logup=args.gkr_log, log_gp=max(args.gkr_log - 2, 2), n_proofs=1,
+                      kernel_log=args.gkr_log)
     else:  # one mixed-size proof after one warm-up proof, batched arm only
         res = mixed_prove_leg(torch, n_proofs=1, arms=("batched",))
     print(json.dumps(res))
@@ -933,7 +1010,11 @@ def main():
     ap.add_argument("--skip-poseidon", action="store_true", help="skip the Poseidon2 prove leg")
     ap.add_argument("--poseidon-log-rows", type=int, default=18, help="log2 rows of the Poseidon2 prove leg")
     ap.add_argument("--skip-mixed-prove", action="store_true", help="skip the mixed-size full-proof leg")
-    ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove"],
+    ap.add_argument("--skip-gkr", action="store_true", help="skip the GKR lookup leg")
+    ap.add_argument("--skip-autotune", action="store_true",
+                    help="keep the default FFT pass plans (no candidate sweep before timing; for profiling)")
+    ap.add_argument("--gkr-log", type=int, default=22, help="log2 values of the --case gkr instance")
+    ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove", "gkr"],
                     help="run one small profiling case instead of the benchmark (for ncu)")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)

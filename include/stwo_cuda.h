@@ -390,6 +390,27 @@ cs_status cs_gkr_sum_as_poly(uint32_t kind, const uint32_t *const h_eq[4], const
                              const uint32_t *const h_den[4], uint32_t log_n, const uint32_t h_lambda[4], uint32_t *d_out,
                              cs_stream stream);
 
+/* GKR batch proof (prove_batch, crates/stwo/src/prover/lookups/gkr_prover.rs,
+   with sumcheck::prove_batch, crates/stwo/src/prover/lookups/sumcheck.rs) with
+   the protocol in native code over the kernels above. Instance i has layer
+   kind h_kinds[i], h_n_variables[i] variables (1..29) and columns
+   h_columns[8 i .. 8 i + 7]: the numerators' 4 coordinates (generic LogUp; the
+   first only for multiplicities; unused otherwise), then the 4 coordinates of
+   the denominators or of the grand-product column. The input columns are read,
+   not changed. h_channel is the Blake2s channel state (8 digest words, then the
+   draw counter), updated on return. The words written (one u64 each):
+     proof:    n_layers, per layer: n_rounds, per round: n_coeffs, coeffs;
+               n_instances, per instance: n_masks, per mask: n_columns, per
+               column: v0, v1; per instance: n_output_claims, claims;
+     artifact: n_ood, ood point; per instance: n_claims, claims to verify;
+               per instance: n_variables,
+   each QM31 as its 4 coordinates. With h_words null only *n_words is set.
+   Uses stream-ordered device scratch; synchronises the stream once per
+   sum-check round. */
+cs_status cs_gkr_prove_batch(uint32_t n_instances, const uint32_t *h_kinds, const uint32_t *h_n_variables,
+                             const uint32_t *const *h_columns, uint32_t h_channel[9], uint64_t *h_words,
+                             size_t capacity, size_t *n_words, cs_stream stream);
+
 /* ------------------------------------------------- native Wide-Fibonacci prover */
 
 /* The whole proof of Wide-Fibonacci components (the generic prover's loop,

@@ -75,6 +75,7 @@ SIGNATURES = {
     "cs_mle_fix_first_variable": [vp, u32, u32, vp, vp, vp],
     "cs_gkr_next_layer": [u32, vp, vp, u32, vp, vp, vp],
     "cs_gkr_sum_as_poly": [u32, vp, vp, vp, u32, vp, vp, vp],
+    "cs_gkr_prove_batch": [u32, vp, vp, vp, vp, vp, sz, ctypes.POINTER(sz), vp],
     "cs_rtc_available": [],
     "cs_rtc_compile_air": [vp, u32, vp, vp, u32, u32, u32, vp, vp, ctypes.c_size_t],
     "cs_rtc_air_composition": [vp, vp, vp, vp, u32, u32, vp, vp],

@@ -1277,3 +1277,461 @@ extern "C" cs_status cs_prove_poseidon(uint32_t log_n_rows, const cs_wide_fib_pr
   if (s != CS_OK) return s;
   return finish(words, h_words, capacity, n_words);
 }
+
+// ---------------------------------------------------------------- GKR batch prover
+// prove_batch (crates/stwo/src/prover/lookups/gkr_prover.rs) and its sum-check
+// (crates/stwo/src/prover/lookups/sumcheck.rs) in native code over this library's
+// GkrOps / MleOps kernels: per sum-check round the device sums of every active
+// instance are read back once, the round polynomials and the channel run here,
+// and the variable is fixed on the device. The values equal
+// proving_gb300.gkr.prove_batch's.
+
+namespace cs {
+namespace hp {
+namespace {
+
+// One column of a GKR layer: 4 coordinate pointers, or one for base values.
+struct GCol {
+  const uint32_t* c[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool base = false;
+  uint32_t* owned = nullptr;  // the allocation holding the coordinates, when this driver made it
+};
+struct GLayer {
+  uint32_t kind = CS_GKR_GRAND_PRODUCT;
+  uint32_t n_vars = 0;
+  GCol num, den;  // a grand product keeps its column in den
+};
+
+const qm31 kOne = qm31_make(1, 0, 0, 0);
+const qm31 kZero = qm31_make(0, 0, 0, 0);
+
+bool q_eq(const qm31& a, const qm31& b) { return a.a.a == b.a.a && a.a.b == b.a.b && a.b.a == b.b.a && a.b.b == b.b.b; }
+bool q_zero(const qm31& a) { return q_eq(a, kZero); }
+
+qm31 eq1(const qm31& x, const qm31& y) {  // eq for one variable (utils.rs eq)
+  return qm31_add(qm31_mul(x, y), qm31_mul(qm31_sub(kOne, x), qm31_sub(kOne, y)));
+}
+
+// inverses of nonzero values with one inversion; false when one is zero
+bool batch_inverse(std::vector<qm31>& xs) {
+  std::vector<qm31> pre(xs.size());
+  qm31 acc = kOne;
+  for (size_t i = 0; i < xs.size(); i++) {
+    if (q_zero(xs[i])) return false;
+    pre[i] = acc;
+    acc = qm31_mul(acc, xs[i]);
+  }
+  qm31 inv = qm31_inv(acc);
+  for (size_t i = xs.size(); i-- > 0;) {
+    const qm31 x = xs[i];
+    xs[i] = qm31_mul(inv, pre[i]);
+    inv = qm31_mul(inv, x);
+  }
+  return true;
+}
+
+using Poly = std::vector<qm31>;
+
+Poly poly_trim(Poly p) {
+  while (!p.empty() && q_zero(p.back())) p.pop_back();
+  return p;
+}
+qm31 poly_eval(const Poly& p, const qm31& x) {
+  qm31 acc = kZero;
+  for (size_t i = p.size(); i-- > 0;) acc = qm31_add(qm31_mul(acc, x), p[i]);
+  return acc;
+}
+
+// correct_sum_as_poly_in_first_variable for every k = 1..|y| (see RoundConstants in
+// proving_gb300/gkr.py): r(t) = (t - b_k) q(t), q through (x, r(x) / (x - b_k)), x = 0, 1, 2.
+struct RoundConstants {
+  std::vector<qm31> a, b, eq0, eq2, i0, i1, i2;  // index k
+  bool ok = true;
+  explicit RoundConstants(const std::vector<qm31>& y) {
+    const size_t n = y.size();
+    a.resize(n + 1), b.resize(n + 1), eq0.resize(n + 1), eq2.resize(n + 1);
+    i0.resize(n + 1), i1.resize(n + 1), i2.resize(n + 1);
+    std::vector<qm31> prefix(n);
+    qm31 acc = kOne;
+    for (size_t i = 0; i < n; i++) prefix[i] = acc = qm31_mul(acc, qm31_sub(kOne, y[i]));
+    std::vector<qm31> inv;
+    for (size_t k = 1; k <= n; k++) inv.push_back(prefix[n - k]);
+    for (size_t k = 1; k <= n; k++) inv.push_back(qm31_sub(kOne, qm31_add(y[n - k], y[n - k])));
+    if (!(ok = batch_inverse(inv))) return;
+    std::vector<qm31> xb;
+    for (size_t k = 1; k <= n; k++) {
+      a[k] = inv[k - 1];
+      b[k] = qm31_mul(qm31_sub(kOne, y[n - k]), inv[n + k - 1]);
+      eq0[k] = eq1(kZero, y[n - k]);
+      eq2[k] = eq1(qm31_make(2, 0, 0, 0), y[n - k]);
+      for (uint32_t x = 0; x < 3; x++) xb.push_back(qm31_sub(qm31_make(x, 0, 0, 0), b[k]));
+    }
+    if (!(ok = batch_inverse(xb))) return;
+    for (size_t k = 1; k <= n; k++) i0[k] = xb[3 * (k - 1)], i1[k] = xb[3 * (k - 1) + 1], i2[k] = xb[3 * (k - 1) + 2];
+  }
+  Poly correct(const qm31& f0, const qm31& f2, const qm31& claim, size_t k) const {
+    const qm31 r0 = qm31_mul(qm31_mul(f0, eq0[k]), a[k]);
+    const qm31 r1 = qm31_sub(claim, r0);
+    const qm31 r2 = qm31_mul(qm31_mul(f2, eq2[k]), a[k]);
+    const qm31 q0 = qm31_mul(r0, i0[k]), q1 = qm31_mul(r1, i1[k]), q2 = qm31_mul(r2, i2[k]);
+    const qm31 c2 = qm31_mul_m31(qm31_add(qm31_sub(q2, qm31_add(q1, q1)), q0), (P + 1) / 2);
+    const qm31 c1 = qm31_sub(qm31_sub(q1, q0), c2);
+    return poly_trim({qm31_neg(qm31_mul(b[k], q0)), qm31_sub(q0, qm31_mul(b[k], c1)), qm31_sub(c1, qm31_mul(b[k], c2)), c2});
+  }
+};
+
+struct Oracle {
+  GLayer layer;  // the input layer, n_vars = oracle variables + 1
+  qm31 corr = kOne;
+  qm31 lambda;
+  uint32_t n_vars() const { return layer.n_vars - 1; }
+};
+
+struct GkrProver {
+  Channel& ch;
+  Arena& ar;
+  cudaStream_t st;
+
+  GCol alloc_secure(uint32_t log_n) {
+    GCol col;
+    uint32_t* p = ar.alloc(4ull << log_n);
+    if (p == nullptr) return col;
+    for (int k = 0; k < 4; k++) col.c[k] = p + ((size_t)k << log_n);
+    col.owned = p;
+    return col;
+  }
+  void drop(GCol& col) {
+    if (col.owned != nullptr) ar.release(col.owned);
+    col.owned = nullptr;
+  }
+  // values 0 .. n-1 of the columns, read back in one synchronisation
+  cs_status read(const std::vector<std::pair<const GCol*, uint32_t>>& reqs, std::vector<std::vector<qm31>>& out) {
+    std::vector<std::vector<uint32_t>> raw(reqs.size());
+    for (size_t r = 0; r < reqs.size(); r++) {
+      const GCol& col = *reqs[r].first;
+      const uint32_t n = reqs[r].second;
+      raw[r].assign(4 * n, 0);
+      for (int k = 0; k < (col.base ? 1 : 4); k++)
+        CS_CUDA(cudaMemcpyAsync(raw[r].data() + k * n, col.c[k], 4 * n, cudaMemcpyDeviceToHost, st));
+    }
+    CS_CUDA(cudaStreamSynchronize(st));
+    out.assign(reqs.size(), {});
+    for (size_t r = 0; r < reqs.size(); r++) {
+      const uint32_t n = reqs[r].second;
+      for (uint32_t i = 0; i < n; i++)
+        out[r].push_back(qm31_make(raw[r][i], raw[r][n + i], raw[r][2 * n + i], raw[r][3 * n + i]));
+    }
+    return CS_OK;
+  }
+  static void tables(const GCol& col, const uint32_t* t[4]) {
+    for (int k = 0; k < 4; k++) t[k] = col.base ? col.c[0] : col.c[k];
+  }
+
+  cs_status next_layer(const GLayer& in, GLayer& out) {
+    out.n_vars = in.n_vars - 1;
+    out.kind = in.kind == CS_GKR_GRAND_PRODUCT ? CS_GKR_GRAND_PRODUCT : CS_GKR_LOGUP_GENERIC;
+    out.den = alloc_secure(out.n_vars);
+    if (out.den.owned == nullptr) return CS_ERR_OOM;
+    uint32_t* od[4] = {const_cast<uint32_t*>(out.den.c[0]), const_cast<uint32_t*>(out.den.c[1]),
+                       const_cast<uint32_t*>(out.den.c[2]), const_cast<uint32_t*>(out.den.c[3])};
+    const uint32_t *n[4], *d[4];
+    tables(in.num, n);
+    tables(in.den, d);
+    if (in.kind == CS_GKR_GRAND_PRODUCT) return cs_gkr_next_layer(in.kind, nullptr, d, in.n_vars, nullptr, od, st);
+    out.num = alloc_secure(out.n_vars);
+    if (out.num.owned == nullptr) return CS_ERR_OOM;
+    uint32_t* on[4] = {const_cast<uint32_t*>(out.num.c[0]), const_cast<uint32_t*>(out.num.c[1]),
+                       const_cast<uint32_t*>(out.num.c[2]), const_cast<uint32_t*>(out.num.c[3])};
+    return cs_gkr_next_layer(in.kind, in.kind == CS_GKR_LOGUP_SINGLES ? nullptr : n, d, in.n_vars, on, od, st);
+  }
+
+  cs_status fix(const GCol& src, uint32_t log_n, const qm31& x, GCol& dst) {
+    dst = alloc_secure(log_n - 1);
+    if (dst.owned == nullptr) return CS_ERR_OOM;
+    const uint32_t* s[4];
+    tables(src, s);
+    uint32_t* d[4] = {const_cast<uint32_t*>(dst.c[0]), const_cast<uint32_t*>(dst.c[1]), const_cast<uint32_t*>(dst.c[2]),
+                      const_cast<uint32_t*>(dst.c[3])};
+    const uint32_t a[4] = {x.a.a, x.a.b, x.b.a, x.b.b};
+    return cs_mle_fix_first_variable(s, src.base ? 1 : 0, log_n, a, d, st);
+  }
+
+  // Oracle::fix_first_variable: the eq correction and every column of the layer
+  cs_status fix_oracle(Oracle& o, const std::vector<qm31>& y, const qm31& x) {
+    const qm31 z0 = y[y.size() - o.n_vars()];
+    o.corr = qm31_mul(o.corr, eq1(x, z0));
+    GLayer next;
+    next.n_vars = o.layer.n_vars - 1;
+    next.kind = o.layer.kind == CS_GKR_LOGUP_MULTIPLICITIES ? CS_GKR_LOGUP_GENERIC : o.layer.kind;
+    if (o.layer.kind == CS_GKR_LOGUP_GENERIC || o.layer.kind == CS_GKR_LOGUP_MULTIPLICITIES)
+      HP_TRY(fix(o.layer.num, o.layer.n_vars, x, next.num));
+    HP_TRY(fix(o.layer.den, o.layer.n_vars, x, next.den));
+    drop(o.layer.num);  // only what an earlier round of this sum-check made
+    drop(o.layer.den);
+    o.layer = next;
+    return CS_OK;
+  }
+
+  cs_status sumcheck(std::vector<qm31> claims, std::vector<Oracle>& oracles, const qm31& lam, const GCol& eq,
+                     const std::vector<qm31>& y, const RoundConstants& rc, std::vector<Poly>& round_polys,
+                     std::vector<qm31>& assignment) {
+    uint32_t n_vars = 0;
+    for (const Oracle& o : oracles) n_vars = std::max(n_vars, o.n_vars());
+    for (size_t i = 0; i < oracles.size(); i++)
+      claims[i] = qm31_mul_m31(claims[i], (uint32_t)((1ull << (n_vars - oracles[i].n_vars())) % P));
+    uint32_t* d_sums = ar.alloc(8 * oracles.size());
+    if (d_sums == nullptr) return CS_ERR_OOM;
+    std::vector<uint32_t> sums(8 * oracles.size());
+    const uint32_t* e[4];
+    tables(eq, e);
+    for (uint32_t rnd = 0; rnd < n_vars; rnd++) {
+      const uint32_t remaining = n_vars - rnd;
+      std::vector<size_t> active;
+      for (size_t i = 0; i < oracles.size(); i++) {
+        if (oracles[i].n_vars() != remaining) continue;
+        const GLayer& L = oracles[i].layer;
+        const uint32_t *n[4], *d[4];
+        tables(L.num, n);
+        tables(L.den, d);
+        const uint32_t l4[4] = {oracles[i].lambda.a.a, oracles[i].lambda.a.b, oracles[i].lambda.b.a,
+                                oracles[i].lambda.b.b};
+        const bool has_num = L.kind == CS_GKR_LOGUP_GENERIC || L.kind == CS_GKR_LOGUP_MULTIPLICITIES;
+        HP_TRY(cs_gkr_sum_as_poly(L.kind, e, has_num ? n : nullptr, d, L.n_vars, l4, d_sums + 8 * active.size(), st));
+        active.push_back(i);
+      }
+      if (!active.empty()) {
+        CS_CUDA(cudaMemcpyAsync(sums.data(), d_sums, 32 * active.size(), cudaMemcpyDeviceToHost, st));
+        CS_CUDA(cudaStreamSynchronize(st));
+      }
+      std::vector<Poly> polys;
+      for (size_t i = 0, j = 0; i < oracles.size(); i++) {
+        Poly p;
+        if (j < active.size() && active[j] == i) {
+          const uint32_t* w = sums.data() + 8 * j++;
+          const qm31 f0 = qm31_mul(qm31_make(w[0], w[1], w[2], w[3]), oracles[i].corr);
+          const qm31 f2 = qm31_mul(qm31_make(w[4], w[5], w[6], w[7]), oracles[i].corr);
+          p = rc.correct(f0, f2, claims[i], oracles[i].n_vars());
+        } else {
+          p = poly_trim({qm31_mul_m31(claims[i], (P + 1) / 2)});
+        }
+        CS_CHECK_ARG(q_eq(qm31_add(poly_eval(p, kZero), poly_eval(p, kOne)), claims[i]) && p.size() <= 4,
+                     "gkr_prove_batch: round polynomial inconsistent with its claim (instance %zu, round %u)", i,
+                     rnd);
+        polys.push_back(p);
+      }
+      Poly comb;  // p_0 + lam p_1 + ..., no trimming
+      for (size_t i = polys.size(); i-- > 0;) {
+        Poly next(std::max(comb.size(), polys[i].size()), kZero);
+        for (size_t t = 0; t < comb.size(); t++) next[t] = qm31_mul(comb[t], lam);
+        for (size_t t = 0; t < polys[i].size(); t++) next[t] = qm31_add(next[t], polys[i][t]);
+        comb = next;
+      }
+      ch.mix_felts(comb);
+      const qm31 x = ch.draw_secure_felt();
+      for (size_t i = 0; i < oracles.size(); i++) claims[i] = poly_eval(polys[i], x);
+      for (size_t i : active) HP_TRY(fix_oracle(oracles[i], y, x));
+      round_polys.push_back(comb);
+      assignment.push_back(x);
+    }
+    ar.release(d_sums);
+    return CS_OK;
+  }
+
+  // prove_batch; the proof and artifact go to `out` in the layout of cs_gkr_prove_batch
+  cs_status prove(const std::vector<GLayer>& inputs, Words& out) {
+    const size_t n_inst = inputs.size();
+    uint32_t n_layers = 0;
+    for (const GLayer& L : inputs) n_layers = std::max(n_layers, L.n_vars);
+    std::vector<std::vector<GLayer>> layers(n_inst);
+    for (size_t i = 0; i < n_inst; i++) {
+      layers[i].push_back(inputs[i]);
+      while (layers[i].back().n_vars > 0) {
+        GLayer next;
+        HP_TRY(next_layer(layers[i].back(), next));
+        layers[i].push_back(next);
+      }
+    }
+    std::vector<int> cursor(n_inst);  // next layer of each instance, from the output layer down
+    for (size_t i = 0; i < n_inst; i++) cursor[i] = (int)inputs[i].n_vars;
+    std::vector<std::vector<Poly>> proofs;
+    std::vector<std::vector<std::vector<std::pair<qm31, qm31>>>> masks(n_inst);
+    std::vector<std::vector<qm31>> outputs(n_inst), claims(n_inst);
+    std::vector<bool> has_claims(n_inst, false);
+    std::vector<qm31> ood;
+    for (uint32_t layer = 0; layer < n_layers; layer++) {
+      const uint32_t remaining = n_layers - layer;
+      for (size_t i = 0; i < n_inst; i++) {
+        if (inputs[i].n_vars != remaining) continue;
+        const GLayer& L = layers[i][cursor[i]--];
+        std::vector<std::vector<qm31>> v;
+        if (L.kind == CS_GKR_GRAND_PRODUCT || L.kind == CS_GKR_LOGUP_SINGLES) {
+          HP_TRY(read({{&L.den, 1}}, v));
+          claims[i] = L.kind == CS_GKR_GRAND_PRODUCT ? std::vector<qm31>{v[0][0]} : std::vector<qm31>{kOne, v[0][0]};
+        } else {
+          HP_TRY(read({{&L.num, 1}, {&L.den, 1}}, v));
+          claims[i] = {v[0][0], v[1][0]};
+        }
+        outputs[i] = claims[i];
+        has_claims[i] = true;
+      }
+      for (size_t i = 0; i < n_inst; i++)
+        if (has_claims[i]) ch.mix_felts(claims[i]);
+      // EqEvals::generate(ood)
+      GCol eq = alloc_secure(ood.empty() ? 0 : (uint32_t)ood.size() - 1);
+      if (eq.owned == nullptr) return CS_ERR_OOM;
+      uint32_t* eqo[4] = {const_cast<uint32_t*>(eq.c[0]), const_cast<uint32_t*>(eq.c[1]), const_cast<uint32_t*>(eq.c[2]),
+                          const_cast<uint32_t*>(eq.c[3])};
+      if (ood.empty()) {
+        const uint32_t one[4] = {1, 0, 0, 0};
+        for (int k = 0; k < 4; k++) CS_CUDA(cudaMemcpyAsync(eqo[k], one + k, 4, cudaMemcpyHostToDevice, st));
+        CS_CUDA(cudaStreamSynchronize(st));  // the host words live on this stack frame
+      } else {
+        std::vector<uint32_t> yw;
+        for (size_t j = 1; j < ood.size(); j++) yw.insert(yw.end(), {ood[j].a.a, ood[j].a.b, ood[j].b.a, ood[j].b.b});
+        const qm31 v = eq1(kZero, ood[0]);
+        const uint32_t v4[4] = {v.a.a, v.a.b, v.b.a, v.b.b};
+        HP_TRY(cs_gkr_gen_eq_evals(yw.empty() ? nullptr : yw.data(), (uint32_t)ood.size() - 1, v4, eqo, st));
+      }
+      const RoundConstants rc(ood);
+      CS_CHECK_ARG(rc.ok, "gkr_prove_batch: division by zero in the round constants");
+      const qm31 alpha = ch.draw_secure_felt();
+      const qm31 lam = ch.draw_secure_felt();
+      std::vector<Oracle> oracles;
+      std::vector<qm31> sc_claims;
+      std::vector<size_t> sc_inst;
+      for (size_t i = 0; i < n_inst; i++) {
+        if (!has_claims[i]) continue;
+        Oracle o;
+        o.layer = layers[i][cursor[i]--];
+        o.layer.num.owned = o.layer.den.owned = nullptr;  // the layer stack keeps its buffers
+        o.lambda = lam;
+        oracles.push_back(o);
+        qm31 c = kZero;  // random_linear_combination (horner)
+        for (size_t t = claims[i].size(); t-- > 0;) c = qm31_add(qm31_mul(c, lam), claims[i][t]);
+        sc_claims.push_back(c);
+        sc_inst.push_back(i);
+      }
+      std::vector<Poly> round_polys;
+      std::vector<qm31> sc_ood;
+      HP_TRY(sumcheck(sc_claims, oracles, alpha, eq, ood, rc, round_polys, sc_ood));
+      proofs.push_back(round_polys);
+      // masks of the constant oracles, one read for all
+      std::vector<std::pair<const GCol*, uint32_t>> reqs;
+      for (const Oracle& o : oracles) {
+        CS_CHECK_ARG(o.layer.kind != CS_GKR_LOGUP_MULTIPLICITIES, "gkr_prove_batch: mask of a multiplicities layer");
+        if (o.layer.kind == CS_GKR_LOGUP_GENERIC) reqs.push_back({&o.layer.num, 2});
+        reqs.push_back({&o.layer.den, 2});
+      }
+      std::vector<std::vector<qm31>> mv;
+      HP_TRY(read(reqs, mv));
+      std::vector<qm31> flat;
+      size_t r = 0;
+      std::vector<std::vector<std::pair<qm31, qm31>>> layer_masks;
+      for (const Oracle& o : oracles) {
+        std::vector<std::pair<qm31, qm31>> cols;
+        if (o.layer.kind == CS_GKR_LOGUP_SINGLES) cols.push_back({kOne, kOne});
+        if (o.layer.kind == CS_GKR_LOGUP_GENERIC) cols.push_back({mv[r][0], mv[r][1]}), r++;
+        cols.push_back({mv[r][0], mv[r][1]}), r++;
+        std::vector<qm31> m;
+        for (const auto& c : cols) m.insert(m.end(), {c.first, c.second});
+        ch.mix_felts(m);
+        layer_masks.push_back(cols);
+      }
+      for (Oracle& o : oracles) drop(o.layer.num), drop(o.layer.den);
+      ar.release(eq.owned);
+      const qm31 x = ch.draw_secure_felt();
+      ood = sc_ood;
+      ood.push_back(x);
+      for (size_t j = 0; j < sc_inst.size(); j++) {
+        masks[sc_inst[j]].push_back(layer_masks[j]);
+        claims[sc_inst[j]].clear();
+        for (const auto& c : layer_masks[j])  // fold_mle_evals
+          claims[sc_inst[j]].push_back(qm31_add(qm31_mul(x, qm31_sub(c.second, c.first)), c.first));
+      }
+    }
+    // proof
+    out.u(proofs.size());
+    for (const auto& rp : proofs) {
+      out.u(rp.size());
+      for (const Poly& p : rp) {
+        out.u(p.size());
+        for (const qm31& c : p) out.q(c);
+      }
+    }
+    out.u(n_inst);
+    for (size_t i = 0; i < n_inst; i++) {
+      out.u(masks[i].size());
+      for (const auto& m : masks[i]) {
+        out.u(m.size());
+        for (const auto& c : m) out.q(c.first), out.q(c.second);
+      }
+    }
+    for (size_t i = 0; i < n_inst; i++) {
+      out.u(outputs[i].size());
+      for (const qm31& c : outputs[i]) out.q(c);
+    }
+    // artifact
+    out.u(ood.size());
+    for (const qm31& c : ood) out.q(c);
+    for (size_t i = 0; i < n_inst; i++) {
+      out.u(claims[i].size());
+      for (const qm31& c : claims[i]) out.q(c);
+    }
+    for (size_t i = 0; i < n_inst; i++) out.u(inputs[i].n_vars);
+    return CS_OK;
+  }
+};
+
+}  // namespace
+}  // namespace hp
+}  // namespace cs
+
+extern "C" cs_status cs_gkr_prove_batch(uint32_t n_instances, const uint32_t* h_kinds, const uint32_t* h_n_variables,
+                                        const uint32_t* const* h_columns, uint32_t h_channel[9], uint64_t* h_words,
+                                        size_t capacity, size_t* n_words, cs_stream stream) {
+  CS_CHECK_ARG(n_instances >= 1 && h_kinds != nullptr && h_n_variables != nullptr && h_columns != nullptr &&
+                   h_channel != nullptr && n_words != nullptr,
+               "gkr_prove_batch: null pointer or no instance");
+  std::vector<hp::GLayer> inputs(n_instances);
+  for (uint32_t i = 0; i < n_instances; i++) {
+    hp::GLayer& L = inputs[i];
+    L.kind = h_kinds[i];
+    L.n_vars = h_n_variables[i];
+    CS_CHECK_ARG(L.kind <= CS_GKR_LOGUP_SINGLES, "gkr_prove_batch: unknown layer kind %u", L.kind);
+    CS_CHECK_ARG(L.n_vars >= 1 && L.n_vars <= 29, "gkr_prove_batch: %u variables (1..29)", L.n_vars);
+    const uint32_t* const* c = h_columns + 8 * (size_t)i;
+    for (int k = 0; k < 4; k++) {
+      L.den.c[k] = c[4 + k];
+      CS_CHECK_ARG(c[4 + k] != nullptr, "gkr_prove_batch: instance %u: null column", i);
+    }
+    if (L.kind == CS_GKR_LOGUP_GENERIC)
+      for (int k = 0; k < 4; k++) {
+        L.num.c[k] = c[k];
+        CS_CHECK_ARG(c[k] != nullptr, "gkr_prove_batch: instance %u: null numerator", i);
+      }
+    if (L.kind == CS_GKR_LOGUP_MULTIPLICITIES) {
+      L.num.c[0] = c[0];
+      L.num.base = true;
+      CS_CHECK_ARG(c[0] != nullptr, "gkr_prove_batch: instance %u: null numerator", i);
+    }
+  }
+  const cudaStream_t st = to_stream(stream);
+  hp::Channel ch;
+  for (int i = 0; i < 8; i++)
+    for (int b = 0; b < 4; b++) ch.digest[4 * i + b] = (uint8_t)(h_channel[i] >> (8 * b));
+  ch.n_draws = h_channel[8];
+  hp::Words words;
+  cs_status s;
+  {
+    hp::Arena arena(st);
+    hp::GkrProver prover{ch, arena, st};
+    s = prover.prove(inputs, words);
+    if (s == CS_OK && arena.status != CS_OK) s = arena.status;
+  }
+  if (s != CS_OK) return s;
+  for (int i = 0; i < 8; i++)
+    h_channel[i] = (uint32_t)ch.digest[4 * i] | ((uint32_t)ch.digest[4 * i + 1] << 8) |
+                   ((uint32_t)ch.digest[4 * i + 2] << 16) | ((uint32_t)ch.digest[4 * i + 3] << 24);
+  h_channel[8] = ch.n_draws;
+  return finish(words.w, h_words, capacity, n_words);
+}

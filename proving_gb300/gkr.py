@@ -547,3 +547,71 @@ class DeviceGkrOps:
                       self._u32(lam), out.data_ptr() + 32 * j, self._stream())
         w = out.cpu().numpy().view(np.uint32).reshape(-1, 8)
         return [(tuple(int(x) for x in r[:4]), tuple(int(x) for x in r[4:])) for r in w]
+
+
+# ------------------------------------------------------------ native driver
+
+def prove_batch_native(channel, input_layers) -> tuple[GkrBatchProof, GkrArtifact]:
+    """prove_batch with the protocol in native code (cs_gkr_prove_batch): the same proof and
+    artifact as prove_batch over DeviceGkrOps, with one host synchronisation per sum-check round and
+    no interpreter between the launches. Inputs are device MLEs (DeviceGkrOps' layout); the
+    channel (proving_gb300.prover.Blake2sChannel) is advanced as prove_batch advances it."""
+    import struct
+    import torch
+    n = len(input_layers)
+    kinds = (ctypes.c_uint32 * n)(*[lay.kind for lay in input_layers])
+    nvars = (ctypes.c_uint32 * n)(*[lay.n_variables for lay in input_layers])
+    cols = (ctypes.c_void_p * (8 * n))()
+    for i, lay in enumerate(input_layers):
+        den = lay.mles[-1].data
+        for k in range(4):
+            cols[8 * i + 4 + k] = den[k].data_ptr()
+        if lay.kind in (LOGUP_GENERIC, LOGUP_MULTIPLICITIES):
+            num = lay.mles[0]
+            for k in range(1 if num.base else 4):
+                cols[8 * i + k] = num.data[k].data_ptr()
+    state = (ctypes.c_uint32 * 9)(*struct.unpack("<8I", channel.digest), channel.n_draws)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    n_words = ctypes.c_size_t()
+    # the proof's size is known only at the end: a bound from the layer sizes, retried once if short
+    layers = max(lay.n_variables for lay in input_layers)
+    cap = 64 + n * 64 + layers * layers * 24 + n * layers * 24 + 8 * layers
+    for _ in range(2):
+        snap = (ctypes.c_uint32 * 9)(*state)
+        words = (ctypes.c_uint64 * cap)()
+        try:
+            _lib.call("cs_gkr_prove_batch", n, kinds, nvars, cols, snap, words, cap, ctypes.byref(n_words), stream)
+        except _lib.CudaBackendError:
+            if n_words.value > cap:
+                cap = n_words.value
+                continue
+            raise
+        break
+    w = list(words[:n_words.value])
+    pos = 0
+
+    def take():
+        nonlocal pos
+        pos += 1
+        return int(w[pos - 1])
+
+    def felt():
+        nonlocal pos
+        pos += 4
+        return tuple(int(x) for x in w[pos - 4:pos])
+
+    proof = GkrBatchProof()
+    for _ in range(take()):
+        proof.sumcheck_proofs.append([[felt() for _ in range(take())] for _ in range(take())])
+    n_inst = take()
+    for _ in range(n_inst):
+        proof.layer_masks_by_instance.append(
+            [GkrMask([(felt(), felt()) for _ in range(take())]) for _ in range(take())])
+    for _ in range(n_inst):
+        proof.output_claims_by_instance.append([felt() for _ in range(take())])
+    ood = [felt() for _ in range(take())]
+    claims = [[felt() for _ in range(take())] for _ in range(n_inst)]
+    n_vars = [take() for _ in range(n_inst)]
+    channel.digest = struct.pack("<8I", *snap[:8])
+    channel.n_draws = snap[8]
+    return proof, GkrArtifact(ood, claims, n_vars)

@@ -107,6 +107,17 @@ def test_gkr_arguments_are_checked_on_host(lib):
     # the sum-check sums need an input layer of at least 4 values
     assert _status(lib, "cs_gkr_sum_as_poly", 0, cols, null, cols, 1, q, ctypes.c_void_p(1 << 30), null) == INVALID
     assert _status(lib, "cs_mle_fix_first_variable", cols, 0, 0, q, cols, null) == INVALID
+    # the native batch prover: no instance, an unknown kind, 0 variables, a null column
+    n_words = ctypes.c_size_t()
+    state = (ctypes.c_uint32 * 9)()
+    tab = (ctypes.c_void_p * 8)(*[1 << (22 + k) for k in range(8)])
+    for kinds, nv, n in (((0,), (5,), 0), ((7,), (5,), 1), ((1,), (0,), 1)):
+        assert _status(lib, "cs_gkr_prove_batch", n, (ctypes.c_uint32 * 1)(*kinds), (ctypes.c_uint32 * 1)(*nv),
+                       tab, state, null, 0, ctypes.byref(n_words), null) == INVALID
+    tab[5] = None
+    assert _status(lib, "cs_gkr_prove_batch", 1, (ctypes.c_uint32 * 1)(0), (ctypes.c_uint32 * 1)(4), tab, state,
+                   null, 0, ctypes.byref(n_words), null) == INVALID
+    assert b"null column" in lib.cs_last_error()
 
 
 def test_error_raises_in_python_mirror(lib):

@@ -143,3 +143,43 @@ def test_large_logup_batch_verifies(dev):
     while lay.n_variables:
         lay = cpu.next_layer(lay)
     assert proof.output_claims_by_instance[1] == cpu.values(lay.mles[0], 1)
+
+
+@pytest.mark.parametrize("spec", [
+    [(G.GRAND_PRODUCT, 1)],
+    [(G.GRAND_PRODUCT, 7)],
+    [(G.GRAND_PRODUCT, 10), (G.LOGUP_GENERIC, 8), (G.LOGUP_SINGLES, 6), (G.LOGUP_MULTIPLICITIES, 9)],
+    [(G.LOGUP_MULTIPLICITIES, 2), (G.LOGUP_GENERIC, 12)],
+    [(G.LOGUP_SINGLES, 14), (G.LOGUP_SINGLES, 14)],
+])
+def test_native_prove_batch_equals_driver(dev, spec):
+    """cs_gkr_prove_batch (the protocol in native code) gives the Python driver's proof, artifact
+    and final channel state; the verifier accepts it."""
+    layers, gates = batch(dev, spec)
+    ch_py, ch_nat = pr.Blake2sChannel(), pr.Blake2sChannel()
+    ch_py.mix_u32s([7, 8, 9])
+    ch_nat.mix_u32s([7, 8, 9])
+    p_py, a_py = G.prove_batch(dev, ch_py, layers)
+    p_nat, a_nat = G.prove_batch_native(ch_nat, layers)
+    assert proof_words(p_nat) == proof_words(p_py)
+    assert (a_nat.ood_point, a_nat.claims_to_verify_by_instance, a_nat.n_variables_by_instance) == \
+        (a_py.ood_point, a_py.claims_to_verify_by_instance, a_py.n_variables_by_instance)
+    assert (ch_nat.digest, ch_nat.n_draws) == (ch_py.digest, ch_py.n_draws)
+    vch = O.Blake2sChannel(ch_py_start_digest(spec))
+    ood, claims, _ = partially_verify_batch(gates, p_nat, vch)
+    assert ood == a_nat.ood_point and claims == a_nat.claims_to_verify_by_instance
+
+
+def ch_py_start_digest(spec):
+    ch = pr.Blake2sChannel()
+    ch.mix_u32s([7, 8, 9])
+    return ch.digest
+
+
+def test_native_prove_batch_large_logup(dev):
+    """2^20-fraction LogUp through the native driver: verifies and ends at the inputs' MLEs."""
+    nums, dens = felts(51, 1 << 20), felts(52, 1 << 20)
+    layers = [G.Layer(G.LOGUP_GENERIC, [dev.mle_from_host(nums), dev.mle_from_host(dens)])]
+    proof, art = G.prove_batch_native(pr.Blake2sChannel(), layers)
+    ood, claims, _ = partially_verify_batch([LOGUP], proof, O.Blake2sChannel())
+    assert claims == [[mle_eval_at_point(nums, ood), mle_eval_at_point(dens, ood)]] == art.claims_to_verify_by_instance
