@@ -95,6 +95,44 @@ __host__ __device__ __forceinline__ qm31 qm31_inv(qm31 x) {
   return {cm31_mul(x.a, di), cm31_mul(cm31_neg(x.b), di)};
 }
 
+// x * c for a QM31 c fixed across many products (a folding challenge, a random coefficient):
+// with x = (a0 + a1 i) + (a2 + a3 i) u, coordinate r of the product is sum_j a_j k[r][j] for a
+// table k built once from c (the rows expand (A + B u)(C + D u) = AC + (2 + i) BD + (AD + BC) u).
+// Four 64-bit multiply-accumulates of canonical words stay below 2^64 and are reduced once, so
+// the canonical product equals qm31_mul's.
+struct qm31_const {
+  uint32_t k[4][4];
+};
+__host__ __device__ inline qm31_const qm31_const_of(qm31 c) {
+  const uint32_t b0 = c.a.a, b1 = c.a.b, b2 = c.b.a, b3 = c.b.b;
+  const uint32_t two_b2_b3 = m31_sub(m31_add(b2, b2), b3), b2_two_b3 = m31_add(b2, m31_add(b3, b3));
+  qm31_const t;
+  const uint32_t rows[4][4] = {{b0, m31_neg(b1), two_b2_b3, m31_neg(b2_two_b3)},
+                               {b1, b0, b2_two_b3, two_b2_b3},
+                               {b2, m31_neg(b3), b0, m31_neg(b1)},
+                               {b3, b2, b1, b0}};
+  for (int r = 0; r < 4; r++)
+    for (int j = 0; j < 4; j++) t.k[r][j] = rows[r][j];
+  return t;
+}
+// x mod P for any 64-bit x (2^31 = 1 mod P, folded twice).
+__host__ __device__ __forceinline__ uint32_t m31_reduce64(uint64_t x) {
+  const uint64_t y = (x & P) + (x >> 31);                       // < 2^33 + 2^31
+  return m31_reduce_once((uint32_t)(y & P) + (uint32_t)(y >> 31));  // < 2^31 + 5
+}
+__host__ __device__ __forceinline__ qm31 qm31_mul_const(qm31 x, const qm31_const& c) {
+  const uint32_t a[4] = {x.a.a, x.a.b, x.b.a, x.b.b};
+  uint32_t r[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    uint64_t acc = (uint64_t)a[0] * c.k[i][0];
+#pragma unroll
+    for (int j = 1; j < 4; j++) acc += (uint64_t)a[j] * c.k[i][j];
+    r[i] = m31_reduce64(acc);
+  }
+  return qm31_make(r[0], r[1], r[2], r[3]);
+}
+
 // Circle group over M31: (x1,y1)+(x2,y2) = (x1x2 - y1y2, x1y2 + y1x2).
 struct cpoint {
   uint32_t x, y;

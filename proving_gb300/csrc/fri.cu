@@ -93,7 +93,7 @@ constexpr uint32_t kFoldTileLog = 10;
 constexpr uint32_t kFoldThreads = 1u << (kFoldTileLog - 1);
 
 struct FoldSteps {
-  qm31 alpha[kFoldTileLog];
+  qm31_const alpha[kFoldTileLog];  // each challenge as its product table
 };
 
 template <bool VEC>
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(kFoldThreads) fold_line_tile_kernel(const Coor
       qm31 f0 = qm31_make(s[0][2 * p], s[1][2 * p], s[2][2 * p], s[3][2 * p]);
       qm31 f1 = qm31_make(s[0][2 * p + 1], s[1][2 * p + 1], s[2][2 * p + 1], s[3][2 * p + 1]);
       qm31_ibfly(f0, f1, tw[off + p]);
-      r = qm31_add(f0, qm31_mul(steps.alpha[j], f1));
+      r = qm31_add(f0, qm31_mul_const(f1, steps.alpha[j]));
     }
     __syncthreads();
     if (p < m) {
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kStreamThreads, 4) fold_line_stream_kernel(con
           qm31 f0 = qm31_make(s[b][0][2 * q], s[b][1][2 * q], s[b][2][2 * q], s[b][3][2 * q]);
           qm31 f1 = qm31_make(s[b][0][2 * q + 1], s[b][1][2 * q + 1], s[b][2][2 * q + 1], s[b][3][2 * q + 1]);
           qm31_ibfly(f0, f1, tw[b][off + q]);
-          r[h] = qm31_add(f0, qm31_mul(steps.alpha[j], f1));
+          r[h] = qm31_add(f0, qm31_mul_const(f1, steps.alpha[j]));
         }
       }
       __syncthreads();
@@ -296,7 +296,8 @@ __global__ void __launch_bounds__(kStreamThreads, 4) fold_line_stream_kernel(con
 // 16-byte loads, one (1/x, 1/y) twiddle pair for the four, and one 16-byte store per coordinate.
 // Needs 16-byte aligned coordinates and a multiple of 4 pairs.
 __global__ void __launch_bounds__(256) fold_circle_wide_kernel(const Coords c, uint32_t quads,
-                                                               const uint32_t* __restrict__ lt1, qm31 alpha) {
+                                                               const uint32_t* __restrict__ lt1,
+                                                               const qm31_const alpha) {
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < quads; t += gridDim.x * blockDim.x) {
     const uint2 xy = __ldg(reinterpret_cast<const uint2*>(lt1) + t);  // (1/x, 1/y) of pair 2t
     const uint32_t tws[4] = {xy.y, m31_neg(xy.y), m31_neg(xy.x), xy.x};
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(256) fold_circle_wide_kernel(const Coords c, u
       if (q == 2) f0 = qm31_make(hi[0].x, hi[1].x, hi[2].x, hi[3].x), f1 = qm31_make(hi[0].y, hi[1].y, hi[2].y, hi[3].y);
       if (q == 3) f0 = qm31_make(hi[0].z, hi[1].z, hi[2].z, hi[3].z), f1 = qm31_make(hi[0].w, hi[1].w, hi[2].w, hi[3].w);
       qm31_ibfly(f0, f1, tws[q]);
-      const qm31 r = qm31_add(qm31_mul(alpha, f1), f0);
+      const qm31 r = qm31_add(qm31_mul_const(f1, alpha), f0);
       o[0][q] = r.a.a, o[1][q] = r.a.b, o[2][q] = r.b.a, o[3][q] = r.b.b;
     }
 #pragma unroll
@@ -415,7 +416,8 @@ cs_status fold_circle_impl(const uint32_t* const h_src[4], uint32_t log_size, qm
   for (int k = 0; k < 4; k++)
     wide = wide && (reinterpret_cast<uintptr_t>(c.in[k]) & 15) == 0 && (reinterpret_cast<uintptr_t>(c.out[k]) & 15) == 0;
   if (wide) {
-    fold_circle_wide_kernel<<<grid_for(half / 4, 256), 256, 0, to_stream(stream)>>>(c, half / 4, lt1, alpha);
+    fold_circle_wide_kernel<<<grid_for(half / 4, 256), 256, 0, to_stream(stream)>>>(c, half / 4, lt1,
+                                                                                qm31_const_of(alpha));
     CS_LAUNCHED("fold_circle_wide_kernel");
     return CS_OK;
   }
@@ -469,7 +471,7 @@ extern "C" cs_status cs_fold_line_steps(const uint32_t* const h_src[4], uint32_t
     FoldSteps steps;
     for (uint32_t j = 0; j < folds; j++) {
       const uint32_t* a = h_alphas + 4 * (size_t)(done + j);
-      steps.alpha[j] = qm31_make(a[0] % P, a[1] % P, a[2] % P, a[3] % P);
+      steps.alpha[j] = qm31_const_of(qm31_make(a[0] % P, a[1] % P, a[2] % P, a[3] % P));
     }
     bool vec = tile_log >= 2;
     for (int k = 0; k < 4; k++) vec = vec && (reinterpret_cast<uintptr_t>(c.in[k]) & 15) == 0;

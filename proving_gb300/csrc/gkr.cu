@@ -202,7 +202,7 @@ __device__ __forceinline__ void block_sum2(qm31& s0, qm31& s2) {
 // cpu/lookups/gkr.rs:66-227); LogUp gates combine numerator + lambda * denominator.
 template <int KIND>
 __global__ void __launch_bounds__(256) sum_poly_kernel(const QIn eq, const QIn num, const QIn den, uint32_t n_terms,
-                                                        qm31 lambda, uint32_t* partial) {
+                                                        const qm31_const lambda, uint32_t* partial) {
   qm31 s0 = q_zero(), s2 = q_zero();
   for (uint32_t i = global_thread(); i < n_terms; i += grid_stride()) {
     qm31 d00, d01, d10, d11;
@@ -240,8 +240,8 @@ __global__ void __launch_bounds__(256) sum_poly_kernel(const QIn eq, const QIn n
         frac_add(n00, d00, n01, d01, num0, den0);
         frac_add(n20, d20, n21, d21, num2, den2);
       }
-      g0 = qm31_add(num0, qm31_mul(lambda, den0));
-      g2 = qm31_add(num2, qm31_mul(lambda, den2));
+      g0 = qm31_add(num0, qm31_mul_const(den0, lambda));
+      g2 = qm31_add(num2, qm31_mul_const(den2, lambda));
     }
     const qm31 e = q_load(eq, i);
     s0 = qm31_add(s0, qm31_mul(e, g0));
@@ -394,7 +394,7 @@ extern "C" cs_status cs_gkr_sum_as_poly(uint32_t kind, const uint32_t* const h_e
                  "gkr_sum_as_poly: input columns must be 8-byte aligned");
   const uint32_t n_terms = 1u << (log_n - 2);
   const uint32_t blocks = stream_blocks(n_terms, 256, 4);
-  const qm31 lambda = host_qm31(h_lambda);
+  const qm31_const lambda = qm31_const_of(host_qm31(h_lambda));
   cudaStream_t st = to_stream(stream);
   uint32_t* partial = nullptr;
   CS_CUDA(stream_alloc(reinterpret_cast<void**>(&partial), sizeof(uint32_t) * 8 * blocks, st));
