@@ -50,6 +50,8 @@ struct FftPass {
   uint32_t tw_log;    // log2 of the tree length
   uint32_t tw_dom;    // log size of the canonic domain whose twiddle layers are used (>= log_n;
                       // larger for a subdomain, which takes the prefix of each layer)
+  uint32_t vec;       // 1: every column is 16-byte aligned and the source mask keeps runs of 4,
+                      // so tiles move between HBM and shared memory as 16-byte words
 };
 
 struct Tile {
@@ -223,7 +225,7 @@ template <bool INV, int T, bool OUTER>
 __global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), tile_min_blocks<T, OUTER>()) fft_tile_kernel(const FftBatch batch, const FftPass p) {
   constexpr int TA = T / 2, TB = T - TA;
   constexpr uint32_t M = 1u << T;
-  extern __shared__ uint32_t s[];
+  extern __shared__ __align__(16) uint32_t s[];
   const uint32_t EB = OUTER ? p.c : 3u;  // inner tiles always hold 8 groups
   uint32_t* dst = batch.dst[blockIdx.y];
   const uint32_t* src = batch.src[blockIdx.y];
@@ -237,8 +239,39 @@ __global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), tile_min_blocks<
     tl.ib = blockIdx.x >> outer_bits;
   }
   // every thread moves exactly 2^TB words (the tile holds 2^(T + EB) words, the block has
-  // 2^(TA + EB) threads); up to 32 of a thread's loads are in flight before its first store
-  {
+  // 2^(TA + EB) threads); up to 32 of a thread's loads are in flight before its first store.
+  // With p.vec a thread moves four consecutive tile words at a time: four consecutive tile slots
+  // are four consecutive column words in both layouts (contiguous tiles: the group index fills the
+  // low bits; strided tiles: a group is 8 adjacent words), and the padding keeps the four together
+  // (a 16-byte-aligned run for strided tiles; for contiguous tiles one pad word per 32 shifts each
+  // 8-lane group by one bank, so the four scalar stores of a warp hit 32 distinct banks).
+  constexpr bool kVecOk = TB >= 2;
+  if (kVecOk && p.vec) {
+    constexpr int GQ = (1 << TB) < 4 ? 1 : ((1 << TB) < 32 ? (1 << TB) : 32) / 4;  // tiles of 1 layer never get here
+#pragma unroll 1
+    for (int k0 = 0; k0 < (1 << TB) / 4; k0 += GQ) {
+      uint4 r[GQ];
+#pragma unroll
+      for (int k = 0; k < GQ; k++) {
+        const uint32_t L = 4 * (threadIdx.x + (k0 + k) * blockDim.x);
+        const uint32_t m = OUTER ? (L & (M - 1)) : (L >> EB);
+        const uint32_t e = OUTER ? (L >> T) : (L & ((1u << EB) - 1));
+        r[k] = __ldg(reinterpret_cast<const uint4*>(src + (tile_gidx(p, tl, m, e) & p.src_mask)));
+      }
+#pragma unroll
+      for (int k = 0; k < GQ; k++) {
+        uint32_t* d = s + pad<OUTER>(4 * (threadIdx.x + (k0 + k) * blockDim.x));
+        if (OUTER) {
+          d[0] = r[k].x;
+          d[1] = r[k].y;
+          d[2] = r[k].z;
+          d[3] = r[k].w;
+        } else {
+          *reinterpret_cast<uint4*>(d) = r[k];
+        }
+      }
+    }
+  } else {
     constexpr int G = (1 << TB) < 32 ? (1 << TB) : 32;
 #pragma unroll 1
     for (int k0 = 0; k0 < (1 << TB); k0 += G) {
@@ -284,6 +317,24 @@ __global__ void __launch_bounds__(tile_max_threads<T, OUTER>(), tile_min_blocks<
       for (int j = 0; j < (1 << TB); j++) s[pad<OUTER>(lin<OUTER>((j << TA) | mb, e, T, EB))] = v[j];
     }
     __syncthreads();
+  }
+  if (kVecOk && p.vec) {
+#pragma unroll 1
+    for (int k0 = 0; k0 < (1 << TB) / 4; k0++) {
+      const uint32_t L = 4 * (threadIdx.x + k0 * blockDim.x);
+      const uint32_t m = OUTER ? (L & (M - 1)) : (L >> EB);
+      const uint32_t e = OUTER ? (L >> T) : (L & ((1u << EB) - 1));
+      const uint32_t* d = s + pad<OUTER>(L);
+      uint4 v = OUTER ? make_uint4(d[0], d[1], d[2], d[3]) : *reinterpret_cast<const uint4*>(d);
+      if (p.scale) {
+        v.x = m31_mul(v.x, p.scale);
+        v.y = m31_mul(v.y, p.scale);
+        v.z = m31_mul(v.z, p.scale);
+        v.w = m31_mul(v.w, p.scale);
+      }
+      *reinterpret_cast<uint4*>(dst + tile_gidx(p, tl, m, e)) = v;
+    }
+    return;
   }
   // stores in groups of four, which keeps the register budget of three blocks per SM
 #pragma unroll 1
@@ -498,11 +549,15 @@ cs_status dispatch_copy(const FftBatch& b, uint32_t n_cols, const FftPass& p, cu
 }
 
 template <bool INV>
-cs_status launch_pass(const FftBatch& b, uint32_t n_cols, const FftPass& p, cudaStream_t st) {
-  if (p.hi == p.lo) {
+cs_status launch_pass(const FftBatch& b, uint32_t n_cols, const FftPass& p_in, cudaStream_t st) {
+  if (p_in.hi == p_in.lo) {
     // zero layers: a copy (replication of a constant column)
-    return dispatch_copy(b, n_cols, p, st);
+    return dispatch_copy(b, n_cols, p_in, st);
   }
+  FftPass p = p_in;
+  p.vec = p.src_mask >= 3;  // replicated reads of fewer than 4 coefficients break the runs of 4
+  for (uint32_t i = 0; i < n_cols && p.vec; i++)
+    p.vec = ((reinterpret_cast<uintptr_t>(b.src[i]) | reinterpret_cast<uintptr_t>(b.dst[i])) & 15) == 0;
   return p.outer ? dispatch_tile<INV, true>(b, n_cols, p, st) : dispatch_tile<INV, false>(b, n_cols, p, st);
 }
 
@@ -529,7 +584,7 @@ cs_status run_fft(const uint32_t* const* srcs, uint32_t* const* dsts, uint32_t n
     }
     const uint32_t n_layers = inverse ? log_n : log_src;
     std::vector<PassPlan> plan = plan_passes(inverse, log_n, n_layers);
-    FftPass p;
+    FftPass p{};
     p.log_n = log_n;
     p.tw = tw;
     p.tw_log = tw_log;
