@@ -393,11 +393,13 @@ extern "C" cs_status cs_gkr_sum_as_poly(uint32_t kind, const uint32_t* const h_e
     CS_CHECK_ARG(aligned8(den.c[k]) && (num.c[k] == nullptr || aligned8(num.c[k])),
                  "gkr_sum_as_poly: input columns must be 8-byte aligned");
   const uint32_t n_terms = 1u << (log_n - 2);
-  const uint32_t blocks = stream_blocks(n_terms, 256, 4);
+  // up to 1024 terms one block sums them and writes the result itself (most sum-check rounds
+  // are small: the columns halve every round); larger sums go through per-block partials
+  const uint32_t blocks = n_terms <= 1024 ? 1 : stream_blocks(n_terms, 256, 4);
   const qm31_const lambda = qm31_const_of(host_qm31(h_lambda));
   cudaStream_t st = to_stream(stream);
-  uint32_t* partial = nullptr;
-  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&partial), sizeof(uint32_t) * 8 * blocks, st));
+  uint32_t* partial = d_out;
+  if (blocks > 1) CS_CUDA(stream_alloc(reinterpret_cast<void**>(&partial), sizeof(uint32_t) * 8 * blocks, st));
   switch (kind) {
     case CS_GKR_GRAND_PRODUCT:
       sum_poly_kernel<CS_GKR_GRAND_PRODUCT><<<blocks, 256, 0, st>>>(eq, num, den, n_terms, lambda, partial);
@@ -413,6 +415,10 @@ extern "C" cs_status cs_gkr_sum_as_poly(uint32_t kind, const uint32_t* const h_e
   }
   note_launch();
   cudaError_t e = cudaGetLastError();
+  if (blocks == 1) {
+    if (e != cudaSuccess) return from_cuda(e, "launch sum_poly_kernel");
+    return CS_OK;
+  }
   if (e == cudaSuccess) {
     sum_partials_kernel<<<1, 256, 0, st>>>(partial, blocks, d_out);
     note_launch();
