@@ -214,11 +214,13 @@ template <int T, bool OUTER>
 constexpr int tile_max_threads() {
   return OUTER ? 256 : (1 << (T / 2 + 3));
 }
-// Blocks per SM the register budget is sized for: tiles of up to 10 layers
-// fit three without spills, larger ones two.
+// Blocks per SM the register budget is sized for: tiles of up to 10 layers fit
+// four (64 registers) without spills, larger ones two. Four blocks keep more
+// tile loads in flight: the strided evaluate pass, which reads each coefficient
+// tile once for its replicas, is otherwise bound by its load latency.
 template <int T, bool OUTER>
 constexpr int tile_min_blocks() {
-  return T <= 10 ? 3 : 2;
+  return T <= 10 ? 4 : 2;
 }
 
 template <bool INV, int T, bool OUTER>
