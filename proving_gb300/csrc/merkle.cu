@@ -110,6 +110,40 @@ __global__ void merkle_node_kernel(const uint32_t* __restrict__ prev, uint32_t l
   o[1] = make_uint4(h[4], h[5], h[6], h[7]);
 }
 
+// The top layers of a tree in one launch: one block builds layers log_in - 1 down to 0 from the
+// layer of 2^log_in digests at `layer`, each written right after the one before it (the layout of
+// cs_merkle_commit), with a barrier between layers. Plain loads, since each layer reads what the
+// block wrote for the previous one; the barrier makes those stores visible to the block.
+constexpr uint32_t kTopLayersLog = 10;  // layers of up to 2^10 nodes
+
+__global__ void __launch_bounds__(1024) merkle_top_kernel(uint32_t* layer, uint32_t log_in, uint32_t one) {
+  const uint32_t* prev = layer;
+  uint32_t* out = layer + ((size_t)8 << log_in);
+  for (int k = (int)log_in - 1; k >= 0; k--) {
+    for (uint32_t i = threadIdx.x; i < (1u << k); i += blockDim.x) {
+      const uint4* src = reinterpret_cast<const uint4*>(prev + (size_t)i * 16);
+      uint32_t m[16];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const uint4 w = src[q];
+        m[4 * q] = w.x;
+        m[4 * q + 1] = w.y;
+        m[4 * q + 2] = w.z;
+        m[4 * q + 3] = w.w;
+      }
+      uint32_t h[8];
+      b2s_init(h);
+      b2s_compress(h, m, 64, 0, true, one);
+      uint4* o = reinterpret_cast<uint4*>(out + (size_t)i * 8);
+      o[0] = make_uint4(h[0], h[1], h[2], h[3]);
+      o[1] = make_uint4(h[4], h[5], h[6], h[7]);
+    }
+    __syncthreads();
+    prev = out;
+    out += (size_t)8 << k;
+  }
+}
+
 }  // namespace
 
 cs_status merkle_leaves(const uint32_t* const* cols, const uint32_t* log_sizes, uint32_t n_cols, uint32_t L,
@@ -228,6 +262,12 @@ extern "C" cs_status cs_merkle_commit(const uint32_t* const* h_cols, const uint3
   if (s != CS_OK) return s;
   uint32_t* cur = d_layers;
   for (uint32_t k = lifting_log_size; k >= 1; k--) {
+    if (k - 1 <= kTopLayersLog) {  // the rest of the tree in one launch
+      const uint32_t threads = std::max(32u, std::min(1024u, 1u << (k - 1)));
+      merkle_top_kernel<<<1, threads, 0, st>>>(cur, k, 1u);
+      CS_LAUNCHED("merkle_top_kernel");
+      break;
+    }
     uint32_t* next = cur + ((size_t)8 << k);
     s = merkle_next_layer(cur, k - 1, next, st);
     if (s != CS_OK) return s;
