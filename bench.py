@@ -449,10 +449,12 @@ def mixed_prove_leg(torch, n_proofs: int = 2, arms=("batched", "plain", "native"
             del traces, values
         out["native"] = {"proofs_per_s": round(1e3 / statistics.median(lat), 3),
                          "p50_ms": round(statistics.median(lat), 3), "max_ms": round(max(lat), 3),
-                         "same_proof_bytes": hashlib.sha256(words).hexdigest() == digests["batched"]}
+                         "same_proof_bytes": (hashlib.sha256(words).hexdigest() == digests["batched"]
+                                              if "batched" in digests else None)}
+        digests["native"] = hashlib.sha256(words).hexdigest()
         del tw
         torch.cuda.empty_cache()
-    out["proof_sha256"] = digests["batched"]
+    out["proof_sha256"] = digests.get("batched", digests.get("native"))
     if "plain" in arms:
         out["same_proof_bytes"] = digests["batched"] == digests["plain"]
         out["batched_speedup"] = round(out["plain"]["p50_ms"] / out["batched"]["p50_ms"], 3)
@@ -986,6 +988,8 @@ def run_case(args):
     cuda_build.build()
     if args.case == "mixed-kernels":
         res = case_mixed_kernels(torch)
+    elif args.case == "mixed-prove-native":  # one native proof after one warm-up proof
+        res = mixed_prove_leg(torch, n_proofs=1, arms=("native",))
     elif args.case == "gkr":
         res = gkr_leg(torch, log_logup=args.gkr_log, log_gp=max(args.gkr_log - 2, 2), n_proofs=1,
                       kernel_log=args.gkr_log)
@@ -1014,7 +1018,7 @@ def main():
     ap.add_argument("--skip-autotune", action="store_true",
                     help="keep the default FFT pass plans (no candidate sweep before timing; for profiling)")
     ap.add_argument("--gkr-log", type=int, default=22, help="log2 values of the --case gkr instance")
-    ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove", "gkr"],
+    ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove", "mixed-prove-native", "gkr"],
                     help="run one small profiling case instead of the benchmark (for ncu)")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
