@@ -990,6 +990,20 @@ def run_case(args):
         res = case_mixed_kernels(torch)
     elif args.case == "mixed-prove-native":  # one native proof after one warm-up proof
         res = mixed_prove_leg(torch, n_proofs=1, arms=("native",))
+    elif args.case == "poseidon-native":  # one native Poseidon2 proof after one warm-up proof
+        from proving_gb300 import poseidon as ps
+        from proving_gb300 import prover as pr
+        from proving_gb300.backend import CudaBackend
+        log_n = args.poseidon_log_rows
+        tw = pr.GpuOps().twiddles(log_n + ps.LOG_EXPAND + 1)
+        lat = []
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            CudaBackend.prove_poseidon_native(log_n, (10, 1, 0, 70), tw)
+            torch.cuda.synchronize()
+            lat.append((time.perf_counter() - t0) * 1e3)
+        res = {"workload": f"native Poseidon2 proof, 2^{log_n} rows", "ms": [round(x, 3) for x in lat]}
     elif args.case == "gkr":
         res = gkr_leg(torch, log_logup=args.gkr_log, log_gp=max(args.gkr_log - 2, 2), n_proofs=1,
                       kernel_log=args.gkr_log)
@@ -1018,7 +1032,7 @@ def main():
     ap.add_argument("--skip-autotune", action="store_true",
                     help="keep the default FFT pass plans (no candidate sweep before timing; for profiling)")
     ap.add_argument("--gkr-log", type=int, default=22, help="log2 values of the --case gkr instance")
-    ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove", "mixed-prove-native", "gkr"],
+    ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove", "mixed-prove-native", "poseidon-native", "gkr"],
                     help="run one small profiling case instead of the benchmark (for ncu)")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
