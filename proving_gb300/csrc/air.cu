@@ -36,18 +36,26 @@ __global__ void __launch_bounds__(256) wide_fib_composition_kernel(const __grid_
                                                                     uint32_t* a3) {
   const uint32_t n = 1u << p.eval_log;
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    // Lazy sums: each weight x constraint product is below 2^62 and is added unreduced (one
+    // 64-bit multiply-add per coordinate); folding every four constraints keeps the sums below
+    // 2^64 (a fold leaves less than 2^34). Each column is squared once, for the constraint that
+    // reads it as b and the next one that reads it as a.
     uint64_t acc[4] = {0, 0, 0, 0};
-    uint32_t a = __ldg(p.cols[0] + r), b = __ldg(p.cols[1] + r);
+    uint32_t sa = m31_sqr(__ldg(p.cols[0] + r)), sb = m31_sqr(__ldg(p.cols[1] + r));
     for (uint32_t k = 0; k + 2 < p.n_cols; k++) {
       const uint32_t c = __ldg(p.cols[k + 2] + r);
-      const uint32_t cons = m31_sub(c, m31_add(m31_sqr(a), m31_sqr(b)));
+      const uint32_t cons = m31_sub(c, m31_add(sa, sb));
       const qm31 w = p.rc[k];
-      acc[0] += m31_mul(w.a.a, cons);
-      acc[1] += m31_mul(w.a.b, cons);
-      acc[2] += m31_mul(w.b.a, cons);
-      acc[3] += m31_mul(w.b.b, cons);
-      a = b;
-      b = c;
+      acc[0] += (uint64_t)w.a.a * cons;
+      acc[1] += (uint64_t)w.a.b * cons;
+      acc[2] += (uint64_t)w.b.a * cons;
+      acc[3] += (uint64_t)w.b.b * cons;
+      if ((k & 3) == 3) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[j] = (acc[j] & P) + (acc[j] >> 31);
+      }
+      sa = sb;
+      sb = m31_sqr(c);
     }
     const uint32_t d = p.den[r >> p.trace_log];
     a0[r] = m31_add(a0[r], m31_mul(fold64(acc[0]), d));
@@ -109,7 +117,7 @@ extern "C" cs_status cs_wide_fib_composition(const uint32_t* const* h_cols, uint
     p.cols[k] = h_cols[k];
   }
   for (uint32_t k = 0; k + 2 < n_cols; k++)
-    p.rc[k] = qm31_make(h_rc[4 * k], h_rc[4 * k + 1], h_rc[4 * k + 2], h_rc[4 * k + 3]);
+    p.rc[k] = qm31_make(h_rc[4 * k] % P, h_rc[4 * k + 1] % P, h_rc[4 * k + 2] % P, h_rc[4 * k + 3] % P);
   // denom_inv[i] = 1 / V_trace(eval_domain.at(i)), i < 2^(eval - trace), then bit-reversed
   // (component_prover.rs:101-108). V of CanonicCoset(t).coset at p is pi^(t-1)(p.x).
   const uint32_t log_expand = eval_log - trace_log, n_den = 1u << log_expand;
