@@ -539,18 +539,21 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
 def serving_leg(n_requests: int = 24, rate_per_s: float = 200.0):
     """Config 5: a seeded Poisson stream of proof requests, half Wide-Fibonacci (100 columns) and
     half Poseidon2 (8 permutations per row), log_n_rows uniform in [12, 20], arriving faster than
-    they can be served (so proofs/s measures capacity). Three arms on the same stream: the plain
-    path (one request at a time, one launch per column per stage), the batched path one request at
-    a time, and the served form (4 worker processes with their own CUDA contexts, HBM-budget
-    admission, batched stage launches)."""
+    they can be served (so proofs/s measures capacity). Four arms on the same stream: the plain
+    path (one request at a time, one launch per column per stage, restated prover), the batched
+    path one request at a time (native provers), the served form (4 worker threads of one process,
+    a CUDA stream each, HBM-budget admission, native provers, which release the interpreter for
+    the whole proof so the threads' kernels overlap on the device), and the same with 4 worker
+    processes (a CUDA context each: their kernels time-slice instead of overlapping)."""
     from proving_gb300 import serving
     out = {"workload": f"{n_requests} requests, 50% Wide-Fibonacci (100 cols) / 50% Poseidon2 (8 perms/row), "
                        f"log_n_rows uniform in [12, 20], Poisson arrivals at {rate_per_s}/s",
            "arms": "plain: 1 worker, one launch per column per stage, restated prover; batched_serial: 1 worker, "
-                   "batched stage launches; served: 4 worker processes (own CUDA context and stream each), "
-                   "HBM-budget admission in arrival order, batched stage launches; batched arms prove "
-                   "Wide-Fibonacci requests with the native prover (same bytes)"}
-    for name, workers, plain in (("plain", 1, True), ("batched_serial", 1, False), ("served", 4, False)):
+                   "batched stage launches, native provers; served: 4 worker threads of one process (one CUDA "
+                   "context, a stream each), HBM-budget admission in arrival order, native provers; "
+                   "served_processes: 4 worker processes (a CUDA context each), otherwise the same; every arm "
+                   "gives the same proof bytes"}
+    for name, workers, plain in (("plain", 1, True), ("batched_serial", 1, False), ("served_processes", 4, False)):
         reqs = serving.poisson_requests(n_requests, rate_per_s, 12, 20, seed=5, poseidon_share=0.5)
         svc = serving.ProcessProverService(n_workers=workers, max_log_n_rows=20, plain=plain)
         try:
@@ -558,6 +561,9 @@ def serving_leg(n_requests: int = 24, rate_per_s: float = 200.0):
         finally:
             svc.close()
         out[name] = serving.summarize(done, wall)
+    reqs = serving.poisson_requests(n_requests, rate_per_s, 12, 20, seed=5, poseidon_share=0.5)
+    done, wall = serving.run_stream(4, reqs, max_log=20, native=True)
+    out["served"] = serving.summarize(done, wall)
     out["served_speedup"] = round(out["served"]["proofs_per_s"] / out["plain"]["proofs_per_s"], 3)
     return out
 

@@ -11,16 +11,16 @@ proofs/s and per-request latency (arrival to proof) percentiles.
 
 Two forms:
 - `ProverService` runs its workers as threads of this process, each on its own
-  CUDA stream;
+  CUDA stream. With the native provers (cs_prove_wide_fib, cs_prove_poseidon)
+  a worker leaves the interpreter for the whole proof, so the workers' host
+  code runs on separate cores and their kernels overlap in the one CUDA
+  context. This is the faster form.
 - `ProcessProverService` runs each worker as a spawned process with its own CUDA
-  context and stream. The host-side orchestration of the proofs (the generic
-  prover's loop, the channel, the decommitment assembly) then runs on separate
-  host cores instead of sharing one interpreter.
+  context and stream; the contexts time-slice the device instead of sharing it.
 
 `plain=True` gives the plain form: one launch per column for the per-column
 stages (prover.PlainGpuOps), orchestrated by the restated prover. Otherwise the
-process workers prove requests with the native prover (cs_prove_wide_fib,
-cs_prove_poseidon), whose bytes are the same.
+workers prove requests with the native provers, whose bytes are the same.
 """
 from __future__ import annotations
 
@@ -141,10 +141,13 @@ def _ops(plain: bool):
 
 class ProverService:
     def __init__(self, n_workers: int = 4, hbm_budget: int = 64 << 30, max_log_n_rows: int = 20,
-                 plain: bool = False):
+                 plain: bool = False, native: bool | None = None):
         import torch
         self.torch = torch
         self.ops = _ops(plain)
+        # the native provers release the interpreter for the whole proof, so worker threads prove
+        # concurrently, each on its own stream of the one CUDA context
+        self.native = (not plain) if native is None else native
         # the worker threads share one CUDA context: a graph capture in one of them would stop the
         # others' work, so the FRI layer loop runs eagerly here (worker processes replay graphs)
         self.ops.fri_graphs = False
@@ -160,7 +163,7 @@ class ProverService:
 
     def _prove(self, req: ProofRequest, stream):
         with self.torch.cuda.stream(stream):
-            proof = prove_request(self.ops, self.twiddles, req)
+            proof = prove_request(self.ops, self.twiddles, req, native=self.native)
             stream.synchronize()
         return proof
 
@@ -204,9 +207,11 @@ class ProverService:
             t.join()
 
 
-def run_stream(n_workers: int, requests, hbm_budget: int = 64 << 30, max_log: int = 20, plain: bool = False):
+def run_stream(n_workers: int, requests, hbm_budget: int = 64 << 30, max_log: int = 20, plain: bool = False,
+               native: bool | None = None):
     """Serves a request stream with worker threads; returns (finished requests, wall seconds)."""
-    svc = ProverService(n_workers=n_workers, hbm_budget=hbm_budget, max_log_n_rows=max_log, plain=plain)
+    svc = ProverService(n_workers=n_workers, hbm_budget=hbm_budget, max_log_n_rows=max_log, plain=plain,
+                        native=native)
     svc.start()
     t0 = time.perf_counter()
     for gap, req in requests:

@@ -16,16 +16,18 @@ def built():
 
 
 def test_results_alone_equal_results_in_the_mix():
-    sizes = [8, 11, 9, 12, 8, 10]
-    reqs = [serving.ProofRequest(i, s, 1000 + 7 * i) for i, s in enumerate(sizes)]
+    # worker threads prove with the native provers, concurrently on their own streams; each proof
+    # equals the restated prover's through the plain one-launch-per-column path, proved alone
+    spec = [(8, "wide_fib"), (11, "wide_fib"), (5, "poseidon"), (9, "wide_fib"), (12, "wide_fib"),
+            (6, "poseidon"), (8, "wide_fib"), (10, "wide_fib")]
+    reqs = [serving.ProofRequest(i, s, 1000 + 7 * i, k) for i, (s, k) in enumerate(spec)]
     mixed, _ = serving.run_stream(4, [(0.0, r) for r in reqs], max_log=12)
-    assert all(r.error is None for r in mixed)
-    alone_reqs = [serving.ProofRequest(i, s, 1000 + 7 * i) for i, s in enumerate(sizes)]
-    # alone, and through the plain one-launch-per-column path: the same bytes
+    assert all(r.error is None for r in mixed), [r.error for r in mixed]
+    alone_reqs = [serving.ProofRequest(i, s, 1000 + 7 * i, k) for i, (s, k) in enumerate(spec)]
     alone, _ = serving.run_stream(1, [(0.0, r) for r in alone_reqs], max_log=12, plain=True)
-    by_id = {r.request_id: r.proof.to_bytes() for r in alone}
+    by_id = {r.request_id: r.proof_bytes() for r in alone}
     for r in mixed:
-        assert r.proof.to_bytes() == by_id[r.request_id]
+        assert r.proof_bytes() == by_id[r.request_id]
 
 
 def test_admission_respects_the_budget():
