@@ -561,6 +561,11 @@ def serving_leg(n_requests: int = 24, rate_per_s: float = 200.0):
         finally:
             svc.close()
         out[name] = serving.summarize(done, wall)
+    # warm-up outside the timed stream (the worker processes warm up the same way): the kernels of
+    # every tile size load on their first launch
+    warm = [serving.ProofRequest(-1 - i, log_n, 1 + i, kind)
+            for i, (log_n, kind) in enumerate((l, k) for l in (12, 16, 20) for k in ("wide_fib", "poseidon"))]
+    serving.run_stream(4, [(0.0, r) for r in warm], max_log=20, native=True)
     reqs = serving.poisson_requests(n_requests, rate_per_s, 12, 20, seed=5, poseidon_share=0.5)
     done, wall = serving.run_stream(4, reqs, max_log=20, native=True)
     out["served"] = serving.summarize(done, wall)
@@ -713,11 +718,12 @@ def run_gpu(args):
         wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
         wf_native = wide_fib_prove_native(torch) if not args.skip_prove else []
     bvp = batched_vs_plain(torch, cs) if not args.skip_plain else None
-    serving_res = serving_leg() if not args.skip_serving else None
     with collector_paused():
         poseidon_res = poseidon_prove_leg(torch, args.poseidon_log_rows) if not args.skip_poseidon else None
         mixed_res = mixed_prove_leg(torch) if not args.skip_mixed_prove else None
     gkr_res = gkr_leg(torch) if not args.skip_gkr else None
+    # last: its threaded arm proves in this process, and the other legs measure a fresh state
+    serving_res = serving_leg() if not args.skip_serving else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
