@@ -761,9 +761,10 @@ def run_gpu(args):
                      "achieved": ff(achieved), "peak": hbm, "unit": "GB/s", "frac": ff(achieved / hbm),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json)", "traffic": eval_traffic,
                      "algorithmic_bytes_per_evaluate": eval_bytes, "launches_per_evaluate": 2,
-                     "note": "achieved and traffic are per evaluate (both passes); the passes are integer-pipe "
-                             "bound (ALU pipe ~75% busy), and traffic counts the intermediate of the two-pass "
-                             "FFT written once and read once"},
+                     "note": "achieved and traffic are per evaluate (both passes); the passes are bound by "
+                             "integer issue (about 11.4 thread instructions per butterfly, most of them the "
+                             "M31 multiply-reduce and the two reduced additions), and traffic counts the "
+                             "intermediate of the two-pass FFT written once and read once"},
         "leaves_roofline": {"bound": "hbm", "kernel": "merkle_leaves_kernel", "achieved": ff(leaf_gbs), "peak": hbm,
                             "unit": "GB/s", "frac": ff(leaf_gbs / hbm), "traffic": traffic,
                             "algorithmic_bytes_per_launch": leaf_bytes,
