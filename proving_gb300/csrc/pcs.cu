@@ -182,7 +182,7 @@ __device__ __forceinline__ uint32_t warp_sum4(const uint32_t r[4], uint32_t lane
   return v;
 }
 
-__global__ void __launch_bounds__(kBaryThreads) bary_partial_kernel(const BaryColumns cols, uint32_t nb,
+__global__ void __launch_bounds__(kBaryThreads, 3) bary_partial_kernel(const BaryColumns cols, uint32_t nb,
                                                                    uint32_t log_n, CSoA w,
                                                                    unsigned long long* partial) {
   __shared__ uint32_t sh[kBaryGroup][kBaryThreads / 32][4];
