@@ -573,6 +573,18 @@ def serving_leg(n_requests: int = 24, rate_per_s: float = 200.0):
     return out
 
 
+def replica_throughput(dist, elapsed_ms: float, steps: int, world: int, device="cpu"):
+    """Whole-job throughput of `world` independent replicas (one per GPU, no data-path collective):
+    every rank processed `steps` units, and the job took the slowest rank's time, so the time is
+    the maximum over ranks (an all-reduce, the only collective). Returns (max_ms, units per s)."""
+    import torch
+    t = torch.tensor([float(elapsed_ms)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    return max_ms, world * steps / (max_ms / 1e3)
+
+
 def run_gpu(args):
     import torch
     from proving_gb300 import _lib
@@ -630,11 +642,7 @@ def run_gpu(args):
     stage_ms = {n: statistics.mean(evs[k][i].elapsed_time(evs[k][i + 1]) for k in range(args.steps))
                 for i, n in enumerate(stage_names)}
     step_lat = [evs[k][0].elapsed_time(evs[k][5]) for k in range(args.steps)]
-    t = torch.tensor([elapsed_ms], device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = world * args.steps / (max_ms / 1e3)
+    max_ms, value = replica_throughput(dist, elapsed_ms, args.steps, world, device="cuda")
 
     # ---- e2e through the C ABI with host buffers: every step copies its trace and FRI column from
     # pinned host memory and reads its Merkle root and last FRI value back. Inputs are double
@@ -707,10 +715,7 @@ def run_gpu(args):
         e2e_ms = e_start.elapsed_time(e_end)
         # the root read back by the last step is the resident step's root
         assert bytes(host_out[args.steps - 1, :8].numpy().astype("<i4").tobytes()) == cs.root()
-    t = torch.tensor([e2e_ms], device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = world * args.steps / (float(t.item()) / 1e3)
+    _, e2e_value = replica_throughput(dist, e2e_ms, args.steps, world, device="cuda")
 
     peaks_int = int_peaks(torch)
     from proving_gb300.serving import collector_paused
