@@ -36,7 +36,7 @@ def _rank(rank: int, world: int, port: int, times, out):
 def test_two_replicas_take_the_slowest_rank():
     port = _free_port()
     times = [100.0, 150.0]  # ms of the timed region on each rank
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork from this multi-threaded process
         out = m.dict()
         mp.start_processes(_rank, args=(2, port, times, out), nprocs=2, start_method="spawn")
         res = dict(out)
