@@ -188,8 +188,8 @@ class CommitStage:
         rec(2)
         call("cs_merkle_build_leaves", self.t_ext, self.logs, N_COLS, LOG_EXT, self.layer_ptr[0], st)
         rec(3)
-        for k in range(LOG_EXT, 0, -1):
-            call("cs_merkle_build_next_layer", self.layer_ptr[LOG_EXT - k], k - 1, self.layer_ptr[LOG_EXT - k + 1], st)
+        # every node layer in the commit layout; the layers of up to 2^10 nodes in one launch
+        call("cs_merkle_build_layers", self.layer_ptr[0], LOG_EXT, st)
         rec(4)
         call("cs_fold_circle_into_line", fri_src, FRI_LOG, self.alpha_tabs[0], self.fri_tabs[1],
              self.itw.data_ptr(), self.tw_log, st)

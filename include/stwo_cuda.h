@@ -146,6 +146,12 @@ cs_status cs_merkle_build_leaves(const uint32_t *const *h_cols, const uint32_t *
 cs_status cs_merkle_build_next_layer(const uint32_t *d_prev, uint32_t out_log_size, uint32_t *d_out,
                                      cs_stream stream);
 
+/* The layer loop of MerkleProverLifted::commit (crates/stwo/src/prover/vcs_lifted/prover.rs:35-80)
+   above given leaves: d_layers holds the 2^lifting_log_size leaf digests followed by room for
+   every node layer (2^(L+1) - 1 digests in all, root last, the layout of cs_merkle_commit).
+   Layers of more than 2^10 nodes take one launch each, the rest of the tree one launch. */
+cs_status cs_merkle_build_layers(uint32_t *d_layers, uint32_t lifting_log_size, cs_stream stream);
+
 /* MerkleProverLifted::commit without leaf packing
    (crates/stwo/src/prover/vcs_lifted/prover.rs:35-80): leaves, then every
    node layer, in one call. Columns are sorted here (stable, by log size).

@@ -39,6 +39,7 @@ SIGNATURES = {
     "cs_evaluate_columns": [vp, vp, u32, u32, u32, vp, u32, vp],
     "cs_merkle_build_leaves": [vp, vp, u32, u32, vp, vp],
     "cs_merkle_build_next_layer": [vp, u32, vp, vp],
+    "cs_merkle_build_layers": [vp, u32, vp],
     "cs_merkle_commit": [vp, vp, u32, u32, vp, vp],
     "cs_pack_leaves_input": [vp, u32, vp, vp],
     "cs_fold_line": [vp, u32, vp, vp, vp, u32, vp],

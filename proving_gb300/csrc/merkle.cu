@@ -226,6 +226,25 @@ cs_status merkle_next_layer(const uint32_t* d_prev, uint32_t log_out, uint32_t* 
   return CS_OK;
 }
 
+// Every node layer above the 2^L leaves at d_layers, each right after the one before (leaves
+// first, root last): one launch per layer of more than 2^10 nodes, then the rest in one.
+cs_status merkle_layers(uint32_t* d_layers, uint32_t L, cudaStream_t st) {
+  uint32_t* cur = d_layers;
+  for (uint32_t k = L; k >= 1; k--) {
+    if (k - 1 <= kTopLayersLog) {
+      const uint32_t threads = std::max(32u, std::min(1024u, 1u << (k - 1)));
+      merkle_top_kernel<<<1, threads, 0, st>>>(cur, k, 1u);
+      CS_LAUNCHED("merkle_top_kernel");
+      break;
+    }
+    uint32_t* next = cur + ((size_t)8 << k);
+    const cs_status s = merkle_next_layer(cur, k - 1, next, st);
+    if (s != CS_OK) return s;
+    cur = next;
+  }
+  return CS_OK;
+}
+
 }  // namespace cs
 
 using namespace cs;
@@ -240,6 +259,12 @@ extern "C" cs_status cs_merkle_build_leaves(const uint32_t* const* h_cols, const
 extern "C" cs_status cs_merkle_build_next_layer(const uint32_t* d_prev, uint32_t out_log_size, uint32_t* d_out,
                                                 cs_stream stream) {
   return merkle_next_layer(d_prev, out_log_size, d_out, to_stream(stream));
+}
+
+extern "C" cs_status cs_merkle_build_layers(uint32_t* d_layers, uint32_t lifting_log_size, cs_stream stream) {
+  CS_CHECK_ARG(d_layers != nullptr, "build_layers: null buffer");
+  CS_CHECK_ARG(lifting_log_size <= 29, "build_layers: log size %u too large", lifting_log_size);
+  return merkle_layers(d_layers, lifting_log_size, to_stream(stream));
 }
 
 extern "C" cs_status cs_merkle_commit(const uint32_t* const* h_cols, const uint32_t* h_log_sizes, uint32_t n_cols,
@@ -260,18 +285,5 @@ extern "C" cs_status cs_merkle_commit(const uint32_t* const* h_cols, const uint3
   cudaStream_t st = to_stream(stream);
   cs_status s = merkle_leaves(cols.data(), logs.data(), n_cols, lifting_log_size, d_layers, st);
   if (s != CS_OK) return s;
-  uint32_t* cur = d_layers;
-  for (uint32_t k = lifting_log_size; k >= 1; k--) {
-    if (k - 1 <= kTopLayersLog) {  // the rest of the tree in one launch
-      const uint32_t threads = std::max(32u, std::min(1024u, 1u << (k - 1)));
-      merkle_top_kernel<<<1, threads, 0, st>>>(cur, k, 1u);
-      CS_LAUNCHED("merkle_top_kernel");
-      break;
-    }
-    uint32_t* next = cur + ((size_t)8 << k);
-    s = merkle_next_layer(cur, k - 1, next, st);
-    if (s != CS_OK) return s;
-    cur = next;
-  }
-  return CS_OK;
+  return merkle_layers(d_layers, lifting_log_size, st);
 }
