@@ -21,8 +21,15 @@
  *  - Every function returns a cs_status. On failure, cs_last_error() gives a
  *    message for the calling thread. The reference's trait methods panic on
  *    misuse; its Rust binding panics on a non-OK status to keep that contract.
- *  - All entry points are thread-safe: they keep no mutable global state
- *    beyond the per-thread error message.
+ *  - All entry points are thread-safe. Process-wide state is limited to:
+ *    the per-thread error message; the FFT pass-plan table (cs_fft_set_plan,
+ *    guarded by a lock); per-device set-up flags (kernel shared-memory
+ *    limits, the memory pool's release threshold; set once under a lock);
+ *    the kernel launch counter; and the static slot array of
+ *    cs_grind_blake2s_noalloc (shared by its calls, see there).
+ *  - Digest and layer buffers of the Merkle entry points must be 16-byte
+ *    aligned (digests move as 16-byte words); a misaligned pointer gives
+ *    CS_ERR_INVALID_ARG.
  */
 #ifndef STWO_CUDA_H
 #define STWO_CUDA_H
@@ -602,7 +609,10 @@ cs_status cs_grind_blake2s(const uint8_t digest[32], uint32_t pow_bits, uint64_t
    instead of allocating, so n_digests above 64 is rejected with
    CS_ERR_INVALID_ARG. The first call on a device, with that device current,
    looks up the array's device address; make that call before any stream
-   capture. Calls share the array: calls that overlap on the GPU race.
+   capture. That address stays cached for the life of the process; a
+   cudaDeviceReset unloads the module and leaves it stale, so a process
+   that resets a device must not call this entry point on it afterwards.
+   Calls share the array: calls that overlap on the GPU race.
    Synchronous on `stream`. */
 cs_status cs_grind_blake2s_noalloc(const uint8_t *digests, uint32_t n_digests, uint32_t pow_bits, uint64_t max_nonce,
                                    uint64_t *nonces_out, cs_stream stream);

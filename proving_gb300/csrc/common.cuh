@@ -13,6 +13,11 @@ namespace cs {
 // Column-pointer tables travel as kernel parameters (no device allocation);
 // larger batches are split into several launches by the host wrappers.
 constexpr int kMaxBatch = 256;
+// Per-device set-up flags (kernel attributes, pool settings) are kept for this many ordinals.
+constexpr int kMaxDevices = 64;
+
+// 16-byte alignment of a device pointer, for kernels that move whole digests or tiles as uint4.
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 void set_error(const char* fmt, ...);
 // Counts kernel launches made by this library (reported by cs_kernel_launch_count).

@@ -499,11 +499,20 @@ std::vector<PassPlan> plan_passes(bool inverse, uint32_t log_n, uint32_t n_layer
 template <bool INV, int T, bool OUTER>
 cs_status launch_tile(const FftBatch& b, uint32_t n_cols, const FftPass& p, cudaStream_t st) {
   const size_t smem = (size_t)4 * padded_words<OUTER>(1u << (T + p.c));
-  static bool configured = false;
-  if (!configured) {
-    CS_CUDA(cudaFuncSetAttribute(fft_tile_kernel<INV, T, OUTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 160 * 1024));
-    configured = true;
+  // the shared-memory limit is a per-device attribute of the kernel: raised once per device,
+  // under a lock (several prover threads may launch the first FFT of a device at once)
+  static std::mutex mu;
+  static bool configured[kMaxDevices] = {false};
+  int dev = 0;
+  CS_CUDA(cudaGetDevice(&dev));
+  CS_CHECK_ARG(dev >= 0 && dev < kMaxDevices, "fft: device ordinal %d out of range", dev);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!configured[dev]) {
+      CS_CUDA(cudaFuncSetAttribute(fft_tile_kernel<INV, T, OUTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   160 * 1024));
+      configured[dev] = true;
+    }
   }
   const uint32_t threads = (1u << (T / 2)) << p.c;
   const uint32_t tiles = 1u << (p.log_n - T - p.c);

@@ -12,7 +12,10 @@
 // every GPU that loads this library until the process exits. Host code cannot
 // use the array's name as a device address, so the first call on each device
 // (with that device current) looks the address up with cudaGetSymbolAddress
-// and caches it; make that first call before any stream capture. Every call
+// and caches it; make that first call before any stream capture. The cached
+// address belongs to the device's current context: cudaDeviceReset unloads
+// this module, so after a reset of a device the process must not call this
+// entry point on that device again. Every call
 // shares the array and re-initialises the slots it uses before each search
 // round, so calls that overlap on the GPU (e.g. on two streams) race on it.
 #include <mutex>
@@ -25,7 +28,6 @@ namespace cs {
 namespace {
 
 constexpr uint32_t kNoAllocMaxDigests = 64;
-constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned long long g_grind_slots[kNoAllocMaxDigests];
 

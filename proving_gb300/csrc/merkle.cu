@@ -152,6 +152,7 @@ cs_status merkle_leaves(const uint32_t* const* cols, const uint32_t* log_sizes, 
   CS_CHECK_ARG(n_cols > 0 || L == 0, "build_leaves: an empty tree must have lifting_log_size 0 (got %u)", L);
   CS_CHECK_ARG(L <= 30, "build_leaves: lifting_log_size %u too large", L);
   CS_CHECK_ARG(d_leaves != nullptr, "build_leaves: null output");
+  CS_CHECK_ARG(aligned16(d_leaves), "build_leaves: output not 16-byte aligned (digests are written as 16-byte words)");
   static thread_local LeafParams p;
   p.n_cols = n_cols;
   p.one = 1;
@@ -219,6 +220,8 @@ cs_status merkle_leaves(const uint32_t* const* cols, const uint32_t* log_sizes, 
 cs_status merkle_next_layer(const uint32_t* d_prev, uint32_t log_out, uint32_t* d_out, cudaStream_t st) {
   CS_CHECK_ARG(d_prev != nullptr && d_out != nullptr, "build_next_layer: null buffer");
   CS_CHECK_ARG(log_out <= 29, "build_next_layer: log size %u too large", log_out);
+  CS_CHECK_ARG(aligned16(d_prev) && aligned16(d_out),
+               "build_next_layer: layers must be 16-byte aligned (digests move as 16-byte words)");
   const uint32_t n = 1u << log_out;
   const uint32_t threads = 128;
   merkle_node_kernel<<<(n + threads - 1) / threads, threads, 0, st>>>(d_prev, log_out, d_out, 1u);
@@ -263,7 +266,8 @@ extern "C" cs_status cs_merkle_build_next_layer(const uint32_t* d_prev, uint32_t
 
 extern "C" cs_status cs_merkle_build_layers(uint32_t* d_layers, uint32_t lifting_log_size, cs_stream stream) {
   CS_CHECK_ARG(d_layers != nullptr, "build_layers: null buffer");
-  CS_CHECK_ARG(lifting_log_size <= 29, "build_layers: log size %u too large", lifting_log_size);
+  CS_CHECK_ARG(lifting_log_size <= 30, "build_layers: log size %u too large", lifting_log_size);
+  CS_CHECK_ARG(aligned16(d_layers), "build_layers: layers must be 16-byte aligned (digests move as 16-byte words)");
   return merkle_layers(d_layers, lifting_log_size, to_stream(stream));
 }
 
@@ -271,6 +275,8 @@ extern "C" cs_status cs_merkle_commit(const uint32_t* const* h_cols, const uint3
                                       uint32_t lifting_log_size, uint32_t* d_layers, cs_stream stream) {
   CS_CHECK_ARG(n_cols == 0 || (h_cols != nullptr && h_log_sizes != nullptr), "commit: null column table");
   CS_CHECK_ARG(n_cols <= kMaxLeafCols, "commit: %u columns exceed the limit of %u", n_cols, kMaxLeafCols);
+  CS_CHECK_ARG(d_layers != nullptr && aligned16(d_layers),
+               "commit: layers must be non-null and 16-byte aligned (digests move as 16-byte words)");
   // Stable sort by length (crates/stwo/src/prover/vcs_lifted/prover.rs:68).
   std::vector<uint32_t> order(n_cols);
   std::iota(order.begin(), order.end(), 0u);

@@ -190,3 +190,36 @@ def test_native_prover_checks_arguments_on_host(lib):
     n = ctypes.c_size_t(0)
     assert _status(lib, "cs_prove_wide_fib", ctypes.byref(p), cols, None, 0, ctypes.byref(n), None) == 1
     assert b"columns" in lib.cs_last_error()
+
+
+def test_merkle_entry_points_reject_misaligned_digest_buffers(lib):
+    # digests move as 16-byte words: a 4-byte-aligned offset into a buffer is refused on the host
+    # instead of faulting the device
+    INVALID = 1
+    null = ctypes.c_void_p(0)
+    odd = ctypes.c_void_p((1 << 22) + 4)
+    even = ctypes.c_void_p(1 << 23)
+    assert _status(lib, "cs_merkle_build_layers", odd, 5, null) == INVALID
+    assert b"aligned" in lib.cs_last_error()
+    assert _status(lib, "cs_merkle_build_next_layer", odd, 4, even, null) == INVALID
+    assert b"aligned" in lib.cs_last_error()
+    assert _status(lib, "cs_merkle_build_next_layer", even, 4, odd, null) == INVALID
+    logs = (ctypes.c_uint32 * 1)(5)
+    cols = (ctypes.c_void_p * 1)(1 << 20)
+    assert _status(lib, "cs_merkle_build_leaves", cols, logs, 1, 5, odd, null) == INVALID
+    assert b"aligned" in lib.cs_last_error()
+    assert _status(lib, "cs_merkle_commit", cols, logs, 1, 5, odd, null) == INVALID
+    assert b"aligned" in lib.cs_last_error()
+
+
+def test_merkle_height_limits_agree(lib):
+    # leaves, layers and commit accept trees up to height 30 and refuse 31 (checked before any
+    # device work: a null buffer is refused after the height check)
+    INVALID = 1
+    null = ctypes.c_void_p(0)
+    assert _status(lib, "cs_merkle_build_layers", ctypes.c_void_p(1 << 22), 31, null) == INVALID
+    assert b"too large" in lib.cs_last_error()
+    logs = (ctypes.c_uint32 * 1)(31)
+    cols = (ctypes.c_void_p * 1)(1 << 20)
+    assert _status(lib, "cs_merkle_build_leaves", cols, logs, 1, 31, ctypes.c_void_p(1 << 22), null) == INVALID
+    assert b"too large" in lib.cs_last_error()

@@ -140,6 +140,29 @@ def test_merkle_empty(B):
     assert tree.root() == hashlib.blake2s(b"").digest()
 
 
+@pytest.mark.parametrize("L", [0, 1, 10, 11, 12])
+def test_merkle_build_layers_above_caller_leaves(B, L):
+    # cs_merkle_build_leaves into a caller-owned layer buffer, then cs_merkle_build_layers on it:
+    # L = 11 and 12 take per-layer launches below the single top launch (layers of up to 2^10
+    # nodes), L <= 10 the top launch alone, L = 0 an empty tree whose root is the leaf
+    from proving_gb300 import _lib
+    from proving_gb300.backend import _ptr, _ptr_table, _stream, _u32_table
+    logs = [] if L == 0 else sorted([max(1, L - k % 3) for k in range(20)])
+    cols_np = [m31_column(300 + i, l) for i, l in enumerate(logs)]
+    cols = [_col(c) for c in cols_np]
+    layers = torch.empty(((1 << (L + 1)) - 1, 8), dtype=torch.int32, device="cuda")
+    _lib.call("cs_merkle_build_leaves", _ptr_table([c.data for c in cols]), _u32_table(logs), len(cols), L,
+              _ptr(layers), _stream())
+    _lib.call("cs_merkle_build_layers", _ptr(layers), L, _stream())
+    torch.cuda.synchronize()
+    root, want = O.merkle_commit(cols_np, L, with_layers=True)
+    off = 0
+    for k, w in zip(range(L, -1, -1), want):
+        assert np.array_equal(_digests(layers[off:off + (1 << k)]), w), f"layer {k}"
+        off += 1 << k
+    assert _digests(layers[-1:]).tobytes() == root
+
+
 def test_merkle_next_layer(B):
     prev = np.frombuffer(np.random.default_rng(3).bytes(32 * 64), np.uint8).reshape(64, 32)
     t = torch.from_numpy(prev.copy().view(np.int32).reshape(64, 8)).cuda()
