@@ -9,6 +9,7 @@
 #ifndef STWO_ORACLE_H
 #define STWO_ORACLE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -29,6 +30,8 @@ void orc_qm31_inv(const uint32_t a[4], uint32_t out[4]);
 
 void orc_precompute_twiddles(uint32_t initial_index, uint32_t log_size, uint32_t *tw, uint32_t *itw);
 void orc_interpolate(uint32_t *v, uint32_t log_n, const uint32_t *itw, uint32_t tw_log);
+void orc_interpolate_on(uint32_t *v, uint32_t log_n, const uint32_t *itw, uint32_t tw_log,
+                        uint32_t half_initial_index);
 void orc_evaluate(const uint32_t *coeffs, uint32_t log_coeffs, uint32_t *out, uint32_t log_n,
                   const uint32_t *tw, uint32_t tw_log);
 void orc_interpolate_batch(uint32_t **cols, const uint32_t *log_sizes, uint32_t n_cols,
@@ -94,6 +97,19 @@ void orc_poseidon_interaction(const uint32_t **trace, uint32_t log_n, const uint
 void orc_poseidon_composition(const uint32_t **trace, const uint32_t **inter, uint32_t eval_log, uint32_t trace_log,
                               const uint32_t lookup[8], const uint32_t claimed[4], const uint32_t *rc,
                               uint32_t *const out[4]);
+
+/* whole proofs (oracle_prover.c): the reference's prove_ex flow restated over the ops above.
+   fri = {pow_bits, log_blowup_factor, log_last_layer_degree_bound, n_queries, fold_step}.
+   Return 0 on success, 1 when the sanity check fails (ConstraintsNotSatisfied), 2 when the last
+   FRI layer is not of low degree, -1 for unsupported arguments, -2 when the words do not fit
+   (*n_words is still set). */
+int orc_prove_fib_and_lookups(const uint32_t fri[5], uint32_t n_fib, const uint32_t *fib_n_cols,
+                              const uint32_t *fib_log_sizes, const uint32_t *const *fib_trace,
+                              uint32_t n_lookups, const uint32_t *lookup_log_sizes,
+                              const uint32_t *const *lookup_values, int check, uint32_t *claimed_out,
+                              uint64_t *words, size_t capacity, size_t *n_words);
+int orc_prove_poseidon(const uint32_t fri[5], uint32_t log_n_rows, uint64_t *words, size_t capacity,
+                       size_t *n_words);
 
 #ifdef __cplusplus
 }

@@ -140,6 +140,16 @@ def interpolate(evals, itw: np.ndarray) -> np.ndarray:
     return v
 
 
+def interpolate_on_subdomain(evals, itw_sub: np.ndarray, parent_log_size: int) -> np.ndarray:
+    """Interpolation on the bit-reversed prefix of CanonicCoset(parent_log_size) of the evaluations'
+    size, with that subdomain's twiddle tree (extract_subdomain_twiddles)."""
+    v = _u32(evals).copy()
+    lib().orc_interpolate_on(_p(v), ctypes.c_uint32(v.size.bit_length() - 1), _p(itw_sub),
+                             ctypes.c_uint32(itw_sub.size.bit_length() - 1),
+                             ctypes.c_uint32(canonic_half_coset_initial_index(parent_log_size)))
+    return v
+
+
 def evaluate(coeffs, log_n: int, tw: np.ndarray) -> np.ndarray:
     c = _u32(coeffs)
     out = np.zeros(1 << log_n, np.uint32)
@@ -559,3 +569,58 @@ def logup_composition(values, inter, trace_log: int, z, claimed, rc, out=None):
     lib().orc_logup_composition(_p(v), _ptr_array(it), ctypes.c_uint32(n.bit_length() - 1), ctypes.c_uint32(trace_log),
                                 _p(zz), _p(cl), _p(r), _ptr_array(out))
     return out
+
+
+# ------------------------------------------------------------ whole proofs (oracle_prover.c)
+
+class ProofError(RuntimeError):
+    """A status other than 0 from the oracle's prover (1: constraints not satisfied)."""
+
+
+_PROOF_CAPACITY = 1 << 23
+
+
+def _fri_words(fri):
+    """(pow_bits, log_blowup_factor, log_last_layer_degree_bound, n_queries[, fold_step])."""
+    f = list(fri) + [1] * (5 - len(fri))
+    return np.asarray(f, np.uint32)
+
+
+def prove_fib_and_lookups(fri, fib_traces, fib_log_sizes, lookup_values=(), lookup_log_sizes=(), check=True):
+    """The whole proof of Wide-Fibonacci components (fib_traces[k]: the columns of component k,
+    evaluations on its trace domain) and single-column LogUp components (their looked-up values),
+    by the oracle's restatement of prove_ex. Returns (proof bytes as u64 LE felts, claimed sums)."""
+    cols = [_u32(c) for t in fib_traces for c in t]
+    n_cols = _u32([len(t) for t in fib_traces])
+    logs = _u32(list(fib_log_sizes))
+    vals = [_u32(v) for v in lookup_values]
+    llogs = _u32(list(lookup_log_sizes)) if len(lookup_log_sizes) else np.zeros(1, np.uint32)
+    claimed = np.zeros((max(1, len(vals)), 4), np.uint32)
+    words = np.zeros(_PROOF_CAPACITY, np.uint64)
+    n = ctypes.c_size_t(0)
+    fw = _fri_words(fri)
+    L = lib()
+    L.orc_prove_fib_and_lookups.restype = ctypes.c_int
+    rc = L.orc_prove_fib_and_lookups(_p(fw), ctypes.c_uint32(len(fib_traces)), _p(n_cols), _p(logs),
+                                     _ptr_array(cols) if cols else None, ctypes.c_uint32(len(vals)), _p(llogs),
+                                     _ptr_array(vals) if vals else None, ctypes.c_int(1 if check else 0),
+                                     _p(claimed), _p(words), ctypes.c_size_t(words.size), ctypes.byref(n))
+    if rc != 0:
+        raise ProofError(f"orc_prove_fib_and_lookups returned {rc}")
+    return (words[:n.value].astype("<u8").tobytes(),
+            [tuple(int(x) for x in row) for row in claimed[:len(vals)]])
+
+
+def prove_poseidon(fri, log_n_rows: int) -> bytes:
+    """The Poseidon2 AIR's proof at 2^log_n_rows rows by the oracle's restatement of prove_ex (the
+    words the reference computes before its sanity check, which this AIR fails when lifted)."""
+    words = np.zeros(_PROOF_CAPACITY, np.uint64)
+    n = ctypes.c_size_t(0)
+    fw = _fri_words(fri)
+    L = lib()
+    L.orc_prove_poseidon.restype = ctypes.c_int
+    rc = L.orc_prove_poseidon(_p(fw), ctypes.c_uint32(log_n_rows), _p(words), ctypes.c_size_t(words.size),
+                              ctypes.byref(n))
+    if rc != 0:
+        raise ProofError(f"orc_prove_poseidon returned {rc}")
+    return words[:n.value].astype("<u8").tobytes()

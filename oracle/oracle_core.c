@@ -138,7 +138,17 @@ static void layer_loop(uint32_t *v, uint32_t i, uint64_t h, m31 t, int inverse) 
  * root coset is a canonic half coset of log >= log_n - 1.
  */
 void orc_interpolate(uint32_t *v, uint32_t log_n, const uint32_t *itw, uint32_t tw_log) {
-    coset_t half = canonic_half_coset(log_n);
+    orc_interpolate_on(v, log_n, itw, tw_log, canonic_half_coset(log_n).initial_index);
+}
+
+/* interpolate on a circle domain whose half coset starts at half_initial_index: a canonic domain,
+   or a subdomain (bit-reversed prefix) of one, e.g. CanonicCoset(L).split(b).0 in
+   compute_quotients_and_combine. Domains of log size 1 and 2 use that first point directly, as
+   the CPU backend does with eval.domain.half_coset.initial (cpu/circle.rs:34-58); larger ones read
+   the twiddle tree, which carries the domain. */
+void orc_interpolate_on(uint32_t *v, uint32_t log_n, const uint32_t *itw, uint32_t tw_log,
+                        uint32_t half_initial_index) {
+    coset_t half = coset_new(half_initial_index, log_n - 1);
     uint64_t n = 1ull << log_n;
     if (log_n == 1) {
         m31 y = half.initial.y, nn = 2;

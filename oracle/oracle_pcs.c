@@ -332,8 +332,9 @@ void orc_logup_composition(const uint32_t *values, const uint32_t *const inter[4
     qm31 z = qm31_from_words(z_w), rc = qm31_from_words(rc_w);
     qm31 shift = qm31_mul_m31(qm31_from_words(claimed_w), m31_inv((m31)((1ull << trace_log) % M31_P)));
     uint64_t n = 1ull << eval_log;
-    for (uint64_t r = 0; r < n; r++) {
-        uint64_t pr = orc_prev_row(r, trace_log, eval_log);
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < (int64_t)n; r++) {
+        uint64_t pr = orc_prev_row((uint64_t)r, trace_log, eval_log);
         qm31 cur = soa_at(inter, r), prev = soa_at(inter, pr);
         qm31 shifted = qm31_add(qm31_sub(cur, prev), shift);
         qm31 cons = qm31_add(qm31_mul(shifted, qm31_sub(qm31_from_m31(values[r]), z)), qm31_from_m31(1));

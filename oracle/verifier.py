@@ -82,6 +82,8 @@ def merkle_verify(root, height, column_log_sizes, query_positions, queried_value
     """MerkleVerifierLifted::verify (crates/stwo/src/core/vcs_lifted/verifier.rs:107-200)."""
     if height == 0:
         return
+    if len(queried_values) != len(column_log_sizes) or any(len(v) != len(query_positions) for v in queried_values):
+        raise VerificationError("queried values do not match the columns and queries")
     order = sorted(range(len(column_log_sizes)), key=lambda i: column_log_sizes[i])
     by_pos = {}
     for k, pos in enumerate(query_positions):
@@ -398,3 +400,68 @@ def _verify_values(proof, ch, sample_points, sizes, heights):
     for e in evals:
         if e != tuple(proof.fri_last_layer_poly[0]):
             raise VerificationError("last layer evaluations invalid")
+
+
+# ---------------------------------------------------------------- proof bytes
+
+class _FriParams:
+    def __init__(self, pow_bits, log_blowup_factor, log_last_layer_degree_bound, n_queries, fold_step):
+        self.pow_bits, self.log_blowup_factor = pow_bits, log_blowup_factor
+        self.log_last_layer_degree_bound, self.n_queries, self.fold_step = (log_last_layer_degree_bound, n_queries,
+                                                                           fold_step)
+
+
+class _PcsConfig:
+    def __init__(self, fri_params, trace_lifting_log_size):
+        self.fri_params, self.trace_lifting_log_size = fri_params, trace_lifting_log_size
+
+
+class ParsedProof:
+    """A StarkProof read back from its CairoSerialize felt stream (crates/cairo-serialize/src/
+    serialize.rs:99-210). Every vector carries its length, so the stream is self-describing; the
+    lifting log size is not serialized and is given by the statement."""
+
+
+def parse_proof(data: bytes, trace_lifting_log_size: int) -> ParsedProof:
+    w = np.frombuffer(data, "<u8").astype(np.uint64)
+    pos = [0]
+
+    def take():
+        if pos[0] >= len(w):
+            raise VerificationError("truncated proof")
+        v = int(w[pos[0]])
+        pos[0] += 1
+        return v
+
+    def vec(f):
+        n = take()
+        if n > len(w) - pos[0]:
+            raise VerificationError("vector length beyond the proof")
+        return [f() for _ in range(n)]
+
+    def hsh():
+        return struct.pack("<8I", *[take() for _ in range(8)])
+
+    def q():
+        return tuple(take() for _ in range(4))
+
+    p = ParsedProof()
+    p.config = _PcsConfig(_FriParams(*[take() for _ in range(5)]), trace_lifting_log_size)
+    p.commitments = vec(hsh)
+    p.oods_proof_of_work = take()
+    p.sampled_values = vec(lambda: vec(lambda: vec(q)))
+    p.decommitments = vec(lambda: vec(hsh))
+    p.queried_values = vec(lambda: vec(lambda: vec(take)))
+
+    def layer():
+        return {"fri_witness": vec(q), "decommitment": vec(hsh), "commitment": hsh()}
+
+    p.fri_first_layer = layer()
+    p.fri_inner_layers = vec(layer)
+    p.fri_last_layer_poly = vec(q)
+    if take() != len(p.fri_last_layer_poly).bit_length() - 1:
+        raise VerificationError("last layer log size")
+    p.fri_proof_of_work = take()
+    if pos[0] != len(w):
+        raise VerificationError("trailing words after the proof")
+    return p

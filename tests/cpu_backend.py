@@ -1,14 +1,15 @@
-"""ORACLE — test infrastructure only: the device operations of the host
-prover (proving_gb300.prover) implemented with the CPU oracle, so the same
-prover code can run on the CPU restatement and on the GPU and the two proofs
-can be compared byte for byte."""
+"""Test helper: the device operations of the restated host prover
+(proving_gb300.prover) implemented with the CPU oracle's ops, so that host
+prover can run without a GPU (CPU tests of its orchestration). Proof-level
+parity does not rest on this: the oracle's own prover (oracle/oracle_prover.c)
+is the independent statement the GPU proofs are compared with."""
 from __future__ import annotations
 
 import numpy as np
 
 from proving_gb300 import prover as pr
 
-from . import oracle as O
+from oracle import oracle as O
 
 
 class Col:
@@ -192,7 +193,7 @@ class CpuOps:
     def compute_quotients_and_combine(self, parts, points, fls, lifting, log_blowup, tw):
         sub = O.quotients_on_subdomain([p.c for p in parts], points, fls, lifting, log_blowup)
         sub_itw = O.extract_subdomain_twiddles(tw.itw, lifting, lifting - log_blowup)
-        return SCol([O.evaluate(O.interpolate(c, sub_itw), lifting, tw.tw) for c in sub])
+        return SCol([O.evaluate(O.interpolate_on_subdomain(c, sub_itw, lifting), lifting, tw.tw) for c in sub])
 
     def fold_circle_into_line(self, col, alpha, tw):
         return SCol(O.fold_circle_into_line(col.c, alpha))

@@ -1,4 +1,4 @@
-"""ORACLE — test infrastructure only: the CPU backend's GkrOps and MleOps
+"""Test helper: the CPU backend's GkrOps and MleOps
 (crates/stwo/src/prover/backend/cpu/lookups/gkr.rs, cpu/lookups/mle.rs)
 restated over numpy arrays, with the methods of proving_gb300.gkr.DeviceGkrOps,
 so the GKR driver runs on it and on the device and the two proofs can be

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from oracle.gkr_cpu import CpuGkrOps, mle_eval_at_point
+from gkr_cpu_backend import CpuGkrOps, mle_eval_at_point
 from oracle.gkr_verifier import GRAND_PRODUCT, LOGUP, GkrError, partially_verify_batch
 from proving_gb300 import gkr as G
 from proving_gb300 import prover as pr

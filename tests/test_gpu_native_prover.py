@@ -1,5 +1,8 @@
-"""The native prover (cs_prove_wide_fib: the generic prover's loop in C++ over the library's kernels)
-gives the proof bytes of the restated prover on the same backend and of the oracle backend."""
+"""The native provers (cs_prove_wide_fib, cs_prove_fib_and_lookups, cs_prove_poseidon: the generic
+prover's loop in C++ over the library's kernels) against the oracle's own prover
+(oracle/oracle_prover.c, the reference's prove_ex restated in C, sharing no code with the product):
+byte-identical proofs, which the restated verifier accepts. Small shapes here, including edge
+sizes; the BASELINE-size proofs are in test_gpu_proof_parity_full.py."""
 import numpy as np
 import pytest
 
@@ -7,8 +10,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 from oracle import oracle as O  # noqa: E402
-from oracle.cpu_ops import CpuOps  # noqa: E402
-from oracle.verifier import verify_wide_fib_components  # noqa: E402
+from oracle.verifier import parse_proof, verify_fib_and_lookups, verify_wide_fib_components  # noqa: E402
 from proving_gb300 import prover as pr  # noqa: E402
 from proving_gb300.synthetic import m31_column  # noqa: E402
 
@@ -27,28 +29,19 @@ def _traces(shape, seed):
 
 
 @pytest.mark.parametrize("shape,n_queries", [([(100, 4)], 70), ([(100, 7)], 70), ([(100, 14)], 70),
-                                             ([(4, 9), (5, 3)], 3), ([(10, 6), (3, 6), (7, 11)], 20)])
-def test_native_proof_bytes_equal_restated_prover(B, shape, n_queries):
+                                             ([(4, 9), (5, 3)], 3), ([(10, 6), (3, 6), (7, 11)], 20),
+                                             ([(3, 2)], 5), ([(5, 2), (3, 1)], 9)])
+def test_native_proof_bytes_equal_oracle_prover(B, shape, n_queries):
     from proving_gb300.backend import BaseColumn
     host = _traces(shape, 50)
     logs = [l for _, l in shape]
     L = max(logs) + 1
-    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=n_queries, fold_step=1)
-    cfg = pr.PcsConfig(fp, trace_lifting_log_size=L)
-    ops = pr.GpuOps()
-    tw = ops.twiddles(L + 1)
+    tw = pr.GpuOps().twiddles(L + 1)
     native = B.prove_wide_fib_native([[BaseColumn.from_cpu(c) for c in t] for t in host], logs,
-                                     (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound,
-                                      fp.n_queries), tw)
-    restated = pr.prove_wide_fib_components(ops, [ops.columns_from_host(t) for t in host], logs, cfg,
-                                            pr.Blake2sChannel(), tw)
-    assert native == restated.to_bytes()
-    if max(logs) <= 10:
-        cpu = CpuOps()
-        oracle = pr.prove_wide_fib_components(cpu, [cpu.columns_from_host(t) for t in host], logs, cfg,
-                                              pr.Blake2sChannel(), cpu.twiddles(L + 1))
-        assert native == oracle.to_bytes()
-        verify_wide_fib_components(restated, [n for n, _ in shape], logs)
+                                     (10, 1, 0, n_queries), tw)
+    want, _ = O.prove_fib_and_lookups((10, 1, 0, n_queries, 1), host, logs)
+    assert native == want
+    verify_wide_fib_components(parse_proof(native, L), [n for n, _ in shape], logs)
 
 
 def _fib_lookup_inputs(shape, lookup_logs, seed):
@@ -59,34 +52,40 @@ def _fib_lookup_inputs(shape, lookup_logs, seed):
 
 
 @pytest.mark.parametrize("shape,lookup_logs,n_queries", [([(4, 9), (5, 3)], [8, 4], 3),
-                                                         ([(10, 5), (3, 8)], [8, 2, 5, 8], 70)])
-def test_native_fib_and_lookups_equal_restated_prover(B, shape, lookup_logs, n_queries):
+                                                         ([(10, 5), (3, 8)], [8, 2, 5, 8], 70),
+                                                         ([(3, 3)], [11, 1], 17)])
+def test_native_fib_and_lookups_equal_oracle_prover(B, shape, lookup_logs, n_queries):
     from proving_gb300.backend import BaseColumn
     host, values = _fib_lookup_inputs(shape, lookup_logs, 7)
     logs = [l for _, l in shape]
     L = max(logs + lookup_logs) + 1
-    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=n_queries, fold_step=1)
-    cfg = pr.PcsConfig(fp, trace_lifting_log_size=L)
-    ops = pr.GpuOps()
-    tw = ops.twiddles(L + 1)
+    tw = pr.GpuOps().twiddles(L + 1)
     native, claimed = B.prove_fib_and_lookups_native(
         [[BaseColumn.from_cpu(c) for c in t] for t in host], logs, [BaseColumn.from_cpu(v) for v in values],
-        lookup_logs, (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound, fp.n_queries), tw)
-    restated = pr.prove_fib_and_lookups(ops, [ops.columns_from_host(t) for t in host], logs,
-                                        [ops.columns_from_host([v])[0] for v in values], lookup_logs, cfg,
-                                        pr.Blake2sChannel(), tw)
-    assert claimed == restated.claimed_sums
-    assert native == restated.to_bytes()
+        lookup_logs, (10, 1, 0, n_queries), tw)
+    want, want_claimed = O.prove_fib_and_lookups((10, 1, 0, n_queries, 1), host, logs, values, lookup_logs)
+    assert claimed == want_claimed
+    assert native == want
+    verify_fib_and_lookups(parse_proof(native, L), [n for n, _ in shape], logs, lookup_logs, claimed)
 
 
 @pytest.mark.parametrize("log_n", [4, 7])
-def test_native_poseidon_equals_restated_prover(B, log_n):
-    from proving_gb300 import poseidon as ps
-    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
-    cfg = ps.poseidon_pcs_config(log_n + 3, fp)
+def test_native_poseidon_equals_oracle_prover(B, log_n):
+    tw = pr.GpuOps().twiddles(log_n + 3)
+    native = B.prove_poseidon_native(log_n, (10, 1, 0, 70), tw)
+    assert native == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
+
+
+@pytest.mark.parametrize("log_n", [4, 9])
+def test_restated_host_prover_equals_native(B, log_n):
+    # the restated (Python) host prover on the same kernels gives the native prover's bytes
+    from proving_gb300.backend import BaseColumn
+    host = _traces([(20, log_n)], 3)
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=30, fold_step=1)
     ops = pr.GpuOps()
-    tw = ops.twiddles(log_n + 3)
-    native = B.prove_poseidon_native(log_n, (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound,
-                                             fp.n_queries), tw)
-    restated = ps.prove_poseidon(ops, log_n, cfg, pr.Blake2sChannel(), tw, check=False)
+    tw = ops.twiddles(log_n + 2)
+    native = B.prove_wide_fib_native([[BaseColumn.from_cpu(c) for c in t] for t in host], [log_n], (10, 1, 0, 30), tw)
+    restated = pr.prove_wide_fib_components(ops, [ops.columns_from_host(t) for t in host], [log_n],
+                                            pr.PcsConfig(fp, trace_lifting_log_size=log_n + 1), pr.Blake2sChannel(),
+                                            tw)
     assert native == restated.to_bytes()

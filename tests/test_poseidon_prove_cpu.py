@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from oracle.cpu_ops import CpuOps
+from cpu_backend import CpuOps
 from proving_gb300 import poseidon as ps
 from proving_gb300 import prover as pr
 from proving_gb300.synthetic import seeded_qm31

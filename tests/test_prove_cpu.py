@@ -7,7 +7,7 @@ import copy
 import pytest
 
 from oracle import oracle as O
-from oracle.cpu_ops import CpuOps
+from cpu_backend import CpuOps
 from oracle.verifier import VerificationError, verify_wide_fib
 from proving_gb300 import prover as pr
 from proving_gb300.synthetic import m31_column
@@ -85,20 +85,26 @@ def test_felt_stream_follows_cairo_serialize():
     assert len(proof.to_bytes()) == 8 * len(w)
 
 
-def lifted_components_proof(ops):
+def lifted_components_inputs():
     # test_e2e_lifted_fib_prove (crates/examples/src/wide_fibonacci/mod.rs:495-577): components of
     # 4 columns x 2^9 and 5 columns x 2^3, inputs a = 1, b = row (generate_test_inputs, :130-134),
     # FriParams::test_params() = (pow 10, last layer 0, blowup 1, 3 queries, fold step 1), tree
-    # height 9 + 1
+    # height 9 + 1. Returns (host traces, log sizes, FRI parameters).
     import numpy as np
     traces = []
     for n_cols, log_n in ((4, 9), (5, 3)):
         a = np.ones(1 << log_n, np.uint32)
         b = np.arange(1 << log_n, dtype=np.uint32)
-        traces.append(ops.columns_from_host(O.wide_fib_trace(a, b, n_cols)))
+        traces.append(O.wide_fib_trace(a, b, n_cols))
+    return traces, [9, 3], (10, 1, 0, 3, 1)
+
+
+def lifted_components_proof(ops):
+    traces, logs, _ = lifted_components_inputs()
     fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=3, fold_step=1)
     cfg = pr.PcsConfig(fp, trace_lifting_log_size=9 + 1)
-    return pr.prove_wide_fib_components(ops, traces, [9, 3], cfg, pr.Blake2sChannel(), ops.twiddles(10))
+    return pr.prove_wide_fib_components(ops, [ops.columns_from_host(t) for t in traces], logs, cfg,
+                                        pr.Blake2sChannel(), ops.twiddles(10))
 
 
 def test_lifted_components_prove_then_verify():
@@ -113,21 +119,24 @@ def test_lifted_components_prove_then_verify():
         verify_wide_fib_components(bad, [4, 5], [9, 3])
 
 
-def fib_and_lookups_proof(ops):
+def fib_and_lookups_inputs():
     # the mixed-size batched trace in one proof: Wide-Fibonacci components of 4 columns x 2^9 and
-    # 5 columns x 2^3, and single-column LogUp components of 2^8 and 2^4 rows (seeded values)
+    # 5 columns x 2^3, and single-column LogUp components of 2^8 and 2^4 rows (seeded values).
+    # Returns (host traces, log sizes, lookup values, lookup log sizes, FRI parameters).
     import numpy as np
-    traces = []
-    for n_cols, log_n in ((4, 9), (5, 3)):
-        a = np.ones(1 << log_n, np.uint32)
-        b = np.arange(1 << log_n, dtype=np.uint32)
-        traces.append(ops.columns_from_host(O.wide_fib_trace(a, b, n_cols)))
+    traces, logs, _ = lifted_components_inputs()
     rng = np.random.default_rng(7)
-    lookups = [ops.columns_from_host([rng.integers(0, O.P, 1 << n, dtype=np.uint32)])[0] for n in (8, 4)]
+    values = [rng.integers(0, O.P, 1 << n, dtype=np.uint32) for n in (8, 4)]
+    return traces, logs, values, [8, 4], (10, 1, 0, 3, 1)
+
+
+def fib_and_lookups_proof(ops):
+    traces, logs, values, lookup_logs, _ = fib_and_lookups_inputs()
     fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=3, fold_step=1)
     cfg = pr.PcsConfig(fp, trace_lifting_log_size=9 + 1)
-    return pr.prove_fib_and_lookups(ops, traces, [9, 3], lookups, [8, 4], cfg, pr.Blake2sChannel(),
-                                    ops.twiddles(10))
+    return pr.prove_fib_and_lookups(ops, [ops.columns_from_host(t) for t in traces], logs,
+                                    [ops.columns_from_host([v])[0] for v in values], lookup_logs, cfg,
+                                    pr.Blake2sChannel(), ops.twiddles(10))
 
 
 def test_fib_and_lookups_prove_then_verify():
