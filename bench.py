@@ -1,10 +1,13 @@
-"""Commit-stage microbenchmark of the Stwo prover hot path on GB300.
+"""Commit-stage microbenchmark of the Stwo prover hot path on GB300, with the proof
+configurations beside it.
 
-Workload (one step = one "proof" of the commit stage):
+Headline workload (one step = one commit stage, config 2 of the benchmark plan):
   256 M31 columns of 2^20 rows (uniform in [0, P), seeded), interpolate, evaluate
   on the 4x blown-up canonic domain (log 22), lifted Blake2s Merkle tree over the
   256-wide leaves (height 22), then 22 FRI folds (fold_circle_into_line + 21
   fold_line) of a seeded QM31 column of log 22 with seeded QM31 challenges.
+  The unit is commit steps/s: a step is not a whole proof. Whole proofs (configs
+  1, 3, 4 and the serving mix, 5) are reported in proofs/s with p50/p99 beside it.
 
 `value` times the step with the trace already resident in HBM; `e2e` times the
 same step through the C ABI with the trace in pinned host memory, including the
@@ -13,8 +16,10 @@ Merkle root and the last FRI value. The trace (1 GiB) and the extended
 evaluation (4 GiB) exceed L2 (129 MB), so no L2 flush is needed between steps.
 
 --impl reference times the CPU restatement of the reference (the oracle; the
-Rust reference cannot be built here) on a bounded sample of the same
-workload, with all host threads, extrapolated per stage to the full step.
+Rust reference cannot be built: no cargo here or on the GPU machine) on whole steps
+of the same workload, with all host threads. --gpus N starts N replicas (one
+process per GPU, torch.distributed.run) when it is not already running under a
+launcher.
 """
 from __future__ import annotations
 
@@ -36,7 +41,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "proofs/s, p50/p99 prove latency on 1 GB300: batched vs plain CUDA, bit-exact"
-UNIT = "proofs/s"
+UNIT = "commit steps/s"
+PROOF_UNIT = "proofs/s"
 N_COLS, LOG_ROWS, LOG_BLOWUP = 256, 20, 2
 LOG_EXT = LOG_ROWS + LOG_BLOWUP
 FRI_LOG = 22
@@ -597,6 +603,10 @@ def run_gpu(args):
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+        # replicas hold every GPU while they run: only the headline step and its end-to-end form are
+        # timed, the per-config legs run in single-GPU runs
+        for leg in ("skip_prove", "skip_plain", "skip_poseidon", "skip_mixed_prove", "skip_gkr", "skip_serving"):
+            setattr(args, leg, True)
     else:
         dist = None
         torch.cuda.set_device(0)
@@ -748,7 +758,8 @@ def run_gpu(args):
     leaf_comp = (1 << LOG_EXT) * ((N_COLS * 4 + 63) // 64)
     traffic = LEAVES_TRAFFIC_BYTES if default_shape else None
     fold_bytes = 16 * (1 << FRI_LOG) + 16 * (1 << (FRI_LOG - 1)) + 16 * (1 << (FRI_LOG - 1)) + 16
-    cpu = cpu_baseline(args) if not args.no_cpu_baseline else None
+    # the CPU baseline is timed once, on rank 0 of a single-GPU run
+    cpu = cpu_baseline(args) if not args.no_cpu_baseline and world == 1 else None
     ff = lambda x: float(f"{x:.6g}")
     res = {
         "metric": METRIC, "value": ff(value), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -817,45 +828,101 @@ def run_gpu(args):
 
 # ----------------------------------------------------------------- CPU arm
 
-def cpu_sample_times(n_fft_cols: int = 32, leaf_log: int = 17):
-    """Times the oracle on a bounded sample; returns per-stage seconds scaled to one full step."""
+class CpuCommitStage:
+    """The commit-stage step on the oracle (the C restatement of the reference's CPU backend, run
+    with OpenMP on every host core): the whole workload, no sampling. As the reference's
+    interpolate consumes its evaluations, each step interpolates a fresh copy of the trace in
+    place; the copy is made before the step's clock starts."""
+
+    def __init__(self, seed: int = 11):
+        from oracle import oracle as O
+        from proving_gb300.synthetic import m31_columns, qm31_column, seeded_qm31
+        self.O = O
+        self.evals = m31_columns(seed, N_COLS, LOG_ROWS)
+        self.work = np.empty_like(self.evals)
+        self.ext = np.empty((N_COLS, 1 << LOG_EXT), np.uint32)
+        self.tw, self.itw = O.canonic_twiddles(LOG_EXT + 1)
+        self.fri = qm31_column(seed + 2, FRI_LOG)
+        self.alphas = [seeded_qm31(k) for k in range(FRI_LOG)]
+        vp = ctypes.c_void_p
+        self.t_work = (vp * N_COLS)(*[self.work[i].ctypes.data for i in range(N_COLS)])
+        self.t_ext = (vp * N_COLS)(*[self.ext[i].ctypes.data for i in range(N_COLS)])
+        self.logs_in = np.full(N_COLS, LOG_ROWS, np.uint32)
+        self.logs_ext = np.full(N_COLS, LOG_EXT, np.uint32)
+
+    def step(self):
+        """One step; returns (seconds per stage, Merkle root)."""
+        O, lib, c32 = self.O, self.O.lib(), ctypes.c_uint32
+        np.copyto(self.work, self.evals)
+        t0 = time.perf_counter()
+        lib.orc_interpolate_batch(self.t_work, O._p(self.logs_in), c32(N_COLS), O._p(self.itw),
+                                  c32(self.itw.size.bit_length() - 1))
+        t1 = time.perf_counter()
+        lib.orc_evaluate_batch(self.t_work, O._p(self.logs_in), self.t_ext, O._p(self.logs_ext), c32(N_COLS),
+                               O._p(self.tw), c32(self.tw.size.bit_length() - 1))
+        t2 = time.perf_counter()
+        root = O.merkle_commit(list(self.ext), LOG_EXT)  # leaves + node layers over 2^LOG_EXT leaves
+        t3 = time.perf_counter()
+        lay = O.fold_circle_into_line(self.fri, self.alphas[0])
+        init = O.line_domain_initial_index(FRI_LOG - 1)
+        for k in range(1, FRI_LOG):
+            lay = O.fold_line(lay, init, self.alphas[k])
+            init = O.double_index(init)
+        t4 = time.perf_counter()
+        return {"interpolate": t1 - t0, "evaluate": t2 - t1, "merkle": t3 - t2, "fri_folds": t4 - t3}, root
+
+
+def cpu_proof_times(mixed: bool = True, poseidon_log_rows: int = 18):
+    """Whole proofs on the oracle's own prover (oracle/oracle_prover.c, every host core): config 1
+    (Wide-Fibonacci 100 x 2^14), config 4 (Poseidon2 at 2^poseidon_log_rows rows) and, when asked,
+    config 3 (the 600 + 120-column mixed trace). The same proof bytes as the GPU provers (checked in
+    tests/test_gpu_proof_parity_full.py). Returns proofs/s and latencies per config."""
     from oracle import oracle as O
-    from proving_gb300.synthetic import m31_columns, qm31_column, seeded_qm31
-    tw, itw = O.canonic_twiddles(LOG_EXT + 1)
-    evals = list(m31_columns(11, n_fft_cols, LOG_ROWS))
+    from proving_gb300.synthetic import m31_column, mixed_trace_shape
+    fri = (10, 1, 0, 70, 1)
+    out = {}
+    lat = []
+    for k in range(6):
+        tr = [O.wide_fib_trace(m31_column(100 + k, 14), m31_column(200 + k, 14), 100)]
+        t0 = time.perf_counter()
+        O.prove_fib_and_lookups(fri, tr, [14])
+        if k:
+            lat.append(time.perf_counter() - t0)
+    out["wide_fib_100x2^14"] = {"proofs_per_s": round(1 / statistics.median(lat), 3),
+                                "p50_ms": round(1e3 * statistics.median(lat), 2), "proofs": len(lat)}
     t0 = time.perf_counter()
-    coeffs = O.interpolate_batch(evals, itw)
-    t1 = time.perf_counter()
-    O.evaluate_batch(coeffs, [LOG_EXT] * n_fft_cols, tw)
-    t2 = time.perf_counter()
-    leaf_cols = list(m31_columns(12, N_COLS, leaf_log))
-    t3 = time.perf_counter()
-    O.merkle_commit(leaf_cols, leaf_log)  # leaves + node layers over 2^leaf_log leaves
-    t4 = time.perf_counter()
-    fri = qm31_column(13, FRI_LOG)
-    t5 = time.perf_counter()
-    lay = O.fold_circle_into_line(fri, seeded_qm31(0))
-    init = O.line_domain_initial_index(FRI_LOG - 1)
-    for k in range(1, FRI_LOG):
-        lay = O.fold_line(lay, init, seeded_qm31(k))
-        init = O.double_index(init)
-    t6 = time.perf_counter()
-    fft_scale = N_COLS / n_fft_cols
-    leaf_scale = (1 << LOG_EXT) / (1 << leaf_log)
-    stages = {"interpolate": (t1 - t0) * fft_scale, "evaluate": (t2 - t1) * fft_scale,
-              "merkle": (t4 - t3) * leaf_scale, "fri_folds": t6 - t5}
-    sample = (f"oracle on {n_fft_cols}/{N_COLS} columns for interpolate+evaluate, {N_COLS} cols x 2^{leaf_log} "
-              f"leaves for the Merkle tree (1/{int(leaf_scale)} of the leaves), the full 22-fold FRI chain; "
-              f"each stage scaled to the full step")
-    return stages, sample
+    O.prove_poseidon(fri, poseidon_log_rows)
+    dt = time.perf_counter() - t0
+    out[f"poseidon_2^{poseidon_log_rows}_rows"] = {"proofs_per_s": round(1 / dt, 4), "ms": round(1e3 * dt, 1),
+                                                   "proofs": 1}
+    if mixed:
+        comps, lookup_logs = mixed_trace_shape()
+        traces = [O.wide_fib_trace(m31_column(300 + i, l), m31_column(400 + i, l), n) for i, (n, l) in enumerate(comps)]
+        values = [m31_column(500 + k, l) for k, l in enumerate(lookup_logs)]
+        t0 = time.perf_counter()
+        O.prove_fib_and_lookups(fri, traces, [l for _, l in comps], values, lookup_logs)
+        dt = time.perf_counter() - t0
+        out["mixed_600+120_cols"] = {"proofs_per_s": round(1 / dt, 4), "ms": round(1e3 * dt, 1), "proofs": 1}
+    return out
 
 
 def cpu_baseline(args):
+    """The reported CPU baseline of the GPU arm: two whole commit-stage steps of the oracle after one
+    warm-up step (about 10 s on 16 cores), and the oracle prover's whole proofs."""
     from oracle import oracle as O
-    stages, sample = cpu_sample_times()
-    total = sum(stages.values())
-    return {"value": float(f"{1.0 / total:.6g}"), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
-            "sample": sample, "stages_s": {k: float(f"{v:.4g}") for k, v in stages.items()}}
+    st = CpuCommitStage()
+    st.step()
+    times = [st.step()[0] for _ in range(2)]
+    total = statistics.mean(sum(t.values()) for t in times)
+    stages = {k: statistics.mean(t[k] for t in times) for k in times[0]}
+    res = {"value": float(f"{1.0 / total:.6g}"), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+           "sample": f"2 whole steps ({N_COLS} x 2^{LOG_ROWS} interpolate, evaluate on 2^{LOG_EXT}, the full "
+                     f"height-{LOG_EXT} tree, {FRI_LOG} folds) after 1 warm-up step; nothing extrapolated",
+           "stages_s": {k: float(f"{v:.4g}") for k, v in stages.items()}}
+    if not args.skip_cpu_proofs:
+        res["proofs"] = cpu_proof_times(mixed=not args.skip_cpu_mixed_proof, poseidon_log_rows=args.poseidon_log_rows)
+        res["proofs_unit"] = PROOF_UNIT
+    return res
 
 
 def run_reference(args):
@@ -864,16 +931,20 @@ def run_reference(args):
         return
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
     from oracle import oracle as O
+    O.set_num_threads(os.cpu_count() or 1)  # this rank alone times the CPU arm: every host core
+    st = CpuCommitStage()
     for _ in range(args.warmup):
-        cpu_sample_times(n_fft_cols=8, leaf_log=14)
+        st.step()
     totals = []
     t0 = time.perf_counter()
-    sample = ""
     for _ in range(args.steps):
-        stages, sample = cpu_sample_times(n_fft_cols=8, leaf_log=14)
+        stages, _ = st.step()
         totals.append(sum(stages.values()))
     wall = time.perf_counter() - t0
     value = args.steps / sum(totals)
+    sample = (f"every step whole: {N_COLS} x 2^{LOG_ROWS} interpolate, evaluate on 2^{LOG_EXT}, the full height-"
+              f"{LOG_EXT} tree, {FRI_LOG} folds; the oracle (C restatement of the reference CPU backend, OpenMP); "
+              "the Rust reference cannot be built: no cargo here or on the GPU box")
     res = {
         "metric": METRIC, "value": float(f"{value:.6g}"), "unit": UNIT, "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": float(f"{1e3 * sum(totals) / args.steps:.6g}"),
@@ -881,7 +952,7 @@ def run_reference(args):
         "data": "synthetic (seeded)", "impl": "reference",
         "config": {"workload": workload_name(), "n_cols": N_COLS, "log_rows": LOG_ROWS, "log_blowup": LOG_BLOWUP},
         "cpu_baseline": {"value": float(f"{value:.6g}"), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
-                         "sample": sample + " (the Rust reference cannot be built: no cargo on this image)"},
+                         "sample": sample},
         "e2e": {"value": float(f"{value:.6g}"), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": float(f"{wall:.4g}"),
     }
@@ -1030,13 +1101,28 @@ def run_case(args):
     print(json.dumps(res))
 
 
+def launch_replicas(n: int) -> int:
+    """Starts this command as n ranks on this node (torch.distributed.run, rendezvous on 127.0.0.1 at a
+    free port) and returns the launcher's exit status."""
+    import socket
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr=127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the timed oracle sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the timed oracle steps and proofs")
+    ap.add_argument("--skip-cpu-proofs", action="store_true", help="skip the oracle's whole proofs in cpu_baseline")
+    ap.add_argument("--skip-cpu-mixed-proof", action="store_true",
+                    help="skip the oracle's mixed-size proof (about a minute) in cpu_baseline")
     ap.add_argument("--n-cols", type=int, default=N_COLS, help="trace columns (smaller cases for profiling)")
     ap.add_argument("--log-rows", type=int, default=LOG_ROWS, help="log2 rows per trace column")
     ap.add_argument("--skip-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
@@ -1054,6 +1140,9 @@ def main():
                     help="run one small profiling case instead of the benchmark (for ncu)")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ and not args.case:
+        # one process per GPU: re-run this command under torch.distributed.run (replicas, weak scaling)
+        sys.exit(launch_replicas(args.gpus))
     if args.case:
         run_case(args)
     elif args.impl == "reference":

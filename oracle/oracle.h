@@ -22,6 +22,7 @@ typedef struct {
 } orc_channel;
 
 int orc_num_threads(void);
+void orc_set_num_threads(int n);
 void orc_bit_reverse(uint32_t *v, uint32_t log_n);
 void orc_circle_index_to_point(uint32_t idx, uint32_t out[2]);
 void orc_m31_mul_batch(const uint32_t *a, const uint32_t *b, uint32_t *out, uint64_t n);

@@ -73,6 +73,10 @@ def num_threads() -> int:
     return lib().orc_num_threads()
 
 
+def set_num_threads(n: int) -> None:
+    lib().orc_set_num_threads(ctypes.c_int(n))
+
+
 # ------------------------------------------------------------------ fields
 
 def qm31_mul(a, b):

@@ -19,6 +19,17 @@
 #include "blake2s.h"
 #include "oracle.h"
 
+/* The OpenMP thread count of the calling process's parallel regions (a launcher such as
+   torch.distributed.run sets OMP_NUM_THREADS=1 per rank; a rank that times the CPU baseline alone
+   raises it back to the host's cores). */
+void orc_set_num_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

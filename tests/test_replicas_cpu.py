@@ -60,3 +60,20 @@ def test_reference_arm_runs_on_rank_zero_only():
                         "--steps", "1", "--warmup", "0"], capture_output=True, text=True, env=env, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.strip() == ""
+
+
+def test_gpus_flag_launches_ranks_and_rank0_reports():
+    # `bench.py --gpus 2` outside a launcher starts two ranks itself (torch.distributed.run); with
+    # --impl reference rank 0 alone times the CPU arm, on every host core although the launcher
+    # sets OMP_NUM_THREADS=1, and prints the one JSON line; rank 1 exits 0 without work
+    import json
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--impl", "reference", "--n-cols", "2",
+                        "--log-rows", "6", "--steps", "2", "--warmup", "1"], cwd=ROOT, env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    res = json.loads(lines[0])
+    assert res["impl"] == "reference" and res["unit"] == "commit steps/s" and res["steps"] == 2
+    assert res["cpu_baseline"]["cores"] == (os.cpu_count() or 1)
