@@ -341,7 +341,7 @@ def plain_commit_step(cs):
              cs.tw_log, st)
 
 
-def wide_fib_prove_native(torch, n_proofs: int = 20, log_n: int = 14, n_cols: int = 100):
+def wide_fib_prove_native(torch, n_proofs: int = 20, log_n: int = 14, n_cols: int = 100, plain: bool = False):
     """Config 1 through the native prover (cs_prove_wide_fib): the same proof bytes as the restated
     prover, the host work in C++. Trace generated on the device from seeded inputs inside the
     timed region. Returns wall-clock latencies in ms."""
@@ -358,7 +358,7 @@ def wide_fib_prove_native(torch, n_proofs: int = 20, log_n: int = 14, n_cols: in
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         trace = CudaBackend.wide_fib_trace(a, b, n_cols)
-        CudaBackend.prove_wide_fib_native([trace], [log_n], fp, tw)
+        CudaBackend.prove_wide_fib_native([trace], [log_n], fp, tw, plain=plain)
         torch.cuda.synchronize()
         if k >= 2:
             lat.append((time.perf_counter() - t0) * 1e3)
@@ -391,7 +391,7 @@ def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: in
     return lat
 
 
-def mixed_prove_leg(torch, n_proofs: int = 2, arms=("batched", "plain", "native")):
+def mixed_prove_leg(torch, n_proofs: int = 2, arms=("batched", "plain", "native", "native_plain")):
     """Config 3 as a full proof: the batched mixed-size trace (mixed_trace_shape: Wide-Fibonacci
     components holding 480 M31 columns and 120 single-column LogUp components, each with one M31
     value column and one QM31 running-sum column, log sizes 10..22 geometric, mean ~16) proved by
@@ -436,31 +436,41 @@ def mixed_prove_leg(torch, n_proofs: int = 2, arms=("batched", "plain", "native"
                      "max_ms": round(max(lat), 3)}
         del proof, tw
         torch.cuda.empty_cache()
-    if "native" in arms:
-        # the batched kernels with the host work in native code (cs_prove_fib_and_lookups)
+    from proving_gb300 import _lib
+    for name in ("native", "native_plain"):
+        if name not in arms:
+            continue
+        # the host work in native code (cs_prove_fib_and_lookups): batched stages, or with CS_PROVE_PLAIN
+        # one launch per column for every per-column stage
         ops = pr.GpuOps()
         tw = ops.twiddles(max_log + 2)
         fpt = (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound, fp.n_queries)
-        lat = []
+        lat, launches = [], []
         for k in range(n_proofs + 1):
             values = [BaseColumn.from_cpu(v) for v in host_values]
             torch.cuda.synchronize()
+            n0 = _lib.load().cs_kernel_launch_count()
             t0 = time.perf_counter()
             traces = [CudaBackend.wide_fib_trace(a, b, n) for (a, b), (n, _) in zip(seeds, comps)]
             words, _ = CudaBackend.prove_fib_and_lookups_native(traces, [l for _, l in comps], values, lookup_logs,
-                                                                 fpt, tw)
+                                                                 fpt, tw, plain=name == "native_plain")
             torch.cuda.synchronize()
             if k >= 1:
                 lat.append((time.perf_counter() - t0) * 1e3)
+                launches.append(_lib.load().cs_kernel_launch_count() - n0)
             del traces, values
-        out["native"] = {"proofs_per_s": round(1e3 / statistics.median(lat), 3),
-                         "p50_ms": round(statistics.median(lat), 3), "max_ms": round(max(lat), 3),
-                         "same_proof_bytes": (hashlib.sha256(words).hexdigest() == digests["batched"]
-                                              if "batched" in digests else None)}
-        digests["native"] = hashlib.sha256(words).hexdigest()
+        digest = hashlib.sha256(words).hexdigest()
+        out[name] = {"proofs_per_s": round(1e3 / statistics.median(lat), 3),
+                     "p50_ms": round(statistics.median(lat), 3), "max_ms": round(max(lat), 3),
+                     "kernel_launches_per_proof": int(statistics.median(launches)),
+                     "same_proof_bytes": (digest == next(iter(digests.values())) if digests else None)}
+        digests[name] = digest
         del tw
         torch.cuda.empty_cache()
-    out["proof_sha256"] = digests.get("batched", digests.get("native"))
+    if "native" in out and "native_plain" in out:
+        out["native_batched_over_plain"] = round(out["native_plain"]["p50_ms"] / out["native"]["p50_ms"], 3)
+    out["proof_sha256"] = next(iter(digests.values())) if digests else None
+    out["all_arms_same_proof_bytes"] = len(set(digests.values())) == 1
     if "plain" in arms:
         out["same_proof_bytes"] = digests["batched"] == digests["plain"]
         out["batched_speedup"] = round(out["plain"]["p50_ms"] / out["batched"]["p50_ms"], 3)
@@ -497,7 +507,7 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
     fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
     cfg = ps.poseidon_pcs_config(log_n_rows + 3, fp)
     tw = ops.twiddles(log_n_rows + ps.LOG_EXPAND + fp.log_blowup_factor)
-    lat, nat = [], []
+    lat, nat, nplain = [], [], []
     fpt = (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound, fp.n_queries)
     for k in range(n_proofs + 1):
         torch.cuda.synchronize()
@@ -507,9 +517,13 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
         t1 = time.perf_counter()
         CudaBackend.prove_poseidon_native(log_n_rows, fpt, tw)
         torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        CudaBackend.prove_poseidon_native(log_n_rows, fpt, tw, plain=True)
+        torch.cuda.synchronize()
         if k >= 1:
             lat.append((t1 - t0) * 1e3)
-            nat.append((time.perf_counter() - t1) * 1e3)
+            nat.append((t2 - t1) * 1e3)
+            nplain.append((time.perf_counter() - t2) * 1e3)
     torch.cuda.empty_cache()
     # the constraint-quotient kernel alone on the evaluation domain CanonicCoset(log_n_rows + 2)
     eval_log = log_n_rows + ps.LOG_EXPAND
@@ -534,6 +548,8 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
            "max_ms": round(max(nat), 3), "prover": "native (cs_prove_poseidon); restated beside it",
            "restated": {"proofs_per_s": round(1e3 / statistics.median(lat), 3),
                         "p50_ms": round(statistics.median(lat), 3)},
+           "native_plain": {"proofs_per_s": round(1e3 / statistics.median(nplain), 3),
+                            "p50_ms": round(statistics.median(nplain), 3)},
            "composition_kernel": {"eval_rows": 1 << eval_log, "ms": round(ms, 4),
                                   "gb_per_s": round(read_bytes / ms / 1e6, 1),
                                   "rows_per_s": round((1 << eval_log) / ms * 1e3, 1)}}
@@ -542,40 +558,87 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
     return out
 
 
-def serving_leg(n_requests: int = 24, rate_per_s: float = 200.0):
-    """Config 5: a seeded Poisson stream of proof requests, half Wide-Fibonacci (100 columns) and
-    half Poseidon2 (8 permutations per row), log_n_rows uniform in [12, 20], arriving faster than
-    they can be served (so proofs/s measures capacity). Four arms on the same stream: the plain
-    path (one request at a time, one launch per column per stage, restated prover), the batched
-    path one request at a time (native provers), the served form (4 worker threads of one process,
-    a CUDA stream each, HBM-budget admission, native provers, which release the interpreter for
-    the whole proof so the threads' kernels overlap on the device), and the same with 4 worker
-    processes (a CUDA context each: their kernels time-slice instead of overlapping)."""
+def _verify_wide_fib_proof(args):
+    """Restated verifier on one served Wide-Fibonacci proof (run in a spawned worker)."""
+    words, log_n = args
+    from oracle.verifier import parse_proof, verify_wide_fib_components
+    verify_wide_fib_components(parse_proof(words, log_n + 1), [100], [log_n])
+    return True
+
+
+def serving_leg(n_requests: int = 200, rate_fracs=(0.25, 0.5, 0.9)):
+    """Config 5: seeded Poisson streams of proof requests, half Wide-Fibonacci (100 columns) and half
+    Poseidon2 (8 permutations per row), log_n_rows uniform in [12, 20]. Arms, all native provers:
+    plain (1 worker, one launch per column for every per-column stage, CS_PROVE_PLAIN), batched_serial
+    (1 worker, batched stages), served (4 worker threads of one process, a CUDA stream each, HBM-budget
+    admission in arrival order: the stages of different requests overlap on the device), and at
+    saturation served_processes (4 worker processes, a CUDA context each). First every arm serves the
+    stream all at once (capacity); then Poisson streams at fractions of the served capacity. Every
+    proof of every arm is compared with the same request proved alone (batched_serial at saturation),
+    and every served Wide-Fibonacci proof is accepted by the restated verifier."""
+    import multiprocessing as mp
     from proving_gb300 import serving
-    out = {"workload": f"{n_requests} requests, 50% Wide-Fibonacci (100 cols) / 50% Poseidon2 (8 perms/row), "
-                       f"log_n_rows uniform in [12, 20], Poisson arrivals at {rate_per_s}/s",
-           "arms": "plain: 1 worker, one launch per column per stage, restated prover; batched_serial: 1 worker, "
-                   "batched stage launches, native provers; served: 4 worker threads of one process (one CUDA "
-                   "context, a stream each), HBM-budget admission in arrival order, native provers; "
-                   "served_processes: 4 worker processes (a CUDA context each), otherwise the same; every arm "
-                   "gives the same proof bytes"}
-    for name, workers, plain in (("plain", 1, True), ("batched_serial", 1, False), ("served_processes", 4, False)):
-        reqs = serving.poisson_requests(n_requests, rate_per_s, 12, 20, seed=5, poseidon_share=0.5)
-        svc = serving.ProcessProverService(n_workers=workers, max_log_n_rows=20, plain=plain)
-        try:
-            done, wall = svc.run(reqs)
-        finally:
-            svc.close()
-        out[name] = serving.summarize(done, wall)
-    # warm-up outside the timed stream (the worker processes warm up the same way): the kernels of
-    # every tile size load on their first launch
+    out = {"workload": f"{n_requests} requests per run, 50% Wide-Fibonacci (100 cols) / 50% Poseidon2 "
+                       "(8 perms/row), log_n_rows uniform in [12, 20]; Poisson arrivals",
+           "arms": "plain: 1 worker, one launch per column per stage (native, CS_PROVE_PLAIN); batched_serial: "
+                   "1 worker, batched stages (native); served: 4 worker threads (one CUDA context, a stream "
+                   "each), HBM-budget admission in arrival order (native); served_processes: 4 worker "
+                   "processes, a CUDA context each"}
+    # warm-up outside the timed streams: the kernels of every tile size load on their first launch
     warm = [serving.ProofRequest(-1 - i, log_n, 1 + i, kind)
             for i, (log_n, kind) in enumerate((l, k) for l in (12, 16, 20) for k in ("wide_fib", "poseidon"))]
     serving.run_stream(4, [(0.0, r) for r in warm], max_log=20, native=True)
-    reqs = serving.poisson_requests(n_requests, rate_per_s, 12, 20, seed=5, poseidon_share=0.5)
-    done, wall = serving.run_stream(4, reqs, max_log=20, native=True)
-    out["served"] = serving.summarize(done, wall)
-    out["served_speedup"] = round(out["served"]["proofs_per_s"] / out["plain"]["proofs_per_s"], 3)
+    serving.run_stream(1, [(0.0, r) for r in warm], max_log=20, native=True, plain=True)
+
+    def stream(rate):
+        reqs = serving.poisson_requests(n_requests, rate if rate else 1.0, 12, 20, seed=5, poseidon_share=0.5)
+        return [(0.0 if rate is None else g, r) for g, r in reqs]
+
+    arms = {"plain": dict(n_workers=1, plain=True), "batched_serial": dict(n_workers=1),
+            "served": dict(n_workers=4)}
+    alone, same, kinds = {}, True, {}
+    sat = {}
+    for name in ("batched_serial", "plain", "served"):
+        done, wall = serving.run_stream(arms[name]["n_workers"], stream(None), max_log=20, native=True,
+                                        plain=arms[name].get("plain", False))
+        sat[name] = serving.summarize(done, wall)
+        for r in done:
+            kinds[r.request_id] = (r.kind, r.log_n_rows)
+            if name == "batched_serial":
+                alone[r.request_id] = r.proof_bytes()
+            else:
+                same = same and r.error is None and r.proof_bytes() == alone.get(r.request_id)
+        if name == "served":
+            served_done = done
+    svc = serving.ProcessProverService(n_workers=4, max_log_n_rows=20)
+    try:
+        done, wall = svc.run(stream(None))
+    finally:
+        svc.close()
+    sat["served_processes"] = serving.summarize(done, wall)
+    same = same and all(r.error is None and r.proof_bytes() == alone.get(r.request_id) for r in done)
+    out["saturation"] = sat
+    capacity = sat["served"]["proofs_per_s"]
+    out["capacity_proofs_per_s"] = capacity
+    sweep = {}
+    for frac in rate_fracs:
+        rate = frac * capacity
+        row = {"rate_per_s": round(rate, 2)}
+        for name in ("plain", "batched_serial", "served"):
+            done, wall = serving.run_stream(arms[name]["n_workers"], stream(rate), max_log=20, native=True,
+                                            plain=arms[name].get("plain", False))
+            row[name] = serving.summarize(done, wall)
+            same = same and all(r.error is None and r.proof_bytes() == alone.get(r.request_id) for r in done)
+        sweep[f"{frac:.2f}"] = row
+    out["sweep"] = sweep
+    out["same_proof_bytes"] = bool(same)
+    # the restated verifier on every served Wide-Fibonacci proof (spawned workers: CUDA is initialised here)
+    items = [(r.proof_bytes(), r.log_n_rows) for r in served_done if r.kind == "wide_fib"]
+    with mp.get_context("spawn").Pool(min(8, os.cpu_count() or 1)) as pool:
+        ok = pool.map(_verify_wide_fib_proof, items)
+    out["verified_wide_fib_proofs"] = int(sum(ok))
+    out["served_over_plain"] = round(sat["served"]["proofs_per_s"] / sat["plain"]["proofs_per_s"], 3)
+    out["batched_serial_over_plain"] = round(sat["batched_serial"]["proofs_per_s"] / sat["plain"]["proofs_per_s"], 3)
     return out
 
 
@@ -732,6 +795,7 @@ def run_gpu(args):
     with collector_paused():
         wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
         wf_native = wide_fib_prove_native(torch) if not args.skip_prove else []
+        wf_plain = wide_fib_prove_native(torch, plain=True) if not args.skip_prove else []
     bvp = batched_vs_plain(torch, cs) if not args.skip_plain else None
     with collector_paused():
         poseidon_res = poseidon_prove_leg(torch, args.poseidon_log_rows) if not args.skip_poseidon else None
@@ -809,6 +873,9 @@ def run_gpu(args):
                             "proofs_per_s": ff(1e3 / statistics.median(wf_native)),
                             "p50_ms": ff(float(np.percentile(wf_native, 50))),
                             "p99_ms": ff(float(np.percentile(wf_native, 99))),
+                            "native_plain": {"proofs_per_s": ff(1e3 / statistics.median(wf_plain)),
+                                             "p50_ms": ff(float(np.percentile(wf_plain, 50))),
+                                             "p99_ms": ff(float(np.percentile(wf_plain, 99)))},
                             "restated": {"proofs_per_s": ff(1e3 / statistics.median(wf_lat)),
                                          "p50_ms": ff(float(np.percentile(wf_lat, 50))),
                                          "p99_ms": ff(float(np.percentile(wf_lat, 99)))}} if wf_lat else None),

@@ -119,6 +119,27 @@ cs_status cs_evaluate_columns(const uint32_t *const *h_coeffs, uint32_t *const *
                               uint32_t log_coeffs, uint32_t log_size, const uint32_t *d_twiddles,
                               uint32_t twiddle_log_size, cs_stream stream);
 
+/* PolyOps::interpolate_columns over a batch of columns of different sizes
+   (crates/stwo/src/prover/poly/circle/ops.rs:30-40; SIMD
+   crates/stwo/src/prover/backend/simd/circle.rs:135-163): column i holds
+   2^h_log_sizes[i] bit-reversed evaluations on CanonicCoset(h_log_sizes[i]);
+   h_coeffs[i] receives the coefficients (it may equal h_evals[i]). The
+   columns of each size take one batched launch sequence, and the size groups
+   run on side streams forked from and joined back into `stream` (events;
+   stream capture follows them), so small sizes run beside large ones. */
+cs_status cs_interpolate_columns_multi(const uint32_t *const *h_evals, uint32_t *const *h_coeffs,
+                                       const uint32_t *h_log_sizes, uint32_t n_cols, const uint32_t *d_itwiddles,
+                                       uint32_t twiddle_log_size, cs_stream stream);
+
+/* PolyOps::evaluate_polynomials over polynomials of different sizes
+   (crates/stwo/src/prover/poly/circle/ops.rs:109-140): coefficients of log
+   size h_log_coeffs[i] evaluated on CanonicCoset(h_log_coeffs[i] + log_blowup)
+   into h_evals[i] (no aliasing), size groups concurrent as in
+   cs_interpolate_columns_multi. */
+cs_status cs_evaluate_columns_multi(const uint32_t *const *h_coeffs, uint32_t *const *h_evals,
+                                    const uint32_t *h_log_coeffs, uint32_t log_blowup, uint32_t n_cols,
+                                    const uint32_t *d_twiddles, uint32_t twiddle_log_size, cs_stream stream);
+
 /* FFT pass plans (no counterpart in the reference; the reference's SIMD FFT
    fixes its radix split in code). A column of 2^log_n words whose FFT runs
    n_layers layers (interpolate: n_layers = log_n; evaluate: the coefficient
@@ -446,7 +467,12 @@ typedef struct {
   uint32_t pow_bits, log_blowup_factor, log_last_layer_degree_bound, n_queries;
   const uint32_t *d_twiddles, *d_itwiddles;
   uint32_t twiddle_log_size;
+  uint32_t flags; /* 0, or CS_PROVE_PLAIN */
 } cs_wide_fib_proof_params;
+/* flags: the plain form, one launch per column for every per-column stage (interpolate, evaluate,
+   running sums, out-of-domain sampling, LogUp quotients), as the trait's default per-column loops
+   run on a backend without batched overrides. Same proof bytes; for comparison. */
+#define CS_PROVE_PLAIN 1u
 cs_status cs_prove_wide_fib(const cs_wide_fib_proof_params *params, uint32_t *const *d_trace, uint64_t *h_words,
                             size_t capacity, size_t *n_words, cs_stream stream);
 /* cs_prove_wide_fib with n_lookups single-column LogUp components beside the

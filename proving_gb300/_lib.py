@@ -37,6 +37,8 @@ SIGNATURES = {
     "cs_interpolate_columns": [vp, u32, u32, vp, u32, vp],
     "cs_interpolate_columns_into": [vp, vp, u32, u32, vp, u32, vp],
     "cs_evaluate_columns": [vp, vp, u32, u32, u32, vp, u32, vp],
+    "cs_interpolate_columns_multi": [vp, vp, vp, u32, vp, u32, vp],
+    "cs_evaluate_columns_multi": [vp, vp, vp, u32, u32, vp, u32, vp],
     "cs_merkle_build_leaves": [vp, vp, u32, u32, vp, vp],
     "cs_merkle_build_next_layer": [vp, u32, vp, vp],
     "cs_merkle_build_layers": [vp, u32, vp],

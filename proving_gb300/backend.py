@@ -104,7 +104,10 @@ class _WideFibProofParams(ctypes.Structure):
                 ("lifting_log_size", ctypes.c_uint32), ("pow_bits", ctypes.c_uint32),
                 ("log_blowup_factor", ctypes.c_uint32), ("log_last_layer_degree_bound", ctypes.c_uint32),
                 ("n_queries", ctypes.c_uint32), ("d_twiddles", ctypes.c_void_p), ("d_itwiddles", ctypes.c_void_p),
-                ("twiddle_log_size", ctypes.c_uint32)]
+                ("twiddle_log_size", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+
+
+PROVE_PLAIN = 1  # CS_PROVE_PLAIN
 
 
 class SecureColumnByCoords:
@@ -460,7 +463,7 @@ class CudaBackend:
                   _ptr_table([c.data for c in accum.columns]), _stream())
 
     @staticmethod
-    def _proof_params(n_cols, log_sizes, lifting_log_size: int, fri_params, twiddles: TwiddleTree):
+    def _proof_params(n_cols, log_sizes, lifting_log_size: int, fri_params, twiddles: TwiddleTree, plain=False):
         params = _WideFibProofParams()
         keep = ((ctypes.c_uint32 * max(1, len(n_cols)))(*n_cols), (ctypes.c_uint32 * max(1, len(log_sizes)))(*log_sizes))
         params.n_components = len(n_cols)
@@ -471,24 +474,26 @@ class CudaBackend:
         params.d_twiddles = twiddles.twiddles.data_ptr()
         params.d_itwiddles = twiddles.itwiddles.data_ptr()
         params.twiddle_log_size = twiddles.log_size
+        params.flags = PROVE_PLAIN if plain else 0
         return params, keep
 
     @staticmethod
-    def prove_wide_fib_native(traces, log_sizes, fri_params, twiddles: TwiddleTree) -> bytes:
+    def prove_wide_fib_native(traces, log_sizes, fri_params, twiddles: TwiddleTree, plain=False) -> bytes:
         """cs_prove_wide_fib: the whole proof of Wide-Fibonacci components with the host work in
         native code. traces[k]: component k's columns (BaseColumns of 2^log_sizes[k] evaluations,
         interpolated in place). fri_params: (pow_bits, log_blowup_factor,
         log_last_layer_degree_bound, n_queries). Returns the proof bytes (u64 LE felts)."""
-        return CudaBackend.prove_fib_and_lookups_native(traces, log_sizes, [], [], fri_params, twiddles)[0]
+        return CudaBackend.prove_fib_and_lookups_native(traces, log_sizes, [], [], fri_params, twiddles, plain)[0]
 
     @staticmethod
     def prove_fib_and_lookups_native(traces, log_sizes, lookup_values, lookup_logs, fri_params,
-                                     twiddles: TwiddleTree):
+                                     twiddles: TwiddleTree, plain=False):
         """cs_prove_fib_and_lookups: Wide-Fibonacci components and single-column LogUp components
         (lookup_values: BaseColumns on their trace domains, kept). Returns (proof bytes, claimed sums)."""
         cols = [c for t in traces for c in t]
         lifting = max(list(log_sizes) + list(lookup_logs)) + fri_params[1]
-        params, keep = CudaBackend._proof_params([len(t) for t in traces], log_sizes, lifting, fri_params, twiddles)
+        params, keep = CudaBackend._proof_params([len(t) for t in traces], log_sizes, lifting, fri_params, twiddles,
+                                                 plain)
         n = ctypes.c_size_t(0)
         cap = 1 << 22
         words = np.empty(cap, np.uint64)
@@ -501,10 +506,10 @@ class CudaBackend:
                 [tuple(int(x) for x in row) for row in claimed[:len(lookup_values)]])
 
     @staticmethod
-    def prove_poseidon_native(log_n_rows: int, fri_params, twiddles: TwiddleTree) -> bytes:
+    def prove_poseidon_native(log_n_rows: int, fri_params, twiddles: TwiddleTree, plain=False) -> bytes:
         """cs_prove_poseidon: the Poseidon2 AIR's proof (2^log_n_rows rows, 8 instances per row), trace
         generated on the device, the words the reference computes before its sanity check."""
-        params, keep = CudaBackend._proof_params([], [], log_n_rows + 2, fri_params, twiddles)
+        params, keep = CudaBackend._proof_params([], [], log_n_rows + 2, fri_params, twiddles, plain)
         n = ctypes.c_size_t(0)
         cap = 1 << 22
         words = np.empty(cap, np.uint64)

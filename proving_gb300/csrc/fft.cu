@@ -646,6 +646,84 @@ cs_status run_fft(const uint32_t* const* srcs, uint32_t* const* dsts, uint32_t n
   return CS_OK;
 }
 
+// Side streams for the size groups of a mixed batch, per thread and device, created on first use
+// (one set per calling thread, so concurrent provers never share them).
+constexpr int kSideStreams = 4;
+cs_status side_streams(cudaStream_t* out) {
+  struct Pool {
+    int dev = -1;
+    cudaStream_t s[kSideStreams] = {};
+    cudaEvent_t fork = nullptr, join[kSideStreams] = {};
+  };
+  static thread_local std::vector<Pool> pools;
+  int dev = 0;
+  CS_CUDA(cudaGetDevice(&dev));
+  for (Pool& p : pools)
+    if (p.dev == dev) {
+      for (int i = 0; i < kSideStreams; i++) out[i] = p.s[i];
+      return CS_OK;
+    }
+  Pool p;
+  p.dev = dev;
+  for (int i = 0; i < kSideStreams; i++) CS_CUDA(cudaStreamCreateWithFlags(&p.s[i], cudaStreamNonBlocking));
+  pools.push_back(p);
+  for (int i = 0; i < kSideStreams; i++) out[i] = p.s[i];
+  return CS_OK;
+}
+
+// The FFT of a batch of columns of different sizes (PolyOps::interpolate_columns /
+// evaluate_polynomials over a mixed batch): one batched launch sequence per size, the size groups
+// spread over side streams forked from and joined back into `st` with events, so the small sizes'
+// launches run beside the large ones instead of after them. Graph capture follows the fork and join.
+// inverse: log_srcs[i] == log_ns[i]; forward: coefficients of log_srcs[i] evaluated on log_ns[i].
+cs_status run_fft_mixed(const uint32_t* const* srcs, uint32_t* const* dsts, const uint32_t* log_srcs,
+                        const uint32_t* log_ns, uint32_t n_cols, bool inverse, const uint32_t* tw, uint32_t tw_log,
+                        cudaStream_t st) {
+  // size groups, largest first (they take longest, so they start first)
+  std::map<std::pair<uint32_t, uint32_t>, std::vector<uint32_t>, std::greater<>> groups;
+  for (uint32_t i = 0; i < n_cols; i++) groups[{log_ns[i], log_srcs[i]}].push_back(i);
+  if (groups.size() <= 1) {
+    if (groups.empty()) return CS_OK;
+    const auto& [key, idx] = *groups.begin();
+    std::vector<const uint32_t*> s(idx.size());
+    std::vector<uint32_t*> d(idx.size());
+    for (size_t k = 0; k < idx.size(); k++) {
+      s[k] = srcs[idx[k]];
+      d[k] = dsts[idx[k]];
+    }
+    return run_fft(s.data(), d.data(), (uint32_t)idx.size(), key.second, key.first, inverse, tw, tw_log, st);
+  }
+  cudaStream_t side[kSideStreams];
+  cs_status r = side_streams(side);
+  if (r != CS_OK) return r;
+  cudaEvent_t fork, join[kSideStreams];
+  CS_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  for (int i = 0; i < kSideStreams; i++) CS_CUDA(cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming));
+  CS_CUDA(cudaEventRecord(fork, st));
+  const int used = std::min<int>(kSideStreams, (int)groups.size());
+  for (int i = 0; i < used; i++) CS_CUDA(cudaStreamWaitEvent(side[i], fork, 0));
+  int g = 0;
+  for (const auto& [key, idx] : groups) {
+    std::vector<const uint32_t*> s(idx.size());
+    std::vector<uint32_t*> d(idx.size());
+    for (size_t k = 0; k < idx.size(); k++) {
+      s[k] = srcs[idx[k]];
+      d[k] = dsts[idx[k]];
+    }
+    r = run_fft(s.data(), d.data(), (uint32_t)idx.size(), key.second, key.first, inverse, tw, tw_log,
+                side[g % used]);
+    if (r != CS_OK) break;
+    g++;
+  }
+  for (int i = 0; i < used; i++) {
+    cudaEventRecord(join[i], side[i]);
+    cudaStreamWaitEvent(st, join[i], 0);
+  }
+  cudaEventDestroy(fork);
+  for (int i = 0; i < kSideStreams; i++) cudaEventDestroy(join[i]);
+  return r;
+}
+
 }  // namespace
 
 }  // namespace cs
@@ -707,6 +785,46 @@ extern "C" cs_status cs_evaluate_columns(const uint32_t* const* h_coeffs, uint32
   }
   return run_fft(h_coeffs, h_evals, n_cols, log_coeffs, log_size, false, d_twiddles, twiddle_log_size,
                  to_stream(stream));
+}
+
+extern "C" cs_status cs_interpolate_columns_multi(const uint32_t* const* h_evals, uint32_t* const* h_coeffs,
+                                                  const uint32_t* h_log_sizes, uint32_t n_cols,
+                                                  const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
+                                                  cs_stream stream) {
+  CS_CHECK_ARG(n_cols == 0 || (h_evals != nullptr && h_coeffs != nullptr && h_log_sizes != nullptr),
+               "interpolate_multi: null table");
+  for (uint32_t i = 0; i < n_cols; i++) {
+    CS_CHECK_ARG(h_evals[i] != nullptr && h_coeffs[i] != nullptr, "interpolate_multi: column %u is null", i);
+    CS_CHECK_ARG(h_log_sizes[i] >= 1 && h_log_sizes[i] <= 28, "interpolate_multi: column %u of log size %u", i,
+                 h_log_sizes[i]);
+    CS_CHECK_ARG(h_log_sizes[i] <= 2 || (d_itwiddles != nullptr && twiddle_log_size + 1 >= h_log_sizes[i]),
+                 "interpolate_multi: twiddle tree of log %u does not cover a domain of log %u", twiddle_log_size,
+                 h_log_sizes[i]);
+  }
+  return run_fft_mixed(h_evals, h_coeffs, h_log_sizes, h_log_sizes, n_cols, true, d_itwiddles, twiddle_log_size,
+                       to_stream(stream));
+}
+
+extern "C" cs_status cs_evaluate_columns_multi(const uint32_t* const* h_coeffs, uint32_t* const* h_evals,
+                                               const uint32_t* h_log_coeffs, uint32_t log_blowup, uint32_t n_cols,
+                                               const uint32_t* d_twiddles, uint32_t twiddle_log_size,
+                                               cs_stream stream) {
+  CS_CHECK_ARG(n_cols == 0 || (h_coeffs != nullptr && h_evals != nullptr && h_log_coeffs != nullptr),
+               "evaluate_multi: null table");
+  CS_CHECK_ARG(log_blowup <= 8, "evaluate_multi: log_blowup %u", log_blowup);
+  std::vector<uint32_t> log_ns(n_cols);
+  for (uint32_t i = 0; i < n_cols; i++) {
+    CS_CHECK_ARG(h_coeffs[i] != nullptr && h_evals[i] != nullptr, "evaluate_multi: column %u is null", i);
+    CS_CHECK_ARG((const void*)h_coeffs[i] != (const void*)h_evals[i], "evaluate_multi: column %u aliases its output",
+                 i);
+    log_ns[i] = h_log_coeffs[i] + log_blowup;
+    CS_CHECK_ARG(log_ns[i] >= 1 && log_ns[i] <= 28, "evaluate_multi: column %u of log size %u", i, log_ns[i]);
+    CS_CHECK_ARG(log_ns[i] <= 2 || (d_twiddles != nullptr && twiddle_log_size + 1 >= log_ns[i]),
+                 "evaluate_multi: twiddle tree of log %u does not cover a domain of log %u", twiddle_log_size,
+                 log_ns[i]);
+  }
+  return run_fft_mixed(h_coeffs, h_evals, h_log_coeffs, log_ns.data(), n_cols, false, d_twiddles, twiddle_log_size,
+                       to_stream(stream));
 }
 
 extern "C" cs_status cs_fft_set_plan(uint32_t inverse, uint32_t log_n, uint32_t n_layers, const uint32_t* pass_layers,

@@ -423,6 +423,10 @@ struct ProofConfig {
   uint32_t L, b, pow_bits, log_last_layer_degree_bound, n_queries;
   const uint32_t *tw, *itw;
   uint32_t tw_log;
+  // one launch per column for every per-column stage (interpolate, evaluate, running sums,
+  // out-of-domain sampling, constraint quotients): the plain form, as a backend without batched
+  // overrides runs the trait's default per-column loops
+  bool plain = false;
 };
 
 }  // namespace
@@ -441,6 +445,10 @@ struct Prover {
   cs_status interpolate(const std::vector<uint32_t*>& cols, uint32_t log) {
     if (cols.empty()) return CS_OK;
     std::vector<uint32_t*> c(cols);
+    if (cfg.plain) {
+      for (uint32_t* x : c) HP_TRY(cs_interpolate_columns(&x, 1, log, cfg.itw, cfg.tw_log, st));
+      return CS_OK;
+    }
     return cs_interpolate_columns(c.data(), (uint32_t)c.size(), log, cfg.itw, cfg.tw_log, st);
   }
   // Coefficient columns of one size evaluated on CanonicCoset(to_log) into one new block.
@@ -451,7 +459,49 @@ struct Prover {
     if (!blk) return A.status;
     for (size_t j = 0; j < coeffs.size(); j++) out.push_back(blk + (j << to_log));
     std::vector<const uint32_t*> src(coeffs.begin(), coeffs.end());
+    if (cfg.plain) {
+      for (size_t j = 0; j < src.size(); j++)
+        HP_TRY(cs_evaluate_columns(&src[j], &out[j], 1, log, to_log, cfg.tw, cfg.tw_log, st));
+      return CS_OK;
+    }
     return cs_evaluate_columns(src.data(), out.data(), (uint32_t)coeffs.size(), log, to_log, cfg.tw, cfg.tw_log, st);
+  }
+  // Columns of any sizes: evaluations src[i] (log size logs[i]) interpolated into dst[i] (which may
+  // be src[i]), every size in one call (PolyOps::interpolate_columns over the mixed batch).
+  cs_status interpolate_mixed(const std::vector<const uint32_t*>& src, const std::vector<uint32_t*>& dst,
+                              const std::vector<uint32_t>& logs) {
+    if (src.empty()) return CS_OK;
+    if (cfg.plain) {
+      for (size_t i = 0; i < src.size(); i++)
+        HP_TRY(cs_interpolate_columns_into(&src[i], &dst[i], 1, logs[i], cfg.itw, cfg.tw_log, st));
+      return CS_OK;
+    }
+    return cs_interpolate_columns_multi(src.data(), dst.data(), logs.data(), (uint32_t)src.size(), cfg.itw, cfg.tw_log,
+                                        st);
+  }
+  // Coefficient columns of any sizes evaluated on CanonicCoset(log + blowup) into one new block,
+  // every size in one call (PolyOps::evaluate_polynomials over the mixed batch).
+  cs_status evaluate_mixed(const std::vector<uint32_t*>& coeffs, const std::vector<uint32_t>& logs,
+                           std::vector<uint32_t*>& out) {
+    out.clear();
+    if (coeffs.empty()) return CS_OK;
+    size_t total = 0;
+    for (uint32_t l : logs) total += 1ull << (l + cfg.b);
+    uint32_t* blk = A.alloc(total);
+    if (!blk) return A.status;
+    size_t off = 0;
+    for (uint32_t l : logs) {
+      out.push_back(blk + off);
+      off += 1ull << (l + cfg.b);
+    }
+    std::vector<const uint32_t*> src(coeffs.begin(), coeffs.end());
+    if (cfg.plain) {
+      for (size_t j = 0; j < src.size(); j++)
+        HP_TRY(cs_evaluate_columns(&src[j], &out[j], 1, logs[j], logs[j] + cfg.b, cfg.tw, cfg.tw_log, st));
+      return CS_OK;
+    }
+    return cs_evaluate_columns_multi(src.data(), out.data(), logs.data(), cfg.b, (uint32_t)src.size(), cfg.tw,
+                                     cfg.tw_log, st);
   }
   std::vector<uint32_t*>& acc_for(std::map<uint32_t, std::vector<uint32_t*>>& acc, uint32_t el) {
     if (!acc.count(el)) {
@@ -603,7 +653,12 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
     std::vector<const uint32_t*> cols;
     for (const Sample& m : members) cols.push_back(trees[m.tree].cols[m.col].p);
     const uint32_t* wcc[4] = {wc[0], wc[1], wc[2], wc[3]};
-    HP_TRY(cs_barycentric_eval(cols.data(), (uint32_t)cols.size(), ls, wcc, d_samples + 4 * row, st));
+    if (cfg.plain) {
+      for (size_t j = 0; j < cols.size(); j++)
+        HP_TRY(cs_barycentric_eval(&cols[j], 1, ls, wcc, d_samples + 4 * (row + j), st));
+    } else {
+      HP_TRY(cs_barycentric_eval(cols.data(), (uint32_t)cols.size(), ls, wcc, d_samples + 4 * row, st));
+    }
     row += members.size();
     A.release(w);
   }
@@ -958,28 +1013,41 @@ struct FibLookupAir : Air {
   qm31 z;
 
   cs_status trace(Prover& P, std::vector<Col>& cols) override {
+    // every column of the tree in one interpolate and one evaluate call across sizes: the
+    // Wide-Fibonacci columns in place, the LogUp value columns out of place (they stay for the
+    // running sums)
+    std::vector<const uint32_t*> src;
+    std::vector<uint32_t*> coeffs;
+    std::vector<uint32_t> tlogs;
     size_t c0 = 0;
+    for (size_t k = 0; k < n_cols.size(); k++)
+      for (uint32_t j = 0; j < n_cols[k]; j++, c0++) {
+        src.push_back(d_trace[c0]);
+        coeffs.push_back(d_trace[c0]);
+        tlogs.push_back(logs[k]);
+      }
+    size_t lookup_words = 0;
+    for (uint32_t l : lookup_logs) lookup_words += 1ull << l;
+    uint32_t* lblk = lookup_words ? P.A.alloc(lookup_words) : nullptr;
+    if (lookup_words && !lblk) return P.A.status;
+    size_t off = 0;
+    for (size_t k = 0; k < lookup_logs.size(); k++) {
+      src.push_back(d_values[k]);
+      coeffs.push_back(lblk + off);
+      tlogs.push_back(lookup_logs[k]);
+      off += 1ull << lookup_logs[k];
+    }
+    HP_TRY(P.interpolate_mixed(src, coeffs, tlogs));
+    std::vector<uint32_t*> ev;
+    HP_TRY(P.evaluate_mixed(coeffs, tlogs, ev));
+    if (lblk) P.A.release(lblk);
+    size_t i = 0;
     for (size_t k = 0; k < n_cols.size(); k++) {
-      std::vector<uint32_t*> c(d_trace + c0, d_trace + c0 + n_cols[k]);
-      HP_TRY(P.interpolate(c, logs[k]));
-      std::vector<uint32_t*> ev;
-      HP_TRY(P.evaluate(c, logs[k], logs[k] + P.cfg.b, ev));
-      for (uint32_t* e : ev) cols.push_back({e, logs[k] + P.cfg.b});
-      fib_evals.push_back(ev);
-      c0 += n_cols[k];
+      fib_evals.emplace_back(ev.begin() + i, ev.begin() + i + n_cols[k]);
+      i += n_cols[k];
     }
-    for (size_t k = 0; k < lookup_logs.size(); k++) {  // out of place: the values stay for the sums
-      const uint32_t l = lookup_logs[k];
-      uint32_t* coeffs = P.A.alloc(1ull << l);
-      if (!coeffs) return P.A.status;
-      const uint32_t* src = d_values[k];
-      HP_TRY(cs_interpolate_columns_into(&src, &coeffs, 1, l, P.cfg.itw, P.cfg.tw_log, P.st));
-      std::vector<uint32_t*> ev;
-      HP_TRY(P.evaluate({coeffs}, l, l + P.cfg.b, ev));
-      lookup_evals.push_back(ev[0]);
-      cols.push_back({ev[0], l + P.cfg.b});
-      P.A.release(coeffs);
-    }
+    for (size_t k = 0; k < lookup_logs.size(); k++) lookup_evals.push_back(ev[i + k]);
+    for (size_t j = 0; j < ev.size(); j++) cols.push_back({ev[j], tlogs[j] + P.cfg.b});
     return CS_OK;
   }
   bool has_interaction() const override { return !lookup_logs.empty(); }
@@ -998,20 +1066,30 @@ struct FibLookupAir : Air {
     if (!d_claimed) return P.A.status;
     const uint32_t zw[4] = {z.a.a, z.a.b, z.b.a, z.b.b};
     std::vector<const uint32_t*> vals(d_values, d_values + n);
-    HP_TRY(cs_logup_running_sums((uint32_t)n, vals.data(), lookup_logs.data(), zw, sums.data(), d_claimed, P.st));
+    if (P.cfg.plain) {
+      for (size_t k = 0; k < n; k++) {
+        uint32_t* out[4] = {sums[4 * k], sums[4 * k + 1], sums[4 * k + 2], sums[4 * k + 3]};
+        HP_TRY(cs_logup_running_sum(vals[k], lookup_logs[k], zw, out, d_claimed + 4 * k, P.st));
+      }
+    } else {
+      HP_TRY(cs_logup_running_sums((uint32_t)n, vals.data(), lookup_logs.data(), zw, sums.data(), d_claimed, P.st));
+    }
     std::vector<uint32_t> cl(4 * n);
     CS_CUDA(cudaMemcpyAsync(cl.data(), d_claimed, 16 * n, cudaMemcpyDeviceToHost, P.st));
     CS_CUDA(cudaStreamSynchronize(P.st));
     claimed.clear();
     for (size_t k = 0; k < n; k++) claimed.push_back(qm31_make(cl[4 * k], cl[4 * k + 1], cl[4 * k + 2], cl[4 * k + 3]));
+    // every running-sum coordinate of every component in one interpolate and one evaluate call
+    std::vector<const uint32_t*> src(sums.begin(), sums.end());
+    std::vector<uint32_t> slogs;
+    for (size_t k = 0; k < n; k++) slogs.insert(slogs.end(), 4, lookup_logs[k]);
+    HP_TRY(P.interpolate_mixed(src, sums, slogs));
+    std::vector<uint32_t*> ev;
+    HP_TRY(P.evaluate_mixed(sums, slogs, ev));
     for (size_t k = 0; k < n; k++) {
-      std::vector<uint32_t*> coords(sums.begin() + 4 * k, sums.begin() + 4 * k + 4);
-      HP_TRY(P.interpolate(coords, lookup_logs[k]));
-      std::vector<uint32_t*> ev;
-      HP_TRY(P.evaluate(coords, lookup_logs[k], lookup_logs[k] + P.cfg.b, ev));
-      inter_evals.push_back(ev);
-      for (uint32_t* e : ev) {
-        cols.push_back({e, lookup_logs[k] + P.cfg.b});
+      inter_evals.emplace_back(ev.begin() + 4 * k, ev.begin() + 4 * k + 4);
+      for (int c = 0; c < 4; c++) {
+        cols.push_back({ev[4 * k + c], lookup_logs[k] + P.cfg.b});
         two.push_back(true);
       }
     }
@@ -1060,8 +1138,14 @@ struct FibLookupAir : Air {
         cl.insert(cl.end(), cw, cw + 4);
       }
       const uint32_t zw[4] = {z.a.a, z.a.b, z.b.a, z.b.b};
-      HP_TRY(cs_logup_compositions((uint32_t)vals.size(), vals.data(), inter.data(), l + 1, l, zw, cl.data(),
-                                   rcs.data(), P.acc_for(acc, l + 1).data(), P.st));
+      if (P.cfg.plain) {
+        for (size_t j = 0; j < vals.size(); j++)
+          HP_TRY(cs_logup_composition(vals[j], &inter[4 * j], l + 1, l, zw, &cl[4 * j], &rcs[4 * j],
+                                      P.acc_for(acc, l + 1).data(), P.st));
+      } else {
+        HP_TRY(cs_logup_compositions((uint32_t)vals.size(), vals.data(), inter.data(), l + 1, l, zw, cl.data(),
+                                     rcs.data(), P.acc_for(acc, l + 1).data(), P.st));
+      }
     }
     return CS_OK;
   }
@@ -1195,6 +1279,7 @@ cs_status finish(std::vector<uint64_t>& words, uint64_t* h_words, size_t capacit
 }
 
 cs_status check_common(const cs_wide_fib_proof_params& pp, uint32_t max_log) {
+  CS_CHECK_ARG((pp.flags & ~(uint32_t)CS_PROVE_PLAIN) == 0, "prove: unknown flags 0x%x", pp.flags);
   CS_CHECK_ARG(pp.log_blowup_factor == 1, "prove: log_blowup_factor 1 (SubDomain evaluation)");
   CS_CHECK_ARG(pp.d_twiddles != nullptr && pp.d_itwiddles != nullptr, "prove: null twiddles");
   CS_CHECK_ARG(pp.pow_bits <= 32 && pp.n_queries >= 1, "prove: bad FRI parameters");
@@ -1208,8 +1293,10 @@ cs_status check_common(const cs_wide_fib_proof_params& pp, uint32_t max_log) {
 }
 
 hp::ProofConfig config_of(const cs_wide_fib_proof_params& pp) {
-  return {pp.lifting_log_size, pp.log_blowup_factor, pp.pow_bits, pp.log_last_layer_degree_bound,
-          pp.n_queries, pp.d_twiddles, pp.d_itwiddles, pp.twiddle_log_size};
+  hp::ProofConfig c{pp.lifting_log_size, pp.log_blowup_factor, pp.pow_bits, pp.log_last_layer_degree_bound,
+                    pp.n_queries, pp.d_twiddles, pp.d_itwiddles, pp.twiddle_log_size};
+  c.plain = (pp.flags & CS_PROVE_PLAIN) != 0;
+  return c;
 }
 
 }  // namespace

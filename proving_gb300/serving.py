@@ -18,9 +18,11 @@ Two forms:
 - `ProcessProverService` runs each worker as a spawned process with its own CUDA
   context and stream; the contexts time-slice the device instead of sharing it.
 
-`plain=True` gives the plain form: one launch per column for the per-column
-stages (prover.PlainGpuOps), orchestrated by the restated prover. Otherwise the
-workers prove requests with the native provers, whose bytes are the same.
+`plain=True` gives the plain form: one launch per column for every per-column
+stage. With the native provers that is their CS_PROVE_PLAIN mode; with
+`native=False` it is prover.PlainGpuOps under the restated (Python) prover.
+Otherwise the workers prove requests with the native provers' batched stages.
+Every form gives the same proof bytes for a request.
 """
 from __future__ import annotations
 
@@ -91,10 +93,11 @@ def twiddle_domain(max_log_n_rows: int) -> int:
     return max_log_n_rows + 3
 
 
-def prove_request(ops, twiddles, req: ProofRequest, native: bool = False):
+def prove_request(ops, twiddles, req: ProofRequest, native: bool = False, plain: bool = False):
     """One proof on the current CUDA stream: the trace generated on the device from the request's
     seed, then the restated prover, or with native=True the native prover (cs_prove_wide_fib /
-    cs_prove_poseidon, the same bytes; returned as bytes)."""
+    cs_prove_poseidon, the same bytes; returned as bytes; plain=True: one launch per column per
+    stage)."""
     from .backend import BaseColumn, CudaBackend
     if req.kind == "poseidon":
         from . import poseidon as ps
@@ -102,7 +105,7 @@ def prove_request(ops, twiddles, req: ProofRequest, native: bool = False):
             fp = fri_params()
             return CudaBackend.prove_poseidon_native(
                 req.log_n_rows, (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound, fp.n_queries),
-                twiddles)
+                twiddles, plain=plain)
         cfg = ps.poseidon_pcs_config(req.log_n_rows + 3, fri_params())
         # the reference's own sanity check fails for this AIR (lifted protocol): check=False
         return ps.prove_poseidon(ops, req.log_n_rows, cfg, pr.Blake2sChannel(), twiddles, check=False)
@@ -113,7 +116,7 @@ def prove_request(ops, twiddles, req: ProofRequest, native: bool = False):
         fp = fri_params()
         return CudaBackend.prove_wide_fib_native(
             [trace], [req.log_n_rows], (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound,
-                                        fp.n_queries), twiddles)
+                                        fp.n_queries), twiddles, plain=plain)
     return pr.prove_wide_fib(ops, trace, req.log_n_rows, default_config(req.log_n_rows), pr.Blake2sChannel(),
                              twiddles)
 
@@ -144,10 +147,11 @@ class ProverService:
                  plain: bool = False, native: bool | None = None):
         import torch
         self.torch = torch
-        self.ops = _ops(plain)
         # the native provers release the interpreter for the whole proof, so worker threads prove
         # concurrently, each on its own stream of the one CUDA context
         self.native = (not plain) if native is None else native
+        self.plain = plain
+        self.ops = _ops(plain and not self.native)
         # the worker threads share one CUDA context: a graph capture in one of them would stop the
         # others' work, so the FRI layer loop runs eagerly here (worker processes replay graphs)
         self.ops.fri_graphs = False
@@ -163,7 +167,7 @@ class ProverService:
 
     def _prove(self, req: ProofRequest, stream):
         with self.torch.cuda.stream(stream):
-            proof = prove_request(self.ops, self.twiddles, req, native=self.native)
+            proof = prove_request(self.ops, self.twiddles, req, native=self.native, plain=self.plain)
             stream.synchronize()
         return proof
 

@@ -223,3 +223,34 @@ def test_merkle_height_limits_agree(lib):
     cols = (ctypes.c_void_p * 1)(1 << 20)
     assert _status(lib, "cs_merkle_build_leaves", cols, logs, 1, 31, ctypes.c_void_p(1 << 22), null) == INVALID
     assert b"too large" in lib.cs_last_error()
+
+
+def test_mixed_size_fft_checks_arguments_on_host(lib):
+    INVALID = 1
+    null = ctypes.c_void_p(0)
+    cols = (ctypes.c_void_p * 2)(1 << 20, 1 << 21)
+    logs = (ctypes.c_uint32 * 2)(5, 0)  # a column of log size 0
+    assert _status(lib, "cs_interpolate_columns_multi", cols, cols, logs, 2, ctypes.c_void_p(1 << 22), 10,
+                   null) == INVALID
+    logs = (ctypes.c_uint32 * 2)(5, 12)  # beyond the twiddle tree
+    assert _status(lib, "cs_interpolate_columns_multi", cols, cols, logs, 2, ctypes.c_void_p(1 << 22), 10,
+                   null) == INVALID
+    assert b"twiddle" in lib.cs_last_error()
+    # evaluate may not write over its coefficients
+    assert _status(lib, "cs_evaluate_columns_multi", cols, cols, (ctypes.c_uint32 * 2)(5, 6), 1, 2,
+                   ctypes.c_void_p(1 << 22), 10, null) == INVALID
+    assert b"aliases" in lib.cs_last_error()
+
+
+def test_native_prover_rejects_unknown_flags(lib):
+    from proving_gb300.backend import _WideFibProofParams
+    p = _WideFibProofParams()
+    n_cols = (ctypes.c_uint32 * 1)(4)
+    logs = (ctypes.c_uint32 * 1)(5)
+    p.n_components, p.n_cols, p.log_sizes = 1, ctypes.cast(n_cols, ctypes.c_void_p), ctypes.cast(logs, ctypes.c_void_p)
+    p.lifting_log_size, p.pow_bits, p.log_blowup_factor, p.log_last_layer_degree_bound, p.n_queries = 6, 10, 1, 0, 3
+    p.d_twiddles, p.d_itwiddles, p.twiddle_log_size, p.flags = 1 << 20, 1 << 21, 6, 6
+    cols = (ctypes.c_void_p * 4)(1 << 22, 1 << 23, 1 << 24, 1 << 25)
+    n = ctypes.c_size_t(0)
+    assert _status(lib, "cs_prove_wide_fib", ctypes.byref(p), cols, None, 0, ctypes.byref(n), None) == 1
+    assert b"flags" in lib.cs_last_error()

@@ -89,3 +89,30 @@ def test_restated_host_prover_equals_native(B, log_n):
                                             pr.PcsConfig(fp, trace_lifting_log_size=log_n + 1), pr.Blake2sChannel(),
                                             tw)
     assert native == restated.to_bytes()
+
+
+def test_plain_form_gives_the_same_proofs(B):
+    # CS_PROVE_PLAIN (one launch per column for every per-column stage) proves the same bytes as the
+    # batched form, for Wide-Fibonacci with LogUp components of several sizes and for Poseidon2
+    from proving_gb300 import _lib
+    from proving_gb300.backend import BaseColumn
+    shape, lookup_logs = [(10, 5), (3, 8), (4, 2)], [8, 2, 5, 8, 11]
+    host, values = _fib_lookup_inputs(shape, lookup_logs, 9)
+    logs = [l for _, l in shape]
+    L = max(logs + lookup_logs) + 1
+    tw = pr.GpuOps().twiddles(L + 1)
+    proofs, launches = [], []
+    for plain in (False, True):
+        n0 = _lib.load().cs_kernel_launch_count()
+        w, cl = B.prove_fib_and_lookups_native([[BaseColumn.from_cpu(c) for c in t] for t in host], logs,
+                                               [BaseColumn.from_cpu(v) for v in values], lookup_logs, (10, 1, 0, 20),
+                                               tw, plain=plain)
+        torch.cuda.synchronize()
+        launches.append(_lib.load().cs_kernel_launch_count() - n0)
+        proofs.append((w, cl))
+    assert proofs[0] == proofs[1]
+    assert launches[1] > launches[0]
+    want, _ = O.prove_fib_and_lookups((10, 1, 0, 20, 1), host, logs, values, lookup_logs)
+    assert proofs[0][0] == want
+    tw = pr.GpuOps().twiddles(7)
+    assert B.prove_poseidon_native(4, (10, 1, 0, 70), tw, plain=True) == B.prove_poseidon_native(4, (10, 1, 0, 70), tw)

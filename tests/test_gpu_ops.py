@@ -82,6 +82,36 @@ def test_evaluate_matches_oracle(B, log_c, log_n):
         assert np.array_equal(o.to_cpu(), w)
 
 
+@pytest.mark.parametrize("logs", [[1, 2, 3, 4, 5, 10, 12, 13, 16, 17, 20, 22], [7] * 5 + [9] * 3 + [3] * 7, [14]])
+def test_mixed_size_interpolate_and_evaluate(B, logs):
+    # cs_interpolate_columns_multi / cs_evaluate_columns_multi: every size of a mixed batch in one call
+    # (size groups on side streams joined back into the caller's stream), out of place and in place
+    from proving_gb300 import _lib
+    from proving_gb300.backend import _ptr_table, _stream, _u32_table
+    top = max(logs) + 1
+    tree = _tree(B, top + 1)
+    tw, itw = O.canonic_twiddles(top + 1)
+    evals_np = [m31_column(700 + i, l) for i, l in enumerate(logs)]
+    src = [_col(e) for e in evals_np]
+    coeffs = [_col(np.zeros(1 << l, np.uint32)) for l in logs]
+    _lib.call("cs_interpolate_columns_multi", _ptr_table([c.data for c in src]), _ptr_table([c.data for c in coeffs]),
+              _u32_table(logs), len(logs), tree.itwiddles.data_ptr(), tree.log_size, _stream())
+    inplace = [_col(e) for e in evals_np]
+    _lib.call("cs_interpolate_columns_multi", _ptr_table([c.data for c in inplace]),
+              _ptr_table([c.data for c in inplace]), _u32_table(logs), len(logs), tree.itwiddles.data_ptr(),
+              tree.log_size, _stream())
+    want_c = O.interpolate_batch(evals_np, itw)
+    for c, ip, w, e in zip(coeffs, inplace, want_c, src):
+        assert np.array_equal(c.to_cpu(), w) and np.array_equal(ip.to_cpu(), w)
+    assert all(np.array_equal(e.to_cpu(), v) for e, v in zip(src, evals_np))  # out of place: sources kept
+    ext = [_col(np.zeros(1 << (l + 1), np.uint32)) for l in logs]
+    _lib.call("cs_evaluate_columns_multi", _ptr_table([c.data for c in coeffs]), _ptr_table([c.data for c in ext]),
+              _u32_table(logs), 1, len(logs), tree.twiddles.data_ptr(), tree.log_size, _stream())
+    want_e = O.evaluate_batch(want_c, [l + 1 for l in logs], tw)
+    for x, w in zip(ext, want_e):
+        assert np.array_equal(x.to_cpu(), w)
+
+
 def test_twiddle_tree_larger_than_domain(B):
     # A tree for a bigger root coset serves every smaller canonic domain.
     tree = _tree(B, 16)

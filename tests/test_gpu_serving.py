@@ -58,3 +58,16 @@ def test_worker_processes_give_the_same_proofs():
     want = {r.request_id: r.proof_bytes() for r in alone_done}
     for r in done:
         assert r.proof_bytes() == want[r.request_id]
+
+
+def test_native_plain_and_served_forms_agree():
+    # the native provers' plain form (one launch per column per stage), one request at a time, gives
+    # the bytes of the served form (worker threads, batched stages)
+    spec = [(9, "wide_fib"), (5, "poseidon"), (12, "wide_fib"), (4, "poseidon")]
+    reqs = [serving.ProofRequest(i, s, 2000 + 5 * i, k) for i, (s, k) in enumerate(spec)]
+    served, _ = serving.run_stream(3, [(0.0, r) for r in reqs], max_log=12, native=True)
+    plain_reqs = [serving.ProofRequest(i, s, 2000 + 5 * i, k) for i, (s, k) in enumerate(spec)]
+    plain, _ = serving.run_stream(1, [(0.0, r) for r in plain_reqs], max_log=12, native=True, plain=True)
+    assert all(r.error is None for r in served + plain), [r.error for r in served + plain]
+    by_id = {r.request_id: r.proof_bytes() for r in plain}
+    assert all(r.proof_bytes() == by_id[r.request_id] for r in served)
