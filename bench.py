@@ -1160,6 +1160,9 @@ def run_case(args):
             torch.cuda.synchronize()
             lat.append((time.perf_counter() - t0) * 1e3)
         res = {"workload": f"native Poseidon2 proof, 2^{log_n} rows", "ms": [round(x, 3) for x in lat]}
+    elif args.case == "wide-fib-native":  # two native config-1 proofs after two warm-up proofs
+        lat = wide_fib_prove_native(torch, n_proofs=2)
+        res = {"workload": "native Wide-Fibonacci proof, 100 x 2^14", "ms": [round(x, 3) for x in lat]}
     elif args.case == "gkr":
         res = gkr_leg(torch, log_logup=args.gkr_log, log_gp=max(args.gkr_log - 2, 2), n_proofs=1,
                       kernel_log=args.gkr_log)
@@ -1203,7 +1206,8 @@ def main():
     ap.add_argument("--skip-autotune", action="store_true",
                     help="keep the default FFT pass plans (no candidate sweep before timing; for profiling)")
     ap.add_argument("--gkr-log", type=int, default=22, help="log2 values of the --case gkr instance")
-    ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove", "mixed-prove-native", "poseidon-native", "gkr"],
+    ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove", "mixed-prove-native", "poseidon-native",
+                                       "wide-fib-native", "gkr"],
                     help="run one small profiling case instead of the benchmark (for ncu)")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
