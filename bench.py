@@ -199,7 +199,7 @@ class CommitStage:
         rec(4)
         call("cs_fold_circle_into_line", fri_src, FRI_LOG, self.alpha_tabs[0], self.fri_tabs[1],
              self.itw.data_ptr(), self.tw_log, st)
-        # FriOps::fold_line with the 21 remaining challenges: one call, the folds staged in shared memory
+        # FriOps::fold_line with the 21 remaining challenges: one call, the folds in registers and shuffles
         call("cs_fold_line_steps", self.fri_tabs[1], FRI_LOG - 1, FRI_LOG - 1, self.line_alphas,
              self.fri_tabs[FRI_LOG], self.itw.data_ptr(), self.tw_log, st)
         rec(5)
@@ -849,7 +849,7 @@ def run_gpu(args):
                             "unit": "GB/s", "frac": ff(leaf_gbs / hbm), "traffic": traffic,
                             "algorithmic_bytes_per_launch": leaf_bytes,
                             "note": "Blake2s leaf hashing is integer-pipe bound; see int_pipe"},
-        "fold_roofline": {"bound": "hbm", "kernels": "fold_circle_kernel + fold_line_tile_kernel (3 launches)",
+        "fold_roofline": {"bound": "hbm", "kernels": "fold_circle_wide_kernel + fold_line_regs_kernel (3 launches: 2^22 -> 2^21, 11 folds, 10 folds)",
                           "achieved": ff(fold_bytes / (stage_ms["fri_folds"] / 1e3) / 1e9), "peak": hbm,
                           "unit": "GB/s", "frac": ff(fold_bytes / (stage_ms["fri_folds"] / 1e3) / 1e9 / hbm),
                           "algorithmic_bytes": fold_bytes,

@@ -11,6 +11,8 @@
 // (circle_twiddles_from_line_twiddles, cpu/circle.rs:306-323).
 #include <algorithm>
 
+#include <vector>
+
 #include "common.cuh"
 #include "field.cuh"
 
@@ -343,6 +345,142 @@ __global__ void pack_leaves_kernel(const Pack p, uint32_t n_rows) {
   }
 }
 
+// FriOps::fold_line with F <= 11 challenges per launch: every 2^F consecutive values of the layer
+// fold into one, with no shared-memory round trip until the last folds. A thread loads 8
+// consecutive values (two 16-byte words per coordinate) and folds them three times in registers
+// (its four, two and one pairs are its own); the 2^(F-3) threads of a group fold their results
+// over shuffles (lane l pairs with lane l + 2^k, up to five folds), and for F > 8 a group is a
+// whole block whose warps' results meet in shared memory for the rest (up to three). For F <= 8 a
+// block of up to 256 threads holds several groups. Every twiddle a thread needs is loaded before
+// the first fold, so the chain of folds waits on one round of loads. Fold j of the launch pairs
+// values (2i, 2i + 1) of its layer with the layer's inverse twiddle i and the challenge's product
+// table, as fold_line_tile_kernel does. Needs 16-byte aligned coordinates and twiddles, F >= 3,
+// and blockDim.x * gridDim.x = 2^(log_size - 3) with blockDim.x a multiple of 2^(F-3), equal to it
+// for F > 8.
+constexpr uint32_t kRegFoldMax = 11;
+constexpr uint32_t kRegFoldThreads = 256;
+struct RegFoldSteps {
+  qm31_const alpha[kRegFoldMax];
+};
+
+// One pair fold, f0 + f1 + ((f0 - f1) itw) alpha (qm31_ibfly, then the challenge product), with fewer
+// reductions: the sum f0 + f1 (below 2P) enters each coordinate's 64-bit accumulator of the
+// challenge product unreduced (4 (P-1)^2 + 2P < 2^64), and the twiddle product takes the doubled
+// twiddle 2 itw (below 2^32): the high word of d * 2 itw is (d itw) >> 31 and its low word shifted
+// right by one is (d itw) mod 2^31. Canonical inputs give the canonical result of the plain form.
+__device__ __forceinline__ qm31 fold_pair(const qm31& f0, const qm31& f1, uint32_t itw, const qm31_const& alpha) {
+  const uint32_t t2 = itw << 1;
+  const uint32_t a0[4] = {f0.a.a, f0.a.b, f0.b.a, f0.b.b};
+  const uint32_t a1[4] = {f1.a.a, f1.a.b, f1.b.a, f1.b.b};
+  uint32_t d[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint64_t q = (uint64_t)m31_sub(a0[j], a1[j]) * t2;
+    d[j] = m31_reduce_once(((uint32_t)q >> 1) + (uint32_t)(q >> 32));
+  }
+  uint32_t r[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    uint64_t acc = (uint64_t)(a0[i] + a1[i]);
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc += (uint64_t)d[j] * alpha.k[i][j];
+    r[i] = m31_reduce64(acc);
+  }
+  return qm31_make(r[0], r[1], r[2], r[3]);
+}
+
+__device__ __forceinline__ qm31 shfl_down_qm31(const qm31& v, uint32_t delta, uint32_t mask) {
+  return qm31_make(__shfl_down_sync(mask, v.a.a, delta), __shfl_down_sync(mask, v.a.b, delta),
+                   __shfl_down_sync(mask, v.b.a, delta), __shfl_down_sync(mask, v.b.b, delta));
+}
+
+__global__ void __launch_bounds__(kRegFoldThreads, 5) fold_line_regs_kernel(const Coords c, uint32_t log_size,
+                                                                         uint32_t n_folds,
+                                                                         const uint32_t* __restrict__ itw,
+                                                                         uint32_t twiddle_log_size,
+                                                                         const RegFoldSteps steps) {
+  __shared__ uint32_t part[4][8];
+  const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const size_t tw_len = (size_t)1 << twiddle_log_size;
+  // twiddles of fold j of this launch: the inverse-twiddle layer of the line domain of log (log_size - j)
+  const auto layer = [&](uint32_t j) { return itw + (tw_len - ((size_t)1 << (log_size - j))); };
+  const size_t g3 = (size_t)blockIdx.x * blockDim.x + t;  // this thread's index in layer 3
+  const size_t base = 8 * g3;                              // and its first value in layer 0
+  const uint32_t warp_folds = min(5u, n_folds - 3);
+  const uint32_t smem_folds = n_folds > 8 ? n_folds - 8 : 0;
+  // every twiddle up front: layers 0..2 (the register folds), 3..7 (the shuffle folds) and, for warp
+  // 0 of a block of F > 8, 8..10 (the shared-memory folds; lane l takes layer-8 index
+  // blockIdx.x * 2^(F-8) + l, lanes past the block's warps repeat lane 0)
+  const uint4 t0 = __ldg(reinterpret_cast<const uint4*>(layer(0) + 4 * g3));
+  const uint2 t1 = __ldg(reinterpret_cast<const uint2*>(layer(1) + 2 * g3));
+  const uint32_t t2 = __ldg(layer(2) + g3);
+  uint32_t tw_w[5], tw_s[3];
+#pragma unroll
+  for (uint32_t k = 0; k < 5; k++) tw_w[k] = k < warp_folds ? __ldg(layer(3 + k) + (g3 >> (k + 1))) : 0;
+  const uint32_t n_warps = blockDim.x >> 5;
+  const size_t g8 = smem_folds ? ((size_t)blockIdx.x << smem_folds) + (lane < n_warps ? lane : 0) : 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 3; k++)
+    tw_s[k] = (warp == 0 && k < smem_folds) ? __ldg(layer(8 + k) + (g8 >> (k + 1))) : 0;
+  uint32_t w[4][8];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const uint4 lo = __ldg(reinterpret_cast<const uint4*>(c.in[k] + base));
+    const uint4 hi = __ldg(reinterpret_cast<const uint4*>(c.in[k] + base) + 1);
+    w[k][0] = lo.x, w[k][1] = lo.y, w[k][2] = lo.z, w[k][3] = lo.w;
+    w[k][4] = hi.x, w[k][5] = hi.y, w[k][6] = hi.z, w[k][7] = hi.w;
+  }
+  qm31 v[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = qm31_make(w[0][i], w[1][i], w[2][i], w[3][i]);
+  v[0] = fold_pair(v[0], v[1], t0.x, steps.alpha[0]);
+  v[1] = fold_pair(v[2], v[3], t0.y, steps.alpha[0]);
+  v[2] = fold_pair(v[4], v[5], t0.z, steps.alpha[0]);
+  v[3] = fold_pair(v[6], v[7], t0.w, steps.alpha[0]);
+  v[0] = fold_pair(v[0], v[1], t1.x, steps.alpha[1]);
+  v[1] = fold_pair(v[2], v[3], t1.y, steps.alpha[1]);
+  qm31 x = fold_pair(v[0], v[1], t2, steps.alpha[2]);
+  // folds over a group's lanes: lane l keeps the fold of l and l + 2^k when its index in the group is
+  // a multiple of 2^(k+1); the other lanes compute values nobody reads
+  const uint32_t mask = blockDim.x >= 32 ? 0xffffffffu : ((1u << blockDim.x) - 1);
+#pragma unroll
+  for (uint32_t k = 0; k < 5; k++) {
+    if (k < warp_folds) {  // the same for the whole block
+      const qm31 y = shfl_down_qm31(x, 1u << k, mask);
+      x = fold_pair(x, y, tw_w[k], steps.alpha[3 + k]);
+    }
+  }
+  if (smem_folds == 0) {  // groups of 2^(F-3) lanes; the first lane of each writes its value
+    if ((t & ((1u << (n_folds - 3)) - 1)) == 0) {
+      const size_t o = g3 >> (n_folds - 3);
+      c.out[0][o] = x.a.a;
+      c.out[1][o] = x.a.b;
+      c.out[2][o] = x.b.a;
+      c.out[3][o] = x.b.b;
+    }
+    return;
+  }
+  // one group per block: the warps' results (layer-8 indices blockIdx.x * 2^(F-8) + warp) meet
+  if (lane == 0) part[0][warp] = x.a.a, part[1][warp] = x.a.b, part[2][warp] = x.b.a, part[3][warp] = x.b.b;
+  __syncthreads();
+  if (warp != 0) return;
+  const uint32_t l = lane < n_warps ? lane : 0;
+  x = qm31_make(part[0][l], part[1][l], part[2][l], part[3][l]);
+#pragma unroll
+  for (uint32_t k = 0; k < 3; k++) {
+    if (k < smem_folds) {
+      const qm31 y = shfl_down_qm31(x, 1u << k, 0xffffffffu);
+      x = fold_pair(x, y, tw_s[k], steps.alpha[8 + k]);
+    }
+  }
+  if (lane == 0) {
+    c.out[0][blockIdx.x] = x.a.a;
+    c.out[1][blockIdx.x] = x.a.b;
+    c.out[2][blockIdx.x] = x.b.a;
+    c.out[3][blockIdx.x] = x.b.b;
+  }
+}
+
 // Resident blocks of fold_line_stream_kernel on the whole device (SMs x blocks per SM), once.
 uint32_t stream_fold_blocks() {
   static uint32_t blocks = [] {
@@ -449,39 +587,71 @@ extern "C" cs_status cs_fold_line_steps(const uint32_t* const h_src[4], uint32_t
                "fold_line_steps: line domain of log %u is not covered by a tree of log %u", log_size,
                twiddle_log_size);
   cudaStream_t st = to_stream(stream);
-  // Launches of at most kFoldTileLog folds; the layers between two launches go to scratch.
-  uint32_t* scratch = nullptr;
-  const uint32_t first_tile = std::min(log_size, kFoldTileLog);
-  const uint32_t first_folds = std::min(n_alphas, first_tile);
-  if (first_folds < n_alphas) {
-    const size_t words = (size_t)1 << (log_size - first_folds);
-    CS_CUDA(stream_alloc(reinterpret_cast<void**>(&scratch), sizeof(uint32_t) * 8 * std::max<size_t>(words, 4), st));
+  // The folds in launches: of up to kRegFoldMax folds by fold_line_regs_kernel (every source
+  // coordinate and the twiddle tree 16-byte aligned, at least 3 folds of a layer of at least 2^3 values),
+  // otherwise of up to kFoldTileLog folds by the tile kernels; the layers between two launches go to
+  // scratch.
+  // (the register kernel loads 16-byte words of its source and of the twiddles and stores single
+  // words, so the destination may have any 4-byte alignment; scratch layers are 16-byte aligned)
+  bool aligned = (reinterpret_cast<uintptr_t>(d_itwiddles) & 15) == 0;
+  for (int k = 0; k < 4; k++) aligned = aligned && (reinterpret_cast<uintptr_t>(h_src[k]) & 15) == 0;
+  struct Pass {
+    uint32_t folds;
+    bool regs;
+  };
+  std::vector<Pass> passes;
+  size_t scratch_words = 0;
+  for (uint32_t cur = log_size, done = 0; done < n_alphas;) {
+    const uint32_t left = n_alphas - done;
+    Pass ps;
+    ps.regs = aligned && cur >= 3 && left >= 3;
+    ps.folds = ps.regs ? std::min(std::min(left, kRegFoldMax), cur) : std::min(left, std::min(cur, kFoldTileLog));
+    passes.push_back(ps);
+    done += ps.folds;
+    cur -= ps.folds;
+    if (done < n_alphas) scratch_words = std::max(scratch_words, std::max<size_t>((size_t)1 << cur, 4));
   }
+  uint32_t* scratch = nullptr;
+  if (scratch_words)
+    CS_CUDA(stream_alloc(reinterpret_cast<void**>(&scratch), sizeof(uint32_t) * 8 * scratch_words, st));
   Coords c;
   for (int k = 0; k < 4; k++) c.in[k] = h_src[k];
   uint32_t cur_log = log_size, done = 0, ping = 0;
   cudaError_t e = cudaSuccess;
-  while (done < n_alphas && e == cudaSuccess) {
-    const uint32_t tile_log = std::min(cur_log, kFoldTileLog);
-    const uint32_t folds = std::min(n_alphas - done, tile_log);
-    const bool last = done + folds == n_alphas;
-    const size_t out_words = std::max<size_t>((size_t)1 << (log_size - first_folds), 4);
+  for (size_t pi = 0; pi < passes.size() && e == cudaSuccess; pi++) {
+    const uint32_t folds = passes[pi].folds;
+    const bool last = pi + 1 == passes.size();
     for (int k = 0; k < 4; k++)
-      c.out[k] = last ? h_dst[k] : scratch + (size_t)ping * 4 * out_words + (size_t)k * out_words;
-    FoldSteps steps;
-    for (uint32_t j = 0; j < folds; j++) {
-      const uint32_t* a = h_alphas + 4 * (size_t)(done + j);
-      steps.alpha[j] = qm31_const_of(qm31_make(a[0] % P, a[1] % P, a[2] % P, a[3] % P));
+      c.out[k] = last ? h_dst[k] : scratch + (size_t)ping * 4 * scratch_words + (size_t)k * scratch_words;
+    if (passes[pi].regs) {
+      RegFoldSteps steps;
+      for (uint32_t j = 0; j < folds; j++) {
+        const uint32_t* a = h_alphas + 4 * (size_t)(done + j);
+        steps.alpha[j] = qm31_const_of(qm31_make(a[0] % P, a[1] % P, a[2] % P, a[3] % P));
+      }
+      // 2^(cur_log - 3) threads in groups of 2^(folds - 3): for more than 8 folds one group per block,
+      // otherwise blocks of up to kRegFoldThreads
+      const uint32_t group = 1u << (folds - 3);
+      const uint32_t threads = folds > 8 ? group : std::max(group, std::min(kRegFoldThreads, 1u << (cur_log - 3)));
+      fold_line_regs_kernel<<<(1u << (cur_log - 3)) / threads, threads, 0, st>>>(c, cur_log, folds, d_itwiddles,
+                                                                               twiddle_log_size, steps);
+    } else {
+      FoldSteps steps;
+      for (uint32_t j = 0; j < folds; j++) {
+        const uint32_t* a = h_alphas + 4 * (size_t)(done + j);
+        steps.alpha[j] = qm31_const_of(qm31_make(a[0] % P, a[1] % P, a[2] % P, a[3] % P));
+      }
+      const uint32_t tile_log = std::min(cur_log, kFoldTileLog);
+      bool vec = tile_log >= 2;
+      for (int k = 0; k < 4; k++) vec = vec && (reinterpret_cast<uintptr_t>(c.in[k]) & 15) == 0;
+      const uint32_t grid = 1u << (cur_log - tile_log);
+      if (vec)
+        fold_line_stream_kernel<<<std::min(grid, stream_fold_blocks()), kStreamThreads, 0, st>>>(
+            c, cur_log, tile_log, folds, d_itwiddles, twiddle_log_size, grid, steps);
+      else
+        fold_line_tile_kernel<false><<<grid, kFoldThreads, 0, st>>>(c, cur_log, tile_log, folds, d_itwiddles,
+                                                                     twiddle_log_size, steps);
     }
-    bool vec = tile_log >= 2;
-    for (int k = 0; k < 4; k++) vec = vec && (reinterpret_cast<uintptr_t>(c.in[k]) & 15) == 0;
-    const uint32_t grid = 1u << (cur_log - tile_log);
-    if (vec)
-      fold_line_stream_kernel<<<std::min(grid, stream_fold_blocks()), kStreamThreads, 0, st>>>(
-          c, cur_log, tile_log, folds, d_itwiddles, twiddle_log_size, grid, steps);
-    else
-      fold_line_tile_kernel<false><<<grid, kFoldThreads, 0, st>>>(c, cur_log, tile_log, folds, d_itwiddles,
-                                                                   twiddle_log_size, steps);
     note_launch();
     e = cudaGetLastError();
     for (int k = 0; k < 4; k++) c.in[k] = c.out[k];
@@ -491,7 +661,7 @@ extern "C" cs_status cs_fold_line_steps(const uint32_t* const h_src[4], uint32_t
   }
   cudaError_t ef = cudaSuccess;
   if (scratch != nullptr) ef = cudaFreeAsync(scratch, st);
-  if (e != cudaSuccess) return from_cuda(e, "launch fold_line_tile_kernel");
+  if (e != cudaSuccess) return from_cuda(e, "launch fold_line kernel");
   if (ef != cudaSuccess) return from_cuda(ef, "cudaFreeAsync");
   return CS_OK;
 }

@@ -11,9 +11,14 @@
 // order and stops as soon as its next nonce is not below the best nonce found
 // so far (an atomicMin'd 64-bit slot). Every nonce below the final answer is
 // therefore tried, so the answer is the smallest qualifying nonce, like the
-// reference's sequential CpuBackend::grind (cpu/grind.rs:5-15). Each launch
-// has a fixed number of tries per thread; the host relaunches over the next
-// nonce range until one is found or max_nonce is reached.
+// reference's sequential CpuBackend::grind (cpu/grind.rs:5-15). The host
+// relaunches over the next nonce range until one is found or max_nonce is
+// reached. On GB300 the slot's update reaches some SMs late (a relaxed,
+// acquire or volatile load; about one SM in eight polled the old value for
+// dozens of hashes), so the early exit only trims work: the first launch
+// tries one nonce per thread (2^18.2 nonces, enough for the 16-bit OODS and
+// 10-bit FRI work almost always) and each relaunch doubles the tries per
+// thread, up to 64.
 #include <algorithm>
 
 #include "blake2s.cuh"
@@ -64,10 +69,11 @@ GrindPrefix grind_prefix(const uint8_t digest[32], uint32_t pow_bits) {
 cs_status grind_with_slot(const uint8_t digest[32], uint32_t pow_bits, uint64_t max_nonce, uint64_t* nonce_out,
                           unsigned long long* d_best, cudaStream_t st) {
   const GrindPrefix pre = grind_prefix(digest, pow_bits);
-  const uint32_t blocks = 152 * 8, threads = 256, tries = 64;
-  const uint64_t span = (uint64_t)blocks * threads * tries;
+  const uint32_t blocks = 152 * 8, threads = 256;
   unsigned long long best = ~0ull;
-  for (uint64_t base = 0; base < max_nonce; base += span) {
+  uint32_t tries = 1;
+  for (uint64_t base = 0; base < max_nonce;) {
+    const uint64_t span = (uint64_t)blocks * threads * tries;
     CS_CUDA(cudaMemsetAsync(d_best, 0xff, sizeof(unsigned long long), st));
     grind_kernel<<<blocks, threads, 0, st>>>(pre, pow_bits, base, tries, d_best);
     CS_LAUNCHED("grind_kernel");
@@ -78,6 +84,8 @@ cs_status grind_with_slot(const uint8_t digest[32], uint32_t pow_bits, uint64_t 
       return CS_OK;
     }
     if (base + span < base) break;  // wrapped
+    base += span;
+    tries = std::min(64u, 2 * tries);
   }
   set_error("grind: no nonce below %llu has %u trailing zero bits", (unsigned long long)max_nonce, pow_bits);
   return CS_ERR_TIMEOUT;

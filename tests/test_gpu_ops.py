@@ -255,11 +255,12 @@ def test_fri_fold_chain_22(B):
     assert len(g) == 1
 
 
-@pytest.mark.parametrize("log_n,k", [(1, 1), (3, 3), (4, 2), (10, 10), (11, 11), (12, 3), (15, 1),
-                                     (20, 13), (21, 10), (21, 20), (21, 21)])
+@pytest.mark.parametrize("log_n,k", [(1, 1), (3, 3), (4, 2), (5, 5), (8, 8), (9, 4), (10, 10), (11, 11), (12, 3),
+                                     (13, 6), (15, 1), (16, 7), (20, 13), (21, 10), (21, 20), (21, 21)])
 def test_fold_line_with_several_alphas(B, log_n, k):
-    # FriOps::fold_line with k challenges (one launch per 10 folds, tiles in shared memory)
-    # equals k single folds of the oracle; only the last layer is returned.
+    # FriOps::fold_line with k challenges (launches of up to 11 folds in registers, shuffles and
+    # shared memory, or of up to 10 folds through shared-memory tiles) equals k single folds of the
+    # oracle; only the last layer is returned.
     from proving_gb300.backend import SecureColumnByCoords
     tree = _tree(B, log_n + 1)
     coords = qm31_column(300 + log_n, log_n)
@@ -303,8 +304,10 @@ def test_grind_pow_kat(B):
     assert nonce <= 649  # 649 passes at 10 bits (blake2s.rs:234)
 
 
-@pytest.mark.parametrize("bits", [0, 1, 5, 12, 16])
+@pytest.mark.parametrize("bits", [0, 1, 5, 12, 16, 20, 21])
 def test_grind_smallest_nonce(B, bits):
+    # 20 and 21 bits usually need several launches (the first tries 2^18.2 nonces, each next one
+    # twice as many as the one before)
     ch = O.Blake2sChannel()
     ch.mix_u64(0x1111222233334344 + bits)
     assert B.grind(ch.digest, bits) == O.grind(ch.digest, bits)
