@@ -589,6 +589,19 @@ cs_status cs_fold_circle_into_line_device_alpha(const uint32_t *const h_src[4], 
 cs_status cs_channel_mix_root(uint32_t *d_state, const uint32_t *d_root, cs_stream stream);
 cs_status cs_channel_draw_secure_felt(uint32_t *d_state, uint32_t *d_felt, cs_stream stream);
 
+/* The small layers of FriProver::commit (crates/stwo/src/prover/fri.rs:113-207, fold_step 1) in one
+   launch: for j = 0 .. n_layers - 1, the line layer j of log (log_size - j) at h_evals[4j .. 4j+3]
+   (four coordinate columns) is committed into h_trees[j] (the cs_merkle_commit layout of a tree of
+   that height: ((2 << m) - 1) x 8 words, leaves first, root last; 16-byte aligned), its root is
+   mixed into the channel at d_state (cs_channel_mix_root), the folding challenge drawn into
+   d_alphas[4j .. 4j+3] (cs_channel_draw_secure_felt), and the layer folded
+   (cs_fold_line_device_alpha) into h_evals[4(j+1) .. 4(j+1)+3]. The same words as those calls made
+   layer by layer; one block, the layer and the tree level in shared memory. 1 <= n_layers <=
+   log_size <= 10. */
+cs_status cs_fri_commit_fold_tail(uint32_t *d_state, uint32_t *d_alphas, uint32_t *const *h_evals,
+                                  uint32_t *const *h_trees, uint32_t log_size, uint32_t n_layers,
+                                  const uint32_t *d_itwiddles, uint32_t twiddle_log_size, cs_stream stream);
+
 /* ------------------------------------------------------- measurement */
 
 /* Integer-pipe throughput probe (no counterpart in the reference): `blocks` x

@@ -73,6 +73,7 @@ SIGNATURES = {
     "cs_fold_circle_into_line_device_alpha": [vp, u32, vp, vp, vp, u32, vp],
     "cs_channel_mix_root": [vp, vp, vp],
     "cs_channel_draw_secure_felt": [vp, vp, vp],
+    "cs_fri_commit_fold_tail": [vp, vp, vp, vp, u32, u32, vp, u32, vp],
     "cs_logup_running_sums": [u32, vp, vp, vp, vp, vp, vp],
     "cs_gkr_gen_eq_evals": [vp, u32, vp, vp, vp],
     "cs_mle_fix_first_variable": [vp, u32, u32, vp, vp, vp],

@@ -13,6 +13,8 @@
 
 #include <vector>
 
+#include "blake2s.cuh"
+#include "channel.cuh"
 #include "common.cuh"
 #include "field.cuh"
 
@@ -481,6 +483,122 @@ __global__ void __launch_bounds__(kRegFoldThreads, 5) fold_line_regs_kernel(cons
   }
 }
 
+// The small layers of FriProver::commit (crates/stwo/src/prover/fri.rs:113-207) in one block, with
+// the channel on the device: for each line layer of 2^m <= 2^kFriTailMaxLog values, commit it (the
+// lifted Blake2s tree of its four coordinate columns, which all have the tree's height: leaf i is
+// Blake2s of the 16 bytes of value i, crates/stwo/src/prover/backend/cpu/merkle_lifted.rs:46-90;
+// node = Blake2s(left || right), crates/stwo/src/core/vcs_lifted/blake2_merkle.rs:29-36), mix the
+// root into the channel, draw the folding challenge and fold the layer (fold_line,
+// crates/stwo/src/prover/backend/cpu/fri.rs:66-91) into the next one. Every tree, challenge and
+// folded layer is written where the per-layer path (cs_merkle_commit, cs_channel_mix_root,
+// cs_channel_draw_secure_felt, cs_fold_line_device_alpha) writes it; the layer being committed
+// and the tree level being built stay in shared memory, so the layers cost one launch instead of
+// about six each. Thread t hashes leaves 2t and 2t + 1 and their parent.
+constexpr uint32_t kFriTailMaxLog = 10;
+constexpr uint32_t kFriTailThreads = 1u << (kFriTailMaxLog - 1);
+
+struct FriTail {
+  uint32_t* eval[kFriTailMaxLog + 1][4];  // layer j's coordinates; j = n_layers: the last fold's output
+  uint32_t* tree[kFriTailMaxLog];         // layer j's tree, leaves first and root last (16-byte aligned)
+};
+
+__device__ __forceinline__ void store_digest(uint32_t* dst, const uint32_t h[8]) {
+  uint4* o = reinterpret_cast<uint4*>(dst);
+  o[0] = make_uint4(h[0], h[1], h[2], h[3]);
+  o[1] = make_uint4(h[4], h[5], h[6], h[7]);
+}
+
+__global__ void __launch_bounds__(kFriTailThreads) fri_tail_kernel(const __grid_constant__ FriTail T,
+                                                                   uint32_t log_size, uint32_t n_layers,
+                                                                   uint32_t* state, uint32_t* alphas,
+                                                                   const uint32_t* __restrict__ itw,
+                                                                   uint32_t twiddle_log_size, uint32_t one) {
+  __shared__ uint32_t v[4][1u << kFriTailMaxLog];  // the layer being committed and folded
+  __shared__ uint32_t d[kFriTailThreads][8];       // the tree level being built
+  __shared__ uint32_t chan[9];
+  __shared__ uint32_t alpha[4];
+  const uint32_t t = threadIdx.x;
+  const size_t tw_len = (size_t)1 << twiddle_log_size;
+  for (uint32_t i = t; i < (4u << log_size); i += blockDim.x)
+    v[i >> log_size][i & ((1u << log_size) - 1)] = T.eval[0][i >> log_size][i & ((1u << log_size) - 1)];
+  if (t < 9) chan[t] = state[t];
+  __syncthreads();
+  for (uint32_t j = 0; j < n_layers; j++) {
+    const uint32_t m = log_size - j, half = 1u << (m - 1);
+    uint32_t* tree = T.tree[j];
+    if (t < half) {  // leaves 2t, 2t + 1, then node t of level m - 1 (tree word (2^m + t) * 8)
+      uint32_t msg[16], h0[8], h1[8], n[8];
+#pragma unroll
+      for (int k = 4; k < 16; k++) msg[k] = 0;
+#pragma unroll
+      for (int k = 0; k < 4; k++) msg[k] = v[k][2 * t];
+      b2s_init(h0);
+      b2s_compress(h0, msg, 16, 0, true, one);
+#pragma unroll
+      for (int k = 0; k < 4; k++) msg[k] = v[k][2 * t + 1];
+      b2s_init(h1);
+      b2s_compress(h1, msg, 16, 0, true, one);
+      store_digest(tree + (size_t)(2 * t) * 8, h0);
+      store_digest(tree + (size_t)(2 * t + 1) * 8, h1);
+#pragma unroll
+      for (int k = 0; k < 8; k++) msg[k] = h0[k], msg[8 + k] = h1[k];
+      b2s_init(n);
+      b2s_compress(n, msg, 64, 0, true, one);
+      store_digest(tree + ((size_t)(1u << m) + t) * 8, n);
+#pragma unroll
+      for (int k = 0; k < 8; k++) d[t][k] = n[k];
+    }
+    __syncthreads();
+    for (int k = (int)m - 2; k >= 0; k--) {  // level k: node t at tree word (2^(m+1) - 2^(k+1) + t) * 8
+      const bool on = t < (1u << k);
+      uint32_t n[8];
+      if (on) {
+        uint32_t msg[16];
+#pragma unroll
+        for (int w = 0; w < 8; w++) msg[w] = d[2 * t][w], msg[8 + w] = d[2 * t + 1][w];
+        b2s_init(n);
+        b2s_compress(n, msg, 64, 0, true, one);
+      }
+      __syncthreads();
+      if (on) {
+#pragma unroll
+        for (int w = 0; w < 8; w++) d[t][w] = n[w];
+        store_digest(tree + ((size_t)(2u << m) - (2u << k) + t) * 8, n);
+      }
+      __syncthreads();
+    }
+    if (t == 0) {  // mix the root (d[0]), draw the challenge
+      uint32_t c[9], r[8], f[4];
+#pragma unroll
+      for (int w = 0; w < 9; w++) c[w] = chan[w];
+#pragma unroll
+      for (int w = 0; w < 8; w++) r[w] = d[0][w];
+      channel_mix_root(c, r);
+      channel_draw_felt(c, f);
+#pragma unroll
+      for (int w = 0; w < 9; w++) chan[w] = c[w];
+#pragma unroll
+      for (int w = 0; w < 4; w++) alpha[w] = f[w], alphas[4 * j + w] = f[w];
+    }
+    __syncthreads();
+    qm31 r;
+    if (t < half) {  // pair (2t, 2t + 1) folds into value t of the next layer
+      qm31 f0 = qm31_make(v[0][2 * t], v[1][2 * t], v[2][2 * t], v[3][2 * t]);
+      qm31 f1 = qm31_make(v[0][2 * t + 1], v[1][2 * t + 1], v[2][2 * t + 1], v[3][2 * t + 1]);
+      qm31_ibfly(f0, f1, __ldg(itw + (tw_len - ((size_t)1 << m)) + t));
+      r = qm31_add(f0, qm31_mul(qm31_make(alpha[0], alpha[1], alpha[2], alpha[3]), f1));
+      T.eval[j + 1][0][t] = r.a.a;
+      T.eval[j + 1][1][t] = r.a.b;
+      T.eval[j + 1][2][t] = r.b.a;
+      T.eval[j + 1][3][t] = r.b.b;
+    }
+    __syncthreads();
+    if (t < half) v[0][t] = r.a.a, v[1][t] = r.a.b, v[2][t] = r.b.a, v[3][t] = r.b.b;
+    __syncthreads();
+  }
+  if (t < 9) state[t] = chan[t];
+}
+
 // Resident blocks of fold_line_stream_kernel on the whole device (SMs x blocks per SM), once.
 uint32_t stream_fold_blocks() {
   static uint32_t blocks = [] {
@@ -710,5 +828,35 @@ extern "C" cs_status cs_pack_leaves_input(const uint32_t* const h_in[4], uint32_
   const uint32_t rows = 1u << (log_size - 2);
   pack_leaves_kernel<<<grid_for(rows, 256), 256, 0, to_stream(stream)>>>(p, rows);
   CS_LAUNCHED("pack_leaves_kernel");
+  return CS_OK;
+}
+
+extern "C" cs_status cs_fri_commit_fold_tail(uint32_t* d_state, uint32_t* d_alphas, uint32_t* const* h_evals,
+                                             uint32_t* const* h_trees, uint32_t log_size, uint32_t n_layers,
+                                             const uint32_t* d_itwiddles, uint32_t twiddle_log_size,
+                                             cs_stream stream) {
+  CS_CHECK_ARG(d_state != nullptr && d_alphas != nullptr && h_evals != nullptr && h_trees != nullptr &&
+                   d_itwiddles != nullptr,
+               "fri_commit_fold_tail: null pointer");
+  CS_CHECK_ARG(log_size >= 1 && log_size <= kFriTailMaxLog && log_size <= twiddle_log_size,
+               "fri_commit_fold_tail: layer of log %u (1..%u, covered by a tree of log %u)", log_size,
+               kFriTailMaxLog, twiddle_log_size);
+  CS_CHECK_ARG(n_layers >= 1 && n_layers <= log_size, "fri_commit_fold_tail: %u layers from log %u", n_layers,
+               log_size);
+  FriTail T;
+  for (uint32_t j = 0; j <= n_layers; j++)
+    for (int k = 0; k < 4; k++) {
+      T.eval[j][k] = h_evals[4 * j + k];
+      CS_CHECK_ARG(T.eval[j][k] != nullptr, "fri_commit_fold_tail: layer %u coordinate %d is null", j, k);
+    }
+  for (uint32_t j = 0; j < n_layers; j++) {
+    T.tree[j] = h_trees[j];
+    CS_CHECK_ARG(T.tree[j] != nullptr && aligned16(T.tree[j]),
+                 "fri_commit_fold_tail: tree %u null or not 16-byte aligned", j);
+  }
+  const uint32_t threads = std::max(32u, 1u << (log_size - 1));
+  fri_tail_kernel<<<1, threads, 0, to_stream(stream)>>>(T, log_size, n_layers, d_state, d_alphas, d_itwiddles,
+                                                        twiddle_log_size, 1u);
+  CS_LAUNCHED("fri_tail_kernel");
   return CS_OK;
 }

@@ -812,6 +812,30 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
     n_felts++;
   }
   while (line_log >= last_log + 1 && n_felts < 64) {  // every layer above the last folds once
+    if (!cfg.plain && line_log <= 10 && n_felts + (line_log - last_log) <= 64) {
+      // the layers of at most 2^10 values, down to the last layer: one launch (cs_fri_commit_fold_tail)
+      const uint32_t n_tail = line_log - last_log;
+      std::vector<uint32_t*> evals(cur.begin(), cur.end()), tree_bufs;
+      for (uint32_t j = 0; j < n_tail; j++) {
+        FriLayer lay;
+        lay.log_size = line_log - j;
+        lay.eval = std::vector<uint32_t*>(evals.end() - 4, evals.end());
+        lay.tree.height = lay.log_size;
+        lay.tree.layers = A.alloc(((2ull << lay.log_size) - 1) * 8);
+        const uint32_t nl = lay.log_size - 1;
+        uint32_t* blk = A.alloc(4ull << nl);
+        if (!lay.tree.layers || !blk) return A.status;
+        for (int c = 0; c < 4; c++) evals.push_back(blk + ((size_t)c << nl));
+        tree_bufs.push_back(lay.tree.layers);
+        layers.push_back(lay);
+      }
+      HP_TRY(cs_fri_commit_fold_tail(d_state, d_felts + 4 * n_felts, evals.data(), tree_bufs.data(), line_log,
+                                     n_tail, cfg.itw, cfg.tw_log, st));
+      n_felts += n_tail;
+      cur.assign(evals.end() - 4, evals.end());
+      line_log = last_log;
+      break;
+    }
     FriLayer lay;
     lay.log_size = line_log;
     lay.eval = cur;

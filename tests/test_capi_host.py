@@ -254,3 +254,22 @@ def test_native_prover_rejects_unknown_flags(lib):
     n = ctypes.c_size_t(0)
     assert _status(lib, "cs_prove_wide_fib", ctypes.byref(p), cols, None, 0, ctypes.byref(n), None) == 1
     assert b"flags" in lib.cs_last_error()
+
+
+def test_fri_tail_checks_arguments_on_host(lib):
+    # cs_fri_commit_fold_tail: layers of at most 2^10 values, at most log_size layers, trees 16-byte
+    # aligned; rejected before any launch
+    INVALID = 1
+    null = ctypes.c_void_p(0)
+    state, alphas, itw = ctypes.c_void_p(1 << 20), ctypes.c_void_p(1 << 21), ctypes.c_void_p(1 << 22)
+    evals = (ctypes.c_void_p * 12)(*[(1 << 24) + (k << 12) for k in range(12)])
+    trees = (ctypes.c_void_p * 2)(1 << 26, 1 << 27)
+    assert _status(lib, "cs_fri_commit_fold_tail", state, alphas, evals, trees, 11, 2, itw, 12, null) == INVALID
+    assert b"log 11" in lib.cs_last_error()
+    assert _status(lib, "cs_fri_commit_fold_tail", state, alphas, evals, trees, 3, 4, itw, 12, null) == INVALID
+    assert _status(lib, "cs_fri_commit_fold_tail", state, alphas, evals, trees, 3, 0, itw, 12, null) == INVALID
+    assert _status(lib, "cs_fri_commit_fold_tail", state, alphas, evals, trees, 5, 2, itw, 4, null) == INVALID
+    bad = (ctypes.c_void_p * 2)(1 << 26, (1 << 27) + 8)
+    assert _status(lib, "cs_fri_commit_fold_tail", state, alphas, evals, bad, 5, 2, itw, 12, null) == INVALID
+    assert b"16-byte" in lib.cs_last_error()
+    assert _status(lib, "cs_fri_commit_fold_tail", null, alphas, evals, trees, 5, 2, itw, 12, null) == INVALID

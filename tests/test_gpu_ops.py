@@ -321,6 +321,58 @@ def test_grind_gives_up(B):
     assert "TIMEOUT" in str(e.value)
 
 
+@pytest.mark.parametrize("log_size,n_layers", [(1, 1), (3, 3), (6, 2), (10, 10), (10, 9)])
+def test_fri_commit_fold_tail_equals_layer_by_layer(B, log_size, n_layers):
+    # cs_fri_commit_fold_tail writes the trees, challenges, folded layers and channel state that
+    # cs_merkle_commit, cs_channel_mix_root, cs_channel_draw_secure_felt and cs_fold_line_device_alpha
+    # write layer by layer (FriProver::commit's loop, fri.rs:113-207); the folds also equal the oracle's
+    import ctypes
+    from proving_gb300 import _lib
+    from proving_gb300.backend import _stream
+    tree = _tree(B, log_size + 1)
+    itw, tw_log = tree.itwiddles.data_ptr(), tree.log_size
+    layer0 = np.stack([np.asarray(c, np.uint32) for c in qm31_column(800 + log_size, log_size)])
+    rng = np.random.default_rng(log_size)
+    state0 = np.concatenate([rng.integers(0, 1 << 32, 8, dtype=np.uint64).astype(np.uint32), [7]]).astype(np.uint32)
+    vp = ctypes.c_void_p
+
+    def buffers():
+        evals = [torch.tensor(layer0.view(np.int32), device="cuda")]
+        evals += [torch.zeros((4, 1 << (log_size - j - 1)), dtype=torch.int32, device="cuda") for j in range(n_layers)]
+        trees = [torch.zeros(((2 << (log_size - j)) - 1) * 8, dtype=torch.int32, device="cuda") for j in range(n_layers)]
+        state = torch.tensor(state0.view(np.int32), device="cuda")
+        alphas = torch.zeros(4 * n_layers, dtype=torch.int32, device="cuda")
+        return evals, trees, state, alphas
+
+    def tab(t):
+        return (vp * 4)(*[t[k].data_ptr() for k in range(4)])
+
+    ev_a, tr_a, st_a, al_a = buffers()
+    for j in range(n_layers):
+        m = log_size - j
+        logs = (ctypes.c_uint32 * 4)(*([m] * 4))
+        _lib.call("cs_merkle_commit", tab(ev_a[j]), logs, 4, m, tr_a[j].data_ptr(), _stream())
+        _lib.call("cs_channel_mix_root", st_a.data_ptr(), tr_a[j].data_ptr() + 4 * (tr_a[j].numel() - 8), _stream())
+        _lib.call("cs_channel_draw_secure_felt", st_a.data_ptr(), al_a.data_ptr() + 16 * j, _stream())
+        _lib.call("cs_fold_line_device_alpha", tab(ev_a[j]), m, al_a.data_ptr() + 16 * j, tab(ev_a[j + 1]), itw, tw_log,
+                  _stream())
+    ev_b, tr_b, st_b, al_b = buffers()
+    ev_tab = (vp * (4 * (n_layers + 1)))(*[e[k].data_ptr() for e in ev_b for k in range(4)])
+    tr_tab = (vp * n_layers)(*[t.data_ptr() for t in tr_b])
+    _lib.call("cs_fri_commit_fold_tail", st_b.data_ptr(), al_b.data_ptr(), ev_tab, tr_tab, log_size, n_layers, itw,
+              tw_log, _stream())
+    assert torch.equal(st_a, st_b) and torch.equal(al_a, al_b)
+    for j in range(n_layers):
+        assert torch.equal(tr_a[j], tr_b[j]), j
+        assert torch.equal(ev_a[j + 1], ev_b[j + 1]), j
+    w, init = [layer0[k] for k in range(4)], O.line_domain_initial_index(log_size)
+    alphas = al_b.cpu().numpy().view(np.uint32).reshape(n_layers, 4)
+    for j in range(n_layers):
+        w = O.fold_line(w, init, tuple(int(x) for x in alphas[j]))
+        init = O.double_index(init)
+    assert all(np.array_equal(a, b) for a, b in zip(ev_b[n_layers].cpu().numpy().view(np.uint32), w))
+
+
 # ------------------------------------------------------------------ decommitment reads
 
 def test_gather_words_matches_indexing(B):
