@@ -12,6 +12,7 @@ tensors holding M31 words; torch is used only for device memory and streams.
 from __future__ import annotations
 
 import ctypes
+import threading
 from dataclasses import dataclass
 
 import numpy as np
@@ -169,6 +170,19 @@ class TwiddleTree:
 
 
 # ------------------------------------------------------------------ backend
+
+_tls = threading.local()
+
+
+def _words_buffer(cap: int) -> np.ndarray:
+    """This thread's buffer for a native prover's felt words, kept across proofs so its pages are
+    faulted in once (the proof bytes returned are a copy)."""
+    b = getattr(_tls, "words", None)
+    if b is None or b.size < cap:
+        b = np.empty(cap, np.uint64)
+        _tls.words = b
+    return b
+
 
 class CudaBackend:
     """The GB300 backend. Every method enqueues on torch's current CUDA stream."""
@@ -496,7 +510,7 @@ class CudaBackend:
                                                  plain)
         n = ctypes.c_size_t(0)
         cap = 1 << 22
-        words = np.empty(cap, np.uint64)
+        words = _words_buffer(cap)
         claimed = np.zeros((max(1, len(lookup_values)), 4), np.uint32)
         _lib.call("cs_prove_fib_and_lookups", ctypes.byref(params), _ptr_table([c.data for c in cols]),
                   len(lookup_values), _ptr_table([v.data for v in lookup_values]), _u32_table(lookup_logs),
@@ -512,7 +526,7 @@ class CudaBackend:
         params, keep = CudaBackend._proof_params([], [], log_n_rows + 2, fri_params, twiddles, plain)
         n = ctypes.c_size_t(0)
         cap = 1 << 22
-        words = np.empty(cap, np.uint64)
+        words = _words_buffer(cap)
         _lib.call("cs_prove_poseidon", log_n_rows, ctypes.byref(params), words.ctypes.data, cap, ctypes.byref(n),
                   _stream())
         del keep

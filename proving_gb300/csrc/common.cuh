@@ -30,6 +30,14 @@ cudaError_t stream_alloc(void** ptr, size_t bytes, cudaStream_t st);
 
 inline cudaStream_t to_stream(cs_stream s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Reads of runs of device words in one launch and one copy back (gather.cu): request k copies
+// words [index[k], index[k] + offset[k+1] - offset[k]) of table entry slot[k] to out[offset[k] ..];
+// offset has n + 1 entries, offset[n] words in all. Every run is checked against its entry's length
+// on the host first. Synchronous on st.
+cs_status gather_runs(const uint32_t* const* h_table, const uint64_t* h_lengths, uint32_t n_table,
+                      const uint32_t* h_slot, const uint32_t* h_index, const uint32_t* h_offset, uint32_t n,
+                      uint32_t* h_out, cudaStream_t st);
+
 inline uint32_t subgroup_gen(uint32_t log_size) { return 1u << (31 - log_size); }
 
 }  // namespace cs

@@ -278,41 +278,76 @@ std::vector<std::pair<uint32_t, std::vector<uint64_t>>> witness_nodes(uint32_t h
   return out;
 }
 
-// Every device read of a proof's decommitment, collected and made in one cs_gather_u32 call.
+// Every device read of a proof's decommitment, collected and made in one gather_runs call (a digest is
+// one request of 8 words).
+// The vectors keep their capacity from one proof to the next (see reads_for), so a proof's tens of
+// thousands of requests do not fault in fresh pages each time.
 struct Reads {
   std::vector<const uint32_t*> table;
   std::vector<uint64_t> lengths;
   std::map<const uint32_t*, uint32_t> slot_of;
-  std::vector<uint32_t> slots, index;
+  std::vector<uint32_t> slots, index, offset{0};  // offset[k]: request k's first word in out
   std::vector<uint32_t> out;
+  size_t n_words = 0;
+  const uint32_t* last_p = nullptr;  // the most recent slot lookup (requests come in runs per buffer)
+  uint32_t last_slot = 0;
+  void clear() {
+    table.clear();
+    lengths.clear();
+    slot_of.clear();
+    slots.clear();
+    index.clear();
+    offset.assign(1, 0);
+    out.clear();
+    n_words = 0;
+    last_p = nullptr;
+  }
   uint32_t slot(const uint32_t* p, uint64_t len) {
+    if (p == last_p) return last_slot;
     auto it = slot_of.find(p);
-    if (it != slot_of.end()) return it->second;
-    const uint32_t s = (uint32_t)table.size();
-    table.push_back(p);
-    lengths.push_back(len);
-    slot_of[p] = s;
+    uint32_t s;
+    if (it != slot_of.end()) {
+      s = it->second;
+    } else {
+      s = (uint32_t)table.size();
+      table.push_back(p);
+      lengths.push_back(len);
+      slot_of[p] = s;
+    }
+    last_p = p;
+    last_slot = s;
     return s;
   }
-  size_t add(const uint32_t* p, uint64_t len, uint64_t i) {
+  // words [i, i + count) of p (len words): out[returned offset ..]
+  size_t add(const uint32_t* p, uint64_t len, uint64_t i, uint32_t count = 1) {
     slots.push_back(slot(p, len));
     index.push_back((uint32_t)i);
-    return slots.size() - 1;
+    const size_t first = n_words;
+    n_words += count;
+    offset.push_back((uint32_t)n_words);
+    return first;
   }
   cs_status run(cudaStream_t st) {
-    out.assign(slots.size(), 0);
+    out.assign(n_words, 0);
     if (slots.empty()) return CS_OK;
-    return cs_gather_u32(table.data(), lengths.data(), (uint32_t)table.size(), slots.data(), index.data(),
-                         (uint32_t)slots.size(), out.data(), st);
+    return gather_runs(table.data(), lengths.data(), (uint32_t)table.size(), slots.data(), index.data(),
+                       offset.data(), (uint32_t)slots.size(), out.data(), st);
   }
 };
 
+// A cleared Reads of this thread (k: 0 or 1, two can be live in one proof).
+Reads& reads_for(int k) {
+  thread_local Reads pool[2];
+  pool[k].clear();
+  return pool[k];
+}
+
 // A tree's witness digests registered with a Reads: (first read, count of digests).
 std::pair<size_t, size_t> read_witness(Reads& R, const Tree& t, const std::vector<uint64_t>& q) {
-  size_t first = R.slots.size(), n = 0;
+  size_t first = R.n_words, n = 0;
   for (auto& [k, nodes] : witness_nodes(t.height, q))
     for (uint64_t node : nodes) {
-      for (int w = 0; w < 8; w++) R.add(t.layers, t.words(), t.node_word(k, node) + w);
+      R.add(t.layers, t.words(), t.node_word(k, node), 8);
       n++;
     }
   return {first, n};
@@ -368,7 +403,7 @@ std::vector<qm31> powers(const qm31& f, uint32_t n) {
 }
 
 struct Words {
-  std::vector<uint64_t> w;
+  std::vector<uint64_t>& w;
   void u(uint64_t x) { w.push_back(x); }
   void q(const qm31& x) {
     w.push_back(x.a.a);
@@ -856,15 +891,15 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   // the state, every layer root and the last layer's evaluation back in one read
   std::vector<qm31> last_poly;
   {
-    Reads R;
-    for (int i = 0; i < 9; i++) R.add(d_state, 9, i);
+    Reads& R = reads_for(0);
+    R.add(d_state, 9, 0, 9);
     std::vector<Tree*> ts = {&first_tree};
     for (FriLayer& l : layers) ts.push_back(&l.tree);
     for (Tree* t : ts)
-      for (int i = 0; i < 8; i++) R.add(t->layers, t->words(), t->words() - 8 + i);
+      R.add(t->layers, t->words(), t->words() - 8, 8);
     const uint32_t last_n = 1u << last_log;
     for (int c = 0; c < 4; c++)
-      for (uint32_t i = 0; i < last_n; i++) R.add(cur[c], last_n, i);
+      R.add(cur[c], last_n, 0, last_n);
     HP_TRY(R.run(st));
     for (int i = 0; i < 8; i++)
       for (int k = 0; k < 4; k++) ch.digest[4 * i + k] = (uint8_t)(R.out[i] >> (8 * k));
@@ -900,7 +935,7 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   queries.erase(std::unique(queries.begin(), queries.end()), queries.end());
 
   // --- decommitments: every read registered, one gather
-  Reads R;
+  Reads& R = reads_for(1);
   struct LayerDec {
     std::vector<uint64_t> positions;
     std::vector<bool> is_witness;
@@ -918,9 +953,9 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
         d.positions.push_back(s0 + j);
         d.is_witness.push_back(!std::binary_search(q.begin(), q.end(), s0 + j));
       }
-    d.coord_first = R.slots.size();
-    for (int c = 0; c < 4; c++)
-      for (uint64_t p : d.positions) R.add(eval[c], 1ull << log_size, p);
+    d.coord_first = R.n_words;
+    for (int c = 0; c < 4; c++)  // positions are the pairs (s0, s0 + 1): one 2-word read each
+      for (uint64_t s0 : starts) R.add(eval[c], 1ull << log_size, s0, 2);
     d.wit = read_witness(R, t, d.positions);
     return d;
   };
@@ -943,7 +978,7 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   std::vector<TreeDec> tree_decs;
   for (TreeCols& t : trees) {  // MerkleProverLifted::decommit: queried values per column, then the witness
     TreeDec d;
-    d.values_first = R.slots.size();
+    d.values_first = R.n_words;
     for (const Col& c : t.cols) {
       const uint32_t shift = L - c.log;
       for (uint64_t q : queries) R.add(c.p, 1ull << c.log, ((q >> (shift + 1)) << 1) + (q & 1));
@@ -969,7 +1004,8 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   }
 
   // --- the felt stream (CairoSerialize for StarkProof)
-  Words W;
+  words.clear();
+  Words W{words};
   W.u(cfg.pow_bits);
   W.u(b);
   W.u(cfg.log_last_layer_degree_bound);
@@ -1019,7 +1055,6 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   for (const qm31& c : last_poly) W.q(c);
   W.u(cfg.log_last_layer_degree_bound);
   W.u(fri_pow);
-  words.swap(W.w);
   return CS_OK;
 }
 
@@ -1294,6 +1329,12 @@ extern "C" cs_status cs_host_blake2s(const uint8_t* msg, size_t n, uint8_t out[3
 
 namespace {
 
+// This thread's proof words: the vector keeps its capacity across proofs.
+std::vector<uint64_t>& proof_words() {
+  thread_local std::vector<uint64_t> words;
+  return words;
+}
+
 cs_status finish(std::vector<uint64_t>& words, uint64_t* h_words, size_t capacity, size_t* n_words) {
   *n_words = words.size();
   CS_CHECK_ARG(h_words == nullptr || capacity >= words.size(), "prove: %zu words do not fit in %zu", words.size(),
@@ -1360,7 +1401,7 @@ extern "C" cs_status cs_prove_fib_and_lookups(const cs_wide_fib_proof_params* pa
   if (n_lookups) air.lookup_logs.assign(h_lookup_log_sizes, h_lookup_log_sizes + n_lookups);
   air.d_trace = d_trace;
   air.d_values = d_values;
-  std::vector<uint64_t> words;
+  std::vector<uint64_t>& words = proof_words();
   std::vector<qm31> claimed;
   const cs_status s = hp::prove(config_of(pp), air, words, claimed, to_stream(stream));
   if (s != CS_OK) return s;
@@ -1382,7 +1423,7 @@ extern "C" cs_status cs_prove_poseidon(uint32_t log_n_rows, const cs_wide_fib_pr
   if (cs != CS_OK) return cs;
   hp::PoseidonAir air;
   air.log_n = log_n_rows;
-  std::vector<uint64_t> words;
+  std::vector<uint64_t>& words = proof_words();
   std::vector<qm31> claimed;
   const cs_status s = hp::prove(config_of(*params), air, words, claimed, to_stream(stream));
   if (s != CS_OK) return s;
@@ -1831,7 +1872,9 @@ extern "C" cs_status cs_gkr_prove_batch(uint32_t n_instances, const uint32_t* h_
   for (int i = 0; i < 8; i++)
     for (int b = 0; b < 4; b++) ch.digest[4 * i + b] = (uint8_t)(h_channel[i] >> (8 * b));
   ch.n_draws = h_channel[8];
-  hp::Words words;
+  std::vector<uint64_t>& proof = proof_words();
+  proof.clear();
+  hp::Words words{proof};
   cs_status s;
   {
     hp::Arena arena(st);
