@@ -37,13 +37,20 @@ CSRC = Path(__file__).resolve().parent / "csrc"
 
 # ------------------------------------------------------------------ expressions
 
+_NODE_IDS: dict = {}  # (op, child keys / literal args) -> key: equal expressions share one key
+
+
 class Expr:
-    """A node of the constraint DAG; `ext` marks QM31 values (else M31)."""
+    """A node of the constraint DAG; `ext` marks QM31 values (else M31). `key` is an integer shared
+    by structurally equal expressions (hash-consing over the children's keys), so keys hash in
+    constant time however large the expression tree under a node grows (Poseidon2's partial rounds
+    fold every state word into every other, round after round)."""
     __slots__ = ("op", "args", "ext", "key")
 
     def __init__(self, op: str, args: tuple, ext: bool):
         self.op, self.args, self.ext = op, args, ext
-        self.key = (op,) + tuple(a.key if isinstance(a, Expr) else a for a in args)
+        k = (op,) + tuple(a.key if isinstance(a, Expr) else a for a in args)
+        self.key = _NODE_IDS.setdefault(k, len(_NODE_IDS))
 
     def _bin(self, op, other, swap=False):
         other = _lift(other)
@@ -108,6 +115,7 @@ class Evaluator:
         self.columns: dict[int, int] = {}    # interaction -> columns taken so far
         self.params: list[str] = []
         self.constraints: list[Expr] = []
+        self.fracs: list[tuple[Expr, Expr]] = []  # LogUp fractions (numerator, denominator) of the row
 
     def _mask(self, interaction: int, column: int, offset: int) -> Expr:
         if offset not in (0, -1):
@@ -121,6 +129,58 @@ class Evaluator:
 
     def next_trace_mask(self) -> Expr:
         return self.next_interaction_mask(1)[0]
+
+    def next_extension_interaction_mask(self, interaction: int, offsets=(0,)) -> list:
+        """EvalAtRow::next_extension_interaction_mask: the next four columns of `interaction` (a QM31
+        column by its coordinates) at each offset, combined per offset (combine_ef)."""
+        cols = [self.next_interaction_mask(interaction, offsets) for _ in range(4)]
+        return [self.secure(*[c[k] for c in cols]) for k in range(len(offsets))]
+
+    def add_to_relation(self, relation: str, multiplicity, values) -> None:
+        """EvalAtRow::add_to_relation (crates/constraint-framework/src/lib.rs:145-151): the fraction
+        multiplicity / combine(values) joins the row's LogUp sum, with LookupElements::combine
+        (crates/constraint-framework/src/logup.rs:80-94) = sum_i alpha^i values[i] - z; z and the
+        alpha powers are the parameters `{relation}_z` and `{relation}_alpha{i}`."""
+        den = None
+        for i, v in enumerate(values):
+            term = self.param(f"{relation}_alpha{i}") * _lift(v)
+            den = term if den is None else den + term
+        den = den - self.param(f"{relation}_z")
+        self.fracs.append((_lift(multiplicity), den))
+
+    def finalize_logup_batched(self, batch_size: int, interaction: int = 2, shift: str = "shift") -> None:
+        """finalize_logup_batched (the logup_proxy macro, crates/constraint-framework/src/lib.rs:
+        185-221): the row's fractions summed in consecutive batches of batch_size (a/b + c/d =
+        (ad + cb)/(bd)); every batch but the last has a cumulative-sum column of `interaction`
+        (the constraint (cur - previous column) den - num = 0), and the last one the running sum's
+        column read at the previous row too: (cur - prev_row - previous column + shift) den - num
+        = 0, with shift = claimed sum / 2^log_size (the parameter `shift`)."""
+        assert self.fracs and batch_size > 0, "no LogUp fractions to finalize"
+        batches = []
+        for i in range(0, len(self.fracs), batch_size):
+            num, den = self.fracs[i]
+            for n2, d2 in self.fracs[i + 1:i + batch_size]:
+                num, den = num * d2 + n2 * den, den * d2
+            batches.append((num, den))
+        self.fracs = []
+        last_num, last_den = batches.pop()
+        prev_col = None
+        for num, den in batches:
+            [cur] = self.next_extension_interaction_mask(interaction, (0,))
+            diff = cur if prev_col is None else cur - prev_col
+            prev_col = cur
+            self.add_constraint(diff * den - num)
+        prev_row, cur = self.next_extension_interaction_mask(interaction, (-1, 0))
+        diff = cur - prev_row if prev_col is None else cur - prev_row - prev_col
+        self.add_constraint((diff + self.param(shift)) * last_den - last_num)
+
+    def finalize_logup(self, **kw) -> None:
+        """finalize_logup: no batching (lib.rs:224-226)."""
+        self.finalize_logup_batched(1, **kw)
+
+    def finalize_logup_in_pairs(self, **kw) -> None:
+        """finalize_logup_in_pairs: batches of two (lib.rs:230-232)."""
+        self.finalize_logup_batched(2, **kw)
 
     def secure(self, b0, b1, b2, b3) -> Expr:
         """SecureField::from_partial_evals of four M31 values."""
@@ -171,6 +231,43 @@ class Air:
         return [columns_by_interaction[m.interaction][m.column] for m in self.masks]
 
 
+_SPLIT_OPS = {"m31_mul": ("uint32_t", "uint32_t a, uint32_t b"), "qm31_add": ("qm31", "qm31 a, qm31 b"),
+              "qm31_sub": ("qm31", "qm31 a, qm31 b"), "qm31_mul": ("qm31", "qm31 a, qm31 b"),
+              "qm31_mul_m31": ("qm31", "qm31 a, uint32_t b")}
+_SINGLE_LINES = 1500  # bodies up to this many lines stay one function
+_CHUNK_NODES = 300    # computed nodes per function of a split body
+_LEAVES = ("mask", "const", "param")
+
+
+def _chunks(constraints, budget: int):
+    """Splits the constraints, in order, into chunks of about `budget` computed nodes (any node but
+    a mask, constant or parameter). A node belongs to the first chunk that reaches it; a later
+    chunk that needs it reads it back instead of recomputing it. Returns (chunks of constraint
+    indices, owner chunk of each computed node's key, keys of the nodes read by a later chunk)."""
+    owner, exported, chunks, size = {}, set(), [[]], 0
+    for k, c in enumerate(constraints):
+        if size >= budget and chunks[-1]:
+            chunks.append([])
+            size = 0
+        ch = len(chunks) - 1
+        stack, seen = [c], set()
+        while stack:
+            x = stack.pop()
+            if x.key in seen or x.op in _LEAVES:
+                continue
+            seen.add(x.key)
+            o = owner.get(x.key)
+            if o is not None:
+                if o != ch:
+                    exported.add(x.key)
+                continue
+            owner[x.key] = ch
+            size += 1
+            stack.extend(a for a in x.args if isinstance(a, Expr))
+        chunks[-1].append(k)
+    return chunks, owner, exported
+
+
 def compile_air(name: str, evaluate, *args) -> Air:
     """Records `evaluate(e, *args)` and generates the kernel source."""
     e = Evaluator()
@@ -179,9 +276,28 @@ def compile_air(name: str, evaluate, *args) -> Air:
     order, slot = [], {}
     temps, lines = {}, []
 
+    split = {"chunk": None, "owner": {}, "slot": {}}  # set while emitting a split body
+
+    def op_name(fn: str) -> str:
+        """A split body calls its QM31 operations and M31 products through non-inlined wrappers
+        (_SPLIT_OPS), the kernel's sum of the functions too: the device compiler then has about half
+        as much code to optimize (a 1,144-constraint body: 66 -> 36 s)."""
+        return f"air_{fn}" if split["chunk"] is not None and fn in _SPLIT_OPS else fn
+
     def visit(x: Expr) -> str:
         if x.key in temps:
             return temps[x.key]
+        ch = split["chunk"]
+        if ch is not None and x.op not in _LEAVES and split["owner"][x.key] < ch:
+            # computed by an earlier function of a split body: read back from xs
+            o = split["slot"][x.key]
+            name = f"x{len(temps)}"
+            if x.ext:
+                lines.append(f"  const qm31 {name} = qm31_make(xs[{o}], xs[{o + 1}], xs[{o + 2}], xs[{o + 3}]);")
+            else:
+                lines.append(f"  const uint32_t {name} = xs[{o}];")
+            temps[x.key] = name
+            return name
         if x.op == "mask":
             k = x.args
             if k not in slot:
@@ -213,28 +329,90 @@ def compile_air(name: str, evaluate, *args) -> Air:
                 a, b = x.args
                 fn = {"add": "add", "sub": "sub", "mul": "mul"}[x.op]
                 if not x.ext:
-                    rhs = f"m31_{fn}({ops[0]}, {ops[1]})"
+                    rhs = f"{op_name('m31_' + fn)}({ops[0]}, {ops[1]})"
                 elif a.ext and b.ext:
-                    rhs = f"qm31_{fn}({ops[0]}, {ops[1]})"
+                    rhs = f"{op_name('qm31_' + fn)}({ops[0]}, {ops[1]})"
                 elif fn == "mul":  # one side M31
                     q, m = (ops[0], ops[1]) if a.ext else (ops[1], ops[0])
-                    rhs = f"qm31_mul_m31({q}, {m})"
+                    rhs = f"{op_name('qm31_mul_m31')}({q}, {m})"
                 else:
                     qa = ops[0] if a.ext else f"qm31_make({ops[0]}, 0, 0, 0)"
                     qb = ops[1] if b.ext else f"qm31_make({ops[1]}, 0, 0, 0)"
-                    rhs = f"qm31_{fn}({qa}, {qb})"
+                    rhs = f"{op_name('qm31_' + fn)}({qa}, {qb})"
             lines.append(f"  const {ty} {name} = {rhs};")
         temps[x.key] = name
         return name
 
-    body = []
-    for k, c in enumerate(e.constraints):
-        v = visit(c)
-        body.extend(lines)
-        lines.clear()
-        w = f"qm31_make(rc[{4 * k}], rc[{4 * k + 1}], rc[{4 * k + 2}], rc[{4 * k + 3}])"
-        body.append(f"  acc = qm31_add(acc, {'qm31_mul' if c.ext else 'qm31_mul_m31'}({w}, {v}));")
-    src = _PRELUDE + f"""
+    def emit(ks) -> list:
+        """The lines that add constraints ks (indices) to acc, sharing the current temps."""
+        body = []
+        for k in ks:
+            c = e.constraints[k]
+            v = visit(c)
+            body.extend(lines)
+            lines.clear()
+            w = f"qm31_make(rc[{4 * k}], rc[{4 * k + 1}], rc[{4 * k + 2}], rc[{4 * k + 3}])"
+            body.append(f"  acc = {op_name('qm31_add')}(acc, {op_name('qm31_mul' if c.ext else 'qm31_mul_m31')}({w}, {v}));")
+        return body
+
+    # One straight-line body when it is small. The device compiler's optimizer takes time
+    # superlinear in the size of one function (Poseidon2's 1,144 constraints in one body did not
+    # compile in ten minutes, one instance's 143 took over a minute), so a large AIR is split, in
+    # constraint order, into non-inlined device functions of about _CHUNK_NODES computed nodes; a
+    # value one function computes and a later one needs passes through the thread's array xs.
+    funcs, calls, xs_words = "", "", 0
+    body = emit(range(len(e.constraints)))
+    if len(body) <= _SINGLE_LINES:
+        inline = chr(10).join('  ' + l for l in body)
+    else:
+        chunks, owner, exported = _chunks(e.constraints, _CHUNK_NODES)
+        nodes = {}
+
+        def collect(x):
+            stack = [x]
+            while stack:
+                y = stack.pop()
+                if y.key in nodes:
+                    continue
+                nodes[y.key] = y
+                stack.extend(a for a in y.args if isinstance(a, Expr))
+        for c in e.constraints:
+            collect(c)
+        xslot = {}
+        for key in sorted(exported, key=lambda kk: owner[kk]):
+            xslot[key] = xs_words
+            xs_words += 4 if nodes[key].ext else 1
+        split.update(owner=owner, slot=xslot)
+        for g, ks in enumerate(chunks):
+            temps.clear()
+            split["chunk"] = g
+            lines_g = emit(ks)
+            for key in [kk for kk in exported if owner[kk] == g]:
+                o, t = xslot[key], temps[key]
+                if nodes[key].ext:
+                    lines_g.append(f"  xs[{o}] = {t}.a.a; xs[{o + 1}] = {t}.a.b; xs[{o + 2}] = {t}.b.a; "
+                                   f"xs[{o + 3}] = {t}.b.b;")
+                else:
+                    lines_g.append(f"  xs[{o}] = {t};")
+            funcs += f"""
+__device__ __noinline__ qm31 cs_air_group{g}(const uint32_t* const* __restrict__ cols,
+                                            const uint32_t* __restrict__ rc,
+                                            const uint32_t* __restrict__ params, uint32_t r, uint32_t pr,
+                                            uint32_t* xs) {{
+  (void)params;
+  (void)pr;
+  (void)xs;
+  qm31 acc = qm31_make(0, 0, 0, 0);
+{chr(10).join(lines_g)}
+  return acc;
+}}
+"""
+            calls += f"    acc = air_qm31_add(acc, cs_air_group{g}(cols, rc, params, r, pr, xs));\n"
+        split["chunk"] = None
+        inline = f"    uint32_t xs[{max(xs_words, 1)}];\n" + calls.rstrip("\n")
+        funcs = "".join(f"__device__ __noinline__ {ty} air_{fn}({args}) {{ return {fn}(a, b); }}\n"
+                        for fn, (ty, args) in _SPLIT_OPS.items()) + funcs
+    src = _PRELUDE + funcs + f"""
 // AIR {name}: {len(order)} masks, {len(e.constraints)} constraints, {len(e.params)} parameters
 extern "C" __global__ void __launch_bounds__(256) cs_air_composition(
     const uint32_t* const* __restrict__ cols, const uint32_t* __restrict__ rc, const uint32_t* __restrict__ params,
@@ -245,7 +423,7 @@ extern "C" __global__ void __launch_bounds__(256) cs_air_composition(
     const uint32_t pr = prev_row(r, trace_log, eval_log);
     (void)pr;
     qm31 acc = qm31_make(0, 0, 0, 0);
-{chr(10).join('  ' + l for l in body)}
+{inline}
     const qm31 v = qm31_mul_m31(acc, den[r >> trace_log]);
     a0[r] = m31_add(a0[r], v.a.a);
     a1[r] = m31_add(a1[r], v.a.b);
@@ -325,3 +503,115 @@ def single_lookup_air(e: Evaluator) -> None:
     cur = e.secure(*[c[1] for c in coords])
     z, shift = e.param("z"), e.param("shift")
     e.add_constraint((cur - prev + shift) * (v - z) + 1)
+
+
+# Poseidon2 (crates/examples/src/poseidon/mod.rs:34-47): 8 instances per row, a 16-word state,
+# 4 + 4 full rounds around 14 partial rounds, every round constant 1234.
+POSEIDON_INSTANCES_PER_ROW = 8
+POSEIDON_STATE = 16
+POSEIDON_PARTIAL_ROUNDS = 14
+POSEIDON_HALF_FULL_ROUNDS = 4
+POSEIDON_ROUND_CONST = 1234
+
+
+def _apply_m4(x):
+    """apply_m4 (mod.rs:74-90): the M4 MDS matrix of eprint 2023/323 section 5.1."""
+    t0 = x[0] + x[1]
+    t02 = t0 + t0
+    t1 = x[2] + x[3]
+    t12 = t1 + t1
+    t2 = x[1] + x[1] + t1
+    t3 = x[3] + x[3] + t0
+    t4 = t12 + t12 + t3
+    t5 = t02 + t02 + t2
+    t6 = t3 + t5
+    t7 = t2 + t4
+    return [t6, t5, t7, t4]
+
+
+def _apply_external_round_matrix(state) -> None:
+    """apply_external_round_matrix (mod.rs:93-115): circ(2 M4, M4, M4, M4)."""
+    for i in range(4):
+        state[4 * i:4 * i + 4] = _apply_m4(state[4 * i:4 * i + 4])
+    for j in range(4):
+        s = state[j] + state[j + 4] + state[j + 8] + state[j + 12]
+        for i in range(4):
+            state[4 * i + j] = state[4 * i + j] + s
+
+
+def _apply_internal_round_matrix(state) -> None:
+    """apply_internal_round_matrix (mod.rs:118-129): s_i <- s_i 2^(i+1) + sum of the state."""
+    total = state[0]
+    for x in state[1:]:
+        total = total + x
+    for i in range(POSEIDON_STATE):
+        state[i] = state[i] * (1 << (i + 1)) + total
+
+
+def _pow5(x):
+    x2 = x * x
+    x4 = x2 * x2
+    return x4 * x
+
+
+def poseidon_air(e: Evaluator) -> None:
+    """eval_poseidon_constraints (crates/examples/src/poseidon/mod.rs:137-187): per instance the
+    round constraints (each S-box output equals its trace column), then the state lookups (the
+    initial state with multiplicity 1, the final state with -1, relation `poseidon`), finalized in
+    pairs. Parameters: poseidon_z, poseidon_alpha0..15 (LookupElements), shift."""
+    for _ in range(POSEIDON_INSTANCES_PER_ROW):
+        state = [e.next_trace_mask() for _ in range(POSEIDON_STATE)]
+        initial = list(state)
+        for half in range(2):
+            if half == 1:
+                for _ in range(POSEIDON_PARTIAL_ROUNDS):
+                    state[0] = state[0] + POSEIDON_ROUND_CONST
+                    _apply_internal_round_matrix(state)
+                    state[0] = _pow5(state[0])
+                    m = e.next_trace_mask()
+                    e.add_constraint(state[0] - m)
+                    state[0] = m
+            for _ in range(POSEIDON_HALF_FULL_ROUNDS):
+                state = [x + POSEIDON_ROUND_CONST for x in state]
+                _apply_external_round_matrix(state)
+                state = [_pow5(x) for x in state]
+                for i in range(POSEIDON_STATE):
+                    m = e.next_trace_mask()
+                    e.add_constraint(state[i] - m)
+                    state[i] = m
+        e.add_to_relation("poseidon", 1, initial)
+        e.add_to_relation("poseidon", -1, state)
+    e.finalize_logup_in_pairs()
+
+
+_POSEIDON_AIR = []
+
+
+def poseidon_air_recorded() -> Air:
+    """poseidon_air recorded once per process (its kernel is then compiled once, CompiledAir.get)."""
+    if not _POSEIDON_AIR:
+        _POSEIDON_AIR.append(compile_air("poseidon", poseidon_air))
+    return _POSEIDON_AIR[0]
+
+
+def poseidon_params(lookup, claimed, trace_log: int) -> dict:
+    """The parameters of poseidon_air from the drawn lookup elements (z, alpha: 8 words) and the
+    claimed sum: alpha^i (LookupElements::draw, logup.rs:70-79) and shift = claimed / 2^trace_log."""
+    def mul(a, b):
+        a0, a1, a2, a3 = (int(x) for x in a)
+        b0, b1, b2, b3 = (int(x) for x in b)
+        # (a + b u)(c + d u) with u^2 = 2 + i over CM31 = M31[i]/(i^2 + 1)
+        ac = ((a0 * b0 - a1 * b1) % P, (a0 * b1 + a1 * b0) % P)
+        bd = ((a2 * b2 - a3 * b3) % P, (a2 * b3 + a3 * b2) % P)
+        ad = ((a0 * b2 - a1 * b3) % P, (a0 * b3 + a1 * b2) % P)
+        bc = ((a2 * b0 - a3 * b1) % P, (a2 * b1 + a3 * b0) % P)
+        rbd = ((2 * bd[0] - bd[1]) % P, (bd[0] + 2 * bd[1]) % P)
+        return ((ac[0] + rbd[0]) % P, (ac[1] + rbd[1]) % P, (ad[0] + bc[0]) % P, (ad[1] + bc[1]) % P)
+    z, alpha = tuple(int(x) for x in lookup[:4]), tuple(int(x) for x in lookup[4:8])
+    params, cur = {"poseidon_z": z}, (1, 0, 0, 0)
+    for i in range(POSEIDON_STATE):
+        params[f"poseidon_alpha{i}"] = cur
+        cur = mul(cur, alpha)
+    inv = pow(1 << trace_log, P - 2, P)
+    params["shift"] = tuple(int(x) * inv % P for x in claimed)
+    return params

@@ -150,9 +150,11 @@ def composition_at_point(point, trace_mask, inter_mask, lookup, claimed, random_
 # ------------------------------------------------------------ the prover
 
 def prove_poseidon(ops, log_n_rows: int, config: pr.PcsConfig, channel: pr.Blake2sChannel, twiddles,
-                   check: bool = True):
+                   check: bool = True, generic: bool = False):
     """prove_poseidon (mod.rs:320-379) + prove_ex (crates/stwo/src/prover/mod.rs:39-138).
-    twiddles: for CanonicCoset(log_n_rows + LOG_EXPAND + log_blowup_factor)."""
+    twiddles: for CanonicCoset(log_n_rows + LOG_EXPAND + log_blowup_factor). generic=True evaluates
+    the constraints through the generic path (proving_gb300.framework.poseidon_air, a run-time
+    compiled kernel) instead of the hand-written composition kernel."""
     fp = config.fri_params
     b = fp.log_blowup_factor
     L = config.trace_lifting_log_size
@@ -198,7 +200,12 @@ def prove_poseidon(ops, log_n_rows: int, config: pr.PcsConfig, channel: pr.Blake
         raise NotImplementedError("log_blowup_factor above the constraint degree (SubDomain with expansion)")
     rc = np.asarray(list(reversed(pr.secure_powers(random_coeff, N_CONSTRAINTS))), np.uint32)
     accum = ops.secure_zeros(1 << eval_log)
-    ops.poseidon_composition(trace_eval, inter_eval, n, lookup, claimed, rc, accum)
+    if generic:
+        from . import framework as fw
+        ops.air_composition(fw.poseidon_air_recorded(), {1: trace_eval, 2: inter_eval}, n,
+                            fw.poseidon_params(lookup, claimed, n), rc, accum)
+    else:
+        ops.poseidon_composition(trace_eval, inter_eval, n, lookup, claimed, rc, accum)
     del trace_eval, inter_eval
     comp_coeffs = ops.interpolate_secure(accum, twiddles)
     left, right = ops.split_at_mid(comp_coeffs)

@@ -84,7 +84,7 @@ class CpuOps:
         return cols, claimed
 
     def air_composition(self, air, columns_by_interaction, trace_log, params, rc, accum):
-        from .air_eval import air_composition
+        from oracle.air_eval import air_composition
         cols = {k: [c.v for c in v] for k, v in columns_by_interaction.items()}
         accum.c = air_composition(air, cols, len(accum).bit_length() - 1, trace_log, params, rc, out=accum.c)
 

@@ -49,3 +49,54 @@ def test_generated_source_shape():
     assert air2.source.count("__ldg(cols[") == 5
     # 3 constraints use the squares of columns 0..3; each square is computed once
     assert air2.source.count("m31_mul(") == 4
+
+
+def _relation_lookup_air(e):
+    # single_lookup_air through add_to_relation + finalize_logup (crates/constraint-framework/src/
+    # lib.rs:145-151, 185-226): multiplicity -1, values [v], relation "lookup"
+    e.add_to_relation("lookup", -1, [e.next_trace_mask()])
+    e.finalize_logup()
+
+
+@pytest.mark.parametrize("trace_log,eval_log", [(2, 3), (5, 6)])
+def test_relation_entries_finalized_like_the_hand_written_logup(trace_log, eval_log):
+    # one entry, no batching: the constraint of single_lookup_air, with z = lookup_z and alpha^0 = 1
+    air = fw.compile_air("lookup_rel", _relation_lookup_air)
+    assert air.n_constraints == 1 and air.params == ["lookup_alpha0", "lookup_z", "shift"]
+    v = m31_column(15, eval_log)
+    inter = [m31_column(16 + k, eval_log) for k in range(4)]
+    z, claimed, rc = seeded_qm31(21), seeded_qm31(22), seeded_qm31(23)
+    shift = (np.asarray(claimed, np.int64) * pow(1 << trace_log, O.P - 2, O.P) % O.P).astype(np.uint32)
+    params = {"lookup_alpha0": (1, 0, 0, 0), "lookup_z": z, "shift": shift}
+    got = air_composition(air, {1: [v], 2: inter}, eval_log, trace_log, params, [rc])
+    want = O.logup_composition(v, inter, trace_log, z, claimed, rc)
+    assert all(np.array_equal(g, w) for g, w in zip(got, want))
+
+
+def test_finalize_batches_need_fractions():
+    e = fw.Evaluator()
+    with pytest.raises(AssertionError):
+        e.finalize_logup_in_pairs()
+
+
+@pytest.mark.parametrize("trace_log,eval_log", [(3, 5), (4, 6)])
+def test_poseidon_air_matches_oracle(trace_log, eval_log):
+    # eval_poseidon_constraints (crates/examples/src/poseidon/mod.rs:137-187) written against the
+    # evaluator, relation entries finalized in pairs: the oracle's Poseidon2 composition
+    from proving_gb300.synthetic import m31_columns
+    air = fw.poseidon_air_recorded()
+    assert air.n_constraints == O.POSEIDON_CONSTRAINTS
+    assert len(air.params) == 18
+    # 1264 trace columns at the row; 28 interaction columns at the row, the last 4 at both rows
+    assert sum(m.interaction == 1 for m in air.masks) == O.POSEIDON_COLS
+    assert sorted((m.column, m.offset) for m in air.masks if m.offset == -1) == [(k, -1) for k in range(28, 32)]
+    trace = m31_columns(500 + eval_log, O.POSEIDON_COLS, eval_log)
+    inter = m31_columns(600 + eval_log, O.POSEIDON_INTERACTION_COLS, eval_log)
+    lookup = list(seeded_qm31(31)) + list(seeded_qm31(32))
+    claimed = list(seeded_qm31(33))
+    rc = np.random.default_rng(eval_log).integers(0, O.P, (O.POSEIDON_CONSTRAINTS, 4)).astype(np.uint32)
+    start = m31_columns(700, 4, eval_log)
+    want = O.poseidon_composition(trace, inter, trace_log, lookup, claimed, rc, out=[s.copy() for s in start])
+    got = air_composition(air, {1: trace, 2: inter}, eval_log, trace_log, fw.poseidon_params(lookup, claimed, trace_log),
+                          rc, out=[s.copy() for s in start])
+    assert all(np.array_equal(np.asarray(g, np.uint32), np.asarray(w, np.uint32)) for g, w in zip(got, want))

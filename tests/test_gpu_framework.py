@@ -82,3 +82,35 @@ def test_generic_path_proof_equals_hand_written(B):
     g = prove(ops, True)
     want, _ = O.prove_fib_and_lookups((10, 1, 0, 3, 1), traces, [9, 3], vals, [8, 4])
     assert g.to_bytes() == prove(ops, False).to_bytes() == want
+
+
+@pytest.mark.parametrize("trace_log,eval_log", [(4, 6), (8, 10)])
+def test_poseidon_generated_equals_hand_written(B, trace_log, eval_log):
+    # eval_poseidon_constraints written against the evaluator (relation entries finalized in pairs),
+    # compiled with NVRTC: the words of the hand-written Poseidon2 composition kernel
+    from proving_gb300.backend import BaseColumn
+    from proving_gb300.synthetic import m31_columns
+    trace = [BaseColumn.from_cpu(c) for c in m31_columns(500 + eval_log, O.POSEIDON_COLS, eval_log)]
+    inter = [BaseColumn.from_cpu(c) for c in m31_columns(600 + eval_log, O.POSEIDON_INTERACTION_COLS, eval_log)]
+    lookup = list(seeded_qm31(41)) + list(seeded_qm31(42))
+    claimed = list(seeded_qm31(43))
+    rc = np.random.default_rng(eval_log).integers(0, O.P, (O.POSEIDON_CONSTRAINTS, 4)).astype(np.uint32)
+    start = m31_columns(700 + eval_log, 4, eval_log)
+    gen, hand = _acc(start), _acc(start)
+    fw.CompiledAir.get(fw.poseidon_air_recorded()).composition(
+        {1: trace, 2: inter}, trace_log, fw.poseidon_params(lookup, claimed, trace_log), rc, gen)
+    B.poseidon_composition(trace, inter, trace_log, lookup, claimed, rc, hand)
+    assert all(np.array_equal(a, b) for a, b in zip(gen.to_cpu(), hand.to_cpu()))
+
+
+def test_generic_poseidon_proof_equals_oracle_prover(B):
+    # the whole Poseidon2 proof with the constraints through the generated kernel: the oracle's words
+    from proving_gb300 import poseidon as ps
+    from proving_gb300 import prover as pr
+    log_n = 4
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    ops = pr.GpuOps()
+    tw = ops.twiddles(log_n + ps.LOG_EXPAND + fp.log_blowup_factor)
+    proof = ps.prove_poseidon(ops, log_n, ps.poseidon_pcs_config(log_n + 3, fp), pr.Blake2sChannel(), tw, check=False,
+                              generic=True)
+    assert proof.to_bytes() == O.prove_poseidon((10, 1, 0, 70, 1), log_n)

@@ -90,14 +90,15 @@ def test_unsatisfied_constraints_are_not_proved():
         O.prove_fib_and_lookups((10, 1, 0, 20, 1), trace, [6])
 
 
-@pytest.mark.parametrize("log_n", [3, 5])
-def test_oracle_poseidon_equals_host_prover(log_n):
-    # the Poseidon2 AIR (the words the reference computes before its sanity check)
+@pytest.mark.parametrize("log_n,generic", [(3, False), (5, False), (3, True)])
+def test_oracle_poseidon_equals_host_prover(log_n, generic):
+    # the Poseidon2 AIR (the words the reference computes before its sanity check); generic: its
+    # constraints through the framework's evaluator (poseidon_air, relation entries in pairs)
     from proving_gb300 import poseidon as ps
     cpu = CpuOps()
     fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
     host = ps.prove_poseidon(cpu, log_n, ps.poseidon_pcs_config(log_n + 3, fp), pr.Blake2sChannel(),
-                             cpu.twiddles(log_n + 3), check=False)
+                             cpu.twiddles(log_n + 3), check=False, generic=generic)
     assert host.to_bytes() == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
 
 
