@@ -344,6 +344,31 @@ cs_status cs_wide_fib_trace(const uint32_t *d_a, const uint32_t *d_b, uint32_t l
 cs_status cs_logup_running_sum(const uint32_t *d_values, uint32_t log_size, const uint32_t z[4], uint32_t *const h_out[4],
                                uint32_t claimed_sum_out[4], cs_stream stream);
 
+/* LogupTraceGenerator (crates/constraint-framework/src/prover/logup.rs:22-196) on the
+   device, for relations of any number of values and multiplicities; columns of
+   2^log_size rows in bit-reversed circle-domain order, QM31 columns as 4
+   coordinate arrays.
+   cs_logup_combine: LookupElements::combine (crates/constraint-framework/src/
+   logup.rs:80-94) per row, den = sum_i alpha^i values_i - z over n_values M31
+   columns h_values[i], alpha_powers holding alpha^i as 4 words each.
+   cs_logup_gen_col: LogupColGenerator::write_frac for every row then
+   finalize_col: out = num / den + prev, with num either the QM31 column h_num
+   (4 coordinates) or the M31 column d_num_m31 (exactly one of them non-null)
+   and prev the generator's previous column (h_prev, 4 coordinates) or null for
+   the first. A zero denominator gives a zero fraction.
+   cs_logup_finalize_last: LogupTraceGenerator::finalize_last in place on the
+   last column: claimed_sum = its sum (returned on the host, synchronous), every
+   value minus claimed_sum / 2^log_size, then the inclusive prefix sum in coset
+   order (1 <= log_size <= 28). */
+cs_status cs_logup_combine(const uint32_t *const *h_values, uint32_t n_values, uint32_t log_size,
+                           const uint32_t *alpha_powers, const uint32_t z[4], uint32_t *const h_den[4],
+                           cs_stream stream);
+cs_status cs_logup_gen_col(const uint32_t *const *h_num, const uint32_t *d_num_m31, const uint32_t *const h_den[4],
+                           const uint32_t *const *h_prev, uint32_t log_size, uint32_t *const h_out[4],
+                           cs_stream stream);
+cs_status cs_logup_finalize_last(uint32_t *const h_col[4], uint32_t log_size, uint32_t claimed_sum_out[4],
+                                 cs_stream stream);
+
 /* cs_logup_running_sum for n_cols columns of any log sizes in [1, 28] in one
    batch of launches (three per 48 columns), with no host synchronization:
    column i reads h_values[i] (2^h_log_sizes[i] device words) and writes its

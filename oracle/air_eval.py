@@ -37,8 +37,11 @@ def _as_q(v, n):
     return q
 
 
-def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, params, rc, out=None):
-    """The accumulator (4 coordinate arrays, created when None) plus the AIR's quotients."""
+def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, params, rc, out=None,
+                    divide: bool = True):
+    """The accumulator (4 coordinate arrays, created when None) plus the AIR's quotients. With
+    divide=False the weighted constraint sums are not divided by V_trace (on the trace domain itself,
+    where V_trace is zero, they show whether every row satisfies the constraints)."""
     n = 1 << eval_log
     prev = O.prev_rows(trace_log, eval_log)
     rows = {0: np.arange(n), -1: prev}
@@ -79,8 +82,9 @@ def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, 
     for c, w in zip(air.constraints, np.asarray(rc, np.int64).reshape(-1, 4)):
         v = _as_q(ev(c), n)
         acc = (acc + _qmul(v, np.tile(w % P, (n, 1)))) % P
-    den = O.vanishing_inverses(eval_log, trace_log)
-    acc = acc * den[:, None] % P
+    if divide:
+        den = O.vanishing_inverses(eval_log, trace_log)
+        acc = acc * den[:, None] % P
     if out is None:
         out = [np.zeros(n, np.uint32) for _ in range(4)]
     return [((np.asarray(o, np.int64) + acc[:, k]) % P).astype(np.uint32) for k, o in enumerate(out)]

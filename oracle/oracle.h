@@ -84,6 +84,11 @@ void orc_wide_fib_composition(const uint32_t **cols, uint32_t n_cols, uint32_t e
 void orc_wide_fib_trace(const uint32_t *a0, const uint32_t *b0, uint32_t log_n, uint32_t n_cols, uint32_t **cols);
 void orc_logup_running_sum(const uint32_t *values, uint32_t log_n, const uint32_t z[4], uint32_t *const out[4],
                            uint32_t claimed_out[4]);
+void orc_logup_combine(const uint32_t *const *values, uint32_t n_values, uint32_t log_n,
+                       const uint32_t *alpha_powers, const uint32_t z[4], uint32_t *const out[4]);
+void orc_logup_gen_col(const uint32_t *const num[4], const uint32_t *num_m31, const uint32_t *const den[4],
+                       const uint32_t *const prev[4], uint32_t log_n, uint32_t *const out[4]);
+void orc_logup_finalize_last(uint32_t *const col[4], uint32_t log_n, uint32_t claimed_out[4]);
 uint64_t orc_prev_row(uint64_t r, uint32_t trace_log, uint32_t eval_log);
 void orc_prev_rows(uint32_t trace_log, uint32_t eval_log, uint64_t *out);
 void orc_logup_composition(const uint32_t *values, const uint32_t *const inter[4], uint32_t eval_log,

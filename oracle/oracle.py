@@ -503,6 +503,46 @@ def logup_running_sum(values, z):
     return out, claimed
 
 
+def logup_combine(values, alpha_powers, z):
+    """LookupElements::combine per row: sum_i alpha_powers[i] values[i] - z (4 coordinate arrays)."""
+    vs = [_u32(v) for v in values]
+    n = vs[0].size
+    aw = np.ascontiguousarray(np.asarray(alpha_powers, np.uint32).reshape(-1))
+    zz = _u32(z)
+    out = [np.zeros(n, np.uint32) for _ in range(4)]
+    lib().orc_logup_combine(_ptr_array(vs), ctypes.c_uint32(len(vs)), ctypes.c_uint32(n.bit_length() - 1), _p(aw),
+                            _p(zz), _ptr_array(out))
+    return out
+
+
+def logup_gen_col(numerator, denominator, prev=None):
+    """LogupColGenerator (write_frac for every row, finalize_col): numerator / denominator + prev.
+    numerator: 4 coordinate arrays (QM31) or one M31 array; denominator, prev: 4 arrays each."""
+    den = [_u32(c) for c in denominator]
+    n = den[0].size
+    out = [np.zeros(n, np.uint32) for _ in range(4)]
+    if isinstance(numerator, (list, tuple)):
+        keep = [_u32(c) for c in numerator]
+        num, num_m31 = _ptr_array(keep), None
+    else:
+        keep = [_u32(numerator)]
+        num, num_m31 = None, _p(keep[0])
+    pvs = [_u32(c) for c in prev] if prev is not None else []
+    pv = _ptr_array(pvs) if prev is not None else None
+    lib().orc_logup_gen_col(num, num_m31, _ptr_array(den), pv, ctypes.c_uint32(n.bit_length() - 1), _ptr_array(out))
+    del keep, pvs
+    return out
+
+
+def logup_finalize_last(col):
+    """LogupTraceGenerator::finalize_last on a copy of col: (the running-sum column, claimed sum)."""
+    out = [_u32(c).copy() for c in col]
+    n = out[0].size
+    claimed = np.zeros(4, np.uint32)
+    lib().orc_logup_finalize_last(_ptr_array(out), ctypes.c_uint32(n.bit_length() - 1), _p(claimed))
+    return out, claimed
+
+
 # ---------------------------------------------------------------- Poseidon2 AIR
 
 POSEIDON_COLS = 1264

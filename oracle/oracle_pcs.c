@@ -305,6 +305,63 @@ void orc_logup_running_sum(const uint32_t *values, uint32_t log_n, const uint32_
 }
 
 /*
+ * LookupElements::combine (crates/constraint-framework/src/logup.rs:80-94) per row:
+ * den[r] = sum_i alpha^i values_i[r] - z, alpha_powers holding alpha^i as 4 words each.
+ */
+void orc_logup_combine(const uint32_t *const *values, uint32_t n_values, uint32_t log_n,
+                       const uint32_t *alpha_powers, const uint32_t z_w[4], uint32_t *const out[4]) {
+    uint64_t n = 1ull << log_n;
+    qm31 z = qm31_from_words(z_w);
+    for (uint64_t r = 0; r < n; r++) {
+        qm31 acc = qm31_from_m31(0);
+        for (uint32_t i = 0; i < n_values; i++)
+            acc = qm31_add(acc, qm31_mul_m31(qm31_from_words(alpha_powers + 4 * i), values[i][r]));
+        soa_set(out, r, qm31_sub(acc, z));
+    }
+}
+
+/*
+ * LogupColGenerator::write_frac for every row, then finalize_col
+ * (crates/constraint-framework/src/prover/logup.rs:133-196): out[r] = num[r] / den[r] + prev[r],
+ * prev the generator's previous column (NULL: none). The numerator is QM31 (num, 4 coordinates)
+ * or, when num is NULL, the M31 column num_m31.
+ */
+void orc_logup_gen_col(const uint32_t *const num[4], const uint32_t *num_m31, const uint32_t *const den[4],
+                       const uint32_t *const prev[4], uint32_t log_n, uint32_t *const out[4]) {
+    uint64_t n = 1ull << log_n;
+    for (uint64_t r = 0; r < n; r++) {
+        qm31 nu = num ? soa_at(num, r) : qm31_from_m31(num_m31[r]);
+        qm31 v = qm31_mul(nu, qm31_inv(soa_at(den, r)));
+        if (prev) v = qm31_add(v, soa_at(prev, r));
+        soa_set(out, r, v);
+    }
+}
+
+/*
+ * LogupTraceGenerator::finalize_last (crates/constraint-framework/src/prover/logup.rs:96-130) in
+ * place: claimed = the column's sum, every value minus claimed / n, then the inclusive prefix sum
+ * in coset order over the bit-reversed circle-domain storage (inclusive_prefix_sum,
+ * crates/stwo/src/prover/backend/simd/prefix_sum.rs:20-149).
+ */
+void orc_logup_finalize_last(uint32_t *const col[4], uint32_t log_n, uint32_t claimed_out[4]) {
+    uint64_t n = 1ull << log_n;
+    qm31 claimed = qm31_from_m31(0);
+    for (uint64_t r = 0; r < n; r++) claimed = qm31_add(claimed, soa_at((const uint32_t *const *)col, r));
+    qm31_to_words(claimed, claimed_out);
+    qm31 shift = qm31_mul_m31(claimed, m31_inv((m31)(n % M31_P)));
+    qm31 *f = (qm31 *)malloc(sizeof(qm31) * n);
+    for (uint64_t r = 0; r < n; r++) f[r] = qm31_sub(soa_at((const uint32_t *const *)col, r), shift);
+    qm31 acc = qm31_from_m31(0);
+    for (uint64_t k = 0; k < n; k++) {
+        uint64_t c = (k & 1) ? n / 2 + (n - 1 - k) / 2 : k / 2; /* circle-domain index of coset index k */
+        uint64_t p = bit_reverse_index((uint32_t)c, log_n);
+        acc = qm31_add(acc, f[p]);
+        soa_set(col, p, acc);
+    }
+    free(f);
+}
+
+/*
  * Constraint quotients of a single-column LogUp component on an evaluation
  * domain: the relation entry (multiplicity -1, values [v]) finalized with
  * finalize_logup (crates/constraint-framework/src/lib.rs:185-227, batch size

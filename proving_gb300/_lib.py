@@ -75,6 +75,9 @@ SIGNATURES = {
     "cs_channel_draw_secure_felt": [vp, vp, vp],
     "cs_fri_commit_fold_tail": [vp, vp, vp, vp, u32, u32, vp, u32, vp],
     "cs_logup_running_sums": [u32, vp, vp, vp, vp, vp, vp],
+    "cs_logup_combine": [vp, u32, u32, vp, vp, vp, vp],
+    "cs_logup_gen_col": [vp, vp, vp, vp, u32, vp, vp],
+    "cs_logup_finalize_last": [vp, u32, vp, vp],
     "cs_gkr_gen_eq_evals": [vp, u32, vp, vp, vp],
     "cs_mle_fix_first_variable": [vp, u32, u32, vp, vp, vp],
     "cs_gkr_next_layer": [u32, vp, vp, u32, vp, vp, vp],

@@ -171,6 +171,60 @@ class TwiddleTree:
 
 # ------------------------------------------------------------------ backend
 
+class LogupTraceGenerator:
+    """LogupTraceGenerator (crates/constraint-framework/src/prover/logup.rs:22-130) over device
+    columns of 2^log_size rows (bit-reversed circle-domain order): each col_from_fractions adds one
+    interaction column, num / den plus the previous column (LogupColGenerator::write_frac for every
+    row, then finalize_col, through cs_logup_gen_col); finalize_last turns the last column into the
+    shifted running sum (cs_logup_finalize_last) and returns every column's four coordinate
+    BaseColumns with the claimed sum, as the reference returns the trace and claimed_sum."""
+
+    def __init__(self, log_size: int):
+        self.log_size = log_size
+        self.trace: list = []
+
+    def col_from_fractions(self, fractions) -> None:
+        """One interaction column from a batch of fractions [(numerator, denominator), ...], summed
+        per row (the reference's caller writes the batch's combined fraction, e.g. n0 d1 + n1 d0 over
+        d0 d1 for a pair): numerator a SecureColumnByCoords or a BaseColumn of M31 numerators
+        (multiplicities), denominator a SecureColumnByCoords."""
+        assert fractions, "an interaction column needs at least one fraction"
+        n = 1 << self.log_size
+        out = SecureColumnByCoords.uninitialized(n)
+        out_tab = _ptr_table([c.data for c in out.columns])
+        prev = _ptr_table([c.data for c in self.trace[-1].columns]) if self.trace else None
+        for numerator, denominator in fractions:
+            assert len(denominator) == n and len(numerator) == n
+            if isinstance(numerator, SecureColumnByCoords):
+                num_tab, num_m31 = _ptr_table([c.data for c in numerator.columns]), None
+            else:
+                num_tab, num_m31 = None, _ptr(numerator.data)
+            # later fractions of the batch add to the column itself (each row reads prev, then writes)
+            _lib.call("cs_logup_gen_col", num_tab, num_m31, _ptr_table([c.data for c in denominator.columns]), prev,
+                      self.log_size, out_tab, _stream())
+            prev = out_tab
+        self.trace.append(out)
+
+    def finalize_last(self):
+        assert self.trace, "no interaction column to finalize"
+        claimed = (ctypes.c_uint32 * 4)()
+        _lib.call("cs_logup_finalize_last", _ptr_table([c.data for c in self.trace[-1].columns]), self.log_size,
+                  claimed, _stream())
+        return [c for col in self.trace for c in col.columns], tuple(int(x) for x in claimed)
+
+
+def logup_combine(values, alpha_powers, z) -> "SecureColumnByCoords":
+    """LookupElements::combine (crates/constraint-framework/src/logup.rs:80-94) per row of the M31
+    columns `values`: sum_i alpha_powers[i] values[i] - z (cs_logup_combine)."""
+    out = SecureColumnByCoords.uninitialized(len(values[0]))
+    aw = np.ascontiguousarray(np.asarray(alpha_powers, np.uint32).reshape(-1))
+    assert aw.size == 4 * len(values)
+    _lib.call("cs_logup_combine", _ptr_table([v.data for v in values]), len(values), values[0].log_size,
+              aw.ctypes.data_as(ctypes.c_void_p), _u32_table(z), _ptr_table([c.data for c in out.columns]),
+              _stream())
+    return out
+
+
 _tls = threading.local()
 
 

@@ -473,6 +473,61 @@ cpoint lookup_point_at(uint32_t idx) {
   return r;
 }
 
+// LookupElements::combine (crates/constraint-framework/src/logup.rs:80-94) per row over up to
+// kCombineBatch value columns: den = sum_i alpha^i values_i - z; later batches of a call add on.
+constexpr uint32_t kCombineBatch = 32;
+struct CombineBatch {
+  const uint32_t* values[kCombineBatch];
+  qm31 alpha[kCombineBatch];
+  uint32_t n;
+  uint32_t first;  // the first batch: subtract z and store; otherwise add to the output
+  qm31 z;
+};
+
+__global__ void logup_combine_kernel(const __grid_constant__ CombineBatch b, uint32_t n_rows, uint32_t* o0,
+                                     uint32_t* o1, uint32_t* o2, uint32_t* o3) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
+    qm31 acc = b.first ? qm31_neg(b.z) : qm31_make(o0[r], o1[r], o2[r], o3[r]);
+    for (uint32_t i = 0; i < b.n; i++) acc = qm31_add(acc, qm31_mul_m31(b.alpha[i], __ldg(b.values[i] + r)));
+    o0[r] = acc.a.a;
+    o1[r] = acc.a.b;
+    o2[r] = acc.b.a;
+    o3[r] = acc.b.b;
+  }
+}
+
+// LogupColGenerator::write_frac for every row, then finalize_col (crates/constraint-framework/src/
+// prover/logup.rs:133-196): out = num / den + prev, the inverse per row (qm31_inv; the reference's
+// batch inversion gives the same values), num QM31 (num0..3) or M31 (num_m31), prev optional.
+struct FracCol {
+  const uint32_t* num[4];
+  const uint32_t* num_m31;
+  const uint32_t* den[4];
+  const uint32_t* prev[4];
+  uint32_t* out[4];
+};
+
+__global__ void logup_frac_kernel(const FracCol f, uint32_t n_rows) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
+    const qm31 den = qm31_make(__ldg(f.den[0] + r), __ldg(f.den[1] + r), __ldg(f.den[2] + r), __ldg(f.den[3] + r));
+    const qm31 inv = qm31_inv(den);
+    qm31 v = f.num_m31 != nullptr
+                 ? qm31_mul_m31(inv, __ldg(f.num_m31 + r))
+                 : qm31_mul(qm31_make(__ldg(f.num[0] + r), __ldg(f.num[1] + r), __ldg(f.num[2] + r),
+                                      __ldg(f.num[3] + r)),
+                            inv);
+    if (f.prev[0] != nullptr)
+      v = qm31_add(v, qm31_make(__ldg(f.prev[0] + r), __ldg(f.prev[1] + r), __ldg(f.prev[2] + r),
+                                __ldg(f.prev[3] + r)));
+    f.out[0][r] = v.a.a;
+    f.out[1][r] = v.a.b;
+    f.out[2][r] = v.b.a;
+    f.out[3][r] = v.b.b;
+  }
+}
+
+uint32_t rows_grid(uint32_t n) { return std::max(1u, std::min<uint32_t>((n + 255) / 256, 152 * 8)); }
+
 }  // namespace
 
 cs_status logup_finalize_last(Q4 col, uint32_t log_size, uint32_t claimed_sum_out[4], cudaStream_t st) {
@@ -601,4 +656,67 @@ extern "C" cs_status cs_logup_composition(const uint32_t* d_values, const uint32
   CS_CHECK_ARG(d_values != nullptr && h_inter != nullptr && claimed_sum != nullptr && rc != nullptr,
                "logup_composition: null pointer");
   return cs_logup_compositions(1, &d_values, h_inter, eval_log, trace_log, z, claimed_sum, rc, h_accum, stream);
+}
+
+extern "C" cs_status cs_logup_combine(const uint32_t* const* h_values, uint32_t n_values, uint32_t log_size,
+                                      const uint32_t* alpha_powers, const uint32_t z[4], uint32_t* const h_den[4],
+                                      cs_stream stream) {
+  CS_CHECK_ARG(h_values != nullptr && alpha_powers != nullptr && z != nullptr && h_den != nullptr,
+               "logup_combine: null pointer");
+  CS_CHECK_ARG(n_values >= 1, "logup_combine: no values");
+  CS_CHECK_ARG(log_size <= 30, "logup_combine: log size %u", log_size);
+  for (int c = 0; c < 4; c++) CS_CHECK_ARG(h_den[c] != nullptr, "logup_combine: null output coordinate");
+  cudaStream_t st = to_stream(stream);
+  const uint32_t n = 1u << log_size;
+  for (uint32_t b0 = 0; b0 < n_values; b0 += kCombineBatch) {
+    CombineBatch b;
+    b.n = std::min(kCombineBatch, n_values - b0);
+    b.first = b0 == 0;
+    b.z = qm31_make(z[0] % P, z[1] % P, z[2] % P, z[3] % P);
+    for (uint32_t i = 0; i < b.n; i++) {
+      CS_CHECK_ARG(h_values[b0 + i] != nullptr, "logup_combine: value column %u is null", b0 + i);
+      b.values[i] = h_values[b0 + i];
+      const uint32_t* a = alpha_powers + 4 * (size_t)(b0 + i);
+      b.alpha[i] = qm31_make(a[0] % P, a[1] % P, a[2] % P, a[3] % P);
+    }
+    logup_combine_kernel<<<rows_grid(n), 256, 0, st>>>(b, n, h_den[0], h_den[1], h_den[2], h_den[3]);
+    CS_LAUNCHED("logup_combine_kernel");
+  }
+  return CS_OK;
+}
+
+extern "C" cs_status cs_logup_gen_col(const uint32_t* const* h_num, const uint32_t* d_num_m31,
+                                      const uint32_t* const h_den[4], const uint32_t* const* h_prev,
+                                      uint32_t log_size, uint32_t* const h_out[4], cs_stream stream) {
+  CS_CHECK_ARG(h_den != nullptr && h_out != nullptr, "logup_gen_col: null pointer");
+  CS_CHECK_ARG((h_num != nullptr) != (d_num_m31 != nullptr),
+               "logup_gen_col: give exactly one numerator (QM31 coordinates or an M31 column)");
+  CS_CHECK_ARG(log_size <= 30, "logup_gen_col: log size %u", log_size);
+  FracCol f;
+  for (int c = 0; c < 4; c++) {
+    CS_CHECK_ARG(h_den[c] != nullptr && h_out[c] != nullptr, "logup_gen_col: null coordinate");
+    f.num[c] = h_num != nullptr ? h_num[c] : nullptr;
+    CS_CHECK_ARG(h_num == nullptr || f.num[c] != nullptr, "logup_gen_col: null numerator coordinate");
+    f.den[c] = h_den[c];
+    f.prev[c] = h_prev != nullptr ? h_prev[c] : nullptr;
+    CS_CHECK_ARG(h_prev == nullptr || f.prev[c] != nullptr, "logup_gen_col: null previous-column coordinate");
+    f.out[c] = h_out[c];
+  }
+  f.num_m31 = d_num_m31;
+  const uint32_t n = 1u << log_size;
+  logup_frac_kernel<<<rows_grid(n), 256, 0, to_stream(stream)>>>(f, n);
+  CS_LAUNCHED("logup_frac_kernel");
+  return CS_OK;
+}
+
+extern "C" cs_status cs_logup_finalize_last(uint32_t* const h_col[4], uint32_t log_size, uint32_t claimed_sum_out[4],
+                                            cs_stream stream) {
+  CS_CHECK_ARG(h_col != nullptr && claimed_sum_out != nullptr, "logup_finalize_last: null pointer");
+  CS_CHECK_ARG(log_size >= 1 && log_size <= 28, "logup_finalize_last: log size %u outside [1, 28]", log_size);
+  Q4 col;
+  for (int c = 0; c < 4; c++) {
+    CS_CHECK_ARG(h_col[c] != nullptr, "logup_finalize_last: null coordinate");
+    col.c[c] = h_col[c];
+  }
+  return logup_finalize_last(col, log_size, claimed_sum_out, to_stream(stream));
 }

@@ -594,24 +594,44 @@ def poseidon_air_recorded() -> Air:
     return _POSEIDON_AIR[0]
 
 
+def _qm31_mul(a, b):
+    """QM31 product of two 4-tuples: (a + b u)(c + d u) with u^2 = 2 + i over CM31 = M31[i]/(i^2 + 1)."""
+    a0, a1, a2, a3 = (int(x) for x in a)
+    b0, b1, b2, b3 = (int(x) for x in b)
+    ac = ((a0 * b0 - a1 * b1) % P, (a0 * b1 + a1 * b0) % P)
+    bd = ((a2 * b2 - a3 * b3) % P, (a2 * b3 + a3 * b2) % P)
+    ad = ((a0 * b2 - a1 * b3) % P, (a0 * b3 + a1 * b2) % P)
+    bc = ((a2 * b0 - a3 * b1) % P, (a2 * b1 + a3 * b0) % P)
+    rbd = ((2 * bd[0] - bd[1]) % P, (bd[0] + 2 * bd[1]) % P)
+    return ((ac[0] + rbd[0]) % P, (ac[1] + rbd[1]) % P, (ad[0] + bc[0]) % P, (ad[1] + bc[1]) % P)
+
+
+def alpha_powers(alpha, n: int) -> list:
+    """alpha^0 .. alpha^(n-1) (LookupElements::draw, crates/constraint-framework/src/logup.rs:70-79)."""
+    out, cur = [], (1, 0, 0, 0)
+    for _ in range(n):
+        out.append(cur)
+        cur = _qm31_mul(cur, alpha)
+    return out
+
+
+def lookup_params(relation: str, z, alpha, n_values: int) -> dict:
+    """The parameters add_to_relation reads for `relation`: {relation}_z and {relation}_alpha{i}."""
+    params = {f"{relation}_z": tuple(int(x) for x in z)}
+    for i, p in enumerate(alpha_powers(alpha, n_values)):
+        params[f"{relation}_alpha{i}"] = p
+    return params
+
+
+def logup_shift(claimed, trace_log: int) -> tuple:
+    """claimed_sum / 2^trace_log, the cumsum shift of the last LogUp column (LogupAtRow::new)."""
+    inv = pow(1 << trace_log, P - 2, P)
+    return tuple(int(x) * inv % P for x in claimed)
+
+
 def poseidon_params(lookup, claimed, trace_log: int) -> dict:
     """The parameters of poseidon_air from the drawn lookup elements (z, alpha: 8 words) and the
-    claimed sum: alpha^i (LookupElements::draw, logup.rs:70-79) and shift = claimed / 2^trace_log."""
-    def mul(a, b):
-        a0, a1, a2, a3 = (int(x) for x in a)
-        b0, b1, b2, b3 = (int(x) for x in b)
-        # (a + b u)(c + d u) with u^2 = 2 + i over CM31 = M31[i]/(i^2 + 1)
-        ac = ((a0 * b0 - a1 * b1) % P, (a0 * b1 + a1 * b0) % P)
-        bd = ((a2 * b2 - a3 * b3) % P, (a2 * b3 + a3 * b2) % P)
-        ad = ((a0 * b2 - a1 * b3) % P, (a0 * b3 + a1 * b2) % P)
-        bc = ((a2 * b0 - a3 * b1) % P, (a2 * b1 + a3 * b0) % P)
-        rbd = ((2 * bd[0] - bd[1]) % P, (bd[0] + 2 * bd[1]) % P)
-        return ((ac[0] + rbd[0]) % P, (ac[1] + rbd[1]) % P, (ad[0] + bc[0]) % P, (ad[1] + bc[1]) % P)
-    z, alpha = tuple(int(x) for x in lookup[:4]), tuple(int(x) for x in lookup[4:8])
-    params, cur = {"poseidon_z": z}, (1, 0, 0, 0)
-    for i in range(POSEIDON_STATE):
-        params[f"poseidon_alpha{i}"] = cur
-        cur = mul(cur, alpha)
-    inv = pow(1 << trace_log, P - 2, P)
-    params["shift"] = tuple(int(x) * inv % P for x in claimed)
+    claimed sum."""
+    params = lookup_params("poseidon", lookup[:4], lookup[4:8], POSEIDON_STATE)
+    params["shift"] = logup_shift(claimed, trace_log)
     return params

@@ -273,3 +273,23 @@ def test_fri_tail_checks_arguments_on_host(lib):
     assert _status(lib, "cs_fri_commit_fold_tail", state, alphas, evals, bad, 5, 2, itw, 12, null) == INVALID
     assert b"16-byte" in lib.cs_last_error()
     assert _status(lib, "cs_fri_commit_fold_tail", null, alphas, evals, trees, 5, 2, itw, 12, null) == INVALID
+
+
+def test_logup_generator_checks_arguments_on_host(lib):
+    INVALID = 1
+    null = ctypes.c_void_p(0)
+    four = (ctypes.c_void_p * 4)(1 << 20, 1 << 21, 1 << 22, 1 << 23)
+    out = (ctypes.c_void_p * 4)(1 << 24, 1 << 25, 1 << 26, 1 << 27)
+    m31 = ctypes.c_void_p(1 << 28)
+    # exactly one numerator
+    assert _status(lib, "cs_logup_gen_col", four, m31, four, null, 5, out, null) == INVALID
+    assert b"exactly one numerator" in lib.cs_last_error()
+    assert _status(lib, "cs_logup_gen_col", null, null, four, null, 5, out, null) == INVALID
+    assert _status(lib, "cs_logup_gen_col", null, m31, four, null, 31, out, null) == INVALID
+    vals = (ctypes.c_void_p * 1)(1 << 20)
+    z = (ctypes.c_uint32 * 4)(1, 2, 3, 4)
+    assert _status(lib, "cs_logup_combine", vals, 0, 5, z, z, out, null) == INVALID
+    assert _status(lib, "cs_logup_combine", (ctypes.c_void_p * 1)(0), 1, 5, z, z, out, null) == INVALID
+    claimed = (ctypes.c_uint32 * 4)()
+    assert _status(lib, "cs_logup_finalize_last", out, 0, claimed, null) == INVALID
+    assert _status(lib, "cs_logup_finalize_last", out, 29, claimed, null) == INVALID
