@@ -100,3 +100,24 @@ def test_poseidon_air_matches_oracle(trace_log, eval_log):
     got = air_composition(air, {1: trace, 2: inter}, eval_log, trace_log, fw.poseidon_params(lookup, claimed, trace_log),
                           rc, out=[s.copy() for s in start])
     assert all(np.array_equal(np.asarray(g, np.uint32), np.asarray(w, np.uint32)) for g, w in zip(got, want))
+
+
+def test_large_bodies_are_split_into_functions():
+    # a body over the single-function limit becomes non-inlined functions in constraint order, values
+    # passed through xs; small AIRs keep one inlined body
+    import re
+    small = fw.compile_air("fib", fw.wide_fib_air, 100).source
+    assert "__noinline__" not in small and "uint32_t xs[" not in small
+    src = fw.poseidon_air_recorded().source
+    groups = re.findall(r"cs_air_group(\d+)\(const uint32_t\* const\* __restrict__ cols", src)
+    assert len(groups) > 8 and groups == [str(g) for g in range(len(groups))]
+    n_xs = int(re.search(r"uint32_t xs\[(\d+)\];", src).group(1))
+    assert 0 < n_xs < 4096
+    # every xs slot a function reads was written by an earlier function
+    written, bodies = set(), src.split("__device__ __noinline__ qm31 cs_air_group")[1:]
+    for body in bodies:
+        reads = {int(x) for x in re.findall(r"= xs\[(\d+)\]", body)} | \
+                {int(x) for x in re.findall(r"qm31_make\(xs\[(\d+)\]", body)}
+        assert reads <= written
+        written |= {int(x) for x in re.findall(r"xs\[(\d+)\] =", body)}
+    assert src.count("air_qm31_add(acc, cs_air_group") == len(groups)
