@@ -258,24 +258,25 @@ cs_status read_root(Arena& A, Tree& t) {
 
 // The witness of MerkleProverLifted::decommit (crates/stwo/src/prover/vcs_lifted/prover.rs:119-150):
 // per layer from the leaves, the sibling of every queried node whose sibling is not queried.
-std::vector<std::pair<uint32_t, std::vector<uint64_t>>> witness_nodes(uint32_t height, std::vector<uint64_t> q) {
-  std::sort(q.begin(), q.end());
+// emit(k, node) is called for each witness node of layer k (2^k nodes), leaves' layer first, in
+// increasing node order; q is this thread's scratch copy of the queried leaves.
+template <class Emit>
+void for_each_witness_node(uint32_t height, const std::vector<uint64_t>& queried, Emit emit) {
+  thread_local std::vector<uint64_t> q, up;
+  q.assign(queried.begin(), queried.end());
+  if (!std::is_sorted(q.begin(), q.end())) std::sort(q.begin(), q.end());  // the callers' are sorted
   q.erase(std::unique(q.begin(), q.end()), q.end());
-  std::vector<std::pair<uint32_t, std::vector<uint64_t>>> out;
   for (int layer = (int)height - 1; layer >= 0; layer--) {
-    std::vector<uint64_t> need;
     for (size_t i = 0; i < q.size(); i++) {
       const uint64_t sib = q[i] ^ 1;
       const bool present = (i + 1 < q.size() && q[i + 1] == sib) || (i > 0 && q[i - 1] == sib);
-      if (!present) need.push_back(sib);
+      if (!present) emit((uint32_t)layer + 1, sib);
     }
-    if (!need.empty()) out.push_back({(uint32_t)layer + 1, need});
-    std::vector<uint64_t> up;
+    up.clear();
     for (uint64_t x : q)
       if (up.empty() || up.back() != (x >> 1)) up.push_back(x >> 1);
-    q = up;
+    q.swap(up);
   }
-  return out;
 }
 
 // Every device read of a proof's decommitment, collected and made in one gather_runs call (a digest is
@@ -345,11 +346,11 @@ Reads& reads_for(int k) {
 // A tree's witness digests registered with a Reads: (first read, count of digests).
 std::pair<size_t, size_t> read_witness(Reads& R, const Tree& t, const std::vector<uint64_t>& q) {
   size_t first = R.n_words, n = 0;
-  for (auto& [k, nodes] : witness_nodes(t.height, q))
-    for (uint64_t node : nodes) {
-      R.add(t.layers, t.words(), t.node_word(k, node), 8);
-      n++;
-    }
+  const uint64_t words = t.words();
+  for_each_witness_node(t.height, q, [&](uint32_t k, uint64_t node) {
+    R.add(t.layers, words, t.node_word(k, node), 8);
+    n++;
+  });
   return {first, n};
 }
 
