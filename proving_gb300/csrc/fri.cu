@@ -508,6 +508,10 @@ __device__ __forceinline__ void store_digest(uint32_t* dst, const uint32_t h[8])
   o[1] = make_uint4(h[4], h[5], h[6], h[7]);
 }
 
+// Every hash of the tail is one final Blake2s block from the initial chaining value (a leaf's 16
+// bytes, a node's 64, the channel's 64-byte mix and 37-byte draw), so each layer is a loop of steps
+// around a single compression call: the kernel holds one copy of the compression (a one-shot kernel
+// whose code is otherwise fetched cold for every inlined copy).
 __global__ void __launch_bounds__(kFriTailThreads) fri_tail_kernel(const __grid_constant__ FriTail T,
                                                                    uint32_t log_size, uint32_t n_layers,
                                                                    uint32_t* state, uint32_t* alphas,
@@ -526,59 +530,77 @@ __global__ void __launch_bounds__(kFriTailThreads) fri_tail_kernel(const __grid_
   for (uint32_t j = 0; j < n_layers; j++) {
     const uint32_t m = log_size - j, half = 1u << (m - 1);
     uint32_t* tree = T.tree[j];
-    if (t < half) {  // leaves 2t, 2t + 1, then node t of level m - 1 (tree word (2^m + t) * 8)
-      uint32_t msg[16], h0[8], h1[8], n[8];
+    // steps: leaf 2t, leaf 2t + 1, their parent (node t of level m - 1), levels m - 2 .. 0, the
+    // root's mix into the channel, the challenge's draw
+    const uint32_t n_steps = 3 + (m - 1) + 2;
+    uint32_t leaves[16];  // this thread's two leaf digests, the message of its first node
+#pragma unroll 1
+    for (uint32_t step = 0; step < n_steps; step++) {
+      uint32_t msg[16], tlo = 64;
+      bool on;
+      int level = -1;  // the node level of a node step
+      if (step < 2) {
+        on = t < half;
+        if (on) {
 #pragma unroll
-      for (int k = 4; k < 16; k++) msg[k] = 0;
+          for (int k = 0; k < 4; k++) msg[k] = v[k][2 * t + step];
 #pragma unroll
-      for (int k = 0; k < 4; k++) msg[k] = v[k][2 * t];
-      b2s_init(h0);
-      b2s_compress(h0, msg, 16, 0, true, one);
+          for (int k = 4; k < 16; k++) msg[k] = 0;
+        }
+        tlo = 16;
+      } else if (step == 2) {
+        on = t < half;
+        level = (int)m - 1;
 #pragma unroll
-      for (int k = 0; k < 4; k++) msg[k] = v[k][2 * t + 1];
-      b2s_init(h1);
-      b2s_compress(h1, msg, 16, 0, true, one);
-      store_digest(tree + (size_t)(2 * t) * 8, h0);
-      store_digest(tree + (size_t)(2 * t + 1) * 8, h1);
+        for (int k = 0; k < 16; k++) msg[k] = leaves[k];
+      } else if (step < n_steps - 2) {
+        level = (int)m - 2 - (int)(step - 3);
+        on = t < (1u << level);
+        if (on) {
 #pragma unroll
-      for (int k = 0; k < 8; k++) msg[k] = h0[k], msg[8 + k] = h1[k];
-      b2s_init(n);
-      b2s_compress(n, msg, 64, 0, true, one);
-      store_digest(tree + ((size_t)(1u << m) + t) * 8, n);
-#pragma unroll
-      for (int k = 0; k < 8; k++) d[t][k] = n[k];
-    }
-    __syncthreads();
-    for (int k = (int)m - 2; k >= 0; k--) {  // level k: node t at tree word (2^(m+1) - 2^(k+1) + t) * 8
-      const bool on = t < (1u << k);
-      uint32_t n[8];
-      if (on) {
-        uint32_t msg[16];
-#pragma unroll
-        for (int w = 0; w < 8; w++) msg[w] = d[2 * t][w], msg[8 + w] = d[2 * t + 1][w];
-        b2s_init(n);
-        b2s_compress(n, msg, 64, 0, true, one);
+          for (int w = 0; w < 8; w++) msg[w] = d[2 * t][w], msg[8 + w] = d[2 * t + 1][w];
+        }
+      } else if (step == n_steps - 2) {  // mix the root (d[0]) into the channel
+        on = t == 0;
+        tlo = kChannelMixBytes;
+        if (on) channel_mix_message(chan, d[0], msg);
+      } else {  // draw the folding challenge
+        on = t == 0;
+        tlo = kChannelDrawBytes;
+        if (on) channel_draw_message(chan, msg);
       }
-      __syncthreads();
+      uint32_t h[8];
       if (on) {
-#pragma unroll
-        for (int w = 0; w < 8; w++) d[t][w] = n[w];
-        store_digest(tree + ((size_t)(2u << m) - (2u << k) + t) * 8, n);
+        b2s_init(h);
+        b2s_compress(h, msg, tlo, 0, true, one);
       }
-      __syncthreads();
-    }
-    if (t == 0) {  // mix the root (d[0]), draw the challenge
-      uint32_t c[9], r[8], f[4];
+      if (step < 2) {
+        if (on) {
+          if (step == 0) {
 #pragma unroll
-      for (int w = 0; w < 9; w++) c[w] = chan[w];
+            for (int w = 0; w < 8; w++) leaves[w] = h[w];
+          } else {
 #pragma unroll
-      for (int w = 0; w < 8; w++) r[w] = d[0][w];
-      channel_mix_root(c, r);
-      channel_draw_felt(c, f);
+            for (int w = 0; w < 8; w++) leaves[8 + w] = h[w];
+          }
+          store_digest(tree + (size_t)(2 * t + step) * 8, h);
+        }
+      } else if (level >= 0) {
+        __syncthreads();  // every read of this level's children is done
+        if (on) {
 #pragma unroll
-      for (int w = 0; w < 9; w++) chan[w] = c[w];
+          for (int w = 0; w < 8; w++) d[t][w] = h[w];
+          store_digest(tree + ((size_t)(2u << m) - (2u << level) + t) * 8, h);
+        }
+        __syncthreads();
+      } else if (step == n_steps - 2) {
+        if (on) channel_after_mix(chan, h);
+      } else if (on) {
+        uint32_t felt[4];
+        channel_after_draw(chan, h, felt);
 #pragma unroll
-      for (int w = 0; w < 4; w++) alpha[w] = f[w], alphas[4 * j + w] = f[w];
+        for (int w = 0; w < 4; w++) alpha[w] = felt[w], alphas[4 * j + w] = felt[w];
+      }
     }
     __syncthreads();
     qm31 r;
