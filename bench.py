@@ -1,13 +1,14 @@
-"""Commit-stage microbenchmark of the Stwo prover hot path on GB300, with the proof
-configurations beside it.
+"""Commit-stage microbenchmark of the Stwo prover hot path on GB300, with whole proofs of the
+other workloads beside it.
 
-Headline workload (one step = one commit stage, config 2 of the benchmark plan):
+Headline workload (one step = one commit stage of 256 columns of 2^20 rows):
   256 M31 columns of 2^20 rows (uniform in [0, P), seeded), interpolate, evaluate
   on the 4x blown-up canonic domain (log 22), lifted Blake2s Merkle tree over the
   256-wide leaves (height 22), then 22 FRI folds (fold_circle_into_line + 21
   fold_line) of a seeded QM31 column of log 22 with seeded QM31 challenges.
-  The unit is commit steps/s: a step is not a whole proof. Whole proofs (configs
-  1, 3, 4 and the serving mix, 5) are reported in proofs/s with p50/p99 beside it.
+  The unit is commit steps/s: a step is not a whole proof. Whole proofs (Wide-Fibonacci
+  100 x 2^14, the 600 + 120-column mixed-size trace, Poseidon2 at 2^18 rows) and the
+  serving mix are reported in proofs/s with p50/p99 beside it.
 
 `value` times the step with the trace already resident in HBM; `e2e` times the
 same step through the C ABI with the trace in pinned host memory, including the
@@ -16,7 +17,7 @@ Merkle root and the last FRI value. The trace (1 GiB) and the extended
 evaluation (4 GiB) exceed L2 (129 MB), so no L2 flush is needed between steps.
 
 --impl reference times the CPU restatement of the reference (the oracle; the
-Rust reference cannot be built: no cargo here or on the GPU machine) on whole steps
+Rust reference cannot be built: neither machine has cargo) on whole steps
 of the same workload, with all host threads. --gpus N starts N replicas (one
 process per GPU, torch.distributed.run) when it is not already running under a
 launcher.
@@ -209,7 +210,7 @@ class CommitStage:
 
 
 class MixedCommit:
-    """Config 3 (batched mixed-size trace): 600 M31 columns with log sizes
+    """The batched mixed-size trace: 600 M31 columns with log sizes
     10 + min(12, G), G geometric with mean ~6 (so the mean log size is ~16),
     plus 120 QM31 interaction columns (480 M31 columns) with sizes drawn the
     same way; blowup 2; lifted Blake2s commit of all 1,080 columns at the
@@ -323,7 +324,7 @@ def batched_vs_plain(torch, cs, steps: int = 5, warmup: int = 2):
 
 
 def plain_commit_step(cs):
-    """Config 2 with one launch per column for interpolate and evaluate."""
+    """The commit stage with one launch per column for interpolate and evaluate."""
     call, st, vp = cs.L.call, cs.stream(), ctypes.c_void_p
     for k in range(N_COLS):
         call("cs_interpolate_columns_into", ctypes.byref(vp(cs.t_evals[k])), ctypes.byref(vp(cs.t_coeffs[k])), 1,
@@ -342,7 +343,7 @@ def plain_commit_step(cs):
 
 
 def wide_fib_prove_native(torch, n_proofs: int = 20, log_n: int = 14, n_cols: int = 100, plain: bool = False):
-    """Config 1 through the native prover (cs_prove_wide_fib): the same proof bytes as the restated
+    """The Wide-Fibonacci proof (100 x 2^14) through the native prover (cs_prove_wide_fib): the same proof bytes as the restated
     prover, the host work in C++. Trace generated on the device from seeded inputs inside the
     timed region. Returns wall-clock latencies in ms."""
     from proving_gb300 import prover as pr
@@ -366,7 +367,7 @@ def wide_fib_prove_native(torch, n_proofs: int = 20, log_n: int = 14, n_cols: in
 
 
 def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: int = 100):
-    """Full Wide-Fibonacci proves (config 1 shape: 100 columns x 2^14 rows, blowup 2,
+    """Full Wide-Fibonacci proves (100 columns x 2^14 rows, blowup 2,
     70 queries, pow 10) through the restated prover on the CUDA backend; the
     trace is generated on the device from seeded inputs. Returns wall-clock
     latencies in ms (host orchestration included)."""
@@ -392,7 +393,7 @@ def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: in
 
 
 def mixed_prove_leg(torch, n_proofs: int = 2, arms=("batched", "plain", "native", "native_plain")):
-    """Config 3 as a full proof: the batched mixed-size trace (mixed_trace_shape: Wide-Fibonacci
+    """The batched mixed-size trace as a full proof (mixed_trace_shape: Wide-Fibonacci
     components holding 480 M31 columns and 120 single-column LogUp components, each with one M31
     value column and one QM31 running-sum column, log sizes 10..22 geometric, mean ~16) proved by
     prove_fib_and_lookups with log_blowup 1, 70 queries, pow 10, one lifted tree per phase.
@@ -494,7 +495,7 @@ def int_peaks(torch):
 
 
 def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
-    """Config 4: the Poseidon2 AIR at 8 permutations per row, 2^log_n_rows rows (1264 trace
+    """The Poseidon2 AIR at 8 permutations per row, 2^log_n_rows rows (1264 trace
     columns), log_blowup_factor 1, 70 queries, pow 10, through prove_poseidon + prove_ex on the
     CUDA backend (trace, interaction trace and constraint quotients on the device). The
     reference's own prove of this AIR stops at its sanity check (lifted protocol, constraint
@@ -567,7 +568,7 @@ def _verify_wide_fib_proof(args):
 
 
 def serving_leg(n_requests: int = 200, rate_fracs=(0.25, 0.5, 0.9)):
-    """Config 5: seeded Poisson streams of proof requests, half Wide-Fibonacci (100 columns) and half
+    """Serving: seeded Poisson streams of proof requests, half Wide-Fibonacci (100 columns) and half
     Poseidon2 (8 permutations per row), log_n_rows uniform in [12, 20]. Arms, all native provers:
     plain (1 worker, one launch per column for every per-column stage, CS_PROVE_PLAIN), batched_serial
     (1 worker, batched stages), served (4 worker threads of one process, a CUDA stream each, HBM-budget
@@ -940,10 +941,10 @@ class CpuCommitStage:
 
 
 def cpu_proof_times(mixed: bool = True, poseidon_log_rows: int = 18):
-    """Whole proofs on the oracle's own prover (oracle/oracle_prover.c, every host core): config 1
-    (Wide-Fibonacci 100 x 2^14), config 4 (Poseidon2 at 2^poseidon_log_rows rows) and, when asked,
-    config 3 (the 600 + 120-column mixed trace). The same proof bytes as the GPU provers (checked in
-    tests/test_gpu_proof_parity_full.py). Returns proofs/s and latencies per config."""
+    """Whole proofs on the oracle's own prover (oracle/oracle_prover.c, every host core):
+    Wide-Fibonacci 100 x 2^14, Poseidon2 at 2^poseidon_log_rows rows and, when asked, the 600 +
+    120-column mixed trace. The same proof bytes as the GPU provers (checked in
+    tests/test_gpu_proof_parity_full.py). Returns proofs/s and latencies per workload."""
     from oracle import oracle as O
     from proving_gb300.synthetic import m31_column, mixed_trace_shape
     fri = (10, 1, 0, 70, 1)
@@ -1160,7 +1161,7 @@ def run_case(args):
             torch.cuda.synchronize()
             lat.append((time.perf_counter() - t0) * 1e3)
         res = {"workload": f"native Poseidon2 proof, 2^{log_n} rows", "ms": [round(x, 3) for x in lat]}
-    elif args.case == "wide-fib-native":  # two native config-1 proofs after two warm-up proofs
+    elif args.case == "wide-fib-native":  # two native 100 x 2^14 Wide-Fibonacci proofs after two warm-up proofs
         lat = wide_fib_prove_native(torch, n_proofs=2)
         res = {"workload": "native Wide-Fibonacci proof, 100 x 2^14", "ms": [round(x, 3) for x in lat]}
     elif args.case == "gkr":

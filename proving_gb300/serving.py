@@ -39,7 +39,7 @@ import numpy as np
 from . import prover as pr
 from .synthetic import m31_column
 
-N_COLS = 100  # Wide-Fibonacci columns (config 1)
+N_COLS = 100  # Wide-Fibonacci columns (the 100 x 2^14 proof's width)
 
 
 @dataclass

@@ -236,7 +236,7 @@ def test_fold_line(B, log_n):
 
 
 def test_fri_fold_chain_22(B):
-    # Config-2 FRI: one QM31 column of log 22, fold_circle_into_line, then 21
+    # The commit stage's FRI: one QM31 column of log 22, fold_circle_into_line, then 21
     # fold_line steps with seeded challenges, bit-exact at every layer.
     from proving_gb300.backend import SecureColumnByCoords
     log_n = 22

@@ -1,7 +1,7 @@
 """Whole Wide-Fibonacci proofs of the restated host prover (proving_gb300.prover) on the CUDA
 backend against the oracle's own prover (oracle/oracle_prover.c: prove_ex, the commitment scheme,
 FRI and the felt stream restated in C from the reference, sharing no code with the product):
-byte-identical proofs, and the restated verifier accepts them. Sizes include the config-1 shape
+byte-identical proofs, and the restated verifier accepts them. Sizes include the benchmark's shape
 (100 columns, 2^14 rows, log blowup 1, 70 queries, pow 10)."""
 import numpy as np
 import pytest

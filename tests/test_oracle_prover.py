@@ -63,7 +63,7 @@ def test_oracle_prover_with_lookups(shape, lookup_logs, n_queries):
 
 
 def test_config1_shape_proves_and_verifies():
-    # 100 columns x 2^14 rows, 70 queries, pow 10 (the config-1 statement)
+    # 100 columns x 2^14 rows, 70 queries, pow 10 (the benchmark's Wide-Fibonacci statement)
     traces = _traces([(100, 14)], 11)
     words, _ = O.prove_fib_and_lookups((10, 1, 0, 70, 1), traces, [14])
     verify_wide_fib_components(parse_proof(words, 15), [100], [14])
