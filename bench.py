@@ -1012,7 +1012,7 @@ def run_reference(args):
     value = args.steps / sum(totals)
     sample = (f"every step whole: {N_COLS} x 2^{LOG_ROWS} interpolate, evaluate on 2^{LOG_EXT}, the full height-"
               f"{LOG_EXT} tree, {FRI_LOG} folds; the oracle (C restatement of the reference CPU backend, OpenMP); "
-              "the Rust reference cannot be built: no cargo here or on the GPU box")
+              "the Rust reference cannot be built: no cargo on either machine")
     res = {
         "metric": METRIC, "value": float(f"{value:.6g}"), "unit": UNIT, "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": float(f"{1e3 * sum(totals) / args.steps:.6g}"),
