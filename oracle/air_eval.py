@@ -1,7 +1,7 @@
 """ORACLE — test infrastructure only: the constraint DAG of proving_gb300.framework evaluated on
 the CPU with numpy, row by row over an evaluation domain, as the reference's CPU constraint
 evaluation does (crates/constraint-framework/src/prover/component_prover.rs:195-268 with
-cpu_domain.rs): masks at the row and at the previous row (orc_prev_row), each constraint times
+cpu_domain.rs): masks at the row and at rows a trace step offset away (orc_offset_row), each constraint times
 its weight, summed, over V_trace(row), added to the accumulator. Field arithmetic is written
 here on int64 arrays, independently of the prover's."""
 from __future__ import annotations
@@ -43,8 +43,10 @@ def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, 
     divide=False the weighted constraint sums are not divided by V_trace (on the trace domain itself,
     where V_trace is zero, they show whether every row satisfies the constraints)."""
     n = 1 << eval_log
-    prev = O.prev_rows(trace_log, eval_log)
-    rows = {0: np.arange(n), -1: prev}
+    rows = {0: np.arange(n)}
+    for m in air.masks:
+        if m.offset not in rows:
+            rows[m.offset] = O.offset_rows(m.offset, trace_log, eval_log)
     memo = {}
 
     def ev(x):

@@ -89,7 +89,9 @@ void orc_logup_combine(const uint32_t *const *values, uint32_t n_values, uint32_
 void orc_logup_gen_col(const uint32_t *const num[4], const uint32_t *num_m31, const uint32_t *const den[4],
                        const uint32_t *const prev[4], uint32_t log_n, uint32_t *const out[4]);
 void orc_logup_finalize_last(uint32_t *const col[4], uint32_t log_n, uint32_t claimed_out[4]);
+uint64_t orc_offset_row(uint64_t r, int64_t offset, uint32_t trace_log, uint32_t eval_log);
 uint64_t orc_prev_row(uint64_t r, uint32_t trace_log, uint32_t eval_log);
+void orc_offset_rows(int64_t offset, uint32_t trace_log, uint32_t eval_log, uint64_t *out);
 void orc_prev_rows(uint32_t trace_log, uint32_t eval_log, uint64_t *out);
 void orc_logup_composition(const uint32_t *values, const uint32_t *const inter[4], uint32_t eval_log,
                            uint32_t trace_log, const uint32_t z[4], const uint32_t claimed[4], const uint32_t rc[4],

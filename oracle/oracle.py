@@ -474,6 +474,14 @@ def prev_rows(trace_log: int, eval_log: int) -> np.ndarray:
     return out.astype(np.int64)
 
 
+def offset_rows(offset: int, trace_log: int, eval_log: int) -> np.ndarray:
+    """The row `offset` trace steps from every row of a bit-reversed evaluation domain
+    (orc_offset_row)."""
+    out = np.zeros(1 << eval_log, np.uint64)
+    lib().orc_offset_rows(ctypes.c_int64(offset), ctypes.c_uint32(trace_log), ctypes.c_uint32(eval_log), _p(out))
+    return out.astype(np.int64)
+
+
 def vanishing_inverses(eval_log: int, trace_log: int) -> np.ndarray:
     """1 / V_trace at every row of CanonicCoset(eval_log) in bit-reversed order, each row's point
     computed from its index (the denominators of evaluate_constraint_quotients_on_domain,

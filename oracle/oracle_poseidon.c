@@ -163,22 +163,36 @@ static m31 ps_coset_vanishing(coset_t c, cpoint p) {
     return x;
 }
 
-/* The row one trace step before row r of a bit-reversed evaluation domain:
+/* The row `offset` trace steps from row r of a bit-reversed evaluation domain:
    offset_bit_reversed_circle_domain_index (crates/stwo/src/core/utils.rs:144-160)
-   when the domain is larger than the trace, the coset-order predecessor
+   when the domain is larger than the trace (the natural index moves by
+   offset * 2^(eval_log - trace_log - 1) forward in the first half and backward in
+   the second, modulo the half), the coset-order neighbour
    (crates/constraint-framework/src/prover/assert.rs:58-66) when it is the trace domain. */
-uint64_t orc_prev_row(uint64_t r, uint32_t trace_log, uint32_t eval_log) {
-    uint64_t i = bit_reverse_index((uint32_t)r, eval_log);
-    uint64_t n = 1ull << eval_log, half = n / 2;
+uint64_t orc_offset_row(uint64_t r, int64_t offset, uint32_t trace_log, uint32_t eval_log) {
+    int64_t i = (int64_t)bit_reverse_index((uint32_t)r, eval_log);
+    int64_t n = 1ll << eval_log, half = n / 2;
     if (eval_log > trace_log) {
-        uint64_t step = 1ull << (eval_log - trace_log - 1);
-        i = i < half ? (i + half - step) % half : ((i - half + step) % half) + half;
+        int64_t step = offset * (1ll << (eval_log - trace_log - 1));
+        if (i < half)
+            i = (((i + step) % half) + half) % half;
+        else
+            i = (((i - step) % half) + half) % half + half;
     } else {
-        uint64_t k = i < half ? 2 * i : 2 * (n - 1 - i) + 1; /* coset index */
-        k = (k + n - 1) % n;
+        int64_t k = i < half ? 2 * i : 2 * (n - 1 - i) + 1; /* coset index */
+        k = (((k + offset) % n) + n) % n;
         i = (k & 1) ? n / 2 + (n - 1 - k) / 2 : k / 2;
     }
     return bit_reverse_index((uint32_t)i, eval_log);
+}
+
+uint64_t orc_prev_row(uint64_t r, uint32_t trace_log, uint32_t eval_log) {
+    return orc_offset_row(r, -1, trace_log, eval_log);
+}
+
+/* orc_offset_row for every row of the domain. */
+void orc_offset_rows(int64_t offset, uint32_t trace_log, uint32_t eval_log, uint64_t *out) {
+    for (uint64_t r = 0; r < (1ull << eval_log); r++) out[r] = orc_offset_row(r, offset, trace_log, eval_log);
 }
 
 /* orc_prev_row for every row of the domain. */

@@ -252,6 +252,105 @@ def verify_fib_and_lookups(proof, n_cols_list, fib_logs, lookup_logs, claimed_su
     _verify_values(proof, ch, sample_points, sizes, [0, lifting, lifting, lifting])
 
 
+def _air_at_point(air, mask, params):
+    """An AIR's constraints at a point (PointEvaluator, crates/constraint-framework/src/point.rs:
+    12-64) from its expression DAG: mask values and parameters are QM31, four base values combine
+    as from_partial_evals."""
+    memo = {}
+
+    def ev(x):
+        if x.key in memo:
+            return memo[x.key]
+        if x.op == "mask":
+            v = tuple(mask[x.args])
+        elif x.op == "const":
+            v = qm(x.args[0])
+        elif x.op == "param":
+            v = tuple(int(c) % P for c in params[x.args[0]])
+        elif x.op == "secure":
+            v = _partial([ev(c) for c in x.args])
+        elif x.op == "neg":
+            v = qsub(qm(0), ev(x.args[0]))
+        else:
+            u, w = ev(x.args[0]), ev(x.args[1])
+            v = {"add": qadd, "sub": qsub, "mul": qmul}[x.op](u, w)
+        memo[x.key] = v
+        return v
+    return [ev(c) for c in air.constraints]
+
+
+def verify_components(proof, ch, components, column_log_sizes, preprocessed_columns=()):
+    """verify (crates/stwo/src/core/verifier.rs:19-119) for components written against the
+    constraint evaluator, after the caller has replayed the trees' commitments and its own draws on
+    ch (as the reference's verifier-side example code does). components: (air, log_size, params)
+    in proving order. column_log_sizes: per committed tree (the composition's aside), the log size
+    of every column's trace domain (CommitmentSchemeVerifier::commit's log_sizes). The columns of
+    each tree are taken by the components in order, the preprocessed tree's by id from
+    preprocessed_columns. The last commitment is the composition tree's."""
+    cfg = proof.config
+    b = cfg.fri_params.log_blowup_factor
+    lifting = cfg.trace_lifting_log_size
+    mldb = lifting - b
+    n_trees = len(proof.commitments) - 1
+    if len(column_log_sizes) != n_trees:
+        raise VerificationError("one list of column sizes per committed tree")
+    random_coeff = tuple(int(v) for v in ch.draw_secure_felt())
+    ch.mix_root(proof.commitments[-1])
+    oods = _draw_oods(ch, proof)
+
+    # every tree's sample points: the components' mask offsets in steps of CanonicCoset(mldb)
+    points = [[[] for _ in sizes] for sizes in column_log_sizes]
+    pre = list(preprocessed_columns)
+    taken = [0] * n_trees
+    places = []
+    for air, log_size, _ in components:
+        place = {}
+        for tree, cols in air.mask_offsets.items():
+            if tree >= n_trees or taken[tree] + len(cols) > len(column_log_sizes[tree]):
+                raise VerificationError("a component reads columns that were not committed")
+            place[tree] = taken[tree]
+            for offsets in cols:
+                if column_log_sizes[tree][taken[tree]] != log_size:
+                    raise VerificationError("a component's column has another size")
+                pts = []
+                for o in offsets:
+                    g = point_of_index((o * (1 << (31 - mldb))) % (1 << 31))
+                    pts.append(_qpoint_add(oods, (qm(int(g[0])), qm(int(g[1])))))
+                points[tree][taken[tree]] = pts
+                taken[tree] += 1
+        pidx = []
+        for name in air.preprocessed:
+            if name not in pre:
+                raise VerificationError(f"preprocessed column {name} is not committed")
+            pidx.append(pre.index(name))
+            points[0][pidx[-1]] = [oods]
+        places.append((place, pidx))
+    sv = proof.sampled_values
+    if (len(sv) != n_trees + 1 or any(len(sv[t]) != len(points[t]) for t in range(n_trees)) or len(sv[-1]) != 8
+            or any(len(sv[t][c]) != len(points[t][c]) for t in range(n_trees) for c in range(len(points[t])))):
+        raise VerificationError("unexpected sampled_values structure")
+
+    # the components' constraints at the point against the composition polynomial's value
+    comp, dinv = _composition_at_oods(sv[-1], oods, mldb)
+    acc = qm(0)
+    for (air, _, params), (place, pidx) in zip(components, places):
+        mask = {}
+        for tree, cols in air.mask_offsets.items():
+            for k, offsets in enumerate(cols):
+                for j, o in enumerate(offsets):
+                    mask[(tree, k, o)] = sv[tree][place[tree] + k][j]
+        for k, idx in enumerate(pidx):
+            mask[(0, k, 0)] = sv[0][idx][0]
+        for cons in _air_at_point(air, mask, params):
+            acc = qadd(qmul(acc, random_coeff), qmul(cons, dinv))
+    if comp != acc:
+        raise VerificationError("OODS values do not match the AIR")
+
+    heights = [lifting if column_log_sizes[t] else 0 for t in range(n_trees)] + [lifting]
+    sizes = [[ls + b for ls in tree] for tree in column_log_sizes] + [[mldb + b] * 8]
+    _verify_values(proof, ch, points + [[[oods]] * 8], sizes, heights)
+
+
 def _verify_values(proof, ch, sample_points, sizes, heights):
     """verify_values (crates/stwo/src/core/pcs/verifier.rs:56-140) with the FRI verifier: sample_points
     and sizes per tree and column (the column's evaluation log size), heights per tree."""

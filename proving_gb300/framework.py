@@ -14,7 +14,8 @@ An AIR is a function `evaluate(e)` that reads masks and adds constraints:
             a, b = b, c
 
 Masks are M31 values of a trace or interaction column at a row offset (0: the
-row, -1: the previous row of the trace domain). `e.secure(m0, m1, m2, m3)` is
+row, -1: the previous row of the trace domain, any other integer that many
+trace steps away). `e.secure(m0, m1, m2, m3)` is
 SecureField::from_partial_evals of four base values (a QM31 interaction column
 by its coordinates), `e.param(name)` a QM31 parameter fixed per launch (lookup
 elements, claimed sums). Constraints may be M31 or QM31; the kernel adds
@@ -113,19 +114,33 @@ class Evaluator:
 
     def __init__(self):
         self.columns: dict[int, int] = {}    # interaction -> columns taken so far
+        self.mask_offsets: dict[int, list] = {}  # interaction -> the offsets of each column taken
+        self.preprocessed: list[str] = []        # the preprocessed columns read, by name
         self.params: list[str] = []
         self.constraints: list[Expr] = []
         self.fracs: list[tuple[Expr, Expr]] = []  # LogUp fractions (numerator, denominator) of the row
 
     def _mask(self, interaction: int, column: int, offset: int) -> Expr:
-        if offset not in (0, -1):
-            raise NotImplementedError("mask offsets 0 and -1 (the previous row)")
+        """A column at the row `offset` trace steps away (0 the row itself, -1 the previous row)."""
+        if not isinstance(offset, int) or not -(1 << 30) <= offset < (1 << 30):
+            raise ValueError(f"a mask offset is an integer of 31 bits or fewer: {offset!r}")
         return Expr("mask", (interaction, column, offset), False)
 
     def next_interaction_mask(self, interaction: int, offsets=(0,)):
+        if interaction < 1:
+            raise ValueError("the preprocessed tree is read with get_preprocessed_column")
         col = self.columns.get(interaction, 0)
         self.columns[interaction] = col + 1
-        return [self._mask(interaction, col, off) for off in offsets]
+        masks = [self._mask(interaction, col, off) for off in offsets]
+        self.mask_offsets.setdefault(interaction, []).append(tuple(offsets))
+        return masks
+
+    def get_preprocessed_column(self, name: str) -> Expr:
+        """EvalAtRow::get_preprocessed_column: a column of the preprocessed tree (interaction 0)
+        at the row, named by its id; the component maps the name to its column in that tree."""
+        if name not in self.preprocessed:
+            self.preprocessed.append(name)
+        return self._mask(0, self.preprocessed.index(name), 0)
 
     def next_trace_mask(self) -> Expr:
         return self.next_interaction_mask(1)[0]
@@ -220,6 +235,10 @@ class Air:
     params: list
     constraints: list
     source: str = field(repr=False)
+    # interaction -> the offsets of every column the AIR takes, in order, whether or not a
+    # constraint reads it (InfoEvaluator's mask_offsets, crates/constraint-framework/src/info.rs)
+    mask_offsets: dict = field(default_factory=dict, repr=False)
+    preprocessed: list = field(default_factory=list)  # preprocessed column ids, interaction 0 order
 
     @property
     def n_constraints(self) -> int:
@@ -275,6 +294,10 @@ def compile_air(name: str, evaluate, *args) -> Air:
     # distinct masks in first-use order over the constraints
     order, slot = [], {}
     temps, lines = {}, []
+    offsets = set()  # the mask offsets other than 0
+
+    def row_name(o: int) -> str:
+        return "r" if o == 0 else "pr" if o == -1 else f"ro_{'m' if o < 0 else 'p'}{abs(o)}"
 
     split = {"chunk": None, "owner": {}, "slot": {}}  # set while emitting a split body
 
@@ -304,7 +327,9 @@ def compile_air(name: str, evaluate, *args) -> Air:
                 slot[k] = len(order)
                 order.append(Mask(*k))
             i = slot[k]
-            row = "r" if k[2] == 0 else "pr"
+            row = row_name(k[2])
+            if k[2]:
+                offsets.add(k[2])
             name = f"m{len(temps)}"
             lines.append(f"  const uint32_t {name} = __ldg(cols[{i}] + {row});")
         elif x.op == "const":
@@ -362,6 +387,13 @@ def compile_air(name: str, evaluate, *args) -> Air:
     # value one function computes and a later one needs passes through the thread's array xs.
     funcs, calls, xs_words = "", "", 0
     body = emit(range(len(e.constraints)))
+    # one row index per mask offset in use, computed once per row
+    row_params = "".join(f", uint32_t {row_name(o)}" for o in sorted(offsets))
+    row_args = "".join(f", {row_name(o)}" for o in sorted(offsets))
+    row_defs = "".join(
+        f"    const uint32_t {row_name(o)} = "
+        + ("prev_row(r, trace_log, eval_log);\n" if o == -1 else f"offset_row(r, {o}, trace_log, eval_log);\n")
+        for o in sorted(offsets))
     if len(body) <= _SINGLE_LINES:
         inline = chr(10).join('  ' + l for l in body)
     else:
@@ -397,17 +429,16 @@ def compile_air(name: str, evaluate, *args) -> Air:
             funcs += f"""
 __device__ __noinline__ qm31 cs_air_group{g}(const uint32_t* const* __restrict__ cols,
                                             const uint32_t* __restrict__ rc,
-                                            const uint32_t* __restrict__ params, uint32_t r, uint32_t pr,
+                                            const uint32_t* __restrict__ params, uint32_t r{row_params},
                                             uint32_t* xs) {{
   (void)params;
-  (void)pr;
   (void)xs;
   qm31 acc = qm31_make(0, 0, 0, 0);
 {chr(10).join(lines_g)}
   return acc;
 }}
 """
-            calls += f"    acc = air_qm31_add(acc, cs_air_group{g}(cols, rc, params, r, pr, xs));\n"
+            calls += f"    acc = air_qm31_add(acc, cs_air_group{g}(cols, rc, params, r{row_args}, xs));\n"
         split["chunk"] = None
         inline = f"    uint32_t xs[{max(xs_words, 1)}];\n" + calls.rstrip("\n")
         funcs = "".join(f"__device__ __noinline__ {ty} air_{fn}({args}) {{ return {fn}(a, b); }}\n"
@@ -420,9 +451,7 @@ extern "C" __global__ void __launch_bounds__(256) cs_air_composition(
     uint32_t* a0, uint32_t* a1, uint32_t* a2, uint32_t* a3) {{
   const uint32_t n = 1u << eval_log;
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {{
-    const uint32_t pr = prev_row(r, trace_log, eval_log);
-    (void)pr;
-    qm31 acc = qm31_make(0, 0, 0, 0);
+{row_defs}    qm31 acc = qm31_make(0, 0, 0, 0);
 {inline}
     const qm31 v = qm31_mul_m31(acc, den[r >> trace_log]);
     a0[r] = m31_add(a0[r], v.a.a);
@@ -432,7 +461,8 @@ extern "C" __global__ void __launch_bounds__(256) cs_air_composition(
   }}
 }}
 """
-    return Air(name, order, list(e.params), list(e.constraints), src)
+    return Air(name, order, list(e.params), list(e.constraints), src,
+               {k: list(v) for k, v in sorted(e.mask_offsets.items())}, list(e.preprocessed))
 
 
 # ------------------------------------------------------------------ device side

@@ -1,0 +1,185 @@
+"""The generic prover on the CPU (the oracle's operations behind the host logic): components
+written against the constraint evaluator, committed tree by tree and proved with prove(), give the
+bytes of the AIR-specific prover and of the oracle's prover for the mixed Wide-Fibonacci + LogUp
+trace; AIRs with masks at other offsets, preprocessed columns and components of several sizes give
+proofs the oracle's restated verifier accepts, and rejects once tampered with."""
+import copy
+
+import numpy as np
+import pytest
+
+from cpu_backend import CpuOps
+from oracle import oracle as O
+from oracle.verifier import VerificationError, verify_components
+from proving_gb300 import air_prover as ap
+from proving_gb300 import framework as fw
+from proving_gb300 import prover as pr
+from proving_gb300.poseidon import ConstraintsNotSatisfied
+from test_mask_offsets_cpu import window_air, window_trace
+from test_prove_cpu import fib_and_lookups_inputs, fib_and_lookups_proof
+
+FRI = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=3, fold_step=1)
+
+
+def fib_and_lookups_generic(ops):
+    """The flow of prove_fib_and_lookups through the generic API: the empty preprocessed tree, the
+    trace tree, the lookup elements, the interaction tree after the claimed sums, then prove()."""
+    traces, logs, values, lookup_logs, _ = fib_and_lookups_inputs()
+    cfg = pr.PcsConfig(FRI, trace_lifting_log_size=10)
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(ops, cfg, ops.twiddles(10))
+    scheme.commit([], ch)
+    vals = [ops.columns_from_host([v])[0] for v in values]
+    scheme.commit([c for t in traces for c in ops.columns_from_host(t)] + vals, ch)
+    z = ch.draw_secure_felt()
+    ch.draw_secure_felt()  # alpha
+    sums, claimed = ops.logup_running_sums(vals, z)
+    ch.mix_felts(claimed)
+    scheme.commit([c for s in sums for c in ops.secure_coords(s)], ch)
+    alloc = ap.TraceLocationAllocator()
+    comps = [ap.FrameworkComponent(alloc, fw.compile_air(f"wide_fib_{len(t)}", fw.wide_fib_air, len(t)), log_n)
+             for t, log_n in zip(traces, logs)]
+    lookup = fw.compile_air("single_lookup", fw.single_lookup_air)
+    comps += [ap.FrameworkComponent(alloc, lookup, log_n, {"z": z}, claimed_sum=c)
+              for log_n, c in zip(lookup_logs, claimed)]
+    return ap.prove(comps, ch, scheme), comps, z, claimed
+
+
+def test_generic_proof_equals_the_air_specific_and_oracle_proofs():
+    ops = CpuOps()
+    proof, comps, z, claimed = fib_and_lookups_generic(ops)
+    assert proof.to_bytes() == fib_and_lookups_proof(ops).to_bytes()
+    traces, logs, values, lookup_logs, fri = fib_and_lookups_inputs()
+    want, _ = O.prove_fib_and_lookups(fri, traces, logs, values, lookup_logs)
+    assert proof.to_bytes() == want
+    # and the generic verifier accepts it, the statement's claimed sums giving the shifts
+    ch = O.Blake2sChannel()
+    ch.mix_root(proof.commitments[0])
+    ch.mix_root(proof.commitments[1])
+    ch.draw_secure_felt()
+    ch.draw_secure_felt()
+    ch.mix_felts(np.asarray([list(c) for c in claimed], np.uint32).reshape(-1, 4))
+    ch.mix_root(proof.commitments[2])
+    sizes = [[], [log_n for t, log_n in zip(traces, logs) for _ in t] + list(lookup_logs),
+             [log_n for log_n in lookup_logs for _ in range(4)]]
+    verify_components(proof, ch, [(c.air, c.log_size, c.params) for c in comps], sizes)
+
+
+def window_proof(log_n, extra=None, bad=False, check=True):
+    """The window AIR (masks at -3, -1, 0, 1, 2) over 2^log_n rows, with optional further
+    (air, host columns, log size) components in the same trace tree."""
+    ops = CpuOps()
+    extra = extra or []
+    lifting = max([log_n] + [e[2] for e in extra]) + 1
+    cfg = pr.PcsConfig(FRI, trace_lifting_log_size=lifting)
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(ops, cfg, ops.twiddles(lifting))
+    scheme.commit([], ch)
+    host = window_trace(log_n, 9, bad=bad)
+    cols = host + [c for _, cs, _ in extra for c in cs]
+    scheme.commit(ops.columns_from_host(cols), ch)
+    alloc = ap.TraceLocationAllocator()
+    comps = [ap.FrameworkComponent(alloc, fw.compile_air("window", window_air), log_n)]
+    comps += [ap.FrameworkComponent(alloc, air, n) for air, _, n in extra]
+    proof = ap.prove(comps, ch, scheme, check=check)
+    sizes = [[], [log_n] * 4 + [n for _, cs, n in extra for _ in cs]]
+    return proof, comps, sizes
+
+
+def verify_window(proof, comps, sizes):
+    ch = O.Blake2sChannel()
+    ch.mix_root(proof.commitments[0])
+    ch.mix_root(proof.commitments[1])
+    verify_components(proof, ch, [(c.air, c.log_size, c.params) for c in comps], sizes)
+
+
+@pytest.mark.parametrize("log_n", [3, 5, 7])
+def test_mask_offsets_prove_then_verify(log_n):
+    proof, comps, sizes = window_proof(log_n)
+    # x is sampled at its five offsets, y, z and w at the row; the x column has five samples, so
+    # it takes no periodicity sample
+    assert [len(c) for c in proof.sampled_values[1]] == [5, 1, 1, 1]
+    verify_window(proof, comps, sizes)
+    bad = copy.deepcopy(proof)
+    bad.sampled_values[1][0][0] = tuple((v + 1) % O.P for v in bad.sampled_values[1][0][0])
+    with pytest.raises(VerificationError):
+        verify_window(bad, comps, sizes)
+
+
+def test_unsatisfied_window_constraints_are_caught():
+    with pytest.raises(ConstraintsNotSatisfied):
+        window_proof(5, bad=True)
+    proof, comps, sizes = window_proof(5, bad=True, check=False)
+    assert not proof.constraints_satisfied
+    with pytest.raises(VerificationError):
+        verify_window(proof, comps, sizes)
+
+
+def test_components_of_several_sizes_in_one_proof():
+    # the window AIR at 2^4 rows beside a Wide-Fibonacci component of 6 columns x 2^6
+    log_f = 6
+    fib = O.wide_fib_trace(np.ones(1 << log_f, np.uint32), np.arange(1 << log_f, dtype=np.uint32), 6)
+    extra = [(fw.compile_air("wide_fib_6", fw.wide_fib_air, 6), list(fib), log_f)]
+    proof, comps, sizes = window_proof(4, extra=extra)
+    assert comps[1].trace_locations == {1: (4, 10)}
+    verify_window(proof, comps, sizes)
+
+
+def seq_air(e):
+    """y = x + seq^2 with seq a preprocessed column and x read at the next row too:
+    x[1] - x[0] = seq (the preprocessed column steps x)."""
+    seq = e.get_preprocessed_column("seq")
+    x0, x1 = e.next_interaction_mask(1, (0, 1))
+    y = e.next_trace_mask()
+    e.add_constraint(y - x0 - seq * seq)
+    e.add_constraint(x1 - x0 - seq)
+
+
+def test_preprocessed_columns_prove_then_verify():
+    log_n = 5
+    n = 1 << log_n
+    ops = CpuOps()
+    cfg = pr.PcsConfig(FRI, trace_lifting_log_size=log_n + 1)
+    # x steps by seq along the trace's coset order and wraps: seq sums to zero over the cycle
+    rng = np.random.default_rng(3)
+    seq_c = rng.integers(0, O.P, n, dtype=np.int64)
+    seq_c[-1] = (-seq_c[:-1].sum()) % O.P
+    x_c = np.concatenate([[5], (5 + np.cumsum(seq_c[:-1])) % O.P])
+    y_c = (x_c + seq_c * seq_c) % O.P
+    k = np.arange(n)
+    nat = np.where(k % 2 == 0, k // 2, n - 1 - (k - 1) // 2)
+    rows = np.array([int(format(int(v), f"0{log_n}b")[::-1], 2) for v in nat])
+    def lay(c):
+        out = np.zeros(n, np.uint32)
+        out[rows] = c
+        return out
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(ops, cfg, ops.twiddles(log_n + 1))
+    scheme.commit(ops.columns_from_host([lay(seq_c)]), ch)
+    scheme.commit(ops.columns_from_host([lay(x_c), lay(y_c)]), ch)
+    alloc = ap.TraceLocationAllocator(preprocessed_columns=["seq"])
+    air = fw.compile_air("seq", seq_air)
+    assert air.preprocessed == ["seq"] and air.mask_offsets == {1: [(0, 1), (0,)]}
+    comp = ap.FrameworkComponent(alloc, air, log_n)
+    assert comp.preprocessed_column_indices == [0]
+    proof = ap.prove([comp], ch, scheme)
+    ch = O.Blake2sChannel()
+    ch.mix_root(proof.commitments[0])
+    ch.mix_root(proof.commitments[1])
+    verify_components(proof, ch, [(air, log_n, {})], [[log_n], [log_n, log_n]], preprocessed_columns=["seq"])
+    with pytest.raises(KeyError):
+        ap.FrameworkComponent(ap.TraceLocationAllocator(preprocessed_columns=["other"]), air, log_n)
+
+
+def test_component_arguments_are_checked():
+    with pytest.raises(ValueError):
+        fw.compile_air("p", lambda e: e.next_interaction_mask(0))
+    with pytest.raises(ValueError):
+        ap.TraceLocationAllocator(preprocessed_columns=["a", "a"])
+    lookup = fw.compile_air("single_lookup", fw.single_lookup_air)
+    with pytest.raises(KeyError):
+        ap.FrameworkComponent(ap.TraceLocationAllocator(), lookup, 4)   # no z
+    c = ap.FrameworkComponent(ap.TraceLocationAllocator(), lookup, 4, {"z": (1, 2, 3, 4)}, claimed_sum=(16, 0, 0, 0))
+    assert c.params["shift"] == (1, 0, 0, 0)
+    with pytest.raises(NotImplementedError):
+        ap.CommitmentSchemeProver(CpuOps(), pr.PcsConfig(pr.FriParams(log_blowup_factor=2), 8), None)

@@ -1,0 +1,80 @@
+"""GPU parity of the generic prover: proofs of components written against the constraint evaluator,
+their constraints run as kernels compiled at run time, equal the oracle's prover (the mixed
+Wide-Fibonacci + LogUp trace) and the host prover on the oracle's operations (masks at several
+offsets, preprocessed columns, components of several sizes), byte for byte."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from cpu_backend import CpuOps  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from proving_gb300 import air_prover as ap  # noqa: E402
+from proving_gb300 import framework as fw  # noqa: E402
+from proving_gb300 import prover as pr  # noqa: E402
+from test_air_prover_cpu import FRI, fib_and_lookups_generic, seq_air  # noqa: E402
+from test_mask_offsets_cpu import window_air, window_trace  # noqa: E402
+from test_prove_cpu import fib_and_lookups_inputs  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def ops():
+    from proving_gb300 import _lib, build
+    build.build()
+    _lib.call("cs_rtc_available")
+    return pr.GpuOps()
+
+
+def test_generic_fib_and_lookups_proof_equals_oracle(ops):
+    proof, _, _, _ = fib_and_lookups_generic(ops)
+    traces, logs, values, lookup_logs, fri = fib_and_lookups_inputs()
+    want, _ = O.prove_fib_and_lookups(fri, traces, logs, values, lookup_logs)
+    assert proof.to_bytes() == want
+
+
+def _window_and_fib(o, log_w, log_f, n_fib):
+    lifting = max(log_w, log_f) + 1
+    cfg = pr.PcsConfig(FRI, trace_lifting_log_size=lifting)
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(o, cfg, o.twiddles(lifting))
+    scheme.commit([], ch)
+    fib = O.wide_fib_trace(np.ones(1 << log_f, np.uint32), np.arange(1 << log_f, dtype=np.uint32), n_fib)
+    scheme.commit(o.columns_from_host(window_trace(log_w, 9) + list(fib)), ch)
+    alloc = ap.TraceLocationAllocator()
+    comps = [ap.FrameworkComponent(alloc, fw.compile_air("window", window_air), log_w),
+             ap.FrameworkComponent(alloc, fw.compile_air(f"wide_fib_{n_fib}", fw.wide_fib_air, n_fib), log_f)]
+    return ap.prove(comps, ch, scheme).to_bytes()
+
+
+@pytest.mark.parametrize("log_w,log_f,n_fib", [(4, 6, 6), (9, 5, 3), (12, 12, 20)])
+def test_mask_offsets_proof_equals_host_prover_on_oracle_ops(ops, log_w, log_f, n_fib):
+    assert _window_and_fib(ops, log_w, log_f, n_fib) == _window_and_fib(CpuOps(), log_w, log_f, n_fib)
+
+
+def _seq_proof(o, log_n):
+    n = 1 << log_n
+    rng = np.random.default_rng(3)
+    seq_c = rng.integers(0, O.P, n, dtype=np.int64)
+    seq_c[-1] = (-seq_c[:-1].sum()) % O.P
+    x_c = np.concatenate([[5], (5 + np.cumsum(seq_c[:-1])) % O.P])
+    y_c = (x_c + seq_c * seq_c) % O.P
+    k = np.arange(n)
+    nat = np.where(k % 2 == 0, k // 2, n - 1 - (k - 1) // 2)
+    rows = np.array([int(format(int(v), f"0{log_n}b")[::-1], 2) for v in nat])
+
+    def lay(c):
+        out = np.zeros(n, np.uint32)
+        out[rows] = c
+        return out
+    cfg = pr.PcsConfig(FRI, trace_lifting_log_size=log_n + 1)
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(o, cfg, o.twiddles(log_n + 1))
+    scheme.commit(o.columns_from_host([lay(seq_c)]), ch)
+    scheme.commit(o.columns_from_host([lay(x_c), lay(y_c)]), ch)
+    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(["seq"]), fw.compile_air("seq", seq_air), log_n)
+    return ap.prove([comp], ch, scheme).to_bytes()
+
+
+def test_preprocessed_column_proof_equals_host_prover_on_oracle_ops(ops):
+    assert _seq_proof(ops, 10) == _seq_proof(CpuOps(), 10)

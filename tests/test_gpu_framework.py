@@ -114,3 +114,24 @@ def test_generic_poseidon_proof_equals_oracle_prover(B):
     proof = ps.prove_poseidon(ops, log_n, ps.poseidon_pcs_config(log_n + 3, fp), pr.Blake2sChannel(), tw, check=False,
                               generic=True)
     assert proof.to_bytes() == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
+
+
+@pytest.mark.parametrize("trace_log,eval_log,split", [(3, 5, False), (10, 12, False), (6, 8, True), (14, 16, True)])
+def test_mask_offsets_generated_equal_oracle(B, monkeypatch, trace_log, eval_log, split):
+    # masks at offsets -3, -1, 0, 1 and 2 (offset_row / prev_row in the kernel), in one body and
+    # split into functions that take each offset's row as an argument
+    from test_mask_offsets_cpu import window_air
+    if split:
+        monkeypatch.setattr(fw, "_SINGLE_LINES", 4)
+        monkeypatch.setattr(fw, "_CHUNK_NODES", 2)
+    air = fw.compile_air("window", window_air)
+    assert ("cs_air_group1(" in air.source) == split
+    host = [m31_column(500 + k, eval_log) for k in range(4)]
+    from proving_gb300.backend import BaseColumn
+    cols = [BaseColumn.from_cpu(c) for c in host]
+    rc = np.stack([seeded_qm31(510 + k) for k in range(air.n_constraints)])
+    base = [m31_column(520 + k, eval_log) for k in range(4)]
+    gen = _acc(base)
+    fw.CompiledAir.get(air).composition({1: cols}, trace_log, {}, rc, gen)
+    want = air_composition(air, {1: host}, eval_log, trace_log, {}, rc, out=base)
+    assert all(np.array_equal(a, b) for a, b in zip(gen.to_cpu(), want))
