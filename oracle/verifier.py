@@ -1,5 +1,7 @@
-"""ORACLE — test infrastructure only: the reference verifier restated for a
-Wide-Fibonacci proof produced by proving_gb300.prover (acceptance check).
+"""ORACLE — test infrastructure only: the reference verifier restated for the
+proofs of proving_gb300.prover and proving_gb300.air_prover (acceptance check):
+Wide-Fibonacci components, their LogUp neighbours, and any AIR recorded by the
+constraint evaluator (verify_components).
 
 Follows verify_ex (crates/stwo/src/core/verifier.rs:30-119),
 CommitmentSchemeVerifier (crates/stwo/src/core/pcs/verifier.rs:20-140),
