@@ -551,6 +551,16 @@ cs_status cs_rtc_compile_air(const char *source, uint32_t n_headers, const char 
 cs_status cs_rtc_air_composition(void *handle, const uint32_t *const *h_cols, const uint32_t *h_rc,
                                  const uint32_t *h_params, uint32_t eval_log, uint32_t trace_log,
                                  uint32_t *const h_accum[4], cs_stream stream);
+/* The same on the subdomain of a committed evaluation (EvaluationMode::SubDomain
+   { log_expansion }, crates/stwo/src/prover/air/accumulation.rs:20-62, with
+   subdomain_eval_domain, crates/constraint-framework/src/prover/component_prover.rs:234-238):
+   the rows are the first 2^eval_log of columns committed on
+   CanonicCoset(eval_log + log_expansion) in bit-reversed order, and the
+   denominators are V_trace at those points. log_expansion 0 is
+   cs_rtc_air_composition. */
+cs_status cs_rtc_air_composition_subdomain(void *handle, const uint32_t *const *h_cols, const uint32_t *h_rc,
+                                           const uint32_t *h_params, uint32_t eval_log, uint32_t trace_log,
+                                           uint32_t log_expansion, uint32_t *const h_accum[4], cs_stream stream);
 cs_status cs_rtc_release(void *handle);
 
 /* ------------------------------------------------------- AIR: Poseidon2 */

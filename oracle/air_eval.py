@@ -38,10 +38,12 @@ def _as_q(v, n):
 
 
 def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, params, rc, out=None,
-                    divide: bool = True):
+                    divide: bool = True, log_expansion: int = 0):
     """The accumulator (4 coordinate arrays, created when None) plus the AIR's quotients. With
     divide=False the weighted constraint sums are not divided by V_trace (on the trace domain itself,
-    where V_trace is zero, they show whether every row satisfies the constraints)."""
+    where V_trace is zero, they show whether every row satisfies the constraints). With
+    log_expansion e the columns are committed on CanonicCoset(eval_log + e) and the rows are their
+    first 2^eval_log, that domain's subdomain (component_prover.rs:36-48, 234-238)."""
     n = 1 << eval_log
     rows = {0: np.arange(n)}
     for m in air.masks:
@@ -85,7 +87,7 @@ def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, 
         v = _as_q(ev(c), n)
         acc = (acc + _qmul(v, np.tile(w % P, (n, 1)))) % P
     if divide:
-        den = O.vanishing_inverses(eval_log, trace_log)
+        den = O.vanishing_inverses(eval_log, trace_log, log_expansion)
         acc = acc * den[:, None] % P
     if out is None:
         out = [np.zeros(n, np.uint32) for _ in range(4)]

@@ -482,13 +482,15 @@ def offset_rows(offset: int, trace_log: int, eval_log: int) -> np.ndarray:
     return out.astype(np.int64)
 
 
-def vanishing_inverses(eval_log: int, trace_log: int) -> np.ndarray:
+def vanishing_inverses(eval_log: int, trace_log: int, log_expansion: int = 0) -> np.ndarray:
     """1 / V_trace at every row of CanonicCoset(eval_log) in bit-reversed order, each row's point
     computed from its index (the denominators of evaluate_constraint_quotients_on_domain,
-    crates/constraint-framework/src/prover/component_prover.rs:101-108)."""
+    crates/constraint-framework/src/prover/component_prover.rs:101-108). With log_expansion e the
+    domain is CanonicCoset(eval_log + e).circle_domain().split(e).0 (subdomain_eval_domain,
+    component_prover.rs:234-238): the larger domain's initial point, the same step."""
     n = 1 << eval_log
     hs = n >> 1
-    half_init = 1 << (31 - (eval_log + 1))
+    half_init = 1 << (31 - (eval_log + log_expansion + 1))
     half_step = (1 << (31 - (eval_log - 1))) if eval_log >= 1 else 0
     mask = (1 << 31) - 1
     nat = bit_reverse(np.arange(n, dtype=np.uint32)).astype(np.int64) if n > 1 else np.zeros(1, np.int64)

@@ -440,20 +440,23 @@ def _verify_values(proof, ch, sample_points, sizes, heights):
             total = qadd(total, (r0[0], r0[1], r1[0], r1[1]))
         answers.append(total)
 
-    # FRI decommitment (fri.rs:306-399, 460-720), fold_step 1
-    def rebuild(qs, evals, witness):
+    # FRI decommitment (fri.rs:306-399, 460-800): each layer's queries grouped in cosets of
+    # 2^step positions, rebuilt from the previous layer's values and the witness, checked against
+    # the layer's tree (leaves of 4 positions when step > 1 and the layer has 4 or more values,
+    # build_merkle_verification_inputs) and folded step times into the next layer's values
+    def rebuild(qs, evals, witness, step):
         wit = iter(witness)
         ev = iter(evals)
         positions, subsets, starts = [], [], []
         i = 0
         while i < len(qs):
             j = i
-            while j + 1 < len(qs) and qs[j + 1] >> 1 == qs[i] >> 1:
+            while j + 1 < len(qs) and qs[j + 1] >> step == qs[i] >> step:
                 j += 1
-            group = qs[i:j + 1]
-            start = (group[0] >> 1) << 1
+            group = set(qs[i:j + 1])
+            start = (qs[i] >> step) << step
             vals = []
-            for pos in (start, start + 1):
+            for pos in range(start, start + (1 << step)):
                 positions.append(pos)
                 if pos in group:
                     vals.append(next(ev))
@@ -469,37 +472,85 @@ def _verify_values(proof, ch, sample_points, sizes, heights):
             raise VerificationError("FRI witness too long")
         return positions, subsets, starts
 
-    def check_layer(layer, log_size, positions, subsets):
+    def check_layer(layer, log_size, positions, subsets, step):
         vals = [v for s in subsets for v in s]
-        cols = [[v[c] for v in vals] for c in range(4)]
-        merkle_verify(layer["commitment"], log_size, [log_size] * 4, positions, cols, layer["decommitment"])
+        if step > 1 and log_size >= 2:
+            # leaf r holds positions 4r..4r+3, column coord + 4 offset (pack_leaves_input)
+            leaves = sorted(set(p_ >> 2 for p_ in positions))
+            by_pos = dict(zip(positions, vals))
+            cols = [[by_pos[4 * r + off][coord] for r in leaves] for off in range(4) for coord in range(4)]
+            merkle_verify(layer["commitment"], log_size - 2, [log_size - 2] * 16, leaves, cols, layer["decommitment"])
+        else:
+            cols = [[v[c] for v in vals] for c in range(4)]
+            merkle_verify(layer["commitment"], log_size, [log_size] * 4, positions, cols, layer["decommitment"])
 
     def ibfly(v0, v1, t):
         return qadd(v0, v1), tuple((x * t) % P for x in qsub(v0, v1))
 
-    pos, subsets, starts = rebuild(queries, answers, [tuple(w) for w in proof.fri_first_layer["fri_witness"]])
-    check_layer(proof.fri_first_layer, column_log, pos, subsets)
+    def fold_coset(vals, init, log_n, alpha):
+        """fold_coset (fri.rs:770-800): values on the x-coordinates of Coset(init, log_n) in
+        bit-reversed order folded log_n times, alpha squared after each fold, the domain doubled."""
+        cur = list(vals)
+        step_idx = (1 << (31 - log_n)) if log_n else 0
+        a = alpha
+        for i in range(log_n):
+            n = log_n - i
+            nxt = []
+            for j in range(0, 1 << n, 2):
+                x, _ = point_of_index(init + bitrev(j, n) * step_idx)
+                f0, f1 = ibfly(cur[j], cur[j + 1], pow(x, P - 2, P))
+                nxt.append(qadd(f0, qmul(a, f1)))
+            cur = nxt
+            init, step_idx, a = 2 * init, 2 * step_idx, qmul(a, a)
+        return cur[0]
+
+    # first layer: the circle fold, then fold_step - 1 line folds with alpha^2 (fold_circle)
+    k = fp.fold_step
+    pos, subsets, starts = rebuild(queries, answers, [tuple(w) for w in proof.fri_first_layer["fri_witness"]], k)
+    check_layer(proof.fri_first_layer, column_log, pos, subsets, k)
     evals = []
-    for s, start in zip(subsets, starts):
-        _, py_ = point_of_index(circle_domain_index(column_log, bitrev(start, column_log)))
-        f0, f1 = ibfly(s[0], s[1], pow(py_, P - 2, P))
-        evals.append(qadd(qmul(first_alpha, f1), f0))
-    qs = sorted(set(q >> 1 for q in queries))
-    for layer, alpha, log_size in zip(proof.fri_inner_layers, inner_alphas, layer_logs):
-        pos, subsets, starts = rebuild(qs, evals, [tuple(w) for w in layer["fri_witness"]])
-        check_layer(layer, log_size, pos, subsets)
-        evals = []
-        init, step = 1 << (31 - (log_size + 2)), 1 << (31 - log_size)
-        for s, start in zip(subsets, starts):
-            x, _ = point_of_index(init + bitrev(start, log_size) * step)
-            f0, f1 = ibfly(s[0], s[1], pow(x, P - 2, P))
-            evals.append(qadd(f0, qmul(alpha, f1)))
-        qs = sorted(set(q >> 1 for q in qs))
-    # last layer: a constant polynomial
-    if fp.log_last_layer_degree_bound != 0:
-        raise NotImplementedError("last layer degree bound > 0")
-    for e in evals:
-        if e != tuple(proof.fri_last_layer_poly[0]):
+    half_init = 1 << (31 - (column_log + 1))
+    half_step = 1 << (31 - (column_log - 1))
+    for sv_, start in zip(subsets, starts):
+        # the subset's circle domain: half coset at the start's point, 2^(k-1) points
+        init = (half_init + bitrev(start, column_log) * half_step) % (1 << 31)
+        sub_step = (1 << (31 - (k - 1))) if k > 1 else 0
+        line = []
+        for j in range(0, 1 << k, 2):
+            _, py_ = point_of_index(init + bitrev(j, k) * sub_step)
+            f0, f1 = ibfly(sv_[j], sv_[j + 1], pow(py_, P - 2, P))
+            line.append(qadd(f0, qmul(first_alpha, f1)))
+        evals.append(fold_coset(line, init, k - 1, qmul(first_alpha, first_alpha)))
+    qs = sorted(set(q >> k for q in queries))
+    for layer, alpha, log_size, step in zip(proof.fri_inner_layers, inner_alphas, layer_logs, steps):
+        pos, subsets, starts = rebuild(qs, evals, [tuple(w) for w in layer["fri_witness"]], step)
+        check_layer(layer, log_size, pos, subsets, step)
+        init0, lstep = 1 << (31 - (log_size + 2)), 1 << (31 - log_size)
+        evals = [fold_coset(sv_, (init0 + bitrev(start, log_size) * lstep) % (1 << 31), step, alpha)
+                 for sv_, start in zip(subsets, starts)]
+        qs = sorted(set(q >> step for q in qs))
+    # last layer (fri.rs:540-560): the polynomial, its coefficients bit-reversed, at each query's
+    # point of the last line domain, by folding with the doublings of x (LinePoly::eval_at_point)
+    last_log = line_log
+    coeffs = [tuple(int(v) for v in c) for c in proof.fri_last_layer_poly]
+    n_log = len(coeffs).bit_length() - 1
+    if len(coeffs) != 1 << n_log:
+        raise VerificationError("last layer size")
+
+    def line_eval(cs, xs_):
+        if len(cs) == 1:
+            return cs[0]
+        h = len(cs) // 2
+        return qadd(line_eval(cs[:h], xs_[1:]), qmul(line_eval(cs[h:], xs_[1:]), xs_[0]))
+    init0, lstep = 1 << (31 - (last_log + 2)), 1 << (31 - last_log)
+    for q, e in zip(qs, evals):
+        x, _ = point_of_index(init0 + bitrev(q, last_log) * lstep)
+        xs_ = []
+        xq = qm(x)
+        for _ in range(n_log):
+            xs_.append(xq)
+            xq = qsub(qadd(qmul(xq, xq), qmul(xq, xq)), qm(1))
+        if e != line_eval(coeffs, xs_):
             raise VerificationError("last layer evaluations invalid")
 
 

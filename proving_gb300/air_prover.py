@@ -65,14 +65,17 @@ class FrameworkComponent:
     """An AIR over a trace of 2^log_size rows with its columns' places in the trees
     (FrameworkComponent::new). params: the AIR's QM31 parameters by name. claimed_sum: the
     component's LogUp claimed sum; when the AIR reads the parameter `shift` and params do not give
-    it, it is claimed_sum / 2^log_size (LogupAtRow::new). The constraints are evaluated on
-    CanonicCoset(log_size + log_expansion) (max_constraint_log_degree_bound)."""
+    it, it is claimed_sum / 2^log_size (LogupAtRow::new). constraint_log_degree: log2 of the
+    constraints' degree bound over the trace's, so that max_constraint_log_degree_bound is
+    log_size + constraint_log_degree (the examples' LOG_EXPAND)."""
 
     def __init__(self, allocator: TraceLocationAllocator, air: Air, log_size: int, params=None,
-                 claimed_sum=None, log_expansion: int = 1):
+                 claimed_sum=None, constraint_log_degree: int = 1):
+        if constraint_log_degree < 1:
+            raise ValueError("the composition polynomial is split in two: constraint_log_degree >= 1")
         self.air = air
         self.log_size = log_size
-        self.log_expansion = log_expansion
+        self.constraint_log_degree = constraint_log_degree
         self.trace_locations = allocator.next_for_structure(air.mask_offsets)
         self.preprocessed_column_indices = [allocator.preprocessed_index(n) for n in air.preprocessed]
         self.claimed_sum = qm(0) if claimed_sum is None else tuple(int(x) % P for x in claimed_sum)
@@ -90,7 +93,7 @@ class FrameworkComponent:
         return self.air.n_constraints
 
     def max_constraint_log_degree_bound(self) -> int:
-        return self.log_size + self.log_expansion
+        return self.log_size + self.constraint_log_degree
 
     def mask_points(self, point, max_log_degree_bound: int) -> dict:
         """(tree, column) -> the points its values are sampled at: the point plus offset steps of
@@ -161,13 +164,28 @@ class _Tree:
         self.evals, self.coeffs, self.log_sizes, self.merkle, self.root = evals, coeffs, log_sizes, merkle, root
 
 
+def evaluation_mode(components, log_blowup_factor: int):
+    """EvaluationMode::infer (crates/stwo/src/prover/air/accumulation.rs:42-62): the common
+    log_expansion = log_blowup_factor - constraint log degree of every component (SubDomain: the
+    constraints are evaluated on a subdomain of the committed evaluations), or None when a
+    component's constraint degree exceeds the blowup or two components differ
+    (ExtendToEvalDomain: the columns are evaluated anew on CanonicCoset(max constraint bound))."""
+    common = None
+    for c in components:
+        if c.constraint_log_degree > log_blowup_factor:
+            return None
+        e = log_blowup_factor - c.constraint_log_degree
+        if common is not None and common != e:
+            return None
+        common = e
+    return 0 if common is None else common
+
+
 class CommitmentSchemeProver:
     """The committed trees of one proof (CommitmentSchemeProver). twiddles: for the largest
-    evaluation domain the proof uses. config.fri_params.log_blowup_factor must be 1."""
+    evaluation domain the proof uses."""
 
     def __init__(self, ops, config: PcsConfig, twiddles):
-        if config.fri_params.log_blowup_factor != 1:
-            raise NotImplementedError("log_blowup_factor = 1 (SubDomain evaluation with log_expansion 0)")
         self.ops, self.config, self.twiddles = ops, config, twiddles
         self.trees: list[_Tree] = []
 
@@ -195,13 +213,13 @@ class CommitmentSchemeProver:
         channel.mix_root(tree.root)
         return tree.root
 
-    def component_columns(self, comp: FrameworkComponent, eval_log: int) -> dict:
-        """interaction -> the component's columns on CanonicCoset(eval_log): the committed
-        evaluations when that is their domain (SubDomain with log_expansion 0), else the
-        coefficients evaluated there (ExtendToEvalDomain)."""
+    def component_columns(self, comp: FrameworkComponent, eval_log: int, subdomain: bool) -> dict:
+        """interaction -> the component's columns for its constraint evaluation
+        (get_trace_columns, crates/constraint-framework/src/prover/component_prover.rs:29-56): in
+        SubDomain mode the committed evaluations, whose first 2^eval_log rows are the evaluation
+        domain; in ExtendToEvalDomain mode the columns on CanonicCoset(eval_log), the committed
+        evaluations when that is their domain, else the coefficients evaluated there."""
         b = self.config.fri_params.log_blowup_factor
-        if eval_log < comp.log_size + b:
-            raise NotImplementedError("log_blowup_factor above the constraint degree (SubDomain with expansion)")
         picks = {t: list(range(s, e)) for t, (s, e) in comp.trace_locations.items()}
         if comp.preprocessed_column_indices:
             picks[0] = comp.preprocessed_column_indices
@@ -212,7 +230,7 @@ class CommitmentSchemeProver:
             tree = self.trees[t]
             if any(tree.log_sizes[i] != comp.log_size for i in idx):
                 raise ValueError(f"{comp.air.name}: a column of tree {t} is not 2^{comp.log_size} rows")
-            if eval_log == comp.log_size + b:
+            if subdomain or eval_log == comp.log_size + b:
                 out[t] = [tree.evals[i] for i in idx]
             else:
                 out[t] = self.ops.evaluate([tree.coeffs[i] for i in idx], eval_log, self.twiddles) if idx else []
@@ -234,6 +252,7 @@ def prove(components, channel: pr.Blake2sChannel, scheme: CommitmentSchemeProver
     # --- composition polynomial (ComponentProvers::compute_composition_polynomial): components in
     # order take the highest powers of the random coefficient, each constraint the next lower one
     random_coeff = channel.draw_secure_felt()
+    log_expansion = evaluation_mode(components, b)
     total = sum(c.n_constraints for c in components)
     powers = ops.secure_powers(random_coeff, total)
     sub_acc, start = {}, 0
@@ -243,13 +262,18 @@ def prove(components, channel: pr.Blake2sChannel, scheme: CommitmentSchemeProver
         eval_log = comp.max_constraint_log_degree_bound()
         if eval_log not in sub_acc:
             sub_acc[eval_log] = ops.secure_zeros(1 << eval_log)
-        ops.air_composition(comp.air, scheme.component_columns(comp, eval_log), comp.log_size, comp.params, rc,
-                            sub_acc[eval_log])
+        cols = scheme.component_columns(comp, eval_log, log_expansion is not None)
+        ops.air_composition(comp.air, cols, comp.log_size, comp.params, rc, sub_acc[eval_log], log_expansion or 0)
         start += n
     accs = [sub_acc[k] for k in sorted(sub_acc)]
     accum = accs[0] if len(accs) == 1 else ops.lift_and_accumulate(accs)
     comp_log = max(sub_acc)
-    comp_coeffs = ops.interpolate_secure(accum, tw)
+    # DomainEvaluationAccumulator::finalize (accumulation.rs:136-180): on the subdomain of
+    # CanonicCoset(comp_log + log_expansion) in SubDomain mode, else on CanonicCoset(comp_log)
+    if log_expansion:
+        comp_coeffs = ops.interpolate_secure_on_subdomain(accum, comp_log + log_expansion, tw)
+    else:
+        comp_coeffs = ops.interpolate_secure(accum, tw)
     left, right = ops.split_at_mid(comp_coeffs)
     comp_evals = ops.evaluate(left + right, (comp_log - 1) + b, tw)
     comp_tree = ops.merkle_commit(comp_evals, L)
@@ -321,4 +345,4 @@ def prove(components, channel: pr.Blake2sChannel, scheme: CommitmentSchemeProver
 
 
 __all__ = ["TraceLocationAllocator", "FrameworkComponent", "CommitmentSchemeProver", "prove",
-           "constraints_at_point", "point_at_offset"]
+           "constraints_at_point", "point_at_offset", "evaluation_mode"]

@@ -157,6 +157,13 @@ extern "C" cs_status cs_rtc_release(void* handle) {
 extern "C" cs_status cs_rtc_air_composition(void* handle, const uint32_t* const* h_cols, const uint32_t* h_rc,
                                             const uint32_t* h_params, uint32_t eval_log, uint32_t trace_log,
                                             uint32_t* const h_accum[4], cs_stream stream) {
+  return cs_rtc_air_composition_subdomain(handle, h_cols, h_rc, h_params, eval_log, trace_log, 0, h_accum, stream);
+}
+
+extern "C" cs_status cs_rtc_air_composition_subdomain(void* handle, const uint32_t* const* h_cols,
+                                                      const uint32_t* h_rc, const uint32_t* h_params,
+                                                      uint32_t eval_log, uint32_t trace_log, uint32_t log_expansion,
+                                                      uint32_t* const h_accum[4], cs_stream stream) {
   CS_CHECK_ARG(handle != nullptr && h_accum != nullptr, "rtc_air_composition: null pointer");
   const RtcKernel* k = static_cast<const RtcKernel*>(handle);
   CS_CHECK_ARG(k->n_cols == 0 || h_cols != nullptr, "rtc_air_composition: null column table");
@@ -164,10 +171,15 @@ extern "C" cs_status cs_rtc_air_composition(void* handle, const uint32_t* const*
   CS_CHECK_ARG(k->n_params == 0 || h_params != nullptr, "rtc_air_composition: null parameters");
   CS_CHECK_ARG(trace_log >= 1 && eval_log >= trace_log && eval_log - trace_log <= 5 && eval_log <= 30,
                "rtc_air_composition: bad sizes eval %u trace %u", eval_log, trace_log);
+  CS_CHECK_ARG(log_expansion <= 8 && eval_log + log_expansion <= 30,
+               "rtc_air_composition: bad log_expansion %u for eval %u", log_expansion, eval_log);
   for (uint32_t c = 0; c < k->n_cols; c++) CS_CHECK_ARG(h_cols[c] != nullptr, "rtc_air_composition: column %u is null", c);
   for (int c = 0; c < 4; c++) CS_CHECK_ARG(h_accum[c] != nullptr, "rtc_air_composition: null accumulator");
   // one staging buffer: column pointers, then the weights, the parameters and 1 / V_trace
-  // (bit-reversed over the 2^(eval - trace) cosets, component_prover.rs:101-108)
+  // (bit-reversed over the 2^(eval - trace) cosets, component_prover.rs:101-108). The evaluation
+  // domain is CanonicCoset(eval + log_expansion).circle_domain().split(log_expansion).0: the
+  // half coset keeps the larger domain's initial point G_2^(eval + log_expansion + 1) and takes
+  // the step G_2^(eval - 1) (CircleDomain::split; log_expansion 0 is CanonicCoset(eval) itself).
   const size_t n_words = 2 * (size_t)k->n_cols + 4 * (size_t)k->n_constraints + 4 * (size_t)k->n_params + 32;
   std::vector<uint32_t> host(n_words, 0);
   for (uint32_t c = 0; c < k->n_cols; c++) {
@@ -180,7 +192,7 @@ extern "C" cs_status cs_rtc_air_composition(void* handle, const uint32_t* const*
   for (size_t i = 0; i < 4 * (size_t)k->n_params; i++) *w++ = h_params[i] % P;
   const uint32_t log_expand = eval_log - trace_log;
   for (uint32_t i = 0; i < (1u << log_expand); i++) {
-    const uint32_t idx = (subgroup_gen(eval_log + 1) + i * subgroup_gen(eval_log - 1)) & 0x7fffffffu;
+    const uint32_t idx = (subgroup_gen(eval_log + log_expansion + 1) + i * subgroup_gen(eval_log - 1)) & 0x7fffffffu;
     uint32_t x = rtc_point_at(idx).x;
     for (uint32_t t = 1; t < trace_log; t++) x = m31_sub(m31_add(m31_sqr(x), m31_sqr(x)), 1);
     uint32_t j = 0;

@@ -216,6 +216,7 @@ class Evaluator:
 
 _PRELUDE = """typedef unsigned int uint32_t;
 typedef unsigned long long uint64_t;
+typedef int int32_t;
 #include "field.cuh"
 #include "rows.cuh"
 using namespace cs;
@@ -494,21 +495,25 @@ class CompiledAir:
             cls._cache[key] = cls(air)
         return cls._cache[key]
 
-    def composition(self, columns_by_interaction, trace_log: int, params, rc, accum) -> None:
-        """Adds the AIR's constraint quotients over accum's domain (the evaluation domain of the
-        columns). params: {name: QM31}; rc: one QM31 weight per constraint."""
+    def composition(self, columns_by_interaction, trace_log: int, params, rc, accum, log_expansion: int = 0) -> None:
+        """Adds the AIR's constraint quotients over accum's domain. params: {name: QM31}; rc: one
+        QM31 weight per constraint. With log_expansion 0 the columns are evaluations on accum's
+        domain, CanonicCoset(log len(accum)); with log_expansion e they are committed on
+        CanonicCoset(log len(accum) + e) and accum's domain is their first len(accum) rows, that
+        domain's subdomain (EvaluationMode::SubDomain)."""
         from . import _lib
         from .backend import _ptr_table, _stream
         cols = self.air.mask_columns(columns_by_interaction)
-        # the kernel reads every mask column at rows below len(accum): the columns must be that long
-        if any(len(c) != len(accum) for c in cols):
-            raise ValueError("mask columns must be evaluations on the accumulator's domain")
+        # the kernel reads every mask column at rows below len(accum)
+        if any(len(c) != len(accum) << log_expansion for c in cols):
+            raise ValueError("mask columns must be evaluations on the accumulator's domain, or on the domain "
+                             "it is the subdomain of")
         rcw = np.ascontiguousarray(np.asarray(rc, np.uint32).reshape(-1))
         assert rcw.size == 4 * self.air.n_constraints
         pw = np.ascontiguousarray(np.asarray([params[p] for p in self.air.params], np.uint32).reshape(-1))
-        _lib.call("cs_rtc_air_composition", self.handle, _ptr_table([c.data for c in cols]),
+        _lib.call("cs_rtc_air_composition_subdomain", self.handle, _ptr_table([c.data for c in cols]),
                   rcw.ctypes.data, pw.ctypes.data if pw.size else None, len(accum).bit_length() - 1, trace_log,
-                  _ptr_table([c.data for c in accum.columns]), _stream())
+                  log_expansion, _ptr_table([c.data for c in accum.columns]), _stream())
 
 
 # ------------------------------------------------------------------ AIRs

@@ -446,7 +446,10 @@ class FriLayerDecommit:
     def __init__(self, reads: Reads, column, tree, query_positions, fold_step: int, ops):
         self.positions, self.is_witness = decommitment_positions(query_positions, fold_step)
         self.coord_handles = [reads.values(c, self.positions) for c in ops.secure_coords(column)]
-        self.merkle = MerkleDecommit(reads, tree, self.positions, [], ops)
+        # a packed tree opens the leaves holding the positions (fri.rs:318-326)
+        packed = packs_leaves(fold_step, ops.secure_len(column).bit_length() - 1)
+        merkle_positions = np.unique(self.positions >> LOG_PACKED_LEAF_SIZE) if packed else self.positions
+        self.merkle = MerkleDecommit(reads, tree, merkle_positions, [], ops)
         self.reads = reads
         self.tree = tree
 
@@ -1006,43 +1009,82 @@ class HostFriChannel:
         pass
 
 
+LOG_PACKED_LEAF_SIZE = 2  # crates/stwo/src/core/vcs_lifted/verifier.rs:16
+
+
+def squared_alpha_powers(alpha, n: int) -> list:
+    """squared_alpha_powers (crates/stwo/src/prover/fri.rs:79-87): alpha, alpha^2, alpha^4, ..."""
+    out = []
+    for _ in range(n):
+        out.append(alpha)
+        alpha = qm_mul(alpha, alpha)
+    return out
+
+
+def packs_leaves(fold_step: int, log_size: int) -> bool:
+    """Whether a FRI layer's tree has leaves of 2^LOG_PACKED_LEAF_SIZE consecutive values
+    (FriFirstLayerProver::new / FriInnerLayerProver::new, fri.rs:294-305, 357-367)."""
+    return fold_step > 1 and log_size >= LOG_PACKED_LEAF_SIZE
+
+
+def _commit_layer(ops, column, log_size: int, fold_step: int):
+    """A FRI layer's lifted Merkle tree over its 4 coordinate columns, or, with packed leaves,
+    over the 16 columns of pack_leaves_input at 2^(log_size - 2) rows."""
+    cols = ops.secure_columns(column)
+    if packs_leaves(fold_step, log_size):
+        return ops.merkle_commit(ops.pack_leaves(cols), log_size - LOG_PACKED_LEAF_SIZE)
+    return ops.merkle_commit(cols, log_size)
+
+
 def fri_layers(ops, ch, fp: FriParams, column, log_size: int, twiddles):
-    """The layer loop of FriProver::commit (crates/stwo/src/prover/fri.rs:113-206), fold_step 1:
-    commit a layer, mix its root, draw the challenge, fold. Returns (first tree, inner layers,
-    the last evaluation); the channel `ch` is finished by the caller."""
-    first_tree = ops.merkle_commit(ops.secure_columns(column), log_size)
+    """The layer loop of FriProver::commit (crates/stwo/src/prover/fri.rs:113-206): commit a
+    layer, mix its root, draw the challenge, fold. The first layer's circle fold is followed by
+    fold_step - 1 line folds with alpha^2, alpha^4, ...; every inner layer folds fold_step times
+    (alpha, alpha^2, ...), the last one the 1..fold_step folds left. Returns (first tree, inner
+    layers, the last evaluation); the channel `ch` is finished by the caller."""
+    k = fp.fold_step
+
+    def fold(layer, alpha, steps):
+        if steps == 1:
+            return ops.fold_line(layer, alpha, twiddles)
+        return ops.fold_line_steps(layer, squared_alpha_powers(alpha, steps), twiddles)
+
+    first_tree = _commit_layer(ops, column, log_size, k)
     ch.mix_root(first_tree)
     alpha = ch.draw()
     layer = ops.fold_circle_into_line(column, alpha, twiddles)
     line_log = log_size - 1
+    if k > 1:
+        layer = fold(layer, qm_mul(alpha, alpha), k - 1)
+        line_log -= k - 1
     last_log = (fp.last_layer_domain_size()).bit_length() - 1
+    if line_log < last_log:
+        raise ValueError("the circle-to-line fold results in a smaller line domain than the last layer")
     inner = []
-    while line_log > last_log + fp.fold_step:
-        tree = ops.merkle_commit(ops.secure_columns(layer), line_log)
+    if line_log == last_log:
+        return first_tree, inner, layer
+    while line_log > last_log + k:
+        tree = _commit_layer(ops, layer, line_log, k)
         ch.mix_root(tree)
         alpha = ch.draw()
-        inner.append({"tree": tree, "eval": layer, "fold_step": fp.fold_step})
-        layer = ops.fold_line(layer, alpha, twiddles)
-        line_log -= fp.fold_step
-    # with fold_step 1 the loop above leaves exactly one fold for the last layer
+        inner.append({"tree": tree, "eval": layer, "fold_step": k})
+        layer = fold(layer, alpha, k)
+        line_log -= k
     last_step = line_log - last_log
-    if last_step != 1:
-        raise NotImplementedError("a last FRI step of more than one fold")
-    tree = ops.merkle_commit(ops.secure_columns(layer), line_log)
+    tree = _commit_layer(ops, layer, line_log, last_step)
     ch.mix_root(tree)
     alpha = ch.draw()
     inner.append({"tree": tree, "eval": layer, "fold_step": last_step})
-    layer = ops.fold_line(layer, alpha, twiddles)
+    layer = fold(layer, alpha, last_step)
     return first_tree, inner, layer
 
 
 def fri_commit(ops, channel, fp: FriParams, column, log_size: int, twiddles):
-    """FriProver::commit (crates/stwo/src/prover/fri.rs:113-226), fold_step 1 (no leaf packing). The
-    ops may run the layer loop themselves (ops.fri_layers: the channel kept on the device, so that
-    mixing each root and drawing each challenge needs no host round trip)."""
-    if fp.fold_step != 1:
-        raise NotImplementedError("fold_step > 1")
-    if hasattr(ops, "fri_layers"):
+    """FriProver::commit (crates/stwo/src/prover/fri.rs:113-226). With fold_step 1 the ops may run
+    the layer loop themselves (ops.fri_layers: the channel kept on the device, so that mixing each
+    root and drawing each challenge needs no host round trip); a larger fold_step squares each
+    challenge on the host."""
+    if hasattr(ops, "fri_layers") and fp.fold_step == 1:
         first_tree, inner, layer = ops.fri_layers(channel, fp, column, log_size, twiddles)
     else:
         ch = HostFriChannel(channel)
@@ -1155,10 +1197,16 @@ class GpuOps:
         cols, claimed = self.B.logup_running_sums(values, np.asarray(z, np.uint32))
         return cols, [tuple(int(x) for x in row) for row in claimed.cpu().numpy().view(np.uint32)]
 
-    def air_composition(self, air, columns_by_interaction, trace_log, params, rc, accum):
+    def air_composition(self, air, columns_by_interaction, trace_log, params, rc, accum, log_expansion=0):
         """An AIR's constraint quotients through the generic path (run-time compiled kernel)."""
         from .framework import CompiledAir
-        CompiledAir.get(air).composition(columns_by_interaction, trace_log, params, rc, accum)
+        CompiledAir.get(air).composition(columns_by_interaction, trace_log, params, rc, accum, log_expansion)
+
+    def interpolate_secure_on_subdomain(self, accum, domain_log_size, tw):
+        """The accumulator interpolated on the subdomain of its size of CanonicCoset(domain_log_size)
+        (DomainEvaluationAccumulator::finalize in SubDomain mode), in place."""
+        self.B.interpolate_on_subdomain(accum.columns, domain_log_size, tw)
+        return accum.columns
 
     def logup_compositions(self, values_evals, inter_evals, trace_log, z, claimed, rcs, accum):
         self.B.logup_compositions(values_evals, [self.be.SecureColumnByCoords(it) for it in inter_evals], trace_log,
@@ -1308,6 +1356,13 @@ class GpuOps:
         if isinstance(alpha, DeviceFelt):
             return self.B.fold_line_device_alpha(col, alpha.data, tw)
         return self.B.fold_line(col, [np.asarray(alpha, np.uint32)], tw)
+
+    def fold_line_steps(self, col, alphas, tw):
+        """len(alphas) folds in one call (cs_fold_line_steps)."""
+        return self.B.fold_line(col, [np.asarray(a, np.uint32) for a in alphas], tw)
+
+    def pack_leaves(self, cols):
+        return self.B.pack_leaves_input(cols)
 
     fri_graphs = True  # replay the FRI layer loop as a CUDA graph per (stream, size, parameters)
 

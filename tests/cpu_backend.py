@@ -83,10 +83,16 @@ class CpuOps:
             claimed.append(tuple(int(x) for x in cs))
         return cols, claimed
 
-    def air_composition(self, air, columns_by_interaction, trace_log, params, rc, accum):
+    def air_composition(self, air, columns_by_interaction, trace_log, params, rc, accum, log_expansion=0):
         from oracle.air_eval import air_composition
         cols = {k: [c.v for c in v] for k, v in columns_by_interaction.items()}
-        accum.c = air_composition(air, cols, len(accum).bit_length() - 1, trace_log, params, rc, out=accum.c)
+        accum.c = air_composition(air, cols, len(accum).bit_length() - 1, trace_log, params, rc, out=accum.c,
+                                  log_expansion=log_expansion)
+
+    def interpolate_secure_on_subdomain(self, accum, domain_log_size, tw):
+        sub_log = len(accum).bit_length() - 1
+        sub_itw = O.extract_subdomain_twiddles(tw.itw, domain_log_size, sub_log)
+        return [Col(O.interpolate_on_subdomain(c, sub_itw, domain_log_size)) for c in accum.c]
 
     def logup_compositions(self, values_evals, inter_evals, trace_log, z, claimed, rcs, accum):
         for v, it, c, r in zip(values_evals, inter_evals, claimed, rcs):
@@ -201,3 +207,12 @@ class CpuOps:
     def fold_line(self, col, alpha, tw):
         n = len(col)
         return SCol(O.fold_line(col.c, O.line_domain_initial_index(n.bit_length() - 1), alpha))
+
+    def fold_line_steps(self, col, alphas, tw):
+        for a in alphas:
+            col = self.fold_line(col, a, tw)
+        return col
+
+    def pack_leaves(self, cols):
+        # pack_leaves_input: column coord + 4 offset holds coordinate coord of row 4 r + offset
+        return [Col(cols[coord].v[off::4]) for off in range(4) for coord in range(4)]

@@ -181,5 +181,96 @@ def test_component_arguments_are_checked():
         ap.FrameworkComponent(ap.TraceLocationAllocator(), lookup, 4)   # no z
     c = ap.FrameworkComponent(ap.TraceLocationAllocator(), lookup, 4, {"z": (1, 2, 3, 4)}, claimed_sum=(16, 0, 0, 0))
     assert c.params["shift"] == (1, 0, 0, 0)
-    with pytest.raises(NotImplementedError):
-        ap.CommitmentSchemeProver(CpuOps(), pr.PcsConfig(pr.FriParams(log_blowup_factor=2), 8), None)
+    with pytest.raises(ValueError):
+        ap.FrameworkComponent(ap.TraceLocationAllocator(), lookup, 4, {"z": (1, 2, 3, 4)}, constraint_log_degree=0)
+
+
+def test_evaluation_mode_is_inferred_like_the_reference():
+    # EvaluationMode::infer (crates/stwo/src/prover/air/accumulation.rs:42-62)
+    air = fw.compile_air("window", window_air)
+
+    def comps(*degrees):
+        alloc = ap.TraceLocationAllocator()
+        return [ap.FrameworkComponent(alloc, air, 4, constraint_log_degree=d) for d in degrees]
+    assert ap.evaluation_mode(comps(1, 1), 1) == 0
+    assert ap.evaluation_mode(comps(1, 1), 3) == 2
+    assert ap.evaluation_mode(comps(2), 1) is None        # degree above the blowup
+    assert ap.evaluation_mode(comps(1, 2), 2) is None     # expansions differ
+    assert ap.evaluation_mode(comps(2, 2), 2) == 0
+
+
+def blowup_proof(ops, log_n, log_blowup, degrees=(1, 1), fold_step=1, last_layer=0, check=True):
+    """The window AIR and a Wide-Fibonacci component of 2^log_n rows with the given constraint
+    log degrees, committed at log blowup log_blowup (as test_wide_fib_prove_with_larger_blowup,
+    crates/examples/src/wide_fibonacci/mod.rs:311-370). The trees are lifted to the composition
+    halves' domain, log_n + max degree - 1 + log_blowup (as poseidon_pcs_config)."""
+    fri = pr.FriParams(pow_bits=10, log_blowup_factor=log_blowup, log_last_layer_degree_bound=last_layer,
+                       n_queries=3, fold_step=fold_step)
+    lifting = log_n + max(degrees) - 1 + log_blowup
+    cfg = pr.PcsConfig(fri, trace_lifting_log_size=lifting)
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(ops, cfg, ops.twiddles(lifting + 1))
+    scheme.commit([], ch)
+    fib = O.wide_fib_trace(np.ones(1 << log_n, np.uint32), np.arange(1 << log_n, dtype=np.uint32), 5)
+    scheme.commit(ops.columns_from_host(window_trace(log_n, 9) + list(fib)), ch)
+    alloc = ap.TraceLocationAllocator()
+    comps = [ap.FrameworkComponent(alloc, fw.compile_air("window", window_air), log_n,
+                                   constraint_log_degree=degrees[0]),
+             ap.FrameworkComponent(alloc, fw.compile_air("wide_fib_5", fw.wide_fib_air, 5), log_n,
+                                   constraint_log_degree=degrees[1])]
+    proof = ap.prove(comps, ch, scheme, check=check)
+    return proof, comps, [[], [log_n] * 9]
+
+
+@pytest.mark.parametrize("log_n,log_blowup", [(4, 2), (5, 2), (6, 2), (7, 2), (5, 3), (4, 4)])
+def test_larger_blowup_prove_then_verify(log_n, log_blowup):
+    # log blowup b over constraints of log degree 1: SubDomain with log_expansion b - 1, the
+    # composition interpolated on the committed domain's subdomain
+    proof, comps, sizes = blowup_proof(CpuOps(), log_n, log_blowup)
+    verify_window(proof, comps, sizes)
+    bad = copy.deepcopy(proof)
+    bad.sampled_values[1][4][0] = tuple((v + 1) % O.P for v in bad.sampled_values[1][4][0])
+    with pytest.raises(VerificationError):
+        verify_window(bad, comps, sizes)
+
+
+@pytest.mark.parametrize("log_blowup,degrees", [(1, (2, 2)), (2, (1, 2)), (3, (2, 2))])
+def test_constraint_degree_two_fails_the_sanity_check_like_the_reference(log_blowup, degrees):
+    # "AIRs with constraint degree >= 2 are not supported yet in the lifted protocol"
+    # (crates/examples/src/poseidon/mod.rs:467): the trace is committed below the trees' height and
+    # lifted, the composition is not, so prove_ex's check compares values at different points
+    with pytest.raises(ConstraintsNotSatisfied):
+        blowup_proof(CpuOps(), 5, log_blowup, degrees)
+    proof, _, _ = blowup_proof(CpuOps(), 5, log_blowup, degrees, check=False)
+    assert not proof.constraints_satisfied
+
+
+@pytest.mark.parametrize("log_n", [4, 5, 6, 7, 8])
+def test_fri_fold_steps_prove_then_verify(log_n):
+    # fold_step 2 for 2^4 and 2^5 rows, else 3, as test_wide_fib_prove_with_blake_with_fri_jumps
+    # (crates/examples/src/wide_fibonacci/mod.rs:372-420): packed FRI leaves, a first layer of a
+    # circle fold and line folds, a shorter last step
+    k = 2 if log_n in (4, 5) else 3
+    proof, comps, sizes = blowup_proof(CpuOps(), log_n, 1, fold_step=k)
+    verify_window(proof, comps, sizes)
+    # the tree height is log_n + 1; after the first layer's k folds, layers of k folds down to the
+    # last layer's 2 values, the last step shorter
+    assert len(proof.fri_inner_layers) == -(-(log_n + 1 - k - 1) // k)
+    bad = copy.deepcopy(proof)
+    w = bad.fri_first_layer["fri_witness"]
+    w[0] = tuple((v + 1) % O.P for v in w[0])
+    with pytest.raises(VerificationError):
+        verify_window(bad, comps, sizes)
+
+
+@pytest.mark.parametrize("log_n,log_blowup,fold_step,last_layer", [(6, 2, 2, 1), (7, 1, 4, 2), (5, 3, 3, 0),
+                                                                     (8, 1, 2, 3)])
+def test_fri_parameters_combined_prove_then_verify(log_n, log_blowup, fold_step, last_layer):
+    # larger blowups, fold steps and last-layer degree bounds together
+    proof, comps, sizes = blowup_proof(CpuOps(), log_n, log_blowup, fold_step=fold_step, last_layer=last_layer)
+    assert len(proof.fri_last_layer_poly) == 1 << last_layer
+    verify_window(proof, comps, sizes)
+    bad = copy.deepcopy(proof)
+    bad.fri_last_layer_poly[-1] = tuple((v + 1) % O.P for v in bad.fri_last_layer_poly[-1])
+    with pytest.raises(VerificationError):
+        verify_window(bad, comps, sizes)

@@ -1,7 +1,8 @@
 """GPU parity of the generic prover: proofs of components written against the constraint evaluator,
 their constraints run as kernels compiled at run time, equal the oracle's prover (the mixed
 Wide-Fibonacci + LogUp trace) and the host prover on the oracle's operations (masks at several
-offsets, preprocessed columns, components of several sizes), byte for byte."""
+offsets, preprocessed columns, components of several sizes, larger blowups, FRI fold steps above
+one with packed leaves, last layers of higher degree), byte for byte."""
 import numpy as np
 import pytest
 
@@ -13,7 +14,7 @@ from oracle import oracle as O  # noqa: E402
 from proving_gb300 import air_prover as ap  # noqa: E402
 from proving_gb300 import framework as fw  # noqa: E402
 from proving_gb300 import prover as pr  # noqa: E402
-from test_air_prover_cpu import FRI, fib_and_lookups_generic, seq_air  # noqa: E402
+from test_air_prover_cpu import FRI, blowup_proof, fib_and_lookups_generic, seq_air  # noqa: E402
 from test_mask_offsets_cpu import window_air, window_trace  # noqa: E402
 from test_prove_cpu import fib_and_lookups_inputs  # noqa: E402
 
@@ -78,3 +79,12 @@ def _seq_proof(o, log_n):
 
 def test_preprocessed_column_proof_equals_host_prover_on_oracle_ops(ops):
     assert _seq_proof(ops, 10) == _seq_proof(CpuOps(), 10)
+
+
+@pytest.mark.parametrize("log_n,log_blowup,fold_step,last_layer", [(6, 2, 1, 0), (8, 1, 3, 0), (10, 2, 2, 1),
+                                                                     (12, 1, 4, 2), (9, 3, 2, 0)])
+def test_blowup_and_fold_steps_equal_host_prover_on_oracle_ops(ops, log_n, log_blowup, fold_step, last_layer):
+    kw = dict(fold_step=fold_step, last_layer=last_layer)
+    got, _, _ = blowup_proof(ops, log_n, log_blowup, **kw)
+    want, _, _ = blowup_proof(CpuOps(), log_n, log_blowup, **kw)
+    assert got.to_bytes() == want.to_bytes()
