@@ -23,7 +23,8 @@
  *    misuse; its Rust binding panics on a non-OK status to keep that contract.
  *  - All entry points are thread-safe. Process-wide state is limited to:
  *    the per-thread error message; the FFT pass-plan table (cs_fft_set_plan,
- *    guarded by a lock); per-device set-up flags (kernel shared-memory
+ *    guarded by a lock); the fold plan (cs_fold_set_plan, one atomic word);
+ *    per-device set-up flags (kernel shared-memory
  *    limits, the memory pool's release threshold; set once under a lock);
  *    the kernel launch counter; and the static slot array of
  *    cs_grind_blake2s_noalloc (shared by its calls, see there).
@@ -211,9 +212,15 @@ cs_status cs_fold_line(const uint32_t *const h_src[4], uint32_t log_size, const 
 /* FriOps::fold_line with n_alphas challenges (crates/stwo/src/prover/fri.rs:27-45):
    the evaluation folded n_alphas times (1 <= n_alphas <= log_size), fold j
    with h_alphas[4 j .. 4 j + 3] (host words), into 2^(log_size - n_alphas)
-   values in h_dst; only the last layer is written. Up to 10 folds per launch
-   on tiles staged in shared memory; uses stream-ordered device scratch between
-   launches. */
+   values in h_dst; only the last layer is written. Up to 12 folds per launch
+   in registers, warp shuffles and shared memory (16-byte aligned source and
+   twiddles), else up to 10 on tiles staged in shared memory; uses
+   stream-ordered device scratch between launches. cs_fold_set_plan sets how
+   many values (2^3 or 2^4, the default) a thread of the register launches
+   folds before the shuffles; it changes the launch shapes, not the results.
+   Process-wide, thread-safe. */
+cs_status cs_fold_set_plan(uint32_t log_values_per_thread);
+cs_status cs_fold_get_plan(uint32_t *log_values_per_thread);
 cs_status cs_fold_line_steps(const uint32_t *const h_src[4], uint32_t log_size, uint32_t n_alphas,
                              const uint32_t *h_alphas, uint32_t *const h_dst[4], const uint32_t *d_itwiddles,
                              uint32_t twiddle_log_size, cs_stream stream);

@@ -66,6 +66,8 @@ SIGNATURES = {
     "cs_poseidon_interaction": [vp, u32, vp, vp, vp, vp],
     "cs_poseidon_composition": [vp, vp, u32, u32, vp, vp, vp, vp, vp],
     "cs_int_peak_probe": [u32, u32, u32, vp, vp],
+    "cs_fold_set_plan": [u32],
+    "cs_fold_get_plan": [vp],
     "cs_fft_set_plan": [u32, u32, u32, vp, u32],
     "cs_fft_get_plan": [u32, u32, u32, vp, vp],
     "cs_fold_line_device_alpha": [vp, u32, vp, vp, vp, u32, vp],

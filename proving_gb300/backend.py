@@ -335,6 +335,17 @@ class CudaBackend:
 
     # FriOps -------------------------------------------------------------------
     @staticmethod
+    def set_fold_plan(log_values_per_thread: int) -> None:
+        """cs_fold_set_plan: 2^3 or 2^4 values per thread in the register fold launches."""
+        _lib.call("cs_fold_set_plan", log_values_per_thread)
+
+    @staticmethod
+    def get_fold_plan() -> int:
+        v = ctypes.c_uint32()
+        _lib.call("cs_fold_get_plan", ctypes.byref(v))
+        return v.value
+
+    @staticmethod
     def fold_line(values: SecureColumnByCoords, alphas, twiddles: TwiddleTree) -> SecureColumnByCoords:
         """fold_line on the line domain x(half_odds(log n)); alphas as in FriOps::fold_line: one
         fold per challenge, only the last layer returned."""

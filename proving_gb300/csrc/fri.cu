@@ -10,6 +10,7 @@
 // [1/y, -1/y, -1/x, 1/x][i & 3] of pair (i >> 2)
 // (circle_twiddles_from_line_twiddles, cpu/circle.rs:306-323).
 #include <algorithm>
+#include <atomic>
 
 #include <vector>
 
@@ -347,19 +348,24 @@ __global__ void pack_leaves_kernel(const Pack p, uint32_t n_rows) {
   }
 }
 
-// FriOps::fold_line with F <= 11 challenges per launch: every 2^F consecutive values of the layer
-// fold into one, with no shared-memory round trip until the last folds. A thread loads 8
-// consecutive values (two 16-byte words per coordinate) and folds them three times in registers
-// (its four, two and one pairs are its own); the 2^(F-3) threads of a group fold their results
-// over shuffles (lane l pairs with lane l + 2^k, up to five folds), and for F > 8 a group is a
-// whole block whose warps' results meet in shared memory for the rest (up to three). For F <= 8 a
-// block of up to 256 threads holds several groups. Every twiddle a thread needs is loaded before
-// the first fold, so the chain of folds waits on one round of loads. Fold j of the launch pairs
-// values (2i, 2i + 1) of its layer with the layer's inverse twiddle i and the challenge's product
-// table, as fold_line_tile_kernel does. Needs 16-byte aligned coordinates and twiddles, F >= 3,
-// and blockDim.x * gridDim.x = 2^(log_size - 3) with blockDim.x a multiple of 2^(F-3), equal to it
-// for F > 8.
-constexpr uint32_t kRegFoldMax = 11;
+// FriOps::fold_line with F <= LOG_V + 8 challenges per launch: every 2^F consecutive values of the
+// layer fold into one, with no shared-memory round trip until the last folds. A thread loads
+// V = 2^LOG_V consecutive values (LOG_V 3 or 4: two or four 16-byte words per coordinate, taken in
+// chunks of 8) and folds them LOG_V times in registers (its pairs are its own); the 2^(F-LOG_V)
+// threads of a group fold their results over shuffles (lane l pairs with lane l + 2^k, up to five
+// folds), and for F > LOG_V + 5 a group is a whole block whose warps' results meet in shared
+// memory for the rest (up to three). For smaller F a block of up to 256 threads holds several
+// groups. Every twiddle a thread needs is loaded before the first fold, so the chain of folds waits
+// on one round of loads. Fold j of the launch pairs values (2i, 2i + 1) of its layer with the
+// layer's inverse twiddle i and the challenge's product table, as fold_line_tile_kernel does.
+// Needs 16-byte aligned coordinates and twiddles, F >= LOG_V, and blockDim.x * gridDim.x =
+// 2^(log_size - LOG_V) with blockDim.x a multiple of 2^(F-LOG_V), equal to it for F > LOG_V + 5.
+// Sixteen values a thread issue a fifth fewer folds than eight for the same layer (the shuffle
+// folds, where every lane computes although half the results are read, cover fewer values) and
+// halve the threads, so the largest launches fit in one wave.
+constexpr uint32_t kRegFoldMax = 12;
+// log2 of the values a thread of fold_line_regs_kernel folds in registers, at most (cs_fold_set_plan)
+std::atomic<uint32_t> g_fold_log_values{4};
 constexpr uint32_t kRegFoldThreads = 256;
 struct RegFoldSteps {
   qm31_const alpha[kRegFoldMax];
@@ -396,52 +402,69 @@ __device__ __forceinline__ qm31 shfl_down_qm31(const qm31& v, uint32_t delta, ui
                    __shfl_down_sync(mask, v.b.a, delta), __shfl_down_sync(mask, v.b.b, delta));
 }
 
-__global__ void __launch_bounds__(kRegFoldThreads, 5) fold_line_regs_kernel(const Coords c, uint32_t log_size,
-                                                                         uint32_t n_folds,
-                                                                         const uint32_t* __restrict__ itw,
-                                                                         uint32_t twiddle_log_size,
-                                                                         const RegFoldSteps steps) {
+template <uint32_t LOG_V>
+__global__ void __launch_bounds__(kRegFoldThreads, LOG_V == 3 ? 5 : 4) fold_line_regs_kernel(
+    const Coords c, uint32_t log_size, uint32_t n_folds, const uint32_t* __restrict__ itw,
+    uint32_t twiddle_log_size, const RegFoldSteps steps) {
+  constexpr uint32_t V = 1u << LOG_V;
+  constexpr uint32_t kChunks = V / 8;
   __shared__ uint32_t part[4][8];
   const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const size_t tw_len = (size_t)1 << twiddle_log_size;
   // twiddles of fold j of this launch: the inverse-twiddle layer of the line domain of log (log_size - j)
   const auto layer = [&](uint32_t j) { return itw + (tw_len - ((size_t)1 << (log_size - j))); };
-  const size_t g3 = (size_t)blockIdx.x * blockDim.x + t;  // this thread's index in layer 3
-  const size_t base = 8 * g3;                              // and its first value in layer 0
-  const uint32_t warp_folds = min(5u, n_folds - 3);
-  const uint32_t smem_folds = n_folds > 8 ? n_folds - 8 : 0;
-  // every twiddle up front: layers 0..2 (the register folds), 3..7 (the shuffle folds) and, for warp
-  // 0 of a block of F > 8, 8..10 (the shared-memory folds; lane l takes layer-8 index
-  // blockIdx.x * 2^(F-8) + l, lanes past the block's warps repeat lane 0)
-  const uint4 t0 = __ldg(reinterpret_cast<const uint4*>(layer(0) + 4 * g3));
-  const uint2 t1 = __ldg(reinterpret_cast<const uint2*>(layer(1) + 2 * g3));
-  const uint32_t t2 = __ldg(layer(2) + g3);
+  const size_t g = (size_t)blockIdx.x * blockDim.x + t;  // this thread's index in layer LOG_V
+  const size_t base = V * g;                             // and its first value in layer 0
+  const uint32_t warp_folds = min(5u, n_folds - LOG_V);
+  const uint32_t smem_folds = n_folds > LOG_V + 5 ? n_folds - LOG_V - 5 : 0;
+  // every twiddle up front: chunk h's register folds (layer 0: four, layer 1: two, layer 2: one,
+  // at chunk index kChunks g + h), for V = 16 the fold of the two chunks (layer 3), the shuffle
+  // folds (layers LOG_V..LOG_V+4) and, for warp 0 of a block of F > LOG_V + 5, the shared-memory
+  // folds (lane l takes index blockIdx.x * 2^smem_folds + l of layer LOG_V + 5, lanes past the
+  // block's warps repeat lane 0)
+  uint4 t0[kChunks];
+  uint2 t1[kChunks];
+  uint32_t t2[kChunks];
+#pragma unroll
+  for (uint32_t h = 0; h < kChunks; h++) {
+    const size_t gc = kChunks * g + h;
+    t0[h] = __ldg(reinterpret_cast<const uint4*>(layer(0) + 4 * gc));
+    t1[h] = __ldg(reinterpret_cast<const uint2*>(layer(1) + 2 * gc));
+    t2[h] = __ldg(layer(2) + gc);
+  }
+  const uint32_t t3 = LOG_V == 4 ? __ldg(layer(3) + g) : 0;
   uint32_t tw_w[5], tw_s[3];
 #pragma unroll
-  for (uint32_t k = 0; k < 5; k++) tw_w[k] = k < warp_folds ? __ldg(layer(3 + k) + (g3 >> (k + 1))) : 0;
+  for (uint32_t k = 0; k < 5; k++) tw_w[k] = k < warp_folds ? __ldg(layer(LOG_V + k) + (g >> (k + 1))) : 0;
   const uint32_t n_warps = blockDim.x >> 5;
-  const size_t g8 = smem_folds ? ((size_t)blockIdx.x << smem_folds) + (lane < n_warps ? lane : 0) : 0;
+  const size_t gs = smem_folds ? ((size_t)blockIdx.x << smem_folds) + (lane < n_warps ? lane : 0) : 0;
 #pragma unroll
   for (uint32_t k = 0; k < 3; k++)
-    tw_s[k] = (warp == 0 && k < smem_folds) ? __ldg(layer(8 + k) + (g8 >> (k + 1))) : 0;
-  uint32_t w[4][8];
+    tw_s[k] = (warp == 0 && k < smem_folds) ? __ldg(layer(LOG_V + 5 + k) + (gs >> (k + 1))) : 0;
+  qm31 h_out[kChunks];
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const uint4 lo = __ldg(reinterpret_cast<const uint4*>(c.in[k] + base));
-    const uint4 hi = __ldg(reinterpret_cast<const uint4*>(c.in[k] + base) + 1);
-    w[k][0] = lo.x, w[k][1] = lo.y, w[k][2] = lo.z, w[k][3] = lo.w;
-    w[k][4] = hi.x, w[k][5] = hi.y, w[k][6] = hi.z, w[k][7] = hi.w;
+  for (uint32_t h = 0; h < kChunks; h++) {
+    uint32_t w[4][8];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const uint4 lo = __ldg(reinterpret_cast<const uint4*>(c.in[k] + base + 8 * h));
+      const uint4 hi = __ldg(reinterpret_cast<const uint4*>(c.in[k] + base + 8 * h) + 1);
+      w[k][0] = lo.x, w[k][1] = lo.y, w[k][2] = lo.z, w[k][3] = lo.w;
+      w[k][4] = hi.x, w[k][5] = hi.y, w[k][6] = hi.z, w[k][7] = hi.w;
+    }
+    qm31 v[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = qm31_make(w[0][i], w[1][i], w[2][i], w[3][i]);
+    v[0] = fold_pair(v[0], v[1], t0[h].x, steps.alpha[0]);
+    v[1] = fold_pair(v[2], v[3], t0[h].y, steps.alpha[0]);
+    v[2] = fold_pair(v[4], v[5], t0[h].z, steps.alpha[0]);
+    v[3] = fold_pair(v[6], v[7], t0[h].w, steps.alpha[0]);
+    v[0] = fold_pair(v[0], v[1], t1[h].x, steps.alpha[1]);
+    v[1] = fold_pair(v[2], v[3], t1[h].y, steps.alpha[1]);
+    h_out[h] = fold_pair(v[0], v[1], t2[h], steps.alpha[2]);
   }
-  qm31 v[8];
-#pragma unroll
-  for (int i = 0; i < 8; i++) v[i] = qm31_make(w[0][i], w[1][i], w[2][i], w[3][i]);
-  v[0] = fold_pair(v[0], v[1], t0.x, steps.alpha[0]);
-  v[1] = fold_pair(v[2], v[3], t0.y, steps.alpha[0]);
-  v[2] = fold_pair(v[4], v[5], t0.z, steps.alpha[0]);
-  v[3] = fold_pair(v[6], v[7], t0.w, steps.alpha[0]);
-  v[0] = fold_pair(v[0], v[1], t1.x, steps.alpha[1]);
-  v[1] = fold_pair(v[2], v[3], t1.y, steps.alpha[1]);
-  qm31 x = fold_pair(v[0], v[1], t2, steps.alpha[2]);
+  qm31 x = h_out[0];
+  if constexpr (LOG_V == 4) x = fold_pair(h_out[0], h_out[kChunks - 1], t3, steps.alpha[3]);
   // folds over a group's lanes: lane l keeps the fold of l and l + 2^k when its index in the group is
   // a multiple of 2^(k+1); the other lanes compute values nobody reads
   const uint32_t mask = blockDim.x >= 32 ? 0xffffffffu : ((1u << blockDim.x) - 1);
@@ -449,12 +472,12 @@ __global__ void __launch_bounds__(kRegFoldThreads, 5) fold_line_regs_kernel(cons
   for (uint32_t k = 0; k < 5; k++) {
     if (k < warp_folds) {  // the same for the whole block
       const qm31 y = shfl_down_qm31(x, 1u << k, mask);
-      x = fold_pair(x, y, tw_w[k], steps.alpha[3 + k]);
+      x = fold_pair(x, y, tw_w[k], steps.alpha[LOG_V + k]);
     }
   }
-  if (smem_folds == 0) {  // groups of 2^(F-3) lanes; the first lane of each writes its value
-    if ((t & ((1u << (n_folds - 3)) - 1)) == 0) {
-      const size_t o = g3 >> (n_folds - 3);
+  if (smem_folds == 0) {  // groups of 2^(F-LOG_V) lanes; the first lane of each writes its value
+    if ((t & ((1u << (n_folds - LOG_V)) - 1)) == 0) {
+      const size_t o = g >> (n_folds - LOG_V);
       c.out[0][o] = x.a.a;
       c.out[1][o] = x.a.b;
       c.out[2][o] = x.b.a;
@@ -462,7 +485,7 @@ __global__ void __launch_bounds__(kRegFoldThreads, 5) fold_line_regs_kernel(cons
     }
     return;
   }
-  // one group per block: the warps' results (layer-8 indices blockIdx.x * 2^(F-8) + warp) meet
+  // one group per block: the warps' results (layer LOG_V + 5 indices blockIdx.x * 2^smem_folds + warp) meet
   if (lane == 0) part[0][warp] = x.a.a, part[1][warp] = x.a.b, part[2][warp] = x.b.a, part[3][warp] = x.b.b;
   __syncthreads();
   if (warp != 0) return;
@@ -472,7 +495,7 @@ __global__ void __launch_bounds__(kRegFoldThreads, 5) fold_line_regs_kernel(cons
   for (uint32_t k = 0; k < 3; k++) {
     if (k < smem_folds) {
       const qm31 y = shfl_down_qm31(x, 1u << k, 0xffffffffu);
-      x = fold_pair(x, y, tw_s[k], steps.alpha[8 + k]);
+      x = fold_pair(x, y, tw_s[k], steps.alpha[LOG_V + 5 + k]);
     }
   }
   if (lane == 0) {
@@ -715,6 +738,19 @@ extern "C" cs_status cs_fold_line(const uint32_t* const h_src[4], uint32_t log_s
                         d_itwiddles, twiddle_log_size, stream);
 }
 
+extern "C" cs_status cs_fold_set_plan(uint32_t log_values_per_thread) {
+  CS_CHECK_ARG(log_values_per_thread == 3 || log_values_per_thread == 4,
+               "fold_set_plan: %u (log2 of the values a thread folds: 3 or 4)", log_values_per_thread);
+  cs::g_fold_log_values.store(log_values_per_thread, std::memory_order_relaxed);
+  return CS_OK;
+}
+
+extern "C" cs_status cs_fold_get_plan(uint32_t* log_values_per_thread) {
+  CS_CHECK_ARG(log_values_per_thread != nullptr, "fold_get_plan: null pointer");
+  *log_values_per_thread = cs::g_fold_log_values.load(std::memory_order_relaxed);
+  return CS_OK;
+}
+
 extern "C" cs_status cs_fold_line_steps(const uint32_t* const h_src[4], uint32_t log_size, uint32_t n_alphas,
                                         const uint32_t* h_alphas, uint32_t* const h_dst[4],
                                         const uint32_t* d_itwiddles, uint32_t twiddle_log_size, cs_stream stream) {
@@ -738,14 +774,17 @@ extern "C" cs_status cs_fold_line_steps(const uint32_t* const h_src[4], uint32_t
   struct Pass {
     uint32_t folds;
     bool regs;
+    uint32_t log_v;  // values per thread of the register kernel, log 3 or 4
   };
   std::vector<Pass> passes;
   size_t scratch_words = 0;
+  const uint32_t log_v_max = g_fold_log_values.load(std::memory_order_relaxed);
   for (uint32_t cur = log_size, done = 0; done < n_alphas;) {
     const uint32_t left = n_alphas - done;
     Pass ps;
     ps.regs = aligned && cur >= 3 && left >= 3;
-    ps.folds = ps.regs ? std::min(std::min(left, kRegFoldMax), cur) : std::min(left, std::min(cur, kFoldTileLog));
+    ps.log_v = (log_v_max == 4 && cur >= 4 && left >= 4) ? 4 : 3;
+    ps.folds = ps.regs ? std::min(std::min(left, ps.log_v + 8), cur) : std::min(left, std::min(cur, kFoldTileLog));
     passes.push_back(ps);
     done += ps.folds;
     cur -= ps.folds;
@@ -769,12 +808,17 @@ extern "C" cs_status cs_fold_line_steps(const uint32_t* const h_src[4], uint32_t
         const uint32_t* a = h_alphas + 4 * (size_t)(done + j);
         steps.alpha[j] = qm31_const_of(qm31_make(a[0] % P, a[1] % P, a[2] % P, a[3] % P));
       }
-      // 2^(cur_log - 3) threads in groups of 2^(folds - 3): for more than 8 folds one group per block,
-      // otherwise blocks of up to kRegFoldThreads
-      const uint32_t group = 1u << (folds - 3);
-      const uint32_t threads = folds > 8 ? group : std::max(group, std::min(kRegFoldThreads, 1u << (cur_log - 3)));
-      fold_line_regs_kernel<<<(1u << (cur_log - 3)) / threads, threads, 0, st>>>(c, cur_log, folds, d_itwiddles,
-                                                                               twiddle_log_size, steps);
+      // 2^(cur_log - LOG_V) threads in groups of 2^(folds - LOG_V): for more than LOG_V + 5 folds one
+      // group per block, otherwise blocks of up to kRegFoldThreads
+      const uint32_t lv = passes[pi].log_v;
+      const uint32_t group = 1u << (folds - lv);
+      const uint32_t threads =
+          folds > lv + 5 ? group : std::max(group, std::min(kRegFoldThreads, 1u << (cur_log - lv)));
+      const uint32_t blocks = (1u << (cur_log - lv)) / threads;
+      if (lv == 4)
+        fold_line_regs_kernel<4><<<blocks, threads, 0, st>>>(c, cur_log, folds, d_itwiddles, twiddle_log_size, steps);
+      else
+        fold_line_regs_kernel<3><<<blocks, threads, 0, st>>>(c, cur_log, folds, d_itwiddles, twiddle_log_size, steps);
     } else {
       FoldSteps steps;
       for (uint32_t j = 0; j < folds; j++) {

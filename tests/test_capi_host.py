@@ -293,3 +293,17 @@ def test_logup_generator_checks_arguments_on_host(lib):
     claimed = (ctypes.c_uint32 * 4)()
     assert _status(lib, "cs_logup_finalize_last", out, 0, claimed, null) == INVALID
     assert _status(lib, "cs_logup_finalize_last", out, 29, claimed, null) == INVALID
+
+
+def test_fold_plan_is_checked_and_kept(lib):
+    INVALID = 1
+    v = ctypes.c_uint32(0)
+    assert _status(lib, "cs_fold_get_plan", ctypes.byref(v)) == 0
+    old = v.value
+    assert old in (3, 4)
+    assert _status(lib, "cs_fold_set_plan", 5) == INVALID
+    assert _status(lib, "cs_fold_set_plan", 2) == INVALID
+    assert _status(lib, "cs_fold_get_plan", ctypes.c_void_p(0)) == INVALID
+    for want in (3, 4, old):
+        assert _status(lib, "cs_fold_set_plan", want) == 0
+        assert _status(lib, "cs_fold_get_plan", ctypes.byref(v)) == 0 and v.value == want

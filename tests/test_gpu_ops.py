@@ -255,12 +255,21 @@ def test_fri_fold_chain_22(B):
     assert len(g) == 1
 
 
-@pytest.mark.parametrize("log_n,k", [(1, 1), (3, 3), (4, 2), (5, 5), (8, 8), (9, 4), (10, 10), (11, 11), (12, 3),
-                                     (13, 6), (15, 1), (16, 7), (20, 13), (21, 10), (21, 20), (21, 21)])
-def test_fold_line_with_several_alphas(B, log_n, k):
-    # FriOps::fold_line with k challenges (launches of up to 11 folds in registers, shuffles and
-    # shared memory, or of up to 10 folds through shared-memory tiles) equals k single folds of the
-    # oracle; only the last layer is returned.
+@pytest.fixture(params=[3, 4], ids=["8_per_thread", "16_per_thread"])
+def fold_plan(B, request):
+    old = B.get_fold_plan()
+    B.set_fold_plan(request.param)
+    yield request.param
+    B.set_fold_plan(old)
+
+
+@pytest.mark.parametrize("log_n,k", [(1, 1), (3, 3), (4, 2), (4, 4), (5, 5), (8, 8), (9, 4), (9, 9), (10, 10),
+                                     (11, 11), (12, 3), (12, 12), (13, 6), (13, 12), (15, 1), (16, 7), (17, 15),
+                                     (20, 13), (21, 10), (21, 20), (21, 21)])
+def test_fold_line_with_several_alphas(B, fold_plan, log_n, k):
+    # FriOps::fold_line with k challenges (launches of up to 11 or 12 folds in registers, shuffles
+    # and shared memory, with 8 or 16 values a thread, or of up to 10 folds through shared-memory
+    # tiles) equals k single folds of the oracle; only the last layer is returned.
     from proving_gb300.backend import SecureColumnByCoords
     tree = _tree(B, log_n + 1)
     coords = qm31_column(300 + log_n, log_n)
