@@ -274,3 +274,33 @@ def test_fri_parameters_combined_prove_then_verify(log_n, log_blowup, fold_step,
     bad.fri_last_layer_poly[-1] = tuple((v + 1) % O.P for v in bad.fri_last_layer_poly[-1])
     with pytest.raises(VerificationError):
         verify_window(bad, comps, sizes)
+
+
+def poseidon_generic(ops, log_n):
+    """prove_poseidon's flow (crates/examples/src/poseidon/mod.rs:320-379) through the generic API:
+    the AIR recorded by the evaluator, LOG_EXPAND 2 over a log blowup of 1 (ExtendToEvalDomain),
+    the lifted configuration whose sanity check the reference itself fails (check=False)."""
+    from proving_gb300 import poseidon as ps
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = ps.poseidon_pcs_config(log_n + 3, fp)
+    tw = ops.twiddles(log_n + ps.LOG_EXPAND + 1)
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(ops, cfg, tw)
+    scheme.commit([], ch)
+    trace = ops.poseidon_trace(log_n)
+    scheme.commit(trace, ch)
+    lookup = list(ch.draw_secure_felt()) + list(ch.draw_secure_felt())
+    inter, claimed = ops.poseidon_interaction(trace, lookup)
+    claimed = tuple(int(x) for x in claimed)
+    scheme.commit(inter, ch)
+    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), fw.poseidon_air_recorded(), log_n,
+                                 fw.poseidon_params(lookup, claimed, log_n), constraint_log_degree=ps.LOG_EXPAND)
+    proof = ap.prove([comp], ch, scheme, check=False)
+    want = ps.prove_poseidon(ops, log_n, cfg, pr.Blake2sChannel(), tw, check=False, generic=True)
+    return proof, want
+
+
+def test_poseidon_through_the_generic_api_equals_prove_poseidon():
+    proof, want = poseidon_generic(CpuOps(), 4)
+    assert not proof.constraints_satisfied and not want.constraints_satisfied
+    assert proof.to_bytes() == want.to_bytes()

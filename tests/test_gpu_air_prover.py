@@ -14,7 +14,7 @@ from oracle import oracle as O  # noqa: E402
 from proving_gb300 import air_prover as ap  # noqa: E402
 from proving_gb300 import framework as fw  # noqa: E402
 from proving_gb300 import prover as pr  # noqa: E402
-from test_air_prover_cpu import FRI, blowup_proof, fib_and_lookups_generic, seq_air  # noqa: E402
+from test_air_prover_cpu import FRI, blowup_proof, fib_and_lookups_generic, poseidon_generic, seq_air  # noqa: E402
 from test_mask_offsets_cpu import window_air, window_trace  # noqa: E402
 from test_prove_cpu import fib_and_lookups_inputs  # noqa: E402
 
@@ -88,3 +88,11 @@ def test_blowup_and_fold_steps_equal_host_prover_on_oracle_ops(ops, log_n, log_b
     got, _, _ = blowup_proof(ops, log_n, log_blowup, **kw)
     want, _, _ = blowup_proof(CpuOps(), log_n, log_blowup, **kw)
     assert got.to_bytes() == want.to_bytes()
+
+
+@pytest.mark.parametrize("log_n", [4, 7])
+def test_poseidon_through_the_generic_api_equals_oracle(ops, log_n):
+    # Poseidon2's 1,144 constraints as the generated kernel, extended to CanonicCoset(n + 2): the
+    # generic API's words equal prove_poseidon's and the oracle prover's
+    proof, want = poseidon_generic(ops, log_n)
+    assert proof.to_bytes() == want.to_bytes() == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
