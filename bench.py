@@ -850,7 +850,7 @@ def run_gpu(args):
                             "unit": "GB/s", "frac": ff(leaf_gbs / hbm), "traffic": traffic,
                             "algorithmic_bytes_per_launch": leaf_bytes,
                             "note": "Blake2s leaf hashing is integer-pipe bound; see int_pipe"},
-        "fold_roofline": {"bound": "hbm", "kernels": "fold_circle_wide_kernel + fold_line_regs_kernel (3 launches: 2^22 -> 2^21, 11 folds, 10 folds)",
+        "fold_roofline": {"bound": "hbm", "kernels": "fold_circle_wide_kernel + fold_line_regs_kernel (3 launches: 2^22 -> 2^21, 12 folds, 9 folds; 16 values a thread)",
                           "achieved": ff(fold_bytes / (stage_ms["fri_folds"] / 1e3) / 1e9), "peak": hbm,
                           "unit": "GB/s", "frac": ff(fold_bytes / (stage_ms["fri_folds"] / 1e3) / 1e9 / hbm),
                           "algorithmic_bytes": fold_bytes,
