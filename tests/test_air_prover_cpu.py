@@ -304,3 +304,24 @@ def test_poseidon_through_the_generic_api_equals_prove_poseidon():
     proof, want = poseidon_generic(CpuOps(), 4)
     assert not proof.constraints_satisfied and not want.constraints_satisfied
     assert proof.to_bytes() == want.to_bytes()
+
+
+def test_larger_blowup_with_components_of_several_sizes():
+    # SubDomain with log_expansion 1 for a 2^4-row and a 2^6-row component: each accumulates on its
+    # own committed domain's subdomain, the two lifted together before the composition is
+    # interpolated on the largest one's subdomain
+    fri = pr.FriParams(pow_bits=10, log_blowup_factor=2, log_last_layer_degree_bound=0, n_queries=3, fold_step=1)
+    log_w, log_f = 4, 6
+    lifting = log_f + 2
+    ops = CpuOps()
+    cfg = pr.PcsConfig(fri, trace_lifting_log_size=lifting)
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(ops, cfg, ops.twiddles(lifting + 1))
+    scheme.commit([], ch)
+    fib = O.wide_fib_trace(np.ones(1 << log_f, np.uint32), np.arange(1 << log_f, dtype=np.uint32), 6)
+    scheme.commit(ops.columns_from_host(window_trace(log_w, 9) + list(fib)), ch)
+    alloc = ap.TraceLocationAllocator()
+    comps = [ap.FrameworkComponent(alloc, fw.compile_air("window", window_air), log_w),
+             ap.FrameworkComponent(alloc, fw.compile_air("wide_fib_6", fw.wide_fib_air, 6), log_f)]
+    proof = ap.prove(comps, ch, scheme)
+    verify_window(proof, comps, [[], [log_w] * 4 + [log_f] * 6])
