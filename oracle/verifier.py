@@ -281,7 +281,8 @@ def _air_at_point(air, mask, params):
     return [ev(c) for c in air.constraints]
 
 
-def verify_components(proof, ch, components, column_log_sizes, preprocessed_columns=()):
+def verify_components(proof, ch, components, column_log_sizes, preprocessed_columns=(),
+                      include_all_preprocessed_columns=False):
     """verify (crates/stwo/src/core/verifier.rs:19-119) for components written against the
     constraint evaluator, after the caller has replayed the trees' commitments and its own draws on
     ch (as the reference's verifier-side example code does). components: (air, log_size, params)
@@ -327,6 +328,8 @@ def verify_components(proof, ch, components, column_log_sizes, preprocessed_colu
             pidx.append(pre.index(name))
             points[0][pidx[-1]] = [oods]
         places.append((place, pidx))
+    if include_all_preprocessed_columns:
+        points[0] = [[oods] for _ in column_log_sizes[0]]
     sv = proof.sampled_values
     if (len(sv) != n_trees + 1 or any(len(sv[t]) != len(points[t]) for t in range(n_trees)) or len(sv[-1]) != 8
             or any(len(sv[t][c]) != len(points[t][c]) for t in range(n_trees) for c in range(len(points[t])))):

@@ -237,11 +237,14 @@ class CommitmentSchemeProver:
         return out
 
 
-def prove(components, channel: pr.Blake2sChannel, scheme: CommitmentSchemeProver, check: bool = True):
-    """prove_ex without the preprocessed columns the components do not read
-    (include_all_preprocessed_columns = false). Raises ConstraintsNotSatisfied when the composition
-    polynomial's OODS value differs from the components' constraints at the point (check=False
-    returns the proof with constraints_satisfied set instead)."""
+def prove(components, channel: pr.Blake2sChannel, scheme: CommitmentSchemeProver, check: bool = True,
+          include_all_preprocessed_columns: bool = False):
+    """prove_ex: with include_all_preprocessed_columns every preprocessed column is sampled at the
+    OODS point, else only those the components read (Components::mask_points,
+    crates/stwo/src/core/air/components.rs:27-51; prove() passes false). Raises
+    ConstraintsNotSatisfied when the composition polynomial's OODS value differs from the
+    components' constraints at the point (check=False returns the proof with constraints_satisfied
+    set instead)."""
     ops, cfg, tw = scheme.ops, scheme.config, scheme.twiddles
     fp = cfg.fri_params
     b = fp.log_blowup_factor
@@ -288,6 +291,8 @@ def prove(components, channel: pr.Blake2sChannel, scheme: CommitmentSchemeProver
     for comp in components:
         for (t, c), pts in comp.mask_points(oods, mldb).items():
             sample_points[t][c] = pts
+    if include_all_preprocessed_columns and scheme.trees:
+        sample_points[0] = [[oods] for _ in scheme.trees[0].evals]
     sample_points.append([[oods]] * 8)
     columns = [t.evals for t in scheme.trees] + [comp_evals]
     sampled = pr.sample_values(ops, columns, sample_points, L)

@@ -171,6 +171,30 @@ def test_preprocessed_columns_prove_then_verify():
         ap.FrameworkComponent(ap.TraceLocationAllocator(preprocessed_columns=["other"]), air, log_n)
 
 
+def test_preprocessed_columns_nobody_reads():
+    # a second preprocessed column no component reads: sampled only with
+    # include_all_preprocessed_columns (prove_ex's flag), decommitted either way
+    log_n = 4
+    ops = CpuOps()
+    cfg = pr.PcsConfig(FRI, trace_lifting_log_size=log_n + 1)
+    air = fw.compile_air("window", window_air)
+    extra = np.arange(1 << log_n, dtype=np.uint32)
+    for include_all in (False, True):
+        ch = pr.Blake2sChannel()
+        scheme = ap.CommitmentSchemeProver(ops, cfg, ops.twiddles(log_n + 1))
+        scheme.commit(ops.columns_from_host([extra]), ch)
+        scheme.commit(ops.columns_from_host(window_trace(log_n, 9)), ch)
+        comp = ap.FrameworkComponent(ap.TraceLocationAllocator(["unused"]), air, log_n)
+        proof = ap.prove([comp], ch, scheme, include_all_preprocessed_columns=include_all)
+        assert [len(c) for c in proof.sampled_values[0]] == [1 if include_all else 0]
+        assert len(proof.queried_values[0]) == 1
+        v = O.Blake2sChannel()
+        v.mix_root(proof.commitments[0])
+        v.mix_root(proof.commitments[1])
+        verify_components(proof, v, [(air, log_n, {})], [[log_n], [log_n] * 4], preprocessed_columns=["unused"],
+                          include_all_preprocessed_columns=include_all)
+
+
 def test_component_arguments_are_checked():
     with pytest.raises(ValueError):
         fw.compile_air("p", lambda e: e.next_interaction_mask(0))
