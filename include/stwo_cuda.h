@@ -569,6 +569,44 @@ cs_status cs_rtc_air_composition_subdomain(void *handle, const uint32_t *const *
                                            const uint32_t *h_params, uint32_t eval_log, uint32_t trace_log,
                                            uint32_t log_expansion, uint32_t *const h_accum[4], cs_stream stream);
 cs_status cs_rtc_release(void *handle);
+/* The column-table size, constraint count and parameter count a kernel was compiled for. */
+cs_status cs_rtc_kernel_shape(void *handle, uint32_t *n_cols, uint32_t *n_constraints, uint32_t *n_params);
+
+/* prove_ex for components written against the constraint evaluator
+   (proving_gb300/air_prover.py's FrameworkComponent), their constraints through
+   kernels compiled with cs_rtc_compile_air: the empty preprocessed tree, one
+   trace tree of every component's columns in component order (d_trace,
+   2^log_size words each on the trace domain, bit-reversed; interpolated in place,
+   so consumed), no interaction tree, constraints of log degree 1 (evaluated on
+   CanonicCoset(log_size + 1)), log_blowup_factor 1, fold_step 1. A component's
+   columns are sampled at the OODS point plus each of its mask offsets in steps of
+   CanonicCoset(lifting_log_size - 1) (component.rs:202-214). Its constraints at
+   the point, for the sanity check (prover/mod.rs:121-132), come from `program`:
+   n_nodes nodes of 5 words (op, a0..a3) in topological order, op 0 = the sampled
+   value of local column a0 at its a1-th offset, 1 = the M31 constant a0, 2 =
+   parameter a0, 3 = from_partial_evals of nodes a0..a3, 4 = -a0, 5 = a0 + a1,
+   6 = a0 - a1, 7 = a0 * a1; constraint k is node constraints[k]. mask_cols[i]
+   is the local column the kernel's mask i reads. params: the FRI parameters
+   and twiddles (n_components, n_cols and log_sizes unused); lifting_log_size =
+   the largest log_size + 1. */
+typedef struct {
+  void *kernel;                  /* cs_rtc_compile_air handle */
+  uint32_t log_size;             /* 2^log_size trace rows */
+  uint32_t n_cols;               /* trace columns the component takes */
+  const int32_t *offsets;        /* every column's mask offsets, concatenated */
+  const uint32_t *offsets_start; /* n_cols + 1 starts into offsets */
+  uint32_t n_masks;              /* the kernel's column table */
+  const uint32_t *mask_cols;
+  const uint32_t *program;       /* 5 words per node */
+  uint32_t n_nodes;
+  const uint32_t *constraints;
+  uint32_t n_constraints;
+  const uint32_t *params;        /* 4 words per parameter */
+  uint32_t n_params;
+} cs_air_component;
+cs_status cs_prove_air(const cs_wide_fib_proof_params *params, const cs_air_component *components,
+                       uint32_t n_components, uint32_t *const *d_trace, uint64_t *h_words, size_t capacity,
+                       size_t *n_words, cs_stream stream);
 
 /* ------------------------------------------------------- AIR: Poseidon2 */
 

@@ -90,6 +90,8 @@ SIGNATURES = {
     "cs_rtc_air_composition": [vp, vp, vp, vp, u32, u32, vp, vp],
     "cs_rtc_air_composition_subdomain": [vp, vp, vp, vp, u32, u32, u32, vp, vp],
     "cs_rtc_release": [vp],
+    "cs_rtc_kernel_shape": [vp, vp, vp, vp],
+    "cs_prove_air": [vp, vp, u32, vp, vp, ctypes.c_size_t, vp, vp],
     "cs_prove_wide_fib": [vp, vp, vp, ctypes.c_size_t, vp, vp],
     "cs_prove_fib_and_lookups": [vp, vp, u32, vp, vp, vp, vp, ctypes.c_size_t, vp, vp],
     "cs_prove_poseidon": [u32, vp, vp, ctypes.c_size_t, vp, vp],

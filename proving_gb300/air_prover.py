@@ -349,5 +349,31 @@ def prove(components, channel: pr.Blake2sChannel, scheme: CommitmentSchemeProver
     return proof
 
 
+def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = False) -> bytes:
+    """The same proof in native code (cs_prove_air) for components that read trace columns only:
+    the empty preprocessed tree, `trace` (device columns on their trace domains, every component's
+    in allocation order; interpolated in place, so consumed) as the one trace tree, then prove()
+    from a fresh channel. Constraint log degree 1, log blowup 1, fold_step 1. Returns the proof
+    bytes, equal to prove()'s for the same flow."""
+    from .backend import CudaBackend
+    from .framework import CompiledAir
+    fp = config.fri_params
+    if fp.fold_step != 1 or fp.log_blowup_factor != 1:
+        raise NotImplementedError("the native prover: log blowup 1, fold_step 1")
+    specs, col = [], 0
+    for c in components:
+        if c.constraint_log_degree != 1:
+            raise NotImplementedError("the native prover: constraint log degree 1")
+        nodes, cons, offs, mask_cols = c.air.point_program()
+        if c.trace_locations.get(1, (col, col))[0] != col:
+            raise ValueError("components' trace columns must follow one another in component order")
+        col += len(offs)
+        params = [c.params[p] for p in c.air.params]
+        specs.append((CompiledAir.get(c.air).handle, c.log_size, offs, mask_cols, nodes, cons, params))
+    return CudaBackend.prove_air_native(specs, trace, config.trace_lifting_log_size,
+                                        (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound,
+                                         fp.n_queries), twiddles, plain)
+
+
 __all__ = ["TraceLocationAllocator", "FrameworkComponent", "CommitmentSchemeProver", "prove",
-           "constraints_at_point", "point_at_offset", "evaluation_mode"]
+           "constraints_at_point", "point_at_offset", "evaluation_mode", "prove_native"]

@@ -111,6 +111,15 @@ class _WideFibProofParams(ctypes.Structure):
 PROVE_PLAIN = 1  # CS_PROVE_PLAIN
 
 
+class _AirComponent(ctypes.Structure):
+    """cs_air_component (include/stwo_cuda.h)."""
+    _fields_ = [("kernel", ctypes.c_void_p), ("log_size", ctypes.c_uint32), ("n_cols", ctypes.c_uint32),
+                ("offsets", ctypes.c_void_p), ("offsets_start", ctypes.c_void_p), ("n_masks", ctypes.c_uint32),
+                ("mask_cols", ctypes.c_void_p), ("program", ctypes.c_void_p), ("n_nodes", ctypes.c_uint32),
+                ("constraints", ctypes.c_void_p), ("n_constraints", ctypes.c_uint32), ("params", ctypes.c_void_p),
+                ("n_params", ctypes.c_uint32)]
+
+
 class SecureColumnByCoords:
     """SecureColumnByCoords (crates/stwo/src/prover/secure_column.rs:13-15): 4 coordinate columns."""
 
@@ -583,6 +592,41 @@ class CudaBackend:
         del keep
         return (words[:n.value].astype("<u8").tobytes(),
                 [tuple(int(x) for x in row) for row in claimed[:len(lookup_values)]])
+
+    @staticmethod
+    def prove_air_native(components, trace, lifting_log_size: int, fri_params, twiddles: TwiddleTree,
+                         plain=False) -> bytes:
+        """cs_prove_air: trace-only components written against the constraint evaluator, proved in
+        native code. components: (kernel handle, log size, per-column offsets, per-mask columns,
+        node program (n, 5), constraint nodes, parameters as QM31 words) each; trace: every
+        component's columns in order (BaseColumns on their trace domains, interpolated in place).
+        Returns the proof bytes."""
+        keep = []
+
+        def arr(values, dtype):
+            a = np.ascontiguousarray(np.asarray(values, dtype).reshape(-1))
+            keep.append(a)
+            return a.ctypes.data if a.size else None
+        comps = (_AirComponent * len(components))()
+        for k, (handle, log_size, offs, mask_cols, nodes, cons, params) in enumerate(components):
+            starts = np.cumsum([0] + [len(o) for o in offs])
+            c = comps[k]
+            c.kernel = handle.value if isinstance(handle, ctypes.c_void_p) else handle
+            c.log_size, c.n_cols = log_size, len(offs)
+            c.offsets = arr([x for o in offs for x in o], np.int32)
+            c.offsets_start = arr(starts, np.uint32)
+            c.n_masks, c.mask_cols = len(mask_cols), arr(mask_cols, np.uint32)
+            c.program, c.n_nodes = arr(nodes, np.uint32), len(nodes)
+            c.constraints, c.n_constraints = arr(cons, np.uint32), len(cons)
+            c.params, c.n_params = arr(params, np.uint32), len(params)
+        params, keep2 = CudaBackend._proof_params([], [], lifting_log_size, fri_params, twiddles, plain)
+        n = ctypes.c_size_t(0)
+        cap = 1 << 22
+        words = _words_buffer(cap)
+        _lib.call("cs_prove_air", ctypes.byref(params), comps, len(components), _ptr_table([c.data for c in trace]),
+                  words.ctypes.data, cap, ctypes.byref(n), _stream())
+        del keep, keep2
+        return words[:n.value].astype("<u8").tobytes()
 
     @staticmethod
     def prove_poseidon_native(log_n_rows: int, fri_params, twiddles: TwiddleTree, plain=False) -> bytes:

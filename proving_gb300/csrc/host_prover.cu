@@ -554,6 +554,8 @@ struct Air {
   virtual ~Air() = default;
   // the trace tree's columns (evaluations on their blown-up domains), in tree order
   virtual cs_status trace(Prover& P, std::vector<Col>& cols) = 0;
+  // the mask offsets of every trace column, in tree order (left empty: every column at the point)
+  virtual void trace_offsets(std::vector<std::vector<int32_t>>&) const {}
   virtual bool has_interaction() const { return false; }
   virtual bool mix_claimed() const { return false; }
   // the interaction tree's columns, whether each is also sampled at the previous row, and the
@@ -588,14 +590,25 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   ch.mix_root(pre_root);
   struct TreeCols {
     std::vector<Col> cols;
-    std::vector<bool> two;  // also sampled at the previous row
+    std::vector<bool> two;                      // also sampled at the previous row
+    std::vector<std::vector<int32_t>> offs;     // the offsets each column is sampled at
     Tree tree;
+  };
+  // a column sampled at the row, or at the previous row and the row
+  const auto offsets_of = [](const std::vector<bool>& two) {
+    std::vector<std::vector<int32_t>> o;
+    for (bool t : two) o.push_back(t ? std::vector<int32_t>{-1, 0} : std::vector<int32_t>{0});
+    return o;
   };
   std::vector<TreeCols> trees;
   // --- trace tree (TreeBuilder::extend_evals + commit)
   trees.emplace_back();
   HP_TRY(air.trace(P, trees.back().cols));
   trees.back().two.assign(trees.back().cols.size(), false);
+  air.trace_offsets(trees.back().offs);
+  if (trees.back().offs.empty()) trees.back().offs = offsets_of(trees.back().two);
+  CS_CHECK_ARG(trees.back().offs.size() == trees.back().cols.size(), "prove: %zu offset lists for %zu columns",
+               trees.back().offs.size(), trees.back().cols.size());
   const auto commit_tree = [&](TreeCols& t) -> cs_status {
     std::vector<uint32_t*> c;
     std::vector<uint32_t> l;
@@ -614,6 +627,7 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
     const qm31 alpha = ch.draw_secure_felt();
     trees.emplace_back();
     HP_TRY(air.interaction(P, z, alpha, trees.back().cols, trees.back().two, claimed));
+    trees.back().offs = offsets_of(trees.back().two);
     HP_TRY(commit_tree(trees.back()));
     if (air.mix_claimed()) ch.mix_felts(claimed);
     ch.mix_root(trees.back().tree.root);
@@ -643,6 +657,7 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   trees.emplace_back();
   for (uint32_t* c : comp_cols) trees.back().cols.push_back({c, comp_eval_log});
   trees.back().two.assign(8, false);
+  trees.back().offs = offsets_of(trees.back().two);
   HP_TRY(commit_tree(trees.back()));
   ch.mix_root(trees.back().tree.root);
 
@@ -653,17 +668,23 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   const qpoint oods = random_point(ch.draw_secure_felt());
   const cpoint g = index_to_point(1u << (31 - mldb));
   const qpoint prev_pt = add_m31_point(oods, {g.x, m31_neg(g.y)});
+  // the point `o` trace steps from the OODS point: o G_mldb added (G^-1 is G's conjugate)
+  const auto point_at = [&](int32_t o) -> qpoint {
+    if (o == 0) return oods;
+    if (o == -1) return prev_pt;
+    return add_m31_point(oods, index_to_point(((uint32_t)o << (31 - mldb)) & 0x7fffffffu));
+  };
 
   // --- sampled values (pcs/mod.rs:175-214): one weight column per (size, point); values read once
   struct Sample {
     size_t tree, col, slot;
   };
-  std::vector<std::pair<std::pair<uint32_t, int>, std::vector<Sample>>> groups;  // (log, 0 oods / 1 prev)
+  std::vector<std::pair<std::pair<uint32_t, int32_t>, std::vector<Sample>>> groups;  // (log, offset)
   for (size_t t = 0; t < trees.size(); t++)
     for (size_t c = 0; c < trees[t].cols.size(); c++) {
-      std::vector<int> pts = trees[t].two[c] ? std::vector<int>{1, 0} : std::vector<int>{0};
+      const std::vector<int32_t>& pts = trees[t].offs[c];
       for (size_t k = 0; k < pts.size(); k++) {
-        const std::pair<uint32_t, int> key{trees[t].cols[c].log, pts[k]};
+        const std::pair<uint32_t, int32_t> key{trees[t].cols[c].log, pts[k]};
         auto it = std::find_if(groups.begin(), groups.end(), [&](auto& g) { return g.first == key; });
         if (it == groups.end()) {
           groups.push_back({key, {}});
@@ -678,7 +699,7 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   if (!d_samples) return A.status;
   size_t row = 0;
   for (auto& [key, members] : groups) {
-    qpoint pt = key.second ? prev_pt : oods;
+    qpoint pt = point_at(key.second);
     for (uint32_t d = key.first; d < L; d++) pt = q_double(pt);
     const uint32_t ls = key.first;
     uint32_t* w = A.alloc(4ull << ls);
@@ -704,7 +725,7 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   std::vector<std::vector<std::vector<qm31>>> sampled(trees.size() + 1);  // [0]: the preprocessed tree
   for (size_t t = 0; t < trees.size(); t++) {
     sampled[t + 1].resize(trees[t].cols.size());
-    for (size_t c = 0; c < trees[t].cols.size(); c++) sampled[t + 1][c].resize(trees[t].two[c] ? 2 : 1);
+    for (size_t c = 0; c < trees[t].cols.size(); c++) sampled[t + 1][c].resize(trees[t].offs[c].size());
   }
   row = 0;
   for (auto& [key, members] : groups)
@@ -733,14 +754,13 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
     for (size_t c = 0; c < trees[t].cols.size(); c++) {
       const Col& col = trees[t].cols[c];
       const auto& v = sampled[t + 1][c];
-      if (trees[t].two[c]) {
-        const qpoint shifted = add_m31_point(oods, index_to_point(1u << (31 - (L - col.log))));
+      const std::vector<int32_t>& o = trees[t].offs[c];
+      if (o.size() == 2) {
+        // the periodicity sample: the second point shifted by the column's period, its value
+        const qpoint shifted = add_m31_point(point_at(o[1]), index_to_point(1u << (31 - (L - col.log))));
         entries.push_back({col.log, col.p, shifted, v[1]});
-        entries.push_back({col.log, col.p, prev_pt, v[0]});
-        entries.push_back({col.log, col.p, oods, v[1]});
-      } else {
-        entries.push_back({col.log, col.p, oods, v[0]});
       }
+      for (size_t k = 0; k < o.size(); k++) entries.push_back({col.log, col.p, point_at(o[k]), v[k]});
     }
   const std::vector<qm31> qp = powers(quotient_coeff, (uint32_t)entries.size());
   struct Acc {
@@ -1240,6 +1260,102 @@ struct FibLookupAir : Air {
   }
 };
 
+// Components written against the constraint evaluator (FrameworkComponent, crates/constraint-framework/
+// src/component.rs), their constraint quotients from kernels compiled at run time
+// (cs_rtc_air_composition) and their constraints at the OODS point from a node program (the
+// PointEvaluator's role, crates/constraint-framework/src/point.rs:12-64). Trace-only: every column
+// in the trace tree, constraints of log degree 1.
+struct RtcComponent {
+  void* kernel = nullptr;
+  uint32_t log_size = 0, col0 = 0, n_cols = 0;
+  std::vector<std::vector<int32_t>> offs;  // per local column
+  std::vector<uint32_t> mask_cols, program, constraints, params;
+};
+
+struct RtcAir : Air {
+  std::vector<RtcComponent> comps;
+  uint32_t* const* d_trace = nullptr;
+  std::vector<uint32_t*> evals;  // every trace column on its blown-up domain
+
+  cs_status trace(Prover& P, std::vector<Col>& cols) override {
+    std::vector<const uint32_t*> src;
+    std::vector<uint32_t*> coeffs;
+    std::vector<uint32_t> tlogs;
+    for (const RtcComponent& k : comps)
+      for (uint32_t j = 0; j < k.n_cols; j++) {
+        src.push_back(d_trace[k.col0 + j]);
+        coeffs.push_back(d_trace[k.col0 + j]);
+        tlogs.push_back(k.log_size);
+      }
+    HP_TRY(P.interpolate_mixed(src, coeffs, tlogs));
+    HP_TRY(P.evaluate_mixed(coeffs, tlogs, evals));
+    for (size_t j = 0; j < evals.size(); j++) cols.push_back({evals[j], tlogs[j] + P.cfg.b});
+    return CS_OK;
+  }
+  void trace_offsets(std::vector<std::vector<int32_t>>& offs) const override {
+    for (const RtcComponent& k : comps) offs.insert(offs.end(), k.offs.begin(), k.offs.end());
+  }
+  uint32_t n_constraints() const override {
+    uint32_t n = 0;
+    for (const RtcComponent& k : comps) n += (uint32_t)k.constraints.size();
+    return n;
+  }
+  cs_status composition(Prover& P, const std::vector<qm31>& pw,
+                        std::map<uint32_t, std::vector<uint32_t*>>& acc) override {
+    const uint32_t total = n_constraints();
+    uint32_t start = 0;
+    for (const RtcComponent& k : comps) {  // each component takes the last powers, reversed
+      const uint32_t n = (uint32_t)k.constraints.size(), el = k.log_size + 1;
+      std::vector<uint32_t> rc(4 * (size_t)n);
+      for (uint32_t j = 0; j < n; j++) {
+        const qm31 x = pw[total - start - 1 - j];
+        rc[4 * j] = x.a.a;
+        rc[4 * j + 1] = x.a.b;
+        rc[4 * j + 2] = x.b.a;
+        rc[4 * j + 3] = x.b.b;
+      }
+      std::vector<const uint32_t*> table;
+      for (uint32_t c : k.mask_cols) table.push_back(evals[k.col0 + c]);
+      HP_TRY(cs_rtc_air_composition(k.kernel, table.data(), rc.data(), k.params.empty() ? nullptr : k.params.data(),
+                                    el, k.log_size, P.acc_for(acc, el).data(), P.st));
+      start += n;
+    }
+    return CS_OK;
+  }
+  bool at_point(const qpoint& oods, uint32_t mldb, const qm31& random_coeff,
+                const std::vector<std::vector<std::vector<qm31>>>& sampled, qm31& expected) override {
+    qm31 x = oods.x;
+    for (uint32_t i = 0; i + 1 < mldb; i++) x = q_double_x(x);
+    qm31 acc = qm31_make(0, 0, 0, 0);
+    std::vector<qm31> v;
+    for (const RtcComponent& k : comps) {
+      const size_t n_nodes = k.program.size() / 5;
+      v.assign(n_nodes, qm31_make(0, 0, 0, 0));
+      for (size_t i = 0; i < n_nodes; i++) {
+        const uint32_t* nd = &k.program[5 * i];
+        switch (nd[0]) {
+          case 0: v[i] = sampled[1][k.col0 + nd[1]][nd[2]]; break;
+          case 1: v[i] = qm31_make(nd[1] % P, 0, 0, 0); break;
+          case 2: v[i] = qm31_make(k.params[4 * nd[1]], k.params[4 * nd[1] + 1], k.params[4 * nd[1] + 2],
+                                   k.params[4 * nd[1] + 3]); break;
+          case 3: {
+            const qm31 parts[4] = {v[nd[1]], v[nd[2]], v[nd[3]], v[nd[4]]};
+            v[i] = from_partial_evals(parts);
+            break;
+          }
+          case 4: v[i] = qm31_sub(qm31_make(0, 0, 0, 0), v[nd[1]]); break;
+          case 5: v[i] = qm31_add(v[nd[1]], v[nd[2]]); break;
+          case 6: v[i] = qm31_sub(v[nd[1]], v[nd[2]]); break;
+          default: v[i] = qm31_mul(v[nd[1]], v[nd[2]]); break;
+        }
+      }
+      for (uint32_t c : k.constraints) acc = qm31_add(qm31_mul(acc, random_coeff), v[c]);
+    }
+    expected = qm31_mul(acc, qm31_inv(x));
+    return true;
+  }
+};
+
 // The Poseidon2 AIR (crates/examples/src/poseidon/mod.rs:320-379): 1264 trace columns generated on the
 // device, 32 interaction columns (the last four also sampled at the previous row), constraint quotients
 // on CanonicCoset(n + 2) (ExtendToEvalDomain). No sanity check: the reference's own prove of this AIR
@@ -1412,6 +1528,74 @@ extern "C" cs_status cs_prove_fib_and_lookups(const cs_wide_fib_proof_params* pa
     h_claimed[4 * k + 2] = claimed[k].b.a;
     h_claimed[4 * k + 3] = claimed[k].b.b;
   }
+  return finish(words, h_words, capacity, n_words);
+}
+
+extern "C" cs_status cs_prove_air(const cs_wide_fib_proof_params* params, const cs_air_component* components,
+                                  uint32_t n_components, uint32_t* const* d_trace, uint64_t* h_words, size_t capacity,
+                                  size_t* n_words, cs_stream stream) {
+  CS_CHECK_ARG(params != nullptr && components != nullptr && d_trace != nullptr && n_words != nullptr,
+               "prove_air: null pointer");
+  CS_CHECK_ARG(n_components >= 1, "prove_air: no components");
+  hp::RtcAir air;
+  air.d_trace = d_trace;
+  uint32_t max_log = 0, col0 = 0;
+  for (uint32_t k = 0; k < n_components; k++) {
+    const cs_air_component& c = components[k];
+    CS_CHECK_ARG(c.kernel != nullptr && c.log_size >= 1 && c.log_size <= 27 && c.n_cols >= 1,
+                 "prove_air: component %u: kernel, 2^%u rows, %u columns", k, c.log_size, c.n_cols);
+    CS_CHECK_ARG(c.offsets_start != nullptr && (c.offsets != nullptr || c.offsets_start[c.n_cols] == 0),
+                 "prove_air: component %u: null offsets", k);
+    CS_CHECK_ARG(c.n_nodes == 0 || c.program != nullptr, "prove_air: component %u: null program", k);
+    CS_CHECK_ARG(c.n_constraints == 0 || c.constraints != nullptr, "prove_air: component %u: null constraints", k);
+    CS_CHECK_ARG(c.n_masks == 0 || c.mask_cols != nullptr, "prove_air: component %u: null mask table", k);
+    CS_CHECK_ARG(c.n_params == 0 || c.params != nullptr, "prove_air: component %u: null parameters", k);
+    uint32_t kc = 0, kn = 0, kp = 0;
+    const cs_status shape = cs_rtc_kernel_shape(c.kernel, &kc, &kn, &kp);
+    if (shape != CS_OK) return shape;
+    CS_CHECK_ARG(kc == c.n_masks && kn == c.n_constraints && kp == c.n_params,
+                 "prove_air: component %u: the kernel has %u masks, %u constraints, %u parameters", k, kc, kn, kp);
+    hp::RtcComponent rc;
+    rc.kernel = c.kernel;
+    rc.log_size = c.log_size;
+    rc.col0 = col0;
+    rc.n_cols = c.n_cols;
+    for (uint32_t j = 0; j < c.n_cols; j++) {
+      CS_CHECK_ARG(c.offsets_start[j] <= c.offsets_start[j + 1], "prove_air: component %u: offsets out of order", k);
+      rc.offs.emplace_back(c.offsets + c.offsets_start[j], c.offsets + c.offsets_start[j + 1]);
+      for (int32_t o : rc.offs.back())
+        CS_CHECK_ARG(o > -(1 << 20) && o < (1 << 20), "prove_air: component %u: offset %d", k, o);
+    }
+    rc.mask_cols.assign(c.mask_cols, c.mask_cols + c.n_masks);
+    for (uint32_t m : rc.mask_cols) CS_CHECK_ARG(m < c.n_cols, "prove_air: component %u: mask column %u", k, m);
+    rc.program.assign(c.program, c.program + 5 * (size_t)c.n_nodes);
+    // every operand names an earlier node, every mask a column and one of its offsets
+    for (uint32_t i = 0; i < c.n_nodes; i++) {
+      const uint32_t* nd = &rc.program[5 * (size_t)i];
+      CS_CHECK_ARG(nd[0] <= 7, "prove_air: component %u: node %u: op %u", k, i, nd[0]);
+      const uint32_t n_in = nd[0] == 3 ? 4 : nd[0] == 4 ? 1 : nd[0] >= 5 ? 2 : 0;
+      for (uint32_t a = 0; a < n_in; a++)
+        CS_CHECK_ARG(nd[1 + a] < i, "prove_air: component %u: node %u reads node %u", k, i, nd[1 + a]);
+      if (nd[0] == 0)
+        CS_CHECK_ARG(nd[1] < c.n_cols && nd[2] < rc.offs[nd[1]].size(),
+                     "prove_air: component %u: node %u: column %u offset %u", k, i, nd[1], nd[2]);
+      if (nd[0] == 2) CS_CHECK_ARG(nd[1] < c.n_params, "prove_air: component %u: node %u: parameter %u", k, i, nd[1]);
+    }
+    rc.constraints.assign(c.constraints, c.constraints + c.n_constraints);
+    for (uint32_t x : rc.constraints) CS_CHECK_ARG(x < c.n_nodes, "prove_air: component %u: constraint node %u", k, x);
+    rc.params.assign(c.params, c.params + 4 * (size_t)c.n_params);
+    for (uint32_t j = 0; j < c.n_cols; j++)
+      CS_CHECK_ARG(d_trace[col0 + j] != nullptr, "prove_air: column %u is null", col0 + j);
+    max_log = std::max(max_log, c.log_size);
+    col0 += c.n_cols;
+    air.comps.push_back(std::move(rc));
+  }
+  const cs_status cs = check_common(*params, max_log);
+  if (cs != CS_OK) return cs;
+  std::vector<uint64_t>& words = proof_words();
+  std::vector<qm31> claimed;
+  const cs_status s = hp::prove(config_of(*params), air, words, claimed, to_stream(stream));
+  if (s != CS_OK) return s;
   return finish(words, h_words, capacity, n_words);
 }
 

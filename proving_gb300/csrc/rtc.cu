@@ -145,6 +145,16 @@ extern "C" cs_status cs_rtc_compile_air(const char* source, uint32_t n_headers, 
   return CS_OK;
 }
 
+extern "C" cs_status cs_rtc_kernel_shape(void* handle, uint32_t* n_cols, uint32_t* n_constraints, uint32_t* n_params) {
+  CS_CHECK_ARG(handle != nullptr && n_cols != nullptr && n_constraints != nullptr && n_params != nullptr,
+               "rtc_kernel_shape: null pointer");
+  const RtcKernel* k = static_cast<const RtcKernel*>(handle);
+  *n_cols = k->n_cols;
+  *n_constraints = k->n_constraints;
+  *n_params = k->n_params;
+  return CS_OK;
+}
+
 extern "C" cs_status cs_rtc_release(void* handle) {
   if (handle == nullptr) return CS_OK;
   RtcKernel* k = static_cast<RtcKernel*>(handle);

@@ -245,6 +245,46 @@ class Air:
     def n_constraints(self) -> int:
         return len(self.constraints)
 
+    def point_program(self):
+        """The constraints at a point as the node program of cs_prove_air, for an AIR that reads only
+        trace columns (interaction 1): nodes of 5 words (op, a0..a3) in topological order; op 0 is
+        the sampled value of column a0 at its a1-th mask offset, 1 the constant a0, 2 parameter a0,
+        3 from_partial_evals of nodes a0..a3, 4 -a0, 5 a0 + a1, 6 a0 - a1, 7 a0 * a1. Returns
+        (nodes (n, 5) uint32, each constraint's node, each column's offsets, each mask's column)."""
+        if set(self.mask_offsets) - {1} or self.preprocessed:
+            raise NotImplementedError("a node program for AIRs that read trace columns only")
+        offs = [list(o) for o in self.mask_offsets.get(1, [])]
+        ids, prog = {}, []
+        codes = {"neg": 4, "add": 5, "sub": 6, "mul": 7}
+        for root in self.constraints:
+            stack = [root]
+            while stack:
+                x = stack[-1]
+                if x.key in ids:
+                    stack.pop()
+                    continue
+                todo = [a for a in x.args if isinstance(a, Expr) and a.key not in ids]
+                if todo:
+                    stack.extend(todo)
+                    continue
+                stack.pop()
+                if x.op == "mask":
+                    _, col, off = x.args
+                    row = [0, col, offs[col].index(off), 0, 0]
+                elif x.op == "const":
+                    row = [1, x.args[0] % P, 0, 0, 0]
+                elif x.op == "param":
+                    row = [2, self.params.index(x.args[0]), 0, 0, 0]
+                elif x.op == "secure":
+                    row = [3] + [ids[a.key] for a in x.args]
+                else:
+                    kids = [ids[a.key] for a in x.args]
+                    row = [codes[x.op]] + kids + [0] * (4 - len(kids))
+                ids[x.key] = len(prog)
+                prog.append(row)
+        nodes = np.asarray(prog, np.uint32).reshape(-1, 5)
+        return nodes, [ids[c.key] for c in self.constraints], offs, [m.column for m in self.masks]
+
     def mask_columns(self, columns_by_interaction) -> list:
         """The device columns of the kernel's column table, in mask order: columns_by_interaction
         maps an interaction to its list of columns (evaluation-domain BaseColumns)."""

@@ -349,3 +349,41 @@ def test_larger_blowup_with_components_of_several_sizes():
              ap.FrameworkComponent(alloc, fw.compile_air("wide_fib_6", fw.wide_fib_air, 6), log_f)]
     proof = ap.prove(comps, ch, scheme)
     verify_window(proof, comps, [[], [log_w] * 4 + [log_f] * 6])
+
+
+def _run_program(nodes, cons, offs, mask, params):
+    """The node program of cs_prove_air read back in Python (the semantics of include/stwo_cuda.h)."""
+    v = []
+    for op, a0, a1, a2, a3 in np.asarray(nodes, np.int64).tolist():
+        if op == 0:
+            v.append(tuple(mask[(1, a0, offs[a0][a1])]))
+        elif op == 1:
+            v.append(pr.qm(a0))
+        elif op == 2:
+            v.append(tuple(params[a0]))
+        elif op == 3:
+            v.append(pr.from_partial_evals([v[a0], v[a1], v[a2], v[a3]]))
+        elif op == 4:
+            v.append(pr.qm_sub(pr.qm(0), v[a0]))
+        else:
+            v.append({5: pr.qm_add, 6: pr.qm_sub, 7: pr.qm_mul}[op](v[a0], v[a1]))
+    return [v[c] for c in cons]
+
+
+@pytest.mark.parametrize("make", [lambda: fw.compile_air("window", window_air),
+                                  lambda: fw.compile_air("wide_fib_7", fw.wide_fib_air, 7)])
+def test_point_program_equals_the_point_evaluation(make):
+    air = make()
+    nodes, cons, offs, mask_cols = air.point_program()
+    assert len(cons) == air.n_constraints and len(mask_cols) == len(air.masks)
+    assert all(offs[m.column][0] is not None and m.offset in offs[m.column] for m in air.masks)
+    rng = np.random.default_rng(5)
+    mask = {(1, c, o): tuple(int(x) for x in rng.integers(0, O.P, 4)) for c, os in enumerate(offs) for o in os}
+    assert _run_program(nodes, cons, offs, mask, []) == ap.constraints_at_point(air, mask, {})
+
+
+def test_point_program_needs_a_trace_only_air():
+    with pytest.raises(NotImplementedError):
+        fw.compile_air("single_lookup", fw.single_lookup_air).point_program()
+    with pytest.raises(NotImplementedError):
+        fw.compile_air("seq", seq_air).point_program()

@@ -307,3 +307,19 @@ def test_fold_plan_is_checked_and_kept(lib):
     for want in (3, 4, old):
         assert _status(lib, "cs_fold_set_plan", want) == 0
         assert _status(lib, "cs_fold_get_plan", ctypes.byref(v)) == 0 and v.value == want
+
+
+def test_prove_air_checks_arguments_on_host(lib):
+    # cs_prove_air: null tables, no components and a component without a kernel are rejected before
+    # any device work
+    INVALID = 1
+    null = ctypes.c_void_p(0)
+    from proving_gb300.backend import _AirComponent, _WideFibProofParams
+    params = _WideFibProofParams()
+    comps = (_AirComponent * 1)()
+    trace = (ctypes.c_void_p * 1)(1 << 20)
+    n = ctypes.c_size_t(0)
+    assert _status(lib, "cs_prove_air", null, comps, 1, trace, null, 0, ctypes.byref(n), null) == INVALID
+    assert _status(lib, "cs_prove_air", ctypes.byref(params), comps, 0, trace, null, 0, ctypes.byref(n), null) == INVALID
+    assert _status(lib, "cs_prove_air", ctypes.byref(params), comps, 1, trace, null, 0, ctypes.byref(n), null) == INVALID
+    assert b"kernel" in lib.cs_last_error()

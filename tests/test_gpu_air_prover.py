@@ -96,3 +96,43 @@ def test_poseidon_through_the_generic_api_equals_oracle(ops, log_n):
     # generic API's words equal prove_poseidon's and the oracle prover's
     proof, want = poseidon_generic(ops, log_n)
     assert proof.to_bytes() == want.to_bytes() == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
+
+
+def _native_against_python(o, specs, plain=False):
+    """specs: (air, log size, host columns) per component, in trace order. Returns (native bytes,
+    bytes of prove() for the same flow)."""
+    lifting = max(n for _, n, _ in specs) + 1
+    cfg = pr.PcsConfig(FRI, trace_lifting_log_size=lifting)
+    tw = o.twiddles(lifting + 1)
+    host = [c for _, _, cols in specs for c in cols]
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(o, cfg, tw)
+    scheme.commit([], ch)
+    scheme.commit(o.columns_from_host(host), ch)
+    alloc = ap.TraceLocationAllocator()
+    comps = [ap.FrameworkComponent(alloc, air, n) for air, n, _ in specs]
+    want = ap.prove(comps, ch, scheme).to_bytes()
+    got = ap.prove_native(comps, o.columns_from_host(host), cfg, tw, plain=plain)
+    return got, want
+
+
+def _fib(log_n, n_cols):
+    return list(O.wide_fib_trace(np.ones(1 << log_n, np.uint32), np.arange(1 << log_n, dtype=np.uint32), n_cols))
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_native_generic_prover_equals_the_python_generic_prover(ops, plain):
+    # masks at -3..2 and components of three sizes through cs_prove_air: the words of air_prover.prove
+    window = fw.compile_air("window", window_air)
+    fib = fw.compile_air("wide_fib_3", fw.wide_fib_air, 3)
+    specs = [(window, 9, window_trace(9, 1)), (fib, 5, _fib(5, 3)), (window, 12, window_trace(12, 2))]
+    got, want = _native_against_python(ops, specs, plain)
+    assert got == want
+
+
+def test_native_generic_prover_single_component_equals_oracle(ops):
+    # one Wide-Fibonacci component through cs_prove_air: the oracle prover's words
+    fib = fw.compile_air("wide_fib_8", fw.wide_fib_air, 8)
+    trace = _fib(10, 8)
+    got, want = _native_against_python(ops, [(fib, 10, trace)])
+    assert got == want == O.prove_fib_and_lookups((10, 1, 0, 3, 1), [trace], [10])[0]
