@@ -392,6 +392,41 @@ def wide_fib_prove_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: in
     return lat
 
 
+def wide_fib_generic_native_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: int = 100):
+    """The same Wide-Fibonacci proves through the native generic prover (cs_prove_air via
+    air_prover.prove_native: the NVRTC kernel of wide_fib_air, the constraints at the OODS point from
+    its node program). The first proof is checked against the restated prover's bytes. Returns
+    wall-clock latencies in ms."""
+    from proving_gb300 import air_prover as ap
+    from proving_gb300 import framework as fw
+    from proving_gb300 import prover as pr
+    from proving_gb300.backend import BaseColumn, CudaBackend
+    from proving_gb300.synthetic import m31_column
+    ops = pr.GpuOps()
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=log_n + 1)
+    tw = ops.twiddles(log_n + 2)
+    air = fw.compile_air(f"wide_fib_{n_cols}", fw.wide_fib_air, n_cols)
+    fw.CompiledAir.get(air)
+    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n)
+    lat = []
+    for k in range(n_proofs + 2):
+        a = BaseColumn.from_cpu(m31_column(100 + k, log_n))
+        b = BaseColumn.from_cpu(m31_column(200 + k, log_n))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        trace = CudaBackend.wide_fib_trace(a, b, n_cols)
+        words = ap.prove_native([comp], trace, cfg, tw)
+        torch.cuda.synchronize()
+        if k >= 2:
+            lat.append((time.perf_counter() - t0) * 1e3)
+        if k == 0:
+            want = pr.prove_wide_fib(ops, CudaBackend.wide_fib_trace(a, b, n_cols), log_n, cfg, pr.Blake2sChannel(), tw)
+            if words != want.to_bytes():
+                raise RuntimeError("native generic prover proof differs from the restated prover's")
+    return lat
+
+
 def wide_fib_generic_latency(torch, n_proofs: int = 8, log_n: int = 14, n_cols: int = 100):
     """The same Wide-Fibonacci proves through the generic prover API (proving_gb300.air_prover: the
     AIR recorded by the constraint evaluator, its composition kernel compiled with NVRTC once,
@@ -834,6 +869,7 @@ def run_gpu(args):
     with collector_paused():
         wf_lat = wide_fib_prove_latency(torch) if not args.skip_prove else []
         wf_generic = wide_fib_generic_latency(torch) if not args.skip_prove else []
+        wf_generic_native = wide_fib_generic_native_latency(torch) if not args.skip_prove else []
         wf_native = wide_fib_prove_native(torch) if not args.skip_prove else []
         wf_plain = wide_fib_prove_native(torch, plain=True) if not args.skip_prove else []
     bvp = batched_vs_plain(torch, cs) if not args.skip_plain else None
@@ -923,7 +959,13 @@ def run_gpu(args):
                                         "p50_ms": ff(float(np.percentile(wf_generic, 50))),
                                         "p99_ms": ff(float(np.percentile(wf_generic, 99))),
                                         "note": "air_prover over the NVRTC kernel of wide_fib_air; "
-                                                "bytes checked against the restated prover"}} if wf_lat else None),
+                                                "bytes checked against the restated prover"},
+                            "generic_native": {"proofs_per_s": ff(1e3 / statistics.median(wf_generic_native)),
+                                               "p50_ms": ff(float(np.percentile(wf_generic_native, 50))),
+                                               "p99_ms": ff(float(np.percentile(wf_generic_native, 99))),
+                                               "note": "cs_prove_air (air_prover.prove_native) over the same "
+                                                       "kernel; bytes checked against the restated prover"}}
+                           if wf_lat else None),
         "batched_vs_plain": bvp,
         "serving": serving_res,
         "poseidon_prove": poseidon_res,

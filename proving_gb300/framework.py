@@ -250,7 +250,11 @@ class Air:
         trace columns (interaction 1): nodes of 5 words (op, a0..a3) in topological order; op 0 is
         the sampled value of column a0 at its a1-th mask offset, 1 the constant a0, 2 parameter a0,
         3 from_partial_evals of nodes a0..a3, 4 -a0, 5 a0 + a1, 6 a0 - a1, 7 a0 * a1. Returns
-        (nodes (n, 5) uint32, each constraint's node, each column's offsets, each mask's column)."""
+        (nodes (n, 5) uint32, each constraint's node, each column's offsets, each mask's column);
+        computed once per Air."""
+        cached = self.__dict__.get("_point_program")
+        if cached is not None:
+            return cached
         if set(self.mask_offsets) - {1} or self.preprocessed:
             raise NotImplementedError("a node program for AIRs that read trace columns only")
         offs = [list(o) for o in self.mask_offsets.get(1, [])]
@@ -283,7 +287,9 @@ class Air:
                 ids[x.key] = len(prog)
                 prog.append(row)
         nodes = np.asarray(prog, np.uint32).reshape(-1, 5)
-        return nodes, [ids[c.key] for c in self.constraints], offs, [m.column for m in self.masks]
+        out = (nodes, [ids[c.key] for c in self.constraints], offs, [m.column for m in self.masks])
+        self.__dict__["_point_program"] = out
+        return out
 
     def mask_columns(self, columns_by_interaction) -> list:
         """The device columns of the kernel's column table, in mask order: columns_by_interaction
