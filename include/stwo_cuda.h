@@ -569,6 +569,20 @@ cs_status cs_rtc_air_composition_subdomain(void *handle, const uint32_t *const *
                                            const uint32_t *h_params, uint32_t eval_log, uint32_t trace_log,
                                            uint32_t log_expansion, uint32_t *const h_accum[4], cs_stream stream);
 cs_status cs_rtc_release(void *handle);
+/* cs_rtc_compile_air for an AIR with LogUp batches (finalize_logup_batched): the
+   source also holds cs_air_fractions(cols, params, log_n, out), which writes at
+   every row of the trace domain each batch's combined numerator and denominator
+   (QM31, out[8 j .. 8 j + 3] and out[8 j + 4 .. 8 j + 7]) from the n_frac_cols
+   trace columns its masks read; cs_rtc_air_fractions launches it (h_cols: those
+   columns on the trace domain, h_out: 8 n_batches device columns of 2^log_n
+   words). The values LogupTraceGenerator's columns are written from
+   (crates/constraint-framework/src/prover/logup.rs:22-130). */
+cs_status cs_rtc_compile_air_logup(const char *source, uint32_t n_headers, const char *const *header_sources,
+                                   const char *const *header_names, uint32_t n_cols, uint32_t n_constraints,
+                                   uint32_t n_params, uint32_t n_frac_cols, uint32_t n_batches, void **handle_out,
+                                   char *log_out, size_t log_capacity);
+cs_status cs_rtc_air_fractions(void *handle, const uint32_t *const *h_cols, const uint32_t *h_params, uint32_t log_n,
+                               uint32_t *const *h_out, cs_stream stream);
 /* The column-table size, constraint count and parameter count a kernel was compiled for. */
 cs_status cs_rtc_kernel_shape(void *handle, uint32_t *n_cols, uint32_t *n_constraints, uint32_t *n_params);
 

@@ -37,18 +37,9 @@ def _as_q(v, n):
     return q
 
 
-def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, params, rc, out=None,
-                    divide: bool = True, log_expansion: int = 0):
-    """The accumulator (4 coordinate arrays, created when None) plus the AIR's quotients. With
-    divide=False the weighted constraint sums are not divided by V_trace (on the trace domain itself,
-    where V_trace is zero, they show whether every row satisfies the constraints). With
-    log_expansion e the columns are committed on CanonicCoset(eval_log + e) and the rows are their
-    first 2^eval_log, that domain's subdomain (component_prover.rs:36-48, 234-238)."""
-    n = 1 << eval_log
-    rows = {0: np.arange(n)}
-    for m in air.masks:
-        if m.offset not in rows:
-            rows[m.offset] = O.offset_rows(m.offset, trace_log, eval_log)
+def _evaluator(columns_by_interaction, rows, params, n):
+    """Row-wise evaluation of expression nodes over n rows: masks read their column at the rows of
+    their offset (rows[offset]), values are int64 arrays, QM31 as (n, 4)."""
     memo = {}
 
     def ev(x):
@@ -82,6 +73,22 @@ def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, 
         memo[x.key] = v
         return v
 
+    return ev
+
+
+def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, params, rc, out=None,
+                    divide: bool = True, log_expansion: int = 0):
+    """The accumulator (4 coordinate arrays, created when None) plus the AIR's quotients. With
+    divide=False the weighted constraint sums are not divided by V_trace (on the trace domain itself,
+    where V_trace is zero, they show whether every row satisfies the constraints). With
+    log_expansion e the columns are committed on CanonicCoset(eval_log + e) and the rows are their
+    first 2^eval_log, that domain's subdomain (component_prover.rs:36-48, 234-238)."""
+    n = 1 << eval_log
+    rows = {0: np.arange(n)}
+    for m in air.masks:
+        if m.offset not in rows:
+            rows[m.offset] = O.offset_rows(m.offset, trace_log, eval_log)
+    ev = _evaluator(columns_by_interaction, rows, params, n)
     acc = np.zeros((n, 4), np.int64)
     for c, w in zip(air.constraints, np.asarray(rc, np.int64).reshape(-1, 4)):
         v = _as_q(ev(c), n)
@@ -92,3 +99,24 @@ def air_composition(air, columns_by_interaction, eval_log: int, trace_log: int, 
     if out is None:
         out = [np.zeros(n, np.uint32) for _ in range(4)]
     return [((np.asarray(o, np.int64) + acc[:, k]) % P).astype(np.uint32) for k, o in enumerate(out)]
+
+
+def air_fractions(air, columns_by_interaction, log_n: int, params):
+    """Each LogUp batch's combined (numerator, denominator) at every row of the trace domain, as
+    4 coordinate arrays each: the values the interaction columns are generated from (the trace
+    domain's coset-order neighbours for offset masks)."""
+    n = 1 << log_n
+    rows = {0: np.arange(n)}
+    for num, den in air.logup:
+        for root in (num, den):
+            stack = [root]
+            while stack:
+                x = stack.pop()
+                if x.op == "mask" and x.args[2] not in rows:
+                    rows[x.args[2]] = O.offset_rows(x.args[2], log_n, log_n)
+                stack.extend(a for a in x.args if hasattr(a, "key"))
+    ev = _evaluator(columns_by_interaction, rows, params, n)
+    out = []
+    for num, den in air.logup:
+        out.append(tuple([_as_q(ev(x), n)[:, k].astype(np.uint32) for k in range(4)] for x in (num, den)))
+    return out

@@ -91,6 +91,8 @@ SIGNATURES = {
     "cs_rtc_air_composition_subdomain": [vp, vp, vp, vp, u32, u32, u32, vp, vp],
     "cs_rtc_release": [vp],
     "cs_rtc_kernel_shape": [vp, vp, vp, vp],
+    "cs_rtc_compile_air_logup": [vp, u32, vp, vp, u32, u32, u32, u32, u32, vp, vp, ctypes.c_size_t],
+    "cs_rtc_air_fractions": [vp, vp, vp, u32, vp, vp],
     "cs_prove_air": [vp, vp, u32, vp, vp, ctypes.c_size_t, vp, vp],
     "cs_prove_wide_fib": [vp, vp, vp, ctypes.c_size_t, vp, vp],
     "cs_prove_fib_and_lookups": [vp, vp, u32, vp, vp, vp, vp, ctypes.c_size_t, vp, vp],

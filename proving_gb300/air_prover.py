@@ -349,6 +349,22 @@ def prove(components, channel: pr.Blake2sChannel, scheme: CommitmentSchemeProver
     return proof
 
 
+def logup_interaction(ops, air: Air, trace, log_size: int, params) -> tuple:
+    """The interaction columns of an AIR's LogUp relations from its trace columns on the trace
+    domain, as the reference's LogupTraceGenerator writes them (crates/constraint-framework/src/
+    prover/logup.rs:22-130): per batch of finalize_logup_batched its combined fraction at every row
+    (from the AIR's fraction kernel), added to the previous batch's column; the last column turned
+    into the shifted running sum. params: the relation's parameters (`{relation}_z`,
+    `{relation}_alpha{i}`). Returns (4 coordinate columns per batch, in interaction order, and the
+    claimed sum)."""
+    if not air.logup:
+        raise ValueError(f"{air.name} has no LogUp relation")
+    gen = ops.logup_generator(log_size)
+    for num, den in ops.air_fractions(air, {1: list(trace)}, log_size, params):
+        gen.col_from_fractions([(num, den)])
+    return gen.finalize_last()
+
+
 def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = False) -> bytes:
     """The same proof in native code (cs_prove_air) for components that read trace columns only:
     the empty preprocessed tree, `trace` (device columns on their trace domains, every component's
@@ -376,4 +392,5 @@ def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = F
 
 
 __all__ = ["TraceLocationAllocator", "FrameworkComponent", "CommitmentSchemeProver", "prove",
-           "constraints_at_point", "point_at_offset", "evaluation_mode", "prove_native"]
+           "constraints_at_point", "point_at_offset", "evaluation_mode", "prove_native",
+           "logup_interaction"]

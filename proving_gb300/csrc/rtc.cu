@@ -71,7 +71,8 @@ Nvrtc& nvrtc() {
 struct RtcKernel {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t fn = nullptr;
-  uint32_t n_cols = 0, n_constraints = 0, n_params = 0;
+  cudaKernel_t fn_frac = nullptr;  // cs_air_fractions, for an AIR with LogUp batches
+  uint32_t n_cols = 0, n_constraints = 0, n_params = 0, n_frac_cols = 0, n_batches = 0;
 };
 
 cpoint rtc_point_at(uint32_t idx) {
@@ -98,7 +99,18 @@ extern "C" cs_status cs_rtc_available(void) {
 extern "C" cs_status cs_rtc_compile_air(const char* source, uint32_t n_headers, const char* const* header_sources,
                                         const char* const* header_names, uint32_t n_cols, uint32_t n_constraints,
                                         uint32_t n_params, void** handle_out, char* log_out, size_t log_capacity) {
+  return cs_rtc_compile_air_logup(source, n_headers, header_sources, header_names, n_cols, n_constraints, n_params, 0,
+                                  0, handle_out, log_out, log_capacity);
+}
+
+extern "C" cs_status cs_rtc_compile_air_logup(const char* source, uint32_t n_headers,
+                                              const char* const* header_sources, const char* const* header_names,
+                                              uint32_t n_cols, uint32_t n_constraints, uint32_t n_params,
+                                              uint32_t n_frac_cols, uint32_t n_batches, void** handle_out,
+                                              char* log_out, size_t log_capacity) {
   CS_CHECK_ARG(source != nullptr && handle_out != nullptr, "rtc_compile_air: null pointer");
+  CS_CHECK_ARG(n_batches <= 1024 && (n_batches > 0 || n_frac_cols == 0), "rtc_compile_air: %u LogUp batches",
+               n_batches);
   CS_CHECK_ARG(n_headers == 0 || (header_sources != nullptr && header_names != nullptr),
                "rtc_compile_air: null header table");
   Nvrtc& n = nvrtc();
@@ -133,6 +145,7 @@ extern "C" cs_status cs_rtc_compile_air(const char* source, uint32_t n_headers, 
   RtcKernel* k = new RtcKernel;
   cudaError_t e = cudaLibraryLoadData(&k->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e == cudaSuccess) e = cudaLibraryGetKernel(&k->fn, k->lib, "cs_air_composition");
+  if (e == cudaSuccess && n_batches > 0) e = cudaLibraryGetKernel(&k->fn_frac, k->lib, "cs_air_fractions");
   if (e != cudaSuccess) {
     if (k->lib != nullptr) cudaLibraryUnload(k->lib);
     delete k;
@@ -141,8 +154,55 @@ extern "C" cs_status cs_rtc_compile_air(const char* source, uint32_t n_headers, 
   k->n_cols = n_cols;
   k->n_constraints = n_constraints;
   k->n_params = n_params;
+  k->n_frac_cols = n_frac_cols;
+  k->n_batches = n_batches;
   *handle_out = k;
   return CS_OK;
+}
+
+extern "C" cs_status cs_rtc_air_fractions(void* handle, const uint32_t* const* h_cols, const uint32_t* h_params,
+                                          uint32_t log_n, uint32_t* const* h_out, cs_stream stream) {
+  CS_CHECK_ARG(handle != nullptr && h_out != nullptr, "rtc_air_fractions: null pointer");
+  const RtcKernel* k = static_cast<const RtcKernel*>(handle);
+  CS_CHECK_ARG(k->fn_frac != nullptr, "rtc_air_fractions: the AIR has no LogUp batches");
+  CS_CHECK_ARG(k->n_frac_cols == 0 || h_cols != nullptr, "rtc_air_fractions: null column table");
+  CS_CHECK_ARG(k->n_params == 0 || h_params != nullptr, "rtc_air_fractions: null parameters");
+  CS_CHECK_ARG(log_n >= 1 && log_n <= 30, "rtc_air_fractions: log size %u", log_n);
+  for (uint32_t c = 0; c < k->n_frac_cols; c++)
+    CS_CHECK_ARG(h_cols[c] != nullptr, "rtc_air_fractions: column %u is null", c);
+  for (uint32_t c = 0; c < 8 * k->n_batches; c++)
+    CS_CHECK_ARG(h_out[c] != nullptr, "rtc_air_fractions: output %u is null", c);
+  // one staging buffer: column pointers, output pointers, then the parameters
+  const size_t n_words = 2 * (size_t)k->n_frac_cols + 16 * (size_t)k->n_batches + 4 * (size_t)k->n_params + 4;
+  std::vector<uint32_t> host(n_words, 0);
+  uint32_t* w = host.data();
+  const auto put_ptr = [&](const void* p) {
+    const uint64_t v = reinterpret_cast<uint64_t>(p);
+    *w++ = (uint32_t)v;
+    *w++ = (uint32_t)(v >> 32);
+  };
+  for (uint32_t c = 0; c < k->n_frac_cols; c++) put_ptr(h_cols[c]);
+  for (uint32_t c = 0; c < 8 * k->n_batches; c++) put_ptr(h_out[c]);
+  for (size_t i = 0; i < 4 * (size_t)k->n_params; i++) *w++ = h_params[i] % P;
+  cudaStream_t st = to_stream(stream);
+  uint32_t* dev = nullptr;
+  CS_CUDA(stream_alloc(reinterpret_cast<void**>(&dev), sizeof(uint32_t) * n_words, st));
+  cs_status result = CS_OK;
+  cudaError_t e = cudaMemcpyAsync(dev, host.data(), sizeof(uint32_t) * n_words, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    const uint32_t* const* cols = reinterpret_cast<const uint32_t* const*>(dev);
+    uint32_t* const* out = reinterpret_cast<uint32_t* const*>(dev + 2 * k->n_frac_cols);
+    const uint32_t* params = dev + 2 * (size_t)k->n_frac_cols + 16 * (size_t)k->n_batches;
+    void* args[] = {&cols, &params, &log_n, &out};
+    const uint32_t n = 1u << log_n;
+    const uint32_t blocks = std::max(1u, std::min((n + 255) / 256, 152u * 8));
+    e = cudaLaunchKernel(reinterpret_cast<const void*>(k->fn_frac), dim3(blocks), dim3(256), args, 0, st);
+    note_launch();
+  }
+  if (e != cudaSuccess) result = from_cuda(e, "rtc_air_fractions");
+  const cudaError_t ef = cudaFreeAsync(dev, st);
+  if (result == CS_OK && ef != cudaSuccess) return from_cuda(ef, "cudaFreeAsync");
+  return result;
 }
 
 extern "C" cs_status cs_rtc_kernel_shape(void* handle, uint32_t* n_cols, uint32_t* n_constraints, uint32_t* n_params) {

@@ -119,6 +119,7 @@ class Evaluator:
         self.params: list[str] = []
         self.constraints: list[Expr] = []
         self.fracs: list[tuple[Expr, Expr]] = []  # LogUp fractions (numerator, denominator) of the row
+        self.logup: list = []  # every finalized batch's combined (numerator, denominator), in column order
 
     def _mask(self, interaction: int, column: int, offset: int) -> Expr:
         """A column at the row `offset` trace steps away (0 the row itself, -1 the previous row)."""
@@ -178,6 +179,7 @@ class Evaluator:
                 num, den = num * d2 + n2 * den, den * d2
             batches.append((num, den))
         self.fracs = []
+        self.logup.extend(batches)
         last_num, last_den = batches.pop()
         prev_col = None
         for num, den in batches:
@@ -240,6 +242,10 @@ class Air:
     # constraint reads it (InfoEvaluator's mask_offsets, crates/constraint-framework/src/info.rs)
     mask_offsets: dict = field(default_factory=dict, repr=False)
     preprocessed: list = field(default_factory=list)  # preprocessed column ids, interaction 0 order
+    # the LogUp batches' combined fractions (numerator, denominator), one per interaction column
+    # of finalize_logup_batched, and the trace masks their kernel (cs_air_fractions) reads
+    logup: list = field(default_factory=list, repr=False)
+    fraction_masks: list = field(default_factory=list, repr=False)
 
     @property
     def n_constraints(self) -> int:
@@ -508,8 +514,104 @@ extern "C" __global__ void __launch_bounds__(256) cs_air_composition(
   }}
 }}
 """
+    frac_masks = []
+    if e.logup:
+        frac_src, frac_masks = _fraction_source(e)
+        src += frac_src
     return Air(name, order, list(e.params), list(e.constraints), src,
-               {k: list(v) for k, v in sorted(e.mask_offsets.items())}, list(e.preprocessed))
+               {k: list(v) for k, v in sorted(e.mask_offsets.items())}, list(e.preprocessed), list(e.logup),
+               frac_masks)
+
+
+def _fraction_source(e: Evaluator):
+    """The kernel cs_air_fractions: at every row of the trace domain, each LogUp batch's combined
+    numerator and denominator (QM31) into out[8 j .. 8 j + 3] and out[8 j + 4 .. 8 j + 7], the
+    values LogupTraceGenerator's columns are written from (crates/constraint-framework/src/prover/
+    logup.rs:22-130). Reads trace masks only (cols[i]: the column of fraction mask i on the trace
+    domain, at its row offset in coset order). Returns (source, the masks in table order)."""
+    masks, slot, temps, lines, offsets = [], {}, {}, [], set()
+
+    def row_name(o: int) -> str:
+        return "r" if o == 0 else f"ro_{'m' if o < 0 else 'p'}{abs(o)}"
+
+    def visit(root) -> str:
+        stack = [root]
+        while stack:
+            x = stack[-1]
+            if x.key in temps:
+                stack.pop()
+                continue
+            todo = [a for a in x.args if isinstance(a, Expr) and a.key not in temps]
+            if todo:
+                stack.extend(todo)
+                continue
+            stack.pop()
+            name = f"f{len(temps)}"
+            if x.op == "mask":
+                inter, col, off = x.args
+                if inter != 1:
+                    raise NotImplementedError("LogUp fractions read trace columns (interaction 1) only")
+                if x.args not in slot:
+                    slot[x.args] = len(masks)
+                    masks.append(Mask(*x.args))
+                if off:
+                    offsets.add(off)
+                lines.append(f"    const uint32_t {name} = __ldg(cols[{slot[x.args]}] + {row_name(off)});")
+            elif x.op == "const":
+                lines.append(f"    const uint32_t {name} = {x.args[0]}u;")
+            elif x.op == "param":
+                j = e.params.index(x.args[0])
+                lines.append(f"    const qm31 {name} = qm31_make(params[{4 * j}], params[{4 * j + 1}], "
+                             f"params[{4 * j + 2}], params[{4 * j + 3}]);")
+            elif x.op == "secure":
+                parts = ", ".join(temps[a.key] for a in x.args)
+                lines.append(f"    const qm31 {name} = qm31_make({parts});")
+            elif x.op == "neg":
+                t = temps[x.args[0].key]
+                lines.append(f"    const {'qm31' if x.ext else 'uint32_t'} {name} = "
+                             f"{'qm31_neg' if x.ext else 'm31_neg'}({t});")
+            else:
+                a, b = x.args
+                ta, tb = temps[a.key], temps[b.key]
+                if not x.ext:
+                    rhs = f"m31_{x.op}({ta}, {tb})"
+                elif a.ext and b.ext:
+                    rhs = f"qm31_{x.op}({ta}, {tb})"
+                elif x.op == "mul":
+                    q, m = (ta, tb) if a.ext else (tb, ta)
+                    rhs = f"qm31_mul_m31({q}, {m})"
+                else:
+                    qa = ta if a.ext else f"qm31_make({ta}, 0, 0, 0)"
+                    qb = tb if b.ext else f"qm31_make({tb}, 0, 0, 0)"
+                    rhs = f"qm31_{x.op}({qa}, {qb})"
+                lines.append(f"    const {'qm31' if x.ext else 'uint32_t'} {name} = {rhs};")
+            temps[x.key] = name
+        v = temps[root.key]
+        return v if root.ext else f"qm31_make({v}, 0, 0, 0)"
+
+    writes = []
+    for j, (num, den) in enumerate(e.logup):
+        for k, part in enumerate((visit(num), visit(den))):
+            q = f"w{j}_{k}"
+            writes.append(f"    const qm31 {q} = {part};")
+            for c, coord in enumerate(("a.a", "a.b", "b.a", "b.b")):
+                writes.append(f"    out[{8 * j + 4 * k + c}][r] = {q}.{coord};")
+    row_defs = "".join(f"    const uint32_t {row_name(o)} = offset_row(r, {o}, log_n, log_n);\n"
+                       for o in sorted(offsets))
+    body = chr(10).join(lines + writes)
+    src = f"""
+// the LogUp batches' fractions of {len(e.logup)} interaction columns at every trace row
+extern "C" __global__ void __launch_bounds__(256) cs_air_fractions(
+    const uint32_t* const* __restrict__ cols, const uint32_t* __restrict__ params, uint32_t log_n,
+    uint32_t* const* __restrict__ out) {{
+  (void)params;
+  const uint32_t n = 1u << log_n;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {{
+{row_defs}{body}
+  }}
+}}
+"""
+    return src, masks
 
 
 # ------------------------------------------------------------------ device side
@@ -529,8 +631,9 @@ class CompiledAir:
         hn = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
         handle = ctypes.c_void_p()
         log = ctypes.create_string_buffer(4096)
-        _lib.call("cs_rtc_compile_air", air.source.encode(), len(names), hs, hn, len(air.masks),
-                  air.n_constraints, len(air.params), ctypes.byref(handle), log, len(log))
+        _lib.call("cs_rtc_compile_air_logup", air.source.encode(), len(names), hs, hn, len(air.masks),
+                  air.n_constraints, len(air.params), len(air.fraction_masks), len(air.logup), ctypes.byref(handle),
+                  log, len(log))
         self.handle = handle
 
     @classmethod
@@ -540,6 +643,24 @@ class CompiledAir:
         if key not in cls._cache:
             cls._cache[key] = cls(air)
         return cls._cache[key]
+
+    def fractions(self, columns_by_interaction, log_n: int, params) -> list:
+        """Each LogUp batch's combined (numerator, denominator) at every row of the trace domain
+        (cs_rtc_air_fractions), as SecureColumnByCoords pairs. columns_by_interaction: the trace
+        columns on the trace domain; parameters the fractions do not read may be left out."""
+        from . import _lib
+        from .backend import SecureColumnByCoords, _ptr_table, _stream
+        n = 1 << log_n
+        cols = [columns_by_interaction[m.interaction][m.column] for m in self.air.fraction_masks]
+        if any(len(c) != n for c in cols):
+            raise ValueError("fraction columns must be trace-domain columns of 2^log_n rows")
+        out = [(SecureColumnByCoords.uninitialized(n), SecureColumnByCoords.uninitialized(n)) for _ in self.air.logup]
+        table = [c.data for pair in out for col in pair for c in col.columns]
+        pw = np.ascontiguousarray(np.asarray([params.get(p, (0, 0, 0, 0)) for p in self.air.params],
+                                             np.uint32).reshape(-1))
+        _lib.call("cs_rtc_air_fractions", self.handle, _ptr_table([c.data for c in cols]),
+                  pw.ctypes.data if pw.size else None, log_n, _ptr_table(table), _stream())
+        return out
 
     def composition(self, columns_by_interaction, trace_log: int, params, rc, accum, log_expansion: int = 0) -> None:
         """Adds the AIR's constraint quotients over accum's domain. params: {name: QM31}; rc: one

@@ -1202,6 +1202,14 @@ class GpuOps:
         from .framework import CompiledAir
         CompiledAir.get(air).composition(columns_by_interaction, trace_log, params, rc, accum, log_expansion)
 
+    def air_fractions(self, air, columns_by_interaction, log_n, params):
+        """An AIR's LogUp batch fractions on the trace domain (run-time compiled kernel)."""
+        from .framework import CompiledAir
+        return CompiledAir.get(air).fractions(columns_by_interaction, log_n, params)
+
+    def logup_generator(self, log_n):
+        return self.be.LogupTraceGenerator(log_n)
+
     def interpolate_secure_on_subdomain(self, accum, domain_log_size, tw):
         """The accumulator interpolated on the subdomain of its size of CanonicCoset(domain_log_size)
         (DomainEvaluationAccumulator::finalize in SubDomain mode), in place."""

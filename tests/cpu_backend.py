@@ -50,6 +50,24 @@ class Twiddles:
         self.log_size = domain_log - 1
 
 
+class _OracleLogupGenerator:
+    """LogupTraceGenerator over the oracle's column generator (O.logup_gen_col, O.logup_finalize_last)."""
+
+    def __init__(self):
+        self.trace = []
+
+    def col_from_fractions(self, fractions):
+        prev = self.trace[-1] if self.trace else None
+        for num, den in fractions:
+            prev = O.logup_gen_col(num.c if isinstance(num, SCol) else num.v, den.c, prev)
+        self.trace.append(prev)
+
+    def finalize_last(self):
+        last, claimed = O.logup_finalize_last(self.trace[-1])
+        self.trace[-1] = last
+        return [Col(c) for col in self.trace for c in col], tuple(int(x) for x in claimed)
+
+
 class CpuOps:
     def secure_powers(self, felt, n):
         return pr.secure_powers(felt, n)
@@ -88,6 +106,15 @@ class CpuOps:
         cols = {k: [c.v for c in v] for k, v in columns_by_interaction.items()}
         accum.c = air_composition(air, cols, len(accum).bit_length() - 1, trace_log, params, rc, out=accum.c,
                                   log_expansion=log_expansion)
+
+    def air_fractions(self, air, columns_by_interaction, log_n, params):
+        from oracle.air_eval import air_fractions
+        cols = {k: [c.v for c in v] for k, v in columns_by_interaction.items()}
+        full = {p: params.get(p, (0, 0, 0, 0)) for p in air.params}
+        return [(SCol(num), SCol(den)) for num, den in air_fractions(air, cols, log_n, full)]
+
+    def logup_generator(self, log_n):
+        return _OracleLogupGenerator()
 
     def interpolate_secure_on_subdomain(self, accum, domain_log_size, tw):
         sub_log = len(accum).bit_length() - 1

@@ -15,6 +15,7 @@ from proving_gb300 import air_prover as ap
 from proving_gb300 import framework as fw
 from proving_gb300 import prover as pr
 from proving_gb300.poseidon import ConstraintsNotSatisfied
+from proving_gb300.synthetic import seeded_qm31
 from test_mask_offsets_cpu import window_air, window_trace
 from test_prove_cpu import fib_and_lookups_inputs, fib_and_lookups_proof
 
@@ -387,3 +388,66 @@ def test_point_program_needs_a_trace_only_air():
         fw.compile_air("single_lookup", fw.single_lookup_air).point_program()
     with pytest.raises(NotImplementedError):
         fw.compile_air("seq", seq_air).point_program()
+
+
+def _relation_lookup_air(e):
+    e.add_to_relation("lookup", -1, [e.next_trace_mask()])
+    e.finalize_logup()
+
+
+@pytest.mark.parametrize("log_n", [1, 4, 9])
+def test_generic_interaction_equals_the_single_column_running_sum(log_n):
+    # the relation of multiplicity -1 and values [v]: fractions -1 / (v - z), the running sum of
+    # logup_running_sum (the reference's LogupTraceGenerator for one batch)
+    air = fw.compile_air("lookup_rel", _relation_lookup_air)
+    ops = CpuOps()
+    v = np.random.default_rng(log_n).integers(0, O.P, 1 << log_n, dtype=np.uint32)
+    z = tuple(int(x) for x in seeded_qm31(41))
+    cols, claimed = ap.logup_interaction(ops, air, ops.columns_from_host([v]), log_n,
+                                         {"lookup_z": z, "lookup_alpha0": (1, 0, 0, 0)})
+    want, want_claimed = O.logup_running_sum(v, z)
+    assert all(np.array_equal(c.v, w) for c, w in zip(cols, want))
+    assert claimed == tuple(int(x) for x in want_claimed)
+
+
+@pytest.mark.parametrize("log_n", [2, 4])
+def test_generic_interaction_equals_the_poseidon_interaction(log_n):
+    # Poseidon2's two relation entries per instance finalized in pairs: the oracle's hand-written
+    # interaction generator (gen_interaction_trace, crates/examples/src/poseidon/mod.rs:277-303)
+    air = fw.poseidon_air_recorded()
+    assert len(air.logup) == 8
+    ops = CpuOps()
+    trace = O.poseidon_trace(log_n)
+    z, alpha = seeded_qm31(42), seeded_qm31(43)
+    params = fw.lookup_params("poseidon", z, alpha, fw.POSEIDON_STATE)
+    cols, claimed = ap.logup_interaction(ops, air, ops.columns_from_host(trace), log_n, params)
+    want, want_claimed = O.poseidon_interaction(trace, z, alpha)
+    assert all(np.array_equal(c.v, w) for c, w in zip(cols, want))
+    assert claimed == tuple(int(x) for x in want_claimed)
+
+
+def poseidon_fully_generic(ops, log_n):
+    """prove_poseidon's flow with the interaction trace from the AIR's own fractions too."""
+    from proving_gb300 import poseidon as ps
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = ps.poseidon_pcs_config(log_n + 3, fp)
+    tw = ops.twiddles(log_n + ps.LOG_EXPAND + 1)
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(ops, cfg, tw)
+    scheme.commit([], ch)
+    trace = ops.poseidon_trace(log_n)
+    scheme.commit(trace, ch)
+    z, alpha = ch.draw_secure_felt(), ch.draw_secure_felt()
+    air = fw.poseidon_air_recorded()
+    params = fw.lookup_params("poseidon", z, alpha, fw.POSEIDON_STATE)
+    inter, claimed = ap.logup_interaction(ops, air, trace, log_n, params)
+    scheme.commit(inter, ch)
+    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n, params, claimed_sum=claimed,
+                                 constraint_log_degree=ps.LOG_EXPAND)
+    return ap.prove([comp], ch, scheme, check=False)
+
+
+def test_poseidon_fully_through_the_generic_api_equals_prove_poseidon():
+    proof = poseidon_fully_generic(CpuOps(), 4)
+    _, want = poseidon_generic(CpuOps(), 4)
+    assert proof.to_bytes() == want.to_bytes()

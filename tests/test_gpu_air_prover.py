@@ -14,7 +14,8 @@ from oracle import oracle as O  # noqa: E402
 from proving_gb300 import air_prover as ap  # noqa: E402
 from proving_gb300 import framework as fw  # noqa: E402
 from proving_gb300 import prover as pr  # noqa: E402
-from test_air_prover_cpu import FRI, blowup_proof, fib_and_lookups_generic, poseidon_generic, seq_air  # noqa: E402
+from test_air_prover_cpu import (FRI, _relation_lookup_air, blowup_proof, fib_and_lookups_generic,  # noqa: E402
+                                 poseidon_fully_generic, poseidon_generic, seq_air)
 from test_mask_offsets_cpu import window_air, window_trace  # noqa: E402
 from test_prove_cpu import fib_and_lookups_inputs  # noqa: E402
 
@@ -136,3 +137,34 @@ def test_native_generic_prover_single_component_equals_oracle(ops):
     trace = _fib(10, 8)
     got, want = _native_against_python(ops, [(fib, 10, trace)])
     assert got == want == O.prove_fib_and_lookups((10, 1, 0, 3, 1), [trace], [10])[0]
+
+
+@pytest.mark.parametrize("log_n", [1, 12])
+def test_generic_interaction_on_gpu_equals_the_running_sum(ops, log_n):
+    from proving_gb300.synthetic import seeded_qm31
+    air = fw.compile_air("lookup_rel", _relation_lookup_air)
+    v = np.random.default_rng(log_n).integers(0, O.P, 1 << log_n, dtype=np.uint32)
+    z = tuple(int(x) for x in seeded_qm31(41))
+    cols, claimed = ap.logup_interaction(ops, air, ops.columns_from_host([v]), log_n,
+                                         {"lookup_z": z, "lookup_alpha0": (1, 0, 0, 0)})
+    want, want_claimed = O.logup_running_sum(v, z)
+    assert all(np.array_equal(c.to_cpu(), w) for c, w in zip(cols, want))
+    assert claimed == tuple(int(x) for x in want_claimed)
+
+
+def test_generic_poseidon_interaction_on_gpu_equals_the_hand_written_kernel(ops):
+    from proving_gb300.synthetic import seeded_qm31
+    log_n = 8
+    air = fw.poseidon_air_recorded()
+    trace = ops.poseidon_trace(log_n)
+    z, alpha = seeded_qm31(42), seeded_qm31(43)
+    params = fw.lookup_params("poseidon", z, alpha, fw.POSEIDON_STATE)
+    cols, claimed = ap.logup_interaction(ops, air, trace, log_n, params)
+    want, want_claimed = ops.poseidon_interaction(trace, [int(x) for x in z] + [int(x) for x in alpha])
+    assert all(np.array_equal(c.to_cpu(), w.to_cpu()) for c, w in zip(cols, want))
+    assert claimed == tuple(int(x) for x in want_claimed)
+
+
+def test_poseidon_fully_through_the_generic_api_equals_oracle(ops):
+    proof = poseidon_fully_generic(ops, 4)
+    assert proof.to_bytes() == O.prove_poseidon((10, 1, 0, 70, 1), 4)

@@ -9,6 +9,12 @@ from test_mask_offsets_cpu import window_air
 nvrtc = pytest.importorskip("cuda.bindings.nvrtc")
 
 
+def _relation_lookup_air(e):
+    # a relation entry (with the fraction kernel beside the composition kernel)
+    e.add_to_relation("lookup", -1, [e.next_trace_mask()])
+    e.finalize_logup()
+
+
 def _compile(source: str):
     names = ["field.cuh", "rows.cuh"]
     headers = [fw._header(n).encode() for n in names]
@@ -28,6 +34,7 @@ def _compile(source: str):
     ("wide_fib", lambda: fw.compile_air("wide_fib", fw.wide_fib_air, 5)),
     ("single_lookup", lambda: fw.compile_air("single_lookup", fw.single_lookup_air)),
     ("window", lambda: fw.compile_air("window", window_air)),
+    ("lookup_relation", lambda: fw.compile_air("lookup_rel", _relation_lookup_air)),
 ])
 def test_generated_source_compiles_under_nvrtc(name, make):
     rc, log = _compile(make().source)
