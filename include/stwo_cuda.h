@@ -588,36 +588,55 @@ cs_status cs_rtc_kernel_shape(void *handle, uint32_t *n_cols, uint32_t *n_constr
 
 /* prove_ex for components written against the constraint evaluator
    (proving_gb300/air_prover.py's FrameworkComponent), their constraints through
-   kernels compiled with cs_rtc_compile_air: the empty preprocessed tree, one
-   trace tree of every component's columns in component order (d_trace,
-   2^log_size words each on the trace domain, bit-reversed; interpolated in place,
-   so consumed), no interaction tree, constraints of log degree 1 (evaluated on
-   CanonicCoset(log_size + 1)), log_blowup_factor 1, fold_step 1. A component's
-   columns are sampled at the OODS point plus each of its mask offsets in steps of
-   CanonicCoset(lifting_log_size - 1) (component.rs:202-214). Its constraints at
-   the point, for the sanity check (prover/mod.rs:121-132), come from `program`:
-   n_nodes nodes of 5 words (op, a0..a3) in topological order, op 0 = the sampled
-   value of local column a0 at its a1-th offset, 1 = the M31 constant a0, 2 =
-   parameter a0, 3 = from_partial_evals of nodes a0..a3, 4 = -a0, 5 = a0 + a1,
-   6 = a0 - a1, 7 = a0 * a1; constraint k is node constraints[k]. mask_cols[i]
-   is the local column the kernel's mask i reads. params: the FRI parameters
-   and twiddles (n_components, n_cols and log_sizes unused); lifting_log_size =
-   the largest log_size + 1. */
+   kernels compiled with cs_rtc_compile_air(_logup): the empty preprocessed tree,
+   one trace tree of every component's columns in component order (d_trace,
+   2^log_size words each on the trace domain, bit-reversed; interpolated in place
+   unless the component has relations, so consumed), then, when a component has
+   LogUp relations, the lookup elements (z, alpha: two channel draws) and one
+   interaction tree of every such component's 4 n_batches coordinate columns,
+   generated from its fraction kernel (cs_rtc_air_fractions) as the
+   LogupTraceGenerator writes them; with flags & CS_PROVE_MIX_CLAIMED the claimed
+   sums are mixed into the channel before that tree's root. log_blowup_factor 1,
+   fold_step 1. Constraints of log degree 1 are evaluated on the committed
+   domain; of degree 2 on CanonicCoset(log_size + 2) from the coefficients
+   (ExtendToEvalDomain), and then without the sanity check, which the reference's
+   lifted protocol fails for them (the words are the proof it computes before it).
+   A trace column is sampled at the OODS point plus each of its mask offsets in
+   steps of CanonicCoset(lifting_log_size - 1) (component.rs:202-214), an
+   interaction column at the point, or at the previous row and the point when
+   inter_two says so. The constraints at the point come from `program`: n_nodes
+   nodes of 5 words (op, a0..a3) in topological order, op 0 = the sampled value
+   of column a0 of tree a2 (1: trace, 2: interaction; local to the component) at
+   its a1-th offset, 1 = the M31 constant a0, 2 = parameter a0, 3 =
+   from_partial_evals of nodes a0..a3, 4 = -a0, 5 = a0 + a1, 6 = a0 - a1, 7 =
+   a0 * a1; constraint k is node constraints[k]. Kernel mask i reads local
+   column mask_cols[i] of tree mask_trees[i]. param_kinds: per parameter, 0 =
+   its value in params, 1 = z, 2 = the shift claimed sum / 2^log_size, 3 + i =
+   alpha^i. params: the FRI parameters and twiddles (n_components, n_cols and
+   log_sizes unused); lifting_log_size = the largest log_size + degree - 1 + 1. */
 typedef struct {
-  void *kernel;                  /* cs_rtc_compile_air handle */
+  void *kernel;                  /* cs_rtc_compile_air(_logup) handle */
   uint32_t log_size;             /* 2^log_size trace rows */
+  uint32_t constraint_log_degree;/* 1 or 2 */
   uint32_t n_cols;               /* trace columns the component takes */
-  const int32_t *offsets;        /* every column's mask offsets, concatenated */
+  const int32_t *offsets;        /* every trace column's mask offsets, concatenated */
   const uint32_t *offsets_start; /* n_cols + 1 starts into offsets */
   uint32_t n_masks;              /* the kernel's column table */
   const uint32_t *mask_cols;
+  const uint32_t *mask_trees;
   const uint32_t *program;       /* 5 words per node */
   uint32_t n_nodes;
   const uint32_t *constraints;
   uint32_t n_constraints;
   const uint32_t *params;        /* 4 words per parameter */
+  const uint32_t *param_kinds;   /* one per parameter */
   uint32_t n_params;
+  uint32_t n_batches;            /* LogUp interaction columns (0: none) */
+  uint32_t n_frac_cols;          /* the trace columns the fraction kernel reads */
+  const uint32_t *frac_cols;
+  const uint32_t *inter_two;     /* 4 n_batches flags */
 } cs_air_component;
+#define CS_PROVE_MIX_CLAIMED 2u
 cs_status cs_prove_air(const cs_wide_fib_proof_params *params, const cs_air_component *components,
                        uint32_t n_components, uint32_t *const *d_trace, uint64_t *h_words, size_t capacity,
                        size_t *n_words, cs_stream stream);

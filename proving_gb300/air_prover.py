@@ -365,12 +365,30 @@ def logup_interaction(ops, air: Air, trace, log_size: int, params) -> tuple:
     return gen.finalize_last()
 
 
-def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = False) -> bytes:
-    """The same proof in native code (cs_prove_air) for components that read trace columns only:
-    the empty preprocessed tree, `trace` (device columns on their trace domains, every component's
-    in allocation order; interpolated in place, so consumed) as the one trace tree, then prove()
-    from a fresh channel. Constraint log degree 1, log blowup 1, fold_step 1. Returns the proof
-    bytes, equal to prove()'s for the same flow."""
+def _param_kind(air: Air, name: str) -> int:
+    """cs_air_component's parameter kinds: 0 a given value, 1 a relation's z, 2 the shift, 3 + i
+    a relation's alpha^i (every relation uses the one lookup-element draw of the proof)."""
+    if name == "shift":
+        return 2
+    for rel in air.relations:
+        if name == f"{rel}_z":
+            return 1
+        if name.startswith(f"{rel}_alpha") and name[len(rel) + 6:].isdigit():
+            return 3 + int(name[len(rel) + 6:])
+    return 0
+
+
+def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = False,
+                 mix_claimed: bool = False) -> bytes:
+    """The same proof in native code (cs_prove_air): the empty preprocessed tree, `trace` (device
+    columns on their trace domains, every component's in allocation order) as the trace tree; when
+    components have LogUp relations, the lookup elements (z, alpha) drawn, the interaction tree of
+    their columns generated from their fraction kernels (the claimed sums mixed first with
+    mix_claimed), then prove() with the relations' parameters filled from the draw and the shift
+    from each claimed sum. The trace columns of components without relations are interpolated in
+    place (consumed). Constraint log degree 1 or 2 (degree 2 without the sanity check, as in the
+    reference's lifted protocol), log blowup 1, fold_step 1. Returns the proof bytes, equal to
+    prove()'s for the same flow."""
     from .backend import CudaBackend
     from .framework import CompiledAir
     fp = config.fri_params
@@ -378,17 +396,24 @@ def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = F
         raise NotImplementedError("the native prover: log blowup 1, fold_step 1")
     specs, col = [], 0
     for c in components:
-        if c.constraint_log_degree != 1:
-            raise NotImplementedError("the native prover: constraint log degree 1")
-        nodes, cons, offs, mask_cols = c.air.point_program()
+        if c.constraint_log_degree not in (1, 2):
+            raise NotImplementedError("the native prover: constraint log degree 1 or 2")
+        nodes, cons, offs, masks, inter_two = c.air.point_program()
         if c.trace_locations.get(1, (col, col))[0] != col:
             raise ValueError("components' trace columns must follow one another in component order")
         col += len(offs)
-        params = [c.params[p] for p in c.air.params]
-        specs.append((CompiledAir.get(c.air).handle, c.log_size, offs, mask_cols, nodes, cons, params))
+        kinds = [_param_kind(c.air, p) for p in c.air.params]
+        params = [c.params.get(p, (0, 0, 0, 0)) if k == 0 else (0, 0, 0, 0) for p, k in zip(c.air.params, kinds)]
+        missing = [p for p, k in zip(c.air.params, kinds) if k == 0 and p not in c.params]
+        if missing:
+            raise KeyError(f"{c.air.name}: no value for the parameters {missing}")
+        specs.append({"kernel": CompiledAir.get(c.air).handle, "log_size": c.log_size,
+                      "degree": c.constraint_log_degree, "offsets": offs, "masks": masks, "nodes": nodes,
+                      "constraints": cons, "params": params, "kinds": kinds, "n_batches": len(c.air.logup),
+                      "frac_cols": [m.column for m in c.air.fraction_masks], "inter_two": inter_two})
     return CudaBackend.prove_air_native(specs, trace, config.trace_lifting_log_size,
                                         (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound,
-                                         fp.n_queries), twiddles, plain)
+                                         fp.n_queries), twiddles, plain, mix_claimed)
 
 
 __all__ = ["TraceLocationAllocator", "FrameworkComponent", "CommitmentSchemeProver", "prove",

@@ -113,11 +113,16 @@ PROVE_PLAIN = 1  # CS_PROVE_PLAIN
 
 class _AirComponent(ctypes.Structure):
     """cs_air_component (include/stwo_cuda.h)."""
-    _fields_ = [("kernel", ctypes.c_void_p), ("log_size", ctypes.c_uint32), ("n_cols", ctypes.c_uint32),
-                ("offsets", ctypes.c_void_p), ("offsets_start", ctypes.c_void_p), ("n_masks", ctypes.c_uint32),
-                ("mask_cols", ctypes.c_void_p), ("program", ctypes.c_void_p), ("n_nodes", ctypes.c_uint32),
-                ("constraints", ctypes.c_void_p), ("n_constraints", ctypes.c_uint32), ("params", ctypes.c_void_p),
-                ("n_params", ctypes.c_uint32)]
+    _fields_ = [("kernel", ctypes.c_void_p), ("log_size", ctypes.c_uint32), ("constraint_log_degree", ctypes.c_uint32),
+                ("n_cols", ctypes.c_uint32), ("offsets", ctypes.c_void_p), ("offsets_start", ctypes.c_void_p),
+                ("n_masks", ctypes.c_uint32), ("mask_cols", ctypes.c_void_p), ("mask_trees", ctypes.c_void_p),
+                ("program", ctypes.c_void_p), ("n_nodes", ctypes.c_uint32), ("constraints", ctypes.c_void_p),
+                ("n_constraints", ctypes.c_uint32), ("params", ctypes.c_void_p), ("param_kinds", ctypes.c_void_p),
+                ("n_params", ctypes.c_uint32), ("n_batches", ctypes.c_uint32), ("n_frac_cols", ctypes.c_uint32),
+                ("frac_cols", ctypes.c_void_p), ("inter_two", ctypes.c_void_p)]
+
+
+PROVE_MIX_CLAIMED = 2  # CS_PROVE_MIX_CLAIMED
 
 
 class SecureColumnByCoords:
@@ -595,12 +600,12 @@ class CudaBackend:
 
     @staticmethod
     def prove_air_native(components, trace, lifting_log_size: int, fri_params, twiddles: TwiddleTree,
-                         plain=False) -> bytes:
-        """cs_prove_air: trace-only components written against the constraint evaluator, proved in
-        native code. components: (kernel handle, log size, per-column offsets, per-mask columns,
-        node program (n, 5), constraint nodes, parameters as QM31 words) each; trace: every
-        component's columns in order (BaseColumns on their trace domains, interpolated in place).
-        Returns the proof bytes."""
+                         plain=False, mix_claimed=False) -> bytes:
+        """cs_prove_air: components written against the constraint evaluator, proved in native code.
+        components: dicts with kernel (handle), log_size, degree, offsets (per trace column),
+        masks ((column, tree) per kernel mask), nodes ((n, 5) program), constraints (nodes),
+        params (QM31 words), kinds (per parameter), n_batches, frac_cols, inter_two; trace: every
+        component's columns in order (BaseColumns on their trace domains). Returns the proof bytes."""
         keep = []
 
         def arr(values, dtype):
@@ -608,18 +613,28 @@ class CudaBackend:
             keep.append(a)
             return a.ctypes.data if a.size else None
         comps = (_AirComponent * len(components))()
-        for k, (handle, log_size, offs, mask_cols, nodes, cons, params) in enumerate(components):
-            starts = np.cumsum([0] + [len(o) for o in offs])
+        for k, spec in enumerate(components):
             c = comps[k]
+            handle = spec["kernel"]
             c.kernel = handle.value if isinstance(handle, ctypes.c_void_p) else handle
-            c.log_size, c.n_cols = log_size, len(offs)
+            c.log_size, c.constraint_log_degree = spec["log_size"], spec["degree"]
+            offs = spec["offsets"]
+            c.n_cols = len(offs)
             c.offsets = arr([x for o in offs for x in o], np.int32)
-            c.offsets_start = arr(starts, np.uint32)
-            c.n_masks, c.mask_cols = len(mask_cols), arr(mask_cols, np.uint32)
-            c.program, c.n_nodes = arr(nodes, np.uint32), len(nodes)
-            c.constraints, c.n_constraints = arr(cons, np.uint32), len(cons)
-            c.params, c.n_params = arr(params, np.uint32), len(params)
+            c.offsets_start = arr(np.cumsum([0] + [len(o) for o in offs]), np.uint32)
+            c.n_masks = len(spec["masks"])
+            c.mask_cols = arr([m[0] for m in spec["masks"]], np.uint32)
+            c.mask_trees = arr([m[1] for m in spec["masks"]], np.uint32)
+            c.program, c.n_nodes = arr(spec["nodes"], np.uint32), len(spec["nodes"])
+            c.constraints, c.n_constraints = arr(spec["constraints"], np.uint32), len(spec["constraints"])
+            c.params, c.param_kinds = arr(spec["params"], np.uint32), arr(spec["kinds"], np.uint32)
+            c.n_params = len(spec["kinds"])
+            c.n_batches = spec["n_batches"]
+            c.n_frac_cols, c.frac_cols = len(spec["frac_cols"]), arr(spec["frac_cols"], np.uint32)
+            c.inter_two = arr(spec["inter_two"], np.uint32)
         params, keep2 = CudaBackend._proof_params([], [], lifting_log_size, fri_params, twiddles, plain)
+        if mix_claimed:
+            params.flags |= PROVE_MIX_CLAIMED
         n = ctypes.c_size_t(0)
         cap = 1 << 22
         words = _words_buffer(cap)

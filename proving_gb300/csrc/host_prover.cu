@@ -1263,29 +1263,74 @@ struct FibLookupAir : Air {
 // Components written against the constraint evaluator (FrameworkComponent, crates/constraint-framework/
 // src/component.rs), their constraint quotients from kernels compiled at run time
 // (cs_rtc_air_composition) and their constraints at the OODS point from a node program (the
-// PointEvaluator's role, crates/constraint-framework/src/point.rs:12-64). Trace-only: every column
-// in the trace tree, constraints of log degree 1.
+// PointEvaluator's role, crates/constraint-framework/src/point.rs:12-64). A component with LogUp
+// relations gets its interaction columns from its fraction kernel (cs_rtc_air_fractions) and the
+// LogupTraceGenerator's column calls, after the lookup elements (z, alpha) are drawn; its
+// parameters name z, the powers of alpha and the shift claimed sum / 2^n by kind.
 struct RtcComponent {
   void* kernel = nullptr;
-  uint32_t log_size = 0, col0 = 0, n_cols = 0;
-  std::vector<std::vector<int32_t>> offs;  // per local column
-  std::vector<uint32_t> mask_cols, program, constraints, params;
+  uint32_t log_size = 0, col0 = 0, n_cols = 0, degree = 1;
+  std::vector<std::vector<int32_t>> offs;  // per trace column
+  std::vector<uint32_t> mask_cols, mask_trees, program, constraints, params, param_kinds;
+  uint32_t n_batches = 0, inter0 = 0;
+  std::vector<uint32_t> frac_cols;
+  std::vector<bool> inter_two;
+  // filled while proving
+  std::vector<uint32_t*> inter_coeffs, inter_evals;
+  qm31 claimed = qm31_make(0, 0, 0, 0);
+  std::vector<uint32_t> resolved;  // the parameters' words once the lookup elements are drawn
 };
 
 struct RtcAir : Air {
   std::vector<RtcComponent> comps;
   uint32_t* const* d_trace = nullptr;
-  std::vector<uint32_t*> evals;  // every trace column on its blown-up domain
+  bool mix = false;
+  std::vector<uint32_t*> coeffs, evals;  // every trace column's coefficients and blown-up evaluations
+  qm31 z = qm31_make(0, 0, 0, 0), alpha = qm31_make(0, 0, 0, 0);
+
+  void resolve(RtcComponent& k, bool with_shift) const {
+    // kinds: 0 the given value, 1 z, 2 the shift, 3 + i alpha^i
+    k.resolved = k.params;
+    for (size_t j = 0; j < k.param_kinds.size(); j++) {
+      const uint32_t kind = k.param_kinds[j];
+      qm31 v;
+      if (kind == 0) continue;
+      if (kind == 1) {
+        v = z;
+      } else if (kind == 2) {
+        v = with_shift ? qm31_mul_m31(k.claimed, m31_inv(1u << k.log_size)) : qm31_make(0, 0, 0, 0);
+      } else {
+        v = qm31_make(1, 0, 0, 0);
+        for (uint32_t i = 3; i < kind; i++) v = qm31_mul(v, alpha);
+      }
+      k.resolved[4 * j] = v.a.a;
+      k.resolved[4 * j + 1] = v.a.b;
+      k.resolved[4 * j + 2] = v.b.a;
+      k.resolved[4 * j + 3] = v.b.b;
+    }
+  }
+  bool any_relation() const {
+    for (const RtcComponent& k : comps)
+      if (k.n_batches) return true;
+    return false;
+  }
 
   cs_status trace(Prover& P, std::vector<Col>& cols) override {
+    // the columns of a component with relations are interpolated out of place: its fraction
+    // kernel reads their trace-domain values after the trace tree is committed
     std::vector<const uint32_t*> src;
-    std::vector<uint32_t*> coeffs;
     std::vector<uint32_t> tlogs;
     for (const RtcComponent& k : comps)
       for (uint32_t j = 0; j < k.n_cols; j++) {
         src.push_back(d_trace[k.col0 + j]);
-        coeffs.push_back(d_trace[k.col0 + j]);
         tlogs.push_back(k.log_size);
+        if (k.n_batches) {
+          uint32_t* c = P.A.alloc(1ull << k.log_size);
+          if (!c) return P.A.status;
+          coeffs.push_back(c);
+        } else {
+          coeffs.push_back(d_trace[k.col0 + j]);
+        }
       }
     HP_TRY(P.interpolate_mixed(src, coeffs, tlogs));
     HP_TRY(P.evaluate_mixed(coeffs, tlogs, evals));
@@ -1294,6 +1339,85 @@ struct RtcAir : Air {
   }
   void trace_offsets(std::vector<std::vector<int32_t>>& offs) const override {
     for (const RtcComponent& k : comps) offs.insert(offs.end(), k.offs.begin(), k.offs.end());
+  }
+  bool has_interaction() const override { return any_relation(); }
+  bool mix_claimed() const override { return mix; }
+  cs_status interaction(Prover& P, const qm31& zz, const qm31& aa, std::vector<Col>& cols, std::vector<bool>& two,
+                        std::vector<qm31>& claimed) override {
+    z = zz;
+    alpha = aa;
+    size_t n_rel = 0;
+    for (RtcComponent& k : comps)
+      if (k.n_batches) n_rel++;
+    uint32_t* d_claimed = P.A.alloc(4 * n_rel);
+    if (!d_claimed) return P.A.status;
+    size_t r = 0;
+    std::vector<const uint32_t*> src;
+    std::vector<uint32_t*> dst;
+    std::vector<uint32_t> slogs;
+    uint32_t inter0 = 0;
+    for (RtcComponent& k : comps) {
+      if (!k.n_batches) continue;
+      const uint32_t n = k.log_size, B = k.n_batches;
+      resolve(k, false);
+      uint32_t* fr = P.A.alloc((8ull * B) << n);
+      uint32_t* ic = P.A.alloc((4ull * B) << n);
+      if (!fr || !ic) return P.A.status;
+      std::vector<const uint32_t*> fcols;
+      for (uint32_t c : k.frac_cols) fcols.push_back(d_trace[k.col0 + c]);
+      std::vector<uint32_t*> fout;
+      for (uint32_t j = 0; j < 8 * B; j++) fout.push_back(fr + ((size_t)j << n));
+      HP_TRY(cs_rtc_air_fractions(k.kernel, fcols.empty() ? nullptr : fcols.data(),
+                                  k.resolved.empty() ? nullptr : k.resolved.data(), n, fout.data(), P.st));
+      for (uint32_t j = 0; j < 4 * B; j++) k.inter_coeffs.push_back(ic + ((size_t)j << n));
+      for (uint32_t b = 0; b < B; b++) {
+        const uint32_t* num[4] = {fout[8 * b], fout[8 * b + 1], fout[8 * b + 2], fout[8 * b + 3]};
+        const uint32_t* den[4] = {fout[8 * b + 4], fout[8 * b + 5], fout[8 * b + 6], fout[8 * b + 7]};
+        const uint32_t* prev[4] = {nullptr, nullptr, nullptr, nullptr};
+        if (b) for (int c = 0; c < 4; c++) prev[c] = k.inter_coeffs[4 * (b - 1) + c];
+        uint32_t* out[4] = {k.inter_coeffs[4 * b], k.inter_coeffs[4 * b + 1], k.inter_coeffs[4 * b + 2],
+                            k.inter_coeffs[4 * b + 3]};
+        HP_TRY(cs_logup_gen_col(num, nullptr, den, b ? prev : nullptr, n, out, P.st));
+      }
+      uint32_t* last[4] = {k.inter_coeffs[4 * (B - 1)], k.inter_coeffs[4 * (B - 1) + 1],
+                           k.inter_coeffs[4 * (B - 1) + 2], k.inter_coeffs[4 * (B - 1) + 3]};
+      HP_TRY(cs_logup_finalize_last(last, n, d_claimed + 4 * r, P.st));
+      P.A.release(fr);
+      k.inter0 = inter0;
+      inter0 += 4 * B;
+      for (uint32_t* c : k.inter_coeffs) {
+        src.push_back(c);
+        dst.push_back(c);
+        slogs.push_back(n);
+      }
+      r++;
+    }
+    std::vector<uint32_t> cl(4 * n_rel);
+    CS_CUDA(cudaMemcpyAsync(cl.data(), d_claimed, 16 * n_rel, cudaMemcpyDeviceToHost, P.st));
+    CS_CUDA(cudaStreamSynchronize(P.st));
+    claimed.clear();
+    r = 0;
+    for (RtcComponent& k : comps) {
+      if (!k.n_batches) continue;
+      k.claimed = qm31_make(cl[4 * r], cl[4 * r + 1], cl[4 * r + 2], cl[4 * r + 3]);
+      claimed.push_back(k.claimed);
+      r++;
+    }
+    // every interaction column of every component in one interpolate and one evaluate call
+    HP_TRY(P.interpolate_mixed(src, dst, slogs));
+    std::vector<uint32_t*> ev;
+    HP_TRY(P.evaluate_mixed(dst, slogs, ev));
+    size_t e0 = 0;
+    for (RtcComponent& k : comps) {
+      if (!k.n_batches) continue;
+      for (uint32_t j = 0; j < 4 * k.n_batches; j++) {
+        k.inter_evals.push_back(ev[e0 + j]);
+        cols.push_back({ev[e0 + j], k.log_size + P.cfg.b});
+        two.push_back(k.inter_two[j]);
+      }
+      e0 += 4 * k.n_batches;
+    }
+    return CS_OK;
   }
   uint32_t n_constraints() const override {
     uint32_t n = 0;
@@ -1304,8 +1428,9 @@ struct RtcAir : Air {
                         std::map<uint32_t, std::vector<uint32_t*>>& acc) override {
     const uint32_t total = n_constraints();
     uint32_t start = 0;
-    for (const RtcComponent& k : comps) {  // each component takes the last powers, reversed
-      const uint32_t n = (uint32_t)k.constraints.size(), el = k.log_size + 1;
+    for (RtcComponent& k : comps) {  // each component takes the last powers, reversed
+      const uint32_t n = (uint32_t)k.constraints.size(), el = k.log_size + k.degree;
+      resolve(k, true);
       std::vector<uint32_t> rc(4 * (size_t)n);
       for (uint32_t j = 0; j < n; j++) {
         const qm31 x = pw[total - start - 1 - j];
@@ -1314,30 +1439,52 @@ struct RtcAir : Air {
         rc[4 * j + 2] = x.b.a;
         rc[4 * j + 3] = x.b.b;
       }
+      // the columns on CanonicCoset(el): the committed evaluations for constraint log degree 1
+      // (SubDomain with log_expansion 0), else the coefficients evaluated there (ExtendToEvalDomain)
+      std::vector<uint32_t*> tcols(evals.begin() + k.col0, evals.begin() + k.col0 + k.n_cols), icols = k.inter_evals;
+      std::vector<uint32_t*> ext_t, ext_i;
+      if (k.degree > P.cfg.b) {
+        std::vector<uint32_t*> tc(coeffs.begin() + k.col0, coeffs.begin() + k.col0 + k.n_cols);
+        HP_TRY(P.evaluate(tc, k.log_size, el, ext_t));
+        tcols = ext_t;
+        if (!k.inter_coeffs.empty()) {
+          HP_TRY(P.evaluate(k.inter_coeffs, k.log_size, el, ext_i));
+          icols = ext_i;
+        }
+      }
       std::vector<const uint32_t*> table;
-      for (uint32_t c : k.mask_cols) table.push_back(evals[k.col0 + c]);
-      HP_TRY(cs_rtc_air_composition(k.kernel, table.data(), rc.data(), k.params.empty() ? nullptr : k.params.data(),
+      for (size_t i = 0; i < k.mask_cols.size(); i++)
+        table.push_back(k.mask_trees[i] == 2 ? icols[k.mask_cols[i]] : tcols[k.mask_cols[i]]);
+      HP_TRY(cs_rtc_air_composition(k.kernel, table.data(), rc.data(), k.resolved.empty() ? nullptr : k.resolved.data(),
                                     el, k.log_size, P.acc_for(acc, el).data(), P.st));
+      if (!ext_t.empty()) P.A.release(ext_t[0]);
+      if (!ext_i.empty()) P.A.release(ext_i[0]);
       start += n;
     }
     return CS_OK;
   }
   bool at_point(const qpoint& oods, uint32_t mldb, const qm31& random_coeff,
                 const std::vector<std::vector<std::vector<qm31>>>& sampled, qm31& expected) override {
+    // constraints of log degree 2 or more: no check, as the reference's lifted protocol fails it
+    for (const RtcComponent& k : comps)
+      if (k.degree > 1) return false;
     qm31 x = oods.x;
     for (uint32_t i = 0; i + 1 < mldb; i++) x = q_double_x(x);
     qm31 acc = qm31_make(0, 0, 0, 0);
     std::vector<qm31> v;
-    for (const RtcComponent& k : comps) {
+    for (RtcComponent& k : comps) {
+      resolve(k, true);
       const size_t n_nodes = k.program.size() / 5;
       v.assign(n_nodes, qm31_make(0, 0, 0, 0));
       for (size_t i = 0; i < n_nodes; i++) {
         const uint32_t* nd = &k.program[5 * i];
         switch (nd[0]) {
-          case 0: v[i] = sampled[1][k.col0 + nd[1]][nd[2]]; break;
+          case 0:
+            v[i] = nd[3] == 2 ? sampled[2][k.inter0 + nd[1]][nd[2]] : sampled[1][k.col0 + nd[1]][nd[2]];
+            break;
           case 1: v[i] = qm31_make(nd[1] % P, 0, 0, 0); break;
-          case 2: v[i] = qm31_make(k.params[4 * nd[1]], k.params[4 * nd[1] + 1], k.params[4 * nd[1] + 2],
-                                   k.params[4 * nd[1] + 3]); break;
+          case 2: v[i] = qm31_make(k.resolved[4 * nd[1]], k.resolved[4 * nd[1] + 1], k.resolved[4 * nd[1] + 2],
+                                   k.resolved[4 * nd[1] + 3]); break;
           case 3: {
             const qm31 parts[4] = {v[nd[1]], v[nd[2]], v[nd[3]], v[nd[4]]};
             v[i] = from_partial_evals(parts);
@@ -1539,17 +1686,25 @@ extern "C" cs_status cs_prove_air(const cs_wide_fib_proof_params* params, const 
   CS_CHECK_ARG(n_components >= 1, "prove_air: no components");
   hp::RtcAir air;
   air.d_trace = d_trace;
+  air.mix = (params->flags & CS_PROVE_MIX_CLAIMED) != 0;
   uint32_t max_log = 0, col0 = 0;
   for (uint32_t k = 0; k < n_components; k++) {
     const cs_air_component& c = components[k];
     CS_CHECK_ARG(c.kernel != nullptr && c.log_size >= 1 && c.log_size <= 27 && c.n_cols >= 1,
                  "prove_air: component %u: kernel, 2^%u rows, %u columns", k, c.log_size, c.n_cols);
+    CS_CHECK_ARG(c.constraint_log_degree == 1 || c.constraint_log_degree == 2,
+                 "prove_air: component %u: constraint log degree %u (1 or 2)", k, c.constraint_log_degree);
     CS_CHECK_ARG(c.offsets_start != nullptr && (c.offsets != nullptr || c.offsets_start[c.n_cols] == 0),
                  "prove_air: component %u: null offsets", k);
     CS_CHECK_ARG(c.n_nodes == 0 || c.program != nullptr, "prove_air: component %u: null program", k);
     CS_CHECK_ARG(c.n_constraints == 0 || c.constraints != nullptr, "prove_air: component %u: null constraints", k);
-    CS_CHECK_ARG(c.n_masks == 0 || c.mask_cols != nullptr, "prove_air: component %u: null mask table", k);
-    CS_CHECK_ARG(c.n_params == 0 || c.params != nullptr, "prove_air: component %u: null parameters", k);
+    CS_CHECK_ARG(c.n_masks == 0 || (c.mask_cols != nullptr && c.mask_trees != nullptr),
+                 "prove_air: component %u: null mask table", k);
+    CS_CHECK_ARG(c.n_params == 0 || (c.params != nullptr && c.param_kinds != nullptr),
+                 "prove_air: component %u: null parameters", k);
+    CS_CHECK_ARG(c.n_batches <= 1024 && (c.n_batches == 0 || (c.inter_two != nullptr &&
+                                                             (c.n_frac_cols == 0 || c.frac_cols != nullptr))),
+                 "prove_air: component %u: relation tables", k);
     uint32_t kc = 0, kn = 0, kp = 0;
     const cs_status shape = cs_rtc_kernel_shape(c.kernel, &kc, &kn, &kp);
     if (shape != CS_OK) return shape;
@@ -1558,43 +1713,61 @@ extern "C" cs_status cs_prove_air(const cs_wide_fib_proof_params* params, const 
     hp::RtcComponent rc;
     rc.kernel = c.kernel;
     rc.log_size = c.log_size;
+    rc.degree = c.constraint_log_degree;
     rc.col0 = col0;
     rc.n_cols = c.n_cols;
+    rc.n_batches = c.n_batches;
     for (uint32_t j = 0; j < c.n_cols; j++) {
       CS_CHECK_ARG(c.offsets_start[j] <= c.offsets_start[j + 1], "prove_air: component %u: offsets out of order", k);
       rc.offs.emplace_back(c.offsets + c.offsets_start[j], c.offsets + c.offsets_start[j + 1]);
       for (int32_t o : rc.offs.back())
         CS_CHECK_ARG(o > -(1 << 20) && o < (1 << 20), "prove_air: component %u: offset %d", k, o);
     }
+    for (uint32_t j = 0; j < 4 * c.n_batches; j++) rc.inter_two.push_back(c.inter_two[j] != 0);
+    rc.frac_cols.assign(c.frac_cols, c.frac_cols + c.n_frac_cols);
+    for (uint32_t f : rc.frac_cols) CS_CHECK_ARG(f < c.n_cols, "prove_air: component %u: fraction column %u", k, f);
     rc.mask_cols.assign(c.mask_cols, c.mask_cols + c.n_masks);
-    for (uint32_t m : rc.mask_cols) CS_CHECK_ARG(m < c.n_cols, "prove_air: component %u: mask column %u", k, m);
+    rc.mask_trees.assign(c.mask_trees, c.mask_trees + c.n_masks);
+    for (uint32_t i = 0; i < c.n_masks; i++) {
+      const bool inter = rc.mask_trees[i] == 2;
+      CS_CHECK_ARG((rc.mask_trees[i] == 1 && rc.mask_cols[i] < c.n_cols) ||
+                       (inter && rc.mask_cols[i] < 4 * c.n_batches),
+                   "prove_air: component %u: mask %u reads column %u of tree %u", k, i, rc.mask_cols[i],
+                   rc.mask_trees[i]);
+    }
     rc.program.assign(c.program, c.program + 5 * (size_t)c.n_nodes);
-    // every operand names an earlier node, every mask a column and one of its offsets
+    // every operand names an earlier node, every sampled value a column and one of its samples
     for (uint32_t i = 0; i < c.n_nodes; i++) {
       const uint32_t* nd = &rc.program[5 * (size_t)i];
       CS_CHECK_ARG(nd[0] <= 7, "prove_air: component %u: node %u: op %u", k, i, nd[0]);
       const uint32_t n_in = nd[0] == 3 ? 4 : nd[0] == 4 ? 1 : nd[0] >= 5 ? 2 : 0;
       for (uint32_t a = 0; a < n_in; a++)
         CS_CHECK_ARG(nd[1 + a] < i, "prove_air: component %u: node %u reads node %u", k, i, nd[1 + a]);
-      if (nd[0] == 0)
-        CS_CHECK_ARG(nd[1] < c.n_cols && nd[2] < rc.offs[nd[1]].size(),
+      if (nd[0] == 0 && nd[3] == 2)
+        CS_CHECK_ARG(nd[1] < 4 * c.n_batches && nd[2] < (rc.inter_two[nd[1]] ? 2u : 1u),
+                     "prove_air: component %u: node %u: interaction column %u sample %u", k, i, nd[1], nd[2]);
+      else if (nd[0] == 0)
+        CS_CHECK_ARG(nd[3] <= 1 && nd[1] < c.n_cols && nd[2] < rc.offs[nd[1]].size(),
                      "prove_air: component %u: node %u: column %u offset %u", k, i, nd[1], nd[2]);
       if (nd[0] == 2) CS_CHECK_ARG(nd[1] < c.n_params, "prove_air: component %u: node %u: parameter %u", k, i, nd[1]);
     }
     rc.constraints.assign(c.constraints, c.constraints + c.n_constraints);
     for (uint32_t x : rc.constraints) CS_CHECK_ARG(x < c.n_nodes, "prove_air: component %u: constraint node %u", k, x);
     rc.params.assign(c.params, c.params + 4 * (size_t)c.n_params);
+    rc.param_kinds.assign(c.param_kinds, c.param_kinds + c.n_params);
     for (uint32_t j = 0; j < c.n_cols; j++)
       CS_CHECK_ARG(d_trace[col0 + j] != nullptr, "prove_air: column %u is null", col0 + j);
-    max_log = std::max(max_log, c.log_size);
+    max_log = std::max(max_log, c.log_size + c.constraint_log_degree - 1);
     col0 += c.n_cols;
     air.comps.push_back(std::move(rc));
   }
-  const cs_status cs = check_common(*params, max_log);
+  cs_wide_fib_proof_params pp = *params;
+  pp.flags &= ~CS_PROVE_MIX_CLAIMED;
+  const cs_status cs = check_common(pp, max_log);
   if (cs != CS_OK) return cs;
   std::vector<uint64_t>& words = proof_words();
   std::vector<qm31> claimed;
-  const cs_status s = hp::prove(config_of(*params), air, words, claimed, to_stream(stream));
+  const cs_status s = hp::prove(config_of(pp), air, words, claimed, to_stream(stream));
   if (s != CS_OK) return s;
   return finish(words, h_words, capacity, n_words);
 }

@@ -120,6 +120,7 @@ class Evaluator:
         self.constraints: list[Expr] = []
         self.fracs: list[tuple[Expr, Expr]] = []  # LogUp fractions (numerator, denominator) of the row
         self.logup: list = []  # every finalized batch's combined (numerator, denominator), in column order
+        self.relations: list[str] = []  # the relations add_to_relation names, in first-use order
 
     def _mask(self, interaction: int, column: int, offset: int) -> Expr:
         """A column at the row `offset` trace steps away (0 the row itself, -1 the previous row)."""
@@ -163,6 +164,8 @@ class Evaluator:
             den = term if den is None else den + term
         den = den - self.param(f"{relation}_z")
         self.fracs.append((_lift(multiplicity), den))
+        if relation not in self.relations:
+            self.relations.append(relation)
 
     def finalize_logup_batched(self, batch_size: int, interaction: int = 2, shift: str = "shift") -> None:
         """finalize_logup_batched (the logup_proxy macro, crates/constraint-framework/src/lib.rs:
@@ -246,24 +249,31 @@ class Air:
     # of finalize_logup_batched, and the trace masks their kernel (cs_air_fractions) reads
     logup: list = field(default_factory=list, repr=False)
     fraction_masks: list = field(default_factory=list, repr=False)
+    relations: list = field(default_factory=list)
 
     @property
     def n_constraints(self) -> int:
         return len(self.constraints)
 
     def point_program(self):
-        """The constraints at a point as the node program of cs_prove_air, for an AIR that reads only
-        trace columns (interaction 1): nodes of 5 words (op, a0..a3) in topological order; op 0 is
-        the sampled value of column a0 at its a1-th mask offset, 1 the constant a0, 2 parameter a0,
-        3 from_partial_evals of nodes a0..a3, 4 -a0, 5 a0 + a1, 6 a0 - a1, 7 a0 * a1. Returns
-        (nodes (n, 5) uint32, each constraint's node, each column's offsets, each mask's column);
-        computed once per Air."""
+        """The constraints at a point as the node program of cs_prove_air, for an AIR that reads
+        trace columns (interaction 1) and the interaction columns of its relations (interaction 2,
+        each at the row, or at the previous row and the row): nodes of 5 words (op, a0..a3) in
+        topological order; op 0 is the sampled value of column a0 of tree a2 at its a1-th sample, 1
+        the constant a0, 2 parameter a0, 3 from_partial_evals of nodes a0..a3, 4 -a0, 5 a0 + a1,
+        6 a0 - a1, 7 a0 * a1. Returns (nodes (n, 5) uint32, each constraint's node, each trace
+        column's offsets, each mask's (column, tree), each interaction column's "also at the
+        previous row" flag); computed once per Air."""
         cached = self.__dict__.get("_point_program")
         if cached is not None:
             return cached
-        if set(self.mask_offsets) - {1} or self.preprocessed:
-            raise NotImplementedError("a node program for AIRs that read trace columns only")
+        if set(self.mask_offsets) - {1, 2} or self.preprocessed:
+            raise NotImplementedError("a node program for AIRs that read trace and interaction columns")
         offs = [list(o) for o in self.mask_offsets.get(1, [])]
+        inter = [list(o) for o in self.mask_offsets.get(2, [])]
+        if any(o not in ([0], [-1, 0]) for o in inter):
+            raise NotImplementedError("interaction columns read at the row, or at the previous row and the row")
+        tree_offs = {1: offs, 2: inter}
         ids, prog = {}, []
         codes = {"neg": 4, "add": 5, "sub": 6, "mul": 7}
         for root in self.constraints:
@@ -279,8 +289,8 @@ class Air:
                     continue
                 stack.pop()
                 if x.op == "mask":
-                    _, col, off = x.args
-                    row = [0, col, offs[col].index(off), 0, 0]
+                    tree, col, off = x.args
+                    row = [0, col, tree_offs[tree][col].index(off), tree, 0]
                 elif x.op == "const":
                     row = [1, x.args[0] % P, 0, 0, 0]
                 elif x.op == "param":
@@ -293,7 +303,8 @@ class Air:
                 ids[x.key] = len(prog)
                 prog.append(row)
         nodes = np.asarray(prog, np.uint32).reshape(-1, 5)
-        out = (nodes, [ids[c.key] for c in self.constraints], offs, [m.column for m in self.masks])
+        out = (nodes, [ids[c.key] for c in self.constraints], offs, [(m.column, m.interaction) for m in self.masks],
+               [len(o) == 2 for o in inter])
         self.__dict__["_point_program"] = out
         return out
 
@@ -520,7 +531,7 @@ extern "C" __global__ void __launch_bounds__(256) cs_air_composition(
         src += frac_src
     return Air(name, order, list(e.params), list(e.constraints), src,
                {k: list(v) for k, v in sorted(e.mask_offsets.items())}, list(e.preprocessed), list(e.logup),
-               frac_masks)
+               frac_masks, list(e.relations))
 
 
 def _fraction_source(e: Evaluator):

@@ -357,7 +357,7 @@ def _run_program(nodes, cons, offs, mask, params):
     v = []
     for op, a0, a1, a2, a3 in np.asarray(nodes, np.int64).tolist():
         if op == 0:
-            v.append(tuple(mask[(1, a0, offs[a0][a1])]))
+            v.append(tuple(mask[(a2, a0, offs[a0][a1])]))
         elif op == 1:
             v.append(pr.qm(a0))
         elif op == 2:
@@ -375,17 +375,17 @@ def _run_program(nodes, cons, offs, mask, params):
                                   lambda: fw.compile_air("wide_fib_7", fw.wide_fib_air, 7)])
 def test_point_program_equals_the_point_evaluation(make):
     air = make()
-    nodes, cons, offs, mask_cols = air.point_program()
-    assert len(cons) == air.n_constraints and len(mask_cols) == len(air.masks)
+    nodes, cons, offs, masks, inter_two = air.point_program()
+    assert len(cons) == air.n_constraints and len(masks) == len(air.masks) and inter_two == []
     assert all(offs[m.column][0] is not None and m.offset in offs[m.column] for m in air.masks)
     rng = np.random.default_rng(5)
     mask = {(1, c, o): tuple(int(x) for x in rng.integers(0, O.P, 4)) for c, os in enumerate(offs) for o in os}
     assert _run_program(nodes, cons, offs, mask, []) == ap.constraints_at_point(air, mask, {})
 
 
-def test_point_program_needs_a_trace_only_air():
-    with pytest.raises(NotImplementedError):
-        fw.compile_air("single_lookup", fw.single_lookup_air).point_program()
+def test_point_program_reads_trace_and_interaction_columns_only():
+    nodes, _, _, masks, inter_two = fw.compile_air("single_lookup", fw.single_lookup_air).point_program()
+    assert inter_two == [True] * 4 and {t for _, t in masks} == {1, 2}
     with pytest.raises(NotImplementedError):
         fw.compile_air("seq", seq_air).point_program()
 

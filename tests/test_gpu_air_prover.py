@@ -168,3 +168,39 @@ def test_generic_poseidon_interaction_on_gpu_equals_the_hand_written_kernel(ops)
 def test_poseidon_fully_through_the_generic_api_equals_oracle(ops):
     proof = poseidon_fully_generic(ops, 4)
     assert proof.to_bytes() == O.prove_poseidon((10, 1, 0, 70, 1), 4)
+
+
+def test_native_generic_prover_with_relations_equals_oracle(ops):
+    # two components of the relation entry -1 / (v - z) (sizes 2^8 and 2^4), their interaction tree
+    # generated from their fraction kernels, the claimed sums mixed before its root: the oracle's
+    # proof of two single-column LogUp components. The relation's parameters are filled from the
+    # draw, so the values given here are placeholders.
+    air = fw.compile_air("lookup_rel", _relation_lookup_air)
+    rng = np.random.default_rng(7)
+    vals = [rng.integers(0, O.P, 1 << n, dtype=np.uint32) for n in (8, 4)]
+    cfg = pr.PcsConfig(FRI, trace_lifting_log_size=9)
+    tw = ops.twiddles(10)
+    alloc = ap.TraceLocationAllocator()
+    placeholder = {"lookup_z": (0, 0, 0, 0), "lookup_alpha0": (0, 0, 0, 0)}
+    comps = [ap.FrameworkComponent(alloc, air, n, placeholder) for n in (8, 4)]
+    got = ap.prove_native(comps, ops.columns_from_host(vals), cfg, tw, mix_claimed=True)
+    want, _ = O.prove_fib_and_lookups((10, 1, 0, 3, 1), [], [], vals, [8, 4])
+    assert got == want
+
+
+@pytest.mark.parametrize("log_n", [4, 7])
+def test_native_generic_poseidon_equals_the_hand_written_native_prover(ops, log_n):
+    # Poseidon2 recorded by the evaluator through cs_prove_air: fraction kernel, generated
+    # interaction, constraint log degree 2 (extended evaluation, no sanity check): the words of
+    # cs_prove_poseidon and of the oracle prover
+    from proving_gb300 import poseidon as ps
+    from proving_gb300.backend import CudaBackend
+    air = fw.poseidon_air_recorded()
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+    cfg = ps.poseidon_pcs_config(log_n + 3, fp)
+    tw = ops.twiddles(log_n + ps.LOG_EXPAND + 1)
+    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n,
+                                 {"shift": (0, 0, 0, 0)}, constraint_log_degree=ps.LOG_EXPAND)
+    got = ap.prove_native([comp], ops.poseidon_trace(log_n), cfg, tw)
+    want = CudaBackend.prove_poseidon_native(log_n, (10, 1, 0, 70), tw)
+    assert got == want == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
