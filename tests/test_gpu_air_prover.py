@@ -199,8 +199,9 @@ def test_native_generic_poseidon_equals_the_hand_written_native_prover(ops, log_
     fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
     cfg = ps.poseidon_pcs_config(log_n + 3, fp)
     tw = ops.twiddles(log_n + ps.LOG_EXPAND + 1)
-    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n,
-                                 {"shift": (0, 0, 0, 0)}, constraint_log_degree=ps.LOG_EXPAND)
+    placeholder = {p: (0, 0, 0, 0) for p in air.params}  # z, alpha^i and the shift come from the proof
+    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n, placeholder,
+                                 constraint_log_degree=ps.LOG_EXPAND)
     got = ap.prove_native([comp], ops.poseidon_trace(log_n), cfg, tw)
     want = CudaBackend.prove_poseidon_native(log_n, (10, 1, 0, 70), tw)
     assert got == want == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
