@@ -598,6 +598,25 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
             lat.append((t1 - t0) * 1e3)
             nat.append((t2 - t1) * 1e3)
             nplain.append((time.perf_counter() - t2) * 1e3)
+    # the same proof through the native generic prover: the AIR recorded by the constraint evaluator
+    # (its composition and fraction kernels compiled once with NVRTC, before the timed proofs), the
+    # interaction trace from its fractions; bytes checked against cs_prove_poseidon
+    from proving_gb300 import air_prover as ap
+    from proving_gb300 import framework as fw
+    air = fw.poseidon_air_recorded()
+    fw.CompiledAir.get(air)
+    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n_rows, {p: (0, 0, 0, 0) for p in air.params},
+                                 constraint_log_degree=ps.LOG_EXPAND)
+    gen = []
+    for k in range(n_proofs + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        words = ap.prove_native([comp], CudaBackend.poseidon_trace(log_n_rows), cfg, tw)
+        torch.cuda.synchronize()
+        if k >= 1:
+            gen.append((time.perf_counter() - t0) * 1e3)
+        if k == 0 and words != CudaBackend.prove_poseidon_native(log_n_rows, fpt, tw):
+            raise RuntimeError("native generic Poseidon2 proof differs from cs_prove_poseidon's")
     torch.cuda.empty_cache()
     # the constraint-quotient kernel alone on the evaluation domain CanonicCoset(log_n_rows + 2)
     eval_log = log_n_rows + ps.LOG_EXPAND
@@ -624,6 +643,10 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
                         "p50_ms": round(statistics.median(lat), 3)},
            "native_plain": {"proofs_per_s": round(1e3 / statistics.median(nplain), 3),
                             "p50_ms": round(statistics.median(nplain), 3)},
+           "generic_native": {"proofs_per_s": round(1e3 / statistics.median(gen), 3),
+                              "p50_ms": round(statistics.median(gen), 3),
+                              "note": "cs_prove_air over the NVRTC kernels of poseidon_air (composition and "
+                                      "LogUp fractions); bytes checked against cs_prove_poseidon"},
            "composition_kernel": {"eval_rows": 1 << eval_log, "ms": round(ms, 4),
                                   "gb_per_s": round(read_bytes / ms / 1e6, 1),
                                   "rows_per_s": round((1 << eval_log) / ms * 1e3, 1)}}
