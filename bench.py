@@ -605,8 +605,7 @@ def poseidon_prove_leg(torch, log_n_rows: int = 18, n_proofs: int = 2):
     from proving_gb300 import framework as fw
     air = fw.poseidon_air_recorded()
     fw.CompiledAir.get(air)
-    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n_rows, {p: (0, 0, 0, 0) for p in air.params},
-                                 constraint_log_degree=ps.LOG_EXPAND)
+    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n_rows, constraint_log_degree=ps.LOG_EXPAND)
     gen = []
     for k in range(n_proofs + 1):
         torch.cuda.synchronize()

@@ -83,7 +83,8 @@ class FrameworkComponent:
         if "shift" in air.params and "shift" not in params:
             inv = m_inv(1 << log_size)
             params["shift"] = tuple(c * inv % P for c in self.claimed_sum)
-        missing = [n for n in air.params if n not in params]
+        # a relation's z and alpha powers may come later (prove() needs them; prove_native draws them)
+        missing = [n for n in air.params if n not in params and _param_kind(air, n) == 0]
         if missing:
             raise KeyError(f"{air.name}: no value for the parameters {missing}")
         self.params = params
@@ -254,6 +255,10 @@ def prove(components, channel: pr.Blake2sChannel, scheme: CommitmentSchemeProver
 
     # --- composition polynomial (ComponentProvers::compute_composition_polynomial): components in
     # order take the highest powers of the random coefficient, each constraint the next lower one
+    for comp in components:
+        missing = [n for n in comp.air.params if n not in comp.params]
+        if missing:
+            raise KeyError(f"{comp.air.name}: no value for the parameters {missing}")
     random_coeff = channel.draw_secure_felt()
     log_expansion = evaluation_mode(components, b)
     total = sum(c.n_constraints for c in components)
@@ -403,10 +408,7 @@ def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = F
             raise ValueError("components' trace columns must follow one another in component order")
         col += len(offs)
         kinds = [_param_kind(c.air, p) for p in c.air.params]
-        params = [c.params.get(p, (0, 0, 0, 0)) if k == 0 else (0, 0, 0, 0) for p, k in zip(c.air.params, kinds)]
-        missing = [p for p, k in zip(c.air.params, kinds) if k == 0 and p not in c.params]
-        if missing:
-            raise KeyError(f"{c.air.name}: no value for the parameters {missing}")
+        params = [c.params[p] if k == 0 else (0, 0, 0, 0) for p, k in zip(c.air.params, kinds)]
         specs.append({"kernel": CompiledAir.get(c.air).handle, "log_size": c.log_size,
                       "degree": c.constraint_log_degree, "offsets": offs, "masks": masks, "nodes": nodes,
                       "constraints": cons, "params": params, "kinds": kinds, "n_batches": len(c.air.logup),

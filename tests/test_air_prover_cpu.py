@@ -203,7 +203,14 @@ def test_component_arguments_are_checked():
         ap.TraceLocationAllocator(preprocessed_columns=["a", "a"])
     lookup = fw.compile_air("single_lookup", fw.single_lookup_air)
     with pytest.raises(KeyError):
-        ap.FrameworkComponent(ap.TraceLocationAllocator(), lookup, 4)   # no z
+        ap.FrameworkComponent(ap.TraceLocationAllocator(), lookup, 4)   # no z (not a relation's parameter)
+    # a relation's parameters may come later; prove() asks for them
+    rel = fw.compile_air("lookup_rel", _relation_lookup_air)
+    late = ap.FrameworkComponent(ap.TraceLocationAllocator(), rel, 4)
+    assert "lookup_z" not in late.params and late.params["shift"] == (0, 0, 0, 0)
+    scheme = ap.CommitmentSchemeProver(CpuOps(), pr.PcsConfig(FRI, trace_lifting_log_size=5), None)
+    with pytest.raises(KeyError):
+        ap.prove([late], pr.Blake2sChannel(), scheme)
     c = ap.FrameworkComponent(ap.TraceLocationAllocator(), lookup, 4, {"z": (1, 2, 3, 4)}, claimed_sum=(16, 0, 0, 0))
     assert c.params["shift"] == (1, 0, 0, 0)
     with pytest.raises(ValueError):

@@ -173,16 +173,14 @@ def test_poseidon_fully_through_the_generic_api_equals_oracle(ops):
 def test_native_generic_prover_with_relations_equals_oracle(ops):
     # two components of the relation entry -1 / (v - z) (sizes 2^8 and 2^4), their interaction tree
     # generated from their fraction kernels, the claimed sums mixed before its root: the oracle's
-    # proof of two single-column LogUp components. The relation's parameters are filled from the
-    # draw, so the values given here are placeholders.
+    # proof of two single-column LogUp components. The relation's parameters come from the draw.
     air = fw.compile_air("lookup_rel", _relation_lookup_air)
     rng = np.random.default_rng(7)
     vals = [rng.integers(0, O.P, 1 << n, dtype=np.uint32) for n in (8, 4)]
     cfg = pr.PcsConfig(FRI, trace_lifting_log_size=9)
     tw = ops.twiddles(10)
     alloc = ap.TraceLocationAllocator()
-    placeholder = {"lookup_z": (0, 0, 0, 0), "lookup_alpha0": (0, 0, 0, 0)}
-    comps = [ap.FrameworkComponent(alloc, air, n, placeholder) for n in (8, 4)]
+    comps = [ap.FrameworkComponent(alloc, air, n) for n in (8, 4)]
     got = ap.prove_native(comps, ops.columns_from_host(vals), cfg, tw, mix_claimed=True)
     want, _ = O.prove_fib_and_lookups((10, 1, 0, 3, 1), [], [], vals, [8, 4])
     assert got == want
@@ -199,9 +197,8 @@ def test_native_generic_poseidon_equals_the_hand_written_native_prover(ops, log_
     fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
     cfg = ps.poseidon_pcs_config(log_n + 3, fp)
     tw = ops.twiddles(log_n + ps.LOG_EXPAND + 1)
-    placeholder = {p: (0, 0, 0, 0) for p in air.params}  # z, alpha^i and the shift come from the proof
-    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n, placeholder,
-                                 constraint_log_degree=ps.LOG_EXPAND)
+    # z, the alpha powers and the shift come from the proof
+    comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n, constraint_log_degree=ps.LOG_EXPAND)
     got = ap.prove_native([comp], ops.poseidon_trace(log_n), cfg, tw)
     want = CudaBackend.prove_poseidon_native(log_n, (10, 1, 0, 70), tw)
     assert got == want == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
