@@ -202,3 +202,28 @@ def test_native_generic_poseidon_equals_the_hand_written_native_prover(ops, log_
     got = ap.prove_native([comp], ops.poseidon_trace(log_n), cfg, tw)
     want = CudaBackend.prove_poseidon_native(log_n, (10, 1, 0, 70), tw)
     assert got == want == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
+
+
+def test_native_generic_prover_rejects_inconsistent_components(ops):
+    # every table is checked against the kernel and the program before any launch
+    from proving_gb300._lib import CudaBackendError
+    from proving_gb300.backend import CudaBackend
+    from proving_gb300.framework import CompiledAir
+    air = fw.compile_air("window", window_air)
+    nodes, cons, offs, masks, inter_two = air.point_program()
+    good = {"kernel": CompiledAir.get(air).handle, "log_size": 6, "degree": 1, "offsets": offs, "masks": masks,
+            "nodes": nodes, "constraints": cons, "params": [], "kinds": [], "n_batches": 0, "frac_cols": [],
+            "inter_two": []}
+    tw = ops.twiddles(8)
+
+    def attempt(**change):
+        spec = dict(good, **change)
+        trace = ops.columns_from_host(window_trace(6, 3))
+        return CudaBackend.prove_air_native([spec], trace, 7, (10, 1, 0, 3), tw)
+    assert len(attempt()) > 0
+    bad_nodes = np.array(nodes, np.uint32)
+    bad_nodes[len(bad_nodes) // 2, 1] = len(bad_nodes) - 1          # reads a later node
+    for change in ({"nodes": bad_nodes}, {"masks": masks[:-1]}, {"constraints": cons[:-1]},
+                   {"degree": 3}, {"masks": [(9, 1)] + masks[1:]}, {"offsets": offs[:-1]}):
+        with pytest.raises(CudaBackendError):
+            attempt(**change)
