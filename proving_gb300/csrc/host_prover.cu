@@ -1320,18 +1320,18 @@ struct RtcAir : Air {
     // kernel reads their trace-domain values after the trace tree is committed
     std::vector<const uint32_t*> src;
     std::vector<uint32_t> tlogs;
-    for (const RtcComponent& k : comps)
+    for (const RtcComponent& k : comps) {
+      uint32_t* blk = nullptr;  // one block for the coefficients of a component with relations
+      if (k.n_batches) {
+        blk = P.A.alloc((size_t)k.n_cols << k.log_size);
+        if (!blk) return P.A.status;
+      }
       for (uint32_t j = 0; j < k.n_cols; j++) {
         src.push_back(d_trace[k.col0 + j]);
         tlogs.push_back(k.log_size);
-        if (k.n_batches) {
-          uint32_t* c = P.A.alloc(1ull << k.log_size);
-          if (!c) return P.A.status;
-          coeffs.push_back(c);
-        } else {
-          coeffs.push_back(d_trace[k.col0 + j]);
-        }
+        coeffs.push_back(blk ? blk + ((size_t)j << k.log_size) : d_trace[k.col0 + j]);
       }
+    }
     HP_TRY(P.interpolate_mixed(src, coeffs, tlogs));
     HP_TRY(P.evaluate_mixed(coeffs, tlogs, evals));
     for (size_t j = 0; j < evals.size(); j++) cols.push_back({evals[j], tlogs[j] + P.cfg.b});
