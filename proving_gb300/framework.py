@@ -433,15 +433,30 @@ def compile_air(name: str, evaluate, *args) -> Air:
         return name
 
     def emit(ks) -> list:
-        """The lines that add constraints ks (indices) to acc, sharing the current temps."""
-        body = []
+        """The lines that add constraints ks (indices) to acc, sharing the current temps. An M31
+        constraint's weighted value goes unreduced into four 64-bit sums, one multiply-add per
+        coordinate (products below 2^62, the sums folded below 2^34 every three terms); the sums
+        are reduced and added to acc once, at the end of the lines."""
+        body = ["  uint64_t lz0 = 0, lz1 = 0, lz2 = 0, lz3 = 0;"]
+        pending = 0
         for k in ks:
             c = e.constraints[k]
             v = visit(c)
             body.extend(lines)
             lines.clear()
-            w = f"qm31_make(rc[{4 * k}], rc[{4 * k + 1}], rc[{4 * k + 2}], rc[{4 * k + 3}])"
-            body.append(f"  acc = {op_name('qm31_add')}(acc, {op_name('qm31_mul' if c.ext else 'qm31_mul_m31')}({w}, {v}));")
+            if c.ext:
+                w = f"qm31_make(rc[{4 * k}], rc[{4 * k + 1}], rc[{4 * k + 2}], rc[{4 * k + 3}])"
+                body.append(f"  acc = {op_name('qm31_add')}(acc, {op_name('qm31_mul')}({w}, {v}));")
+                continue
+            if pending == 3:
+                body.append("  lz0 = (lz0 & P) + (lz0 >> 31); lz1 = (lz1 & P) + (lz1 >> 31); "
+                            "lz2 = (lz2 & P) + (lz2 >> 31); lz3 = (lz3 & P) + (lz3 >> 31);")
+                pending = 0
+            body.append(f"  lz0 += (uint64_t)rc[{4 * k}] * {v}; lz1 += (uint64_t)rc[{4 * k + 1}] * {v}; "
+                        f"lz2 += (uint64_t)rc[{4 * k + 2}] * {v}; lz3 += (uint64_t)rc[{4 * k + 3}] * {v};")
+            pending += 1
+        body.append(f"  acc = {op_name('qm31_add')}(acc, qm31_make(m31_reduce64(lz0), m31_reduce64(lz1), "
+                    "m31_reduce64(lz2), m31_reduce64(lz3)));")
         return body
 
     # One straight-line body when it is small. The device compiler's optimizer takes time
@@ -502,7 +517,8 @@ __device__ __noinline__ qm31 cs_air_group{g}(const uint32_t* const* __restrict__
   return acc;
 }}
 """
-            calls += f"    acc = air_qm31_add(acc, cs_air_group{g}(cols, rc, params, r{row_args}, xs));\n"
+            add = "air_qm31_add" if "qm31_add" in _SPLIT_OPS else "qm31_add"
+            calls += f"    acc = {add}(acc, cs_air_group{g}(cols, rc, params, r{row_args}, xs));\n"
         split["chunk"] = None
         inline = f"    uint32_t xs[{max(xs_words, 1)}];\n" + calls.rstrip("\n")
         funcs = "".join(f"__device__ __noinline__ {ty} air_{fn}({args}) {{ return {fn}(a, b); }}\n"
