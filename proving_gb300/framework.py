@@ -314,9 +314,12 @@ class Air:
         return [columns_by_interaction[m.interaction][m.column] for m in self.masks]
 
 
-_SPLIT_OPS = {"m31_mul": ("uint32_t", "uint32_t a, uint32_t b"), "qm31_add": ("qm31", "qm31 a, qm31 b"),
-              "qm31_sub": ("qm31", "qm31 a, qm31 b"), "qm31_mul": ("qm31", "qm31 a, qm31 b"),
-              "qm31_mul_m31": ("qm31", "qm31 a, uint32_t b")}
+# Operations a split body calls through non-inlined wrappers, name -> (result type, parameters),
+# e.g. {"qm31_mul": ("qm31", "qm31 a, qm31 b")}: the device compiler then has less code to
+# optimize, at a cost in run time. Empty: everything is inlined. For the 1,144 constraints of
+# Poseidon2 at 2^18 rows the proof takes 28.9 ms inlined (30 s to compile on the Grace host)
+# against 34.1 ms with M31 products and QM31 operations wrapped (22 s).
+_SPLIT_OPS: dict = {}
 _SINGLE_LINES = 1500  # bodies up to this many lines stay one function
 _CHUNK_NODES = 300    # computed nodes per function of a split body
 _LEAVES = ("mask", "const", "param")
@@ -366,9 +369,8 @@ def compile_air(name: str, evaluate, *args) -> Air:
     split = {"chunk": None, "owner": {}, "slot": {}}  # set while emitting a split body
 
     def op_name(fn: str) -> str:
-        """A split body calls its QM31 operations and M31 products through non-inlined wrappers
-        (_SPLIT_OPS), the kernel's sum of the functions too: the device compiler then has about half
-        as much code to optimize (a 1,144-constraint body: 66 -> 36 s)."""
+        """The name a split body calls an operation by: its non-inlined wrapper when _SPLIT_OPS
+        lists it (the kernel's sum of the functions too), else the operation itself."""
         return f"air_{fn}" if split["chunk"] is not None and fn in _SPLIT_OPS else fn
 
     def visit(x: Expr) -> str:

@@ -120,4 +120,4 @@ def test_large_bodies_are_split_into_functions():
                 {int(x) for x in re.findall(r"qm31_make\(xs\[(\d+)\]", body)}
         assert reads <= written
         written |= {int(x) for x in re.findall(r"xs\[(\d+)\] =", body)}
-    assert src.count("air_qm31_add(acc, cs_air_group") == len(groups)
+    assert src.count(" qm31_add(acc, cs_air_group") == len(groups)
