@@ -1269,6 +1269,27 @@ def run_case(args):
             torch.cuda.synchronize()
             lat.append((time.perf_counter() - t0) * 1e3)
         res = {"workload": f"native Poseidon2 proof, 2^{log_n} rows", "ms": [round(x, 3) for x in lat]}
+    elif args.case == "poseidon-generic-native":
+        # twice: a Poseidon2 proof through the native generic prover (the AIR recorded by the
+        # constraint evaluator, its kernels compiled first), then one through cs_prove_poseidon
+        from proving_gb300 import air_prover as ap
+        from proving_gb300 import framework as fw
+        from proving_gb300 import poseidon as ps
+        from proving_gb300 import prover as pr
+        from proving_gb300.backend import CudaBackend
+        log_n = args.poseidon_log_rows
+        ops = pr.GpuOps()
+        fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=0, n_queries=70, fold_step=1)
+        cfg = ps.poseidon_pcs_config(log_n + 3, fp)
+        tw = ops.twiddles(log_n + ps.LOG_EXPAND + 1)
+        air = fw.poseidon_air_recorded()
+        fw.CompiledAir.get(air)
+        comp = ap.FrameworkComponent(ap.TraceLocationAllocator(), air, log_n, constraint_log_degree=ps.LOG_EXPAND)
+        same = []
+        for _ in range(2):
+            words = ap.prove_native([comp], CudaBackend.poseidon_trace(log_n), cfg, tw)
+            same.append(words == CudaBackend.prove_poseidon_native(log_n, (10, 1, 0, 70), tw))
+        res = {"workload": f"Poseidon2 at 2^{log_n} rows, generic native then hand-written native", "same": same}
     elif args.case == "wide-fib-native":  # two native 100 x 2^14 Wide-Fibonacci proofs after two warm-up proofs
         lat = wide_fib_prove_native(torch, n_proofs=2)
         res = {"workload": "native Wide-Fibonacci proof, 100 x 2^14", "ms": [round(x, 3) for x in lat]}
@@ -1316,7 +1337,7 @@ def main():
                     help="keep the default FFT pass plans (no candidate sweep before timing; for profiling)")
     ap.add_argument("--gkr-log", type=int, default=22, help="log2 values of the --case gkr instance")
     ap.add_argument("--case", choices=["mixed-kernels", "mixed-prove", "mixed-prove-native", "poseidon-native",
-                                       "wide-fib-native", "gkr"],
+                                       "poseidon-generic-native", "wide-fib-native", "gkr"],
                     help="run one small profiling case instead of the benchmark (for ncu)")
     args = ap.parse_args()
     set_shape(args.n_cols, args.log_rows)
