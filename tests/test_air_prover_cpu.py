@@ -458,3 +458,60 @@ def test_poseidon_fully_through_the_generic_api_equals_prove_poseidon():
     proof = poseidon_fully_generic(CpuOps(), 4)
     _, want = poseidon_generic(CpuOps(), 4)
     assert proof.to_bytes() == want.to_bytes()
+
+
+def test_everything_in_one_proof_verifies():
+    # a window AIR (offset masks), a relation entry with its interaction generated from the AIR's
+    # fractions, and an AIR over a preprocessed column, in one proof: the restated verifier accepts
+    # it after replaying the same commitments and draws, and rejects a wrong claimed sum
+    log_n = 5
+    n = 1 << log_n
+    ops = CpuOps()
+    cfg = pr.PcsConfig(FRI, trace_lifting_log_size=log_n + 1)
+    rng = np.random.default_rng(11)
+    seq_c = rng.integers(0, O.P, n, dtype=np.int64)
+    seq_c[-1] = (-seq_c[:-1].sum()) % O.P
+    x_c = np.concatenate([[5], (5 + np.cumsum(seq_c[:-1])) % O.P])
+    y_c = (x_c + seq_c * seq_c) % O.P
+    k = np.arange(n)
+    nat = np.where(k % 2 == 0, k // 2, n - 1 - (k - 1) // 2)
+    rows = np.array([int(format(int(v), f"0{log_n}b")[::-1], 2) for v in nat])
+
+    def lay(c):
+        out = np.zeros(n, np.uint32)
+        out[rows] = c
+        return out
+    window, rel, seq = (fw.compile_air("window", window_air), fw.compile_air("lookup_rel", _relation_lookup_air),
+                        fw.compile_air("seq", seq_air))
+    values = rng.integers(0, O.P, n, dtype=np.uint32)
+    trace = window_trace(log_n, 4) + [values, lay(x_c), lay(y_c)]
+    ch = pr.Blake2sChannel()
+    scheme = ap.CommitmentSchemeProver(ops, cfg, ops.twiddles(log_n + 1))
+    scheme.commit(ops.columns_from_host([lay(seq_c)]), ch)
+    trace_cols = ops.columns_from_host(trace)
+    scheme.commit(trace_cols, ch)
+    z, alpha = ch.draw_secure_felt(), ch.draw_secure_felt()
+    params = fw.lookup_params("lookup", z, alpha, 1)
+    inter, claimed = ap.logup_interaction(ops, rel, [trace_cols[4]], log_n, params)
+    ch.mix_felts([claimed])
+    scheme.commit(inter, ch)
+    alloc = ap.TraceLocationAllocator(preprocessed_columns=["seq"])
+    comps = [ap.FrameworkComponent(alloc, window, log_n), ap.FrameworkComponent(alloc, rel, log_n, params, claimed),
+             ap.FrameworkComponent(alloc, seq, log_n)]
+    assert [c.trace_locations[1] for c in comps] == [(0, 4), (4, 5), (5, 7)]
+    proof = ap.prove(comps, ch, scheme)
+
+    def verify(claimed_sum):
+        v = O.Blake2sChannel()
+        v.mix_root(proof.commitments[0])
+        v.mix_root(proof.commitments[1])
+        vz, va = v.draw_secure_felt(), v.draw_secure_felt()
+        vp = fw.lookup_params("lookup", vz, va, 1)
+        vp["shift"] = fw.logup_shift(claimed_sum, log_n)
+        v.mix_felts(np.asarray([list(claimed_sum)], np.uint32))
+        v.mix_root(proof.commitments[2])
+        verify_components(proof, v, [(window, log_n, {}), (rel, log_n, vp), (seq, log_n, {})],
+                          [[log_n], [log_n] * 7, [log_n] * 4], preprocessed_columns=["seq"])
+    verify(claimed)
+    with pytest.raises(VerificationError):
+        verify(tuple((c + 1) % O.P for c in claimed))
