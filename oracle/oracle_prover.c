@@ -15,7 +15,7 @@
  *     log_expansion 0, crates/stwo/src/prover/air/accumulation.rs:42-62).
  *   orc_prove_poseidon — the Poseidon2 AIR of crates/examples/src/poseidon/
  *     mod.rs:320-379 (ExtendToEvalDomain, coefficients stored).
- * FRI uses fold_step 1 (every configuration here does).
+ * FRI folds fold_step times per layer (leaves of 4 values when it is above one).
  */
 #include <stdlib.h>
 #include <string.h>
@@ -452,50 +452,92 @@ static void fri_quotients(const scheme_t *s, qm31 **sampled, const qpoint *const
     free(accs); free(order); free(pt_accs); free(pt_logs); free(pt_words); free(pt_fl);
 }
 
-/* One committed FRI layer (FriFirstLayerProver / FriInnerLayerProver without leaf packing,
-   crates/stwo/src/prover/fri.rs:287-392): the 4 coordinate columns and their tree. */
+/* One committed FRI layer (FriFirstLayerProver / FriInnerLayerProver, crates/stwo/src/prover/fri.rs:
+   287-392): the 4 coordinate columns, the layer's fold step and its tree. With a fold step above
+   one and at least 4 values, a leaf holds 4 consecutive values (pack_leaves_input: column
+   coord + 4 offset holds coordinate coord of row 4 r + offset, the tree 2 levels lower). */
 typedef struct {
-    uint32_t log;
+    uint32_t log, step, packed, height;
     uint32_t *v[4];
     uint8_t *layers;
     uint8_t root[32];
 } fri_layer_t;
 
-static void fri_layer_commit(fri_layer_t *f, uint32_t *v[4], uint32_t log) {
+static void fri_layer_commit(fri_layer_t *f, uint32_t *v[4], uint32_t log, uint32_t step) {
     f->log = log;
+    f->step = step;
+    f->packed = step > 1 && log >= 2;
     for (int c = 0; c < 4; c++) f->v[c] = v[c];
-    uint32_t logs[4] = {log, log, log, log};
-    f->layers = (uint8_t *)malloc(32 * ((2ull << log) - 1));
-    orc_merkle_commit((const uint32_t **)f->v, logs, 4, log, f->root, f->layers);
+    if (!f->packed) {
+        uint32_t logs[4] = {log, log, log, log};
+        f->height = log;
+        f->layers = (uint8_t *)malloc(32 * ((2ull << log) - 1));
+        orc_merkle_commit((const uint32_t **)f->v, logs, 4, log, f->root, f->layers);
+        return;
+    }
+    const uint32_t h = log - 2;
+    const uint64_t rows = 1ull << h;
+    uint32_t *pk[16];
+    uint32_t logs[16];
+    for (int c = 0; c < 16; c++) {
+        pk[c] = (uint32_t *)malloc(sizeof(uint32_t) * rows);
+        logs[c] = h;
+    }
+    for (uint64_t r = 0; r < rows; r++)
+        for (int off = 0; off < 4; off++)
+            for (int coord = 0; coord < 4; coord++) pk[coord + 4 * off][r] = v[coord][4 * r + off];
+    f->height = h;
+    f->layers = (uint8_t *)malloc(32 * ((2ull << h) - 1));
+    orc_merkle_commit((const uint32_t **)pk, logs, 16, h, f->root, f->layers);
+    for (int c = 0; c < 16; c++) free(pk[c]);
 }
 
-/* compute_decommitment_positions_and_witness_evals (fri.rs:398-430) with fold_step 1, then the
-   layer's Merkle witness; serialized as FriLayerProof (serialize.rs:69-79). */
+/* compute_decommitment_positions_and_witness_evals (fri.rs:398-430): every coset of 2^step
+   positions around the queries, the values that are not queries as the witness, then the layer's
+   Merkle witness of those positions (of the leaves holding them when packed, fri.rs:318-326);
+   serialized as FriLayerProof (serialize.rs:69-79). */
 static void fri_layer_decommit(const fri_layer_t *f, const uint32_t *queries, uint32_t nq, felts_t *out) {
-    uint32_t *pos = (uint32_t *)calloc(2 * (size_t)(nq ? nq : 1), sizeof(uint32_t));
-    qm31 *wit = (qm31 *)malloc(sizeof(qm31) * 2 * (nq ? nq : 1));
+    const uint32_t k = f->step, m = 1u << k;
+    uint32_t *pos = (uint32_t *)calloc((size_t)m * (nq ? nq : 1), sizeof(uint32_t));
+    qm31 *wit = (qm31 *)malloc(sizeof(qm31) * (size_t)m * (nq ? nq : 1));
     uint32_t npos = 0, nw = 0;
     for (uint32_t i = 0; i < nq;) {
         uint32_t j = i;
-        while (j < nq && (queries[j] >> 1) == (queries[i] >> 1)) j++;
-        uint32_t start = (queries[i] >> 1) << 1;
+        while (j < nq && (queries[j] >> k) == (queries[i] >> k)) j++;
+        uint32_t start = (queries[i] >> k) << k;
         uint32_t qi = i;
-        for (uint32_t p = start; p < start + 2; p++) {
+        for (uint32_t p = start; p < start + m; p++) {
             pos[npos++] = p;
             if (qi < j && queries[qi] == p) qi++;
             else wit[nw++] = soa_get((uint32_t *const *)f->v, p);
         }
         i = j;
     }
+    uint32_t nmp = npos;
+    if (f->packed) {  /* the leaves holding the positions, each once (positions are sorted) */
+        nmp = 0;
+        for (uint32_t i = 0; i < npos; i++)
+            if (nmp == 0 || pos[nmp - 1] != (pos[i] >> 2)) pos[nmp++] = pos[i] >> 2;
+    }
     uint8_t *hw = NULL;
     uint32_t nhw = 0;
-    merkle_witness(f->layers, f->log, pos, npos, &hw, &nhw);
+    merkle_witness(f->layers, f->height, pos, nmp, &hw, &nhw);
     fpush(out, nw);
-    for (uint32_t k = 0; k < nw; k++) fpush_qm31(out, wit[k]);
+    for (uint32_t q = 0; q < nw; q++) fpush_qm31(out, wit[q]);
     fpush(out, nhw);
-    for (uint32_t k = 0; k < nhw; k++) fpush_hash(out, hw + 32 * k);
+    for (uint32_t q = 0; q < nhw; q++) fpush_hash(out, hw + 32 * q);
     fpush_hash(out, f->root);
     free(hw); free(pos); free(wit);
+}
+
+/* Queries::fold (crates/stwo/src/core/queries.rs:50-56) in place; returns the new count. */
+static uint32_t fold_queries_inplace(uint32_t *q, uint32_t n, uint32_t k) {
+    uint32_t m = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t v = q[i] >> k;
+        if (m == 0 || q[m - 1] != v) q[m++] = v;
+    }
+    return m;
 }
 
 /* The part of prove_ex after the composition tree is committed (crates/stwo/src/prover/mod.rs:75-135)
@@ -558,10 +600,13 @@ static int prove_tail(scheme_t *s, orc_channel *ch, const fri_params_t *fp, uint
     soa_alloc(quot, L);
     fri_quotients(s, sampled, (const qpoint *const *)points, random_coeff, L, b, tw, quot);
 
-    /* FRI commitment (fri.rs:113-242), fold_step 1 */
+    /* FRI commitment (fri.rs:113-242): the first layer folds circle -> line then fold_step - 1 line
+       folds with alpha^2, alpha^4, ...; each inner layer folds fold_step times (alpha, alpha^2,
+       ...), the last one the 1..fold_step folds left */
+    const uint32_t k = fp->fold_step;
     const uint32_t last_log = fp->log_last_layer_degree_bound + b;
     fri_layer_t first;
-    fri_layer_commit(&first, quot, L);
+    fri_layer_commit(&first, quot, L, k);
     orc_channel_mix_root(ch, first.root);
     uint32_t n_inner_cap = L + 1, n_inner = 0;
     fri_layer_t *inner = (fri_layer_t *)malloc(sizeof(fri_layer_t) * n_inner_cap);
@@ -575,18 +620,42 @@ static int prove_tail(scheme_t *s, orc_channel *ch, const fri_params_t *fp, uint
     }
     uint32_t line_log = L - 1;
     uint32_t dom_index = cidx_subgroup_gen(line_log + 2);  /* LineDomain(Coset::half_odds(L - 1)) */
-    while (line_log > last_log) {
+    /* fold `steps` times with a, a^2, a^4, ...; the folded columns replace cur */
+    #define FOLD_STEPS(a_start, steps)                                                         \
+        do {                                                                                   \
+            qm31 fa = (a_start);                                                               \
+            for (uint32_t st = 0; st < (steps); st++) {                                        \
+                uint32_t aw[4], *nxt[4];                                                       \
+                qm31_to_words(fa, aw);                                                         \
+                soa_alloc(nxt, line_log - 1);                                                  \
+                orc_fold_line((const uint32_t *const *)cur, dom_index, line_log, aw, nxt);     \
+                if (st > 0 || !keep_cur) soa_free(cur);                                        \
+                for (int cc = 0; cc < 4; cc++) cur[cc] = nxt[cc];                              \
+                dom_index = (uint32_t)(((uint64_t)dom_index * 2) & CIRCLE_INDEX_MASK);         \
+                line_log--;                                                                    \
+                fa = qm31_mul(fa, fa);                                                         \
+            }                                                                                  \
+        } while (0)
+    int keep_cur = 0;
+    if (k > 1) FOLD_STEPS(qm31_mul(alpha, alpha), k - 1);
+    if (line_log > last_log) {
+        while (line_log > last_log + k) {
+            fri_layer_t *lay = &inner[n_inner++];
+            fri_layer_commit(lay, cur, line_log, k);
+            orc_channel_mix_root(ch, lay->root);
+            alpha = draw_felt(ch);
+            keep_cur = 1;  /* the layer keeps its columns for the decommitment */
+            FOLD_STEPS(alpha, k);
+        }
+        const uint32_t last_step = line_log - last_log;
         fri_layer_t *lay = &inner[n_inner++];
-        fri_layer_commit(lay, cur, line_log);
+        fri_layer_commit(lay, cur, line_log, last_step);
         orc_channel_mix_root(ch, lay->root);
         alpha = draw_felt(ch);
-        uint32_t a[4];
-        qm31_to_words(alpha, a);
-        soa_alloc(cur, line_log - 1);
-        orc_fold_line((const uint32_t *const *)lay->v, dom_index, line_log, a, cur);
-        dom_index = (uint32_t)(((uint64_t)dom_index * 2) & CIRCLE_INDEX_MASK);
-        line_log--;
+        keep_cur = 1;
+        FOLD_STEPS(alpha, last_step);
     }
+    #undef FOLD_STEPS
     /* last layer (fri.rs:212-241): interpolate, the top coefficients must vanish */
     uint64_t n_last = 1ull << line_log;
     qm31 *lv = (qm31 *)malloc(sizeof(qm31) * n_last);
@@ -661,19 +730,11 @@ static int prove_tail(scheme_t *s, orc_channel *ch, const fri_params_t *fp, uint
     fri_layer_decommit(&first, queries, nq, out);
     fpush(out, n_inner);
     uint32_t *lq = (uint32_t *)malloc(sizeof(uint32_t) * (nq ? nq : 1));
-    uint32_t nlq = 0;
-    for (uint32_t k = 0; k < nq; k++) {
-        uint32_t v = queries[k] >> 1;
-        if (nlq == 0 || lq[nlq - 1] != v) lq[nlq++] = v;
-    }
+    for (uint32_t q = 0; q < nq; q++) lq[q] = queries[q];
+    uint32_t nlq = fold_queries_inplace(lq, nq, k);
     for (uint32_t i = 0; i < n_inner; i++) {
         fri_layer_decommit(&inner[i], lq, nlq, out);
-        uint32_t m = 0;
-        for (uint32_t k = 0; k < nlq; k++) {
-            uint32_t v = lq[k] >> 1;
-            if (m == 0 || lq[m - 1] != v) lq[m++] = v;
-        }
-        nlq = m;
+        nlq = fold_queries_inplace(lq, nlq, inner[i].step);
     }
     fpush(out, keep);
     for (uint64_t k = 0; k < keep; k++) fpush_qm31(out, last_poly[k]);
@@ -785,7 +846,7 @@ int orc_prove_fib_and_lookups(const uint32_t fri[5], uint32_t n_fib, const uint3
                               const uint32_t *const *lookup_values, int check, uint32_t *claimed_out,
                               uint64_t *words, size_t capacity, size_t *n_words) {
     fri_params_t fp = {fri[0], fri[1], fri[2], fri[3], fri[4]};
-    if (fp.log_blowup_factor != 1 || fp.fold_step != 1 || n_fib + n_lookups == 0) return -1;
+    if (fp.log_blowup_factor != 1 || fp.fold_step < 1 || n_fib + n_lookups == 0) return -1;
     const uint32_t b = fp.log_blowup_factor;
     uint32_t max_log = 0, n_fib_cols = 0;
     for (uint32_t k = 0; k < n_fib; k++) {
@@ -961,7 +1022,7 @@ int orc_prove_fib_and_lookups(const uint32_t fri[5], uint32_t n_fib, const uint3
 int orc_prove_poseidon(const uint32_t fri[5], uint32_t log_n_rows, uint64_t *words, size_t capacity,
                        size_t *n_words) {
     fri_params_t fp = {fri[0], fri[1], fri[2], fri[3], fri[4]};
-    if (fp.fold_step != 1 || log_n_rows < 1) return -1;
+    if (fp.fold_step < 1 || log_n_rows < 1) return -1;
     const uint32_t b = fp.log_blowup_factor;
     const uint32_t n = log_n_rows;
     /* poseidon_pcs_config (crates/examples/src/poseidon/mod.rs:305-318): the split composition is

@@ -82,6 +82,22 @@ def test_fib_and_lookups_match_oracle_prover(gpu):
                            lookup_logs, claimed)
 
 
+@pytest.mark.parametrize("fold_step,last_layer", [(2, 0), (3, 1), (4, 2)])
+def test_fold_steps_match_oracle_prover(gpu, fold_step, last_layer):
+    # FRI with several folds per layer (packed leaves) and last layers of higher degree on the
+    # device: the oracle prover's bytes
+    from test_prove_cpu import fib_and_lookups_inputs
+    traces, logs, values, lookup_logs, _ = fib_and_lookups_inputs()
+    want, _ = O.prove_fib_and_lookups((10, 1, last_layer, 3, fold_step), traces, logs, values, lookup_logs)
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=last_layer, n_queries=3,
+                      fold_step=fold_step)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=10)
+    got = pr.prove_fib_and_lookups(gpu, [gpu.columns_from_host(t) for t in traces], logs,
+                                   [gpu.columns_from_host([v])[0] for v in values], lookup_logs, cfg,
+                                   pr.Blake2sChannel(), gpu.twiddles(10))
+    assert got.to_bytes() == want
+
+
 def test_mixed_shape_proof_matches_oracle_prover(gpu):
     # the batched mixed-size trace at a reduced scale (60 base columns, 12 LogUp components, log sizes
     # 4..11): Wide-Fibonacci components per size plus LogUp components

@@ -106,4 +106,25 @@ def test_unsupported_arguments_are_refused():
     with pytest.raises(O.ProofError):
         O.prove_fib_and_lookups((10, 2, 0, 5, 1), _traces([(3, 4)], 1), [4])  # log blowup 2
     with pytest.raises(O.ProofError):
-        O.prove_fib_and_lookups((10, 1, 0, 5, 2), _traces([(3, 4)], 1), [4])  # fold step 2
+        O.prove_fib_and_lookups((10, 1, 0, 5, 0), _traces([(3, 4)], 1), [4])  # fold step 0
+
+
+@pytest.mark.parametrize("fold_step,last_layer", [(2, 0), (3, 0), (2, 2), (4, 1)])
+def test_oracle_prover_fold_steps_equal_the_host_prover(fold_step, last_layer):
+    # FRI with several folds per layer and packed leaves, and last layers of higher degree: the
+    # oracle's own prover and the host prover on the oracle's operations give the same words, and
+    # the restated verifier accepts them
+    from test_prove_cpu import fib_and_lookups_inputs
+    from oracle.verifier import parse_proof, verify_fib_and_lookups
+    traces, logs, values, lookup_logs, _ = fib_and_lookups_inputs()
+    fri = (10, 1, last_layer, 3, fold_step)
+    want, claimed = O.prove_fib_and_lookups(fri, traces, logs, values, lookup_logs)
+    ops = CpuOps()
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=last_layer, n_queries=3,
+                      fold_step=fold_step)
+    cfg = pr.PcsConfig(fp, trace_lifting_log_size=10)
+    got = pr.prove_fib_and_lookups(ops, [ops.columns_from_host(t) for t in traces], logs,
+                                   [ops.columns_from_host([v])[0] for v in values], lookup_logs, cfg,
+                                   pr.Blake2sChannel(), ops.twiddles(10))
+    assert got.to_bytes() == want
+    verify_fib_and_lookups(parse_proof(want, 10), [4, 5], logs, lookup_logs, claimed)
