@@ -596,10 +596,15 @@ cs_status cs_rtc_kernel_shape(void *handle, uint32_t *n_cols, uint32_t *n_constr
    interaction tree of every such component's 4 n_batches coordinate columns,
    generated from its fraction kernel (cs_rtc_air_fractions) as the
    LogupTraceGenerator writes them; with flags & CS_PROVE_MIX_CLAIMED the claimed
-   sums are mixed into the channel before that tree's root. log_blowup_factor 1,
-   fold_step 1. Constraints of log degree 1 are evaluated on the committed
-   domain; of degree 2 on CanonicCoset(log_size + 2) from the coefficients
-   (ExtendToEvalDomain), and then without the sanity check, which the reference's
+   sums are mixed into the channel before that tree's root. log_blowup_factor
+   1..16, fold_step 1. The evaluation mode is EvaluationMode::infer's
+   (crates/stwo/src/prover/air/accumulation.rs:42-62): when every component's
+   constraint log degree d is at most the blowup b, by the same b - d, the
+   constraints run on the first 2^(log_size + d) committed evaluations (SubDomain)
+   and the composition is interpolated on that subdomain; else on
+   CanonicCoset(log_size + d), the committed evaluations when that is their
+   domain, else the coefficients evaluated there (ExtendToEvalDomain). Constraints
+   of log degree 2 are proved without the sanity check, which the reference's
    lifted protocol fails for them (the words are the proof it computes before it).
    A trace column is sampled at the OODS point plus each of its mask offsets in
    steps of CanonicCoset(lifting_log_size - 1) (component.rs:202-214), an
@@ -613,7 +618,8 @@ cs_status cs_rtc_kernel_shape(void *handle, uint32_t *n_cols, uint32_t *n_constr
    column mask_cols[i] of tree mask_trees[i]. param_kinds: per parameter, 0 =
    its value in params, 1 = z, 2 = the shift claimed sum / 2^log_size, 3 + i =
    alpha^i. params: the FRI parameters and twiddles (n_components, n_cols and
-   log_sizes unused); lifting_log_size = the largest log_size + degree - 1 + 1. */
+   log_sizes unused); lifting_log_size = the largest log_size + degree - 1 +
+   log_blowup_factor. */
 typedef struct {
   void *kernel;                  /* cs_rtc_compile_air(_logup) handle */
   uint32_t log_size;             /* 2^log_size trace rows */

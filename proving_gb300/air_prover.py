@@ -392,13 +392,14 @@ def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = F
     mix_claimed), then prove() with the relations' parameters filled from the draw and the shift
     from each claimed sum. The trace columns of components without relations are interpolated in
     place (consumed). Constraint log degree 1 or 2 (degree 2 without the sanity check, as in the
-    reference's lifted protocol), log blowup 1, fold_step 1. Returns the proof bytes, equal to
-    prove()'s for the same flow."""
+    reference's lifted protocol), any log blowup up to 16 (the evaluation mode inferred as
+    evaluation_mode does), fold_step 1. Returns the proof bytes, equal to prove()'s for the same
+    flow."""
     from .backend import CudaBackend
     from .framework import CompiledAir
     fp = config.fri_params
-    if fp.fold_step != 1 or fp.log_blowup_factor != 1:
-        raise NotImplementedError("the native prover: log blowup 1, fold_step 1")
+    if fp.fold_step != 1:
+        raise NotImplementedError("the native prover: fold_step 1")
     specs, col = [], 0
     for c in components:
         if c.constraint_log_degree not in (1, 2):

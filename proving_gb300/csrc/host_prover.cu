@@ -565,6 +565,9 @@ struct Air {
     return CS_OK;
   }
   virtual uint32_t n_constraints() const = 0;
+  // EvaluationMode::SubDomain's log_expansion (accumulation.rs:42-62): the accumulator holds the
+  // evaluation on the subdomain of CanonicCoset(its log size + this); 0 for a canonic coset
+  virtual uint32_t log_expansion() const { return 0; }
   // the constraint quotients added to per-size accumulators, powers of the random coefficient given
   virtual cs_status composition(Prover& P, const std::vector<qm31>& powers,
                                 std::map<uint32_t, std::vector<uint32_t*>>& acc) = 0;
@@ -647,7 +650,12 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
     HP_TRY(cs_lift_and_accumulate(acc_cols.data(), acc_logs.data(), (uint32_t)acc_logs.size(), st));
   const uint32_t comp_log = acc_logs.back();
   std::vector<uint32_t*> accum(acc_cols.end() - 4, acc_cols.end());
-  HP_TRY(P.interpolate(accum, comp_log));
+  // DomainEvaluationAccumulator::finalize (accumulation.rs:136-180)
+  if (air.log_expansion())
+    HP_TRY(cs_interpolate_columns_on_subdomain(accum.data(), 4, comp_log, comp_log + air.log_expansion(), cfg.itw,
+                                               cfg.tw_log, st));
+  else
+    HP_TRY(P.interpolate(accum, comp_log));
   const size_t half = 1ull << (comp_log - 1);
   std::vector<uint32_t*> split(accum);
   for (int c = 0; c < 4; c++) split.push_back(accum[c] + half);
@@ -1285,6 +1293,7 @@ struct RtcAir : Air {
   std::vector<RtcComponent> comps;
   uint32_t* const* d_trace = nullptr;
   bool mix = false;
+  int32_t sub_e = 0;  // EvaluationMode: SubDomain's log_expansion, or -1 for ExtendToEvalDomain
   std::vector<uint32_t*> coeffs, evals;  // every trace column's coefficients and blown-up evaluations
   qm31 z = qm31_make(0, 0, 0, 0), alpha = qm31_make(0, 0, 0, 0);
 
@@ -1424,6 +1433,7 @@ struct RtcAir : Air {
     for (const RtcComponent& k : comps) n += (uint32_t)k.constraints.size();
     return n;
   }
+  uint32_t log_expansion() const override { return sub_e > 0 ? (uint32_t)sub_e : 0; }
   cs_status composition(Prover& P, const std::vector<qm31>& pw,
                         std::map<uint32_t, std::vector<uint32_t*>>& acc) override {
     const uint32_t total = n_constraints();
@@ -1439,11 +1449,13 @@ struct RtcAir : Air {
         rc[4 * j + 2] = x.b.a;
         rc[4 * j + 3] = x.b.b;
       }
-      // the columns on CanonicCoset(el): the committed evaluations for constraint log degree 1
-      // (SubDomain with log_expansion 0), else the coefficients evaluated there (ExtendToEvalDomain)
+      // get_trace_columns (component_prover.rs:29-56): in SubDomain mode the committed evaluations,
+      // whose first 2^el rows are the evaluation domain; in ExtendToEvalDomain mode the columns on
+      // CanonicCoset(el), the committed evaluations when that is their domain, else the
+      // coefficients evaluated there
       std::vector<uint32_t*> tcols(evals.begin() + k.col0, evals.begin() + k.col0 + k.n_cols), icols = k.inter_evals;
       std::vector<uint32_t*> ext_t, ext_i;
-      if (k.degree > P.cfg.b) {
+      if (sub_e < 0 && el != k.log_size + P.cfg.b) {
         std::vector<uint32_t*> tc(coeffs.begin() + k.col0, coeffs.begin() + k.col0 + k.n_cols);
         HP_TRY(P.evaluate(tc, k.log_size, el, ext_t));
         tcols = ext_t;
@@ -1455,8 +1467,9 @@ struct RtcAir : Air {
       std::vector<const uint32_t*> table;
       for (size_t i = 0; i < k.mask_cols.size(); i++)
         table.push_back(k.mask_trees[i] == 2 ? icols[k.mask_cols[i]] : tcols[k.mask_cols[i]]);
-      HP_TRY(cs_rtc_air_composition(k.kernel, table.data(), rc.data(), k.resolved.empty() ? nullptr : k.resolved.data(),
-                                    el, k.log_size, P.acc_for(acc, el).data(), P.st));
+      HP_TRY(cs_rtc_air_composition_subdomain(k.kernel, table.data(), rc.data(),
+                                              k.resolved.empty() ? nullptr : k.resolved.data(), el, k.log_size,
+                                              sub_e > 0 ? (uint32_t)sub_e : 0, P.acc_for(acc, el).data(), P.st));
       if (!ext_t.empty()) P.A.release(ext_t[0]);
       if (!ext_i.empty()) P.A.release(ext_i[0]);
       start += n;
@@ -1607,13 +1620,16 @@ cs_status finish(std::vector<uint64_t>& words, uint64_t* h_words, size_t capacit
   return CS_OK;
 }
 
-cs_status check_common(const cs_wide_fib_proof_params& pp, uint32_t max_log) {
+// max_blowup: the largest log blowup the AIR's evaluation supports (1 for the hand-written AIRs,
+// whose constraints run on the committed evaluations)
+cs_status check_common(const cs_wide_fib_proof_params& pp, uint32_t max_log, uint32_t max_blowup = 1) {
   CS_CHECK_ARG((pp.flags & ~(uint32_t)CS_PROVE_PLAIN) == 0, "prove: unknown flags 0x%x", pp.flags);
-  CS_CHECK_ARG(pp.log_blowup_factor == 1, "prove: log_blowup_factor 1 (SubDomain evaluation)");
+  CS_CHECK_ARG(pp.log_blowup_factor >= 1 && pp.log_blowup_factor <= max_blowup,
+               "prove: log_blowup_factor %u outside [1, %u]", pp.log_blowup_factor, max_blowup);
   CS_CHECK_ARG(pp.d_twiddles != nullptr && pp.d_itwiddles != nullptr, "prove: null twiddles");
   CS_CHECK_ARG(pp.pow_bits <= 32 && pp.n_queries >= 1, "prove: bad FRI parameters");
   CS_CHECK_ARG(pp.lifting_log_size == max_log + pp.log_blowup_factor,
-               "prove: lifting_log_size must be the largest evaluation size (%u)", max_log + 1);
+               "prove: lifting_log_size must be the largest evaluation size (%u)", max_log + pp.log_blowup_factor);
   CS_CHECK_ARG(pp.lifting_log_size > pp.log_last_layer_degree_bound + pp.log_blowup_factor + 1 &&
                    pp.lifting_log_size <= 28,
                "prove: lifting_log_size %u outside the FRI parameters' range", pp.lifting_log_size);
@@ -1761,9 +1777,21 @@ extern "C" cs_status cs_prove_air(const cs_wide_fib_proof_params* params, const 
     col0 += c.n_cols;
     air.comps.push_back(std::move(rc));
   }
+  // EvaluationMode::infer (accumulation.rs:42-62): SubDomain when every component's constraint log
+  // degree is at most the blowup, by the same log_expansion; else ExtendToEvalDomain
+  const uint32_t b = params->log_blowup_factor;
+  air.sub_e = -2;
+  for (const hp::RtcComponent& rc : air.comps) {
+    const int32_t e = rc.degree > b ? -1 : (int32_t)(b - rc.degree);
+    if (e < 0 || (air.sub_e != -2 && air.sub_e != e)) {
+      air.sub_e = -1;
+      break;
+    }
+    air.sub_e = e;
+  }
   cs_wide_fib_proof_params pp = *params;
   pp.flags &= ~CS_PROVE_MIX_CLAIMED;
-  const cs_status cs = check_common(pp, max_log);
+  const cs_status cs = check_common(pp, max_log, 16);
   if (cs != CS_OK) return cs;
   std::vector<uint64_t>& words = proof_words();
   std::vector<qm31> claimed;
