@@ -483,7 +483,7 @@ cs_status cs_gkr_prove_batch(uint32_t n_instances, const uint32_t *h_kinds, cons
    prove_ex, crates/stwo/src/prover/mod.rs:39-138, over this library's
    kernels, with the host work in native code): the empty preprocessed tree,
    the components' traces in one lifted tree, the constraint quotients, the
-   OODS samples, FRI with fold_step 1 and the decommitments, returned as the
+   OODS samples, FRI (fold_step folds per layer) and the decommitments, returned as the
    CairoSerialize felt stream of the StarkProof (one u64 per felt). The
    channel starts from the zero digest. d_trace holds the components'
    columns one after another (2^log_sizes[k] words each, bit-reversed
@@ -500,6 +500,9 @@ typedef struct {
   const uint32_t *d_twiddles, *d_itwiddles;
   uint32_t twiddle_log_size;
   uint32_t flags; /* 0, or CS_PROVE_PLAIN */
+  uint32_t fold_step; /* FRI folds per layer, 1..8 (0 reads as 1); above 1 the layer
+                         trees commit packed leaves of 4 values per coordinate and the
+                         channel stays on the host for the layer loop */
 } cs_wide_fib_proof_params;
 /* flags: the plain form, one launch per column for every per-column stage (interpolate, evaluate,
    running sums, out-of-domain sampling, LogUp quotients), as the trait's default per-column loops
@@ -597,7 +600,7 @@ cs_status cs_rtc_kernel_shape(void *handle, uint32_t *n_cols, uint32_t *n_constr
    generated from its fraction kernel (cs_rtc_air_fractions) as the
    LogupTraceGenerator writes them; with flags & CS_PROVE_MIX_CLAIMED the claimed
    sums are mixed into the channel before that tree's root. log_blowup_factor
-   1..16, fold_step 1. The evaluation mode is EvaluationMode::infer's
+   1..16, any fold_step. The evaluation mode is EvaluationMode::infer's
    (crates/stwo/src/prover/air/accumulation.rs:42-62): when every component's
    constraint log degree d is at most the blowup b, by the same b - d, the
    constraints run on the first 2^(log_size + d) committed evaluations (SubDomain)

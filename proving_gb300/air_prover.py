@@ -393,13 +393,11 @@ def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = F
     from each claimed sum. The trace columns of components without relations are interpolated in
     place (consumed). Constraint log degree 1 or 2 (degree 2 without the sanity check, as in the
     reference's lifted protocol), any log blowup up to 16 (the evaluation mode inferred as
-    evaluation_mode does), fold_step 1. Returns the proof bytes, equal to prove()'s for the same
-    flow."""
+    evaluation_mode does), any fold_step up to 8. Returns the proof bytes, equal to prove()'s for
+    the same flow."""
     from .backend import CudaBackend
     from .framework import CompiledAir
     fp = config.fri_params
-    if fp.fold_step != 1:
-        raise NotImplementedError("the native prover: fold_step 1")
     specs, col = [], 0
     for c in components:
         if c.constraint_log_degree not in (1, 2):
@@ -416,7 +414,7 @@ def prove_native(components, trace, config: PcsConfig, twiddles, plain: bool = F
                       "frac_cols": [m.column for m in c.air.fraction_masks], "inter_two": inter_two})
     return CudaBackend.prove_air_native(specs, trace, config.trace_lifting_log_size,
                                         (fp.pow_bits, fp.log_blowup_factor, fp.log_last_layer_degree_bound,
-                                         fp.n_queries), twiddles, plain, mix_claimed)
+                                         fp.n_queries, fp.fold_step), twiddles, plain, mix_claimed)
 
 
 __all__ = ["TraceLocationAllocator", "FrameworkComponent", "CommitmentSchemeProver", "prove",

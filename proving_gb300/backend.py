@@ -105,7 +105,7 @@ class _WideFibProofParams(ctypes.Structure):
                 ("lifting_log_size", ctypes.c_uint32), ("pow_bits", ctypes.c_uint32),
                 ("log_blowup_factor", ctypes.c_uint32), ("log_last_layer_degree_bound", ctypes.c_uint32),
                 ("n_queries", ctypes.c_uint32), ("d_twiddles", ctypes.c_void_p), ("d_itwiddles", ctypes.c_void_p),
-                ("twiddle_log_size", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+                ("twiddle_log_size", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("fold_step", ctypes.c_uint32)]
 
 
 PROVE_PLAIN = 1  # CS_PROVE_PLAIN
@@ -563,7 +563,9 @@ class CudaBackend:
         params.n_cols = ctypes.cast(keep[0], ctypes.c_void_p)
         params.log_sizes = ctypes.cast(keep[1], ctypes.c_void_p)
         params.lifting_log_size = lifting_log_size
-        params.pow_bits, params.log_blowup_factor, params.log_last_layer_degree_bound, params.n_queries = fri_params
+        # (pow_bits, log_blowup_factor, log_last_layer_degree_bound, n_queries[, fold_step])
+        params.pow_bits, params.log_blowup_factor, params.log_last_layer_degree_bound, params.n_queries = fri_params[:4]
+        params.fold_step = fri_params[4] if len(fri_params) > 4 else 1
         params.d_twiddles = twiddles.twiddles.data_ptr()
         params.d_itwiddles = twiddles.itwiddles.data_ptr()
         params.twiddle_log_size = twiddles.log_size
@@ -575,7 +577,7 @@ class CudaBackend:
         """cs_prove_wide_fib: the whole proof of Wide-Fibonacci components with the host work in
         native code. traces[k]: component k's columns (BaseColumns of 2^log_sizes[k] evaluations,
         interpolated in place). fri_params: (pow_bits, log_blowup_factor,
-        log_last_layer_degree_bound, n_queries). Returns the proof bytes (u64 LE felts)."""
+        log_last_layer_degree_bound, n_queries[, fold_step]). Returns the proof bytes (u64 LE felts)."""
         return CudaBackend.prove_fib_and_lookups_native(traces, log_sizes, [], [], fri_params, twiddles, plain)[0]
 
     @staticmethod

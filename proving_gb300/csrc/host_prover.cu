@@ -427,6 +427,7 @@ struct FriLayer {
   Tree tree;
   std::vector<uint32_t*> eval;  // 4 coordinates
   uint32_t log_size;
+  uint32_t step = 1;  // the folds from this layer to the next
 };
 
 struct Col {
@@ -459,6 +460,7 @@ struct ProofConfig {
   uint32_t L, b, pow_bits, log_last_layer_degree_bound, n_queries;
   const uint32_t *tw, *itw;
   uint32_t tw_log;
+  uint32_t fold_step = 1;
   // one launch per column for every per-column stage (interpolate, evaluate, running sums,
   // out-of-domain sampling, constraint quotients): the plain form, as a backend without batched
   // overrides runs the trait's default per-column loops
@@ -580,7 +582,8 @@ struct Air {
 };
 
 // prove_ex (crates/stwo/src/prover/mod.rs:39-138) over the trees [preprocessed (empty), trace,
-// interaction (if any), composition], FRI with fold_step 1, the felt stream of the StarkProof.
+// interaction (if any), composition], FRI with cfg.fold_step folds per layer, the felt stream of the
+// StarkProof.
 cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, std::vector<qm31>& claimed,
                 cudaStream_t st) {
   Prover P(st, cfg);
@@ -849,95 +852,177 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   std::vector<uint32_t*> quotients;
   HP_TRY(P.evaluate(std::vector<uint32_t*>(qcols, qcols + 4), sub_log, L, quotients));
 
-  // --- FRI commit (fri.rs:113-226), fold_step 1, the channel kept on the device for the layer loop
   const uint32_t last_log = cfg.log_last_layer_degree_bound + b;
-  // 9 state words, then (from word 12, 16-byte aligned) room for the challenges of up to 64 layers
-  uint32_t* d_state = A.alloc(12 + 4 * 64);
-  if (!d_state) return A.status;
-  uint32_t state[9];
-  std::memcpy(state, ch.digest, 32);
-  state[8] = ch.n_draws;
-  CS_CUDA(cudaMemcpyAsync(d_state, state, sizeof(state), cudaMemcpyHostToDevice, st));
-  uint32_t* d_felts = d_state + 12;
-  uint32_t n_felts = 0;
   std::vector<FriLayer> layers;
   Tree first_tree;
-  HP_TRY(commit(A, quotients, std::vector<uint32_t>(4, L), L, first_tree));
-  HP_TRY(cs_channel_mix_root(d_state, first_tree.layers + first_tree.words() - 8, st));
-  HP_TRY(cs_channel_draw_secure_felt(d_state, d_felts + 4 * n_felts, st));
   std::vector<uint32_t*> cur;
-  uint32_t line_log = L - 1;
-  {
-    uint32_t* blk = A.alloc(4ull << line_log);
-    if (!blk) return A.status;
-    cur = {blk, blk + (1ull << line_log), blk + (2ull << line_log), blk + (3ull << line_log)};
-    const uint32_t* src[4] = {quotients[0], quotients[1], quotients[2], quotients[3]};
-    HP_TRY(cs_fold_circle_into_line_device_alpha(src, L, d_felts + 4 * n_felts, cur.data(), cfg.itw, cfg.tw_log, st));
-    n_felts++;
-  }
-  while (line_log >= last_log + 1 && n_felts < 64) {  // every layer above the last folds once
-    if (!cfg.plain && line_log <= 10 && n_felts + (line_log - last_log) <= 64) {
-      // the layers of at most 2^10 values, down to the last layer: one launch (cs_fri_commit_fold_tail)
-      const uint32_t n_tail = line_log - last_log;
-      std::vector<uint32_t*> evals(cur.begin(), cur.end()), tree_bufs;
-      for (uint32_t j = 0; j < n_tail; j++) {
-        FriLayer lay;
-        lay.log_size = line_log - j;
-        lay.eval = std::vector<uint32_t*>(evals.end() - 4, evals.end());
-        lay.tree.height = lay.log_size;
-        lay.tree.layers = A.alloc(((2ull << lay.log_size) - 1) * 8);
-        const uint32_t nl = lay.log_size - 1;
-        uint32_t* blk = A.alloc(4ull << nl);
-        if (!lay.tree.layers || !blk) return A.status;
-        for (int c = 0; c < 4; c++) evals.push_back(blk + ((size_t)c << nl));
-        tree_bufs.push_back(lay.tree.layers);
-        layers.push_back(lay);
+  uint32_t* d_state = nullptr;  // the device channel of the fold_step 1 loop
+  if (cfg.fold_step > 1) {
+    // --- FRI commit (fri.rs:113-226) with fold_step k: the first layer's circle fold is followed by
+    // k - 1 line folds with alpha^2, alpha^4, ..., every inner layer folds k times (alpha, alpha^2,
+    // ... : squared_alpha_powers, fri.rs:79-87), the last the 1..k folds left; a layer folded more
+    // than once commits packed leaves of 4 values per coordinate (fri.rs:294-305, 357-367). The
+    // channel stays on the host.
+    const uint32_t k = cfg.fold_step;
+    const auto commit_layer = [&](const std::vector<uint32_t*>& ev, uint32_t log, uint32_t step,
+                                  Tree& t) -> cs_status {
+      if (step > 1 && log >= 2) {
+        uint32_t* blk = A.alloc(16ull << (log - 2));
+        if (!blk) return A.status;
+        std::vector<uint32_t*> packed;
+        for (int c = 0; c < 16; c++) packed.push_back(blk + ((size_t)c << (log - 2)));
+        const uint32_t* src[4] = {ev[0], ev[1], ev[2], ev[3]};
+        HP_TRY(cs_pack_leaves_input(src, log, packed.data(), st));
+        HP_TRY(commit(A, packed, std::vector<uint32_t>(16, log - 2), log - 2, t));
+        A.release(blk);
+      } else {
+        HP_TRY(commit(A, ev, std::vector<uint32_t>(4, log), log, t));
       }
-      HP_TRY(cs_fri_commit_fold_tail(d_state, d_felts + 4 * n_felts, evals.data(), tree_bufs.data(), line_log,
-                                     n_tail, cfg.itw, cfg.tw_log, st));
-      n_felts += n_tail;
-      cur.assign(evals.end() - 4, evals.end());
-      line_log = last_log;
-      break;
+      return read_root(A, t);
+    };
+    const auto words_of = [](const qm31& x, uint32_t* w) {
+      w[0] = x.a.a;
+      w[1] = x.a.b;
+      w[2] = x.b.a;
+      w[3] = x.b.b;
+    };
+    // `steps` folds of the line evaluation `ev` (2^log values) with alpha, alpha^2, alpha^4, ...
+    const auto fold = [&](std::vector<uint32_t*>& ev, uint32_t log, qm31 alpha, uint32_t steps) -> cs_status {
+      const uint32_t nl = log - steps;
+      uint32_t* blk = A.alloc(4ull << nl);
+      if (!blk) return A.status;
+      std::vector<uint32_t*> nxt = {blk, blk + (1ull << nl), blk + (2ull << nl), blk + (3ull << nl)};
+      std::vector<uint32_t> alphas(4 * steps);
+      for (uint32_t j = 0; j < steps; j++) {
+        words_of(alpha, &alphas[4 * j]);
+        alpha = qm31_mul(alpha, alpha);
+      }
+      const uint32_t* src[4] = {ev[0], ev[1], ev[2], ev[3]};
+      HP_TRY(cs_fold_line_steps(src, log, steps, alphas.data(), nxt.data(), cfg.itw, cfg.tw_log, st));
+      ev = nxt;
+      return CS_OK;
+    };
+    HP_TRY(commit_layer(quotients, L, k, first_tree));
+    ch.mix_root(first_tree.root);
+    qm31 alpha = ch.draw_secure_felt();
+    uint32_t line_log = L - 1;
+    {
+      uint32_t* blk = A.alloc(4ull << line_log);
+      if (!blk) return A.status;
+      cur = {blk, blk + (1ull << line_log), blk + (2ull << line_log), blk + (3ull << line_log)};
+      const uint32_t* src[4] = {quotients[0], quotients[1], quotients[2], quotients[3]};
+      uint32_t aw[4];
+      words_of(alpha, aw);
+      HP_TRY(cs_fold_circle_into_line(src, L, aw, cur.data(), cfg.itw, cfg.tw_log, st));
     }
-    FriLayer lay;
-    lay.log_size = line_log;
-    lay.eval = cur;
-    HP_TRY(commit(A, cur, std::vector<uint32_t>(4, line_log), line_log, lay.tree));
-    HP_TRY(cs_channel_mix_root(d_state, lay.tree.layers + lay.tree.words() - 8, st));
+    HP_TRY(fold(cur, line_log, qm31_mul(alpha, alpha), k - 1));
+    line_log -= k - 1;
+    while (line_log > last_log) {
+      FriLayer lay;
+      lay.log_size = line_log;
+      lay.eval = cur;
+      lay.step = line_log > last_log + k ? k : line_log - last_log;
+      HP_TRY(commit_layer(cur, line_log, lay.step, lay.tree));
+      ch.mix_root(lay.tree.root);
+      alpha = ch.draw_secure_felt();
+      HP_TRY(fold(cur, line_log, alpha, lay.step));
+      line_log -= lay.step;
+      layers.push_back(lay);
+    }
+  } else {
+    // --- FRI commit (fri.rs:113-226), fold_step 1, the channel kept on the device for the layer loop
+    // 9 state words, then (from word 12, 16-byte aligned) room for the challenges of up to 64 layers
+    d_state = A.alloc(12 + 4 * 64);
+    if (!d_state) return A.status;
+    uint32_t state[9];
+    std::memcpy(state, ch.digest, 32);
+    state[8] = ch.n_draws;
+    CS_CUDA(cudaMemcpyAsync(d_state, state, sizeof(state), cudaMemcpyHostToDevice, st));
+    uint32_t* d_felts = d_state + 12;
+    uint32_t n_felts = 0;
+    HP_TRY(commit(A, quotients, std::vector<uint32_t>(4, L), L, first_tree));
+    HP_TRY(cs_channel_mix_root(d_state, first_tree.layers + first_tree.words() - 8, st));
     HP_TRY(cs_channel_draw_secure_felt(d_state, d_felts + 4 * n_felts, st));
-    const uint32_t nl = line_log - 1;
-    uint32_t* blk = A.alloc(4ull << nl);
-    if (!blk) return A.status;
-    std::vector<uint32_t*> nxt = {blk, blk + (1ull << nl), blk + (2ull << nl), blk + (3ull << nl)};
-    const uint32_t* src[4] = {cur[0], cur[1], cur[2], cur[3]};
-    HP_TRY(cs_fold_line_device_alpha(src, line_log, d_felts + 4 * n_felts, nxt.data(), cfg.itw, cfg.tw_log, st));
-    n_felts++;
-    layers.push_back(lay);
-    cur = nxt;
-    line_log = nl;
+    uint32_t line_log = L - 1;
+    {
+      uint32_t* blk = A.alloc(4ull << line_log);
+      if (!blk) return A.status;
+      cur = {blk, blk + (1ull << line_log), blk + (2ull << line_log), blk + (3ull << line_log)};
+      const uint32_t* src[4] = {quotients[0], quotients[1], quotients[2], quotients[3]};
+      HP_TRY(cs_fold_circle_into_line_device_alpha(src, L, d_felts + 4 * n_felts, cur.data(), cfg.itw, cfg.tw_log, st));
+      n_felts++;
+    }
+    while (line_log >= last_log + 1 && n_felts < 64) {  // every layer above the last folds once
+      if (!cfg.plain && line_log <= 10 && n_felts + (line_log - last_log) <= 64) {
+        // the layers of at most 2^10 values, down to the last layer: one launch (cs_fri_commit_fold_tail)
+        const uint32_t n_tail = line_log - last_log;
+        std::vector<uint32_t*> evals(cur.begin(), cur.end()), tree_bufs;
+        for (uint32_t j = 0; j < n_tail; j++) {
+          FriLayer lay;
+          lay.log_size = line_log - j;
+          lay.eval = std::vector<uint32_t*>(evals.end() - 4, evals.end());
+          lay.tree.height = lay.log_size;
+          lay.tree.layers = A.alloc(((2ull << lay.log_size) - 1) * 8);
+          const uint32_t nl = lay.log_size - 1;
+          uint32_t* blk = A.alloc(4ull << nl);
+          if (!lay.tree.layers || !blk) return A.status;
+          for (int c = 0; c < 4; c++) evals.push_back(blk + ((size_t)c << nl));
+          tree_bufs.push_back(lay.tree.layers);
+          layers.push_back(lay);
+        }
+        HP_TRY(cs_fri_commit_fold_tail(d_state, d_felts + 4 * n_felts, evals.data(), tree_bufs.data(), line_log,
+                                       n_tail, cfg.itw, cfg.tw_log, st));
+        n_felts += n_tail;
+        cur.assign(evals.end() - 4, evals.end());
+        line_log = last_log;
+        break;
+      }
+      FriLayer lay;
+      lay.log_size = line_log;
+      lay.eval = cur;
+      HP_TRY(commit(A, cur, std::vector<uint32_t>(4, line_log), line_log, lay.tree));
+      HP_TRY(cs_channel_mix_root(d_state, lay.tree.layers + lay.tree.words() - 8, st));
+      HP_TRY(cs_channel_draw_secure_felt(d_state, d_felts + 4 * n_felts, st));
+      const uint32_t nl = line_log - 1;
+      uint32_t* blk = A.alloc(4ull << nl);
+      if (!blk) return A.status;
+      std::vector<uint32_t*> nxt = {blk, blk + (1ull << nl), blk + (2ull << nl), blk + (3ull << nl)};
+      const uint32_t* src[4] = {cur[0], cur[1], cur[2], cur[3]};
+      HP_TRY(cs_fold_line_device_alpha(src, line_log, d_felts + 4 * n_felts, nxt.data(), cfg.itw, cfg.tw_log, st));
+      n_felts++;
+      layers.push_back(lay);
+      cur = nxt;
+      line_log = nl;
+    }
   }
-  // the state, every layer root and the last layer's evaluation back in one read
+  // the state, every layer root and the last layer's evaluation back in one read (with fold_step
+  // above 1 the channel and the roots are already on the host: the evaluation alone)
   std::vector<qm31> last_poly;
   {
+    const bool device_channel = cfg.fold_step == 1;
     Reads& R = reads_for(0);
-    R.add(d_state, 9, 0, 9);
     std::vector<Tree*> ts = {&first_tree};
     for (FriLayer& l : layers) ts.push_back(&l.tree);
-    for (Tree* t : ts)
-      R.add(t->layers, t->words(), t->words() - 8, 8);
+    if (device_channel) {
+      R.add(d_state, 9, 0, 9);
+      for (Tree* t : ts)
+        R.add(t->layers, t->words(), t->words() - 8, 8);
+    }
     const uint32_t last_n = 1u << last_log;
     for (int c = 0; c < 4; c++)
       R.add(cur[c], last_n, 0, last_n);
     HP_TRY(R.run(st));
-    for (int i = 0; i < 8; i++)
-      for (int k = 0; k < 4; k++) ch.digest[4 * i + k] = (uint8_t)(R.out[i] >> (8 * k));
-    ch.n_draws = R.out[8];
-    size_t o = 9;
-    for (Tree* t : ts) {
+    size_t o = 0;
+    if (device_channel) {
       for (int i = 0; i < 8; i++)
-        for (int k = 0; k < 4; k++) t->root[4 * i + k] = (uint8_t)(R.out[o + i] >> (8 * k));
-      o += 8;
+        for (int k = 0; k < 4; k++) ch.digest[4 * i + k] = (uint8_t)(R.out[i] >> (8 * k));
+      ch.n_draws = R.out[8];
+      o = 9;
+      for (Tree* t : ts) {
+        for (int i = 0; i < 8; i++)
+          for (int k = 0; k < 4; k++) t->root[4 * i + k] = (uint8_t)(R.out[o + i] >> (8 * k));
+        o += 8;
+      }
     }
     std::vector<qm31> last_values(last_n);
     for (uint32_t i = 0; i < last_n; i++)
@@ -971,34 +1056,45 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
     size_t coord_first;
     std::pair<size_t, size_t> wit;
   };
+  // compute_decommitment_positions_and_witness_evals (fri.rs:408-438): every coset of 2^step
+  // positions around a query; a packed tree opens the leaves holding them (fri.rs:318-326)
   const auto fri_layer = [&](const std::vector<uint32_t*>& eval, uint32_t log_size, const Tree& t,
-                             const std::vector<uint64_t>& q) {
+                             const std::vector<uint64_t>& q, uint32_t step) {
     LayerDec d;
     std::vector<uint64_t> starts;
     for (uint64_t x : q)
-      if (starts.empty() || starts.back() != ((x >> 1) << 1)) starts.push_back((x >> 1) << 1);
+      if (starts.empty() || starts.back() != ((x >> step) << step)) starts.push_back((x >> step) << step);
     for (uint64_t s0 : starts)
-      for (uint64_t j = 0; j < 2; j++) {
+      for (uint64_t j = 0; j < (1ull << step); j++) {
         d.positions.push_back(s0 + j);
         d.is_witness.push_back(!std::binary_search(q.begin(), q.end(), s0 + j));
       }
     d.coord_first = R.n_words;
-    for (int c = 0; c < 4; c++)  // positions are the pairs (s0, s0 + 1): one 2-word read each
-      for (uint64_t s0 : starts) R.add(eval[c], 1ull << log_size, s0, 2);
-    d.wit = read_witness(R, t, d.positions);
+    for (int c = 0; c < 4; c++)  // each coset is a run of 2^step words
+      for (uint64_t s0 : starts) R.add(eval[c], 1ull << log_size, s0, 1ull << step);
+    if (step > 1 && log_size >= 2) {
+      std::vector<uint64_t> leaves;
+      for (uint64_t x : d.positions)
+        if (leaves.empty() || leaves.back() != (x >> 2)) leaves.push_back(x >> 2);
+      d.wit = read_witness(R, t, leaves);
+    } else {
+      d.wit = read_witness(R, t, d.positions);
+    }
     return d;
   };
-  const LayerDec first_dec = fri_layer(quotients, L, first_tree, queries);
+  // Queries::fold (queries.rs:50-56)
+  const auto fold_queries = [](const std::vector<uint64_t>& q, uint32_t n) {
+    std::vector<uint64_t> out;
+    for (uint64_t x : q)
+      if (out.empty() || out.back() != (x >> n)) out.push_back(x >> n);
+    return out;
+  };
+  const LayerDec first_dec = fri_layer(quotients, L, first_tree, queries, cfg.fold_step);
   std::vector<LayerDec> inner_dec;
-  std::vector<uint64_t> lq;
-  for (uint64_t x : queries)
-    if (lq.empty() || lq.back() != (x >> 1)) lq.push_back(x >> 1);
+  std::vector<uint64_t> lq = fold_queries(queries, cfg.fold_step);
   for (FriLayer& l : layers) {
-    inner_dec.push_back(fri_layer(l.eval, l.log_size, l.tree, lq));
-    std::vector<uint64_t> nq;
-    for (uint64_t x : lq)
-      if (nq.empty() || nq.back() != (x >> 1)) nq.push_back(x >> 1);
-    lq = nq;
+    inner_dec.push_back(fri_layer(l.eval, l.log_size, l.tree, lq, l.step));
+    lq = fold_queries(lq, l.step);
   }
   struct TreeDec {
     size_t values_first;
@@ -1039,7 +1135,7 @@ cs_status prove(const ProofConfig& cfg, Air& air, std::vector<uint64_t>& words, 
   W.u(b);
   W.u(cfg.log_last_layer_degree_bound);
   W.u(cfg.n_queries);
-  W.u(1);
+  W.u(cfg.fold_step);
   W.u(trees.size() + 1);  // commitments
   W.h(pre_root);
   for (TreeCols& t : trees) W.h(t.tree.root);
@@ -1634,6 +1730,10 @@ cs_status check_common(const cs_wide_fib_proof_params& pp, uint32_t max_log, uin
                    pp.lifting_log_size <= 28,
                "prove: lifting_log_size %u outside the FRI parameters' range", pp.lifting_log_size);
   CS_CHECK_ARG(pp.twiddle_log_size >= pp.lifting_log_size, "prove: twiddle tree too small");
+  // the first layer's k folds must not go below the last layer (fri.rs:143-146)
+  const uint32_t k = pp.fold_step ? pp.fold_step : 1;
+  CS_CHECK_ARG(k <= 8 && pp.lifting_log_size >= pp.log_last_layer_degree_bound + pp.log_blowup_factor + k,
+               "prove: fold_step %u outside [1, 8] or below the last layer", pp.fold_step);
   return CS_OK;
 }
 
@@ -1641,6 +1741,7 @@ hp::ProofConfig config_of(const cs_wide_fib_proof_params& pp) {
   hp::ProofConfig c{pp.lifting_log_size, pp.log_blowup_factor, pp.pow_bits, pp.log_last_layer_degree_bound,
                     pp.n_queries, pp.d_twiddles, pp.d_itwiddles, pp.twiddle_log_size};
   c.plain = (pp.flags & CS_PROVE_PLAIN) != 0;
+  c.fold_step = pp.fold_step ? pp.fold_step : 1;
   return c;
 }
 

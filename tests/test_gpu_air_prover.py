@@ -131,16 +131,18 @@ def test_native_generic_prover_equals_the_python_generic_prover(ops, plain):
     assert got == want
 
 
-@pytest.mark.parametrize("log_blowup,degrees", [(2, (1, 1)), (3, (1, 1)), (2, (2, 2)), (2, (1, 2)), (3, (1, 2))])
-def test_native_generic_prover_with_larger_blowups_equals_the_python_generic_prover(ops, log_blowup, degrees):
+@pytest.mark.parametrize("log_blowup,degrees,fold_step", [(2, (1, 1), 1), (3, (1, 1), 2), (2, (2, 2), 1),
+                                                          (2, (1, 2), 3), (3, (1, 2), 1)])
+def test_native_generic_prover_with_larger_blowups_equals_the_python_generic_prover(ops, log_blowup, degrees,
+                                                                                    fold_step):
     # SubDomain evaluation (every constraint degree at most the blowup, by the same log_expansion)
-    # and ExtendToEvalDomain (degrees that differ, or above the blowup) through cs_prove_air: the
-    # words of air_prover.prove for the same components
+    # and ExtendToEvalDomain (degrees that differ, or above the blowup), FRI with one or several
+    # folds per layer, through cs_prove_air: the words of air_prover.prove for the same components
     log_n = 7
-    want, comps, _ = blowup_proof(ops, log_n, log_blowup, degrees, check=max(degrees) == 1)
+    want, comps, _ = blowup_proof(ops, log_n, log_blowup, degrees, fold_step=fold_step, check=max(degrees) == 1)
     lifting = log_n + max(degrees) - 1 + log_blowup
     fri = pr.FriParams(pow_bits=10, log_blowup_factor=log_blowup, log_last_layer_degree_bound=0, n_queries=3,
-                       fold_step=1)
+                       fold_step=fold_step)
     fib = O.wide_fib_trace(np.ones(1 << log_n, np.uint32), np.arange(1 << log_n, dtype=np.uint32), 5)
     trace = ops.columns_from_host(window_trace(log_n, 9) + list(fib))
     got = ap.prove_native(comps, trace, pr.PcsConfig(fri, trace_lifting_log_size=lifting), ops.twiddles(lifting + 1))

@@ -69,6 +69,32 @@ def test_native_fib_and_lookups_equal_oracle_prover(B, shape, lookup_logs, n_que
     verify_fib_and_lookups(parse_proof(native, L), [n for n, _ in shape], logs, lookup_logs, claimed)
 
 
+@pytest.mark.parametrize("fold_step,last_layer,n_queries", [(2, 0, 3), (3, 1, 20), (4, 2, 70), (2, 3, 5)])
+def test_native_fold_steps_equal_oracle_prover(B, fold_step, last_layer, n_queries):
+    # FRI with several folds per layer in the native loop (packed leaves, the channel on the host
+    # for the layer loop) and last layers of higher degree: the oracle prover's words
+    from proving_gb300.backend import BaseColumn
+    shape, lookup_logs = [(4, 9), (5, 3)], [8, 4]
+    host, values = _fib_lookup_inputs(shape, lookup_logs, 7)
+    logs = [l for _, l in shape]
+    L = max(logs + lookup_logs) + 1
+    tw = pr.GpuOps().twiddles(L + 1)
+    fri = (10, 1, last_layer, n_queries, fold_step)
+    native, claimed = B.prove_fib_and_lookups_native(
+        [[BaseColumn.from_cpu(c) for c in t] for t in host], logs, [BaseColumn.from_cpu(v) for v in values],
+        lookup_logs, fri, tw)
+    want, want_claimed = O.prove_fib_and_lookups(fri, host, logs, values, lookup_logs)
+    assert claimed == want_claimed
+    assert native == want
+
+
+@pytest.mark.parametrize("fold_step,last_layer", [(2, 0), (3, 1)])
+def test_native_poseidon_fold_steps_equal_oracle_prover(B, fold_step, last_layer):
+    tw = pr.GpuOps().twiddles(7)
+    assert B.prove_poseidon_native(4, (10, 1, last_layer, 70, fold_step), tw) == \
+        O.prove_poseidon((10, 1, last_layer, 70, fold_step), 4)
+
+
 @pytest.mark.parametrize("log_n", [4, 7])
 def test_native_poseidon_equals_oracle_prover(B, log_n):
     tw = pr.GpuOps().twiddles(log_n + 3)
