@@ -192,6 +192,25 @@ def test_native_prover_checks_arguments_on_host(lib):
     assert b"columns" in lib.cs_last_error()
 
 
+@pytest.mark.parametrize("fold_step,blowup,word", [(9, 1, b"fold_step"), (6, 1, b"fold_step"), (1, 2, b"blowup")])
+def test_native_prover_checks_fri_parameters_on_host(lib, fold_step, blowup, word):
+    # fold steps above 8 or past the last layer, and a blowup the hand-written AIR does not take,
+    # are refused before any device work
+    from proving_gb300.backend import _WideFibProofParams
+    p = _WideFibProofParams()
+    n_cols = (ctypes.c_uint32 * 1)(3)
+    logs = (ctypes.c_uint32 * 1)(5)
+    p.n_components, p.n_cols, p.log_sizes = 1, ctypes.cast(n_cols, ctypes.c_void_p), ctypes.cast(logs, ctypes.c_void_p)
+    p.lifting_log_size, p.pow_bits, p.log_blowup_factor, p.log_last_layer_degree_bound, p.n_queries = \
+        5 + blowup, 10, blowup, 0, 3
+    p.d_twiddles, p.d_itwiddles, p.twiddle_log_size = 1 << 20, 1 << 21, 8
+    p.fold_step = fold_step
+    cols = (ctypes.c_void_p * 3)(1 << 22, 1 << 23, 1 << 24)
+    n = ctypes.c_size_t(0)
+    assert _status(lib, "cs_prove_wide_fib", ctypes.byref(p), cols, None, 0, ctypes.byref(n), None) == 1
+    assert word in lib.cs_last_error()
+
+
 def test_merkle_entry_points_reject_misaligned_digest_buffers(lib):
     # digests move as 16-byte words: a 4-byte-aligned offset into a buffer is refused on the host
     # instead of faulting the device
