@@ -102,6 +102,17 @@ def test_oracle_poseidon_equals_host_prover(log_n, generic):
     assert host.to_bytes() == O.prove_poseidon((10, 1, 0, 70, 1), log_n)
 
 
+@pytest.mark.parametrize("fold_step,last_layer", [(2, 0), (3, 1)])
+def test_oracle_poseidon_fold_steps_equal_host_prover(fold_step, last_layer):
+    # the Poseidon2 proof with several folds per FRI layer: the oracle's prover and the host prover
+    from proving_gb300 import poseidon as ps
+    cpu = CpuOps()
+    fp = pr.FriParams(pow_bits=10, log_blowup_factor=1, log_last_layer_degree_bound=last_layer, n_queries=70,
+                      fold_step=fold_step)
+    host = ps.prove_poseidon(cpu, 4, ps.poseidon_pcs_config(7, fp), pr.Blake2sChannel(), cpu.twiddles(7), check=False)
+    assert host.to_bytes() == O.prove_poseidon((10, 1, last_layer, 70, fold_step), 4)
+
+
 def test_unsupported_arguments_are_refused():
     with pytest.raises(O.ProofError):
         O.prove_fib_and_lookups((10, 2, 0, 5, 1), _traces([(3, 4)], 1), [4])  # log blowup 2
